@@ -1,0 +1,127 @@
+"""Initial conditions of the benchmark workloads, built the way the
+reference's host does (initialize_variables, SRC/params.f90:305-580: step
+profiles in T, p, u and mole fractions, the "other species" fill, then
+density and energy per cell). Synthetic, seeded; no external data.
+
+Cell centres are (i + 1/2) dx. The reference accumulates them block by
+block (SRC/block.f90:256-304); for step profiles whose discontinuity does
+not fall on a centre the cell classification is the same.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from .edyn import GRI30_DIR, species_names
+
+ATM = 101325.0
+
+
+def mole_vector(names, comp: dict, fill: str | None = None) -> np.ndarray:
+    x = np.zeros(len(names))
+    for k, v in comp.items():
+        x[names.index(k)] = v
+    if fill is not None:  # "other species" fill (SRC/params.f90:453-459)
+        x[names.index(fill)] += 1.0 - x.sum()
+    return x
+
+
+@dataclass
+class TubeCase:
+    name: str
+    ncell: int
+    dx: float
+    T: np.ndarray
+    p: np.ndarray
+    u: np.ndarray
+    X: np.ndarray
+    flags: dict = field(default_factory=dict)
+    cfl: float = 0.5
+    tend: float = 0.0
+
+
+def sod(names=None, ncell: int = 1000, length: float = 1.0) -> TubeCase:
+    """1-D Sod tube: p_L/p_R = 10, rho_L/rho_R = 8 (T_L = 375 K, T_R = 300 K),
+    stoichiometric CH4/air (WORK/Examples/CH4_GRI3.0/SOD/initial.txt:17-24),
+    frozen chemistry, MUSCL-minmod + HLLC, TVDRK3, CFL 0.5, walls, 0.6 ms."""
+    names = names or species_names(GRI30_DIR)
+    dx = length / ncell
+    xm = (np.arange(ncell) + 0.5) * dx
+    left = xm <= 0.5 * length
+    x = mole_vector(names, {"CH4": 0.0950570342, "O2": 0.1901140684, "N2": 0.7148288973}, fill="N2")
+    T = np.where(left, 375.0, 300.0)
+    p = np.where(left, 10 * ATM, ATM)
+    X = np.tile(x, (ncell, 1))
+    return TubeCase("sod_ch4air_1000", ncell, dx, T, p, np.zeros(ncell), X,
+                    dict(select_time=1, select_riemann=2, flag_acu=1, flag_muscl=2, flag_weno=0,
+                         flag_lbound=0, flag_rbound=0, do_reaction=0), cfl=0.5, tend=0.6e-3)
+
+
+# Burnt driver gas: a fixed, documented CH4/O2 product mixture (major
+# species of the stoichiometric products with dissociation) used in place of
+# an equilibrium solve, which the reference delegates to Cantera.
+BURNT_CH4_O2 = {"CO2": 0.18, "H2O": 0.42, "CO": 0.14, "OH": 0.10, "H2": 0.05, "O2": 0.07, "H": 0.02, "O": 0.02}
+
+
+def detonation(names=None, ncell: int = 20000, length: float = 1.0, driver: float = 0.01, T_drv: float = 3000.0,
+               p_drv: float = 30 * ATM, phi: float = 1.0, p0: float = ATM, T0: float = 300.0,
+               oxidizer: str = "O2", weno: int = 3) -> TubeCase:
+    """CH4 detonation tube: fresh stoichiometric CH4/O2 at 1 atm, 300 K; a
+    hot high-pressure driver at x <= 1 cm; reflecting left wall, fixed
+    pressure outlet at 1 atm on the right; WENO5 + HLLC, TVDRK3, CFL 0.4."""
+    names = names or species_names(GRI30_DIR)
+    dx = length / ncell
+    xm = (np.arange(ncell) + 0.5) * dx
+    drv = xm <= driver
+    if oxidizer == "O2":
+        fresh = mole_vector(names, {"CH4": phi / (phi + 2.0), "O2": 2.0 / (phi + 2.0)})
+    else:  # air: O2 + 3.76 N2
+        n = phi + 2.0 * 4.76
+        fresh = mole_vector(names, {"CH4": phi / n, "O2": 2.0 / n, "N2": 2.0 * 3.76 / n})
+    burnt = mole_vector(names, BURNT_CH4_O2)
+    burnt /= burnt.sum()
+    T = np.where(drv, T_drv, T0)
+    p = np.where(drv, p_drv, p0)
+    X = np.where(drv[:, None], burnt[None, :], fresh[None, :])
+    return TubeCase(f"ch4_{oxidizer.lower()}_detonation_{ncell}", ncell, dx, T, p, np.zeros(ncell), X,
+                    dict(select_time=1, select_riemann=2, flag_acu=2, flag_muscl=2, flag_weno=weno,
+                         flag_lbound=0, flag_rbound=1, do_reaction=1, p_out=p0), cfl=0.4, tend=200e-6)
+
+
+def ch4_air_mixture(names, phi: float) -> np.ndarray:
+    n = phi + 2.0 * 4.76
+    return mole_vector(names, {"CH4": phi / n, "O2": 2.0 / n, "N2": 2.0 * 3.76 / n})
+
+
+def x_to_y(names, X: np.ndarray, W: np.ndarray) -> np.ndarray:
+    Y = X * W
+    return Y / Y.sum(axis=-1, keepdims=True)
+
+
+def molecular_weights(mech_dir=GRI30_DIR) -> np.ndarray:
+    txt = (mech_dir / "mech.edyn").read_text().split()
+    i = txt.index("SPECIES")
+    n = int(txt[i + 1])
+    nel = int(txt[txt.index("ELEMENTS") + 1])
+    per = 5 + 14 + nel
+    return np.array([float(txt[i + 2 + k * per + 1]) for k in range(n)])
+
+
+def reactor_batch(n: int, seed: int = 0, names=None):
+    """Fresh CH4/air reactors: T ~ U[900, 2500] K, p log-uniform in
+    [1, 50] atm, phi ~ U[0.5, 2.0], dt log-uniform in [1e-8, 1e-6] s.
+    Returns (rho [kg/m^3], dt [s], yiT (n x (K+1)), phi)."""
+    names = names or species_names(GRI30_DIR)
+    W = molecular_weights()
+    rng = np.random.default_rng(seed)
+    T = rng.uniform(900.0, 2500.0, n)
+    p = ATM * np.exp(rng.uniform(np.log(1.0), np.log(50.0), n))
+    phi = rng.uniform(0.5, 2.0, n)
+    dt = np.exp(rng.uniform(np.log(1e-8), np.log(1e-6), n))
+    X = np.stack([ch4_air_mixture(names, f) for f in phi])
+    Y = x_to_y(names, X, W)
+    wbar = 1.0 / (Y / W).sum(axis=1)
+    rho = p * wbar / (8314.51 * T)
+    yiT = np.concatenate([Y, T[:, None]], axis=1)
+    return rho, dt, np.ascontiguousarray(yiT), phi

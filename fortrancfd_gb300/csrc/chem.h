@@ -1,0 +1,53 @@
+// Chemistry (per-cell stiff integrator) launch interface.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "edyn_dev.cuh"
+#include "mechanism.h"
+
+namespace edyn {
+
+struct ChemCounters {
+  unsigned long long rhs, steps, rejects, failed, jac, cells;
+};
+
+struct ChemState {
+  void* d_tables = nullptr;       // packed reaction/species tables (global, staged to smem)
+  size_t table_bytes = 0;
+  int nr = 0, ns = 0, nf = 0, ntb = 0, nscat = 0, ntbl = 0;
+  int nr_pad = 0;
+  unsigned* d_next = nullptr;     // work-stealing counter
+  ChemCounters* d_count = nullptr;
+  int ctas = 0, warps = 0;
+  size_t smem = 0;
+};
+
+struct ChemLaunch {
+  int n, ld;
+  // tube mode
+  double* qf;
+  double* qc;
+  double* hrr;
+  double dt;
+  const int* step_active;
+  const double* dt_dev;
+  unsigned long long* cvel_out;
+  double* time;
+  long long* nsteps;
+  int strict_newton;
+  // batch mode
+  const double* rho_batch;
+  const double* dt_batch;
+  double* yiT_batch;
+  double rtol, atol;
+  unsigned* err;
+};
+
+int chem_init(ChemState& s, const edyn_mech& m, const ThermoTable& tb, cudaStream_t st);
+cudaError_t chem_launch_tube(ChemState& s, const ChemLaunch& L, cudaStream_t st);
+cudaError_t chem_launch_batch(ChemState& s, const ChemLaunch& L, cudaStream_t st);
+cudaError_t chem_read_counters(ChemState& s, ChemCounters* out, cudaStream_t st);
+void chem_free(ChemState& s);
+
+}  // namespace edyn

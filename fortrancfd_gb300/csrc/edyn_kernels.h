@@ -1,0 +1,55 @@
+// Host-visible declarations of the device kernels' launch interfaces.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+
+namespace edyn {
+
+constexpr int GHOST = 4;          // ghost columns allocated per tube end (max lvir)
+constexpr int STAGE_THREADS = 64; // threads per stage CTA (faces; cells = threads - 1)
+
+struct ThermoTable;
+
+// Boundary data of SRC/flow_bound.f90 (inlet) and the outlet pressure.
+struct FluidBC {
+  double rho_u_in;     // kg/(m^2 s)
+  double t_in;         // K
+  double e_in;         // specific internal energy at (T_in, X_in), J/kg
+  double y_in[64];
+};
+
+struct StageArgs {
+  int n, ld, lvir, ns;
+  const double* qf_in;   // primitive rows read by the stencil
+  double* qf_out;        // primitive rows written for owned cells
+  double* qc;            // conserved rows, updated in place
+  double* q0;            // stage-0 conserved rows (TVDRK3)
+  int kind;              // 0: Q - c dF (Euler, first TVDRK3 stage); 1: h1 Q0 + h2 (Q - c dF)
+  int save_q0;           // copy Q into q0 before the update (first TVDRK3 stage)
+  double h1, h2;
+  double dx, dt;         // dt used when dt_dev is null
+  const int* step_active;// device loop: skip the stage when zero
+  const double* dt_dev;  // device loop: time step of this step
+  double* time;          // last kernel of a step advances time and the step count
+  long long* nsteps;
+  unsigned long long* cvel_out;  // max signal speed of the new state (bit pattern)
+  int lbound, rbound;
+  double p_out;
+  int strict_newton;     // 1: T Newton starts at 1000 K as the reference
+};
+
+int fluid_upload_tables(const ThermoTable& tb, const FluidBC& bc, cudaStream_t s);
+size_t stage_smem_bytes(int acu, int ns, int nt);
+cudaError_t launch_stage(const StageArgs& a, int acu, int lim, int wflag, int rm, int nt, cudaStream_t s);
+cudaError_t launch_cvel(const double* qf, int n, int ld, unsigned long long* cvel, cudaStream_t s);
+cudaError_t launch_step_begin(const double* time, double tend, double cfl, double dx, unsigned long long* cvel,
+                              int* step_active, double* dt_dev, cudaStream_t s);
+cudaError_t launch_aos_to_soa(const double* aos, int ne, int n, double* soa, int ld, cudaStream_t s);
+cudaError_t launch_soa_to_aos(const double* soa, int ne, int n, int ld, double* aos, cudaStream_t s);
+cudaError_t launch_qc_to_qf(const StageArgs& a, cudaStream_t s);
+cudaError_t launch_init_cells(int n, int ns, const double* T, const double* p, const double* u, const double* X,
+                              int ldx, double* qf, double* qc, int ld, cudaStream_t s);
+
+}  // namespace edyn

@@ -1,0 +1,635 @@
+// Fused fluid stage kernel and its helpers (sm_103a).
+//
+// One launch performs one stage of the reference's explicit time integrator
+// for a whole tube (SRC/timeintegration.f90: explicit_euler 12-96, TVDRK3
+// 99-219): face reconstruction (SRC/muscl.f90, SRC/weno.f90), the face
+// equation of state (qfToQc, SRC/eos.f90:11-46, plus pressure and sound
+// speed), the LxF / HLL / HLLC flux (SRC/flux.f90:130-373), the conservative
+// Runge-Kutta update, and QcToqf with the temperature Newton solve
+// (SRC/eos.f90:49-83, SRC/thermo.f90:211-257) for every owned cell. Ghost
+// cells at the tube ends are produced in the consuming kernel from the
+// boundary rule (SRC/boundary.f90:12-199), so no separate boundary pass or
+// ghost-copy launch exists. The stage that finishes a step also reduces the
+// maximum signal speed for the next CFL time step (SRC/update.f90:13-59).
+//
+// Layout in HBM: structure of arrays, one row of ld = n + 2*GHOST doubles
+// per variable; cell i lives at column i + GHOST. qf rows are (rho, u, T,
+// Y_1..Y_K), Qc rows are (rho, rho u, rho e, rho Y_1..rho Y_K).
+//
+// Work split: one thread per face and per cell (team size 1); a CTA of NT
+// threads owns NT-1 cells and the NT faces that bound them, stages the
+// primitive state of its cells plus lvir halo cells in shared memory with
+// coalesced row loads, writes face fluxes to shared memory and then updates
+// its cells. Every per-species quantity is a streaming loop over constant
+// memory tables, so the kernel is bound by the FP64 pipe, not by HBM.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+
+#include "edyn_dev.cuh"
+#include "edyn_kernels.h"
+#include "recon.cuh"
+
+namespace edyn {
+
+__constant__ ThermoTable c_thermo;
+__constant__ FluidBC c_bc;
+
+static_assert(sizeof(ThermoTable) + sizeof(FluidBC) < 60000, "constant tables too large");
+
+// ---------------------------------------------------------------------------
+// Cell equation of state: QcToqf (SRC/eos.f90:49-83).
+// ys: per-thread strided species scratch holding rho*Y_k on entry; on exit it
+// holds the clipped, renormalised mass fractions (the qf species entries).
+// Returns T; writes u. strict = Newton starts at 1000 K as the reference.
+// ---------------------------------------------------------------------------
+struct CellEOS {
+  double T, u, Sz, cpR;  // cpR = Cp(T) of the final premix, for the sound speed
+};
+
+__device__ __forceinline__ void premix_cell(const double* ys, int st, double T, Premix& pm, double& Sz) {
+  const ThermoTable& tb = c_thermo;
+  pm.zero(t_interval(tb, T));
+  double sz = 0.0;
+  for (int k = 0; k < tb.ns; ++k) {
+    double z = ys[k * st] * tb.invW[k];
+    sz += z;
+    premix_add(tb, pm, k, z, T);
+  }
+  Sz = sz;
+}
+
+// Newton on sum z_k u_k(T) = e for T (temperature_con, SRC/thermo.f90:211-257)
+// in the premixed variables: g(T) = H(T) - T Sz - E, dg/dT = Cp(T) - Sz.
+// Stopping rules and the [20, 6000] K clamp are the reference's.
+__device__ __forceinline__ double t_newton(const double* ys, int st, double E, double T0, Premix& pm, double& Sz,
+                                           int& iters) {
+  const ThermoTable& tb = c_thermo;
+  double T = T0, g = 1e30, dT = 1e30;
+  int it = 0;
+  premix_cell(ys, st, T, pm, Sz);
+  while (fabs(g) >= fabs(E) * 1e-9 && fabs(dT) >= T * 1e-6 && it < 10) {
+    if (t_interval(tb, T) != pm.interval) premix_cell(ys, st, T, pm, Sz);
+    g = pm.H(T) - T * Sz - E;
+    double cvR = pm.Cp(T) - Sz;
+    dT = -g / cvR;
+    T = fmax(20.0, fmin(6000.0, T + dT));
+    ++it;
+  }
+  if (t_interval(tb, T) != pm.interval) premix_cell(ys, st, T, pm, Sz);
+  iters = it;
+  return T;
+}
+
+// Full QcToqf. On entry ys[k*st] = rho*Y_k. Writes the normalised Y_k back.
+__device__ __forceinline__ CellEOS qc_to_qf_cell(double rho, double rhou, double rhoe, double* ys, int st,
+                                                 double Tguess, bool strict, int& iters) {
+  const ThermoTable& tb = c_thermo;
+  CellEOS r;
+  const double inv_rho = 1.0 / rho;
+  r.u = rhou * inv_rho;
+  double s = 0.0;
+  for (int k = 0; k < tb.ns; ++k) {
+    double y = clip0(ys[k * st] * inv_rho);
+    ys[k * st] = y;
+    s += y;
+  }
+  const double inv_s = 1.0 / s;
+  for (int k = 0; k < tb.ns; ++k) ys[k * st] *= inv_s;
+  const double e_int = rhoe * inv_rho - 0.5 * (r.u * r.u);
+  const double E = e_int * (1.0 / R_SI);
+  Premix pm;
+  double Sz;
+  r.T = t_newton(ys, st, E, strict ? 1000.0 : Tguess, pm, Sz, iters);
+  r.Sz = Sz;
+  r.cpR = pm.Cp(r.T);
+  return r;
+}
+
+// Signal speed max(|u-a|,|u|,|u+a|) = |u| + a of calc_dt (SRC/update.f90:33-41)
+// from a cell's primitive state: a^2 = gamma p / rho = gamma R T Sz / S_Y.
+__device__ __forceinline__ double cell_speed(double u, double T, double Sz, double cpR) {
+  double gamma = cpR / (cpR - Sz);
+  double a = sqrt(gamma * R_SI * T * Sz);
+  return fabs(u) + a;
+}
+
+__device__ __forceinline__ void atomic_max_pos(unsigned long long* addr, double v) {
+  atomicMax(addr, (unsigned long long)__double_as_longlong(v));
+}
+
+// ---------------------------------------------------------------------------
+// Face equation of state for a reconstructed state (qfToQc + pressure +
+// sonic_speed, SRC/eos.f90:11-46, SRC/thermo.f90:166-179, 421-430).
+// ---------------------------------------------------------------------------
+struct FaceState {
+  double rho, u, T, p, a, E;     // E = rho e (total)
+  double inv_SY;                 // 1 / sum max(Y,0)
+};
+
+__device__ __forceinline__ void face_finish(FaceState& f, const Premix& pm, double SY, double Sz) {
+  f.inv_SY = 1.0 / SY;
+  const double rt = f.rho * f.T;
+  const double zr = Sz * f.inv_SY;              // S_z / S_Y = 1 / mean molar weight
+  f.p = R_SI * rt * zr;
+  const double e_int = R_SI * (pm.H(f.T) - f.T * Sz) * f.inv_SY;
+  f.E = f.rho * (e_int + 0.5 * (f.u * f.u));
+  const double cpR = pm.Cp(f.T);
+  const double gamma = cpR / (cpR - Sz);
+  f.a = sqrt(gamma * R_SI * f.T * zr);
+}
+
+// ---------------------------------------------------------------------------
+// Boundary ghost cells (SRC/boundary.f90). Computes the ghost cell g
+// (g < 0 left, g >= n right) primitive state from the interior conserved
+// state in global memory and stores it into the shared stencil.
+// ---------------------------------------------------------------------------
+__device__ void ghost_cell(const StageArgs& a, int g, double* dst, int dst_st, double* ys, int st) {
+  const ThermoTable& tb = c_thermo;
+  const int ns = tb.ns;
+  const int ld = a.ld;
+  double q0, q1, q2;
+  int iters;
+  if (g < 0) {
+    const int l = -g;  // 1..lvir
+    const int src = l - 1;
+    const double* Q = a.qc + src + GHOST;
+    if (a.lbound == 0) {  // lbound_wall 152-174
+      q0 = Q[0];
+      q1 = -Q[ld];
+      q2 = Q[2 * ld];
+      for (int k = 0; k < ns; ++k) ys[k * st] = Q[(3 + k) * ld];
+    } else {  // lbound_inlet 70-103
+      const double rho_in = Q[0];
+      const double u_in = c_bc.rho_u_in / rho_in;
+      q0 = rho_in;
+      q1 = c_bc.rho_u_in;
+      q2 = rho_in * (c_bc.e_in + 0.5 * (u_in * u_in));
+      for (int k = 0; k < ns; ++k) ys[k * st] = rho_in * c_bc.y_in[k];
+    }
+  } else {
+    const int l = g - a.n + 1;  // 1..lvir
+    const int src = a.n - l;
+    const double* Q = a.qc + src + GHOST;
+    if (a.rbound == 0) {  // rbound_wall 177-199
+      q0 = Q[0];
+      q1 = -Q[ld];
+      q2 = Q[2 * ld];
+      for (int k = 0; k < ns; ++k) ys[k * st] = Q[(3 + k) * ld];
+    } else {  // rbound_outlet 106-149: fixed p_out, T from the interior energy
+      const double rho_i = Q[0], inv = 1.0 / rho_i;
+      const double u_out = Q[ld] * inv;
+      const double e_out = Q[2 * ld] * inv - 0.5 * (u_out * u_out);
+      double sy = 0.0, sz = 0.0;
+      for (int k = 0; k < ns; ++k) {
+        double y = Q[(3 + k) * ld] * inv;  // no clipping in the reference here
+        ys[k * st] = y;
+        sy += y;
+        sz += y * tb.invW[k];
+      }
+      // temperature_con with the unclipped mole fractions: E scaled by S_Y.
+      Premix pm;
+      double Sz;
+      const double E = e_out * sy * (1.0 / R_SI);
+      double T_out = t_newton(ys, st, E, 1000.0, pm, Sz, iters);
+      (void)sz;
+      const double rho_out = a.p_out * sy / (R_SI * T_out * Sz);
+      const double e2 = R_SI * (pm.H(T_out) - T_out * Sz) / sy;
+      q0 = rho_out;
+      q1 = rho_out * u_out;
+      q2 = rho_out * (e2 + 0.5 * (u_out * u_out));
+      for (int k = 0; k < ns; ++k) ys[k * st] = rho_out * ys[k * st];
+    }
+  }
+  CellEOS e = qc_to_qf_cell(q0, q1, q2, ys, st, 1000.0, true, iters);
+  dst[0] = q0;
+  dst[dst_st] = e.u;
+  dst[2 * dst_st] = e.T;
+  for (int k = 0; k < ns; ++k) dst[(3 + k) * dst_st] = ys[k * st];
+}
+
+// ---------------------------------------------------------------------------
+// The stage kernel.
+// ---------------------------------------------------------------------------
+template <int ACU, int LIM, int WFLAG, int RIEMANN>
+__global__ void __launch_bounds__(STAGE_THREADS) k_stage(StageArgs a) {
+  constexpr int LV = acu_lvir(ACU);
+  extern __shared__ double sm[];
+  const int NT = blockDim.x;
+  const int TC = NT - 1;
+  const int tid = threadIdx.x;
+  const int c0 = blockIdx.x * TC;
+  const int Wd = TC + 2 * LV;  // stencil window [c0 - LV, c0 + TC + LV)
+  const ThermoTable& tb = c_thermo;
+  const int ns = a.ns, ne = ns + 3;
+  double* s_q = sm;                 // [ne][Wd]
+  double* s_y = s_q + ne * Wd;      // [2*ns][NT] raw Y_L, Y_R per face; reused
+  double* s_f = s_y + 2 * ns * NT;  // [ne][NT] face fluxes
+
+  // Device-driven time loop: k_step_begin decided whether this step runs
+  // and published its dt.
+  double dt = a.dt;
+  if (a.step_active) {
+    if (*a.step_active == 0) return;
+    dt = *a.dt_dev;
+  }
+
+  // 1. stage the primitive state window (coalesced row loads)
+  for (int idx = tid; idx < ne * Wd; idx += NT) {
+    const int v = idx / Wd, j = idx - v * Wd;
+    const int cell = c0 - LV + j;
+    if (cell >= 0 && cell < a.n) s_q[idx] = a.qf_in[(size_t)v * a.ld + cell + GHOST];
+  }
+  // ghost cells of the tube ends inside the window: thread t < LV takes the
+  // left ghost -1-t, thread LV <= t < 2 LV the right ghost n + t - LV.
+  if (tid < 2 * LV) {
+    const int g = (tid < LV) ? -1 - tid : a.n + (tid - LV);
+    if (g >= c0 - LV && g < c0 + TC + LV) ghost_cell(a, g, s_q + (g - (c0 - LV)), Wd, s_y + tid, NT);
+  }
+  __syncthreads();
+
+  // 2. one face per thread: face f between cells f-1 and f
+  const int f = c0 + tid;
+  if (f <= a.n) {
+    const int c = tid + LV - 1;  // window index of cell f-1
+    FaceState L, R;
+    recon<ACU, LIM, WFLAG>(s_q + 0 * Wd, c, L.rho, R.rho);
+    recon<ACU, LIM, WFLAG>(s_q + 1 * Wd, c, L.u, R.u);
+    recon<ACU, LIM, WFLAG>(s_q + 2 * Wd, c, L.T, R.T);
+    Premix pl, pr;
+    pl.zero(t_interval(tb, L.T));
+    pr.zero(t_interval(tb, R.T));
+    double syl = 0.0, syr = 0.0, szl = 0.0, szr = 0.0;
+    for (int k = 0; k < ns; ++k) {
+      double yl, yr;
+      recon<ACU, LIM, WFLAG>(s_q + (3 + k) * Wd, c, yl, yr);
+      s_y[(2 * k) * NT + tid] = yl;
+      s_y[(2 * k + 1) * NT + tid] = yr;
+      const double pl_ = clip0(yl), pr_ = clip0(yr);
+      syl += pl_;
+      syr += pr_;
+      const double zl = pl_ * tb.invW[k], zr = pr_ * tb.invW[k];
+      szl += zl;
+      szr += zr;
+      premix_add(tb, pl, k, zl, L.T);
+      premix_add(tb, pr, k, zr, R.T);
+    }
+    face_finish(L, pl, syl, szl);
+    face_finish(R, pr, syr, szr);
+    const double ml = L.rho * L.u, mr = R.rho * R.u;
+    // physical fluxes of the three bulk rows
+    const double fl0 = ml, fr0 = mr;
+    const double fl1 = ml * L.u + L.p, fr1 = mr * R.u + R.p;
+    const double fl2 = (L.E + L.p) * L.u, fr2 = (R.E + R.p) * R.u;
+    double* F = s_f + tid;
+    // species row k: flux = aL * YL + bL * max(YL,0) + aR * YR + bR * max(YR,0)
+    double aL = 0.0, bL = 0.0, aR = 0.0, bR = 0.0;
+    if (RIEMANN == 0) {  // LxF, SRC/flux.f90:287-294
+      const double lamL = fabs(L.u) + L.a, lamR = fabs(R.u) + R.a;
+      const double alpha = fmax(lamL, lamR);
+      F[0] = 0.5 * (fl0 + fr0 - alpha * (R.rho - L.rho));
+      F[NT] = 0.5 * (fl1 + fr1 - alpha * (mr - ml));
+      F[2 * NT] = 0.5 * (fl2 + fr2 - alpha * (R.E - L.E));
+      aL = 0.5 * ml;
+      aR = 0.5 * mr;
+      bR = -0.5 * alpha * R.rho * R.inv_SY;
+      bL = 0.5 * alpha * L.rho * L.inv_SY;
+    } else {
+      const double rt = sqrt(R.rho / L.rho);
+      const double inv1 = 1.0 / (1.0 + rt);
+      const double u_roe = (L.u + rt * R.u) * inv1;
+      const double a_roe = (L.a + rt * R.a) * inv1;
+      const double sL = fmin(L.u - L.a, u_roe - a_roe);
+      const double sR = fmax(R.u + R.a, u_roe + a_roe);
+      if (RIEMANN == 1) {  // HLL, SRC/flux.f90:296-315
+        if (0.0 <= sL) {
+          F[0] = fl0; F[NT] = fl1; F[2 * NT] = fl2;
+          aL = ml;
+        } else if (0.0 <= sR) {
+          const double inv = 1.0 / (sR - sL), ss = sL * sR;
+          F[0] = (sR * fl0 - sL * fr0 + ss * (R.rho - L.rho)) * inv;
+          F[NT] = (sR * fl1 - sL * fr1 + ss * (mr - ml)) * inv;
+          F[2 * NT] = (sR * fl2 - sL * fr2 + ss * (R.E - L.E)) * inv;
+          aL = sR * ml * inv;
+          aR = -sL * mr * inv;
+          bR = ss * R.rho * R.inv_SY * inv;
+          bL = -ss * L.rho * L.inv_SY * inv;
+        } else {
+          F[0] = fr0; F[NT] = fr1; F[2 * NT] = fr2;
+          aR = mr;
+        }
+      } else {  // HLLC, SRC/flux.f90:317-354
+        const double sM = (L.p - R.p + mr * (sR - R.u) - ml * (sL - L.u)) /
+                          (R.rho * (sR - R.u) - L.rho * (sL - L.u));
+        if (0.0 <= sL) {
+          F[0] = fl0; F[NT] = fl1; F[2 * NT] = fl2;
+          aL = ml;
+        } else if (0.0 <= sM) {
+          const double fac = L.rho * (sL - L.u) / (sL - sM);
+          const double ve = L.E / L.rho + (sM - L.u) * (sM + L.p / (L.rho * (sL - L.u)));
+          F[0] = fl0 + sL * (fac - L.rho);
+          F[NT] = fl1 + sL * (fac * sM - ml);
+          F[2 * NT] = fl2 + sL * (fac * ve - L.E);
+          aL = ml;
+          bL = sL * (fac - L.rho) * L.inv_SY;
+        } else if (0.0 <= sR) {
+          const double fac = R.rho * (sR - R.u) / (sR - sM);
+          const double ve = R.E / R.rho + (sM - R.u) * (sM + R.p / (R.rho * (sR - R.u)));
+          F[0] = fr0 + sR * (fac - R.rho);
+          F[NT] = fr1 + sR * (fac * sM - mr);
+          F[2 * NT] = fr2 + sR * (fac * ve - R.E);
+          aR = mr;
+          bR = sR * (fac - R.rho) * R.inv_SY;
+        } else {
+          F[0] = fr0; F[NT] = fr1; F[2 * NT] = fr2;
+          aR = mr;
+        }
+      }
+    }
+    for (int k = 0; k < ns; ++k) {
+      const double yl = s_y[(2 * k) * NT + tid], yr = s_y[(2 * k + 1) * NT + tid];
+      double v = aL * yl;
+      v = fma(bL, clip0(yl), v);
+      v = fma(aR, yr, v);
+      v = fma(bR, clip0(yr), v);
+      F[(3 + k) * NT] = v;
+    }
+  }
+  __syncthreads();
+
+  // 3. one cell per thread: conservative update + QcToqf
+  const int i = c0 + tid;
+  double speed = 0.0;
+  if (tid < TC && i < a.n) {
+    const double c = dt / a.dx;
+    const size_t ld = (size_t)a.ld;
+    double* Q = a.qc + i + GHOST;
+    double* Q0 = a.q0 + i + GHOST;
+    double* ys = s_y + tid;  // strided by NT
+    double q[3];
+    for (int v = 0; v < ne; ++v) {
+      const double dF = s_f[v * NT + tid + 1] - s_f[v * NT + tid];
+      const double qv = Q[v * ld];
+      double qn;
+      if (a.kind == 0) {  // Euler or first TVDRK3 stage: Q0 + (0 - c dF)
+        if (a.save_q0) Q0[v * ld] = qv;
+        qn = qv - c * dF;
+      } else {
+        qn = fma(a.h1, Q0[v * ld], a.h2 * (qv - c * dF));
+      }
+      Q[v * ld] = qn;
+      if (v < 3) q[v] = qn; else ys[(v - 3) * NT] = qn;
+    }
+    int iters;
+    const double Tg = s_q[2 * Wd + tid + LV];
+    CellEOS e = qc_to_qf_cell(q[0], q[1], q[2], ys, NT, Tg, a.strict_newton != 0, iters);
+    double* out = a.qf_out + i + GHOST;
+    out[0] = q[0];
+    out[ld] = e.u;
+    out[2 * ld] = e.T;
+    for (int k = 0; k < ns; ++k) out[(3 + k) * ld] = ys[k * NT];
+    if (a.cvel_out) speed = cell_speed(e.u, e.T, e.Sz, e.cpR);
+  }
+  if (a.cvel_out) {
+    double m = speed;
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((tid & 31) == 0 && m > 0.0) atomic_max_pos(a.cvel_out, m);
+  }
+  if (a.time && blockIdx.x == 0 && tid == 0) {
+    // No CTA of this kernel reads the clock; k_step_begin of the next step does.
+    *a.time = *a.time + dt;
+    *a.nsteps = *a.nsteps + 1;
+  }
+}
+
+// One thread: decides whether the step runs (time < tend, the loop test of
+// SRC/main.f90:130), computes dt = cfl dx / max speed (SRC/update.f90:50)
+// from the maximum left by the previous step, and clears the accumulator.
+__global__ void k_step_begin(const double* time, double tend, double cfl, double dx, unsigned long long* cvel,
+                             int* step_active, double* dt_dev) {
+  if (!(*time < tend)) {
+    *step_active = 0;
+    return;
+  }
+  const double cv = __longlong_as_double((long long)*cvel);
+  *dt_dev = (cfl * dx) / cv;
+  *step_active = 1;
+  *cvel = 0ull;
+}
+
+// Signal-speed maximum of the current primitive state (calc_dt).
+__global__ void k_cvel(const double* qf, int n, int ld, unsigned long long* cvel) {
+  const ThermoTable& tb = c_thermo;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double sp = 0.0;
+  if (i < n) {
+    const double* q = qf + i + GHOST;
+    const double T = q[2 * (size_t)ld];
+    Premix pm;
+    pm.zero(t_interval(tb, T));
+    double sz = 0.0, sy = 0.0;
+    for (int k = 0; k < tb.ns; ++k) {
+      const double y = q[(3 + k) * (size_t)ld];
+      const double z = y * tb.invW[k];
+      sy += y;
+      sz += z;
+      premix_add(tb, pm, k, z, T);
+    }
+    // calc_dt uses CKYTX without the clip; the stored Y are non-negative.
+    const double cpR = pm.Cp(T);
+    const double gamma = cpR / (cpR - sz);
+    const double a = sqrt(gamma * R_SI * T * sz / sy);
+    sp = fabs(q[ld]) + a;
+  }
+  double m = sp;
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomic_max_pos(cvel, m);
+}
+
+// ---------------------------------------------------------------------------
+// Layout conversion between the reference's AoS (nequ, ncell) arrays and
+// the device SoA rows.
+// ---------------------------------------------------------------------------
+__global__ void k_aos_to_soa(const double* aos, int ne, int n, double* soa, int ld) {
+  const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (size_t)ne * n) return;
+  const int i = (int)(idx / ne), v = (int)(idx - (size_t)i * ne);
+  soa[(size_t)v * ld + i + GHOST] = aos[idx];
+}
+
+__global__ void k_soa_to_aos(const double* soa, int ne, int n, int ld, double* aos) {
+  const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (size_t)ne * n) return;
+  const int i = (int)(idx / ne), v = (int)(idx - (size_t)i * ne);
+  aos[idx] = soa[(size_t)v * ld + i + GHOST];
+}
+
+// QcToqf for every interior cell (used after chemistry and when only Qc is
+// uploaded). Tguess from the current qf when warm.
+__global__ void k_qc_to_qf(StageArgs a) {
+  extern __shared__ double sm[];
+  const int ns = c_thermo.ns;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  const size_t ld = (size_t)a.ld;
+  double* ys = sm + threadIdx.x;
+  const double* Q = a.qc + i + GHOST;
+  for (int k = 0; k < ns; ++k) ys[k * blockDim.x] = Q[(3 + k) * ld];
+  int iters;
+  double* out = a.qf_out + i + GHOST;
+  const double Tg = a.qf_in ? a.qf_in[2 * ld + i + GHOST] : 1000.0;
+  CellEOS e = qc_to_qf_cell(Q[0], Q[ld], Q[2 * ld], ys, blockDim.x, Tg, a.strict_newton != 0 || !a.qf_in, iters);
+  out[0] = Q[0];
+  out[ld] = e.u;
+  out[2 * ld] = e.T;
+  for (int k = 0; k < ns; ++k) out[(3 + k) * ld] = ys[k * blockDim.x];
+}
+
+// Initial state of one cell from (T, p, u, X): initialize_variables
+// (SRC/params.f90:305-580, step profiles) and set_block_params
+// (SRC/block.f90:394-431).
+__global__ void k_init_cells(int n, const double* T, const double* p, const double* u, const double* X, int ldx,
+                             double* qf, double* qc, int ld) {
+  extern __shared__ double sm[];
+  const ThermoTable& tb = c_thermo;
+  const int ns = tb.ns;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double* xs = sm + threadIdx.x;
+  const int st = blockDim.x;
+  double s = 0.0;
+  for (int k = 0; k < ns; ++k) {
+    double x = clip0(X[(size_t)i * ldx + k]);
+    xs[k * st] = x;
+    s += x;
+  }
+  const double inv_s = 1.0 / s;
+  double wsum = 0.0;
+  for (int k = 0; k < ns; ++k) {
+    const double x = xs[k * st] * inv_s;
+    xs[k * st] = x;
+    wsum += x * tb.W[k];
+  }
+  const double Ti = T[i];
+  Premix pm;
+  pm.zero(t_interval(tb, Ti));
+  double sz = 0.0;
+  const double inv_w = 1.0 / wsum;
+  for (int k = 0; k < ns; ++k) {
+    const double y = xs[k * st] * tb.W[k] * inv_w;  // CKXTY
+    xs[k * st] = y;
+    const double z = y * tb.invW[k];
+    sz += z;
+    premix_add(tb, pm, k, z, Ti);
+  }
+  const double rho = p[i] * wsum / (R_SI * Ti);  // density(): sum X W p / (R T)
+  const double e_int = R_SI * (pm.H(Ti) - Ti * sz);
+  const double ui = u[i];
+  double* F = qf + i + GHOST;
+  double* C = qc + i + GHOST;
+  const size_t L = (size_t)ld;
+  F[0] = rho;
+  F[L] = ui;
+  F[2 * L] = Ti;
+  C[0] = rho;
+  C[L] = rho * ui;
+  C[2 * L] = rho * (e_int + 0.5 * (ui * ui));
+  for (int k = 0; k < ns; ++k) {
+    const double y = xs[k * st];
+    F[(3 + k) * L] = y;
+    C[(3 + k) * L] = rho * y;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Host side launchers
+// ---------------------------------------------------------------------------
+int fluid_upload_tables(const ThermoTable& tb, const FluidBC& bc, cudaStream_t s) {
+  cudaError_t e = cudaMemcpyToSymbolAsync(c_thermo, &tb, sizeof(tb), 0, cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) return (int)e;
+  e = cudaMemcpyToSymbolAsync(c_bc, &bc, sizeof(bc), 0, cudaMemcpyHostToDevice, s);
+  return (int)e;
+}
+
+size_t stage_smem_bytes(int acu, int ns, int nt) {
+  const int lv = acu_lvir(acu);
+  const int ne = ns + 3;
+  return sizeof(double) * ((size_t)ne * (nt - 1 + 2 * lv) + (size_t)2 * ns * nt + (size_t)ne * nt);
+}
+
+template <int ACU, int LIM, int WF, int RM>
+static cudaError_t launch_t(const StageArgs& a, int nt, cudaStream_t s) {
+  const size_t smem = stage_smem_bytes(ACU, a.ns, nt);
+  auto kern = k_stage<ACU, LIM, WF, RM>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  const int tc = nt - 1;
+  const int grid = (a.n + tc - 1) / tc;
+  kern<<<grid, nt, smem, s>>>(a);
+  return cudaGetLastError();
+}
+
+template <int ACU, int LIM, int WF>
+static cudaError_t launch_rm(const StageArgs& a, int rm, int nt, cudaStream_t s) {
+  if (rm == 0) return launch_t<ACU, LIM, WF, 0>(a, nt, s);
+  if (rm == 1) return launch_t<ACU, LIM, WF, 1>(a, nt, s);
+  return launch_t<ACU, LIM, WF, 2>(a, nt, s);
+}
+
+cudaError_t launch_stage(const StageArgs& a, int acu, int lim, int wflag, int rm, int nt, cudaStream_t s) {
+  switch (acu) {
+    case ACU_FIRST: return launch_rm<ACU_FIRST, 2, 3>(a, rm, nt, s);
+    case ACU_MUSCL:
+      if (lim == 1) return launch_rm<ACU_MUSCL, 1, 3>(a, rm, nt, s);
+      if (lim == 3) return launch_rm<ACU_MUSCL, 3, 3>(a, rm, nt, s);
+      if (lim == 4) return launch_rm<ACU_MUSCL, 4, 3>(a, rm, nt, s);
+      return launch_rm<ACU_MUSCL, 2, 3>(a, rm, nt, s);
+    case ACU_WENO3: return launch_rm<ACU_WENO3, 2, 3>(a, rm, nt, s);
+    case ACU_WENO5:
+      if (wflag == 2) return launch_rm<ACU_WENO5, 2, 2>(a, rm, nt, s);
+      return launch_rm<ACU_WENO5, 2, 3>(a, rm, nt, s);
+    default: return launch_rm<ACU_WENO7, 2, 3>(a, rm, nt, s);
+  }
+}
+
+cudaError_t launch_cvel(const double* qf, int n, int ld, unsigned long long* cvel, cudaStream_t s) {
+  k_cvel<<<(n + 127) / 128, 128, 0, s>>>(qf, n, ld, cvel);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_aos_to_soa(const double* aos, int ne, int n, double* soa, int ld, cudaStream_t s) {
+  const size_t tot = (size_t)ne * n;
+  k_aos_to_soa<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(aos, ne, n, soa, ld);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_soa_to_aos(const double* soa, int ne, int n, int ld, double* aos, cudaStream_t s) {
+  const size_t tot = (size_t)ne * n;
+  k_soa_to_aos<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(soa, ne, n, ld, aos);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_step_begin(const double* time, double tend, double cfl, double dx, unsigned long long* cvel,
+                              int* step_active, double* dt_dev, cudaStream_t s) {
+  k_step_begin<<<1, 1, 0, s>>>(time, tend, cfl, dx, cvel, step_active, dt_dev);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_qc_to_qf(const StageArgs& a, cudaStream_t s) {
+  const int nt = 64;
+  const size_t smem = sizeof(double) * (size_t)a.ns * nt;
+  k_qc_to_qf<<<(a.n + nt - 1) / nt, nt, smem, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_init_cells(int n, int ns, const double* T, const double* p, const double* u, const double* X,
+                              int ldx, double* qf, double* qc, int ld, cudaStream_t s) {
+  const int nt = 64;
+  const size_t smem = sizeof(double) * (size_t)ns * nt;
+  k_init_cells<<<(n + nt - 1) / nt, nt, smem, s>>>(n, T, p, u, X, ldx, qf, qc, ld);
+  return cudaGetLastError();
+}
+
+}  // namespace edyn

@@ -1,0 +1,185 @@
+// Face reconstruction of primitive variables (device).
+//
+// Restates SRC/muscl.f90 (muscl3 with minmod / superbee / MC limiters,
+// kappa = 1/3) and SRC/weno.f90 (weno3z, weno5 JS/Z, weno7z) for the fused
+// stage kernel. The limiter arithmetic is reorganised to spend as few FP64
+// instructions as possible: minmod is evaluated with integer compares and
+// the kappa blend is folded into two FMAs, which changes results only at
+// the level of rounding.
+#pragma once
+
+#include "edyn_dev.cuh"
+
+namespace edyn {
+
+enum Acu : int { ACU_FIRST = 0, ACU_MUSCL = 1, ACU_WENO3 = 2, ACU_WENO5 = 3, ACU_WENO7 = 4 };
+
+// Ghost depth per scheme (SRC/params.f90:161-173).
+__host__ __device__ constexpr int acu_lvir(int acu) {
+  return acu == ACU_FIRST ? 1 : acu == ACU_MUSCL ? 2 : acu == ACU_WENO3 ? 2 : acu == ACU_WENO5 ? 3 : 4;
+}
+
+#ifdef __CUDACC__
+
+// b = (3 - kappa) / (1 - kappa) evaluated as the reference does.
+__device__ __forceinline__ double muscl_b() { return (3.0 - 1.0 / 3.0) / (1.0 - 1.0 / 3.0); }
+
+__device__ __forceinline__ double superbee_f(double x, double y) {
+  return fmax(fmax(0.0, fmin(x, 2.0 * y)), fmin(2.0 * x, y));
+}
+__device__ __forceinline__ double mc_f(double x, double y) {
+  return fmax(0.0, fmin(fmin(2.0 * x, 2.0 * y), 0.5 * (x + y)));
+}
+
+// s points at q(i-1); faces between q(i) and q(i+1). LIM: 1 none, 2 minmod,
+// 3 superbee, 4 MC.
+template <int LIM>
+__device__ __forceinline__ void muscl3_d(const double* s, int stride, double& sl, double& sr) {
+  const double s0 = s[0], s1 = s[stride], s2 = s[2 * stride], s3 = s[3 * stride];
+  const double cm = 0.25 * (1.0 - 1.0 / 3.0), cp = 0.25 * (1.0 + 1.0 / 3.0);
+  const double dm_i = s1 - s0, dp_i = s2 - s1, dp_ip = s3 - s2;
+  const double dm_ip = dp_i;
+  if (LIM == 1) {
+    sl = fma(cp, dp_i, fma(cm, dm_i, s1));
+    sr = s2 - fma(cp, dm_ip, cm * dp_ip);
+    return;
+  }
+  const double b = muscl_b();
+  const double bdm_i = b * dm_i, bdp_i = b * dp_i, bdp_ip = b * dp_ip;
+  double lp_i, lm_i, lp_ip, lm_ip;
+  if (LIM == 2) {
+    lp_i = minmod_i(dp_i, bdm_i);
+    lm_i = minmod_i(dm_i, bdp_i);
+    lp_ip = minmod_i(dp_ip, bdp_i);  // b * dminus_ip == b * dplus_i
+    lm_ip = minmod_i(dm_ip, bdp_ip);
+  } else if (LIM == 3) {
+    lp_i = superbee_f(dp_i, bdm_i);
+    lm_i = superbee_f(dm_i, bdp_i);
+    lp_ip = superbee_f(dp_ip, bdp_i);
+    lm_ip = superbee_f(dm_ip, bdp_ip);
+  } else {
+    lp_i = mc_f(dp_i, bdm_i);
+    lm_i = mc_f(dm_i, bdp_i);
+    lp_ip = mc_f(dp_ip, bdp_i);
+    lm_ip = mc_f(dm_ip, bdp_ip);
+  }
+  sl = fma(cp, lp_i, fma(cm, lm_i, s1));
+  sr = s2 - fma(cp, lm_ip, cm * lp_ip);
+}
+
+// weno3z, s points at q(i-1).
+__device__ __forceinline__ void weno3z_d(const double* s, int st, double& sl, double& sr) {
+  const double eps = 1.0e-6;
+  const double s0 = s[0], s1 = s[st], s2 = s[2 * st], s3 = s[3 * st];
+  double b2 = (s0 - s1) * (s0 - s1), b1 = (s1 - s2) * (s1 - s2);
+  double tau = fabs(b2 - b1);
+  double q2 = tau / (eps + b2), q1 = tau / (eps + b1);
+  double a2 = 2.0 * fma(q2, q2, 1.0), a1 = fma(q1, q1, 1.0);
+  sl = 0.5 * (a2 * (3.0 * s1 - s0) + a1 * (s1 + s2)) / (a2 + a1);
+  b2 = (s3 - s2) * (s3 - s2);
+  b1 = (s2 - s1) * (s2 - s1);
+  tau = fabs(b2 - b1);
+  q2 = tau / (eps + b2);
+  q1 = tau / (eps + b1);
+  a2 = 2.0 * fma(q2, q2, 1.0);
+  a1 = fma(q1, q1, 1.0);
+  sr = 0.5 * (a2 * (3.0 * s2 - s3) + a1 * (s1 + s2)) / (a2 + a1);
+}
+
+template <int FLAG>  // 2 JS, 3 Z
+__device__ __forceinline__ void weno5_side(double p0, double p1, double p2, double p3, double p4, double& out) {
+  // p0..p4 ordered away from the face: candidate stencils as SRC/weno.f90:79-116.
+  const double eps = 1.0e-6, c13 = 13.0 / 12.0;
+  double t3a = p0 - 2.0 * p1 + p2, t3b = p0 - 4.0 * p1 + 3.0 * p2;
+  double t2a = p1 - 2.0 * p2 + p3, t2b = p1 - p3;
+  double t1a = p2 - 2.0 * p3 + p4, t1b = 3.0 * p2 - 4.0 * p3 + p4;
+  double b3 = fma(c13 * t3a, t3a, 0.25 * t3b * t3b);
+  double b2 = fma(c13 * t2a, t2a, 0.25 * t2b * t2b);
+  double b1 = fma(c13 * t1a, t1a, 0.25 * t1b * t1b);
+  double w3, w2, w1;
+  if (FLAG == 2) {
+    double e3 = eps + b3, e2 = eps + b2, e1 = eps + b1;
+    w3 = 1.0 / (e3 * e3);
+    w2 = 6.0 / (e2 * e2);
+    w1 = 3.0 / (e1 * e1);
+  } else {
+    double tau = fabs(b3 - b1);
+    double q3 = tau / (eps + b3), q2 = tau / (eps + b2), q1 = tau / (eps + b1);
+    w3 = fma(q3, q3, 1.0);
+    w2 = 6.0 * fma(q2, q2, 1.0);
+    w1 = 3.0 * fma(q1, q1, 1.0);
+  }
+  double v3 = 2.0 * p0 - 7.0 * p1 + 11.0 * p2;
+  double v2 = -p1 + 5.0 * p2 + 2.0 * p3;
+  double v1 = 2.0 * p2 + 5.0 * p3 - p4;
+  out = (w3 * v3 + w2 * v2 + w1 * v1) / (6.0 * (w3 + w2 + w1));
+}
+
+// weno5, s points at q(i-2).
+template <int FLAG>
+__device__ __forceinline__ void weno5_d(const double* s, int st, double& sl, double& sr) {
+  const double q0 = s[0], q1 = s[st], q2 = s[2 * st], q3 = s[3 * st], q4 = s[4 * st], q5 = s[5 * st];
+  weno5_side<FLAG>(q0, q1, q2, q3, q4, sl);
+  weno5_side<FLAG>(q5, q4, q3, q2, q1, sr);
+}
+
+// weno7z, s points at q(i-3); the eighth point repeats q(i+3) as the
+// reference does (SRC/flux.f90:231-232).
+__device__ __forceinline__ void weno7z_d(const double* s, int st, double& sl, double& sr) {
+  const double eps = 1.0e-6;
+  double q[8];
+#pragma unroll
+  for (int j = 0; j < 7; ++j) q[j] = s[j * st];
+  q[7] = q[6];
+#pragma unroll
+  for (int side = 0; side < 2; ++side) {
+    double p[7];
+#pragma unroll
+    for (int j = 0; j < 7; ++j) p[j] = side == 0 ? q[j] : q[7 - j];
+    double b4 = p[0] * (547.0 * p[0] - 3882.0 * p[1] + 4642.0 * p[2] - 1854.0 * p[3]) +
+                p[1] * (7043.0 * p[1] - 17246.0 * p[2] + 7042.0 * p[3]) + p[2] * (11003.0 * p[2] - 9402.0 * p[3]) +
+                2107.0 * (p[3] * p[3]);
+    double b3 = p[1] * (267.0 * p[1] - 1642.0 * p[2] + 1602.0 * p[3] - 494.0 * p[4]) +
+                p[2] * (2843.0 * p[2] - 5966.0 * p[3] + 1922.0 * p[4]) + p[3] * (3443.0 * p[3] - 2522.0 * p[4]) +
+                547.0 * (p[4] * p[4]);
+    double b2 = p[2] * (547.0 * p[2] - 2522.0 * p[3] + 1922.0 * p[4] - 494.0 * p[5]) +
+                p[3] * (3443.0 * p[3] - 5966.0 * p[4] + 1602.0 * p[5]) + p[4] * (2843.0 * p[4] - 1642.0 * p[5]) +
+                267.0 * (p[5] * p[5]);
+    double b1 = p[3] * (2107.0 * p[3] - 9402.0 * p[4] + 7042.0 * p[5] - 1854.0 * p[6]) +
+                p[4] * (11003.0 * p[4] - 17246.0 * p[5] + 4642.0 * p[6]) + p[5] * (7043.0 * p[5] - 3882.0 * p[6]) +
+                547.0 * (p[6] * p[6]);
+    double tau = fabs(b4 - b1);
+    double r4 = tau / (eps + b4), r3 = tau / (eps + b3), r2 = tau / (eps + b2), r1 = tau / (eps + b1);
+    double a4 = (1.0 / 35.0) * fma(r4, r4, 1.0), a3 = (12.0 / 35.0) * fma(r3, r3, 1.0);
+    double a2 = (18.0 / 35.0) * fma(r2, r2, 1.0), a1 = (4.0 / 35.0) * fma(r1, r1, 1.0);
+    double v4 = -3.0 * p[0] + 13.0 * p[1] - 23.0 * p[2] + 25.0 * p[3];
+    double v3 = 1.0 * p[1] - 5.0 * p[2] + 13.0 * p[3] + 3.0 * p[4];
+    double v2 = -1.0 * p[2] + 7.0 * p[3] + 7.0 * p[4] - 1.0 * p[5];
+    double v1 = 3.0 * p[3] + 13.0 * p[4] - 5.0 * p[5] + 1.0 * p[6];
+    double r = (a4 * v4 + a3 * v3 + a2 * v2 + a1 * v1) / (12.0 * (a4 + a3 + a2 + a1));
+    if (side == 0) sl = r; else sr = r;
+  }
+}
+
+// Reconstructs one variable at face f (between cells f-1 and f). `row`
+// points at the shared-memory row of the variable, `c` is the row index of
+// cell f-1.
+template <int ACU, int LIM, int WFLAG>
+__device__ __forceinline__ void recon(const double* row, int c, double& l, double& r) {
+  if (ACU == ACU_FIRST) {
+    l = row[c];
+    r = row[c + 1];
+  } else if (ACU == ACU_MUSCL) {
+    muscl3_d<LIM>(row + c - 1, 1, l, r);
+  } else if (ACU == ACU_WENO3) {
+    weno3z_d(row + c - 1, 1, l, r);
+  } else if (ACU == ACU_WENO5) {
+    weno5_d<WFLAG>(row + c - 2, 1, l, r);
+  } else {
+    weno7z_d(row + c - 3, 1, l, r);
+  }
+}
+
+#endif
+
+}  // namespace edyn

@@ -1,0 +1,234 @@
+"""Python host side of the GB300 hot path.
+
+A thin mirror of the reference's hot-path interface over the C ABI of
+``include/edyn_gpu.h``: ``Tube`` stands for the reference's per-rank block
+state with its calc_dt / solve_fluid / solve_source / post-step calls
+(SRC/update.f90:13-150, SRC/main.f90:130-163), ``Reactors`` for the batched
+``macks(dt, nspe+1, yiT, rho)`` contract (SRC/source.f90:58). Arrays follow
+the reference's layout: per cell a row of ``nequ`` values
+(rho, u, T, Y_1..Y_K) or (rho, rho u, rho e, rho Y_k), SI units.
+
+The compiled library is required: importing works without it, but every
+call raises ``RuntimeError`` when ``_lib/libedyn_gb300.so`` is missing. There
+is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from pathlib import Path
+from typing import Optional, Sequence
+
+import numpy as np
+
+PKG = Path(__file__).resolve().parent
+LIB_PATH = PKG / "_lib" / "libedyn_gb300.so"
+GRI30_DIR = PKG / "data" / "gri30"
+
+EDYN_OK = 0
+EDYN_E_ARG, EDYN_E_CUDA, EDYN_E_MECH, EDYN_E_NEWTON, EDYN_E_CHEM, EDYN_E_STATE = 1, 2, 4, 8, 16, 32
+
+# iflags / rparams slots (include/edyn_gpu.h)
+IF_SELECT_TIME, IF_SELECT_RIEMANN, IF_FLAG_ACU, IF_FLAG_MUSCL, IF_FLAG_WENO = 0, 1, 2, 3, 4
+IF_FLAG_LBOUND, IF_FLAG_RBOUND, IF_DO_REACTION, IF_STRICT_NEWTON, IF_CHEM_MODE = 5, 6, 7, 8, 9
+RP_DX, RP_P_OUT, RP_T_IN, RP_RHO_U_IN, RP_RTOL, RP_ATOL = 0, 1, 2, 3, 4, 5
+
+_D = ctypes.POINTER(ctypes.c_double)
+_lib = None
+
+
+class EdynError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"edyn status {code}: {msg}")
+        self.code = code
+
+
+def lib() -> ctypes.CDLL:
+    """Loads the in-tree GB300 library; raises if it was not built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        raise RuntimeError(
+            f"{LIB_PATH} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'`; "
+            "the hot path has no CPU fallback")
+    L = ctypes.CDLL(str(LIB_PATH))
+    vp, ip, dp, i, d, cp = ctypes.c_void_p, ctypes.POINTER(ctypes.c_int), _D, ctypes.c_int, ctypes.c_double, ctypes.c_char_p
+    L.edyn_init.argtypes = [cp, i, i, i, i, ip, i, dp, i, dp, ctypes.POINTER(vp)]
+    L.edyn_upload.argtypes = [vp, dp, dp]
+    L.edyn_init_cells.argtypes = [vp, dp, dp, dp, dp]
+    L.edyn_calc_dt.argtypes = [vp, d, dp]
+    L.edyn_solve_fluid.argtypes = [vp, d]
+    L.edyn_solve_source.argtypes = [vp, d, d]
+    L.edyn_post_step.argtypes = [vp]
+    L.edyn_step.argtypes = [vp, d, dp]
+    L.edyn_advance.argtypes = [vp, d, d, ctypes.c_longlong, dp, ctypes.POINTER(ctypes.c_longlong)]
+    L.edyn_download.argtypes = [vp, dp, dp, dp]
+    L.edyn_reactors.argtypes = [vp, i, dp, dp, dp, dp]
+    L.edyn_reactors_device.argtypes = [vp, i, vp, vp, vp, dp]
+    L.edyn_set_stream.argtypes = [vp, vp]
+    L.edyn_last_error.argtypes = [vp, ctypes.c_char_p, i]
+    L.edyn_finalize.argtypes = [vp]
+    L.edyn_mech_compile.argtypes = [cp, cp, ctypes.c_char_p, i]
+    L.edyn_version.restype = ctypes.c_char_p
+    _lib = L
+    return L
+
+
+def _ptr(a: Optional[np.ndarray]):
+    if a is None:
+        return None
+    assert a.dtype == np.float64 and a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data_as(_D)
+
+
+def mech_compile(chem_dir: str, out_path: str) -> None:
+    """CHEMKIN directory -> mech.edyn (the CKINTERP step)."""
+    buf = ctypes.create_string_buffer(512)
+    rc = lib().edyn_mech_compile(str(chem_dir).encode(), str(out_path).encode(), buf, 512)
+    if rc:
+        raise EdynError(rc, buf.value.decode())
+
+
+def species_names(mech_dir: str | os.PathLike = GRI30_DIR) -> list:
+    """Species names in mechanism order (from mech.edyn)."""
+    txt = (Path(mech_dir) / "mech.edyn").read_text().split()
+    i = txt.index("SPECIES")
+    n = int(txt[i + 1])
+    nel = int(txt[txt.index("ELEMENTS") + 1])
+    per = 5 + 14 + nel
+    return [txt[i + 2 + k * per] for k in range(n)]
+
+
+def lvir_for(flag_acu: int, flag_weno: int) -> int:
+    """Ghost depth of the scheme (SRC/params.f90:161-173)."""
+    if flag_acu == 0:
+        return 1
+    if flag_acu == 1:
+        return 2
+    return {1: 2, 2: 3, 3: 3, 4: 4}[flag_weno]
+
+
+class _Ctx:
+    def __init__(self, chem_dir, nspe, ncell, lvir, iflags, rparams, x_in):
+        L = lib()
+        self._h = ctypes.c_void_p()
+        fl = (ctypes.c_int * len(iflags))(*iflags)
+        rp = np.ascontiguousarray(rparams, dtype=np.float64)
+        xi = None if x_in is None else np.ascontiguousarray(x_in, dtype=np.float64)
+        rc = L.edyn_init(str(chem_dir).encode(), nspe, nspe + 3, ncell, lvir, fl, len(iflags), _ptr(rp), len(rp),
+                         _ptr(xi), ctypes.byref(self._h))
+        self.nspe, self.nequ, self.ncell = nspe, nspe + 3, ncell
+        if rc:
+            msg = self.last_error()
+            self.close()
+            raise EdynError(rc, msg)
+
+    def last_error(self) -> str:
+        buf = ctypes.create_string_buffer(512)
+        lib().edyn_last_error(self._h, buf, 512)
+        return buf.value.decode()
+
+    def _check(self, rc: int):
+        if rc:
+            raise EdynError(rc, self.last_error())
+
+    def set_stream(self, stream_handle: int | None):
+        self._check(lib().edyn_set_stream(self._h, ctypes.c_void_p(stream_handle or 0)))
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            lib().edyn_finalize(self._h)
+        self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Tube(_Ctx):
+    """One 1-D tube on the GPU, driven like the reference's time loop."""
+
+    def __init__(self, ncell: int, dx: float, *, chem_dir=GRI30_DIR, select_time=1, select_riemann=2, flag_acu=1,
+                 flag_muscl=2, flag_weno=0, flag_lbound=0, flag_rbound=0, do_reaction=0, strict_newton=1,
+                 chem_mode=0, p_out=101325.0, t_in=300.0, rho_u_in=0.0, rtol=1e-5, atol=1e-13,
+                 x_in: Optional[Sequence[float]] = None, nspe: Optional[int] = None):
+        names = species_names(chem_dir) if (Path(chem_dir) / "mech.edyn").exists() else None
+        nspe = nspe if nspe is not None else len(names)
+        lv = lvir_for(flag_acu, flag_weno)
+        iflags = [select_time, select_riemann, flag_acu, flag_muscl, flag_weno, flag_lbound, flag_rbound,
+                  do_reaction, strict_newton, chem_mode]
+        super().__init__(chem_dir, nspe, ncell, lv, iflags, [dx, p_out, t_in, rho_u_in, rtol, atol], x_in)
+        self.lvir = lv
+        self.dx = dx
+
+    def upload(self, qf: Optional[np.ndarray], qc: np.ndarray):
+        qc = np.ascontiguousarray(qc, dtype=np.float64)
+        qf = None if qf is None else np.ascontiguousarray(qf, dtype=np.float64)
+        self._check(lib().edyn_upload(self._h, _ptr(qf), _ptr(qc)))
+
+    def init_cells(self, T, p, u, X):
+        T, p, u = (np.ascontiguousarray(a, dtype=np.float64) for a in (T, p, u))
+        X = np.ascontiguousarray(X, dtype=np.float64)
+        self._check(lib().edyn_init_cells(self._h, _ptr(T), _ptr(p), _ptr(u), _ptr(X)))
+
+    def calc_dt(self, cfl: float) -> float:
+        d = ctypes.c_double()
+        self._check(lib().edyn_calc_dt(self._h, cfl, ctypes.byref(d)))
+        return d.value
+
+    def solve_fluid(self, dt: float):
+        self._check(lib().edyn_solve_fluid(self._h, dt))
+
+    def solve_source(self, dt: float, time: float = 0.0):
+        self._check(lib().edyn_solve_source(self._h, dt, time))
+
+    def post_step(self):
+        self._check(lib().edyn_post_step(self._h))
+
+    def step(self, cfl: float) -> float:
+        d = ctypes.c_double()
+        self._check(lib().edyn_step(self._h, cfl, ctypes.byref(d)))
+        return d.value
+
+    def advance(self, cfl: float, tend: float, time: float = 0.0, max_steps: int = 1 << 62):
+        t = ctypes.c_double(time)
+        n = ctypes.c_longlong(0)
+        self._check(lib().edyn_advance(self._h, cfl, tend, max_steps, ctypes.byref(t), ctypes.byref(n)))
+        return t.value, n.value
+
+    def download(self):
+        qf = np.empty((self.ncell, self.nequ))
+        qc = np.empty((self.ncell, self.nequ))
+        hrr = np.empty(self.ncell)
+        self._check(lib().edyn_download(self._h, _ptr(qf), _ptr(qc), _ptr(hrr)))
+        return qf, qc, hrr
+
+
+class Reactors(_Ctx):
+    """Batched constant-volume reactors (the macks contract) on the GPU."""
+
+    def __init__(self, *, chem_dir=GRI30_DIR, rtol=1e-5, atol=1e-13, chem_mode=0):
+        names = species_names(chem_dir)
+        iflags = [1, 2, 1, 2, 0, 0, 0, 1, 1, chem_mode]
+        super().__init__(chem_dir, len(names), 16, 2, iflags, [1.0, 101325.0, 300.0, 0.0, rtol, atol], None)
+
+    def integrate(self, rho: np.ndarray, dt: np.ndarray, yiT: np.ndarray, raise_on_fail: bool = True):
+        """Advances yiT (n x (nspe+1), [Y, T]) in place; returns the counters."""
+        rho = np.ascontiguousarray(rho, dtype=np.float64)
+        dt = np.ascontiguousarray(dt, dtype=np.float64)
+        assert yiT.dtype == np.float64 and yiT.flags["C_CONTIGUOUS"] and yiT.shape[1] == self.nspe + 1
+        st = np.zeros(4)
+        rc = lib().edyn_reactors(self._h, yiT.shape[0], _ptr(rho), _ptr(dt), _ptr(yiT), _ptr(st))
+        if rc and raise_on_fail:
+            raise EdynError(rc, self.last_error())
+        return {"rhs": int(st[0]), "steps": int(st[1]), "rejects": int(st[2]), "failed": int(st[3]), "status": rc}
+
+    def integrate_device(self, n: int, rho_ptr: int, dt_ptr: int, yiT_ptr: int):
+        st = np.zeros(4)
+        rc = lib().edyn_reactors_device(self._h, n, ctypes.c_void_p(rho_ptr), ctypes.c_void_p(dt_ptr),
+                                        ctypes.c_void_p(yiT_ptr), _ptr(st))
+        self._check(rc)
+        return {"rhs": int(st[0]), "steps": int(st[1]), "rejects": int(st[2]), "failed": int(st[3])}

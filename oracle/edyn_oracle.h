@@ -1,0 +1,149 @@
+/*
+ * CPU oracle for the EdynCFD per-cell hot path -- TEST INFRASTRUCTURE ONLY.
+ *
+ * This is a plain-C FP64 restatement of the reference's CPU algorithm
+ * (Keisuke043/fortranCFD, the SRC directory, plus the CHEMKIN-II v4.5 routines it
+ * calls, GRI/cklib.f). It exists to check the GPU library and to serve as
+ * the timed CPU baseline; nothing in the product links, imports or calls it.
+ * Every function follows the reference's operation order (compile with
+ * -ffp-contract=off) and cites the file:line it restates.
+ *
+ * Parity status: the reference cannot be compiled in this environment (no
+ * Fortran compiler, MPI or HDF5, and its chemistry integrator odes.f90 is not
+ * shipped), so the fluid path is "parity unpinned" against a reference run.
+ * The thermodynamics and equilibrium constants are pinned against the
+ * Cantera TP-equilibrium composition shipped with the reference
+ * (WORK/Examples/CH4_GRI3.0/MFR/equilTP_phi1.0_p1.0_T1300.0.txt); the stiff
+ * integrator is the project's own FP64 method (the reference's MACKS solver
+ * is absent), checked by self-convergence and conservation.
+ *
+ * Layouts follow the reference: per-cell vectors are AoS, qf(nequ) =
+ * (rho, u, T, Y_1..Y_nspe) and Qc(nequ) = (rho, rho*u, rho*e, rho*Y_k),
+ * SI units outside the CHEMKIN routines and cgs inside.
+ */
+#ifndef EDYN_ORACLE_H
+#define EDYN_ORACLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define OR_MAXSP 64
+#define OR_MAXRX 512
+
+typedef struct or_mech {
+  int nelem, kk, ii;
+  char ename[8][4];
+  double awt[8];
+  char kname[OR_MAXSP][24];
+  double wt[OR_MAXSP];
+  double tt[OR_MAXSP][3];         /* T low, T mid, T high */
+  double aa[OR_MAXSP][2][7];      /* [k][range 0 low, 1 high][coef] */
+  int ncf[OR_MAXSP][8];
+  int nspec_sign[OR_MAXRX];       /* +1 reversible, -1 irreversible */
+  int nu[OR_MAXRX][6], nunk[OR_MAXRX][6];
+  double par[OR_MAXRX][3];        /* A, beta, E/R */
+  int tb[OR_MAXRX], kfal[OR_MAXRX], ifop[OR_MAXRX];
+  double fpar[OR_MAXRX][7];       /* low A, beta, E/R, troe a, T***, T*, T** */
+  int ntbs[OR_MAXRX], nktb[OR_MAXRX][16];
+  double aik[OR_MAXRX][16];
+  double ru, patm;
+  double hf298[OR_MAXSP];         /* CKHMS(298.15) [erg/g] */
+} or_mech;
+
+/* Mechanism */
+int or_mech_load(const char* path, or_mech* m);
+int or_mech_sizeof(void);
+
+/* CHEMKIN-II restatements (cgs) */
+void or_ckytx(const or_mech* m, const double* y, double* x);
+void or_ckxty(const or_mech* m, const double* x, double* y);
+void or_ckpx(const or_mech* m, double rho, double t, const double* x, double* p);
+void or_ckrhox(const or_mech* m, double p, double t, const double* x, double* rho);
+void or_ckhml(const or_mech* m, double t, double* hml);
+void or_ckuml(const or_mech* m, double t, double* uml);
+void or_ckcpml(const or_mech* m, double t, double* cpml);
+void or_ckcvml(const or_mech* m, double t, double* cvml);
+void or_ckubml(const or_mech* m, double t, const double* x, double* ubml);
+void or_ckcvbl(const or_mech* m, double t, const double* x, double* cvbml);
+void or_ckcpbl(const or_mech* m, double t, const double* x, double* cpbml);
+void or_cksmh(const or_mech* m, double t, double* smh);
+void or_ckhms(const or_mech* m, double t, double* hms);
+void or_ckwyr(const or_mech* m, double rho, double t, const double* y, double* wdot);
+void or_ckrop(const or_mech* m, double rho, double t, const double* y, double* qf, double* qr);
+/* same, plus the effective rate constants (rate of progress per unit concentration product) */
+void or_ckrop_k(const or_mech* m, double rho, double t, const double* y, double* qf, double* qr, double* kf_eff,
+                double* kr_eff);
+void or_ckcdyr(const or_mech* m, double rho, double t, const double* y, double* cdot, double* ddot);
+
+/* SRC/thermo.f90 restatements (SI) */
+void or_adjust_sum(int n, double* v);
+double or_pressure(const or_mech* m, double rho, double t, const double* x);
+double or_density(const or_mech* m, double p, double t, const double* x);
+double or_temperature_con(const or_mech* m, double e, const double* x, int* iters);
+double or_cv(const or_mech* m, double t, const double* x);
+double or_cp(const or_mech* m, double t, const double* x);
+double or_specific_energy(const or_mech* m, double t, const double* x);
+double or_sonic_speed(const or_mech* m, double rho, double p, double t, const double* x);
+
+/* SRC/eos.f90 */
+void or_qf_to_qc(const or_mech* m, const double* qf, double* qc);
+void or_qc_to_qf(const or_mech* m, const double* qc, double* qf);
+
+/* SRC/muscl.f90, SRC/weno.f90 */
+void or_muscl3(const double* s, double* sl, double* sr, int flag_muscl);
+void or_weno3z(const double* s, double* sl, double* sr);
+void or_weno5(const double* s, double* sl, double* sr, int flag_weno);
+void or_weno7z(const double* s, double* sl, double* sr);
+
+/* 1-D tube state with ghost cells (equal-dx blocks collapse to one array). */
+typedef struct or_tube {
+  const or_mech* m;
+  int n, lvir, nequ, nspe;
+  int select_time, select_riemann, flag_acu, flag_muscl, flag_weno;
+  int flag_lbound, flag_rbound, do_reaction;
+  double dx;
+  double p_out, t_in, rho_u_in;
+  double x_in[OR_MAXSP], y_in[OR_MAXSP];
+  double rtol, atol;
+  double* qf;   /* (n + 2*lvir) * nequ, cell i at offset (i + lvir) * nequ */
+  double* qc;
+  double* q0;   /* n * nequ */
+  double* fplus;/* (n + 1) * nequ, face i-1/2 of cell i at offset i * nequ */
+  double* hrr;  /* n */
+  double* hrr_dot;
+  long chem_rhs_evals, chem_steps;
+} or_tube;
+
+or_tube* or_tube_create(const or_mech* m, int n, int lvir, const int* iflags, const double* rparams,
+                        const double* x_in);
+void or_tube_destroy(or_tube* t);
+void or_tube_set_interior(or_tube* t, const double* qf, const double* qc);
+void or_tube_get_interior(const or_tube* t, double* qf, double* qc);
+void or_tube_get_all(const or_tube* t, double* qf, double* qc);
+void or_update_boundary(or_tube* t);
+void or_ghost_qf(or_tube* t);
+double or_calc_dt(or_tube* t, double cfl);
+void or_calc_flux_advection(or_tube* t);
+void or_solve_fluid(or_tube* t, double dt);
+void or_solve_source(or_tube* t, double dt);
+void or_post_step(or_tube* t);
+double or_step(or_tube* t, double cfl);
+
+/* Initial conditions (SRC/params.f90:305-580 + SRC/block.f90:394-431). */
+void or_init_cell(const or_mech* m, double T, double p, double u, const double* x_in, double* qf, double* qc);
+
+/* Chemistry: project FP64 SDIRK4 reference integrator on [Y_1..Y_kk, T]. */
+typedef struct or_chem_stats { long steps, rejects, rhs, jac, newton_fail; } or_chem_stats;
+int or_reactor(const or_mech* m, double rho_si, double dt, double* yiT, double rtol, double atol,
+               or_chem_stats* st);
+void or_chem_rhs(const or_mech* m, double rho_cgs, const double* yT, double* f);
+int or_reactor_batch(const or_mech* m, int n, const double* rho_si, const double* dt, double* yiT, double rtol,
+                     double atol, int nthreads, long* rhs_total);
+
+int or_num_threads(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,33 @@
+import os
+import sys
+from pathlib import Path
+
+import pytest
+
+ROOT = Path(__file__).resolve().parent.parent
+sys.path.insert(0, str(ROOT))
+sys.path.insert(0, str(Path(__file__).resolve().parent))
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300) and the built sm_103a library")
+
+
+@pytest.fixture(scope="session")
+def oracle():
+    from oracle_ctypes import Oracle
+
+    return Oracle()
+
+
+@pytest.fixture(scope="session")
+def names():
+    from fortrancfd_gb300 import species_names
+
+    return species_names()
+
+
+def reference_dir():
+    """The reference checkout, when it is present on this machine."""
+    p = Path(os.environ.get("EDYN_REFERENCE", "/root/reference"))
+    return p if p.exists() else None

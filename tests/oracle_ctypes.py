@@ -1,0 +1,166 @@
+"""ctypes binding of the CPU oracle (oracle/_build/libedyn_oracle.so).
+
+Test infrastructure only: the oracle is the checker the GPU library is
+compared with, never part of the product path.
+"""
+from __future__ import annotations
+
+import ctypes
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent.parent
+ORACLE_SO = ROOT / "oracle" / "_build" / "libedyn_oracle.so"
+MECH = ROOT / "fortrancfd_gb300" / "data" / "gri30" / "mech.edyn"
+_D = ctypes.POINTER(ctypes.c_double)
+
+
+def _p(a):
+    return None if a is None else np.ascontiguousarray(a).ctypes.data_as(_D)
+
+
+class Oracle:
+    def __init__(self, mech_path: Path = MECH):
+        if not ORACLE_SO.exists():
+            subprocess.run(["make", "-s", "-C", str(ROOT / "oracle")], check=True)
+        L = ctypes.CDLL(str(ORACLE_SO))
+        self.L = L
+        self.mech = ctypes.create_string_buffer(L.or_mech_sizeof())
+        assert L.or_mech_load(str(mech_path).encode(), self.mech) == 0
+        vp, d, i = ctypes.c_void_p, ctypes.c_double, ctypes.c_int
+        L.or_tube_create.restype = vp
+        L.or_tube_create.argtypes = [vp, i, i, ctypes.POINTER(i), _D, _D]
+        L.or_tube_destroy.argtypes = [vp]
+        L.or_tube_set_interior.argtypes = [vp, _D, _D]
+        L.or_tube_get_interior.argtypes = [vp, _D, _D]
+        L.or_calc_dt.restype = d
+        L.or_calc_dt.argtypes = [vp, d]
+        L.or_solve_fluid.argtypes = [vp, d]
+        L.or_solve_source.argtypes = [vp, d]
+        L.or_post_step.argtypes = [vp]
+        L.or_step.restype = d
+        L.or_step.argtypes = [vp, d]
+        L.or_init_cell.argtypes = [vp, d, d, d, _D, _D, _D]
+        L.or_reactor.restype = i
+        L.or_reactor.argtypes = [vp, d, d, _D, d, d, ctypes.c_void_p]
+        L.or_reactor_batch.restype = i
+        L.or_reactor_batch.argtypes = [vp, i, _D, _D, _D, d, d, i, ctypes.POINTER(ctypes.c_long)]
+        L.or_chem_rhs.argtypes = [vp, d, _D, _D]
+        for nm in ("or_ckwyr", "or_ckrop"):
+            pass
+        L.or_ckwyr.argtypes = [vp, d, d, _D, _D]
+        L.or_ckrop.argtypes = [vp, d, d, _D, _D, _D]
+        L.or_cksmh.argtypes = [vp, d, _D]
+        L.or_ckhml.argtypes = [vp, d, _D]
+        L.or_ckuml.argtypes = [vp, d, _D]
+        L.or_ckcpml.argtypes = [vp, d, _D]
+        L.or_ckcvml.argtypes = [vp, d, _D]
+        L.or_ckytx.argtypes = [vp, _D, _D]
+        L.or_ckxty.argtypes = [vp, _D, _D]
+        L.or_temperature_con.restype = d
+        L.or_temperature_con.argtypes = [vp, d, _D, ctypes.POINTER(i)]
+        L.or_specific_energy.restype = d
+        L.or_specific_energy.argtypes = [vp, d, _D]
+        L.or_pressure.restype = d
+        L.or_pressure.argtypes = [vp, d, d, _D]
+        L.or_density.restype = d
+        L.or_density.argtypes = [vp, d, d, _D]
+        L.or_cv.restype = d
+        L.or_cv.argtypes = [vp, d, _D]
+        L.or_cp.restype = d
+        L.or_cp.argtypes = [vp, d, _D]
+        L.or_qc_to_qf.argtypes = [vp, _D, _D]
+        L.or_qf_to_qc.argtypes = [vp, _D, _D]
+        L.or_muscl3.argtypes = [_D, _D, _D, i]
+        L.or_weno5.argtypes = [_D, _D, _D, i]
+        L.or_weno3z.argtypes = [_D, _D, _D]
+        L.or_weno7z.argtypes = [_D, _D, _D]
+        L.or_adjust_sum.argtypes = [i, _D]
+        L.or_num_threads.restype = i
+        self.kk = 53
+        self.nequ = self.kk + 3
+
+    # --- per-point helpers
+    def vec(self, fn, T):
+        out = np.zeros(self.kk)
+        getattr(self.L, fn)(self.mech, T, _p(out))
+        return out
+
+    def wdot(self, rho_cgs, T, Y):
+        out = np.zeros(self.kk)
+        self.L.or_ckwyr(self.mech, rho_cgs, T, _p(np.ascontiguousarray(Y, dtype=float)), _p(out))
+        return out
+
+    def rop(self, rho_cgs, T, Y, nr=325):
+        qf = np.zeros(nr)
+        qr = np.zeros(nr)
+        self.L.or_ckrop(self.mech, rho_cgs, T, _p(np.ascontiguousarray(Y, dtype=float)), _p(qf), _p(qr))
+        return qf, qr
+
+    def init_cells(self, T, p, u, X):
+        n = len(T)
+        qf = np.zeros((n, self.nequ))
+        qc = np.zeros((n, self.nequ))
+        for i in range(n):
+            x = np.ascontiguousarray(X[i], dtype=float)
+            self.L.or_init_cell(self.mech, float(T[i]), float(p[i]), float(u[i]), _p(x), qf[i].ctypes.data_as(_D),
+                                qc[i].ctypes.data_as(_D))
+        return qf, qc
+
+    def tube(self, n, lvir, flags, rparams, x_in=None):
+        fl = (ctypes.c_int * 8)(*flags[:8])
+        rp = np.ascontiguousarray(rparams, dtype=float)
+        xi = np.zeros(self.kk) if x_in is None else np.ascontiguousarray(x_in, dtype=float)
+        h = self.L.or_tube_create(self.mech, n, lvir, fl, _p(rp), _p(xi))
+        return OracleTube(self, h, n, (rp, xi))
+
+    def reactor(self, rho_si, dt, yiT, rtol, atol):
+        y = np.ascontiguousarray(yiT, dtype=float).copy()
+        rc = self.L.or_reactor(self.mech, rho_si, dt, _p(y), rtol, atol, ctypes.c_void_p(
+            ctypes.addressof(ctypes.create_string_buffer(64))))
+        return y, rc
+
+    def reactor_batch(self, rho, dt, yiT, rtol, atol, nthreads=0):
+        y = np.ascontiguousarray(yiT, dtype=float).copy()
+        rhs = ctypes.c_long(0)
+        fails = self.L.or_reactor_batch(self.mech, len(rho), _p(np.ascontiguousarray(rho, dtype=float)),
+                                        _p(np.ascontiguousarray(dt, dtype=float)), _p(y), rtol, atol, nthreads,
+                                        ctypes.byref(rhs))
+        return y, fails, rhs.value
+
+
+class OracleTube:
+    def __init__(self, o: Oracle, h, n, keep):
+        self.o, self.h, self.n, self._keep = o, h, n, keep
+
+    def set_interior(self, qf, qc):
+        self.o.L.or_tube_set_interior(self.h, _p(np.ascontiguousarray(qf)), _p(np.ascontiguousarray(qc)))
+
+    def get(self):
+        qf = np.zeros((self.n, self.o.nequ))
+        qc = np.zeros((self.n, self.o.nequ))
+        self.o.L.or_tube_get_interior(self.h, _p(qf), _p(qc))
+        return qf, qc
+
+    def step(self, cfl):
+        return self.o.L.or_step(self.h, cfl)
+
+    def calc_dt(self, cfl):
+        return self.o.L.or_calc_dt(self.h, cfl)
+
+    def solve_fluid(self, dt):
+        self.o.L.or_solve_fluid(self.h, dt)
+
+    def solve_source(self, dt):
+        self.o.L.or_solve_source(self.h, dt)
+
+    def post_step(self):
+        self.o.L.or_post_step(self.h)
+
+    def __del__(self):
+        try:
+            self.o.L.or_tube_destroy(self.h)
+        except Exception:
+            pass

@@ -1,0 +1,97 @@
+"""GPU chemistry vs the FP64 reference integrator of the oracle.
+
+Bar (the benchmark spec): species within 1e-3 relative and peak temperature within
+0.1% of the FP64 reference for reacting cases. Species below 1e-6 in mass
+fraction are compared in absolute terms (1e-9).
+"""
+import numpy as np
+import pytest
+
+from fortrancfd_gb300 import Reactors, Tube, configs
+
+pytestmark = pytest.mark.gpu
+
+REF_RTOL, REF_ATOL = 1e-10, 1e-16
+
+
+def species_err(Yg, Yr, floor=1e-6):
+    big = np.abs(Yr) >= floor
+    rel = np.where(big, np.abs(Yg - Yr) / np.maximum(np.abs(Yr), floor), 0.0)
+    ab = np.where(~big, np.abs(Yg - Yr), 0.0)
+    return float(rel.max()), float(ab.max())
+
+
+def element_moles(Y, names, W):
+    # O, H, C, N, Ar atoms per unit mass
+    comp = {"O": [], "H": [], "C": [], "N": []}
+    import re
+    out = np.zeros((Y.shape[0], 4))
+    for k, nm in enumerate(names):
+        for e_i, e in enumerate("OHCN"):
+            cnt = 0
+            for sym, num in re.findall(r"([A-Z][a-z]?)(\d*)", nm.replace("(S)", "")):
+                if sym == e:
+                    cnt += int(num) if num else 1
+            out[:, e_i] += cnt * Y[:, k] / W[k]
+    return out
+
+
+def test_reactor_batch_vs_fp64_reference(oracle, names):
+    rho, dt, yiT, _ = configs.reactor_batch(96, seed=3)
+    ref, fails, _ = oracle.reactor_batch(rho, dt, yiT, REF_RTOL, REF_ATOL)
+    assert fails == 0
+    r = Reactors(rtol=1e-6, atol=1e-14)
+    y = yiT.copy()
+    st = r.integrate(rho, dt, y)
+    assert st["failed"] == 0 and st["rhs"] > 0
+    K = len(names)
+    rel_err, abs_err = species_err(y[:, :K], ref[:, :K])
+    assert rel_err < 1e-3, rel_err
+    assert abs_err < 1e-9, abs_err
+    assert np.max(np.abs(y[:, K] - ref[:, K]) / ref[:, K]) < 1e-3
+
+
+def test_reactor_conservation(oracle, names):
+    rho, dt, yiT, _ = configs.reactor_batch(64, seed=4)
+    W = configs.molecular_weights()
+    K = len(names)
+    r = Reactors(rtol=1e-6, atol=1e-14)
+    y = yiT.copy()
+    r.integrate(rho, dt, y)
+    e0 = element_moles(yiT[:, :K], names, W)
+    e1 = element_moles(y[:, :K], names, W)
+    assert np.max(np.abs(e1 - e0) / np.maximum(e0, 1e-12)) < 1e-6
+    assert np.max(np.abs(y[:, :K].sum(axis=1) - 1.0)) < 1e-8
+
+
+def test_reactor_matches_oracle_same_tolerance(oracle, names):
+    """Same method, same tolerance: only the FP32 Jacobian/LU differ."""
+    rho, dt, yiT, _ = configs.reactor_batch(48, seed=5)
+    ref, fails, _ = oracle.reactor_batch(rho, dt, yiT, 1e-6, 1e-14)
+    y = yiT.copy()
+    Reactors(rtol=1e-6, atol=1e-14).integrate(rho, dt, y)
+    K = len(names)
+    rel_err, _ = species_err(y[:, :K], ref[:, :K])
+    assert rel_err < 1e-3
+
+
+def test_tube_chemistry_short_run(oracle, names):
+    """Reacting detonation tube, a few full steps (fluid + chemistry)."""
+    case = configs.detonation(ncell=512, length=512 * 50e-6, driver=64 * 50e-6)
+    fl = case.flags
+    qf0, qc0 = oracle.init_cells(case.T, case.p, case.u, case.X)
+    ot = oracle.tube(case.ncell, 3, [1, 2, 2, 2, 3, 0, 1, 1], [case.dx, 101325.0, 300.0, 0.0, REF_RTOL, REF_ATOL])
+    ot.set_interior(qf0, qc0)
+    g = Tube(case.ncell, case.dx, flag_acu=2, flag_weno=3, flag_rbound=1, do_reaction=1, rtol=1e-6, atol=1e-14)
+    g.upload(qf0, qc0)
+    for _ in range(5):
+        ot.step(case.cfl)
+        g.step(case.cfl)
+    qf_o, _ = ot.get()
+    qf_g, _, hrr = g.download()
+    K = len(names)
+    assert np.max(np.abs(qf_g[:, 2] - qf_o[:, 2]) / qf_o[:, 2]) < 1e-3
+    rel_err, abs_err = species_err(qf_g[:, 3:], qf_o[:, 3:])
+    assert rel_err < 1e-3, rel_err
+    assert abs(qf_g[:, 2].max() - qf_o[:, 2].max()) / qf_o[:, 2].max() < 1e-3
+    assert np.all(np.isfinite(hrr))

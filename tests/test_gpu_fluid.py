@@ -1,0 +1,133 @@
+"""GPU fluid path vs the CPU oracle (restatement of the reference's CPU code).
+
+Tolerance: the reference's north star asks for pressure, velocity and
+temperature within 1e-10 relative for non-reacting flow; that is the bar
+used here, on the full Sod run and on short runs of every scheme.
+"""
+import numpy as np
+import pytest
+
+from fortrancfd_gb300 import Tube, configs, lvir_for
+
+pytestmark = pytest.mark.gpu
+
+R_SI = 8314.51
+TOL = 1e-10
+
+
+def pressure(qf, W):
+    Y = qf[:, 3:]
+    return qf[:, 0] * R_SI * qf[:, 2] * (Y / W).sum(axis=1)
+
+
+def rel(a, b, scale=None):
+    scale = np.maximum(np.abs(b), 1e-300) if scale is None else scale
+    return float(np.max(np.abs(a - b) / scale))
+
+
+def run_pair(oracle, case, nsteps, strict=1, use_advance=False):
+    W = configs.molecular_weights()
+    qf0, qc0 = oracle.init_cells(case.T, case.p, case.u, case.X)
+    fl = case.flags
+    lv = lvir_for(fl["flag_acu"], fl.get("flag_weno", 0))
+    ot = oracle.tube(case.ncell, lv, [fl["select_time"], fl["select_riemann"], fl["flag_acu"], fl["flag_muscl"],
+                                      fl.get("flag_weno", 0), fl["flag_lbound"], fl["flag_rbound"], 0],
+                     [case.dx, fl.get("p_out", 101325.0), 300.0, 0.0, 1e-5, 1e-13])
+    ot.set_interior(qf0, qc0)
+    kw = {k: v for k, v in fl.items() if k != "do_reaction"}
+    g = Tube(case.ncell, case.dx, strict_newton=strict, do_reaction=0, **kw)
+    g.upload(qf0, qc0)
+    t_o = 0.0
+    for _ in range(nsteps):
+        t_o += ot.step(case.cfl)
+    if use_advance:
+        t_g, n_g = g.advance(case.cfl, tend=1e9, max_steps=nsteps)
+        assert n_g >= nsteps
+    else:
+        t_g = 0.0
+        for _ in range(nsteps):
+            t_g += g.step(case.cfl)
+    qf_o, _ = ot.get()
+    qf_g, qc_g, _ = g.download()
+    return qf_o, qf_g, pressure(qf_o, W), pressure(qf_g, W), t_o, t_g
+
+
+def test_sod_full_run_parity(oracle):
+    """Config 1 to t_end = 0.6 ms: p, u, T within 1e-10 relative."""
+    case = configs.sod()
+    nsteps = 879
+    qf_o, qf_g, p_o, p_g, t_o, t_g = run_pair(oracle, case, nsteps)
+    umax = np.abs(qf_o[:, 1]).max()
+    assert t_o == pytest.approx(t_g, rel=1e-12)
+    assert t_o >= case.tend * 0.999
+    assert rel(p_g, p_o) < TOL
+    assert rel(qf_g[:, 2], qf_o[:, 2]) < TOL
+    # velocity: relative to the peak speed (u crosses zero)
+    assert float(np.max(np.abs(qf_g[:, 1] - qf_o[:, 1]))) / umax < TOL
+    assert rel(qf_g[:, 0], qf_o[:, 0]) < TOL
+
+
+def test_sod_device_loop_matches_host_loop(oracle):
+    case = configs.sod()
+    qf_o, qf_g, p_o, p_g, t_o, t_g = run_pair(oracle, case, 64, use_advance=True)
+    assert rel(p_g, p_o) < TOL
+    assert rel(qf_g[:, 2], qf_o[:, 2]) < TOL
+
+
+def test_sod_warm_newton_deviation(oracle):
+    """Warm-started temperature Newton: deviation from the reference's
+    1000 K start stays within the parity bar."""
+    case = configs.sod()
+    qf_o, qf_g, p_o, p_g, _, _ = run_pair(oracle, case, 200, strict=0)
+    assert rel(p_g, p_o) < TOL
+    assert rel(qf_g[:, 2], qf_o[:, 2]) < TOL
+
+
+@pytest.mark.parametrize("scheme", [
+    dict(flag_acu=0, select_riemann=2),
+    dict(flag_acu=1, flag_muscl=1, select_riemann=2),
+    dict(flag_acu=1, flag_muscl=3, select_riemann=1),
+    dict(flag_acu=1, flag_muscl=4, select_riemann=0),
+    dict(flag_acu=2, flag_weno=1, select_riemann=2),
+    dict(flag_acu=2, flag_weno=2, select_riemann=2),
+    dict(flag_acu=2, flag_weno=3, select_riemann=2),
+    dict(flag_acu=2, flag_weno=4, select_riemann=2),
+    dict(flag_acu=1, flag_muscl=2, select_riemann=2, select_time=0),
+])
+def test_schemes_short_run(oracle, scheme):
+    case = configs.sod(ncell=400)
+    case.flags.update(scheme)
+    case.flags.setdefault("flag_weno", 0)
+    qf_o, qf_g, p_o, p_g, _, _ = run_pair(oracle, case, 60)
+    assert rel(p_g, p_o) < TOL
+    assert rel(qf_g[:, 2], qf_o[:, 2]) < TOL
+
+
+def test_outlet_boundary_short_run(oracle):
+    """Fixed-pressure outlet (rbound_outlet) with WENO5 on a pressure jump."""
+    case = configs.sod(ncell=300)
+    case.flags.update(flag_acu=2, flag_weno=3, flag_rbound=1, p_out=101325.0)
+    qf_o, qf_g, p_o, p_g, _, _ = run_pair(oracle, case, 80)
+    assert rel(p_g, p_o) < TOL
+    assert rel(qf_g[:, 2], qf_o[:, 2]) < TOL
+
+
+def test_init_cells_matches_oracle(oracle):
+    case = configs.detonation(ncell=256)
+    qf_o, qc_o = oracle.init_cells(case.T, case.p, case.u, case.X)
+    g = Tube(case.ncell, case.dx, flag_acu=2, flag_weno=3, flag_rbound=1)
+    g.init_cells(case.T, case.p, case.u, case.X)
+    qf_g, qc_g, _ = g.download()
+    assert rel(qc_g[:, 2], qc_o[:, 2], np.abs(qc_o[:, 2]).max()) < 1e-13
+    assert rel(qf_g[:, 0], qf_o[:, 0]) < 1e-13
+    assert np.max(np.abs(qf_g[:, 3:] - qf_o[:, 3:])) < 1e-15
+
+
+def test_calc_dt_matches_oracle(oracle):
+    case = configs.sod()
+    qf0, qc0 = oracle.init_cells(case.T, case.p, case.u, case.X)
+    ot = oracle.tube(case.ncell, 2, [1, 2, 1, 2, 0, 0, 0, 0], [case.dx, 101325.0, 300.0, 0.0, 1e-5, 1e-13])
+    ot.set_interior(qf0, qc0)
+    g = Tube(case.ncell, case.dx)
+    g.upload(qf0, qc0)
+    assert g.calc_dt(0.5) == pytest.approx(ot.calc_dt(0.5), rel=1e-14)

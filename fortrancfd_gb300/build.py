@@ -1,4 +1,4 @@
-"""Builds the GB300 library (``_lib/libedyn_gb300.so``) and the CPU oracle.
+"""Builds the GB300 library (``_lib/libedyn_gb300.so``).
 
 The CUDA and C++ sources under ``csrc/`` compile for sm_103a only, one
 translation unit per nvcc process, in parallel, then link into one shared
@@ -71,17 +71,6 @@ def build_library(verbose: bool = False, force: bool = False) -> Path:
     return lib
 
 
-def build_oracle(verbose: bool = False) -> Path:
-    """Compiles the CPU oracle (test infrastructure) with its Makefile."""
-    r = subprocess.run(["make", "-s", "-C", str(ROOT / "oracle")], stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
-    if r.returncode != 0:
-        raise RuntimeError("oracle build failed:\n" + r.stdout.decode(errors="replace"))
-    if verbose and r.stdout:
-        print(r.stdout.decode(errors="replace"))
-    return ROOT / "oracle" / "_build" / "libedyn_oracle.so"
-
-
 if __name__ == "__main__":
     v = "-v" in sys.argv
     print(build_library(verbose=v, force="-f" in sys.argv))
-    print(build_oracle(verbose=v))

@@ -56,9 +56,9 @@ __constant__ double c_se[5] = {25.0 / 24.0 - 59.0 / 48.0, -49.0 / 48.0 + 17.0 / 
 // Packed table header (all offsets in bytes from the blob start).
 struct TabHdr {
   int ns, nr, nrp, nsp, npc, ntbl, total_bytes;
-  int o_A, o_B, o_E;          // double[nrp]
+  int o_A, o_B, o_E, o_lnA;    // double[nrp]
   int o_w0, o_w1, o_w2, o_w3, o_w4, o_w5;  // uint[nrp]
-  int o_sp_aux;               // double[nsp*8]: lowA lowB lowE troe_a T3 T1 T2 ifop
+  int o_sp_aux;               // double[nsp*9]: lowA lowB lowE troe_a T3 T1 T2 ifop ln(lowA)
   int o_sp_i;                 // int[nsp*4]: tb_off, tb_cnt, kfal (-1 mixture), flags
   int o_tb_am1;               // double[ntbl]
   int o_tb_sp;                // int[ntbl]
@@ -75,7 +75,7 @@ struct TabHdr {
 
 struct Tabs {
   const TabHdr* h;
-  const double *A, *B, *E, *aux, *tb_am1, *W, *invW, *tmid, *hf, *cs, *ch;
+  const double *A, *B, *E, *lnA, *aux, *tb_am1, *W, *invW, *tmid, *hf, *cs, *ch;
   const unsigned *w0, *w1, *w2, *w3, *w4, *w5, *ent;
   const int *spi, *tb_sp, *pc, *lane, *spc, *spp;
   int ns, nr, nrp, npc;
@@ -88,6 +88,7 @@ __device__ __forceinline__ Tabs bind_tabs(const char* base) {
   t.A = (const double*)(base + h.o_A);
   t.B = (const double*)(base + h.o_B);
   t.E = (const double*)(base + h.o_E);
+  t.lnA = (const double*)(base + h.o_lnA);
   t.w0 = (const unsigned*)(base + h.o_w0);
   t.w1 = (const unsigned*)(base + h.o_w1);
   t.w2 = (const unsigned*)(base + h.o_w2);
@@ -191,8 +192,16 @@ __device__ __forceinline__ RxnEval<R> eval_rxn(const Tabs& t, int i, R logT, R i
   RxnEval<R> o;
   const unsigned w0 = t.w0[i], w1 = t.w1[i], w2 = t.w2[i];
   const unsigned fl = w0 >> 24;
-  R kf = (R)t.A[i];
-  if (fl & F_EXP) kf = kf * M::ex((R)t.B[i] * logT - (R)t.E[i] * invT);
+  R kf;
+  if (sizeof(R) == sizeof(double)) {
+    // CKRATT 6645: A exp(beta ln T - E/T), as the reference evaluates it
+    kf = (R)t.A[i];
+    if (fl & F_EXP) kf = kf * M::ex((R)t.B[i] * logT - (R)t.E[i] * invT);
+  } else {
+    // single precision (Jacobian only): pre-exponentials up to 1e74 do not
+    // fit in FP32, so the logarithmic form is used
+    kf = M::ex((R)t.lnA[i] + (R)t.B[i] * logT - (R)t.E[i] * invT);
+  }
   R kr = 0;
   if (fl & F_REV) {
     // 1/Kc = exp(-sum nu (S/R - H/RT)) * pfac^(-sum nu)  (CKRATT, 6647-6667)
@@ -204,12 +213,12 @@ __device__ __forceinline__ RxnEval<R> eval_rxn(const Tabs& t, int i, R logT, R i
       const int nr_ = (w2 >> (4 * s)) & 15, np = (w2 >> (12 + 4 * s)) & 15;
       if (kr_ != 255u) {
         R mm = m[kr_];
-        mant *= (nr_ == 1) ? mm : mm * mm;
+        mant *= (nr_ == 1) ? mm : (nr_ == 2 ? mm * mm : mm * mm * mm);
         ex2 += nr_ * en[kr_];
       }
       if (kp != 255u) {
         R mm = (R)1 / m[kp];
-        mant *= (np == 1) ? mm : mm * mm;
+        mant *= (np == 1) ? mm : (np == 2 ? mm * mm : mm * mm * mm);
         ex2 -= np * en[kp];
       }
     }
@@ -220,6 +229,7 @@ __device__ __forceinline__ RxnEval<R> eval_rxn(const Tabs& t, int i, R logT, R i
     else if (dnu != 0) ikc = ikc * pow(pfac, (R)(-dnu));
     ikc = fmin(ikc, M::big());  // kr = kf / max(Kc, SMALL)
     kr = kf * ikc;
+    if (sizeof(R) != sizeof(double)) kr = fmin(kr, (R)1e30f);
   }
   o.cm = 1;
   o.pr = 0;
@@ -236,8 +246,9 @@ __device__ __forceinline__ RxnEval<R> eval_rxn(const Tabs& t, int i, R logT, R i
     }
     o.cm = cm;
     if (fl & F_FALL) {
-      const double* fp = t.aux + aux * 8;
-      const R k0 = (R)fp[0] * M::ex((R)fp[1] * logT - (R)fp[2] * invT);
+      const double* fp = t.aux + aux * 9;
+      const R k0 = (sizeof(R) == sizeof(double)) ? (R)fp[0] * M::ex((R)fp[1] * logT - (R)fp[2] * invT)
+                                                 : M::ex((R)fp[8] + (R)fp[1] * logT - (R)fp[2] * invT);
       const R pr = k0 * cm / kf;
       R pcor = pr / (1 + pr);
       const int ifop = (int)fp[7];
@@ -483,6 +494,10 @@ __device__ void jacobian32(const Tabs& t, WarpWork& w, const double* y, double r
   }
   const float idT = 1.f / ((float)((double)T + (double)dT - (double)T));
   for (int k = lane; k < n; k += 32) J[k * JS + ns] = (w.f2[k] - w.f1[k]) * idT;
+  __syncwarp();
+  // an entry that overflowed single precision carries no usable slope
+  for (int q = lane; q < n * JS; q += 32)
+    if (!isfinite(J[q])) J[q] = 0.f;
   __syncwarp();
 }
 
@@ -932,7 +947,7 @@ int chem_init(ChemState& s, const edyn_mech& m, const ThermoTable& tb, cudaStrea
   };
   std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return kind(a) < kind(b); });
   const int nrp = (nr + 31) / 32 * 32;
-  std::vector<double> A(nrp, 0.0), B(nrp, 0.0), E(nrp, 0.0);
+  std::vector<double> A(nrp, 0.0), B(nrp, 0.0), E(nrp, 0.0), lnA(nrp, -700.0);
   std::vector<unsigned> w0(nrp, 0xffffffu), w1(nrp, 0x08ffffffu), w2(nrp, 0u), w3(nrp, 0u), w4(nrp, 0u), w5(nrp, 0u);
   std::vector<double> aux;
   std::vector<int> spi, tb_sp;
@@ -943,6 +958,7 @@ int chem_init(ChemState& s, const edyn_mech& m, const ThermoTable& tb, cudaStrea
   for (int q = 0; q < nr; ++q) {
     const int i = order[q];
     A[q] = m.A[i];
+    lnA[q] = m.A[i] > 0 ? std::log(m.A[i]) : -700.0;
     B[q] = m.beta[i];
     E[q] = m.E_R[i];
     unsigned fl = 0;
@@ -999,9 +1015,9 @@ int chem_init(ChemState& s, const edyn_mech& m, const ThermoTable& tb, cudaStrea
       } else {
         fl |= F_CM | F_TB;
       }
-      double a8[8] = {m.low[i][0], m.low[i][1], m.low[i][2], m.troe[i][0], m.troe[i][1], m.troe[i][2], m.troe[i][3],
-                      (double)m.ifop[i]};
-      aux.insert(aux.end(), a8, a8 + 8);
+      double a9[9] = {m.low[i][0], m.low[i][1], m.low[i][2], m.troe[i][0], m.troe[i][1], m.troe[i][2], m.troe[i][3],
+                      (double)m.ifop[i], m.low[i][0] > 0 ? std::log(m.low[i][0]) : -700.0};
+      aux.insert(aux.end(), a9, a9 + 9);
       spi.push_back((int)tb_sp.size());
       spi.push_back(m.neff[i]);
       spi.push_back(m.kfal[i]);
@@ -1113,6 +1129,7 @@ int chem_init(ChemState& s, const edyn_mech& m, const ThermoTable& tb, cudaStrea
   h.o_A = bl.put(A.data(), A.size() * 8);
   h.o_B = bl.put(B.data(), B.size() * 8);
   h.o_E = bl.put(E.data(), E.size() * 8);
+  h.o_lnA = bl.put(lnA.data(), lnA.size() * 8);
   h.o_w0 = bl.put(w0.data(), w0.size() * 4);
   h.o_w1 = bl.put(w1.data(), w1.size() * 4);
   h.o_w2 = bl.put(w2.data(), w2.size() * 4);

@@ -124,7 +124,22 @@ __device__ __forceinline__ void weno5_d(const double* s, int st, double& sl, dou
 }
 
 // weno7z, s points at q(i-3); the eighth point repeats q(i+3) as the
-// reference does (SRC/flux.f90:231-232).
+// reference does (SRC/flux.f90:231-232). The smoothness indicators are sums
+// of O(1e4) q^2 terms that cancel almost completely where the data are
+// smooth; their weights then amplify rounding, so they are evaluated in the
+// reference's operation order without FMA contraction.
+__device__ __forceinline__ double m_(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double a_(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double s_(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double w7beta(double p0, double p1, double p2, double p3, double c00, double c01,
+                                         double c02, double c03, double c11, double c12, double c13, double c22,
+                                         double c23, double c33) {
+  // p0*(c00 p0 + c01 p1 + c02 p2 + c03 p3) + p1*(c11 p1 + c12 p2 + c13 p3) + p2*(c22 p2 + c23 p3) + c33 p3^2
+  double t0 = a_(a_(a_(m_(c00, p0), m_(c01, p1)), m_(c02, p2)), m_(c03, p3));
+  double t1 = a_(a_(m_(c11, p1), m_(c12, p2)), m_(c13, p3));
+  double t2 = a_(m_(c22, p2), m_(c23, p3));
+  return a_(a_(a_(m_(p0, t0), m_(p1, t1)), m_(p2, t2)), m_(c33, m_(p3, p3)));
+}
 __device__ __forceinline__ void weno7z_d(const double* s, int st, double& sl, double& sr) {
   const double eps = 1.0e-6;
   double q[8];
@@ -136,27 +151,24 @@ __device__ __forceinline__ void weno7z_d(const double* s, int st, double& sl, do
     double p[7];
 #pragma unroll
     for (int j = 0; j < 7; ++j) p[j] = side == 0 ? q[j] : q[7 - j];
-    double b4 = p[0] * (547.0 * p[0] - 3882.0 * p[1] + 4642.0 * p[2] - 1854.0 * p[3]) +
-                p[1] * (7043.0 * p[1] - 17246.0 * p[2] + 7042.0 * p[3]) + p[2] * (11003.0 * p[2] - 9402.0 * p[3]) +
-                2107.0 * (p[3] * p[3]);
-    double b3 = p[1] * (267.0 * p[1] - 1642.0 * p[2] + 1602.0 * p[3] - 494.0 * p[4]) +
-                p[2] * (2843.0 * p[2] - 5966.0 * p[3] + 1922.0 * p[4]) + p[3] * (3443.0 * p[3] - 2522.0 * p[4]) +
-                547.0 * (p[4] * p[4]);
-    double b2 = p[2] * (547.0 * p[2] - 2522.0 * p[3] + 1922.0 * p[4] - 494.0 * p[5]) +
-                p[3] * (3443.0 * p[3] - 5966.0 * p[4] + 1602.0 * p[5]) + p[4] * (2843.0 * p[4] - 1642.0 * p[5]) +
-                267.0 * (p[5] * p[5]);
-    double b1 = p[3] * (2107.0 * p[3] - 9402.0 * p[4] + 7042.0 * p[5] - 1854.0 * p[6]) +
-                p[4] * (11003.0 * p[4] - 17246.0 * p[5] + 4642.0 * p[6]) + p[5] * (7043.0 * p[5] - 3882.0 * p[6]) +
-                547.0 * (p[6] * p[6]);
-    double tau = fabs(b4 - b1);
-    double r4 = tau / (eps + b4), r3 = tau / (eps + b3), r2 = tau / (eps + b2), r1 = tau / (eps + b1);
-    double a4 = (1.0 / 35.0) * fma(r4, r4, 1.0), a3 = (12.0 / 35.0) * fma(r3, r3, 1.0);
-    double a2 = (18.0 / 35.0) * fma(r2, r2, 1.0), a1 = (4.0 / 35.0) * fma(r1, r1, 1.0);
-    double v4 = -3.0 * p[0] + 13.0 * p[1] - 23.0 * p[2] + 25.0 * p[3];
-    double v3 = 1.0 * p[1] - 5.0 * p[2] + 13.0 * p[3] + 3.0 * p[4];
-    double v2 = -1.0 * p[2] + 7.0 * p[3] + 7.0 * p[4] - 1.0 * p[5];
-    double v1 = 3.0 * p[3] + 13.0 * p[4] - 5.0 * p[5] + 1.0 * p[6];
-    double r = (a4 * v4 + a3 * v3 + a2 * v2 + a1 * v1) / (12.0 * (a4 + a3 + a2 + a1));
+    const double b4 = w7beta(p[0], p[1], p[2], p[3], 547.0, -3882.0, 4642.0, -1854.0, 7043.0, -17246.0, 7042.0,
+                             11003.0, -9402.0, 2107.0);
+    const double b3 = w7beta(p[1], p[2], p[3], p[4], 267.0, -1642.0, 1602.0, -494.0, 2843.0, -5966.0, 1922.0,
+                             3443.0, -2522.0, 547.0);
+    const double b2 = w7beta(p[2], p[3], p[4], p[5], 547.0, -2522.0, 1922.0, -494.0, 3443.0, -5966.0, 1602.0,
+                             2843.0, -1642.0, 267.0);
+    const double b1 = w7beta(p[3], p[4], p[5], p[6], 2107.0, -9402.0, 7042.0, -1854.0, 11003.0, -17246.0, 4642.0,
+                             7043.0, -3882.0, 547.0);
+    const double tau = fabs(s_(b4, b1));
+    const double r4 = tau / a_(eps, b4), r3 = tau / a_(eps, b3), r2 = tau / a_(eps, b2), r1 = tau / a_(eps, b1);
+    const double a4 = m_(1.0 / 35.0, a_(1.0, m_(r4, r4))), a3 = m_(12.0 / 35.0, a_(1.0, m_(r3, r3)));
+    const double a2 = m_(18.0 / 35.0, a_(1.0, m_(r2, r2))), a1 = m_(4.0 / 35.0, a_(1.0, m_(r1, r1)));
+    const double al = 1.0 / a_(a_(a_(a4, a3), a2), a1);
+    const double v4 = a_(a_(a_(m_(-3.0, p[0]), m_(13.0, p[1])), m_(-23.0, p[2])), m_(25.0, p[3]));
+    const double v3 = a_(a_(a_(m_(1.0, p[1]), m_(-5.0, p[2])), m_(13.0, p[3])), m_(3.0, p[4]));
+    const double v2 = a_(a_(a_(m_(-1.0, p[2]), m_(7.0, p[3])), m_(7.0, p[4])), m_(-1.0, p[5]));
+    const double v1 = a_(a_(a_(m_(3.0, p[3]), m_(13.0, p[4])), m_(-5.0, p[5])), m_(1.0, p[6]));
+    const double r = m_(m_(1.0 / 12.0, al), a_(a_(a_(m_(a4, v4), m_(a3, v3)), m_(a2, v2)), m_(a1, v1)));
     if (side == 0) sl = r; else sr = r;
   }
 }

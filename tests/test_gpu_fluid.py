@@ -99,8 +99,36 @@ def test_schemes_short_run(oracle, scheme):
     case.flags.update(scheme)
     case.flags.setdefault("flag_weno", 0)
     qf_o, qf_g, p_o, p_g, _, _ = run_pair(oracle, case, 60)
-    assert rel(p_g, p_o) < TOL
-    assert rel(qf_g[:, 2], qf_o[:, 2]) < TOL
+    tol = TOL
+    if case.flags["flag_acu"] == 2 and case.flags["flag_weno"] == 4:
+        # WENO7-Z (SRC/weno.f90:169-267) is ill-conditioned: its smoothness
+        # indicators are sums of ~1e4 q^2 terms that cancel where the data
+        # are smooth, so a one-ulp change of the input moves the reference
+        # algorithm's own result by ~1e-7. The bar is ten times that
+        # measured sensitivity of the oracle.
+        tol = max(TOL, 10 * ulp_sensitivity(oracle, case, 60))
+    assert rel(p_g, p_o) < tol
+    assert rel(qf_g[:, 2], qf_o[:, 2]) < tol
+
+
+def ulp_sensitivity(oracle, case, nsteps):
+    W = configs.molecular_weights()
+    fl = case.flags
+    lv = lvir_for(fl["flag_acu"], fl["flag_weno"])
+    qf0, qc0 = oracle.init_cells(case.T, case.p, case.u, case.X)
+    out = []
+    for pert in (False, True):
+        qc = qc0.copy()
+        if pert:
+            qc[:, 2] = np.nextafter(qc[:, 2], np.inf)
+        ot = oracle.tube(case.ncell, lv, [fl["select_time"], fl["select_riemann"], fl["flag_acu"], fl["flag_muscl"],
+                                          fl["flag_weno"], fl["flag_lbound"], fl["flag_rbound"], 0],
+                         [case.dx, 101325.0, 300.0, 0.0, 1e-5, 1e-13])
+        ot.set_interior(qf0, qc)
+        for _ in range(nsteps):
+            ot.step(case.cfl)
+        out.append(pressure(ot.get()[0], W))
+    return rel(out[1], out[0])
 
 
 def test_outlet_boundary_short_run(oracle):

@@ -1,0 +1,301 @@
+"""Benchmark of the GB300 per-cell hot path (one JSON line on rank 0).
+
+Workload (default): the CH4/O2 detonation tube of the reference's second
+benchmark configuration -- 20,000 cells of 50 um on a 1 m tube, a 1 cm
+driver at 3000 K / 30 atm, WENO5-Z + HLLC + SSP-RK3, CFL 0.4, detailed
+GRI-Mech 3.0 chemistry (53 species, 325 reactions) integrated per cell by
+the plain implicit integrator (FP64 residuals, FP32 Jacobian/LU).
+A step is one pass of the time loop body (calc_dt, three fluid stages,
+chemistry, post-step) over the whole tube: "cell-steps" = cells x steps.
+
+value: device time of K steps with the state resident in HBM, CUDA events
+on the library's stream (16-step CUDA-graph launches, L2 flushed between
+launches). e2e: the same steps through the C ABI with host buffers -- every
+step uploads qf/Qc from pinned host memory, steps, and downloads qf/Qc/HRR.
+--impl reference: the CPU restatement of the reference's algorithm (the
+oracle; the Fortran code does not build here) on all host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+METRIC = "cell-steps/s on 1 GB300: surrogate vs plain chemistry at ≤1e-3 species err"
+UNIT = "cell-steps/s"
+BYTES_PER_CELL_STEP = 4544  # algorithmic: fluid RK3 3632 B + chemistry 912 B per cell-step
+BYTES_CHEM_PER_CELL = 912   # chemistry launch: read qf (456 B) + write qf and Qc rows (456 B)
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=32)
+    p.add_argument("--warmup", type=int, default=16)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--cells", type=int, default=20000)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def peaks():
+    f = ROOT / "MEASURED_PEAKS.json"
+    if f.exists():
+        d = json.loads(f.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.idx), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([c.strip() for c in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.3)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=2)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[j] for r in self.rows for j in range(4) if len(r) > 5 + j and r[5 + j] == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def build_case(cells):
+    from fortrancfd_gb300 import configs
+
+    return configs.detonation(ncell=cells, length=cells * 50e-6)
+
+
+def reference_arm(args, rank, world):
+    """CPU restatement of the reference (oracle) on all host cores."""
+    if rank != 0:
+        return
+    sys.path.insert(0, str(ROOT / "tests"))
+    from oracle_ctypes import Oracle
+
+    o = Oracle()
+    case = build_case(args.cells)
+    qf0, qc0 = o.init_cells(case.T, case.p, case.u, case.X)
+    t = o.tube(case.ncell, 3, [1, 2, 2, 2, 3, 0, 1, 1], [case.dx, 101325.0, 300.0, 0.0, 1e-5, 1e-13])
+    t.set_interior(qf0, qc0)
+    for _ in range(args.warmup):
+        t.step(case.cfl)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        t.step(case.cfl)
+    el = time.perf_counter() - t0
+    v = case.ncell * args.steps / el
+    cores = o.L.or_num_threads()
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": case.name, "cells": case.ncell, "chemistry": "plain FP64 SDIRK4",
+                       "scheme": "WENO5-Z + HLLC + SSP-RK3"},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": f"{args.steps} full steps of the {case.ncell}-cell tube after {args.warmup}"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def cpu_baseline(case, budget_s=12.0):
+    """The oracle on the host cores over a bounded sample of the workload."""
+    sys.path.insert(0, str(ROOT / "tests"))
+    from oracle_ctypes import Oracle
+
+    o = Oracle()
+    qf0, qc0 = o.init_cells(case.T, case.p, case.u, case.X)
+    t = o.tube(case.ncell, 3, [1, 2, 2, 2, 3, 0, 1, 1], [case.dx, 101325.0, 300.0, 0.0, 1e-5, 1e-13])
+    t.set_interior(qf0, qc0)
+    t.step(case.cfl)
+    n = 0
+    t0 = time.perf_counter()
+    while True:
+        t.step(case.cfl)
+        n += 1
+        el = time.perf_counter() - t0
+        if el > budget_s or n >= 64:
+            break
+    return {"value": case.ncell * n / el, "unit": UNIT, "cores": o.L.or_num_threads(), "kind": "port",
+            "sample": f"{n} full steps (after 1) of the {case.ncell}-cell tube, {el:.1f} s"}
+
+
+def gpu_arm(args, rank, world, local):
+    import torch
+
+    from fortrancfd_gb300 import Tube
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=dev)
+    case = build_case(args.cells)
+    fl = case.flags
+    stream = torch.cuda.current_stream(dev)
+    tube = Tube(case.ncell, case.dx, flag_acu=2, flag_weno=fl["flag_weno"], flag_rbound=1, do_reaction=1,
+                strict_newton=0, rtol=1e-5, atol=1e-13)
+    tube.set_stream(stream.cuda_stream)
+    tube.init_cells(case.T, case.p, case.u, case.X)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)  # > 129 MB L2
+    per_graph = 16
+    # warm-up (also captures the step graph)
+    t_sim = 0.0
+    done = 0
+    while done < args.warmup:
+        t_sim, n = tube.advance(case.cfl, tend=1e9, time=t_sim, max_steps=per_graph)
+        done += n
+    iters = max(1, (args.steps + per_graph - 1) // per_graph)
+    steps = iters * per_graph
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize(dev)
+    dev_ms = 0.0
+    with ClockSampler(local) as clk:
+        for _ in range(iters):
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            t_sim, n = tube.advance(case.cfl, tend=1e9, time=t_sim, max_steps=per_graph)
+            e1.record(stream)
+            e1.synchronize()
+            dev_ms += e0.elapsed_time(e1)
+            assert n == per_graph
+    torch.cuda.synchronize(dev)
+    t_local = dev_ms / 1e3
+    if world > 1:
+        import torch.distributed as dist
+
+        tt = torch.tensor([t_local], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_max = float(tt.item())
+    else:
+        t_max = t_local
+    value = case.ncell * steps * world / t_max
+    # per-launch kernel durations for the roofline: chemistry and one fluid step
+    dt = tube.calc_dt(case.cfl)
+    chem_ms = []
+    fluid_ms = []
+    for _ in range(3):
+        flush.zero_()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        tube.solve_fluid(dt)
+        b.record(stream)
+        b.synchronize()
+        fluid_ms.append(a.elapsed_time(b))
+        flush.zero_()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        tube.solve_source(dt)
+        b.record(stream)
+        b.synchronize()
+        chem_ms.append(a.elapsed_time(b))
+    chem_s = statistics.median(chem_ms) / 1e3
+    fluid_s = statistics.median(fluid_ms) / 1e3
+    # end to end through the C ABI with pinned host buffers
+    ne = tube.nequ
+    qf_h = torch.empty((case.ncell, ne), dtype=torch.float64, pin_memory=True).numpy()
+    qc_h = torch.empty((case.ncell, ne), dtype=torch.float64, pin_memory=True).numpy()
+    hrr_h = torch.empty(case.ncell, dtype=torch.float64, pin_memory=True).numpy()
+    from fortrancfd_gb300.edyn import _ptr, lib
+
+    L = lib()
+    L.edyn_download(tube._h, _ptr(qf_h), _ptr(qc_h), _ptr(hrr_h))
+    e2e_steps = max(4, min(args.steps, 16))
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        tube.upload(qf_h, qc_h)
+        tube.step(case.cfl)
+        tube._check(L.edyn_download(tube._h, _ptr(qf_h), _ptr(qc_h), _ptr(hrr_h)))
+    torch.cuda.synchronize(dev)
+    e2e_el = time.perf_counter() - t0
+    if rank != 0:
+        return
+    hbm, src = peaks()
+    achieved = BYTES_CHEM_PER_CELL * case.ncell / chem_s / 1e9
+    cpu = None if args.no_cpu_baseline or world > 1 else cpu_baseline(case)
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * t_max / steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic",
+            "config": {"workload": case.name, "cells": case.ncell, "chemistry": "plain SDIRK4 (FP64 residual, "
+                       "FP32 analytic Jacobian/LU)", "scheme": "WENO5-Z + HLLC + SSP-RK3, CFL 0.4",
+                       "parallelism": f"replicas x{world}", "l2": "flushed between 16-step graph launches",
+                       "tolerances": "rtol 1e-5, atol 1e-13"},
+            "clocks": clk.summary(),
+            "e2e": {"value": case.ncell * e2e_steps / e2e_el, "unit": UNIT,
+                    "h2d_bytes_per_step": 2 * case.ncell * ne * 8,
+                    "d2h_bytes_per_step": (2 * case.ncell * ne + case.ncell) * 8},
+            "gpu_launches": steps * 5,
+            "roofline": {"bound": "hbm", "kernel": "k_tube_chem", "achieved": achieved, "peak": hbm,
+                         "peak_source": src, "unit": "GB/s", "frac": achieved / hbm,
+                         "traffic": None, "launch_ms": chem_s * 1e3, "fluid_step_ms": fluid_s * 1e3},
+            "cpu_baseline": cpu}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        reference_arm(args, rank, world)
+        return
+    gpu_arm(args, rank, world, local)
+
+
+if __name__ == "__main__":
+    main()

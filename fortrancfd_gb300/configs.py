@@ -10,6 +10,7 @@ not fall on a centre the cell classification is the same.
 from __future__ import annotations
 
 from dataclasses import dataclass, field
+from pathlib import Path
 
 import numpy as np
 
@@ -58,18 +59,86 @@ def sod(names=None, ncell: int = 1000, length: float = 1.0) -> TubeCase:
                          flag_lbound=0, flag_rbound=0, do_reaction=0), cfl=0.5, tend=0.6e-3)
 
 
-# Burnt driver gas: a fixed, documented CH4/O2 product mixture (major
-# species of the stoichiometric products with dissociation) used in place of
-# an equilibrium solve, which the reference delegates to Cantera.
-BURNT_CH4_O2 = {"CO2": 0.18, "H2O": 0.42, "CO": 0.14, "OH": 0.10, "H2": 0.05, "O2": 0.07, "H": 0.02, "O": 0.02}
+def _thermo_tables(mech_dir=GRI30_DIR):
+    txt = (Path(mech_dir) / "mech.edyn").read_text().split()
+    ne = int(txt[txt.index("ELEMENTS") + 1])
+    enames = [txt[txt.index("ELEMENTS") + 2 + 2 * e] for e in range(ne)]
+    i = txt.index("SPECIES")
+    n = int(txt[i + 1])
+    per = 5 + 14 + ne
+    tmid = np.zeros(n)
+    a = np.zeros((n, 2, 7))
+    comp = np.zeros((n, ne))
+    for k in range(n):
+        b = i + 2 + k * per
+        tmid[k] = float(txt[b + 3])
+        a[k] = np.array([float(v) for v in txt[b + 5:b + 19]]).reshape(2, 7)
+        comp[k] = [int(v) for v in txt[b + 19:b + 19 + ne]]
+    return enames, tmid, a, comp
+
+
+def gibbs_rt(T, mech_dir=GRI30_DIR):
+    """g_k / (R T) of every species from the NASA-7 polynomials."""
+    _, tmid, a, _ = _thermo_tables(mech_dir)
+    c = a[np.arange(len(tmid)), (T > tmid).astype(int)]
+    h = c[:, 0] + c[:, 1] * T / 2 + c[:, 2] * T ** 2 / 3 + c[:, 3] * T ** 3 / 4 + c[:, 4] * T ** 4 / 5 + c[:, 5] / T
+    s = c[:, 0] * np.log(T) + c[:, 1] * T + c[:, 2] * T ** 2 / 2 + c[:, 3] * T ** 3 / 3 + c[:, 4] * T ** 4 / 4 + c[:, 6]
+    return h - s
+
+
+def equilibrium_tp(X0: np.ndarray, T: float, p: float, mech_dir=GRI30_DIR, iters: int = 200) -> np.ndarray:
+    """Ideal-gas chemical equilibrium at fixed T [K], p [Pa] holding the
+    element totals of X0: Gibbs minimisation by the element-potential
+    method (n_k = N exp(-g_k/RT - ln(p/p0) + sum_e lambda_e a_ek), Newton on
+    lambda and ln N with step damping). Returns mole fractions."""
+    _, _, _, comp = _thermo_tables(mech_dir)
+    g = gibbs_rt(T, mech_dir) + np.log(p / ATM)
+    b = comp.T @ X0
+    act = b > 0
+    allowed = np.all(comp[:, ~act] == 0, axis=1)
+    A = comp[allowed][:, act]
+    gk = g[allowed]
+    be = b[act]
+    ne = A.shape[1]
+    # start: one reference species per element (O2, H2, CO, N2, AR) at a
+    # mole fraction of 0.1 fixes the element potentials
+    enames, _, _, _ = _thermo_tables(mech_dir)
+    names = species_names(mech_dir)
+    names_ok = [n for n, ok in zip(names, allowed) if ok]
+    act_names = [e for e, a_ in zip(enames, act) if a_]
+    ref = {"O": "O2", "H": "H2", "C": "CO", "N": "N2", "AR": "AR"}
+    rows = [names_ok.index(ref[e]) for e in act_names]
+    lam = np.linalg.solve(A[rows], gk[rows] + np.log(0.1))
+    lnN = 0.0
+    for _ in range(iters):
+        mu = np.clip(-gk + lnN + A @ lam, -700, 700)
+        n = np.exp(mu)
+        N = np.exp(lnN)
+        F = np.concatenate([A.T @ n - be, [n.sum() - N]])
+        J = np.zeros((ne + 1, ne + 1))
+        J[:ne, :ne] = (A * n[:, None]).T @ A
+        J[:ne, ne] = A.T @ n
+        J[ne, :ne] = A.T @ n
+        J[ne, ne] = n.sum() - N
+        d = np.linalg.lstsq(J, -F, rcond=None)[0]
+        step = 1.0 / max(1.0, np.abs(d).max() / 2.0)
+        lam += step * d[:ne]
+        lnN += step * d[ne]
+        if np.abs(F).max() < 1e-14 * max(1.0, be.max()):
+            break
+    mu = np.clip(-gk + lnN + A @ lam, -700, 700)
+    x = np.zeros(len(g))
+    x[allowed] = np.exp(mu)
+    return x / x.sum()
 
 
 def detonation(names=None, ncell: int = 20000, length: float = 1.0, driver: float = 0.01, T_drv: float = 3000.0,
                p_drv: float = 30 * ATM, phi: float = 1.0, p0: float = ATM, T0: float = 300.0,
                oxidizer: str = "O2", weno: int = 3) -> TubeCase:
     """CH4 detonation tube: fresh stoichiometric CH4/O2 at 1 atm, 300 K; a
-    hot high-pressure driver at x <= 1 cm; reflecting left wall, fixed
-    pressure outlet at 1 atm on the right; WENO5 + HLLC, TVDRK3, CFL 0.4."""
+    driver at x <= 1 cm holding the TP-equilibrium products of the fresh
+    mixture at 3000 K, 30 atm; reflecting left wall, fixed-pressure outlet at
+    1 atm on the right; WENO5 + HLLC, TVDRK3, CFL 0.4."""
     names = names or species_names(GRI30_DIR)
     dx = length / ncell
     xm = (np.arange(ncell) + 0.5) * dx
@@ -79,8 +148,8 @@ def detonation(names=None, ncell: int = 20000, length: float = 1.0, driver: floa
     else:  # air: O2 + 3.76 N2
         n = phi + 2.0 * 4.76
         fresh = mole_vector(names, {"CH4": phi / n, "O2": 2.0 / n, "N2": 2.0 * 3.76 / n})
-    burnt = mole_vector(names, BURNT_CH4_O2)
-    burnt /= burnt.sum()
+    # equilibrium products of the fresh mixture at the driver's T and p
+    burnt = equilibrium_tp(fresh, T_drv, p_drv)
     T = np.where(drv, T_drv, T0)
     p = np.where(drv, p_drv, p0)
     X = np.where(drv[:, None], burnt[None, :], fresh[None, :])

@@ -105,6 +105,7 @@ StageArgs base_args(Ctx* c) {
   a.rbound = c->rbound;
   a.p_out = c->p_out;
   a.strict_newton = c->strict;
+  a.bc = c->bc;
   return a;
 }
 
@@ -305,7 +306,8 @@ int edyn_init(const char* chem_dir, int nspe, int nequ, int ncell, int lvir, con
   CK(cudaMalloc(&c->d_cvel, sizeof(unsigned long long)));
   CK(cudaMalloc(&c->d_err, sizeof(unsigned)));
   CK(cudaMemsetAsync(c->d_err, 0, sizeof(unsigned), c->stream));
-  int rc = fluid_upload_tables(c->tb, c->bc, c->stream);
+  int rc = fluid_upload_tables(c->tb, c->stream);
+  if (rc == -1) return fail(c, EDYN_E_MECH, "a different mechanism is already loaded in this process");
   if (rc) return fail(c, EDYN_E_CUDA, "constant tables: %s", cudaGetErrorString((cudaError_t)rc));
   rc = chem_init(c->chem, m, c->tb, c->stream);
   if (rc) return fail(c, EDYN_E_CUDA, "chemistry tables: %s", cudaGetErrorString((cudaError_t)rc));

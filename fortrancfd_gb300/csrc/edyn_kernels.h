@@ -38,9 +38,10 @@ struct StageArgs {
   int lbound, rbound;
   double p_out;
   int strict_newton;     // 1: T Newton starts at 1000 K as the reference
+  FluidBC bc;            // inlet data (SRC/flow_bound.f90), passed by value
 };
 
-int fluid_upload_tables(const ThermoTable& tb, const FluidBC& bc, cudaStream_t s);
+int fluid_upload_tables(const ThermoTable& tb, cudaStream_t s);
 size_t stage_smem_bytes(int acu, int ns, int nt);
 cudaError_t launch_stage(const StageArgs& a, int acu, int lim, int wflag, int rm, int nt, cudaStream_t s);
 cudaError_t launch_cvel(const double* qf, int n, int ld, unsigned long long* cvel, cudaStream_t s);

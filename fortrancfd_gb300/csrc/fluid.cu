@@ -27,6 +27,8 @@
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
+#include <cstring>
+#include <mutex>
 
 #include "edyn_dev.cuh"
 #include "edyn_kernels.h"
@@ -35,9 +37,8 @@
 namespace edyn {
 
 __constant__ ThermoTable c_thermo;
-__constant__ FluidBC c_bc;
 
-static_assert(sizeof(ThermoTable) + sizeof(FluidBC) < 60000, "constant tables too large");
+static_assert(sizeof(ThermoTable) < 60000, "constant tables too large");
 
 // ---------------------------------------------------------------------------
 // Cell equation of state: QcToqf (SRC/eos.f90:49-83).
@@ -163,11 +164,11 @@ __device__ void ghost_cell(const StageArgs& a, int g, double* dst, int dst_st, d
       for (int k = 0; k < ns; ++k) ys[k * st] = Q[(3 + k) * ld];
     } else {  // lbound_inlet 70-103
       const double rho_in = Q[0];
-      const double u_in = c_bc.rho_u_in / rho_in;
+      const double u_in = a.bc.rho_u_in / rho_in;
       q0 = rho_in;
-      q1 = c_bc.rho_u_in;
-      q2 = rho_in * (c_bc.e_in + 0.5 * (u_in * u_in));
-      for (int k = 0; k < ns; ++k) ys[k * st] = rho_in * c_bc.y_in[k];
+      q1 = a.bc.rho_u_in;
+      q2 = rho_in * (a.bc.e_in + 0.5 * (u_in * u_in));
+      for (int k = 0; k < ns; ++k) ys[k * st] = rho_in * a.bc.y_in[k];
     }
   } else {
     const int l = g - a.n + 1;  // 1..lvir
@@ -546,11 +547,26 @@ __global__ void k_init_cells(int n, const double* T, const double* p, const doub
 // ---------------------------------------------------------------------------
 // Host side launchers
 // ---------------------------------------------------------------------------
-int fluid_upload_tables(const ThermoTable& tb, const FluidBC& bc, cudaStream_t s) {
-  cudaError_t e = cudaMemcpyToSymbolAsync(c_thermo, &tb, sizeof(tb), 0, cudaMemcpyHostToDevice, s);
+// The thermodynamic table lives in constant memory, once per device: every
+// context on a device must use the same mechanism (checked against the
+// table uploaded first on that device).
+int fluid_upload_tables(const ThermoTable& tb, cudaStream_t s) {
+  static std::mutex mu;
+  static bool loaded[64];
+  static ThermoTable first[64];
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return (int)e;
-  e = cudaMemcpyToSymbolAsync(c_bc, &bc, sizeof(bc), 0, cudaMemcpyHostToDevice, s);
-  return (int)e;
+  if (dev < 0 || dev >= 64) return (int)cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lock(mu);
+  if (loaded[dev]) return std::memcmp(&first[dev], &tb, sizeof(tb)) == 0 ? (int)cudaSuccess : -1;
+  e = cudaMemcpyToSymbolAsync(c_thermo, &tb, sizeof(tb), 0, cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) return (int)e;
+  e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return (int)e;
+  first[dev] = tb;
+  loaded[dev] = true;
+  return (int)cudaSuccess;
 }
 
 size_t stage_smem_bytes(int acu, int ns, int nt) {

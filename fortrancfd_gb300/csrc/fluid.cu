@@ -221,7 +221,19 @@ __global__ void __launch_bounds__(STAGE_THREADS) k_stage(StageArgs a) {
   const int NT = blockDim.x;
   const int TC = NT - 1;
   const int tid = threadIdx.x;
-  const int c0 = blockIdx.x * TC;
+  // Tile of this CTA: cells [c0, c1), TC wide. The right-end ghost cells are
+  // built from the conserved state of the last LV cells, which the stage
+  // updates in place, so those cells and every window that holds a ghost
+  // built from them must belong to one CTA: when the last tile would hold
+  // fewer than LV cells, the boundary between the last two tiles moves to
+  // n - LV. (The first tile always holds the first LV cells.)
+  const int nb = gridDim.x;
+  int c0 = blockIdx.x * TC;
+  int c1 = min(c0 + TC, a.n);
+  if (nb >= 2 && a.n - (nb - 1) * TC < LV) {
+    if ((int)blockIdx.x == nb - 1) c0 = a.n - LV;
+    if ((int)blockIdx.x == nb - 2) c1 = a.n - LV;
+  }
   const int Wd = TC + 2 * LV;  // stencil window [c0 - LV, c0 + TC + LV)
   const ThermoTable& tb = c_thermo;
   const int ns = a.ns, ne = ns + 3;
@@ -247,13 +259,13 @@ __global__ void __launch_bounds__(STAGE_THREADS) k_stage(StageArgs a) {
   // left ghost -1-t, thread LV <= t < 2 LV the right ghost n + t - LV.
   if (tid < 2 * LV) {
     const int g = (tid < LV) ? -1 - tid : a.n + (tid - LV);
-    if (g >= c0 - LV && g < c0 + TC + LV) ghost_cell(a, g, s_q + (g - (c0 - LV)), Wd, s_y + tid, NT);
+    if (g >= c0 - LV && g < c1 + LV) ghost_cell(a, g, s_q + (g - (c0 - LV)), Wd, s_y + tid, NT);
   }
   __syncthreads();
 
   // 2. one face per thread: face f between cells f-1 and f
   const int f = c0 + tid;
-  if (f <= a.n) {
+  if (f <= c1) {
     const int c = tid + LV - 1;  // window index of cell f-1
     FaceState L, R;
     recon<ACU, LIM, WFLAG>(s_q + 0 * Wd, c, L.rho, R.rho);
@@ -363,7 +375,7 @@ __global__ void __launch_bounds__(STAGE_THREADS) k_stage(StageArgs a) {
   // 3. one cell per thread: conservative update + QcToqf
   const int i = c0 + tid;
   double speed = 0.0;
-  if (tid < TC && i < a.n) {
+  if (i < c1) {
     const double c = dt / a.dx;
     const size_t ld = (size_t)a.ld;
     double* Q = a.qc + i + GHOST;

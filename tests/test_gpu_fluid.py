@@ -140,6 +140,25 @@ def test_outlet_boundary_short_run(oracle):
     assert rel(qf_g[:, 2], qf_o[:, 2]) < TOL
 
 
+@pytest.mark.parametrize("ncell,scheme", [
+    (316, dict(flag_acu=1, flag_muscl=2)),                                  # last tile 1 cell, ghost depth 2
+    (317, dict(flag_acu=2, flag_weno=3)),                                   # last tile 2 cells, ghost depth 3
+    (316, dict(flag_acu=2, flag_weno=3, flag_rbound=1, p_out=101325.0)),   # outlet, last tile 1 cell
+])
+def test_short_last_tile(oracle, ncell, scheme):
+    """Tube lengths whose last 63-cell stage tile holds fewer cells than the
+    ghost depth, run until the waves have crossed the right end: the right
+    ghosts are built from cells that the stage updates in place."""
+    case = configs.sod(ncell=ncell)
+    case.flags.update(scheme)
+    case.flags.setdefault("flag_weno", 0)
+    qf_o, qf_g, p_o, p_g, _, _ = run_pair(oracle, case, 400)
+    assert rel(p_g, p_o) < TOL
+    assert rel(qf_g[:, 2], qf_o[:, 2]) < TOL
+    umax = np.abs(qf_o[:, 1]).max()
+    assert float(np.max(np.abs(qf_g[:, 1] - qf_o[:, 1]))) / umax < TOL
+
+
 def test_init_cells_matches_oracle(oracle):
     case = configs.detonation(ncell=256)
     qf_o, qc_o = oracle.init_cells(case.T, case.p, case.u, case.X)

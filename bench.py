@@ -35,6 +35,9 @@ METRIC = "cell-steps/s on 1 GB300: surrogate vs plain chemistry at ≤1e-3 speci
 UNIT = "cell-steps/s"
 BYTES_PER_CELL_STEP = 4544  # algorithmic: fluid RK3 3632 B + chemistry 912 B per cell-step
 BYTES_CHEM_PER_CELL = 912   # chemistry launch: read qf (456 B) + write qf and Qc rows (456 B)
+# DRAM bytes (read + write) of one chemistry launch per cell, from an ncu
+# capture of the 4,000-cell tube (2.22 MB read, 0 B written), scaled by cells
+TRAFFIC_CHEM_PER_CELL = 2.22e6 / 4000
 
 
 def parse():
@@ -53,6 +56,25 @@ def dist_env():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     return rank, world, local
+
+
+def max_over_ranks(t_local: float, world: int, device=None) -> float:
+    """Max of a per-rank time over all ranks (the whole job ends with the
+    slowest rank); the identity at world size 1."""
+    if world == 1:
+        return t_local
+    import torch
+    import torch.distributed as dist
+
+    tt = torch.tensor([t_local], dtype=torch.float64, device=device)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    return float(tt.item())
+
+
+def job_value(cells_per_rank: int, steps: int, world: int, t_max: float) -> float:
+    """Whole-job cell-steps/s: every rank advances its own replica of the
+    tube, so the units of all ranks count over the slowest rank's time."""
+    return cells_per_rank * steps * world / t_max
 
 
 def peaks():
@@ -213,16 +235,8 @@ def gpu_arm(args, rank, world, local):
             dev_ms += e0.elapsed_time(e1)
             assert n == per_graph
     torch.cuda.synchronize(dev)
-    t_local = dev_ms / 1e3
-    if world > 1:
-        import torch.distributed as dist
-
-        tt = torch.tensor([t_local], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_max = float(tt.item())
-    else:
-        t_max = t_local
-    value = case.ncell * steps * world / t_max
+    t_max = max_over_ranks(dev_ms / 1e3, world, dev)
+    value = job_value(case.ncell, steps, world, t_max)
     # per-launch kernel durations for the roofline: chemistry and one fluid step
     dt = tube.calc_dt(case.cfl)
     chem_ms = []
@@ -283,7 +297,7 @@ def gpu_arm(args, rank, world, local):
             "gpu_launches": steps * 5,
             "roofline": {"bound": "hbm", "kernel": "k_tube_chem", "achieved": achieved, "peak": hbm,
                          "peak_source": src, "unit": "GB/s", "frac": achieved / hbm,
-                         "traffic": None, "launch_ms": chem_s * 1e3, "fluid_step_ms": fluid_s * 1e3},
+                         "traffic": TRAFFIC_CHEM_PER_CELL * case.ncell, "launch_ms": chem_s * 1e3, "fluid_step_ms": fluid_s * 1e3},
             "cpu_baseline": cpu}
     print(json.dumps(line), flush=True)
 

@@ -17,6 +17,8 @@
 // afterwards each h, u, cv, cp evaluation is a 5-term Horner polynomial.
 #pragma once
 
+#include <cstring>
+
 #include <cstdint>
 
 #include "mechanism.h"
@@ -47,6 +49,7 @@ struct ThermoTable {
 
 // Builds the table on the host from a parsed mechanism.
 inline void build_thermo_table(const edyn_mech& m, ThermoTable& t) {
+  std::memset(&t, 0, sizeof(t));  // tables of one mechanism compare equal byte for byte
   t.ns = m.nspec;
   t.nbreak = 0;
   for (int k = 0; k < m.nspec; ++k) {

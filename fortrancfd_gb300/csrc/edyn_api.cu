@@ -10,7 +10,9 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdint>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <string>
 #include <vector>
@@ -587,3 +589,100 @@ int edyn_finalize(void* ctx) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Fluid step on caller-owned arrays, allocating nothing.
+//
+// For hosts that own every device array and cannot let the library allocate
+// device memory while they run (the state sits in arrays that the host's own
+// runtime sized at start-up: a cudaMalloc at step time can fail against that
+// runtime's reservation, and a cudaFree synchronises the whole device).
+// The step needs scratch beyond its inputs and outputs: the second primitive
+// buffer of the stage double buffer and the stage-0 conserved copy of TVDRK3.
+// Both live in one statically sized device array, which every GPU that loads
+// this library holds until the process exits.
+//
+// Nothing in the array has to start at zero: a call writes every element it
+// reads before reading it (the owned-cell columns of each stage's primitive
+// output and of the stage-0 copy; ghost columns are never read, ghost states
+// are rebuilt from the boundary rule). All calls share the array and it keeps
+// the last call's contents, so calls whose work overlaps on the GPU race on it.
+// ---------------------------------------------------------------------------
+static __device__ __align__(256) double g_fluid_scratch[EDYN_NOALLOC_SCRATCH_DOUBLES];
+
+namespace {
+
+constexpr int kMaxDevices = 64;
+
+// Device address of g_fluid_scratch on the current device. In host code the
+// symbol's name stands for the device array and is not a device address; the
+// address is looked up once per device, on the first call made with that
+// device current, and cached.
+int fluid_scratch(Ctx* c, double** out) {
+  int dev = -1;
+  CK(cudaGetDevice(&dev));
+  int sdev = -1;
+  CK(cudaStreamGetDevice(c->stream, &sdev));
+  if (sdev != dev)
+    return fail(c, EDYN_E_ARG, "edyn_solve_fluid_noalloc: the context's device %d is not the current device %d", sdev,
+                dev);
+  if (dev < 0 || dev >= kMaxDevices) return fail(c, EDYN_E_ARG, "device ordinal %d out of range", dev);
+  static std::mutex mu;
+  static double* addr[kMaxDevices] = {};
+  std::lock_guard<std::mutex> lock(mu);
+  if (!addr[dev]) {
+    void* p = nullptr;
+    CK(cudaGetSymbolAddress(&p, g_fluid_scratch));
+    addr[dev] = static_cast<double*>(p);
+  }
+  *out = addr[dev];
+  return EDYN_OK;
+}
+
+}  // namespace
+
+extern "C" int edyn_solve_fluid_noalloc(void* ctx, double* qf_d, double* qc_d, double dt) {
+  Ctx* c = (Ctx*)ctx;
+  if (!c || !c->qc) return EDYN_E_ARG;
+  if (!qf_d || !qc_d || qf_d == qc_d)
+    return fail(c, EDYN_E_ARG, "edyn_solve_fluid_noalloc: two distinct device arrays (qf, Qc) are required");
+  if ((reinterpret_cast<uintptr_t>(qf_d) | reinterpret_cast<uintptr_t>(qc_d)) % alignof(double))
+    return fail(c, EDYN_E_ARG, "edyn_solve_fluid_noalloc: qf and Qc must be 8-byte aligned");
+  const size_t rows = (size_t)c->ne * c->ld;
+  if (2 * rows > (size_t)EDYN_NOALLOC_SCRATCH_DOUBLES)
+    return fail(c, EDYN_E_ARG,
+                "edyn_solve_fluid_noalloc: the tube needs 2*nequ*(ncell+8) = %zu doubles of scratch, the static "
+                "scratch holds %d (ncell <= %d at nequ = %d)",
+                2 * rows, EDYN_NOALLOC_SCRATCH_DOUBLES, EDYN_NOALLOC_SCRATCH_DOUBLES / (2 * c->ne) - 2 * GHOST, c->ne);
+  double* scr = nullptr;
+  int rc = fluid_scratch(c, &scr);
+  if (rc) return rc;
+
+  StageArgs a = base_args(c);
+  a.qc = qc_d;
+  a.q0 = scr + rows;
+  a.dt = dt;
+  double* buf[2] = {qf_d, scr};
+  int cur = 0;
+  const int nst = c->select_time == 0 ? 1 : 3;
+  static const double h1[3] = {0.0, 3.0 / 4.0, 1.0 / 3.0};
+  static const double h2[3] = {0.0, 1.0 / 4.0, 2.0 / 3.0};
+  for (int s = 0; s < nst; ++s) {
+    a.qf_in = buf[cur];
+    a.qf_out = buf[cur ^ 1];
+    a.kind = s == 0 ? 0 : 1;
+    a.save_q0 = (s == 0 && nst == 3) ? 1 : 0;
+    a.h1 = h1[s];
+    a.h2 = h2[s];
+    cudaError_t e = launch_stage(a, c->acu, c->lim, c->wflag, c->riemann, c->stage_threads, c->stream);
+    if (e != cudaSuccess) return fail(c, EDYN_E_CUDA, "stage launch: %s", cudaGetErrorString(e));
+    cur ^= 1;
+  }
+  // An odd number of stages leaves the new primitive state in the scratch:
+  // copy its owned columns back into the caller's qf.
+  const size_t pitch = (size_t)c->ld * sizeof(double);
+  CK(cudaMemcpy2DAsync(qf_d + GHOST, pitch, scr + GHOST, pitch, (size_t)c->n * sizeof(double), (size_t)c->ne,
+                       cudaMemcpyDeviceToDevice, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return EDYN_OK;
+}

@@ -59,6 +59,7 @@ def lib() -> ctypes.CDLL:
     L.edyn_init_cells.argtypes = [vp, dp, dp, dp, dp]
     L.edyn_calc_dt.argtypes = [vp, d, dp]
     L.edyn_solve_fluid.argtypes = [vp, d]
+    L.edyn_solve_fluid_noalloc.argtypes = [vp, vp, vp, d]
     L.edyn_solve_source.argtypes = [vp, d, d]
     L.edyn_post_step.argtypes = [vp]
     L.edyn_step.argtypes = [vp, d, dp]
@@ -181,6 +182,12 @@ class Tube(_Ctx):
 
     def solve_fluid(self, dt: float):
         self._check(lib().edyn_solve_fluid(self._h, dt))
+
+    def solve_fluid_noalloc(self, qf_ptr: int, qc_ptr: int, dt: float):
+        """One fluid step on caller-owned device arrays (nequ rows of
+        ncell + 8 doubles, cell i at column i + 4), allocating nothing; the
+        scratch is a static device array of the library."""
+        self._check(lib().edyn_solve_fluid_noalloc(self._h, ctypes.c_void_p(qf_ptr), ctypes.c_void_p(qc_ptr), dt))
 
     def solve_source(self, dt: float, time: float = 0.0):
         self._check(lib().edyn_solve_source(self._h, dt, time))

@@ -76,6 +76,44 @@ int edyn_calc_dt(void* ctx, double cfl, double* dt);
 /* solve_fluid (SRC/update.f90:62): one explicit Euler or TVDRK3 step. */
 int edyn_solve_fluid(void* ctx, double dt);
 
+/* Size of the static scratch of edyn_solve_fluid_noalloc, in doubles
+ * (8 MiB): a tube fits when 2 * nequ * (ncell + 8) <= this value, i.e.
+ * ncell <= 9354 with the 53 species of GRI-Mech 3.0 (nequ = 56). */
+#define EDYN_NOALLOC_SCRATCH_DOUBLES 1048576
+
+/* One explicit Euler or TVDRK3 fluid step, like edyn_solve_fluid, on arrays
+ * that the caller owns, allocating nothing. This entry point has no
+ * counterpart in the reference.
+ *
+ * It is for callers that cannot allocate device memory while they run: a
+ * host whose tube state lives in device arrays sized once by its own
+ * runtime (OpenACC or CUDA Fortran data regions, a pool allocator that
+ * reserves the device up front), where a cudaMalloc at step time can fail
+ * against that reservation and a cudaFree synchronises the whole device.
+ * The call makes no cudaMalloc, cudaFree or other allocating call; the
+ * scratch it needs (the second primitive buffer and the TVDRK3 stage-0
+ * copy) is a static device array of EDYN_NOALLOC_SCRATCH_DOUBLES doubles,
+ * which every GPU that loads this library holds until the process exits.
+ *
+ * ctx comes from edyn_init (which allocates, once, at set-up); the call uses
+ * its scheme, boundary data, mechanism tables and stream, and neither reads
+ * nor writes the context's own state buffers. qf_d and qc_d are device
+ * arrays in the library's device layout: nequ rows of ld = ncell + 8
+ * doubles, row v holding variable v, cell i at column i + 4 (the columns
+ * outside the cells are neither read nor written). On entry qf_d holds
+ * QcToqf(qc_d); on return qc_d holds the state after the step and qf_d its
+ * primitive variables. Returns after the step has finished on the stream.
+ *
+ * Tubes with 2 * nequ * (ncell + 8) > EDYN_NOALLOC_SCRATCH_DOUBLES are
+ * rejected with EDYN_E_ARG and a message naming the limit. The first call
+ * on a device looks up the scratch array's device address with that device
+ * current (it must be the context's device); make that first call before
+ * any stream capture. All calls share the scratch array, which keeps the
+ * last call's contents; nothing in it needs to start at zero, since each call
+ * writes every scratch element before reading it. Calls that overlap on the
+ * GPU (from two threads, or on two streams) race on it. */
+int edyn_solve_fluid_noalloc(void* ctx, double* qf_d, double* qc_d, double dt);
+
 /* solve_source (SRC/update.f90:100): per-cell chemistry over dt, heat
  * release rates, qfToQc (SRC/source.f90:17-84). No-op when frozen. */
 int edyn_solve_source(void* ctx, double dt, double time);

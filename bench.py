@@ -258,6 +258,7 @@ def gpu_arm(args, rank, world, local):
         b.record(stream)
         b.synchronize()
         chem_ms.append(a.elapsed_time(b))
+    chem_stats = tube.chem_stats()
     chem_s = statistics.median(chem_ms) / 1e3
     fluid_s = statistics.median(fluid_ms) / 1e3
     # end to end through the C ABI with pinned host buffers
@@ -298,7 +299,10 @@ def gpu_arm(args, rank, world, local):
             "roofline": {"bound": "hbm", "kernel": "k_tube_chem", "achieved": achieved, "peak": hbm,
                          "peak_source": src, "unit": "GB/s", "frac": achieved / hbm,
                          "traffic": TRAFFIC_CHEM_PER_CELL * case.ncell, "launch_ms": chem_s * 1e3, "fluid_step_ms": fluid_s * 1e3},
-            "cpu_baseline": cpu}
+            "cpu_baseline": cpu,
+            "chem_launch": {"rhs_per_cell": chem_stats["rhs"] / max(1, chem_stats["cells"]),
+                            "rejects": chem_stats["rejects"], "team_cells": chem_stats["team_cells"],
+                            "failed": chem_stats["failed"]}}
     print(json.dumps(line), flush=True)
 
 

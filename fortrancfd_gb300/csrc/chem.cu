@@ -144,7 +144,9 @@ __device__ __forceinline__ Tabs bind_tabs(const char* base) {
 // reaction flag bits (w0 >> 24)
 constexpr unsigned F_REV = 1, F_CM = 2, F_FALL = 4, F_KFAL = 8, F_EXP = 16, F_TB = 32;
 
-// Per-warp shared workspace.
+// Per-team shared workspace. A team is the group of threads that works on
+// one cell: one warp, or four warps of a CTA (one per SM sub-partition, each
+// with its own FP64 unit) for the cells that cost the most.
 struct alignas(16) WarpWork {
   double y0[NV], Y[NV], sv[NV], fy[NV], F[5][NV], dl[NV];
   double C[NV], m[NV], uR[NV], cvm[NV], wdot[NV];
@@ -160,6 +162,10 @@ struct alignas(16) WarpWork {
   float yf[NV];       // FP32 copy of the state for the Jacobian
 };
 
+constexpr int TEAM = 128;        // threads of a four-warp team
+constexpr int TEAM_PIECES = 128; // gather pieces per warp row of a team's partial sums
+constexpr int HOT_MIN_RHS = 64;  // right-hand sides in the last call that make a cell hot
+
 __device__ __forceinline__ double clip0_d(double x) { return __double_as_longlong(x) < 0 ? 0.0 : x; }
 
 template <class R>
@@ -174,6 +180,61 @@ __device__ __forceinline__ R warp_max(R v) {
   for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
   return v;
 }
+
+// Team primitives. TW = 32: one warp, warp-synchronous. TW = 128: four warps
+// of one CTA synchronised by a named barrier; cross-warp reductions go
+// through `red` in a fixed order, so results do not depend on timing.
+template <int TW>
+struct Team {
+  int tid;        // thread index within the team
+  int bar;        // named barrier id (four-warp teams)
+  double* red;    // cross-warp scratch, 256 doubles (four-warp teams)
+  double* part4;  // gather partial sums, [4][TEAM_PIECES] (four-warp teams)
+  __device__ __forceinline__ void sync() const {
+    if constexpr (TW == 32) {
+      __syncwarp();
+    } else {
+      asm volatile("bar.sync %0, %1;" ::"r"(bar), "n"(TW) : "memory");
+    }
+  }
+  template <class R>
+  __device__ __forceinline__ R sum(R v) const {
+    v = warp_sum(v);
+    if constexpr (TW == 32) {
+      return v;
+    } else {
+      R* r = reinterpret_cast<R*>(red);
+      if ((tid & 31) == 0) r[tid >> 5] = v;
+      sync();
+      R s = r[0];
+#pragma unroll
+      for (int q = 1; q < TW / 32; ++q) s += r[q];
+      sync();
+      return s;
+    }
+  }
+  template <class R, int N>
+  __device__ __forceinline__ void sumv(R (&v)[N]) const {
+#pragma unroll
+    for (int j = 0; j < N; ++j) v[j] = warp_sum(v[j]);
+    if constexpr (TW > 32) {
+      R* r = reinterpret_cast<R*>(red);
+      if ((tid & 31) == 0) {
+#pragma unroll
+        for (int j = 0; j < N; ++j) r[j * 4 + (tid >> 5)] = v[j];
+      }
+      sync();
+#pragma unroll
+      for (int j = 0; j < N; ++j) {
+        R s = r[j * 4];
+#pragma unroll
+        for (int q = 1; q < TW / 32; ++q) s += r[j * 4 + q];
+        v[j] = s;
+      }
+      sync();
+    }
+  }
+};
 
 template <class R>
 struct Math;
@@ -325,13 +386,13 @@ __device__ __forceinline__ RxnEval<R> eval_rxn(const Tabs& t, int i, R logT, R i
 
 // Thermodynamic pass over species (lanes over k): concentrations, scaled
 // exp(S/R - H/RT) and its reciprocal, u_k/R and cv_k/(R W_k).
-template <class R>
-__device__ __forceinline__ R species_pass(const Tabs& t, const R* y, R rho, R T, R logT, R invT, R* C, R* m, R* mi,
-                                          int* en, R* uR, R* cvm, int lane) {
+template <class R, int TW>
+__device__ __forceinline__ R species_pass(const Tabs& t, const Team<TW>& tm, const R* y, R rho, R T, R logT, R invT,
+                                          R* C, R* m, R* mi, int* en, R* uR, R* cvm) {
   using M = Math<R>;
   const RTabs<R>& x = t.r<R>();
   R csum = 0;
-  for (int k = lane; k < t.ns; k += 32) {
+  for (int k = tm.tid; k < t.ns; k += TW) {
     const R c = rho * y[k] * x.invW[k];
     C[k] = c;
     csum += c;
@@ -361,23 +422,23 @@ __device__ __forceinline__ R species_pass(const Tabs& t, const R* y, R rho, R T,
     cp = fma(cp, T, cc[0 * NSMAX + k]);
     cvm[k] = (cp - 1) * x.invW[k];
   }
-  return warp_sum(csum);
+  return tm.sum(csum);
 }
 
 // Full right-hand side in precision R. y (shared, R) -> f (shared, R).
-template <class R>
-__device__ void rhs(const Tabs& t, WarpWork& w, const R* y, R rho, R* f, R* C, R* m, R* mi, R* uR, R* cvm, R* rop,
-                    R* part, int lane) {
+template <class R, int TW>
+__device__ void rhs(const Tabs& t, const Team<TW>& tm, WarpWork& w, const R* y, R rho, R* f, R* C, R* m, R* mi,
+                    R* uR, R* cvm, R* rop, R* part) {
   const RTabs<R>& x = t.r<R>();
   const int ns = t.ns;
   const R T = y[ns];
   const R logT = Math<R>::lg(T);
   const R invT = (R)1 / T;
-  const R ctot = species_pass<R>(t, y, rho, T, logT, invT, C, m, mi, w.en, uR, cvm, lane);
+  const R ctot = species_pass<R, TW>(t, tm, y, rho, T, logT, invT, C, m, mi, w.en, uR, cvm);
   const R pfac = (R)(PATM_CGS / RU_CGS) * invT;
   const R ipfac = T * (R)(RU_CGS / PATM_CGS);
-  __syncwarp();
-  for (int i = lane; i < t.nrp; i += 32) {
+  tm.sync();
+  for (int i = tm.tid; i < t.nrp; i += TW) {
     R r = 0;
     if (i < t.nr) {
       RxnEval<R> e = eval_rxn<R>(t, i, logT, invT, T, pfac, ipfac, ctot, C, m, mi, w.en);
@@ -385,39 +446,65 @@ __device__ void rhs(const Tabs& t, WarpWork& w, const R* y, R rho, R* f, R* C, R
     }
     rop[i] = r;
   }
-  __syncwarp();
-  // production rates: load-balanced pieces of the species-major list
-  for (int p = t.lane[lane]; p < t.lane[lane + 1]; ++p) {
-    const int e0 = t.pc[p * 3 + 1], e1 = t.pc[p * 3 + 2];
-    R s = 0;
-    for (int q = e0; q < e1; ++q) s = fma(x.nu[q], rop[t.ent[q]], s);
-    part[p] = s;
-  }
-  __syncwarp();
+  tm.sync();
+  // production rates: load-balanced pieces of the species-major list; a
+  // four-warp team splits each piece's entries over its warps
   R su = 0, cv = 0;
-  for (int k = lane; k < ns; k += 32) {
-    R s = 0;
-    for (int q = t.spc[k]; q < t.spc[k + 1]; ++q) s += part[t.spp[q]];
-    f[k] = s * x.W[k] / rho;
-    su = fma(uR[k], s, su);
-    cv = fma(y[k], cvm[k], cv);
+  if constexpr (TW == 32) {
+    for (int p = t.lane[tm.tid]; p < t.lane[tm.tid + 1]; ++p) {
+      const int e0 = t.pc[p * 3 + 1], e1 = t.pc[p * 3 + 2];
+      R s = 0;
+      for (int q = e0; q < e1; ++q) s = fma(x.nu[q], rop[t.ent[q]], s);
+      part[p] = s;
+    }
+    tm.sync();
+    for (int k = tm.tid; k < ns; k += TW) {
+      R s = 0;
+      for (int q = t.spc[k]; q < t.spc[k + 1]; ++q) s += part[t.spp[q]];
+      f[k] = s * x.W[k] / rho;
+      su = fma(uR[k], s, su);
+      cv = fma(y[k], cvm[k], cv);
+    }
+  } else {
+    R* p4 = reinterpret_cast<R*>(tm.part4);
+    const int l = tm.tid & 31, wq = tm.tid >> 5;
+    for (int p = t.lane[l]; p < t.lane[l + 1]; ++p) {
+      const int e0 = t.pc[p * 3 + 1], e1 = t.pc[p * 3 + 2];
+      R s = 0;
+      for (int q = e0 + wq; q < e1; q += 4) s = fma(x.nu[q], rop[t.ent[q]], s);
+      p4[wq * TEAM_PIECES + p] = s;
+    }
+    tm.sync();
+    for (int k = tm.tid; k < ns; k += TW) {
+      R s = 0;
+      for (int q = t.spc[k]; q < t.spc[k + 1]; ++q) {
+        const int pp = t.spp[q];
+        s += ((p4[pp] + p4[TEAM_PIECES + pp]) + p4[2 * TEAM_PIECES + pp]) + p4[3 * TEAM_PIECES + pp];
+      }
+      f[k] = s * x.W[k] / rho;
+      su = fma(uR[k], s, su);
+      cv = fma(y[k], cvm[k], cv);
+    }
   }
-  su = warp_sum(su);
-  cv = warp_sum(cv);
-  if (lane == 0) f[ns] = -su / (rho * cv);  // RU cancels in u/cv
-  __syncwarp();
+  R sc[2] = {su, cv};
+  tm.sumv(sc);
+  if (tm.tid == 0) f[ns] = -sc[0] / (rho * sc[1]);  // RU cancels in u/cv
+  tm.sync();
 }
 
-__device__ __forceinline__ void rhs64(const Tabs& t, WarpWork& w, const double* y, double rho_cgs, double* f,
-                                      int lane) {
-  rhs<double>(t, w, y, rho_cgs, f, w.C, w.m, w.wdot, w.uR, w.cvm, w.rop, w.part, lane);
+template <int TW>
+__device__ __forceinline__ void rhs64(const Tabs& t, const Team<TW>& tm, WarpWork& w, const double* y,
+                                      double rho_cgs, double* f) {
+  rhs<double, TW>(t, tm, w, y, rho_cgs, f, w.C, w.m, w.wdot, w.uR, w.cvm, w.rop, w.part);
 }
 
 // Analytic FP32 Jacobian of the mass-action species block plus finite
 // differences in T. J (row-major, stride JS) receives d f / d y at y.
-__device__ void jacobian32(const Tabs& t, WarpWork& w, const double* y, double rho_cgs, int lane) {
+template <int TW>
+__device__ void jacobian32(const Tabs& t, const Team<TW>& tm, WarpWork& w, const double* y, double rho_cgs) {
   const RTabs<float>& x = t.f;
   const int ns = t.ns, n = ns + 1;
+  const int tid = tm.tid;
   float* J = w.J;
   float* Cf = (float*)w.C;
   float* mf = (float*)w.m;
@@ -427,30 +514,30 @@ __device__ void jacobian32(const Tabs& t, WarpWork& w, const double* y, double r
   float* ropf = (float*)w.rop;
   float* partf = (float*)w.part;
   float* rowc = (float*)w.sv;  // per-species collider coefficients
-  for (int q = lane; q < n * JS; q += 32) J[q] = 0.f;
+  for (int q = tid; q < n * JS; q += TW) J[q] = 0.f;
   const float T = (float)y[ns];
   const float dT = fmaxf(1e-3f * T, 0.05f);
   const float rho = (float)rho_cgs;
   // perturbed-T state first, base state second: the species-pass arrays
   // then hold the base state for the analytic part
-  for (int k = lane; k < n; k += 32) w.yf[k] = (float)y[k];
-  __syncwarp();
-  if (lane == 0) w.yf[ns] = T + dT;
-  __syncwarp();
-  rhs<float>(t, w, w.yf, rho, w.f2, Cf, mf, mif, uRf, cvmf, ropf, partf, lane);
-  if (lane == 0) w.yf[ns] = T;
-  __syncwarp();
-  rhs<float>(t, w, w.yf, rho, w.f1, Cf, mf, mif, uRf, cvmf, ropf, partf, lane);
-  for (int k = lane; k < n; k += 32) rowc[k] = 0.f;
+  for (int k = tid; k < n; k += TW) w.yf[k] = (float)y[k];
+  tm.sync();
+  if (tid == 0) w.yf[ns] = T + dT;
+  tm.sync();
+  rhs<float, TW>(t, tm, w, w.yf, rho, w.f2, Cf, mf, mif, uRf, cvmf, ropf, partf);
+  if (tid == 0) w.yf[ns] = T;
+  tm.sync();
+  rhs<float, TW>(t, tm, w, w.yf, rho, w.f1, Cf, mf, mif, uRf, cvmf, ropf, partf);
+  for (int k = tid; k < n; k += TW) rowc[k] = 0.f;
   const float logT = __logf(T), invT = 1.f / T;
   float ctot = 0.f;
-  for (int k = lane; k < ns; k += 32) ctot += Cf[k];
-  ctot = warp_sum(ctot);
+  for (int k = tid; k < ns; k += TW) ctot += Cf[k];
+  ctot = tm.sum(ctot);
   const float pfac = (float)(PATM_CGS / RU_CGS) * invT;
   const float ipfac = T * (float)(RU_CGS / PATM_CGS);
-  __syncwarp();
+  tm.sync();
   // d w_k / d C_j accumulated into J[k][j] (concentration space)
-  for (int i = lane; i < t.nr; i += 32) {
+  for (int i = tid; i < t.nr; i += TW) {
     RxnEval<float> e = eval_rxn<float>(t, i, logT, invT, T, pfac, ipfac, ctot, Cf, mf, mif, w.en);
     const unsigned w0 = t.w0[i], w1 = t.w1[i], w2 = t.w2[i], w3 = t.w3[i], w4 = t.w4[i], w5 = t.w5[i];
     const int nk = (w5 >> 8) & 15;
@@ -511,32 +598,53 @@ __device__ void jacobian32(const Tabs& t, WarpWork& w, const double* y, double r
   // to mass-fraction space: d f_k / d y_j = (W_k / W_j) (d w_k / d C_j + rowc_k);
   // T row d f_T / d y_j = -(sum_k e_k J_kj + f_T cvm_j) / cv with e_k = u_k/W_k.
   float cv = 0.f;
-  for (int k = lane; k < ns; k += 32) cv = fmaf(w.yf[k], cvmf[k], cv);
-  cv = warp_sum(cv);
+  for (int k = tid; k < ns; k += TW) cv = fmaf(w.yf[k], cvmf[k], cv);
+  cv = tm.sum(cv);
   const float fT = w.f1[ns];
-  for (int j = lane; j < ns; j += 32) {
-    const float wj = x.invW[j];
-    float acc = 0.f;
-    for (int k = 0; k < ns; ++k) {
-      const float v = (J[k * JS + j] + rowc[k]) * x.W[k] * wj;
-      J[k * JS + j] = v;
-      acc = fmaf(uRf[k] * x.invW[k], v, acc);
+  if constexpr (TW == 32) {
+    for (int j = tid; j < ns; j += TW) {
+      const float wj = x.invW[j];
+      float acc = 0.f;
+      for (int k = 0; k < ns; ++k) {
+        const float v = (J[k * JS + j] + rowc[k]) * x.W[k] * wj;
+        J[k * JS + j] = v;
+        acc = fmaf(uRf[k] * x.invW[k], v, acc);
+      }
+      J[ns * JS + j] = -(acc + fT * cvmf[j]) / cv;
     }
-    J[ns * JS + j] = -(acc + fT * cvmf[j]) / cv;
+  } else {
+    // columns over threads, the rows of each column in two halves; the
+    // halves' T-row partial sums meet in the team scratch
+    float* accp = reinterpret_cast<float*>(tm.red + 64);  // [2][64]
+    const int kh = (ns + 1) / 2;
+    for (int it = tid; it < 2 * ns; it += TW) {
+      const int j = it % ns, hf = it / ns;
+      const float wj = x.invW[j];
+      float acc = 0.f;
+      const int k1 = hf == 0 ? kh : ns;
+      for (int k = hf * kh; k < k1; ++k) {
+        const float v = (J[k * JS + j] + rowc[k]) * x.W[k] * wj;
+        J[k * JS + j] = v;
+        acc = fmaf(uRf[k] * x.invW[k], v, acc);
+      }
+      accp[hf * 64 + j] = acc;
+    }
+    tm.sync();
+    for (int j = tid; j < ns; j += TW) J[ns * JS + j] = -((accp[j] + accp[64 + j]) + fT * cvmf[j]) / cv;
   }
   const float idT = 1.f / ((T + dT) - T);
-  for (int k = lane; k < n; k += 32) J[k * JS + ns] = (w.f2[k] - w.f1[k]) * idT;
-  __syncwarp();
+  for (int k = tid; k < n; k += TW) J[k * JS + ns] = (w.f2[k] - w.f1[k]) * idT;
+  tm.sync();
   // an entry that overflowed single precision carries no usable slope
-  for (int q = lane; q < n * JS; q += 32)
+  for (int q = tid; q < n * JS; q += TW)
     if (!isfinite(J[q])) J[q] = 0.f;
-  __syncwarp();
+  tm.sync();
 }
 
 // In-place Gauss-Jordan inversion with partial pivoting (FP32, one warp).
 // Each Newton solve is then a matrix-vector product without the serial
 // dependence chain of triangular substitution.
-__device__ bool gj_invert(float* A, int* perm, float* col, int n, int lane) {
+__device__ bool gj_invert_warp(float* A, int* perm, float* col, int n, int lane) {
   bool ok = true;
   for (int k = 0; k < n; ++k) {
     float bv = -1.f;
@@ -567,10 +675,7 @@ __device__ bool gj_invert(float* A, int* perm, float* col, int n, int lane) {
     __syncwarp();
     for (int j = lane; j < n; j += 32) {
       const float rk = A[k * JS + j];
-      if (j == k) {
-        for (int i = 0; i < n; ++i)
-          if (i != k) A[i * JS + k] = -col[i] * inv;
-      } else {
+      if (j != k) {
         int i = 0;
         for (; i + 6 <= n; i += 6) {
           float a0 = A[(i + 0) * JS + j], a1 = A[(i + 1) * JS + j], a2 = A[(i + 2) * JS + j];
@@ -591,6 +696,9 @@ __device__ bool gj_invert(float* A, int* perm, float* col, int n, int lane) {
         for (; i < n; ++i) A[i * JS + j] = fmaf(-col[i], rk, A[i * JS + j]);
       }
     }
+    // the pivot column, in parallel over rows (row k already holds inv)
+    for (int i = lane; i < n; i += 32)
+      if (i != k) A[i * JS + k] = -col[i] * inv;
     __syncwarp();
   }
   // row interchanges of the elimination become column interchanges of the inverse
@@ -607,8 +715,136 @@ __device__ bool gj_invert(float* A, int* perm, float* col, int n, int lane) {
   return ok;
 }
 
+// The same inversion by a four-warp team, with the matrix in registers: thread
+// t holds rows rg + 8a (a < 7) and columns cg + 16b (b < 4), rg = t % 8,
+// cg = t / 8, of an up-to-56 x 64 tile. Pivoting is implicit: the pivot of
+// column k is the largest remaining entry among the rows not yet used, and no
+// rows move; the pivot column and row travel through double-buffered shared
+// memory, so a step costs two barriers. With pivot rows p_k the result B
+// satisfies inv(A)[k][p_j] = B[p_k][j], which the write-back applies.
+__device__ bool gj_invert_team(const Team<TEAM>& tm, float* A, int* perm, float* col, int n) {
+  (void)col;
+  const int tid = tm.tid;
+  const int rg = tid & 7, cg = tid >> 3;
+  float* colb = reinterpret_cast<float*>(tm.red);          // [2][64]
+  float* rowb = colb + 128;                                // [2][64]
+  float* cval = rowb + 128;                                // [2][8]
+  int* crow = reinterpret_cast<int*>(cval + 16);           // [2][8]
+  int* pinv = crow + 16;                                   // [64]
+  float B[7][4];
+#pragma unroll
+  for (int a = 0; a < 7; ++a)
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+      const int i = rg + 8 * a, j = cg + 16 * b;
+      B[a][b] = (i < n && j < n) ? A[i * JS + j] : 0.f;
+    }
+  unsigned long long used = 0ull;
+  bool ok = true;
+  for (int k = 0; k < n; ++k) {
+    const int buf = k & 1;
+    const int kb = k >> 4;
+    if (cg == (k & 15)) {
+      // owners of column k: publish it, and their best remaining row
+      float bv = -1.f;
+      int bi = n;
+#pragma unroll
+      for (int a = 0; a < 7; ++a) {
+        const int i = rg + 8 * a;
+        float v = 0.f;
+#pragma unroll
+        for (int b = 0; b < 4; ++b)
+          if (b == kb) v = B[a][b];
+        if (i < n) {
+          colb[buf * 64 + i] = v;
+          const float av = fabsf(v);
+          if (!((used >> i) & 1ull) && av > bv) { bv = av; bi = i; }
+        }
+      }
+      cval[buf * 8 + rg] = bv;
+      crow[buf * 8 + rg] = bi;
+    }
+    tm.sync();
+    // the pivot: largest candidate, lowest row on ties (loads first, then selects)
+    float cv8[8];
+    int cr8[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      cv8[q] = cval[buf * 8 + q];
+      cr8[q] = crow[buf * 8 + q];
+    }
+    float bv = cv8[0];
+    int p = cr8[0];
+#pragma unroll
+    for (int q = 1; q < 8; ++q) {
+      const bool take = cv8[q] > bv || (cv8[q] == bv && cr8[q] < p);
+      bv = take ? cv8[q] : bv;
+      p = take ? cr8[q] : p;
+    }
+    if (!(bv > 0.f) || p >= n) { ok = false; p = (p >= n) ? k : p; }
+    const int ap = p >> 3;
+    if (rg == (p & 7)) {
+      // owners of row p: publish it
+#pragma unroll
+      for (int b = 0; b < 4; ++b) {
+        float v = B[0][b];
+#pragma unroll
+        for (int a = 1; a < 7; ++a) v = (a == ap) ? B[a][b] : v;
+        rowb[buf * 64 + cg + 16 * b] = v;
+      }
+    }
+    if (tid == 0) perm[k] = p;
+    tm.sync();
+    // update: all shared loads first, then branch-free selects
+    float ci[7], rk[4];
+#pragma unroll
+    for (int a = 0; a < 7; ++a) ci[a] = colb[buf * 64 + min(rg + 8 * a, 63)];
+#pragma unroll
+    for (int b = 0; b < 4; ++b) rk[b] = rowb[buf * 64 + cg + 16 * b];
+    const float inv = 1.f / colb[buf * 64 + p];
+#pragma unroll
+    for (int b = 0; b < 4; ++b) rk[b] *= inv;
+#pragma unroll
+    for (int a = 0; a < 7; ++a) {
+      const bool rp = (rg + 8 * a) == p;
+#pragma unroll
+      for (int b = 0; b < 4; ++b) {
+        const bool ck = (cg + 16 * b) == k;
+        const float other = ck ? -ci[a] * inv : fmaf(-ci[a], rk[b], B[a][b]);
+        const float prow = ck ? inv : B[a][b] * inv;
+        B[a][b] = rp ? prow : other;
+      }
+    }
+    used |= 1ull << p;
+  }
+  // write back the inverse: inv(A)[k][p_j] = B[p_k][j]
+  if (tid < 64) pinv[tid] = 0;
+  tm.sync();
+  for (int k = tid; k < n; k += TEAM) pinv[perm[k]] = k;
+  tm.sync();
+#pragma unroll
+  for (int a = 0; a < 7; ++a) {
+    const int r = rg + 8 * a;
+    if (r >= n) continue;
+    const int kk = pinv[r];
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+      const int j = cg + 16 * b;
+      if (j < n) A[kk * JS + perm[j]] = B[a][b];
+    }
+  }
+  tm.sync();
+  return ok;
+}
+
+template <int TW>
+__device__ __forceinline__ bool gj_invert(const Team<TW>& tm, float* A, int* perm, float* col, int n) {
+  if constexpr (TW == 32) return gj_invert_warp(A, perm, col, n, tm.tid);
+  else return gj_invert_team(tm, A, perm, col, n);
+}
+
 // b <- A b for the n x n inverse in A (lanes over rows).
-__device__ __forceinline__ void gemv_solve(const float* A, float* b, int n, int lane) {
+__device__ __forceinline__ void gemv_solve_warp(const float* A, float* b, int n, int lane) {
   float r0 = 0.f, r1 = 0.f;
   const int i0 = lane, i1 = lane + 32;
   float a0 = 0.f, a1 = 0.f, c0 = 0.f, c1 = 0.f;
@@ -636,6 +872,23 @@ __device__ __forceinline__ void gemv_solve(const float* A, float* b, int n, int 
   __syncwarp();
 }
 
+// b <- A b by a four-warp team: two threads per row, even and odd columns.
+template <int TW>
+__device__ __forceinline__ void gemv_solve(const Team<TW>& tm, const float* A, float* b, int n) {
+  if constexpr (TW == 32) {
+    gemv_solve_warp(A, b, n, tm.tid);
+  } else {
+    const int i = tm.tid >> 1, h = tm.tid & 1;
+    float a = 0.f;
+    if (i < n)
+      for (int j = h; j < n; j += 2) a = fmaf(A[i * JS + j], b[j], a);
+    a += __shfl_xor_sync(0xffffffffu, a, 1);
+    tm.sync();
+    if (i < n && h == 0) b[i] = a;
+    tm.sync();
+  }
+}
+
 struct Cell {
   double rho_cgs, dt, rtol, atol;
 };
@@ -646,7 +899,9 @@ struct CellStats {
 };
 
 // Integrates w.y0 over [0, dt] with SDIRK4. Returns the statistics.
-__device__ CellStats integrate(const Tabs& t, WarpWork& w, const Cell& c, int lane) {
+template <int TW>
+__device__ CellStats integrate(const Tabs& t, const Team<TW>& tm, WarpWork& w, const Cell& c) {
+  const int lane = tm.tid;
   const int n = t.ns + 1;
   CellStats st = {0, 0, 0, 0, false};
   double tcur = 0.0, h = c.dt;
@@ -658,7 +913,7 @@ __device__ CellStats integrate(const Tabs& t, WarpWork& w, const Cell& c, int la
     if (tcur + h > c.dt) h = c.dt - tcur;
     // f0 = f(y0) in FP64 (kept across rejections)
     if (need_f0) {
-      rhs64(t, w, w.y0, c.rho_cgs, w.dl, lane);
+      rhs64<TW>(t, tm, w, w.y0, c.rho_cgs, w.dl);
       st.rhs++;
       need_f0 = false;
       if (tcur == 0.0) {
@@ -667,21 +922,21 @@ __device__ CellStats integrate(const Tabs& t, WarpWork& w, const Cell& c, int la
         // one explicit step is accurate far below the tolerance and the
         // implicit machinery is skipped.
         float ss = 0.f;
-        for (int i = lane; i < n; i += 32) {
+        for (int i = lane; i < n; i += TW) {
           const float q = (float)(c.dt * w.dl[i] / (c.atol + c.rtol * fabs(w.y0[i])));
           ss = fmaf(q, q, ss);
         }
-        const float nrm = sqrtf(warp_sum(ss) / (float)n);
+        const float nrm = sqrtf(tm.sum(ss) / (float)n);
         if (nrm <= 1e-3f) {
-          for (int i = lane; i < n; i += 32) w.y0[i] = fma(c.dt, w.dl[i], w.y0[i]);
-          __syncwarp();
+          for (int i = lane; i < n; i += TW) w.y0[i] = fma(c.dt, w.dl[i], w.y0[i]);
+          tm.sync();
           st.steps++;
           break;
         }
       }
     }
     if (need_jac) {
-      jacobian32(t, w, w.y0, c.rho_cgs, lane);
+      jacobian32<TW>(t, tm, w, w.y0, c.rho_cgs);
       st.jac++;
     }
     // Newton matrix I - h g J equilibrated with the error weights,
@@ -689,40 +944,40 @@ __device__ CellStats integrate(const Tabs& t, WarpWork& w, const Cell& c, int la
     // row (K per unit mass fraction) wins the pivot search and the species
     // rows lose their accuracy. Inverted in place (J is rebuilt after a
     // rejection).
-    for (int i = lane; i < n; i += 32) w.sc32[i] = (float)(c.atol + c.rtol * fabs(w.y0[i]));
-    __syncwarp();
-    for (int q = lane; q < n * JS; q += 32) {
+    for (int i = lane; i < n; i += TW) w.sc32[i] = (float)(c.atol + c.rtol * fabs(w.y0[i]));
+    tm.sync();
+    for (int q = lane; q < n * JS; q += TW) {
       const int i = q / JS, j = q - i * JS;
       if (j < n) w.J[q] = ((i == j ? 1.f : 0.f) - (float)(h * g) * w.J[q]) * (w.sc32[j] / w.sc32[i]);
     }
-    __syncwarp();
-    bool newton_ok = gj_invert(w.J, w.piv, w.col, n, lane);
+    tm.sync();
+    bool newton_ok = gj_invert<TW>(tm, w.J, w.piv, w.col, n);
     for (int s = 0; s < 5 && newton_ok; ++s) {
-      for (int i = lane; i < n; i += 32) {
+      for (int i = lane; i < n; i += TW) {
         double acc = w.y0[i];
         for (int j = 0; j < s; ++j) acc = fma(h * c_sa[s][j], w.F[j][i], acc);
         w.sv[i] = acc;
         const double fp = (s == 0) ? w.dl[i] : w.F[s - 1][i];
         w.Y[i] = fma(h * g, fp, acc);
       }
-      __syncwarp();
+      tm.sync();
       float nrm_prev = 0.f;
       bool conv = false;
       for (int it = 0; it < 8; ++it) {
         const double Tn = w.Y[n - 1];
         if (!(Tn > 100.0 && Tn < 8000.0)) break;
-        rhs64(t, w, w.Y, c.rho_cgs, w.fy, lane);
+        rhs64<TW>(t, tm, w, w.Y, c.rho_cgs, w.fy);
         st.rhs++;
-        for (int i = lane; i < n; i += 32)
+        for (int i = lane; i < n; i += TW)
           w.b32[i] = (float)(-(w.Y[i] - w.sv[i] - h * g * w.fy[i]) / (double)w.sc32[i]);
-        __syncwarp();
-        gemv_solve(w.J, w.b32, n, lane);
+        tm.sync();
+        gemv_solve<TW>(tm, w.J, w.b32, n);
         float ss = 0.f;
-        for (int i = lane; i < n; i += 32) {
+        for (int i = lane; i < n; i += TW) {
           const float q = w.b32[i];  // scaled correction
           ss = fmaf(q, q, ss);
         }
-        const float nrm = sqrtf(warp_sum(ss) / (float)n);
+        const float nrm = sqrtf(tm.sum(ss) / (float)n);
         if (!(nrm == nrm)) break;
         // convergence: weighted correction below 1e-2 of the local
         // tolerance, directly or predicted from the contraction rate; one
@@ -737,15 +992,15 @@ __device__ CellStats integrate(const Tabs& t, WarpWork& w, const Cell& c, int la
           // stage derivative = the FP64 right-hand side at the converged
           // iterate; the stage value is rebuilt from it, so mass and
           // elements are conserved to rounding
-          for (int i = lane; i < n; i += 32) {
+          for (int i = lane; i < n; i += TW) {
             w.F[s][i] = w.fy[i];
             w.Y[i] = fma(h * g, w.fy[i], w.sv[i]);
           }
-          __syncwarp();
+          tm.sync();
           break;
         }
-        for (int i = lane; i < n; i += 32) w.Y[i] += (double)w.b32[i] * (double)w.sc32[i];
-        __syncwarp();
+        for (int i = lane; i < n; i += TW) w.Y[i] += (double)w.b32[i] * (double)w.sc32[i];
+        tm.sync();
         nrm_prev = nrm;
       }
       if (!conv) { newton_ok = false; break; }
@@ -758,24 +1013,24 @@ __device__ CellStats integrate(const Tabs& t, WarpWork& w, const Cell& c, int la
       continue;
     }
     // embedded error, filtered through the inverted matrix
-    for (int i = lane; i < n; i += 32) {
+    for (int i = lane; i < n; i += TW) {
       double e = 0.0;
       for (int j = 0; j < 5; ++j) e = fma(c_se[j], w.F[j][i], e);
       w.b32[i] = (float)(h * e / (double)w.sc32[i]);
     }
-    __syncwarp();
-    gemv_solve(w.J, w.b32, n, lane);
+    tm.sync();
+    gemv_solve<TW>(tm, w.J, w.b32, n);
     float ss = 0.f;
-    for (int i = lane; i < n; i += 32) {
+    for (int i = lane; i < n; i += TW) {
       const double sc = c.atol + c.rtol * fmax(fabs(w.y0[i]), fabs(w.Y[i]));
       const float q = (float)((double)w.b32[i] * (double)w.sc32[i] / sc);
       ss = fmaf(q, q, ss);
     }
-    const float en = sqrtf(warp_sum(ss) / (float)n);
+    const float en = sqrtf(tm.sum(ss) / (float)n);
     const float fac = 0.9f * powf(fmaxf(en, 1e-10f), -0.25f);
     if (en <= 1.f) {
-      for (int i = lane; i < n; i += 32) w.y0[i] = w.Y[i];
-      __syncwarp();
+      for (int i = lane; i < n; i += TW) w.y0[i] = w.Y[i];
+      tm.sync();
       tcur += h;
       st.steps++;
       need_f0 = true;
@@ -797,15 +1052,18 @@ __device__ __forceinline__ void stage_tables(char* smem_tab, const char* g_tab, 
   __syncthreads();
 }
 
-__device__ __forceinline__ void add_stats(ChemCounters* cnt, const CellStats& s, int lane) {
-  if (lane == 0) {
-    atomicAdd(&cnt->rhs, (unsigned long long)s.rhs);
-    atomicAdd(&cnt->steps, (unsigned long long)s.steps);
-    atomicAdd(&cnt->rejects, (unsigned long long)s.rejects);
-    atomicAdd(&cnt->jac, (unsigned long long)s.jac);
-    atomicAdd(&cnt->cells, 1ull);
-    if (s.failed) atomicAdd(&cnt->failed, 1ull);
-  }
+__device__ __forceinline__ void add_stats(ChemCounters* cnt, const CellStats& s, bool team) {
+  atomicAdd(&cnt->rhs, (unsigned long long)s.rhs);
+  atomicAdd(&cnt->steps, (unsigned long long)s.steps);
+  atomicAdd(&cnt->rejects, (unsigned long long)s.rejects);
+  atomicAdd(&cnt->jac, (unsigned long long)s.jac);
+  atomicAdd(&cnt->cells, 1ull);
+  if (team) atomicAdd(&cnt->team_cells, 1ull);
+  if (s.failed) atomicAdd(&cnt->failed, 1ull);
+}
+
+__device__ __forceinline__ WarpWork* work_slots(char* smem, int tab_bytes) {
+  return (WarpWork*)(smem + ((tab_bytes + 255) / 256) * 256);
 }
 
 // Batch of independent reactors (macks contract).
@@ -815,8 +1073,9 @@ __global__ void __launch_bounds__(MAXW * 32, 1)
   extern __shared__ __align__(16) char smem[];
   stage_tables(smem, g_tab, tab_bytes);
   const Tabs t = bind_tabs(smem);
-  WarpWork& w = ((WarpWork*)(smem + ((tab_bytes + 255) / 256) * 256))[threadIdx.x >> 5];
+  WarpWork& w = work_slots(smem, tab_bytes)[threadIdx.x >> 5];
   const int lane = threadIdx.x & 31;
+  const Team<32> tm{lane, 0, nullptr, nullptr};
   const int nv = t.ns + 1;
   for (int guard = 0; guard < (1 << 30); ++guard) {
     unsigned cell = 0;
@@ -827,189 +1086,283 @@ __global__ void __launch_bounds__(MAXW * 32, 1)
     for (int i = lane; i < nv; i += 32) w.y0[i] = src[i];
     __syncwarp();
     Cell c{rho[cell] * 1e-3, dt[cell], rtol, atol};
-    CellStats s = integrate(t, w, c, lane);
+    CellStats s = integrate<32>(t, tm, w, c);
     double* dst = yiT + (size_t)cell * nv;
     for (int i = lane; i < nv; i += 32) dst[i] = w.y0[i];
-    add_stats(cnt, s, lane);
-    if (s.failed && lane == 0) atomicOr(err, (unsigned)EDYN_E_CHEM);
+    if (lane == 0) {
+      add_stats(cnt, s, false);
+      if (s.failed) atomicOr(err, (unsigned)EDYN_E_CHEM);
+    }
     __syncwarp();
   }
 }
 
-// Tube mode: reaction_macks (SRC/source.f90:17-84) followed by the post-step
-// QcToqf (SRC/main.f90:157-161) for every interior cell.
+// One tube cell: reaction_macks (SRC/source.f90:17-84) followed by the
+// post-step QcToqf (SRC/main.f90:157-161). Returns the right-hand sides the
+// cell took (its cost, which picks the cells that get a team next time).
+template <int TW>
+__device__ int tube_cell(const Tabs& t, const Team<TW>& tm, WarpWork& w, const ChemLaunch& L, unsigned cell,
+                         double dt, double& speed_max, ChemCounters* cnt) {
+  const int tid = tm.tid;
+  const int ns = t.ns;
+  const size_t ld = (size_t)L.ld;
+  double* q = L.qf + cell + GHOST;
+  double* Q = L.qc + cell + GHOST;
+  const double rho = q[0];
+  // reaction_macks: y_sp = adjust_sum(Y), yiT = [y_sp, T] (SRC/source.f90:47-56);
+  // the raw Y stay in the qf rows for the heat release rate.
+  double s = 0.0;
+  for (int k = tid; k < ns; k += TW) {
+    const double yp = clip0_d(q[(3 + k) * ld]);
+    w.y0[k] = yp;
+    s += yp;
+  }
+  s = tm.sum(s);
+  const double inv_s = 1.0 / s;
+  for (int k = tid; k < ns; k += TW) w.y0[k] *= inv_s;
+  if (tid == 0) w.y0[ns] = q[2 * ld];
+  tm.sync();
+  Cell c{rho * 1e-3, dt, L.rtol, L.atol};
+  CellStats st = integrate<TW>(t, tm, w, c);
+  if (tid == 0) {
+    add_stats(cnt, st, TW > 32);
+    if (st.failed) atomicOr(L.err, (unsigned)EDYN_E_CHEM);
+  }
+  // adjust_sum(Y) after the step
+  double s2 = 0.0;
+  for (int k = tid; k < ns; k += TW) {
+    const double y = clip0_d(w.y0[k]);
+    w.y0[k] = y;
+    s2 += y;
+  }
+  s2 = tm.sum(s2);
+  const double inv2 = 1.0 / s2;
+  const double Tn = w.y0[ns];
+  // heat release rate, SRC/thermo.f90:83-103 (qf rows still hold Y0 raw)
+  const double rho_cgs = rho * 1e-3;
+  double hsum[3] = {0.0, 0.0, 0.0};  // hr, hs, sz
+  for (int k = tid; k < ns; k += TW) {
+    const double yn = w.y0[k] * inv2;
+    w.y0[k] = yn;
+    const double y0raw = q[(3 + k) * ld];
+    hsum[0] = fma(rho_cgs * t.d.hf[k], yn - y0raw, hsum[0]);
+    // qfToQc energy: e = R (H(T) - T Sz)/S_Y with the adjusted Y (S_Y = 1)
+    const int r = (Tn > t.d.tmid[k]) ? 1 : 0;
+    const double* ch = t.d.ch + r * 6 * NSMAX;
+    double hh = fma(ch[4 * NSMAX + k], Tn, ch[3 * NSMAX + k]);
+    hh = fma(hh, Tn, ch[2 * NSMAX + k]);
+    hh = fma(hh, Tn, ch[1 * NSMAX + k]);
+    hh = fma(hh, Tn, ch[0 * NSMAX + k]);
+    hh = fma(hh, Tn, ch[5 * NSMAX + k]);
+    const double z = yn * t.d.invW[k];
+    hsum[1] = fma(z, hh, hsum[1]);
+    hsum[2] += z;
+  }
+  tm.sumv(hsum);
+  const double u = q[ld];
+  const double e_int = R_SI * (hsum[1] - Tn * hsum[2]);
+  const double rhoe = rho * (e_int + 0.5 * (u * u));
+  // write Qc = qfToQc(qf) and qf (T, Y); the post-step QcToqf then
+  // recovers T from rho e with the Newton solve.
+  tm.sync();  // every thread has read the raw Y rows
+  for (int k = tid; k < ns; k += TW) {
+    q[(3 + k) * ld] = w.y0[k];
+    Q[(3 + k) * ld] = rho * w.y0[k];
+  }
+  if (tid == 0) {
+    Q[2 * ld] = rhoe;
+    L.hrr[cell] = -(hsum[0] / dt) * 1e-1;
+  }
+  tm.sync();
+  // post-step QcToqf: Newton on rho e for T (from 1000 K when strict)
+  double T = L.strict_newton ? 1000.0 : Tn;
+  const double E = (rhoe / rho - 0.5 * (u * u)) / R_SI;
+  double gN = 1e30, dTN = 1e30;
+  int it = 0;
+  while (fabs(gN) >= fabs(E) * 1e-9 && fabs(dTN) >= T * 1e-6 && it < 10) {
+    // premixed NASA coefficients at the current T (threads over species)
+    double A[7] = {0, 0, 0, 0, 0, 0, 0};
+    for (int k = tid; k < ns; k += TW) {
+      const int r = (T > t.d.tmid[k]) ? 1 : 0;
+      const double* ch = t.d.ch + r * 6 * NSMAX;
+      const double z = w.y0[k] * t.d.invW[k];
+      A[0] = fma(z, ch[0 * NSMAX + k], A[0]);
+      A[1] = fma(z, ch[1 * NSMAX + k], A[1]);
+      A[2] = fma(z, ch[2 * NSMAX + k], A[2]);
+      A[3] = fma(z, ch[3 * NSMAX + k], A[3]);
+      A[4] = fma(z, ch[4 * NSMAX + k], A[4]);
+      A[5] = fma(z, ch[5 * NSMAX + k], A[5]);
+      A[6] += z;
+    }
+    tm.sumv(A);
+    const double Sz = A[6];
+    double p = fma(A[4], T, A[3]);
+    p = fma(p, T, A[2]);
+    p = fma(p, T, A[1]);
+    p = fma(p, T, A[0]);
+    const double H = fma(p, T, A[5]);
+    double cp = fma(5.0 * A[4], T, 4.0 * A[3]);
+    cp = fma(cp, T, 3.0 * A[2]);
+    cp = fma(cp, T, 2.0 * A[1]);
+    cp = fma(cp, T, A[0]);
+    gN = H - T * Sz - E;
+    dTN = -gN / (cp - Sz);
+    T = fmax(20.0, fmin(6000.0, T + dTN));
+    ++it;
+  }
+  if (tid == 0) q[2 * ld] = T;
+  // signal speed of the new state for the next time step
+  if (L.cvel_out) {
+    double a[6] = {0, 0, 0, 0, 0, 0};
+    for (int k = tid; k < ns; k += TW) {
+      const int r = (T > t.d.tmid[k]) ? 1 : 0;
+      const double* ch = t.d.ch + r * 6 * NSMAX;
+      const double z = w.y0[k] * t.d.invW[k];
+      a[0] = fma(z, ch[0 * NSMAX + k], a[0]);
+      a[1] = fma(z, ch[1 * NSMAX + k], a[1]);
+      a[2] = fma(z, ch[2 * NSMAX + k], a[2]);
+      a[3] = fma(z, ch[3 * NSMAX + k], a[3]);
+      a[4] = fma(z, ch[4 * NSMAX + k], a[4]);
+      a[5] += z;
+    }
+    tm.sumv(a);
+    double cp = fma(5.0 * a[4], T, 4.0 * a[3]);
+    cp = fma(cp, T, 3.0 * a[2]);
+    cp = fma(cp, T, 2.0 * a[1]);
+    cp = fma(cp, T, a[0]);
+    const double gamma = cp / (cp - a[5]);
+    const double sp = fabs(u) + sqrt(gamma * R_SI * T * a[5]);
+    speed_max = fmax(speed_max, sp);
+  }
+  tm.sync();
+  return st.rhs;
+}
+
+// Picks the cells that get a four-warp team in the next launch: those whose
+// neighbourhood [i-2, i+2] took at least HOT_MIN_RHS right-hand sides in
+// this launch (the reaction front moves under a cell per step), the costliest
+// power-of-two classes first, at most HOT_MAX, listed in cell order. Run by
+// the last CTA of a launch, after every cell's cost is written.
+__device__ void select_hot(const int* cost, int n, unsigned* hot, unsigned* scratch) {
+  unsigned* hist = scratch;        // [33]
+  unsigned* cnt = scratch + 40;    // [blockDim]
+  const int nt = blockDim.x, tid = threadIdx.x;
+  for (int b = tid; b < 33; b += nt) hist[b] = 0;
+  __syncthreads();
+  const int chunk = (n + nt - 1) / nt;
+  const int c0 = min(n, tid * chunk), c1 = min(n, c0 + chunk);
+  auto nmax = [&](int i) {
+    int m = 0;
+    for (int j = max(0, i - 2); j <= min(n - 1, i + 2); ++j) m = max(m, __ldcg(cost + j));
+    return m;
+  };
+  for (int i = c0; i < c1; ++i) {
+    const int m = nmax(i);
+    if (m >= HOT_MIN_RHS) atomicAdd(&hist[31 - __clz(m)], 1u);
+  }
+  __syncthreads();
+  if (tid == 0) {
+    // smallest class threshold whose cumulative count fits; if the top
+    // class alone overflows, it is taken and capped in cell order
+    int B = 32;
+    unsigned cum = 0;
+    for (int b = 30; b >= 0 && (1 << b) >= HOT_MIN_RHS; --b) {
+      if (hist[b] == 0) continue;
+      if (cum + hist[b] > (unsigned)HOT_MAX) {
+        if (B == 32) B = b;
+        break;
+      }
+      cum += hist[b];
+      B = b;
+    }
+    hist[32] = (unsigned)B;
+  }
+  __syncthreads();
+  const int B = (int)hist[32];
+  unsigned mine = 0;
+  if (B < 32)
+    for (int i = c0; i < c1; ++i) mine += (nmax(i) >= (1 << B)) ? 1u : 0u;
+  cnt[tid] = mine;
+  __syncthreads();
+  if (tid == 0) {
+    unsigned run = 0;
+    for (int q = 0; q < nt; ++q) {
+      const unsigned v = cnt[q];
+      cnt[q] = run;
+      run += v;
+    }
+    hot[0] = min(run, (unsigned)HOT_MAX);
+  }
+  __syncthreads();
+  if (B < 32) {
+    unsigned pos = cnt[tid];
+    for (int i = c0; i < c1 && pos < (unsigned)HOT_MAX; ++i)
+      if (nmax(i) >= (1 << B)) hot[1 + pos++] = (unsigned)i;
+  }
+}
+
+// Tube mode: every interior cell of the tube. The cells listed as hot by the
+// previous launch go first, one per CTA, each to a four-warp team (warps
+// 0-3, one per SM sub-partition; the CTA's other warps wait); then all warps
+// take the remaining cells one per warp from the work counter.
 __global__ void __launch_bounds__(MAXW * 32, 1)
     k_tube_chem(const char* g_tab, int tab_bytes, ChemLaunch L, unsigned* next, ChemCounters* cnt) {
   extern __shared__ __align__(16) char smem[];
+  __shared__ unsigned s_hot[HOT_MAX + 1];
+  __shared__ int s_last;
   if (L.step_active && *L.step_active == 0) return;
   const double dt = L.dt_dev ? *L.dt_dev : L.dt;
+  for (int i = threadIdx.x; i <= HOT_MAX; i += blockDim.x) s_hot[i] = L.hot ? L.hot[i] : 0u;
   stage_tables(smem, g_tab, tab_bytes);
   const Tabs t = bind_tabs(smem);
-  WarpWork& w = ((WarpWork*)(smem + ((tab_bytes + 255) / 256) * 256))[threadIdx.x >> 5];
-  const int lane = threadIdx.x & 31;
-  const int ns = t.ns;
-  const size_t ld = (size_t)L.ld;
+  WarpWork* ww = work_slots(smem, tab_bytes);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   double speed_max = 0.0;
+  const int nwarps = blockDim.x >> 5;
+  const unsigned nteam = (nwarps >= TEAM / 32) ? min(min(s_hot[0], (unsigned)HOT_MAX), gridDim.x) : 0u;
+  if (blockIdx.x < nteam) {
+    if (warp < TEAM / 32) {
+      // team scratch: the second work slot, unused while the team runs
+      double* spare = reinterpret_cast<double*>(&ww[1]);
+      const Team<TEAM> tm{(int)threadIdx.x, 1, spare, spare + 256};
+      const unsigned cell = s_hot[1 + blockIdx.x];
+      const int c = tube_cell<TEAM>(t, tm, ww[0], L, cell, dt, speed_max, cnt);
+      if (threadIdx.x == 0 && L.cost) L.cost[cell] = c;
+    }
+    __syncthreads();
+  }
+  const Team<32> tw{lane, 0, nullptr, nullptr};
+  WarpWork& w = ww[warp];
   for (int guard = 0; guard < (1 << 30); ++guard) {
     unsigned cell = 0;
     if (lane == 0) cell = atomicAdd(next, 1u);
     cell = __shfl_sync(0xffffffffu, cell, 0);
     if (cell >= (unsigned)L.n) break;
-    double* q = L.qf + cell + GHOST;
-    double* Q = L.qc + cell + GHOST;
-    const double rho = q[0];
-    // reaction_macks: y_sp = adjust_sum(Y), yiT = [y_sp, T] (SRC/source.f90:47-56);
-    // the raw Y stay in the qf rows for the heat release rate.
-    double s = 0.0;
-    for (int k = lane; k < ns; k += 32) {
-      const double yp = clip0_d(q[(3 + k) * ld]);
-      w.y0[k] = yp;
-      s += yp;
-    }
-    s = warp_sum(s);
-    const double inv_s = 1.0 / s;
-    for (int k = lane; k < ns; k += 32) w.y0[k] *= inv_s;
-    if (lane == 0) w.y0[ns] = q[2 * ld];
-    __syncwarp();
-    Cell c{rho * 1e-3, dt, L.rtol, L.atol};
-    CellStats st = integrate(t, w, c, lane);
-    add_stats(cnt, st, lane);
-    if (st.failed && lane == 0) atomicOr(L.err, (unsigned)EDYN_E_CHEM);
-    // adjust_sum(Y) after the step
-    double s2 = 0.0;
-    for (int k = lane; k < ns; k += 32) {
-      const double y = clip0_d(w.y0[k]);
-      w.y0[k] = y;
-      s2 += y;
-    }
-    s2 = warp_sum(s2);
-    const double inv2 = 1.0 / s2;
-    const double Tn = w.y0[ns];
-    // heat release rate, SRC/thermo.f90:83-103 (qf rows still hold Y0 raw)
-    const double rho_cgs = rho * 1e-3;
-    double hr = 0.0, hs = 0.0, sz = 0.0;
-    for (int k = lane; k < ns; k += 32) {
-      const double yn = w.y0[k] * inv2;
-      w.y0[k] = yn;
-      const double y0raw = q[(3 + k) * ld];
-      hr = fma(rho_cgs * t.d.hf[k], yn - y0raw, hr);
-      // qfToQc energy: e = R (H(T) - T Sz)/S_Y with the adjusted Y (S_Y = 1)
-      const int r = (Tn > t.d.tmid[k]) ? 1 : 0;
-      const double* ch = t.d.ch + r * 6 * NSMAX;
-      double hh = fma(ch[4 * NSMAX + k], Tn, ch[3 * NSMAX + k]);
-      hh = fma(hh, Tn, ch[2 * NSMAX + k]);
-      hh = fma(hh, Tn, ch[1 * NSMAX + k]);
-      hh = fma(hh, Tn, ch[0 * NSMAX + k]);
-      hh = fma(hh, Tn, ch[5 * NSMAX + k]);
-      const double z = yn * t.d.invW[k];
-      hs = fma(z, hh, hs);
-      sz += z;
-    }
-    hr = warp_sum(hr);
-    hs = warp_sum(hs);
-    sz = warp_sum(sz);
-    const double u = q[ld];
-    const double e_int = R_SI * (hs - Tn * sz);
-    const double rhoe = rho * (e_int + 0.5 * (u * u));
-    // write Qc = qfToQc(qf) and qf (T, Y); the post-step QcToqf then
-    // recovers T from rho e with the Newton solve.
-    for (int k = lane; k < ns; k += 32) {
-      q[(3 + k) * ld] = w.y0[k];
-      Q[(3 + k) * ld] = rho * w.y0[k];
-    }
-    if (lane == 0) {
-      Q[2 * ld] = rhoe;
-      L.hrr[cell] = -(hr / dt) * 1e-1;
-    }
-    __syncwarp();
-    // post-step QcToqf: Newton on rho e for T (from 1000 K when strict)
-    double T = L.strict_newton ? 1000.0 : Tn;
-    const double E = (rhoe / rho - 0.5 * (u * u)) / R_SI;
-    double gN = 1e30, dTN = 1e30;
-    int it = 0;
-    double A[6];
-    double Sz = 0.0;
-    while (fabs(gN) >= fabs(E) * 1e-9 && fabs(dTN) >= T * 1e-6 && it < 10) {
-      // premixed NASA coefficients at the current T (lanes over species)
-      double a0 = 0, a1 = 0, a2 = 0, a3 = 0, a4 = 0, a5 = 0, sz_ = 0;
-      for (int k = lane; k < ns; k += 32) {
-        const int r = (T > t.d.tmid[k]) ? 1 : 0;
-        const double* ch = t.d.ch + r * 6 * NSMAX;
-        const double z = w.y0[k] * t.d.invW[k];
-        a0 = fma(z, ch[0 * NSMAX + k], a0);
-        a1 = fma(z, ch[1 * NSMAX + k], a1);
-        a2 = fma(z, ch[2 * NSMAX + k], a2);
-        a3 = fma(z, ch[3 * NSMAX + k], a3);
-        a4 = fma(z, ch[4 * NSMAX + k], a4);
-        a5 = fma(z, ch[5 * NSMAX + k], a5);
-        sz_ += z;
-      }
-      A[0] = warp_sum(a0);
-      A[1] = warp_sum(a1);
-      A[2] = warp_sum(a2);
-      A[3] = warp_sum(a3);
-      A[4] = warp_sum(a4);
-      A[5] = warp_sum(a5);
-      Sz = warp_sum(sz_);
-      double p = fma(A[4], T, A[3]);
-      p = fma(p, T, A[2]);
-      p = fma(p, T, A[1]);
-      p = fma(p, T, A[0]);
-      const double H = fma(p, T, A[5]);
-      double cp = fma(5.0 * A[4], T, 4.0 * A[3]);
-      cp = fma(cp, T, 3.0 * A[2]);
-      cp = fma(cp, T, 2.0 * A[1]);
-      cp = fma(cp, T, A[0]);
-      gN = H - T * Sz - E;
-      dTN = -gN / (cp - Sz);
-      T = fmax(20.0, fmin(6000.0, T + dTN));
-      ++it;
-    }
-    if (lane == 0) q[2 * ld] = T;
-    // signal speed of the new state for the next time step
-    if (L.cvel_out) {
-      double a0 = 0, a1 = 0, a2 = 0, a3 = 0, a4 = 0, sz_ = 0;
-      for (int k = lane; k < ns; k += 32) {
-        const int r = (T > t.d.tmid[k]) ? 1 : 0;
-        const double* ch = t.d.ch + r * 6 * NSMAX;
-        const double z = w.y0[k] * t.d.invW[k];
-        a0 = fma(z, ch[0 * NSMAX + k], a0);
-        a1 = fma(z, ch[1 * NSMAX + k], a1);
-        a2 = fma(z, ch[2 * NSMAX + k], a2);
-        a3 = fma(z, ch[3 * NSMAX + k], a3);
-        a4 = fma(z, ch[4 * NSMAX + k], a4);
-        sz_ += z;
-      }
-      a0 = warp_sum(a0);
-      a1 = warp_sum(a1);
-      a2 = warp_sum(a2);
-      a3 = warp_sum(a3);
-      a4 = warp_sum(a4);
-      sz_ = warp_sum(sz_);
-      double cp = fma(5.0 * a4, T, 4.0 * a3);
-      cp = fma(cp, T, 3.0 * a2);
-      cp = fma(cp, T, 2.0 * a1);
-      cp = fma(cp, T, a0);
-      const double gamma = cp / (cp - sz_);
-      const double sp = fabs(u) + sqrt(gamma * R_SI * T * sz_);
-      speed_max = fmax(speed_max, sp);
-    }
-    __syncwarp();
+    // cells taken by a team in this launch
+    bool taken = false;
+    for (unsigned j = lane; j < nteam; j += 32) taken |= (s_hot[1 + j] == cell);
+    if (__any_sync(0xffffffffu, taken)) continue;
+    const int c = tube_cell<32>(t, tw, w, L, cell, dt, speed_max, cnt);
+    if (lane == 0 && L.cost) L.cost[cell] = c;
   }
   if (L.cvel_out && lane == 0 && speed_max > 0.0)
     atomicMax(L.cvel_out, (unsigned long long)__double_as_longlong(speed_max));
-  if (L.time) {
-    // one CTA advances the clock after all warps of the grid have taken
-    // their last cell: count finished CTAs.
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      __threadfence();
-      const unsigned done = atomicAdd(next + 1, 1u);
-      if (done == gridDim.x - 1) {
-        *L.time = *L.time + dt;
-        *L.nsteps = *L.nsteps + 1;
-      }
+  // the last CTA to finish advances the clock (device loop) and picks the
+  // next launch's team cells
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    const unsigned done = atomicAdd(next + 1, 1u);
+    s_last = (done == gridDim.x - 1) ? 1 : 0;
+  }
+  __syncthreads();
+  if (s_last) {
+    __threadfence();
+    if (threadIdx.x == 0 && L.time) {
+      *L.time = *L.time + dt;
+      *L.nsteps = *L.nsteps + 1;
     }
+    if (L.cost && L.hot) select_hot(L.cost, L.n, L.hot, reinterpret_cast<unsigned*>(ww));
   }
 }
 
@@ -1288,7 +1641,10 @@ int chem_init(ChemState& s, const edyn_mech& m, const ThermoTable& tb, cudaStrea
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   int maxs = 0;
   cudaDeviceGetAttribute(&maxs, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-  const long room = (long)maxs - (long)tot;
+  cudaFuncAttributes fa;
+  e = cudaFuncGetAttributes(&fa, k_tube_chem);
+  if (e != cudaSuccess) return (int)e;
+  const long room = (long)maxs - (long)tot - (long)fa.sharedSizeBytes;
   s.warps = (int)std::min<long>(MAXW, room / (long)sizeof(WarpWork));
   if (s.warps < 1) return (int)cudaErrorInvalidConfiguration;
   s.smem = tot + sizeof(WarpWork) * (size_t)s.warps;
@@ -1316,6 +1672,8 @@ cudaError_t chem_launch_batch(ChemState& s, const ChemLaunch& L, cudaStream_t st
 
 cudaError_t chem_launch_tube(ChemState& s, const ChemLaunch& L, cudaStream_t st) {
   cudaError_t e = cudaMemsetAsync(s.d_next, 0, 2 * sizeof(unsigned), st);
+  if (e != cudaSuccess) return e;
+  e = cudaMemsetAsync(s.d_count, 0, sizeof(ChemCounters), st);
   if (e != cudaSuccess) return e;
   const int grid = std::min(s.ctas, (L.n + s.warps - 1) / s.warps);
   k_tube_chem<<<std::max(1, grid), s.warps * 32, s.smem, st>>>((const char*)s.d_tables, (int)s.table_bytes, L,

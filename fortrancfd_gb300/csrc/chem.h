@@ -8,8 +8,11 @@
 
 namespace edyn {
 
+// Cells of a tube launch that get a four-warp team, at most.
+constexpr int HOT_MAX = 64;
+
 struct ChemCounters {
-  unsigned long long rhs, steps, rejects, failed, jac, cells;
+  unsigned long long rhs, steps, rejects, failed, jac, cells, team_cells;
 };
 
 struct ChemState {
@@ -36,6 +39,8 @@ struct ChemLaunch {
   double* time;
   long long* nsteps;
   int strict_newton;
+  int* cost;        // right-hand sides each cell took in the last launch (n)
+  unsigned* hot;    // [0] count, [1..HOT_MAX] cells that get a team next launch
   // batch mode
   const double* rho_batch;
   const double* dt_batch;

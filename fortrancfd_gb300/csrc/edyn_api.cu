@@ -55,6 +55,8 @@ struct Ctx {
   double* d_dt = nullptr;
   unsigned long long* d_cvel = nullptr;
   unsigned* d_err = nullptr;
+  int* d_cost = nullptr;      // right-hand sides per cell in the last chemistry launch
+  unsigned* d_hot = nullptr;  // cells that get a four-warp team in the next one
   cudaGraphExec_t graph = nullptr;
   int graph_steps = 0;
   double graph_cfl = -1, graph_tend = -1;
@@ -174,6 +176,8 @@ int source_step(Ctx* c, double dt, bool dev) {
     L.nsteps = c->d_nsteps;
   }
   L.err = c->d_err;
+  L.cost = c->d_cost;
+  L.hot = c->d_hot;
   cudaError_t e = chem_launch_tube(c->chem, L, c->stream);
   if (e != cudaSuccess) return fail(c, EDYN_E_CUDA, "chemistry launch: %s", cudaGetErrorString(e));
   return EDYN_OK;
@@ -308,6 +312,10 @@ int edyn_init(const char* chem_dir, int nspe, int nequ, int ncell, int lvir, con
   CK(cudaMalloc(&c->d_cvel, sizeof(unsigned long long)));
   CK(cudaMalloc(&c->d_err, sizeof(unsigned)));
   CK(cudaMemsetAsync(c->d_err, 0, sizeof(unsigned), c->stream));
+  CK(cudaMalloc(&c->d_cost, (size_t)ncell * sizeof(int)));
+  CK(cudaMalloc(&c->d_hot, (HOT_MAX + 1) * sizeof(unsigned)));
+  CK(cudaMemsetAsync(c->d_cost, 0, (size_t)ncell * sizeof(int), c->stream));
+  CK(cudaMemsetAsync(c->d_hot, 0, (HOT_MAX + 1) * sizeof(unsigned), c->stream));
   int rc = fluid_upload_tables(c->tb, c->stream);
   if (rc == -1) return fail(c, EDYN_E_MECH, "a different mechanism is already loaded in this process");
   if (rc) return fail(c, EDYN_E_CUDA, "constant tables: %s", cudaGetErrorString((cudaError_t)rc));
@@ -504,6 +512,17 @@ int edyn_download(void* ctx, double* qf_aos, double* qc_aos, double* hrr) {
   return EDYN_OK;
 }
 
+int edyn_chem_stats(void* ctx, double* stats) {
+  Ctx* c = (Ctx*)ctx;
+  if (!c || !c->qc || !stats) return EDYN_E_ARG;
+  ChemCounters k;
+  cudaError_t e = chem_read_counters(c->chem, &k, c->stream);
+  if (e != cudaSuccess) return fail(c, EDYN_E_CUDA, "counters: %s", cudaGetErrorString(e));
+  const unsigned long long v[7] = {k.rhs, k.steps, k.rejects, k.failed, k.jac, k.cells, k.team_cells};
+  for (int i = 0; i < 7; ++i) stats[i] = (double)v[i];
+  return EDYN_OK;
+}
+
 int edyn_reactors_device(void* ctx, int n, const double* rho_d, const double* dt_d, double* yiT_d, double* stats) {
   Ctx* c = (Ctx*)ctx;
   if (!c || n < 0 || (n > 0 && (!rho_d || !dt_d || !yiT_d))) return EDYN_E_ARG;
@@ -583,6 +602,8 @@ int edyn_finalize(void* ctx) {
   cudaFree(c->d_dt);
   cudaFree(c->d_cvel);
   cudaFree(c->d_err);
+  cudaFree(c->d_cost);
+  cudaFree(c->d_hot);
   if (c->own) cudaStreamDestroy(c->own);
   delete c;
   return EDYN_OK;

@@ -68,6 +68,7 @@ def lib() -> ctypes.CDLL:
     L.edyn_reactors.argtypes = [vp, i, dp, dp, dp, dp]
     L.edyn_reactors_device.argtypes = [vp, i, vp, vp, vp, dp]
     L.edyn_set_stream.argtypes = [vp, vp]
+    L.edyn_chem_stats.argtypes = [vp, dp]
     L.edyn_last_error.argtypes = [vp, ctypes.c_char_p, i]
     L.edyn_finalize.argtypes = [vp]
     L.edyn_mech_compile.argtypes = [cp, cp, ctypes.c_char_p, i]
@@ -205,6 +206,13 @@ class Tube(_Ctx):
         n = ctypes.c_longlong(0)
         self._check(lib().edyn_advance(self._h, cfl, tend, max_steps, ctypes.byref(t), ctypes.byref(n)))
         return t.value, n.value
+
+    def chem_stats(self) -> dict:
+        """Counters of the last chemistry launch."""
+        st = np.zeros(7)
+        self._check(lib().edyn_chem_stats(self._h, _ptr(st)))
+        keys = ("rhs", "steps", "rejects", "failed", "jac", "cells", "team_cells")
+        return {k: int(v) for k, v in zip(keys, st)}
 
     def download(self):
         qf = np.empty((self.ncell, self.nequ))

@@ -145,6 +145,13 @@ int edyn_reactors(void* ctx, int n, const double* rho, const double* dt, double*
 /* Same, on device pointers already resident in GPU memory (no copies). */
 int edyn_reactors_device(void* ctx, int n, const double* rho_d, const double* dt_d, double* yiT_d, double* stats);
 
+/* Counters of the last chemistry launch of this context (tube or batch),
+ * 7 values: right-hand-side evaluations, accepted steps, rejected steps,
+ * failed cells, Jacobians, cells, cells integrated by a four-warp team.
+ * No counterpart in the reference, which reports none (its solver's
+ * statistics stay inside macks, SRC/source.f90:58). */
+int edyn_chem_stats(void* ctx, double* stats);
+
 /* Binds the context to a caller-owned CUDA stream (cudaStream_t as void*);
  * NULL returns to the context's own stream. */
 int edyn_set_stream(void* ctx, void* stream);

@@ -84,9 +84,13 @@ def test_tube_chemistry_short_run(oracle, names):
     ot.set_interior(qf0, qc0)
     g = Tube(case.ncell, case.dx, flag_acu=2, flag_weno=3, flag_rbound=1, do_reaction=1, rtol=1e-6, atol=1e-14)
     g.upload(qf0, qc0)
+    teams = []
     for _ in range(5):
         ot.step(case.cfl)
         g.step(case.cfl)
+        teams.append(g.chem_stats()["team_cells"])
+    # the costliest cells of each call after the first go to four-warp teams
+    assert teams[0] == 0 and min(teams[1:]) > 0, teams
     qf_o, _ = ot.get()
     qf_g, _, hrr = g.download()
     K = len(names)

@@ -75,6 +75,8 @@ struct TabHdr {
   int o_ch[2];                 // [2][6][NSMAX] H/R coefficients (a1, a2/2, .., a6)
   int o_cp[2];                 // [2][5][NSMAX] Cp/R coefficients (a1..a5)
   int o_nu[2];                 // [nent] net stoichiometric coefficient of each entry
+  int o_e2;                    // double[64]: 2^(j/64), the table of texp
+  int fr0, nfr;                // the fall-off reactions fill rounds [fr0, fr0 + nfr) of 32
 };
 
 template <class R>
@@ -86,6 +88,7 @@ struct Tabs {
   const TabHdr* h;
   const unsigned *w0, *w1, *w2, *w3, *w4, *w5, *ent;
   const int *spi, *tb_sp, *pc, *lane, *spc, *spp;
+  const double* e2;
   int ns, nr, nrp, npc;
   RTabs<double> d;
   RTabs<float> f;
@@ -132,6 +135,7 @@ __device__ __forceinline__ Tabs bind_tabs(const char* base) {
   t.spc = (const int*)(base + h.o_spc);
   t.spp = (const int*)(base + h.o_spp);
   t.ent = (const unsigned*)(base + h.o_ent);
+  t.e2 = (const double*)(base + h.o_e2);
   t.ns = h.ns;
   t.nr = h.nr;
   t.nrp = h.nrp;
@@ -190,6 +194,7 @@ struct Team {
   int bar;        // named barrier id (four-warp teams)
   double* red;    // cross-warp scratch, 256 doubles (four-warp teams)
   double* part4;  // gather partial sums, [4][TEAM_PIECES] (four-warp teams)
+  double* pre;    // temperature-only rate parts, 480 doubles (four-warp teams)
   __device__ __forceinline__ void sync() const {
     if constexpr (TW == 32) {
       __syncwarp();
@@ -261,109 +266,141 @@ struct Math<float> {
   static __device__ __forceinline__ float rint_(float x) { return rintf(x); }
 };
 
+// exp(x) in FP64 by the table-driven method of P. T. P. Tang (ACM TOMS 15,
+// 1989): x = (64 m + j) ln2/64 + r with |r| <= ln2/128, so exp(x) =
+// 2^m 2^(j/64) e^r, with 2^(j/64) from a 64-entry table (built on the host)
+// and e^r - 1 from its degree-5 Taylor polynomial (truncation below 4e-17).
+// About ten FP64 instructions, within 1 ulp of CUDA's exp. texp_r: arguments
+// of a few units (no range handling); texp: x clamped to [-708, 709.7], so
+// the result stays a normal number (exp(-708) stands in for anything smaller).
+__device__ __forceinline__ double texp_r(double x, const double* e2) {
+  const double magic = 6755399441055744.0;  // 1.5 * 2^52: rounds to an integer
+  const double k64 = 92.33248261689366;     // 64 / ln 2
+  const double l1 = 0.010830424695086549;   // ln2/64, leading bits (low 20 bits zero)
+  const double l2 = 1.162596423439437e-12;  // ln2/64 - l1
+  const double tk = fma(x, k64, magic);
+  const double kd = tk - magic;
+  const int ki = __double2loint(tk);
+  double r = fma(-kd, l1, x);
+  r = fma(-kd, l2, r);
+  double s = fma(r, 1.0 / 120.0, 1.0 / 24.0);
+  s = fma(s, r, 1.0 / 6.0);
+  s = fma(s, r, 0.5);
+  const double p = fma(r * r, s, r);
+  const double tj = e2[ki & 63];
+  const double v = fma(tj, p, tj);
+  return __hiloint2double(__double2hiint(v) + ((ki >> 6) << 20), __double2loint(v));
+}
+__device__ __forceinline__ double texp(double x, const double* e2) {
+  return texp_r(fmin(fmax(x, -708.0), 709.7), e2);
+}
+
+// exp in the rate evaluation: the table method in FP64, the SFU in FP32
+template <class R>
+__device__ __forceinline__ R ex_t(R x, const Tabs& t);
+template <>
+__device__ __forceinline__ double ex_t<double>(double x, const Tabs& t) { return texp(x, t.e2); }
+template <>
+__device__ __forceinline__ float ex_t<float>(float x, const Tabs& t) { return __expf(x); }
+
 __device__ __forceinline__ unsigned sp_of(unsigned w, int s) { return (w >> (8 * s)) & 0xffu; }
 
 // Rate constants of one reaction (CKRATT + the third-body/fall-off part of
-// CKRATX) and its net rate of progress. Returns qf - qr; also returns the
-// forward/reverse parts for the Jacobian. invKc uses the scaled species
-// exponentials m[k] 2^en[k] = exp(S_k/R - H_k/RT).
+// CKRATX) and its net rate of progress, in pieces that the four-warp FP64
+// right-hand side also uses with precomputed temperature-only parts. invKc
+// uses the scaled species exponentials m[k] 2^en[k] = exp(S_k/R - H_k/RT).
 template <class R>
 struct RxnEval {
   R kf, kr, qf, qr, cm, pr, pcor_d;  // pcor_d: d ln(pcor)/d ln(CM) (fall-off, F held fixed)
 };
 
+// Arrhenius k = A exp(beta ln T - E/T) (CKRATT 6645), as the reference
+// evaluates it in FP64; FP32 (Jacobian only) uses the logarithmic form since
+// pre-exponentials up to 1e74 do not fit in single precision.
 template <class R>
-__device__ __forceinline__ RxnEval<R> eval_rxn(const Tabs& t, int i, R logT, R invT, R T, R pfac, R ipfac, R ctot,
-                                               const R* C, const R* m, const R* mi, const int* en) {
-  using M = Math<R>;
+__device__ __forceinline__ R arrhenius(const Tabs& t, int i, unsigned fl, R logT, R invT) {
   const RTabs<R>& x = t.r<R>();
-  RxnEval<R> o;
-  const unsigned w0 = t.w0[i], w1 = t.w1[i], w2 = t.w2[i];
-  const unsigned fl = w0 >> 24;
-  R kf;
-  if (sizeof(R) == sizeof(double)) {
-    // CKRATT 6645: A exp(beta ln T - E/T), as the reference evaluates it
-    kf = x.A[i];
-    if (fl & F_EXP) kf = kf * M::ex(x.B[i] * logT - x.E[i] * invT);
+  if constexpr (sizeof(R) == sizeof(double)) {
+    R kf = x.A[i];
+    if (fl & F_EXP) kf = kf * ex_t<R>(x.B[i] * logT - x.E[i] * invT, t);
+    return kf;
   } else {
-    // single precision (Jacobian only): pre-exponentials up to 1e74 do not
-    // fit in FP32, so the logarithmic form is used
-    kf = M::ex(x.lnA[i] + x.B[i] * logT - x.E[i] * invT);
+    return Math<R>::ex(x.lnA[i] + x.B[i] * logT - x.E[i] * invT);
   }
-  R kr = 0;
-  if (fl & F_REV) {
-    // 1/Kc = exp(-sum nu (S/R - H/RT)) * pfac^(-sum nu)  (CKRATT, 6647-6667),
-    // from the scaled species exponentials m 2^en and their reciprocals
-    R mant = 1;
-    int ex2 = 0;
+}
+
+// 1/Kc = exp(-sum nu (S/R - H/RT)) * pfac^(-sum nu)  (CKRATT, 6647-6667),
+// from the scaled species exponentials m 2^en and their reciprocals
+template <class R>
+__device__ __forceinline__ R inv_kc(unsigned w0, unsigned w1, unsigned w2, R pfac, R ipfac, const R* m, const R* mi,
+                                    const int* en) {
+  using M = Math<R>;
+  R mant = 1;
+  int ex2 = 0;
 #pragma unroll
-    for (int s = 0; s < 3; ++s) {
-      const unsigned kr_ = sp_of(w0, s), kp = sp_of(w1, s);
-      const int nr_ = (w2 >> (4 * s)) & 15, np = (w2 >> (12 + 4 * s)) & 15;
-      if (kr_ != 255u) {
-        const R mm = m[kr_];
-        mant *= (nr_ == 1) ? mm : (nr_ == 2 ? mm * mm : mm * mm * mm);
-        ex2 += nr_ * en[kr_];
-      }
-      if (kp != 255u) {
-        const R mm = mi[kp];
-        mant *= (np == 1) ? mm : (np == 2 ? mm * mm : mm * mm * mm);
-        ex2 -= np * en[kp];
-      }
+  for (int s = 0; s < 3; ++s) {
+    const unsigned kr_ = sp_of(w0, s), kp = sp_of(w1, s);
+    const int nr_ = (w2 >> (4 * s)) & 15, np = (w2 >> (12 + 4 * s)) & 15;
+    if (kr_ != 255u) {
+      const R mm = m[kr_];
+      mant *= (nr_ == 1) ? mm : (nr_ == 2 ? mm * mm : mm * mm * mm);
+      ex2 += nr_ * en[kr_];
     }
-    const int dnu = (int)(w1 >> 24) - 8;
-    R ikc = M::ldx(mant, ex2);
-    if (dnu == 1) ikc = ikc * ipfac;
-    else if (dnu == -1) ikc = ikc * pfac;
-    else if (dnu != 0) ikc = ikc * pow(pfac, (R)(-dnu));
-    ikc = fmin(ikc, M::big());  // kr = kf / max(Kc, SMALL)
-    kr = kf * ikc;
-    if (sizeof(R) != sizeof(double)) kr = fmin(kr, (R)1e30f);
-  }
-  o.cm = 1;
-  o.pr = 0;
-  o.pcor_d = 0;
-  const int aux = (int)(w2 >> 24);
-  if (fl & (F_CM | F_KFAL)) {
-    R cm;
-    if (fl & F_KFAL) {
-      cm = C[t.spi[aux * 4 + 2]];
-    } else {
-      cm = ctot;
-      const int b = t.spi[aux * 4 + 0], c = t.spi[aux * 4 + 1];
-      for (int q = b; q < b + c; ++q) cm += x.tb_am1[q] * C[t.tb_sp[q]];
-    }
-    o.cm = cm;
-    if (fl & F_FALL) {
-      const R* fp = x.aux + aux * 9;
-      const R k0 = (sizeof(R) == sizeof(double)) ? fp[0] * M::ex(fp[1] * logT - fp[2] * invT)
-                                                 : M::ex(fp[8] + fp[1] * logT - fp[2] * invT);
-      const R pr = k0 * cm / kf;
-      R pcor = pr / (1 + pr);
-      const int ifop = (int)fp[7];
-      if (ifop > 1) {
-        const R prlog = M::l10(fmax(pr, M::small()));
-        R fcent = (1 - fp[3]) * M::ex(-T / fp[4]) + fp[3] * M::ex(-T / fp[5]);
-        if (ifop == 4) fcent += M::ex(-fp[6] * invT);
-        const R fclog = M::l10(fmax(fcent, M::small()));
-        const R xn = (R)0.75 - (R)(double)1.27f * fclog;
-        const R cprlog = prlog - ((R)(double)0.4f + (R)(double)0.67f * fclog);
-        const R q = cprlog / (xn - (R)(double)0.14f * cprlog);
-        const R flog = fclog / (1 + q * q);
-        pcor = M::p10(flog) * pcor;
-      }
-      kf *= pcor;
-      kr *= pcor;
-      o.pr = pr;
-      o.pcor_d = 1 / (1 + pr);
-    } else {
-      kf *= cm;
-      kr *= cm;
-      o.pcor_d = 1;
+    if (kp != 255u) {
+      const R mm = mi[kp];
+      mant *= (np == 1) ? mm : (np == 2 ? mm * mm : mm * mm * mm);
+      ex2 -= np * en[kp];
     }
   }
-  // mass-action products (CKRATX 6900-6915)
-  R qf = kf, qr = kr;
+  const int dnu = (int)(w1 >> 24) - 8;
+  R ikc = M::ldx(mant, ex2);
+  if (dnu == 1) ikc = ikc * ipfac;
+  else if (dnu == -1) ikc = ikc * pfac;
+  else if (dnu != 0) ikc = ikc * pow(pfac, (R)(-dnu));
+  return fmin(ikc, M::big());  // kr = kf / max(Kc, SMALL)
+}
+
+// third-body concentration: a named collider (fall-off "(+X)") or the mixture
+// with efficiencies (CKRATX 6860-6890)
+template <class R>
+__device__ __forceinline__ R collider(const Tabs& t, unsigned fl, int aux, R ctot, const R* C) {
+  const RTabs<R>& x = t.r<R>();
+  if (fl & F_KFAL) return C[t.spi[aux * 4 + 2]];
+  R cm = ctot;
+  const int b = t.spi[aux * 4 + 0], c = t.spi[aux * 4 + 1];
+  for (int q = b; q < b + c; ++q) cm += x.tb_am1[q] * C[t.tb_sp[q]];
+  return cm;
+}
+
+// log10 of the Troe centering factor (temperature only; CKRATX 6895-6905)
+template <class R>
+__device__ __forceinline__ R troe_fclog(const Tabs& t, const R* fp, int ifop, R T, R invT) {
+  using M = Math<R>;
+  R fcent = (1 - fp[3]) * ex_t<R>(-T / fp[4], t) + fp[3] * ex_t<R>(-T / fp[5], t);
+  if (ifop == 4) fcent += ex_t<R>(-fp[6] * invT, t);
+  return M::l10(fmax(fcent, M::small()));
+}
+
+// fall-off blending factor pr/(1+pr) F from the reduced pressure and, for
+// Troe, log10 Fcent (the CHEMKIN-II single-precision constants widened)
+template <class R>
+__device__ __forceinline__ R falloff_pcor(const Tabs& t, R pr, int ifop, R fclog) {
+  using M = Math<R>;
+  R pcor = pr / (1 + pr);
+  if (ifop > 1) {
+    const R prlog = M::l10(fmax(pr, M::small()));
+    const R xn = (R)0.75 - (R)(double)1.27f * fclog;
+    const R cprlog = prlog - ((R)(double)0.4f + (R)(double)0.67f * fclog);
+    const R q = cprlog / (xn - (R)(double)0.14f * cprlog);
+    const R flog = fclog / (1 + q * q);
+    pcor = ex_t<R>((R)2.302585092994045684 * flog, t) * pcor;  // 10^flog
+  }
+  return pcor;
+}
+
+// mass-action products (CKRATX 6900-6915)
+template <class R>
+__device__ __forceinline__ void mass_action(unsigned w0, unsigned w1, unsigned w2, const R* C, R& qf, R& qr) {
 #pragma unroll
   for (int s = 0; s < 3; ++s) {
     const unsigned kr_ = sp_of(w0, s), kp = sp_of(w1, s);
@@ -377,6 +414,48 @@ __device__ __forceinline__ RxnEval<R> eval_rxn(const Tabs& t, int i, R logT, R i
       qr *= (np == 1) ? c : (np == 2 ? c * c : c * c * c);
     }
   }
+}
+
+template <class R>
+__device__ __forceinline__ RxnEval<R> eval_rxn(const Tabs& t, int i, R logT, R invT, R T, R pfac, R ipfac, R ctot,
+                                               const R* C, const R* m, const R* mi, const int* en) {
+  const RTabs<R>& x = t.r<R>();
+  RxnEval<R> o;
+  const unsigned w0 = t.w0[i], w1 = t.w1[i], w2 = t.w2[i];
+  const unsigned fl = w0 >> 24;
+  R kf = arrhenius<R>(t, i, fl, logT, invT);
+  R kr = 0;
+  if (fl & F_REV) {
+    kr = kf * inv_kc<R>(w0, w1, w2, pfac, ipfac, m, mi, en);
+    if (sizeof(R) != sizeof(double)) kr = fmin(kr, (R)1e30f);
+  }
+  o.cm = 1;
+  o.pr = 0;
+  o.pcor_d = 0;
+  const int aux = (int)(w2 >> 24);
+  if (fl & (F_CM | F_KFAL)) {
+    const R cm = collider<R>(t, fl, aux, ctot, C);
+    o.cm = cm;
+    if (fl & F_FALL) {
+      const R* fp = x.aux + aux * 9;
+      const R k0 = (sizeof(R) == sizeof(double)) ? fp[0] * ex_t<R>(fp[1] * logT - fp[2] * invT, t)
+                                                 : Math<R>::ex(fp[8] + fp[1] * logT - fp[2] * invT);
+      const R pr = k0 * cm / kf;
+      const int ifop = (int)fp[7];
+      const R fclog = (ifop > 1) ? troe_fclog<R>(t, fp, ifop, T, invT) : (R)0;
+      const R pcor = falloff_pcor<R>(t, pr, ifop, fclog);
+      kf *= pcor;
+      kr *= pcor;
+      o.pr = pr;
+      o.pcor_d = 1 / (1 + pr);
+    } else {
+      kf *= cm;
+      kr *= cm;
+      o.pcor_d = 1;
+    }
+  }
+  R qf = kf, qr = kr;
+  mass_action<R>(w0, w1, w2, C, qf, qr);
   o.kf = kf;
   o.kr = kr;
   o.qf = qf;
@@ -384,44 +463,82 @@ __device__ __forceinline__ RxnEval<R> eval_rxn(const Tabs& t, int i, R logT, R i
   return o;
 }
 
-// Thermodynamic pass over species (lanes over k): concentrations, scaled
+// Net rate of progress of reaction i in FP64 from its precomputed Arrhenius
+// constant kf and, for fall-off, k0[aux] and log10 Fcent fcl[aux]: the
+// concentration-dependent rest of eval_rxn, with the same arithmetic.
+__device__ __forceinline__ double rop_pre(const Tabs& t, int i, double kf, const double* k0a, const double* fcl,
+                                          double pfac, double ipfac, double ctot, const double* C, const double* m,
+                                          const double* mi, const int* en) {
+  const unsigned w0 = t.w0[i], w1 = t.w1[i], w2 = t.w2[i];
+  const unsigned fl = w0 >> 24;
+  double kr = 0;
+  if (fl & F_REV) kr = kf * inv_kc<double>(w0, w1, w2, pfac, ipfac, m, mi, en);
+  const int aux = (int)(w2 >> 24);
+  if (fl & (F_CM | F_KFAL)) {
+    const double cm = collider<double>(t, fl, aux, ctot, C);
+    if (fl & F_FALL) {
+      const double pr = k0a[aux] * cm / kf;
+      const double pcor = falloff_pcor<double>(t, pr, (int)t.d.aux[aux * 9 + 7], fcl[aux]);
+      kf *= pcor;
+      kr *= pcor;
+    } else {
+      kf *= cm;
+      kr *= cm;
+    }
+  }
+  double qf = kf, qr = kr;
+  mass_action<double>(w0, w1, w2, C, qf, qr);
+  return qf - qr;
+}
+
+// Thermodynamics of species k: its concentration (returned), scaled
 // exp(S/R - H/RT) and its reciprocal, u_k/R and cv_k/(R W_k).
+template <class R>
+__device__ __forceinline__ R species_one(const Tabs& t, int k, const R* y, R rho, R T, R logT, R invT, R* C, R* m,
+                                         R* mi, int* en, R* uR, R* cvm) {
+  using M = Math<R>;
+  const RTabs<R>& x = t.r<R>();
+  const R c = rho * y[k] * x.invW[k];
+  C[k] = c;
+  const int r = (T > x.tmid[k]) ? 1 : 0;
+  const R* cs = x.cs + r * 7 * NSMAX;
+  // S/R - H/RT = a1 (lnT - 1) + a2/2 T + a3/6 T^2 + a4/12 T^3 + a5/20 T^4 + a7 - a6/T (CKSMH, 7501)
+  R p = fma(cs[4 * NSMAX + k], T, cs[3 * NSMAX + k]);
+  p = fma(p, T, cs[2 * NSMAX + k]);
+  p = fma(p, T, cs[1 * NSMAX + k]);
+  const R smh = fma(p, T, fma(cs[0 * NSMAX + k], logT - 1, cs[6 * NSMAX + k])) - cs[5 * NSMAX + k] * invT;
+  // Cody-Waite: smh = n ln2 + r, exp(smh) = exp(r) 2^n
+  const R nn = M::rint_(smh * (R)1.4426950408889634);
+  const R rr = fma(-nn, (R)6.93147180369123816490e-01, smh) - nn * (R)1.90821492927058770002e-10;
+  if constexpr (sizeof(R) == sizeof(double)) {
+    m[k] = texp_r(rr, t.e2);
+    mi[k] = __drcp_rn(m[k]);
+  } else {
+    m[k] = M::ex(rr);
+    mi[k] = M::ex(-rr);
+  }
+  en[k] = (int)nn;
+  const R* ch = x.ch + r * 6 * NSMAX;
+  R h = fma(ch[4 * NSMAX + k], T, ch[3 * NSMAX + k]);
+  h = fma(h, T, ch[2 * NSMAX + k]);
+  h = fma(h, T, ch[1 * NSMAX + k]);
+  h = fma(h, T, ch[0 * NSMAX + k]);
+  uR[k] = fma(h, T, ch[5 * NSMAX + k]) - T;  // u/R = h/R - T
+  const R* cc = x.cp + r * 5 * NSMAX;
+  R cp = fma(cc[4 * NSMAX + k], T, cc[3 * NSMAX + k]);
+  cp = fma(cp, T, cc[2 * NSMAX + k]);
+  cp = fma(cp, T, cc[1 * NSMAX + k]);
+  cp = fma(cp, T, cc[0 * NSMAX + k]);
+  cvm[k] = (cp - 1) * x.invW[k];
+  return c;
+}
+
+// Thermodynamic pass over species (threads over k); returns sum of C_k.
 template <class R, int TW>
 __device__ __forceinline__ R species_pass(const Tabs& t, const Team<TW>& tm, const R* y, R rho, R T, R logT, R invT,
                                           R* C, R* m, R* mi, int* en, R* uR, R* cvm) {
-  using M = Math<R>;
-  const RTabs<R>& x = t.r<R>();
   R csum = 0;
-  for (int k = tm.tid; k < t.ns; k += TW) {
-    const R c = rho * y[k] * x.invW[k];
-    C[k] = c;
-    csum += c;
-    const int r = (T > x.tmid[k]) ? 1 : 0;
-    const R* cs = x.cs + r * 7 * NSMAX;
-    // S/R - H/RT = a1 (lnT - 1) + a2/2 T + a3/6 T^2 + a4/12 T^3 + a5/20 T^4 + a7 - a6/T (CKSMH, 7501)
-    R p = fma(cs[4 * NSMAX + k], T, cs[3 * NSMAX + k]);
-    p = fma(p, T, cs[2 * NSMAX + k]);
-    p = fma(p, T, cs[1 * NSMAX + k]);
-    const R smh = fma(p, T, fma(cs[0 * NSMAX + k], logT - 1, cs[6 * NSMAX + k])) - cs[5 * NSMAX + k] * invT;
-    // Cody-Waite: smh = n ln2 + r, exp(smh) = exp(r) 2^n
-    const R nn = M::rint_(smh * (R)1.4426950408889634);
-    const R rr = fma(-nn, (R)6.93147180369123816490e-01, smh) - nn * (R)1.90821492927058770002e-10;
-    m[k] = M::ex(rr);
-    mi[k] = M::ex(-rr);
-    en[k] = (int)nn;
-    const R* ch = x.ch + r * 6 * NSMAX;
-    R h = fma(ch[4 * NSMAX + k], T, ch[3 * NSMAX + k]);
-    h = fma(h, T, ch[2 * NSMAX + k]);
-    h = fma(h, T, ch[1 * NSMAX + k]);
-    h = fma(h, T, ch[0 * NSMAX + k]);
-    uR[k] = fma(h, T, ch[5 * NSMAX + k]) - T;  // u/R = h/R - T
-    const R* cc = x.cp + r * 5 * NSMAX;
-    R cp = fma(cc[4 * NSMAX + k], T, cc[3 * NSMAX + k]);
-    cp = fma(cp, T, cc[2 * NSMAX + k]);
-    cp = fma(cp, T, cc[1 * NSMAX + k]);
-    cp = fma(cp, T, cc[0 * NSMAX + k]);
-    cvm[k] = (cp - 1) * x.invW[k];
-  }
+  for (int k = tm.tid; k < t.ns; k += TW) csum += species_one<R>(t, k, y, rho, T, logT, invT, C, m, mi, en, uR, cvm);
   return tm.sum(csum);
 }
 
@@ -492,10 +609,106 @@ __device__ void rhs(const Tabs& t, const Team<TW>& tm, WarpWork& w, const R* y, 
   tm.sync();
 }
 
+// The FP64 right-hand side by a four-warp team, balanced over its warps.
+// Phase 1: warps 0-1 run the species pass while warp 2 evaluates the
+// temperature-only parts of the fall-off reactions (k_inf, k0, log10 Fcent:
+// the transcendental-heavy part) and warp 3 the Arrhenius constants of all
+// other reactions. Phase 2: warp 3 takes the fall-off rounds, warps 0-2 the
+// others. Phase 3: production rates from the species-major entry list.
+__device__ void rhs64_team(const Tabs& t, const Team<TEAM>& tm, WarpWork& w, const double* y, double rho,
+                           double* f) {
+  const RTabs<double>& x = t.d;
+  const int ns = t.ns, tid = tm.tid, wq = tid >> 5, lane = tid & 31;
+  double* kfe = tm.pre;       // [352] Arrhenius constants
+  double* k0a = tm.pre + 352; // [64] low-pressure limits, by special-reaction index
+  double* fcl = k0a + 64;     // [64] log10 Fcent
+  const double T = y[ns];
+  const double logT = log(T);
+  const double invT = 1.0 / T;
+  const int fr0 = t.h->fr0, nfr = t.h->nfr;
+  const int nround = t.nrp >> 5;
+  double csum = 0.0;
+  if (wq < 2) {
+    for (int k = tid; k < ns; k += 64)
+      csum += species_one<double>(t, k, y, rho, T, logT, invT, w.C, w.m, w.wdot, w.en, w.uR, w.cvm);
+  } else if (wq == 2) {
+    for (int r = 0; r < nfr; ++r) {
+      const int i = (fr0 + r) * 32 + lane;
+      if (i < t.nr) {
+        const unsigned fl = t.w0[i] >> 24;
+        if (fl & F_FALL) {
+          const int aux = (int)(t.w2[i] >> 24);
+          const double* fp = x.aux + aux * 9;
+          const int ifop = (int)fp[7];
+          kfe[i] = arrhenius<double>(t, i, fl, logT, invT);
+          k0a[aux] = fp[0] * texp(fp[1] * logT - fp[2] * invT, t.e2);
+          fcl[aux] = (ifop > 1) ? troe_fclog<double>(t, fp, ifop, T, invT) : 0.0;
+        }
+      }
+    }
+  } else {
+    for (int r = 0; r < nround; ++r) {
+      const int i = r * 32 + lane;
+      if (i < t.nr) {
+        const unsigned fl = t.w0[i] >> 24;
+        if (!(fl & F_FALL)) kfe[i] = arrhenius<double>(t, i, fl, logT, invT);
+      }
+    }
+  }
+  const double ctot = tm.sum(csum);  // its barriers close phase 1
+  const double pfac = (PATM_CGS / RU_CGS) * invT;
+  const double ipfac = T * (RU_CGS / PATM_CGS);
+  if (nfr > 0 && wq == 3) {
+    for (int r = 0; r < nfr; ++r) {
+      const int i = (fr0 + r) * 32 + lane;
+      w.rop[i] = (i < t.nr) ? rop_pre(t, i, kfe[i], k0a, fcl, pfac, ipfac, ctot, w.C, w.m, w.wdot, w.en) : 0.0;
+    }
+  } else {
+    const int nw = nfr > 0 ? 3 : 4;
+    for (int q = wq; q < nround - nfr; q += nw) {
+      const int rr = (q >= fr0) ? q + nfr : q;
+      const int i = rr * 32 + lane;
+      w.rop[i] = (i < t.nr) ? rop_pre(t, i, kfe[i], k0a, fcl, pfac, ipfac, ctot, w.C, w.m, w.wdot, w.en) : 0.0;
+    }
+  }
+  tm.sync();
+  // production rates: each 32-lane piece list split over the four warps,
+  // two accumulators per thread
+  double* p4 = tm.part4;
+  for (int p = t.lane[lane]; p < t.lane[lane + 1]; ++p) {
+    const int e0 = t.pc[p * 3 + 1], e1 = t.pc[p * 3 + 2];
+    double s0 = 0.0, s1 = 0.0;
+    int q = e0 + wq;
+    for (; q + 4 < e1; q += 8) {
+      s0 = fma(x.nu[q], w.rop[t.ent[q]], s0);
+      s1 = fma(x.nu[q + 4], w.rop[t.ent[q + 4]], s1);
+    }
+    if (q < e1) s0 = fma(x.nu[q], w.rop[t.ent[q]], s0);
+    p4[wq * TEAM_PIECES + p] = s0 + s1;
+  }
+  tm.sync();
+  const double irho = 1.0 / rho;
+  double sc[2] = {0.0, 0.0};  // sum u_k/R w_k, sum Y_k cv_k
+  for (int k = tid; k < ns; k += TEAM) {
+    double s = 0.0;
+    for (int q = t.spc[k]; q < t.spc[k + 1]; ++q) {
+      const int pp = t.spp[q];
+      s += ((p4[pp] + p4[TEAM_PIECES + pp]) + p4[2 * TEAM_PIECES + pp]) + p4[3 * TEAM_PIECES + pp];
+    }
+    f[k] = s * x.W[k] * irho;
+    sc[0] = fma(w.uR[k], s, sc[0]);
+    sc[1] = fma(y[k], w.cvm[k], sc[1]);
+  }
+  tm.sumv(sc);
+  if (tid == 0) f[ns] = -sc[0] / (rho * sc[1]);  // RU cancels in u/cv
+  tm.sync();
+}
+
 template <int TW>
 __device__ __forceinline__ void rhs64(const Tabs& t, const Team<TW>& tm, WarpWork& w, const double* y,
                                       double rho_cgs, double* f) {
-  rhs<double, TW>(t, tm, w, y, rho_cgs, f, w.C, w.m, w.wdot, w.uR, w.cvm, w.rop, w.part);
+  if constexpr (TW == 32) rhs<double, TW>(t, tm, w, y, rho_cgs, f, w.C, w.m, w.wdot, w.uR, w.cvm, w.rop, w.part);
+  else rhs64_team(t, tm, w, y, rho_cgs, f);
 }
 
 // Analytic FP32 Jacobian of the mass-action species block plus finite
@@ -1075,7 +1288,7 @@ __global__ void __launch_bounds__(MAXW * 32, 1)
   const Tabs t = bind_tabs(smem);
   WarpWork& w = work_slots(smem, tab_bytes)[threadIdx.x >> 5];
   const int lane = threadIdx.x & 31;
-  const Team<32> tm{lane, 0, nullptr, nullptr};
+  const Team<32> tm{lane, 0, nullptr, nullptr, nullptr};
   const int nv = t.ns + 1;
   for (int guard = 0; guard < (1 << 30); ++guard) {
     unsigned cell = 0;
@@ -1324,14 +1537,14 @@ __global__ void __launch_bounds__(MAXW * 32, 1)
     if (warp < TEAM / 32) {
       // team scratch: the second work slot, unused while the team runs
       double* spare = reinterpret_cast<double*>(&ww[1]);
-      const Team<TEAM> tm{(int)threadIdx.x, 1, spare, spare + 256};
+      const Team<TEAM> tm{(int)threadIdx.x, 1, spare, spare + 256, spare + 768};
       const unsigned cell = s_hot[1 + blockIdx.x];
       const int c = tube_cell<TEAM>(t, tm, ww[0], L, cell, dt, speed_max, cnt);
       if (threadIdx.x == 0 && L.cost) L.cost[cell] = c;
     }
     __syncthreads();
   }
-  const Team<32> tw{lane, 0, nullptr, nullptr};
+  const Team<32> tw{lane, 0, nullptr, nullptr, nullptr};
   WarpWork& w = ww[warp];
   for (int guard = 0; guard < (1 << 30); ++guard) {
     unsigned cell = 0;
@@ -1385,16 +1598,26 @@ int chem_init(ChemState& s, const edyn_mech& m, const ThermoTable& tb, cudaStrea
   (void)tb;
   const int ns = m.nspec, nr = m.nreac;
   if (ns + 1 > 54 + 2 || ns > NSMAX - 8 || nr > 352) return (int)cudaErrorInvalidValue;
-  // reaction order: group by kind so a 32-wide round rarely diverges
-  std::vector<int> order(nr);
-  for (int i = 0; i < nr; ++i) order[i] = i;
+  // reaction order: the fall-off reactions fill the rounds of 32 from round
+  // fr0 = 3 on (a four-warp team gives those rounds to one warp); the others
+  // are grouped by kind so that a 32-wide round rarely diverges: third-body,
+  // Arrhenius with an exponential, constant.
+  std::vector<int> fall, rest;
+  for (int i = 0; i < nr; ++i) (m.tb[i] == EDYN_TB_FALLOFF ? fall : rest).push_back(i);
   auto kind = [&](int i) {
-    if (m.tb[i] == EDYN_TB_FALLOFF) return 0;
     if (m.tb[i] == EDYN_TB_M) return 1;
     const bool ex = !(m.beta[i] == 0.0 && m.E_R[i] == 0.0);
     return ex ? 2 : 3;
   };
-  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return kind(a) < kind(b); });
+  std::stable_sort(rest.begin(), rest.end(), [&](int a, int b) { return kind(a) < kind(b); });
+  const int nfr = ((int)fall.size() + 31) / 32;
+  const int fr0 = nfr > 0 ? std::min(3, (int)rest.size() / 32) : 0;
+  std::vector<int> order;
+  size_t ri = 0;
+  while ((int)order.size() < fr0 * 32) order.push_back(rest[ri++]);
+  for (int i : fall) order.push_back(i);
+  while ((int)order.size() < (fr0 + nfr) * 32 && ri < rest.size()) order.push_back(rest[ri++]);
+  while (ri < rest.size()) order.push_back(rest[ri++]);
   const int nrp = (nr + 31) / 32 * 32;
   std::vector<double> A(nrp, 0.0), B(nrp, 0.0), E(nrp, 0.0), lnA(nrp, -700.0);
   std::vector<unsigned> w0(nrp, 0xffffffu), w1(nrp, 0x08ffffffu), w2(nrp, 0u), w3(nrp, 0u), w4(nrp, 0u), w5(nrp, 0u);
@@ -1499,7 +1722,7 @@ int chem_init(ChemState& s, const edyn_mech& m, const ThermoTable& tb, cudaStrea
     if (b == e) pieces.push_back({k, b, b});
   }
   const int npc = (int)pieces.size();
-  if (npc > 100) return (int)cudaErrorInvalidValue;
+  if (npc > 100 || nsp > 64) return (int)cudaErrorInvalidValue;
   std::vector<int> idx(npc);
   for (int p = 0; p < npc; ++p) idx[p] = p;
   std::sort(idx.begin(), idx.end(), [&](int a, int b) {
@@ -1578,6 +1801,8 @@ int chem_init(ChemState& s, const edyn_mech& m, const ThermoTable& tb, cudaStrea
   h.ns = ns;
   h.nr = nr;
   h.nrp = nrp;
+  h.fr0 = fr0;
+  h.nfr = nfr;
   h.nsp = nsp;
   h.npc = npc;
   h.ntbl = (int)tb_sp.size();
@@ -1617,6 +1842,11 @@ int chem_init(ChemState& s, const edyn_mech& m, const ThermoTable& tb, cudaStrea
   put2(h.o_ch, ch);
   put2(h.o_cp, cpt);
   put2(h.o_nu, ent_nu);
+  {
+    double e2[64];
+    for (int j = 0; j < 64; ++j) e2[j] = (double)std::exp2((long double)j / 64.0L);
+    h.o_e2 = bl.put(e2, sizeof(e2));
+  }
   bl.put(nullptr, 16);
   size_t tot = (bl.b.size() + 255) / 256 * 256;
   bl.b.resize(tot, 0);

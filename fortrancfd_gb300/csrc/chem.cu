@@ -1911,6 +1911,29 @@ cudaError_t chem_launch_tube(ChemState& s, const ChemLaunch& L, cudaStream_t st)
   return cudaGetLastError();
 }
 
+namespace {
+// texp against CUDA's exp on the same arguments: the largest difference in
+// units in the last place of CUDA's result (device-wide max via the bit
+// pattern of a non-negative double).
+__global__ void k_check_exp(const char* g_tab, int n, const double* x, unsigned long long* maxulp) {
+  __shared__ double e2[64];
+  const TabHdr* h = (const TabHdr*)g_tab;
+  if (threadIdx.x < 64) e2[threadIdx.x] = ((const double*)(g_tab + h->o_e2))[threadIdx.x];
+  __syncthreads();
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double a = exp(x[i]), b = texp(x[i], e2);
+  const double ulp = __longlong_as_double(__double_as_longlong(fabs(a)) + 1) - fabs(a);
+  const double u = fabs(a - b) / ulp;
+  atomicMax(maxulp, (unsigned long long)__double_as_longlong(u));
+}
+}  // namespace
+
+cudaError_t chem_check_exp(ChemState& s, int n, const double* x_d, unsigned long long* maxulp_d, cudaStream_t st) {
+  k_check_exp<<<(n + 255) / 256, 256, 0, st>>>((const char*)s.d_tables, n, x_d, maxulp_d);
+  return cudaGetLastError();
+}
+
 cudaError_t chem_read_counters(ChemState& s, ChemCounters* out, cudaStream_t st) {
   cudaError_t e = cudaMemcpyAsync(out, s.d_count, sizeof(ChemCounters), cudaMemcpyDeviceToHost, st);
   if (e != cudaSuccess) return e;

@@ -523,6 +523,32 @@ int edyn_chem_stats(void* ctx, double* stats) {
   return EDYN_OK;
 }
 
+int edyn_chem_cost(void* ctx, int* cost, unsigned* hot) {
+  Ctx* c = (Ctx*)ctx;
+  if (!c || !c->qc) return EDYN_E_ARG;
+  if (cost) CK(cudaMemcpyAsync(cost, c->d_cost, (size_t)c->n * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  if (hot) CK(cudaMemcpyAsync(hot, c->d_hot, (HOT_MAX + 1) * sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return EDYN_OK;
+}
+
+int edyn_check_exp(void* ctx, int n, const double* x, double* max_ulp) {
+  Ctx* c = (Ctx*)ctx;
+  if (!c || !c->qc || n <= 0 || !x || !max_ulp) return EDYN_E_ARG;
+  int rc = ensure_staging(c, (size_t)n * sizeof(double) + 16);
+  if (rc) return rc;
+  double* xd = c->staging;
+  unsigned long long* md = (unsigned long long*)(c->staging + n);
+  CK(cudaMemcpyAsync(xd, x, (size_t)n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemsetAsync(md, 0, sizeof(unsigned long long), c->stream));
+  CK(chem_check_exp(c->chem, n, xd, md, c->stream));
+  unsigned long long bits = 0;
+  CK(cudaMemcpyAsync(&bits, md, sizeof(bits), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  std::memcpy(max_ulp, &bits, sizeof(double));
+  return EDYN_OK;
+}
+
 int edyn_reactors_device(void* ctx, int n, const double* rho_d, const double* dt_d, double* yiT_d, double* stats) {
   Ctx* c = (Ctx*)ctx;
   if (!c || n < 0 || (n > 0 && (!rho_d || !dt_d || !yiT_d))) return EDYN_E_ARG;

@@ -69,6 +69,8 @@ def lib() -> ctypes.CDLL:
     L.edyn_reactors_device.argtypes = [vp, i, vp, vp, vp, dp]
     L.edyn_set_stream.argtypes = [vp, vp]
     L.edyn_chem_stats.argtypes = [vp, dp]
+    L.edyn_chem_cost.argtypes = [vp, ip, ctypes.POINTER(ctypes.c_uint)]
+    L.edyn_check_exp.argtypes = [vp, i, dp, dp]
     L.edyn_last_error.argtypes = [vp, ctypes.c_char_p, i]
     L.edyn_finalize.argtypes = [vp]
     L.edyn_mech_compile.argtypes = [cp, cp, ctypes.c_char_p, i]
@@ -214,6 +216,15 @@ class Tube(_Ctx):
         keys = ("rhs", "steps", "rejects", "failed", "jac", "cells", "team_cells")
         return {k: int(v) for k, v in zip(keys, st)}
 
+    def chem_cost(self):
+        """Right-hand sides each cell took in the last chemistry launch, and
+        the cells listed for four-warp teams in the next one."""
+        cost = np.zeros(self.ncell, dtype=np.int32)
+        hot = np.zeros(65, dtype=np.uint32)
+        self._check(lib().edyn_chem_cost(self._h, cost.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                                         hot.ctypes.data_as(ctypes.POINTER(ctypes.c_uint))))
+        return cost, hot[1:1 + int(hot[0])].astype(np.int64)
+
     def download(self):
         qf = np.empty((self.ncell, self.nequ))
         qc = np.empty((self.ncell, self.nequ))
@@ -240,6 +251,14 @@ class Reactors(_Ctx):
         if rc and raise_on_fail:
             raise EdynError(rc, self.last_error())
         return {"rhs": int(st[0]), "steps": int(st[1]), "rejects": int(st[2]), "failed": int(st[3]), "status": rc}
+
+    def check_exp(self, x: np.ndarray) -> float:
+        """Largest difference, in ulp of CUDA's exp, of the chemistry's FP64
+        exponential on the arguments x (within [-700, 700])."""
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        out = ctypes.c_double()
+        self._check(lib().edyn_check_exp(self._h, len(x), _ptr(x), ctypes.byref(out)))
+        return out.value
 
     def integrate_device(self, n: int, rho_ptr: int, dt_ptr: int, yiT_ptr: int):
         st = np.zeros(4)

@@ -152,6 +152,18 @@ int edyn_reactors_device(void* ctx, int n, const double* rho_d, const double* dt
  * statistics stay inside macks, SRC/source.f90:58). */
 int edyn_chem_stats(void* ctx, double* stats);
 
+/* Per-cell cost of the last chemistry launch of a tube: cost receives ncell
+ * right-hand-side counts; hot (optional, 65 values) the cell list that gets
+ * four-warp teams in the next launch ([0] = count). No counterpart in the
+ * reference (a load-balance diagnostic of this implementation). */
+int edyn_chem_cost(void* ctx, int* cost, unsigned* hot);
+
+/* Self-check of the FP64 exponential used in the chemistry rates against
+ * CUDA's exp on n host-supplied arguments in [-700, 700]: *max_ulp receives
+ * the largest difference in units in the last place. No counterpart in the
+ * reference. */
+int edyn_check_exp(void* ctx, int n, const double* x, double* max_ulp);
+
 /* Binds the context to a caller-owned CUDA stream (cudaStream_t as void*);
  * NULL returns to the context's own stream. */
 int edyn_set_stream(void* ctx, void* stream);

@@ -91,6 +91,9 @@ def test_tube_chemistry_short_run(oracle, names):
         teams.append(g.chem_stats()["team_cells"])
     # the costliest cells of each call after the first go to four-warp teams
     assert teams[0] == 0 and min(teams[1:]) > 0, teams
+    cost, hot = g.chem_cost()
+    assert cost.max() >= 64 and len(hot) > 0
+    assert int(np.argmax(cost)) in set(hot.tolist())
     qf_o, _ = ot.get()
     qf_g, _, hrr = g.download()
     K = len(names)
@@ -99,3 +102,13 @@ def test_tube_chemistry_short_run(oracle, names):
     assert rel_err < 1e-3, rel_err
     assert abs(qf_g[:, 2].max() - qf_o[:, 2].max()) / qf_o[:, 2].max() < 1e-3
     assert np.all(np.isfinite(hrr))
+
+
+def test_table_exp_within_one_ulp():
+    """The FP64 exponential of the rate evaluation (table-driven, Tang's
+    method) against CUDA's exp: at most 1 ulp apart."""
+    r = Reactors()
+    rng = np.random.default_rng(11)
+    x = np.concatenate([rng.uniform(-700.0, 700.0, 1 << 20), rng.uniform(-0.7, 0.7, 1 << 16),
+                        rng.uniform(-60.0, 5.0, 1 << 16)])
+    assert r.check_exp(x) <= 1.0

@@ -195,6 +195,7 @@ struct Team {
   double* red;    // cross-warp scratch, 256 doubles (four-warp teams)
   double* part4;  // gather partial sums, [4][TEAM_PIECES] (four-warp teams)
   double* pre;    // temperature-only rate parts, 480 doubles (four-warp teams)
+  float* jsave;   // the Jacobian kept across steps (four-warp teams; warps rebuild it)
   __device__ __forceinline__ void sync() const {
     if constexpr (TW == 32) {
       __syncwarp();
@@ -714,11 +715,10 @@ __device__ __forceinline__ void rhs64(const Tabs& t, const Team<TW>& tm, WarpWor
 // Analytic FP32 Jacobian of the mass-action species block plus finite
 // differences in T. J (row-major, stride JS) receives d f / d y at y.
 template <int TW>
-__device__ void jacobian32(const Tabs& t, const Team<TW>& tm, WarpWork& w, const double* y, double rho_cgs) {
+__device__ void jacobian32(const Tabs& t, const Team<TW>& tm, WarpWork& w, const double* y, double rho_cgs, float* J) {
   const RTabs<float>& x = t.f;
   const int ns = t.ns, n = ns + 1;
   const int tid = tm.tid;
-  float* J = w.J;
   float* Cf = (float*)w.C;
   float* mf = (float*)w.m;
   float* mif = (float*)w.wdot;
@@ -1104,25 +1104,39 @@ __device__ __forceinline__ void gemv_solve(const Team<TW>& tm, const float* A, f
 
 struct Cell {
   double rho_cgs, dt, rtol, atol;
+  double h0;  // first step size to try (<= dt)
 };
 
 struct CellStats {
   int rhs, steps, rejects, jac;
   bool failed;
+  double hnext;  // step size the controller proposes after the window
 };
+
+constexpr float THETA_JAC = 0.1f;  // Newton contraction above which a kept Jacobian is rebuilt
+constexpr int JAC_MAX_AGE = 10;    // accepted steps a kept Jacobian serves at most
 
 // Integrates w.y0 over [0, dt] with SDIRK4. Returns the statistics.
 template <int TW>
 __device__ CellStats integrate(const Tabs& t, const Team<TW>& tm, WarpWork& w, const Cell& c) {
   const int lane = tm.tid;
   const int n = t.ns + 1;
-  CellStats st = {0, 0, 0, 0, false};
-  double tcur = 0.0, h = c.dt;
+  CellStats st = {0, 0, 0, 0, false, c.dt};
+  double tcur = 0.0, h = c.h0;
   const int max_steps = 4000;
   bool need_jac = true, need_f0 = true;
+  // A four-warp team keeps its Jacobian in a separate buffer and reuses it
+  // across steps while the Newton iterations contract fast (the iteration is
+  // inexact anyway); a warp forms the Newton matrix over its Jacobian.
+  constexpr bool keep_jac = TW > 32;
+  float* Jd = keep_jac ? tm.jsave : w.J;
+  bool jac_fresh = false;  // Jacobian evaluated at the current y0
+  int jac_age = 0;         // accepted steps since it was evaluated
+  double h_want = h;       // step size before truncation at the window end
   const double g = 0.25;
   while (tcur < c.dt) {
     if (st.steps + st.rejects >= max_steps) { st.failed = true; break; }
+    h_want = h;
     if (tcur + h > c.dt) h = c.dt - tcur;
     // f0 = f(y0) in FP64 (kept across rejections)
     if (need_f0) {
@@ -1144,13 +1158,16 @@ __device__ CellStats integrate(const Tabs& t, const Team<TW>& tm, WarpWork& w, c
           for (int i = lane; i < n; i += TW) w.y0[i] = fma(c.dt, w.dl[i], w.y0[i]);
           tm.sync();
           st.steps++;
+          st.hnext = c.dt;
           break;
         }
       }
     }
     if (need_jac) {
-      jacobian32<TW>(t, tm, w, w.y0, c.rho_cgs);
+      jacobian32<TW>(t, tm, w, w.y0, c.rho_cgs, Jd);
       st.jac++;
+      jac_fresh = true;
+      jac_age = 0;
     }
     // Newton matrix I - h g J equilibrated with the error weights,
     // Ms = D^-1 M D, D = diag(atol + rtol |y0|); unscaled, the temperature
@@ -1161,10 +1178,11 @@ __device__ CellStats integrate(const Tabs& t, const Team<TW>& tm, WarpWork& w, c
     tm.sync();
     for (int q = lane; q < n * JS; q += TW) {
       const int i = q / JS, j = q - i * JS;
-      if (j < n) w.J[q] = ((i == j ? 1.f : 0.f) - (float)(h * g) * w.J[q]) * (w.sc32[j] / w.sc32[i]);
+      if (j < n) w.J[q] = ((i == j ? 1.f : 0.f) - (float)(h * g) * Jd[q]) * (w.sc32[j] / w.sc32[i]);
     }
     tm.sync();
     bool newton_ok = gj_invert<TW>(tm, w.J, w.piv, w.col, n);
+    float theta_max = 0.f;  // largest Newton contraction of this step
     for (int s = 0; s < 5 && newton_ok; ++s) {
       for (int i = lane; i < n; i += TW) {
         double acc = w.y0[i];
@@ -1196,6 +1214,7 @@ __device__ CellStats integrate(const Tabs& t, const Team<TW>& tm, WarpWork& w, c
         // tolerance, directly or predicted from the contraction rate; one
         // non-contracting iteration (theta < 2) is tolerated
         if (nrm <= 1e-2f) conv = true;
+        if (it > 0) theta_max = fmaxf(theta_max, nrm / nrm_prev);
         if (!conv && it > 0) {
           const float th = nrm / nrm_prev;
           if (th >= 2.f || (th >= 0.99f && it >= 2)) break;
@@ -1221,7 +1240,7 @@ __device__ CellStats integrate(const Tabs& t, const Team<TW>& tm, WarpWork& w, c
     if (!newton_ok) {
       st.rejects++;
       h *= 0.25;
-      need_jac = true;
+      need_jac = !(keep_jac && jac_fresh);
       if (h < c.dt * 1e-12) { st.failed = true; break; }
       continue;
     }
@@ -1247,12 +1266,18 @@ __device__ CellStats integrate(const Tabs& t, const Team<TW>& tm, WarpWork& w, c
       tcur += h;
       st.steps++;
       need_f0 = true;
-      h = h * (double)fminf(5.f, fmaxf(0.2f, fac));
-      need_jac = true;
+      const double hprop = h * (double)fminf(5.f, fmaxf(0.2f, fac));
+      // the proposal after a step cut short by the window end is measured
+      // on the shorter step; the step size wanted before the cut stands too
+      st.hnext = (h < h_want) ? fmax(hprop, h_want) : hprop;
+      h = hprop;
+      jac_fresh = false;
+      ++jac_age;
+      need_jac = !keep_jac || theta_max > THETA_JAC || jac_age >= JAC_MAX_AGE;
     } else {
       st.rejects++;
       h = h * (double)fminf(1.f, fmaxf(0.2f, fac));
-      need_jac = true;
+      need_jac = !keep_jac;
     }
   }
   return st;
@@ -1288,7 +1313,7 @@ __global__ void __launch_bounds__(MAXW * 32, 1)
   const Tabs t = bind_tabs(smem);
   WarpWork& w = work_slots(smem, tab_bytes)[threadIdx.x >> 5];
   const int lane = threadIdx.x & 31;
-  const Team<32> tm{lane, 0, nullptr, nullptr, nullptr};
+  const Team<32> tm{lane, 0, nullptr, nullptr, nullptr, nullptr};
   const int nv = t.ns + 1;
   for (int guard = 0; guard < (1 << 30); ++guard) {
     unsigned cell = 0;
@@ -1298,7 +1323,7 @@ __global__ void __launch_bounds__(MAXW * 32, 1)
     const double* src = yiT + (size_t)cell * nv;
     for (int i = lane; i < nv; i += 32) w.y0[i] = src[i];
     __syncwarp();
-    Cell c{rho[cell] * 1e-3, dt[cell], rtol, atol};
+    Cell c{rho[cell] * 1e-3, dt[cell], rtol, atol, dt[cell]};
     CellStats s = integrate<32>(t, tm, w, c);
     double* dst = yiT + (size_t)cell * nv;
     for (int i = lane; i < nv; i += 32) dst[i] = w.y0[i];
@@ -1335,8 +1360,11 @@ __device__ int tube_cell(const Tabs& t, const Team<TW>& tm, WarpWork& w, const C
   for (int k = tid; k < ns; k += TW) w.y0[k] *= inv_s;
   if (tid == 0) w.y0[ns] = q[2 * ld];
   tm.sync();
-  Cell c{rho * 1e-3, dt, L.rtol, L.atol};
+  // start from the step size this cell's last window ended with
+  const double hl = L.hlast ? L.hlast[cell] : 0.0;
+  Cell c{rho * 1e-3, dt, L.rtol, L.atol, (hl > 0.0 && hl < dt) ? hl : dt};
   CellStats st = integrate<TW>(t, tm, w, c);
+  if (tid == 0 && L.hlast) L.hlast[cell] = st.hnext;
   if (tid == 0) {
     add_stats(cnt, st, TW > 32);
     if (st.failed) atomicOr(L.err, (unsigned)EDYN_E_CHEM);
@@ -1537,14 +1565,14 @@ __global__ void __launch_bounds__(MAXW * 32, 1)
     if (warp < TEAM / 32) {
       // team scratch: the second work slot, unused while the team runs
       double* spare = reinterpret_cast<double*>(&ww[1]);
-      const Team<TEAM> tm{(int)threadIdx.x, 1, spare, spare + 256, spare + 768};
+      const Team<TEAM> tm{(int)threadIdx.x, 1, spare, spare + 256, spare + 768, ww[2].J};
       const unsigned cell = s_hot[1 + blockIdx.x];
       const int c = tube_cell<TEAM>(t, tm, ww[0], L, cell, dt, speed_max, cnt);
       if (threadIdx.x == 0 && L.cost) L.cost[cell] = c;
     }
     __syncthreads();
   }
-  const Team<32> tw{lane, 0, nullptr, nullptr, nullptr};
+  const Team<32> tw{lane, 0, nullptr, nullptr, nullptr, nullptr};
   WarpWork& w = ww[warp];
   for (int guard = 0; guard < (1 << 30); ++guard) {
     unsigned cell = 0;

@@ -41,6 +41,7 @@ struct ChemLaunch {
   int strict_newton;
   int* cost;        // right-hand sides each cell took in the last launch (n)
   unsigned* hot;    // [0] count, [1..HOT_MAX] cells that get a team next launch
+  double* hlast;    // step size each cell's integration proposed at the end of its last window (n)
   // batch mode
   const double* rho_batch;
   const double* dt_batch;

@@ -57,6 +57,7 @@ struct Ctx {
   unsigned* d_err = nullptr;
   int* d_cost = nullptr;      // right-hand sides per cell in the last chemistry launch
   unsigned* d_hot = nullptr;  // cells that get a four-warp team in the next one
+  double* d_hlast = nullptr;  // step size each cell's integrator proposed last
   cudaGraphExec_t graph = nullptr;
   int graph_steps = 0;
   double graph_cfl = -1, graph_tend = -1;
@@ -178,6 +179,7 @@ int source_step(Ctx* c, double dt, bool dev) {
   L.err = c->d_err;
   L.cost = c->d_cost;
   L.hot = c->d_hot;
+  L.hlast = c->d_hlast;
   cudaError_t e = chem_launch_tube(c->chem, L, c->stream);
   if (e != cudaSuccess) return fail(c, EDYN_E_CUDA, "chemistry launch: %s", cudaGetErrorString(e));
   return EDYN_OK;
@@ -316,6 +318,8 @@ int edyn_init(const char* chem_dir, int nspe, int nequ, int ncell, int lvir, con
   CK(cudaMalloc(&c->d_hot, (HOT_MAX + 1) * sizeof(unsigned)));
   CK(cudaMemsetAsync(c->d_cost, 0, (size_t)ncell * sizeof(int), c->stream));
   CK(cudaMemsetAsync(c->d_hot, 0, (HOT_MAX + 1) * sizeof(unsigned), c->stream));
+  CK(cudaMalloc(&c->d_hlast, (size_t)ncell * sizeof(double)));
+  CK(cudaMemsetAsync(c->d_hlast, 0, (size_t)ncell * sizeof(double), c->stream));
   int rc = fluid_upload_tables(c->tb, c->stream);
   if (rc == -1) return fail(c, EDYN_E_MECH, "a different mechanism is already loaded in this process");
   if (rc) return fail(c, EDYN_E_CUDA, "constant tables: %s", cudaGetErrorString((cudaError_t)rc));
@@ -630,6 +634,7 @@ int edyn_finalize(void* ctx) {
   cudaFree(c->d_err);
   cudaFree(c->d_cost);
   cudaFree(c->d_hot);
+  cudaFree(c->d_hlast);
   if (c->own) cudaStreamDestroy(c->own);
   delete c;
   return EDYN_OK;

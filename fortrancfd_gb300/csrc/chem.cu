@@ -43,6 +43,7 @@ constexpr int NSMAX = 64;
 constexpr int NV = 56;      // padded state vector length (54 used for GRI)
 constexpr int MAXW = 8;     // warps per CTA at most; the launch uses what shared memory allows
 constexpr int JS = 55;      // FP32 matrix row stride (odd: conflict-free column walks)
+constexpr int AUXW = 11;    // values per third-body / fall-off reaction in the aux table
 
 // SDIRK4 (Hairer & Wanner, Solving ODEs II, Table 6.5), gamma = 1/4.
 __constant__ double c_sa[5][5] = {{0.25, 0, 0, 0, 0},
@@ -68,7 +69,7 @@ struct TabHdr {
   int o_ent;                  // uint[nent]: scheduled reaction index
   // real tables: [0] FP64 offset, [1] FP32 offset
   int o_A[2], o_lnA[2], o_B[2], o_E[2];  // [nrp]
-  int o_aux[2];                // [nsp*9]: lowA lowB lowE troe_a T3 T1 T2 ifop ln(lowA)
+  int o_aux[2];                // [nsp*AUXW]: lowA lowB lowE troe_a T3 T1 T2 ifop ln(lowA) 1/T3 1/T1
   int o_tb_am1[2];             // [ntbl]
   int o_W[2], o_invW[2], o_tmid[2], o_hf[2];  // [NSMAX]
   int o_cs[2];                 // [2][7][NSMAX] S/R - H/RT coefficients
@@ -295,6 +296,29 @@ __device__ __forceinline__ double texp_r(double x, const double* e2) {
 __device__ __forceinline__ double texp(double x, const double* e2) {
   return texp_r(fmin(fmax(x, -708.0), 709.7), e2);
 }
+// texp for arguments of magnitude below 1e13 (Arrhenius, fall-off): the
+// range is clamped on the integer pipe instead of by two FP64 min/max
+// (206 cycles each on GB300); beyond [-708, 709.7] it returns the
+// bound's value, exp(-708) standing in for anything smaller.
+__device__ __forceinline__ double texp_a(double x, const double* e2) {
+  const double magic = 6755399441055744.0;
+  const double k64 = 92.33248261689366;
+  const double l1 = 0.010830424695086549;
+  const double l2 = 1.162596423439437e-12;
+  const double tk = fma(x, k64, magic);
+  const double kd = tk - magic;
+  double r = fma(-kd, l1, x);
+  r = fma(-kd, l2, r);
+  double s = fma(r, 1.0 / 120.0, 1.0 / 24.0);
+  s = fma(s, r, 1.0 / 6.0);
+  s = fma(s, r, 0.5);
+  const double p = fma(r * r, s, r);
+  // 64 m + j, kept where 2^m (1 + p) 2^(j/64) stays a normal number
+  const int ki = min(max(__double2loint(tk), -65344), 65471);
+  const double tj = e2[ki & 63];
+  const double v = fma(tj, p, tj);
+  return __hiloint2double(__double2hiint(v) + ((ki >> 6) << 20), __double2loint(v));
+}
 
 // exp in the rate evaluation: the table method in FP64, the SFU in FP32
 template <class R>
@@ -323,7 +347,7 @@ __device__ __forceinline__ R arrhenius(const Tabs& t, int i, unsigned fl, R logT
   const RTabs<R>& x = t.r<R>();
   if constexpr (sizeof(R) == sizeof(double)) {
     R kf = x.A[i];
-    if (fl & F_EXP) kf = kf * ex_t<R>(x.B[i] * logT - x.E[i] * invT, t);
+    if (fl & F_EXP) kf = kf * texp_a(x.B[i] * logT - x.E[i] * invT, t.e2);
     return kf;
   } else {
     return Math<R>::ex(x.lnA[i] + x.B[i] * logT - x.E[i] * invT);
@@ -354,11 +378,22 @@ __device__ __forceinline__ R inv_kc(unsigned w0, unsigned w1, unsigned w2, R pfa
     }
   }
   const int dnu = (int)(w1 >> 24) - 8;
-  R ikc = M::ldx(mant, ex2);
-  if (dnu == 1) ikc = ikc * ipfac;
-  else if (dnu == -1) ikc = ikc * pfac;
-  else if (dnu != 0) ikc = ikc * pow(pfac, (R)(-dnu));
-  return fmin(ikc, M::big());  // kr = kf / max(Kc, SMALL)
+  R ikc;
+  if constexpr (sizeof(R) == sizeof(double)) {
+    // mant (a product of at most six factors in [0.7, 1.42]) times 2^ex2
+    // from its exponent bits. From 2^900 on, the result with up to three
+    // factors ipfac <= 7e5 could pass the cap kr = kf / max(Kc, SMALL), and
+    // the cap stands for it; 2^-1000 and below are zero.
+    if (ex2 >= 900) return M::big();
+    ikc = (ex2 <= -1000) ? 0.0 : mant * __hiloint2double((ex2 + 1023) << 20, 0);
+  } else {
+    ikc = M::ldx(mant, ex2);
+  }
+  // pfac^(-dnu); |dnu| <= 3 for three-slot reactions
+  const R pm = dnu > 0 ? ipfac : pfac;
+  for (int q = dnu > 0 ? dnu : -dnu; q > 0; --q) ikc = ikc * pm;
+  if constexpr (sizeof(R) != sizeof(double)) ikc = fmin(ikc, M::big());
+  return ikc;
 }
 
 // third-body concentration: a named collider (fall-off "(+X)") or the mixture
@@ -377,7 +412,8 @@ __device__ __forceinline__ R collider(const Tabs& t, unsigned fl, int aux, R cto
 template <class R>
 __device__ __forceinline__ R troe_fclog(const Tabs& t, const R* fp, int ifop, R T, R invT) {
   using M = Math<R>;
-  R fcent = (1 - fp[3]) * ex_t<R>(-T / fp[4], t) + fp[3] * ex_t<R>(-T / fp[5], t);
+  // -T/T*** and -T/T* with reciprocals precomputed on the host
+  R fcent = (1 - fp[3]) * ex_t<R>(-T * fp[9], t) + fp[3] * ex_t<R>(-T * fp[10], t);
   if (ifop == 4) fcent += ex_t<R>(-fp[6] * invT, t);
   return M::l10(fmax(fcent, M::small()));
 }
@@ -394,7 +430,8 @@ __device__ __forceinline__ R falloff_pcor(const Tabs& t, R pr, int ifop, R fclog
     const R cprlog = prlog - ((R)(double)0.4f + (R)(double)0.67f * fclog);
     const R q = cprlog / (xn - (R)(double)0.14f * cprlog);
     const R flog = fclog / (1 + q * q);
-    pcor = ex_t<R>((R)2.302585092994045684 * flog, t) * pcor;  // 10^flog
+    if constexpr (sizeof(R) == sizeof(double)) pcor = texp_a(2.302585092994045684 * flog, t.e2) * pcor;  // 10^flog
+    else pcor = Math<R>::ex((R)2.302585092994045684 * flog) * pcor;
   }
   return pcor;
 }
@@ -438,8 +475,8 @@ __device__ __forceinline__ RxnEval<R> eval_rxn(const Tabs& t, int i, R logT, R i
     const R cm = collider<R>(t, fl, aux, ctot, C);
     o.cm = cm;
     if (fl & F_FALL) {
-      const R* fp = x.aux + aux * 9;
-      const R k0 = (sizeof(R) == sizeof(double)) ? fp[0] * ex_t<R>(fp[1] * logT - fp[2] * invT, t)
+      const R* fp = x.aux + aux * AUXW;
+      const R k0 = (sizeof(R) == sizeof(double)) ? fp[0] * texp_a(fp[1] * logT - fp[2] * invT, t.e2)
                                                  : Math<R>::ex(fp[8] + fp[1] * logT - fp[2] * invT);
       const R pr = k0 * cm / kf;
       const int ifop = (int)fp[7];
@@ -479,7 +516,7 @@ __device__ __forceinline__ double rop_pre(const Tabs& t, int i, double kf, const
     const double cm = collider<double>(t, fl, aux, ctot, C);
     if (fl & F_FALL) {
       const double pr = k0a[aux] * cm / kf;
-      const double pcor = falloff_pcor<double>(t, pr, (int)t.d.aux[aux * 9 + 7], fcl[aux]);
+      const double pcor = falloff_pcor<double>(t, pr, (int)t.d.aux[aux * AUXW + 7], fcl[aux]);
       kf *= pcor;
       kr *= pcor;
     } else {
@@ -628,49 +665,71 @@ __device__ void rhs64_team(const Tabs& t, const Team<TEAM>& tm, WarpWork& w, con
   const double invT = 1.0 / T;
   const int fr0 = t.h->fr0, nfr = t.h->nfr;
   const int nround = t.nrp >> 5;
+  // Non-fall-off rounds e = 0..nE-1 sit at round re(e); phase 1 gives their
+  // Arrhenius constants to warps 0 (e < 1), 1 (e < 3), 2 (e < 5) and 3 (the
+  // rest), after each warp's own part: the species pass (warps 0-1), log10
+  // Fcent of the fall-off reactions (warp 2), and k_inf / k0 of every slot
+  // of the fall-off rounds (warp 3).
+  const int nE = nround - nfr;
+  auto re = [&](int e) { return (nfr > 0 && e >= fr0) ? e + nfr : e; };
+  auto prep_round = [&](int rr) {
+    const int i = rr * 32 + lane;
+    if (i < t.nr) kfe[i] = arrhenius<double>(t, i, t.w0[i] >> 24, logT, invT);
+  };
   double csum = 0.0;
+  int e0 = 0, e1 = 0;
   if (wq < 2) {
     for (int k = tid; k < ns; k += 64)
       csum += species_one<double>(t, k, y, rho, T, logT, invT, w.C, w.m, w.wdot, w.en, w.uR, w.cvm);
+    e0 = wq == 0 ? 0 : 1;
+    e1 = wq == 0 ? 1 : 3;
   } else if (wq == 2) {
     for (int r = 0; r < nfr; ++r) {
       const int i = (fr0 + r) * 32 + lane;
+      if (i < t.nr && ((t.w0[i] >> 24) & F_FALL)) {
+        const int aux = (int)(t.w2[i] >> 24);
+        const double* fp = x.aux + aux * AUXW;
+        const int ifop = (int)fp[7];
+        fcl[aux] = (ifop > 1) ? troe_fclog<double>(t, fp, ifop, T, invT) : 0.0;
+      }
+    }
+    e0 = 3;
+    e1 = 5;
+  } else {
+    for (int r = 0; r < nfr; ++r) {
+      const int i = (fr0 + r) * 32 + lane;
       if (i < t.nr) {
         const unsigned fl = t.w0[i] >> 24;
+        kfe[i] = arrhenius<double>(t, i, fl, logT, invT);
         if (fl & F_FALL) {
           const int aux = (int)(t.w2[i] >> 24);
-          const double* fp = x.aux + aux * 9;
-          const int ifop = (int)fp[7];
-          kfe[i] = arrhenius<double>(t, i, fl, logT, invT);
-          k0a[aux] = fp[0] * texp(fp[1] * logT - fp[2] * invT, t.e2);
-          fcl[aux] = (ifop > 1) ? troe_fclog<double>(t, fp, ifop, T, invT) : 0.0;
+          const double* fp = x.aux + aux * AUXW;
+          k0a[aux] = fp[0] * texp_a(fp[1] * logT - fp[2] * invT, t.e2);
         }
       }
     }
-  } else {
-    for (int r = 0; r < nround; ++r) {
-      const int i = r * 32 + lane;
-      if (i < t.nr) {
-        const unsigned fl = t.w0[i] >> 24;
-        if (!(fl & F_FALL)) kfe[i] = arrhenius<double>(t, i, fl, logT, invT);
-      }
-    }
+    e0 = 5;
+    e1 = nE;
   }
+  for (int e = min(e0, nE); e < min(e1, nE); ++e) prep_round(re(e));
   const double ctot = tm.sum(csum);  // its barriers close phase 1
   const double pfac = (PATM_CGS / RU_CGS) * invT;
   const double ipfac = T * (RU_CGS / PATM_CGS);
-  if (nfr > 0 && wq == 3) {
-    for (int r = 0; r < nfr; ++r) {
-      const int i = (fr0 + r) * 32 + lane;
-      w.rop[i] = (i < t.nr) ? rop_pre(t, i, kfe[i], k0a, fcl, pfac, ipfac, ctot, w.C, w.m, w.wdot, w.en) : 0.0;
+  // phase 2: warp 3 takes the fall-off rounds and the last other round,
+  // warps 0-2 the other rounds in turn (all four in turn without fall-off)
+  auto rate_round = [&](int rr) {
+    const int i = rr * 32 + lane;
+    w.rop[i] = (i < t.nr) ? rop_pre(t, i, kfe[i], k0a, fcl, pfac, ipfac, ctot, w.C, w.m, w.wdot, w.en) : 0.0;
+  };
+  if (nfr > 0) {
+    if (wq == 3) {
+      for (int r = 0; r < nfr; ++r) rate_round(fr0 + r);
+      if (nE > 0) rate_round(re(nE - 1));
+    } else {
+      for (int e = wq; e < nE - 1; e += 3) rate_round(re(e));
     }
   } else {
-    const int nw = nfr > 0 ? 3 : 4;
-    for (int q = wq; q < nround - nfr; q += nw) {
-      const int rr = (q >= fr0) ? q + nfr : q;
-      const int i = rr * 32 + lane;
-      w.rop[i] = (i < t.nr) ? rop_pre(t, i, kfe[i], k0a, fcl, pfac, ipfac, ctot, w.C, w.m, w.wdot, w.en) : 0.0;
-    }
+    for (int e = wq; e < nE; e += 4) rate_round(e);
   }
   tm.sync();
   // production rates: each 32-lane piece list split over the four warps,
@@ -1715,9 +1774,10 @@ int chem_init(ChemState& s, const edyn_mech& m, const ThermoTable& tb, cudaStrea
       } else {
         fl |= F_CM | F_TB;
       }
-      double a9[9] = {m.low[i][0], m.low[i][1], m.low[i][2], m.troe[i][0], m.troe[i][1], m.troe[i][2], m.troe[i][3],
-                      (double)m.ifop[i], m.low[i][0] > 0 ? std::log(m.low[i][0]) : -700.0};
-      aux.insert(aux.end(), a9, a9 + 9);
+      double a9[AUXW] = {m.low[i][0], m.low[i][1], m.low[i][2], m.troe[i][0], m.troe[i][1], m.troe[i][2], m.troe[i][3],
+                      (double)m.ifop[i], m.low[i][0] > 0 ? std::log(m.low[i][0]) : -700.0,
+                      1.0 / m.troe[i][1], 1.0 / m.troe[i][2]};
+      aux.insert(aux.end(), a9, a9 + AUXW);
       spi.push_back((int)tb_sp.size());
       spi.push_back(m.neff[i]);
       spi.push_back(m.kfal[i]);

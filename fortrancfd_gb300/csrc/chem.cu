@@ -77,6 +77,7 @@ struct TabHdr {
   int o_cp[2];                 // [2][5][NSMAX] Cp/R coefficients (a1..a5)
   int o_nu[2];                 // [nent] net stoichiometric coefficient of each entry
   int o_e2;                    // double[64]: 2^(j/64), the table of texp
+  int o_lg;                    // double[2][92]: ln(j/128), 128/j for j = 90..181, the tables of tlog
   int fr0, nfr;                // the fall-off reactions fill rounds [fr0, fr0 + nfr) of 32
 };
 
@@ -90,6 +91,7 @@ struct Tabs {
   const unsigned *w0, *w1, *w2, *w3, *w4, *w5, *ent;
   const int *spi, *tb_sp, *pc, *lane, *spc, *spp;
   const double* e2;
+  const double* lg;
   int ns, nr, nrp, npc;
   RTabs<double> d;
   RTabs<float> f;
@@ -137,6 +139,7 @@ __device__ __forceinline__ Tabs bind_tabs(const char* base) {
   t.spp = (const int*)(base + h.o_spp);
   t.ent = (const unsigned*)(base + h.o_ent);
   t.e2 = (const double*)(base + h.o_e2);
+  t.lg = (const double*)(base + h.o_lg);
   t.ns = h.ns;
   t.nr = h.nr;
   t.nrp = h.nrp;
@@ -328,6 +331,54 @@ __device__ __forceinline__ double ex_t<double>(double x, const Tabs& t) { return
 template <>
 __device__ __forceinline__ float ex_t<float>(float x, const Tabs& t) { return __expf(x); }
 
+// ln(x) in FP64 for normal x > 0, table-driven: x = 2^m f with f in
+// [sqrt(1/2), sqrt(2)), F = j/128 the grid point nearest f (j in [90, 181]),
+// r = (f - F)/F with |r| <= 0.0056; f - F is exact and 1/F comes from the
+// table. ln x = m ln2 + ln F + log1p(r), log1p from its series to r^7
+// (truncation below 2e-19). Near x = 1, F = 1 and ln x = log1p(r) without
+// cancellation; elsewhere |ln F| or |m ln2| dominates the sum. About a dozen
+// FP64 instructions against ~2,000 cycles for CUDA's log on GB300.
+__device__ __forceinline__ double tlog(double x, const double* lg) {
+  const double ln2_hi = 0.6931467056274414;   // ln 2, low 32 bits zero: m ln2_hi is exact
+  const double ln2_lo = 4.7493250390316726e-07; // ln 2 - ln2_hi
+  const int hi = __double2hiint(x), lo = __double2loint(x);
+  const int mant = hi & 0xfffff;
+  int m = ((hi >> 20) & 0x7ff) - 1023;
+  int j, fe;
+  if (mant < 0x6a09e) {  // f = 1.mant < sqrt 2
+    j = 128 + ((mant + (1 << 12)) >> 13);
+    fe = 0x3ff00000;
+  } else {               // use f/2 in [sqrt(1/2), 1)
+    j = 64 + ((mant + (1 << 13)) >> 14);
+    fe = 0x3fe00000;
+    m += 1;
+  }
+  const double f = __hiloint2double(mant | fe, lo);
+  const double r = (f - j * 0.0078125) * lg[92 + j - 90];
+  double s = fma(r, 1.0 / 7.0, -1.0 / 6.0);
+  s = fma(s, r, 0.2);
+  s = fma(s, r, -0.25);
+  s = fma(s, r, 1.0 / 3.0);
+  s = fma(s, r, -0.5);
+  const double p = fma(r * r, s, r);
+  // (double)m from its bits: 2^52 + 2^31 + m, minus the offset
+  const double md = __hiloint2double(0x43300000, m ^ 0x80000000) - 4503601774854144.0;
+  return fma(md, ln2_hi, lg[j - 90]) + fma(md, ln2_lo, p);
+}
+
+// ln and log10 in the rate evaluation: the table method in FP64, the SFU in FP32
+template <class R>
+__device__ __forceinline__ R lg_t(R x, const Tabs& t);
+template <>
+__device__ __forceinline__ double lg_t<double>(double x, const Tabs& t) { return tlog(x, t.lg); }
+template <>
+__device__ __forceinline__ float lg_t<float>(float x, const Tabs& t) { return __logf(x); }
+template <class R>
+__device__ __forceinline__ R l10_t(R x, const Tabs& t) {
+  if constexpr (sizeof(R) == sizeof(double)) return tlog(x, t.lg) * 0.43429448190325182765;
+  else return __log10f(x);
+}
+
 __device__ __forceinline__ unsigned sp_of(unsigned w, int s) { return (w >> (8 * s)) & 0xffu; }
 
 // Rate constants of one reaction (CKRATT + the third-body/fall-off part of
@@ -413,9 +464,16 @@ template <class R>
 __device__ __forceinline__ R troe_fclog(const Tabs& t, const R* fp, int ifop, R T, R invT) {
   using M = Math<R>;
   // -T/T*** and -T/T* with reciprocals precomputed on the host
-  R fcent = (1 - fp[3]) * ex_t<R>(-T * fp[9], t) + fp[3] * ex_t<R>(-T * fp[10], t);
-  if (ifop == 4) fcent += ex_t<R>(-fp[6] * invT, t);
-  return M::l10(fmax(fcent, M::small()));
+  R fcent, f3 = 0;
+  if constexpr (sizeof(R) == sizeof(double)) {
+    fcent = (1 - fp[3]) * texp_a(-T * fp[9], t.e2) + fp[3] * texp_a(-T * fp[10], t.e2);
+    if (ifop == 4) f3 = texp_a(-fp[6] * invT, t.e2);
+  } else {
+    fcent = (1 - fp[3]) * ex_t<R>(-T * fp[9], t) + fp[3] * ex_t<R>(-T * fp[10], t);
+    if (ifop == 4) f3 = ex_t<R>(-fp[6] * invT, t);
+  }
+  fcent += f3;
+  return l10_t<R>(fmax(fcent, M::small()), t);
 }
 
 // fall-off blending factor pr/(1+pr) F from the reduced pressure and, for
@@ -425,7 +483,7 @@ __device__ __forceinline__ R falloff_pcor(const Tabs& t, R pr, int ifop, R fclog
   using M = Math<R>;
   R pcor = pr / (1 + pr);
   if (ifop > 1) {
-    const R prlog = M::l10(fmax(pr, M::small()));
+    const R prlog = l10_t<R>(fmax(pr, M::small()), t);
     const R xn = (R)0.75 - (R)(double)1.27f * fclog;
     const R cprlog = prlog - ((R)(double)0.4f + (R)(double)0.67f * fclog);
     const R q = cprlog / (xn - (R)(double)0.14f * cprlog);
@@ -587,7 +645,7 @@ __device__ void rhs(const Tabs& t, const Team<TW>& tm, WarpWork& w, const R* y, 
   const RTabs<R>& x = t.r<R>();
   const int ns = t.ns;
   const R T = y[ns];
-  const R logT = Math<R>::lg(T);
+  const R logT = lg_t<R>(T, t);
   const R invT = (R)1 / T;
   const R ctot = species_pass<R, TW>(t, tm, y, rho, T, logT, invT, C, m, mi, w.en, uR, cvm);
   const R pfac = (R)(PATM_CGS / RU_CGS) * invT;
@@ -661,7 +719,7 @@ __device__ void rhs64_team(const Tabs& t, const Team<TEAM>& tm, WarpWork& w, con
   double* k0a = tm.pre + 352; // [64] low-pressure limits, by special-reaction index
   double* fcl = k0a + 64;     // [64] log10 Fcent
   const double T = y[ns];
-  const double logT = log(T);
+  const double logT = tlog(T, t.lg);
   const double invT = 1.0 / T;
   const int fr0 = t.h->fr0, nfr = t.h->nfr;
   const int nround = t.nrp >> 5;
@@ -1776,7 +1834,9 @@ int chem_init(ChemState& s, const edyn_mech& m, const ThermoTable& tb, cudaStrea
       }
       double a9[AUXW] = {m.low[i][0], m.low[i][1], m.low[i][2], m.troe[i][0], m.troe[i][1], m.troe[i][2], m.troe[i][3],
                       (double)m.ifop[i], m.low[i][0] > 0 ? std::log(m.low[i][0]) : -700.0,
-                      1.0 / m.troe[i][1], 1.0 / m.troe[i][2]};
+                      // 1/T*** and 1/T*, capped at 1e4: beyond, exp(-T/T) is below 1e-400 at
+                      // T >= 100 K, and the capped argument stays in the table exponential's range
+                      std::min(1e4, 1.0 / m.troe[i][1]), std::min(1e4, 1.0 / m.troe[i][2])};
       aux.insert(aux.end(), a9, a9 + AUXW);
       spi.push_back((int)tb_sp.size());
       spi.push_back(m.neff[i]);
@@ -1934,6 +1994,12 @@ int chem_init(ChemState& s, const edyn_mech& m, const ThermoTable& tb, cudaStrea
     double e2[64];
     for (int j = 0; j < 64; ++j) e2[j] = (double)std::exp2((long double)j / 64.0L);
     h.o_e2 = bl.put(e2, sizeof(e2));
+    double lgt[2 * 92];
+    for (int j = 90; j < 182; ++j) {
+      lgt[j - 90] = (double)std::log((long double)j / 128.0L);
+      lgt[92 + j - 90] = (double)(128.0L / (long double)j);
+    }
+    h.o_lg = bl.put(lgt, sizeof(lgt));
   }
   bl.put(nullptr, 16);
   size_t tot = (bl.b.size() + 255) / 256 * 256;
@@ -2015,7 +2081,25 @@ __global__ void k_check_exp(const char* g_tab, int n, const double* x, unsigned 
   const double u = fabs(a - b) / ulp;
   atomicMax(maxulp, (unsigned long long)__double_as_longlong(u));
 }
+// tlog against CUDA's log, as k_check_exp.
+__global__ void k_check_log(const char* g_tab, int n, const double* x, unsigned long long* maxulp) {
+  __shared__ double lg[184];
+  const TabHdr* h = (const TabHdr*)g_tab;
+  for (int q = threadIdx.x; q < 184; q += blockDim.x) lg[q] = ((const double*)(g_tab + h->o_lg))[q];
+  __syncthreads();
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double a = log(x[i]), b = tlog(x[i], lg);
+  const double ulp = __longlong_as_double(__double_as_longlong(fabs(a)) + 1) - fabs(a);
+  const double u = fabs(a - b) / ulp;
+  atomicMax(maxulp, (unsigned long long)__double_as_longlong(u));
+}
 }  // namespace
+
+cudaError_t chem_check_log(ChemState& s, int n, const double* x_d, unsigned long long* maxulp_d, cudaStream_t st) {
+  k_check_log<<<(n + 255) / 256, 256, 0, st>>>((const char*)s.d_tables, n, x_d, maxulp_d);
+  return cudaGetLastError();
+}
 
 cudaError_t chem_check_exp(ChemState& s, int n, const double* x_d, unsigned long long* maxulp_d, cudaStream_t st) {
   k_check_exp<<<(n + 255) / 256, 256, 0, st>>>((const char*)s.d_tables, n, x_d, maxulp_d);

@@ -55,6 +55,7 @@ cudaError_t chem_launch_tube(ChemState& s, const ChemLaunch& L, cudaStream_t st)
 cudaError_t chem_launch_batch(ChemState& s, const ChemLaunch& L, cudaStream_t st);
 cudaError_t chem_read_counters(ChemState& s, ChemCounters* out, cudaStream_t st);
 cudaError_t chem_check_exp(ChemState& s, int n, const double* x_d, unsigned long long* maxulp_d, cudaStream_t st);
+cudaError_t chem_check_log(ChemState& s, int n, const double* x_d, unsigned long long* maxulp_d, cudaStream_t st);
 void chem_free(ChemState& s);
 
 }  // namespace edyn

@@ -536,7 +536,8 @@ int edyn_chem_cost(void* ctx, int* cost, unsigned* hot) {
   return EDYN_OK;
 }
 
-int edyn_check_exp(void* ctx, int n, const double* x, double* max_ulp) {
+namespace {
+int check_fn(void* ctx, int n, const double* x, double* max_ulp, bool is_log) {
   Ctx* c = (Ctx*)ctx;
   if (!c || !c->qc || n <= 0 || !x || !max_ulp) return EDYN_E_ARG;
   int rc = ensure_staging(c, (size_t)n * sizeof(double) + 16);
@@ -545,13 +546,19 @@ int edyn_check_exp(void* ctx, int n, const double* x, double* max_ulp) {
   unsigned long long* md = (unsigned long long*)(c->staging + n);
   CK(cudaMemcpyAsync(xd, x, (size_t)n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
   CK(cudaMemsetAsync(md, 0, sizeof(unsigned long long), c->stream));
-  CK(chem_check_exp(c->chem, n, xd, md, c->stream));
+  if (is_log) CK(chem_check_log(c->chem, n, xd, md, c->stream));
+  else CK(chem_check_exp(c->chem, n, xd, md, c->stream));
   unsigned long long bits = 0;
   CK(cudaMemcpyAsync(&bits, md, sizeof(bits), cudaMemcpyDeviceToHost, c->stream));
   CK(cudaStreamSynchronize(c->stream));
   std::memcpy(max_ulp, &bits, sizeof(double));
   return EDYN_OK;
 }
+}  // namespace
+
+int edyn_check_exp(void* ctx, int n, const double* x, double* max_ulp) { return check_fn(ctx, n, x, max_ulp, false); }
+
+int edyn_check_log(void* ctx, int n, const double* x, double* max_ulp) { return check_fn(ctx, n, x, max_ulp, true); }
 
 int edyn_reactors_device(void* ctx, int n, const double* rho_d, const double* dt_d, double* yiT_d, double* stats) {
   Ctx* c = (Ctx*)ctx;

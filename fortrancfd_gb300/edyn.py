@@ -71,6 +71,7 @@ def lib() -> ctypes.CDLL:
     L.edyn_chem_stats.argtypes = [vp, dp]
     L.edyn_chem_cost.argtypes = [vp, ip, ctypes.POINTER(ctypes.c_uint)]
     L.edyn_check_exp.argtypes = [vp, i, dp, dp]
+    L.edyn_check_log.argtypes = [vp, i, dp, dp]
     L.edyn_last_error.argtypes = [vp, ctypes.c_char_p, i]
     L.edyn_finalize.argtypes = [vp]
     L.edyn_mech_compile.argtypes = [cp, cp, ctypes.c_char_p, i]
@@ -258,6 +259,14 @@ class Reactors(_Ctx):
         x = np.ascontiguousarray(x, dtype=np.float64)
         out = ctypes.c_double()
         self._check(lib().edyn_check_exp(self._h, len(x), _ptr(x), ctypes.byref(out)))
+        return out.value
+
+    def check_log(self, x: np.ndarray) -> float:
+        """Largest difference, in ulp of CUDA's log, of the chemistry's FP64
+        natural logarithm on the positive arguments x."""
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        out = ctypes.c_double()
+        self._check(lib().edyn_check_log(self._h, len(x), _ptr(x), ctypes.byref(out)))
         return out.value
 
     def integrate_device(self, n: int, rho_ptr: int, dt_ptr: int, yiT_ptr: int):

@@ -164,6 +164,10 @@ int edyn_chem_cost(void* ctx, int* cost, unsigned* hot);
  * reference. */
 int edyn_check_exp(void* ctx, int n, const double* x, double* max_ulp);
 
+/* The same self-check for the FP64 natural logarithm of the chemistry rates
+ * (positive normal arguments). No counterpart in the reference. */
+int edyn_check_log(void* ctx, int n, const double* x, double* max_ulp);
+
 /* Binds the context to a caller-owned CUDA stream (cudaStream_t as void*);
  * NULL returns to the context's own stream. */
 int edyn_set_stream(void* ctx, void* stream);

@@ -112,3 +112,13 @@ def test_table_exp_within_one_ulp():
     x = np.concatenate([rng.uniform(-700.0, 700.0, 1 << 20), rng.uniform(-0.7, 0.7, 1 << 16),
                         rng.uniform(-60.0, 5.0, 1 << 16)])
     assert r.check_exp(x) <= 1.0
+
+
+def test_table_log_within_two_ulp():
+    """The FP64 natural logarithm of the rate evaluation (table-driven)
+    against CUDA's log: at most 2 ulp apart, including arguments near 1."""
+    r = Reactors()
+    rng = np.random.default_rng(12)
+    x = np.concatenate([np.exp(rng.uniform(-690.0, 690.0, 1 << 20)), 1.0 + rng.uniform(-0.05, 0.05, 1 << 16),
+                        rng.uniform(100.0, 8000.0, 1 << 16)])
+    assert r.check_log(x) <= 2.0

@@ -277,7 +277,7 @@ int edyn_init(const char* chem_dir, int nspe, int nequ, int ncell, int lvir, con
     return fail(c, EDYN_E_ARG, "lvir=%d does not match the scheme (needs %d)", lvir, acu_lvir(c->acu));
   if (c->lbound < 0 || c->lbound > 1 || c->rbound < 0 || c->rbound > 1)
     return fail(c, EDYN_E_ARG, "boundary flags must be 0 or 1");
-  if (ncell < 2 * STAGE_THREADS / 8) return fail(c, EDYN_E_ARG, "ncell=%d too small (>= 16)", ncell);
+  if (ncell < 16) return fail(c, EDYN_E_ARG, "ncell=%d too small (>= 16)", ncell);
   if (!(c->dx > 0)) return fail(c, EDYN_E_ARG, "dx must be positive");
   c->ns = nspe;
   c->ne = nequ;

@@ -8,7 +8,7 @@
 namespace edyn {
 
 constexpr int GHOST = 4;          // ghost columns allocated per tube end (max lvir)
-constexpr int STAGE_THREADS = 64; // threads per stage CTA (faces; cells = threads - 1)
+constexpr int STAGE_THREADS = 128; // threads per stage CTA (two per cell position; cells = threads/2 - 2)
 
 struct ThermoTable;
 

@@ -218,8 +218,9 @@ template <int ACU, int LIM, int WFLAG, int RIEMANN>
 __global__ void __launch_bounds__(STAGE_THREADS) k_stage(StageArgs a) {
   constexpr int LV = acu_lvir(ACU);
   extern __shared__ double sm[];
-  const int NT = blockDim.x;
-  const int TC = NT - 1;
+  const int NT = blockDim.x;  // threads: two per cell position in the reconstruction
+  const int P = NT / 2;       // positions: the cells c0-1..c0+TC, or the faces c0..c0+TC
+  const int TC = P - 2;
   const int tid = threadIdx.x;
   // Tile of this CTA: cells [c0, c1), TC wide. The right-end ghost cells are
   // built from the conserved state of the last LV cells, which the stage
@@ -234,12 +235,16 @@ __global__ void __launch_bounds__(STAGE_THREADS) k_stage(StageArgs a) {
     if ((int)blockIdx.x == nb - 1) c0 = a.n - LV;
     if ((int)blockIdx.x == nb - 2) c1 = a.n - LV;
   }
-  const int Wd = TC + 2 * LV;  // stencil window [c0 - LV, c0 + TC + LV)
+  // stencil window [c0 - LV, c0 + TC + LV): the cells c0-1..c1 whose face
+  // values the tile needs, each with its reconstruction radius LV - 1
+  const int Wd = TC + 2 * LV;
   const ThermoTable& tb = c_thermo;
   const int ns = a.ns, ne = ns + 3;
-  double* s_q = sm;                 // [ne][Wd]
-  double* s_y = s_q + ne * Wd;      // [2*ns][NT] raw Y_L, Y_R per face; reused
-  double* s_f = s_y + 2 * ns * NT;  // [ne][NT] face fluxes
+  double* s_q = sm;             // [ne][Wd] primitive window
+  double* s_l = s_q + ne * Wd;  // [ne][P] value at the right face of cell c0-1+p (left state of face c0+p);
+                                //         then the flux of face c0+p
+  double* s_r = s_l + ne * P;   // [ne][P] value at the left face of cell c0-1+p (right state of face c0-1+p);
+                                //         then per-thread species scratch
 
   // Device-driven time loop: k_step_begin decided whether this step runs
   // and published its dt.
@@ -259,27 +264,42 @@ __global__ void __launch_bounds__(STAGE_THREADS) k_stage(StageArgs a) {
   // left ghost -1-t, thread LV <= t < 2 LV the right ghost n + t - LV.
   if (tid < 2 * LV) {
     const int g = (tid < LV) ? -1 - tid : a.n + (tid - LV);
-    if (g >= c0 - LV && g < c1 + LV) ghost_cell(a, g, s_q + (g - (c0 - LV)), Wd, s_y + tid, NT);
+    if (g >= c0 - LV && g < c1 + LV) ghost_cell(a, g, s_q + (g - (c0 - LV)), Wd, s_r + tid, P);
   }
   __syncthreads();
 
-  // 2. one face per thread: face f between cells f-1 and f
-  const int f = c0 + tid;
-  if (f <= c1) {
-    const int c = tid + LV - 1;  // window index of cell f-1
+  // 2. face values of the cells c0-1..c1: position p = tid % P, rows split
+  //    between the two halves of the CTA
+  {
+    const int p = tid % P, half = tid / P;
+    if (c0 - 1 + p <= c1) {
+      const int c = p + LV - 1;  // window index of cell c0-1+p
+      for (int v = half; v < ne; v += 2) {
+        double vr, vl;
+        recon_cell<ACU, LIM, WFLAG>(s_q + v * Wd, c, vr, vl);
+        s_l[v * P + p] = vr;
+        s_r[v * P + p] = vl;
+      }
+    }
+  }
+  __syncthreads();
+
+  // 3. one face per thread: face c0+f between cells c0-1+f and c0+f
+  const int f = tid;
+  if (f < P && c0 + f <= c1) {
     FaceState L, R;
-    recon<ACU, LIM, WFLAG>(s_q + 0 * Wd, c, L.rho, R.rho);
-    recon<ACU, LIM, WFLAG>(s_q + 1 * Wd, c, L.u, R.u);
-    recon<ACU, LIM, WFLAG>(s_q + 2 * Wd, c, L.T, R.T);
+    L.rho = s_l[0 * P + f];
+    L.u = s_l[1 * P + f];
+    L.T = s_l[2 * P + f];
+    R.rho = s_r[0 * P + f + 1];
+    R.u = s_r[1 * P + f + 1];
+    R.T = s_r[2 * P + f + 1];
     Premix pl, pr;
     pl.zero(t_interval(tb, L.T));
     pr.zero(t_interval(tb, R.T));
     double syl = 0.0, syr = 0.0, szl = 0.0, szr = 0.0;
     for (int k = 0; k < ns; ++k) {
-      double yl, yr;
-      recon<ACU, LIM, WFLAG>(s_q + (3 + k) * Wd, c, yl, yr);
-      s_y[(2 * k) * NT + tid] = yl;
-      s_y[(2 * k + 1) * NT + tid] = yr;
+      const double yl = s_l[(3 + k) * P + f], yr = s_r[(3 + k) * P + f + 1];
       const double pl_ = clip0(yl), pr_ = clip0(yr);
       syl += pl_;
       syr += pr_;
@@ -296,15 +316,15 @@ __global__ void __launch_bounds__(STAGE_THREADS) k_stage(StageArgs a) {
     const double fl0 = ml, fr0 = mr;
     const double fl1 = ml * L.u + L.p, fr1 = mr * R.u + R.p;
     const double fl2 = (L.E + L.p) * L.u, fr2 = (R.E + R.p) * R.u;
-    double* F = s_f + tid;
+    double* F = s_l + f;
     // species row k: flux = aL * YL + bL * max(YL,0) + aR * YR + bR * max(YR,0)
     double aL = 0.0, bL = 0.0, aR = 0.0, bR = 0.0;
     if (RIEMANN == 0) {  // LxF, SRC/flux.f90:287-294
       const double lamL = fabs(L.u) + L.a, lamR = fabs(R.u) + R.a;
       const double alpha = fmax(lamL, lamR);
       F[0] = 0.5 * (fl0 + fr0 - alpha * (R.rho - L.rho));
-      F[NT] = 0.5 * (fl1 + fr1 - alpha * (mr - ml));
-      F[2 * NT] = 0.5 * (fl2 + fr2 - alpha * (R.E - L.E));
+      F[P] = 0.5 * (fl1 + fr1 - alpha * (mr - ml));
+      F[2 * P] = 0.5 * (fl2 + fr2 - alpha * (R.E - L.E));
       aL = 0.5 * ml;
       aR = 0.5 * mr;
       bR = -0.5 * alpha * R.rho * R.inv_SY;
@@ -318,72 +338,74 @@ __global__ void __launch_bounds__(STAGE_THREADS) k_stage(StageArgs a) {
       const double sR = fmax(R.u + R.a, u_roe + a_roe);
       if (RIEMANN == 1) {  // HLL, SRC/flux.f90:296-315
         if (0.0 <= sL) {
-          F[0] = fl0; F[NT] = fl1; F[2 * NT] = fl2;
+          F[0] = fl0; F[P] = fl1; F[2 * P] = fl2;
           aL = ml;
         } else if (0.0 <= sR) {
           const double inv = 1.0 / (sR - sL), ss = sL * sR;
           F[0] = (sR * fl0 - sL * fr0 + ss * (R.rho - L.rho)) * inv;
-          F[NT] = (sR * fl1 - sL * fr1 + ss * (mr - ml)) * inv;
-          F[2 * NT] = (sR * fl2 - sL * fr2 + ss * (R.E - L.E)) * inv;
+          F[P] = (sR * fl1 - sL * fr1 + ss * (mr - ml)) * inv;
+          F[2 * P] = (sR * fl2 - sL * fr2 + ss * (R.E - L.E)) * inv;
           aL = sR * ml * inv;
           aR = -sL * mr * inv;
           bR = ss * R.rho * R.inv_SY * inv;
           bL = -ss * L.rho * L.inv_SY * inv;
         } else {
-          F[0] = fr0; F[NT] = fr1; F[2 * NT] = fr2;
+          F[0] = fr0; F[P] = fr1; F[2 * P] = fr2;
           aR = mr;
         }
       } else {  // HLLC, SRC/flux.f90:317-354
         const double sM = (L.p - R.p + mr * (sR - R.u) - ml * (sL - L.u)) /
                           (R.rho * (sR - R.u) - L.rho * (sL - L.u));
         if (0.0 <= sL) {
-          F[0] = fl0; F[NT] = fl1; F[2 * NT] = fl2;
+          F[0] = fl0; F[P] = fl1; F[2 * P] = fl2;
           aL = ml;
         } else if (0.0 <= sM) {
           const double fac = L.rho * (sL - L.u) / (sL - sM);
           const double ve = L.E / L.rho + (sM - L.u) * (sM + L.p / (L.rho * (sL - L.u)));
           F[0] = fl0 + sL * (fac - L.rho);
-          F[NT] = fl1 + sL * (fac * sM - ml);
-          F[2 * NT] = fl2 + sL * (fac * ve - L.E);
+          F[P] = fl1 + sL * (fac * sM - ml);
+          F[2 * P] = fl2 + sL * (fac * ve - L.E);
           aL = ml;
           bL = sL * (fac - L.rho) * L.inv_SY;
         } else if (0.0 <= sR) {
           const double fac = R.rho * (sR - R.u) / (sR - sM);
           const double ve = R.E / R.rho + (sM - R.u) * (sM + R.p / (R.rho * (sR - R.u)));
           F[0] = fr0 + sR * (fac - R.rho);
-          F[NT] = fr1 + sR * (fac * sM - mr);
-          F[2 * NT] = fr2 + sR * (fac * ve - R.E);
+          F[P] = fr1 + sR * (fac * sM - mr);
+          F[2 * P] = fr2 + sR * (fac * ve - R.E);
           aR = mr;
           bR = sR * (fac - R.rho) * R.inv_SY;
         } else {
-          F[0] = fr0; F[NT] = fr1; F[2 * NT] = fr2;
+          F[0] = fr0; F[P] = fr1; F[2 * P] = fr2;
           aR = mr;
         }
       }
     }
+    // species row k: flux = aL * YL + bL * max(YL,0) + aR * YR + bR * max(YR,0);
+    // the flux replaces YL, which no other thread reads
     for (int k = 0; k < ns; ++k) {
-      const double yl = s_y[(2 * k) * NT + tid], yr = s_y[(2 * k + 1) * NT + tid];
+      const double yl = s_l[(3 + k) * P + f], yr = s_r[(3 + k) * P + f + 1];
       double v = aL * yl;
       v = fma(bL, clip0(yl), v);
       v = fma(aR, yr, v);
       v = fma(bR, clip0(yr), v);
-      F[(3 + k) * NT] = v;
+      F[(3 + k) * P] = v;
     }
   }
   __syncthreads();
 
-  // 3. one cell per thread: conservative update + QcToqf
+  // 4. one cell per thread: conservative update + QcToqf
   const int i = c0 + tid;
   double speed = 0.0;
-  if (i < c1) {
+  if (tid < P && i < c1) {
     const double c = dt / a.dx;
     const size_t ld = (size_t)a.ld;
     double* Q = a.qc + i + GHOST;
     double* Q0 = a.q0 + i + GHOST;
-    double* ys = s_y + tid;  // strided by NT
+    double* ys = s_r + tid;  // strided by P
     double q[3];
     for (int v = 0; v < ne; ++v) {
-      const double dF = s_f[v * NT + tid + 1] - s_f[v * NT + tid];
+      const double dF = s_l[v * P + tid + 1] - s_l[v * P + tid];
       const double qv = Q[v * ld];
       double qn;
       if (a.kind == 0) {  // Euler or first TVDRK3 stage: Q0 + (0 - c dF)
@@ -393,16 +415,16 @@ __global__ void __launch_bounds__(STAGE_THREADS) k_stage(StageArgs a) {
         qn = fma(a.h1, Q0[v * ld], a.h2 * (qv - c * dF));
       }
       Q[v * ld] = qn;
-      if (v < 3) q[v] = qn; else ys[(v - 3) * NT] = qn;
+      if (v < 3) q[v] = qn; else ys[(v - 3) * P] = qn;
     }
     int iters;
     const double Tg = s_q[2 * Wd + tid + LV];
-    CellEOS e = qc_to_qf_cell(q[0], q[1], q[2], ys, NT, Tg, a.strict_newton != 0, iters);
+    CellEOS e = qc_to_qf_cell(q[0], q[1], q[2], ys, P, Tg, a.strict_newton != 0, iters);
     double* out = a.qf_out + i + GHOST;
     out[0] = q[0];
     out[ld] = e.u;
     out[2 * ld] = e.T;
-    for (int k = 0; k < ns; ++k) out[(3 + k) * ld] = ys[k * NT];
+    for (int k = 0; k < ns; ++k) out[(3 + k) * ld] = ys[k * P];
     if (a.cvel_out) speed = cell_speed(e.u, e.T, e.Sz, e.cpR);
   }
   if (a.cvel_out) {
@@ -584,7 +606,8 @@ int fluid_upload_tables(const ThermoTable& tb, cudaStream_t s) {
 size_t stage_smem_bytes(int acu, int ns, int nt) {
   const int lv = acu_lvir(acu);
   const int ne = ns + 3;
-  return sizeof(double) * ((size_t)ne * (nt - 1 + 2 * lv) + (size_t)2 * ns * nt + (size_t)ne * nt);
+  const int p = nt / 2, tc = p - 2;
+  return sizeof(double) * ((size_t)ne * (tc + 2 * lv) + (size_t)2 * ne * p);
 }
 
 template <int ACU, int LIM, int WF, int RM>
@@ -593,7 +616,7 @@ static cudaError_t launch_t(const StageArgs& a, int nt, cudaStream_t s) {
   auto kern = k_stage<ACU, LIM, WF, RM>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  const int tc = nt - 1;
+  const int tc = nt / 2 - 2;
   const int grid = (a.n + tc - 1) / tc;
   kern<<<grid, nt, smem, s>>>(a);
   return cudaGetLastError();

@@ -559,39 +559,103 @@ __device__ __forceinline__ RxnEval<R> eval_rxn(const Tabs& t, int i, R logT, R i
   return o;
 }
 
+// Net rate of progress in FP64 from the effective forward constant kfe (kf
+// times the collider or fall-off factor) and the species factors of the FP64
+// species pass, a_k = m_k pfac and b_k = C_k ipfac / m_k with m_k 2^en_k =
+// exp(S_k/R - H_k/RT): qf = kfe prod C_r^nu and, when reversible,
+// qr = kfe 2^ex2 prod a_r^nu prod b_p^nu, which is kf / Kc times the
+// collider factor and prod C_p^nu of CKRATT/CKRATX with the pressure power
+// and the product concentrations folded into b. From 2^900 on, 1/Kc stands
+// at the cap kr = kf / max(Kc, SMALL) as in inv_kc.
+__device__ __forceinline__ double net_rate(unsigned w0, unsigned w1, unsigned w2, bool rev, double kfe,
+                                           const double* C, const double* a, const double* b, const int* en) {
+  double qf = kfe, qr = kfe;
+  int ex2 = 0;
+#pragma unroll
+  for (int s = 0; s < 3; ++s) {
+    const unsigned kr_ = sp_of(w0, s), kp = sp_of(w1, s);
+    const int nr_ = (w2 >> (4 * s)) & 15, np = (w2 >> (12 + 4 * s)) & 15;
+    if (kr_ != 255u) {
+      const double c = C[kr_], x = a[kr_];
+      qf *= (nr_ == 1) ? c : (nr_ == 2 ? c * c : c * c * c);
+      qr *= (nr_ == 1) ? x : (nr_ == 2 ? x * x : x * x * x);
+      ex2 += nr_ * en[kr_];
+    }
+    if (kp != 255u) {
+      const double x = b[kp];
+      qr *= (np == 1) ? x : (np == 2 ? x * x : x * x * x);
+      ex2 -= np * en[kp];
+    }
+  }
+  if (!rev) return qf;
+  if (ex2 >= 900) {
+    qr = kfe * 1e300;
+#pragma unroll
+    for (int s = 0; s < 3; ++s) {
+      const unsigned kp = sp_of(w1, s);
+      const int np = (w2 >> (12 + 4 * s)) & 15;
+      if (kp != 255u) {
+        const double c = C[kp];
+        qr *= (np == 1) ? c : (np == 2 ? c * c : c * c * c);
+      }
+    }
+  } else {
+    qr = (ex2 <= -1000) ? 0.0 : qr * __hiloint2double((ex2 + 1023) << 20, 0);
+  }
+  return qf - qr;
+}
+
+// The FP64 net rate of reaction i evaluated from scratch (warp path).
+__device__ __forceinline__ double rop_d(const Tabs& t, int i, double logT, double invT, double T, double ctot,
+                                       const double* C, const double* a, const double* b, const int* en) {
+  const RTabs<double>& x = t.d;
+  const unsigned w0 = t.w0[i], w1 = t.w1[i], w2 = t.w2[i];
+  const unsigned fl = w0 >> 24;
+  double kf = arrhenius<double>(t, i, fl, logT, invT);
+  if (fl & (F_CM | F_KFAL)) {
+    const int aux = (int)(w2 >> 24);
+    const double cm = collider<double>(t, fl, aux, ctot, C);
+    if (fl & F_FALL) {
+      const double* fp = x.aux + aux * AUXW;
+      const double k0 = fp[0] * texp_a(fp[1] * logT - fp[2] * invT, t.e2);
+      const int ifop = (int)fp[7];
+      const double fclog = (ifop > 1) ? troe_fclog<double>(t, fp, ifop, T, invT) : 0.0;
+      kf *= falloff_pcor<double>(t, k0 * cm / kf, ifop, fclog);
+    } else {
+      kf *= cm;
+    }
+  }
+  return net_rate(w0, w1, w2, (fl & F_REV) != 0, kf, C, a, b, en);
+}
+
 // Net rate of progress of reaction i in FP64 from its precomputed Arrhenius
 // constant kf and, for fall-off, k0[aux] and log10 Fcent fcl[aux]: the
 // concentration-dependent rest of eval_rxn, with the same arithmetic.
 __device__ __forceinline__ double rop_pre(const Tabs& t, int i, double kf, const double* k0a, const double* fcl,
                                           double pfac, double ipfac, double ctot, const double* C, const double* m,
                                           const double* mi, const int* en) {
+  (void)pfac;
+  (void)ipfac;
   const unsigned w0 = t.w0[i], w1 = t.w1[i], w2 = t.w2[i];
   const unsigned fl = w0 >> 24;
-  double kr = 0;
-  if (fl & F_REV) kr = kf * inv_kc<double>(w0, w1, w2, pfac, ipfac, m, mi, en);
   const int aux = (int)(w2 >> 24);
   if (fl & (F_CM | F_KFAL)) {
     const double cm = collider<double>(t, fl, aux, ctot, C);
     if (fl & F_FALL) {
       const double pr = k0a[aux] * cm / kf;
-      const double pcor = falloff_pcor<double>(t, pr, (int)t.d.aux[aux * AUXW + 7], fcl[aux]);
-      kf *= pcor;
-      kr *= pcor;
+      kf *= falloff_pcor<double>(t, pr, (int)t.d.aux[aux * AUXW + 7], fcl[aux]);
     } else {
       kf *= cm;
-      kr *= cm;
     }
   }
-  double qf = kf, qr = kr;
-  mass_action<double>(w0, w1, w2, C, qf, qr);
-  return qf - qr;
+  return net_rate(w0, w1, w2, (fl & F_REV) != 0, kf, C, m, mi, en);
 }
 
 // Thermodynamics of species k: its concentration (returned), scaled
 // exp(S/R - H/RT) and its reciprocal, u_k/R and cv_k/(R W_k).
 template <class R>
-__device__ __forceinline__ R species_one(const Tabs& t, int k, const R* y, R rho, R T, R logT, R invT, R* C, R* m,
-                                         R* mi, int* en, R* uR, R* cvm) {
+__device__ __forceinline__ R species_one(const Tabs& t, int k, const R* y, R rho, R T, R logT, R invT, R pfac,
+                                         R ipfac, R* C, R* m, R* mi, int* en, R* uR, R* cvm) {
   using M = Math<R>;
   const RTabs<R>& x = t.r<R>();
   const R c = rho * y[k] * x.invW[k];
@@ -607,8 +671,11 @@ __device__ __forceinline__ R species_one(const Tabs& t, int k, const R* y, R rho
   const R nn = M::rint_(smh * (R)1.4426950408889634);
   const R rr = fma(-nn, (R)6.93147180369123816490e-01, smh) - nn * (R)1.90821492927058770002e-10;
   if constexpr (sizeof(R) == sizeof(double)) {
-    m[k] = texp_r(rr, t.e2);
-    mi[k] = __drcp_rn(m[k]);
+    // the FP64 rates take the species factors of net_rate: a_k = m_k pfac
+    // for reactants, b_k = C_k ipfac / m_k for products
+    const double e = texp_r(rr, t.e2);
+    m[k] = e * pfac;
+    mi[k] = (c * ipfac) * __drcp_rn(e);
   } else {
     m[k] = M::ex(rr);
     mi[k] = M::ex(-rr);
@@ -632,9 +699,10 @@ __device__ __forceinline__ R species_one(const Tabs& t, int k, const R* y, R rho
 // Thermodynamic pass over species (threads over k); returns sum of C_k.
 template <class R, int TW>
 __device__ __forceinline__ R species_pass(const Tabs& t, const Team<TW>& tm, const R* y, R rho, R T, R logT, R invT,
-                                          R* C, R* m, R* mi, int* en, R* uR, R* cvm) {
+                                          R pfac, R ipfac, R* C, R* m, R* mi, int* en, R* uR, R* cvm) {
   R csum = 0;
-  for (int k = tm.tid; k < t.ns; k += TW) csum += species_one<R>(t, k, y, rho, T, logT, invT, C, m, mi, en, uR, cvm);
+  for (int k = tm.tid; k < t.ns; k += TW)
+    csum += species_one<R>(t, k, y, rho, T, logT, invT, pfac, ipfac, C, m, mi, en, uR, cvm);
   return tm.sum(csum);
 }
 
@@ -647,15 +715,19 @@ __device__ void rhs(const Tabs& t, const Team<TW>& tm, WarpWork& w, const R* y, 
   const R T = y[ns];
   const R logT = lg_t<R>(T, t);
   const R invT = (R)1 / T;
-  const R ctot = species_pass<R, TW>(t, tm, y, rho, T, logT, invT, C, m, mi, w.en, uR, cvm);
   const R pfac = (R)(PATM_CGS / RU_CGS) * invT;
   const R ipfac = T * (R)(RU_CGS / PATM_CGS);
+  const R ctot = species_pass<R, TW>(t, tm, y, rho, T, logT, invT, pfac, ipfac, C, m, mi, w.en, uR, cvm);
   tm.sync();
   for (int i = tm.tid; i < t.nrp; i += TW) {
     R r = 0;
     if (i < t.nr) {
-      RxnEval<R> e = eval_rxn<R>(t, i, logT, invT, T, pfac, ipfac, ctot, C, m, mi, w.en);
-      r = e.qf - e.qr;
+      if constexpr (sizeof(R) == sizeof(double)) {
+        r = rop_d(t, i, logT, invT, T, ctot, C, m, mi, w.en);
+      } else {
+        RxnEval<R> e = eval_rxn<R>(t, i, logT, invT, T, pfac, ipfac, ctot, C, m, mi, w.en);
+        r = e.qf - e.qr;
+      }
     }
     rop[i] = r;
   }
@@ -723,6 +795,8 @@ __device__ void rhs64_team(const Tabs& t, const Team<TEAM>& tm, WarpWork& w, con
   const double invT = 1.0 / T;
   const int fr0 = t.h->fr0, nfr = t.h->nfr;
   const int nround = t.nrp >> 5;
+  const double pfac = (PATM_CGS / RU_CGS) * invT;
+  const double ipfac = T * (RU_CGS / PATM_CGS);
   // Non-fall-off rounds e = 0..nE-1 sit at round re(e); phase 1 gives their
   // Arrhenius constants to warps 0 (e < 1), 1 (e < 3), 2 (e < 5) and 3 (the
   // rest), after each warp's own part: the species pass (warps 0-1), log10
@@ -738,7 +812,7 @@ __device__ void rhs64_team(const Tabs& t, const Team<TEAM>& tm, WarpWork& w, con
   int e0 = 0, e1 = 0;
   if (wq < 2) {
     for (int k = tid; k < ns; k += 64)
-      csum += species_one<double>(t, k, y, rho, T, logT, invT, w.C, w.m, w.wdot, w.en, w.uR, w.cvm);
+      csum += species_one<double>(t, k, y, rho, T, logT, invT, pfac, ipfac, w.C, w.m, w.wdot, w.en, w.uR, w.cvm);
     e0 = wq == 0 ? 0 : 1;
     e1 = wq == 0 ? 1 : 3;
   } else if (wq == 2) {
@@ -771,8 +845,6 @@ __device__ void rhs64_team(const Tabs& t, const Team<TEAM>& tm, WarpWork& w, con
   }
   for (int e = min(e0, nE); e < min(e1, nE); ++e) prep_round(re(e));
   const double ctot = tm.sum(csum);  // its barriers close phase 1
-  const double pfac = (PATM_CGS / RU_CGS) * invT;
-  const double ipfac = T * (RU_CGS / PATM_CGS);
   // phase 2: warp 3 takes the fall-off rounds and the last other round,
   // warps 0-2 the other rounds in turn (all four in turn without fall-off)
   auto rate_round = [&](int rr) {

@@ -1322,6 +1322,12 @@ __device__ CellStats integrate(const Tabs& t, const Team<TW>& tm, WarpWork& w, c
   bool jac_fresh = false;  // Jacobian evaluated at the current y0
   int jac_age = 0;         // accepted steps since it was evaluated
   double h_want = h;       // step size before truncation at the window end
+  // The inverted Newton matrix in w.J stays valid while h, the Jacobian and
+  // the scaling it was built with are unchanged: after a step whose Newton
+  // iterations contracted fast, a proposed growth of h by 0-20 % keeps h
+  // instead and reuses the matrix (Hairer and Wanner, Solving ODEs II, IV.8).
+  bool m_ok = false;
+  double h_m = 0.0;
   const double g = 0.25;
   while (tcur < c.dt) {
     if (st.steps + st.rejects >= max_steps) { st.failed = true; break; }
@@ -1352,6 +1358,7 @@ __device__ CellStats integrate(const Tabs& t, const Team<TW>& tm, WarpWork& w, c
         }
       }
     }
+    const bool form_m = need_jac || !m_ok || h != h_m;
     if (need_jac) {
       jacobian32<TW>(t, tm, w, w.y0, c.rho_cgs, Jd);
       st.jac++;
@@ -1363,14 +1370,19 @@ __device__ CellStats integrate(const Tabs& t, const Team<TW>& tm, WarpWork& w, c
     // row (K per unit mass fraction) wins the pivot search and the species
     // rows lose their accuracy. Inverted in place (J is rebuilt after a
     // rejection).
-    for (int i = lane; i < n; i += TW) w.sc32[i] = (float)(c.atol + c.rtol * fabs(w.y0[i]));
-    tm.sync();
-    for (int q = lane; q < n * JS; q += TW) {
-      const int i = q / JS, j = q - i * JS;
-      if (j < n) w.J[q] = ((i == j ? 1.f : 0.f) - (float)(h * g) * Jd[q]) * (w.sc32[j] / w.sc32[i]);
+    bool newton_ok = true;
+    if (form_m) {
+      for (int i = lane; i < n; i += TW) w.sc32[i] = (float)(c.atol + c.rtol * fabs(w.y0[i]));
+      tm.sync();
+      for (int q = lane; q < n * JS; q += TW) {
+        const int i = q / JS, j = q - i * JS;
+        if (j < n) w.J[q] = ((i == j ? 1.f : 0.f) - (float)(h * g) * Jd[q]) * (w.sc32[j] / w.sc32[i]);
+      }
+      tm.sync();
+      newton_ok = gj_invert<TW>(tm, w.J, w.piv, w.col, n);
+      m_ok = newton_ok;
+      h_m = h;
     }
-    tm.sync();
-    bool newton_ok = gj_invert<TW>(tm, w.J, w.piv, w.col, n);
     float theta_max = 0.f;  // largest Newton contraction of this step
     for (int s = 0; s < 5 && newton_ok; ++s) {
       for (int i = lane; i < n; i += TW) {
@@ -1428,6 +1440,7 @@ __device__ CellStats integrate(const Tabs& t, const Team<TW>& tm, WarpWork& w, c
     }
     if (!newton_ok) {
       st.rejects++;
+      m_ok = false;
       h *= 0.25;
       need_jac = !(keep_jac && jac_fresh);
       if (h < c.dt * 1e-12) { st.failed = true; break; }
@@ -1455,14 +1468,22 @@ __device__ CellStats integrate(const Tabs& t, const Team<TW>& tm, WarpWork& w, c
       tcur += h;
       st.steps++;
       need_f0 = true;
-      const double hprop = h * (double)fminf(5.f, fmaxf(0.2f, fac));
+      const float q = fminf(5.f, fmaxf(0.2f, fac));
+      const double hprop = h * (double)q;
       // the proposal after a step cut short by the window end is measured
       // on the shorter step; the step size wanted before the cut stands too
       st.hnext = (h < h_want) ? fmax(hprop, h_want) : hprop;
-      h = hprop;
       jac_fresh = false;
       ++jac_age;
-      need_jac = !keep_jac || theta_max > THETA_JAC || jac_age >= JAC_MAX_AGE;
+      const bool jac_next = !keep_jac || theta_max > THETA_JAC || jac_age >= JAC_MAX_AGE;
+      const bool hold = q >= 1.f && q <= 1.2f && theta_max <= THETA_JAC && (keep_jac ? !jac_next : true) &&
+                        h == h_want;
+      if (hold) {
+        need_jac = false;  // h and the inverted matrix stay
+      } else {
+        h = hprop;
+        need_jac = jac_next;
+      }
     } else {
       st.rejects++;
       h = h * (double)fminf(1.f, fmaxf(0.2f, fac));

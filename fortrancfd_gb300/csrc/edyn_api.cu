@@ -61,7 +61,7 @@ struct Ctx {
   cudaGraphExec_t graph = nullptr;
   int graph_steps = 0;
   double graph_cfl = -1, graph_tend = -1;
-  int stage_threads = STAGE_THREADS;
+  int stage_tc = 0;        // cells per stage tile
   ChemState chem;
   std::string err;
 };
@@ -103,6 +103,7 @@ StageArgs base_args(Ctx* c) {
   a.ld = c->ld;
   a.lvir = c->lvir;
   a.ns = c->ns;
+  a.tc = c->stage_tc;
   a.qc = c->qc;
   a.q0 = c->q0;
   a.dx = c->dx;
@@ -149,7 +150,7 @@ int fluid_step(Ctx* c, double dt, bool dev, bool last_is_fluid) {
     a.cvel_out = (dev && last && last_is_fluid) ? c->d_cvel : nullptr;
     a.time = (dev && last && last_is_fluid) ? c->d_time : nullptr;
     a.nsteps = (dev && last && last_is_fluid) ? c->d_nsteps : nullptr;
-    cudaError_t e = launch_stage(a, c->acu, c->lim, c->wflag, c->riemann, c->stage_threads, c->stream);
+    cudaError_t e = launch_stage(a, c->acu, c->lim, c->wflag, c->riemann, c->stream);
     if (e != cudaSuccess) return fail(c, EDYN_E_CUDA, "stage launch: %s", cudaGetErrorString(e));
     c->cur ^= 1;
   }
@@ -325,7 +326,29 @@ int edyn_init(const char* chem_dir, int nspe, int nequ, int ncell, int lvir, con
   if (rc) return fail(c, EDYN_E_CUDA, "constant tables: %s", cudaGetErrorString((cudaError_t)rc));
   rc = chem_init(c->chem, m, c->tb, c->stream);
   if (rc) return fail(c, EDYN_E_CUDA, "chemistry tables: %s", cudaGetErrorString((cudaError_t)rc));
+  CK(stage_tiling(c->acu, c->lim, c->wflag, c->riemann, c->ns, c->n, &c->stage_tc));
   CK(cudaStreamSynchronize(c->stream));
+  return EDYN_OK;
+}
+
+int edyn_set_stage_tile(void* ctx, int cells) {
+  Ctx* c = (Ctx*)ctx;
+  if (!c || !c->qc) return EDYN_E_ARG;
+  if (cells != 0 && (cells < STAGE_MIN_CELLS || cells > STAGE_MAX_THREADS / 2 - 2))
+    return fail(c, EDYN_E_ARG, "stage tile of %d cells outside [%d, %d] (0: automatic)", cells, STAGE_MIN_CELLS,
+                STAGE_MAX_THREADS / 2 - 2);
+  int tc = cells;
+  if (cells == 0) CK(stage_tiling(c->acu, c->lim, c->wflag, c->riemann, c->ns, c->n, &tc));
+  c->stage_tc = tc;
+  drop_graph(c);
+  return EDYN_OK;
+}
+
+int edyn_stage_tile(void* ctx, int* cells, int* threads) {
+  Ctx* c = (Ctx*)ctx;
+  if (!c || !c->qc) return EDYN_E_ARG;
+  if (cells) *cells = c->stage_tc;
+  if (threads) *threads = 2 * (c->stage_tc + 2);
   return EDYN_OK;
 }
 
@@ -733,7 +756,7 @@ extern "C" int edyn_solve_fluid_noalloc(void* ctx, double* qf_d, double* qc_d, d
     a.save_q0 = (s == 0 && nst == 3) ? 1 : 0;
     a.h1 = h1[s];
     a.h2 = h2[s];
-    cudaError_t e = launch_stage(a, c->acu, c->lim, c->wflag, c->riemann, c->stage_threads, c->stream);
+    cudaError_t e = launch_stage(a, c->acu, c->lim, c->wflag, c->riemann, c->stream);
     if (e != cudaSuccess) return fail(c, EDYN_E_CUDA, "stage launch: %s", cudaGetErrorString(e));
     cur ^= 1;
   }

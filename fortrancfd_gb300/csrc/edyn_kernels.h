@@ -8,7 +8,8 @@
 namespace edyn {
 
 constexpr int GHOST = 4;          // ghost columns allocated per tube end (max lvir)
-constexpr int STAGE_THREADS = 128; // threads per stage CTA (two per cell position; cells = threads/2 - 2)
+constexpr int STAGE_MAX_THREADS = 256; // stage CTA: two threads per cell position, positions = cells + 2
+constexpr int STAGE_MIN_CELLS = 8;     // smallest stage tile (the tile rule needs at least lvir cells)
 
 struct ThermoTable;
 
@@ -22,6 +23,7 @@ struct FluidBC {
 
 struct StageArgs {
   int n, ld, lvir, ns;
+  int tc;                // cells per stage tile (CTA); the CTA has 2 (tc + 2) threads
   const double* qf_in;   // primitive rows read by the stencil
   double* qf_out;        // primitive rows written for owned cells
   double* qc;            // conserved rows, updated in place
@@ -42,8 +44,9 @@ struct StageArgs {
 };
 
 int fluid_upload_tables(const ThermoTable& tb, cudaStream_t s);
-size_t stage_smem_bytes(int acu, int ns, int nt);
-cudaError_t launch_stage(const StageArgs& a, int acu, int lim, int wflag, int rm, int nt, cudaStream_t s);
+size_t stage_smem_bytes(int acu, int ns, int tc);
+cudaError_t stage_tiling(int acu, int lim, int wflag, int rm, int ns, int n, int* tc);
+cudaError_t launch_stage(const StageArgs& a, int acu, int lim, int wflag, int rm, cudaStream_t s);
 cudaError_t launch_cvel(const double* qf, int n, int ld, unsigned long long* cvel, cudaStream_t s);
 cudaError_t launch_step_begin(const double* time, double tend, double cfl, double dx, unsigned long long* cvel,
                               int* step_active, double* dt_dev, cudaStream_t s);

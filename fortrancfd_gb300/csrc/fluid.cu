@@ -24,6 +24,7 @@
 // memory tables, so the kernel is bound by the FP64 pipe, not by HBM.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -215,12 +216,12 @@ __device__ void ghost_cell(const StageArgs& a, int g, double* dst, int dst_st, d
 // The stage kernel.
 // ---------------------------------------------------------------------------
 template <int ACU, int LIM, int WFLAG, int RIEMANN>
-__global__ void __launch_bounds__(STAGE_THREADS) k_stage(StageArgs a) {
+__global__ void __launch_bounds__(STAGE_MAX_THREADS) k_stage(StageArgs a) {
   constexpr int LV = acu_lvir(ACU);
   extern __shared__ double sm[];
-  const int NT = blockDim.x;  // threads: two per cell position in the reconstruction
-  const int P = NT / 2;       // positions: the cells c0-1..c0+TC, or the faces c0..c0+TC
-  const int TC = P - 2;
+  const int TC = a.tc;        // cells of a tile
+  const int P = TC + 2;       // positions: the cells c0-1..c0+TC, or the faces c0..c0+TC
+  const int NT = 2 * P;       // threads: two per position in the reconstruction
   const int tid = threadIdx.x;
   // Tile of this CTA: cells [c0, c1), TC wide. The right-end ghost cells are
   // built from the conserved state of the last LV cells, which the stage
@@ -255,6 +256,7 @@ __global__ void __launch_bounds__(STAGE_THREADS) k_stage(StageArgs a) {
   }
 
   // 1. stage the primitive state window (coalesced row loads)
+#pragma unroll 4
   for (int idx = tid; idx < ne * Wd; idx += NT) {
     const int v = idx / Wd, j = idx - v * Wd;
     const int cell = c0 - LV + j;
@@ -603,46 +605,97 @@ int fluid_upload_tables(const ThermoTable& tb, cudaStream_t s) {
   return (int)cudaSuccess;
 }
 
-size_t stage_smem_bytes(int acu, int ns, int nt) {
+size_t stage_smem_bytes(int acu, int ns, int tc) {
   const int lv = acu_lvir(acu);
   const int ne = ns + 3;
-  const int p = nt / 2, tc = p - 2;
+  const int p = tc + 2;
   return sizeof(double) * ((size_t)ne * (tc + 2 * lv) + (size_t)2 * ne * p);
 }
 
-template <int ACU, int LIM, int WF, int RM>
-static cudaError_t launch_t(const StageArgs& a, int nt, cudaStream_t s) {
-  const size_t smem = stage_smem_bytes(ACU, a.ns, nt);
-  auto kern = k_stage<ACU, LIM, WF, RM>;
-  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
-  const int tc = nt / 2 - 2;
-  const int grid = (a.n + tc - 1) / tc;
-  kern<<<grid, nt, smem, s>>>(a);
-  return cudaGetLastError();
-}
+namespace {
+
+using StageFn = void (*)(StageArgs);
 
 template <int ACU, int LIM, int WF>
-static cudaError_t launch_rm(const StageArgs& a, int rm, int nt, cudaStream_t s) {
-  if (rm == 0) return launch_t<ACU, LIM, WF, 0>(a, nt, s);
-  if (rm == 1) return launch_t<ACU, LIM, WF, 1>(a, nt, s);
-  return launch_t<ACU, LIM, WF, 2>(a, nt, s);
+StageFn stage_fn_rm(int rm) {
+  if (rm == 0) return k_stage<ACU, LIM, WF, 0>;
+  if (rm == 1) return k_stage<ACU, LIM, WF, 1>;
+  return k_stage<ACU, LIM, WF, 2>;
 }
 
-cudaError_t launch_stage(const StageArgs& a, int acu, int lim, int wflag, int rm, int nt, cudaStream_t s) {
+StageFn stage_fn(int acu, int lim, int wflag, int rm) {
   switch (acu) {
-    case ACU_FIRST: return launch_rm<ACU_FIRST, 2, 3>(a, rm, nt, s);
+    case ACU_FIRST: return stage_fn_rm<ACU_FIRST, 2, 3>(rm);
     case ACU_MUSCL:
-      if (lim == 1) return launch_rm<ACU_MUSCL, 1, 3>(a, rm, nt, s);
-      if (lim == 3) return launch_rm<ACU_MUSCL, 3, 3>(a, rm, nt, s);
-      if (lim == 4) return launch_rm<ACU_MUSCL, 4, 3>(a, rm, nt, s);
-      return launch_rm<ACU_MUSCL, 2, 3>(a, rm, nt, s);
-    case ACU_WENO3: return launch_rm<ACU_WENO3, 2, 3>(a, rm, nt, s);
+      if (lim == 1) return stage_fn_rm<ACU_MUSCL, 1, 3>(rm);
+      if (lim == 3) return stage_fn_rm<ACU_MUSCL, 3, 3>(rm);
+      if (lim == 4) return stage_fn_rm<ACU_MUSCL, 4, 3>(rm);
+      return stage_fn_rm<ACU_MUSCL, 2, 3>(rm);
+    case ACU_WENO3: return stage_fn_rm<ACU_WENO3, 2, 3>(rm);
     case ACU_WENO5:
-      if (wflag == 2) return launch_rm<ACU_WENO5, 2, 2>(a, rm, nt, s);
-      return launch_rm<ACU_WENO5, 2, 3>(a, rm, nt, s);
-    default: return launch_rm<ACU_WENO7, 2, 3>(a, rm, nt, s);
+      if (wflag == 2) return stage_fn_rm<ACU_WENO5, 2, 2>(rm);
+      return stage_fn_rm<ACU_WENO5, 2, 3>(rm);
+    default: return stage_fn_rm<ACU_WENO7, 2, 3>(rm);
   }
+}
+
+}  // namespace
+
+// Cells per stage tile for a tube of n cells. A CTA's time hardly depends on
+// its tile (each thread reconstructs one position, solves one face and one
+// cell, so the CTA is as long as one thread's chain of FP64 latencies), so
+// the launch lasts about one CTA time per wave of resident CTAs. The choice:
+// the fewest waves over the thread counts 64..STAGE_MAX_THREADS (their
+// occupancy, limited by the shared-memory window, from the runtime), then
+// the smallest tile that keeps that number of waves, so that the CTAs spread
+// over all resident slots. 20,000 cells with WENO5 and GRI-3.0: 66-cell tiles,
+// 304 CTAs, two per SM, one wave (62-cell tiles would need 323 CTAs, and the
+// 19 of a second wave would double the launch).
+cudaError_t stage_tiling(int acu, int lim, int wflag, int rm, int ns, int n, int* tc_out) {
+  int dev = 0, nsm = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return e;
+  const StageFn kern = stage_fn(acu, lim, wflag, rm);
+  long best_waves = -1, best_slots = 0;
+  int best_tcmax = 0;
+  for (int nt = 64; nt <= STAGE_MAX_THREADS; nt += 32) {
+    const int tcmax = nt / 2 - 2;
+    const size_t smem = stage_smem_bytes(acu, ns, tcmax);
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) {
+      (void)cudaGetLastError();
+      continue;  // window larger than a CTA may hold
+    }
+    int occ = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, nt, smem);
+    if (e != cudaSuccess) return e;
+    if (occ < 1) continue;
+    const long slots = (long)occ * nsm;
+    const long nb = (n + tcmax - 1) / tcmax;
+    const long waves = (nb + slots - 1) / slots;
+    if (best_waves < 0 || waves < best_waves) {
+      best_waves = waves;
+      best_slots = slots;
+      best_tcmax = tcmax;
+    }
+  }
+  if (best_waves < 0) return cudaErrorInvalidConfiguration;
+  long tc = (n + best_waves * best_slots - 1) / (best_waves * best_slots);
+  tc = std::max<long>(tc, 16);
+  tc = std::min<long>(tc, best_tcmax);
+  *tc_out = (int)tc;
+  return cudaSuccess;
+}
+
+cudaError_t launch_stage(const StageArgs& a, int acu, int lim, int wflag, int rm, cudaStream_t s) {
+  const StageFn kern = stage_fn(acu, lim, wflag, rm);
+  const size_t smem = stage_smem_bytes(acu, a.ns, a.tc);
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  const int grid = (a.n + a.tc - 1) / a.tc;
+  kern<<<grid, 2 * (a.tc + 2), smem, s>>>(a);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_cvel(const double* qf, int n, int ld, unsigned long long* cvel, cudaStream_t s) {

@@ -72,6 +72,8 @@ def lib() -> ctypes.CDLL:
     L.edyn_chem_cost.argtypes = [vp, ip, ctypes.POINTER(ctypes.c_uint)]
     L.edyn_check_exp.argtypes = [vp, i, dp, dp]
     L.edyn_check_log.argtypes = [vp, i, dp, dp]
+    L.edyn_set_stage_tile.argtypes = [vp, i]
+    L.edyn_stage_tile.argtypes = [vp, ip, ip]
     L.edyn_last_error.argtypes = [vp, ctypes.c_char_p, i]
     L.edyn_finalize.argtypes = [vp]
     L.edyn_mech_compile.argtypes = [cp, cp, ctypes.c_char_p, i]
@@ -225,6 +227,16 @@ class Tube(_Ctx):
         self._check(lib().edyn_chem_cost(self._h, cost.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
                                          hot.ctypes.data_as(ctypes.POINTER(ctypes.c_uint))))
         return cost, hot[1:1 + int(hot[0])].astype(np.int64)
+
+    def set_stage_tile(self, cells: int = 0) -> None:
+        """Cells per fluid stage tile; 0 chooses it from the tube length."""
+        self._check(lib().edyn_set_stage_tile(self._h, int(cells)))
+
+    def stage_tile(self):
+        """(cells per stage tile, threads per stage CTA) in use."""
+        cells, threads = ctypes.c_int(), ctypes.c_int()
+        self._check(lib().edyn_stage_tile(self._h, ctypes.byref(cells), ctypes.byref(threads)))
+        return cells.value, threads.value
 
     def download(self):
         qf = np.empty((self.ncell, self.nequ))

@@ -25,7 +25,7 @@ def rel(a, b, scale=None):
     return float(np.max(np.abs(a - b) / scale))
 
 
-def run_pair(oracle, case, nsteps, strict=1, use_advance=False):
+def run_pair(oracle, case, nsteps, strict=1, use_advance=False, tile=0):
     W = configs.molecular_weights()
     qf0, qc0 = oracle.init_cells(case.T, case.p, case.u, case.X)
     fl = case.flags
@@ -36,6 +36,9 @@ def run_pair(oracle, case, nsteps, strict=1, use_advance=False):
     ot.set_interior(qf0, qc0)
     kw = {k: v for k, v in fl.items() if k != "do_reaction"}
     g = Tube(case.ncell, case.dx, strict_newton=strict, do_reaction=0, **kw)
+    if tile:
+        g.set_stage_tile(tile)
+        assert g.stage_tile() == (tile, 2 * (tile + 2))
     g.upload(qf0, qc0)
     t_o = 0.0
     for _ in range(nsteps):
@@ -152,11 +155,40 @@ def test_short_last_tile(oracle, ncell, scheme):
     case = configs.sod(ncell=ncell)
     case.flags.update(scheme)
     case.flags.setdefault("flag_weno", 0)
-    qf_o, qf_g, p_o, p_g, _, _ = run_pair(oracle, case, 400)
+    assert ncell % 63 < lvir_for(case.flags["flag_acu"], case.flags["flag_weno"])
+    qf_o, qf_g, p_o, p_g, _, _ = run_pair(oracle, case, 400, tile=63)
     assert rel(p_g, p_o) < TOL
     assert rel(qf_g[:, 2], qf_o[:, 2]) < TOL
     umax = np.abs(qf_o[:, 1]).max()
     assert float(np.max(np.abs(qf_g[:, 1] - qf_o[:, 1]))) / umax < TOL
+
+
+def test_stage_tile_does_not_change_results():
+    """The stage result is bit-identical for every tile size (each face and
+    cell is computed by the same arithmetic whatever CTA owns it), and the
+    automatic tile keeps the launch to whole waves."""
+    case = configs.detonation(ncell=1500)
+    qf0, qc0 = None, None
+    runs = []
+    for tile in (0, 8, 40, 63, 126):
+        g = Tube(case.ncell, case.dx, flag_acu=2, flag_weno=3, flag_rbound=1, do_reaction=0)
+        if tile:
+            g.set_stage_tile(tile)
+        g.init_cells(case.T, case.p, case.u, case.X)
+        for _ in range(6):
+            g.step(case.cfl)
+        runs.append(g.download()[:2])
+        if tile == 0:
+            cells, threads = g.stage_tile()
+            assert 16 <= cells <= 126 and threads == 2 * (cells + 2)
+    for qf, qc in runs[1:]:
+        assert np.array_equal(qf, runs[0][0])
+        assert np.array_equal(qc, runs[0][1])
+    g = Tube(case.ncell, case.dx)
+    with pytest.raises(RuntimeError):
+        g.set_stage_tile(7)
+    with pytest.raises(RuntimeError):
+        g.set_stage_tile(127)
 
 
 def test_init_cells_matches_oracle(oracle):

@@ -348,7 +348,7 @@ int edyn_stage_tile(void* ctx, int* cells, int* threads) {
   Ctx* c = (Ctx*)ctx;
   if (!c || !c->qc) return EDYN_E_ARG;
   if (cells) *cells = c->stage_tc;
-  if (threads) *threads = 2 * (c->stage_tc + 2);
+  if (threads) *threads = stage_threads(c->stage_tc);
   return EDYN_OK;
 }
 

@@ -10,6 +10,8 @@ namespace edyn {
 constexpr int GHOST = 4;          // ghost columns allocated per tube end (max lvir)
 constexpr int STAGE_MAX_THREADS = 256; // stage CTA: two threads per cell position, positions = cells + 2
 constexpr int STAGE_MIN_CELLS = 8;     // smallest stage tile (the tile rule needs at least lvir cells)
+// threads of a stage CTA for a tile of tc cells: two per position, whole warps
+constexpr int stage_threads(int tc) { return (2 * (tc + 2) + 31) / 32 * 32; }
 
 struct ThermoTable;
 
@@ -23,7 +25,7 @@ struct FluidBC {
 
 struct StageArgs {
   int n, ld, lvir, ns;
-  int tc;                // cells per stage tile (CTA); the CTA has 2 (tc + 2) threads
+  int tc;                // cells per stage tile (CTA); the CTA has stage_threads(tc) threads
   const double* qf_in;   // primitive rows read by the stencil
   double* qf_out;        // primitive rows written for owned cells
   double* qc;            // conserved rows, updated in place

@@ -51,60 +51,85 @@ struct CellEOS {
   double T, u, Sz, cpR;  // cpR = Cp(T) of the final premix, for the sound speed
 };
 
-__device__ __forceinline__ void premix_cell(const double* ys, int st, double T, Premix& pm, double& Sz) {
+// Sum of v over the two threads of a lane pair (2j, 2j+1) that split a
+// cell's species between them (S = 2; identity for S = 1). Both threads get
+// the same bits: v0 + v1 and v1 + v0 round alike.
+template <int S>
+__device__ __forceinline__ double pair_sum(double v, unsigned mask) {
+  if constexpr (S == 2) return v + __shfl_xor_sync(mask, v, 1);
+  return v;
+}
+
+template <int S>
+__device__ __forceinline__ void pair_sum(Premix& pm, unsigned mask) {
+#pragma unroll
+  for (int n = 0; n < 6; ++n) pm.A[n] = pair_sum<S>(pm.A[n], mask);
+}
+
+// Premixed NASA-7 coefficients of a cell; with S = 2 the thread takes the
+// species k = h, h + 2, ... and the pair sums its parts.
+template <int S = 1>
+__device__ __forceinline__ void premix_cell(const double* ys, int st, double T, Premix& pm, double& Sz, int h = 0,
+                                            unsigned mask = 0u) {
   const ThermoTable& tb = c_thermo;
   pm.zero(t_interval(tb, T));
   double sz = 0.0;
-  for (int k = 0; k < tb.ns; ++k) {
+  for (int k = h; k < tb.ns; k += S) {
     double z = ys[k * st] * tb.invW[k];
     sz += z;
     premix_add(tb, pm, k, z, T);
   }
-  Sz = sz;
+  Sz = pair_sum<S>(sz, mask);
+  pair_sum<S>(pm, mask);
 }
 
 // Newton on sum z_k u_k(T) = e for T (temperature_con, SRC/thermo.f90:211-257)
 // in the premixed variables: g(T) = H(T) - T Sz - E, dg/dT = Cp(T) - Sz.
-// Stopping rules and the [20, 6000] K clamp are the reference's.
+// Both threads of a pair iterate alike (same sums, same iterates).
+template <int S = 1>
 __device__ __forceinline__ double t_newton(const double* ys, int st, double E, double T0, Premix& pm, double& Sz,
-                                           int& iters) {
+                                           int& iters, int h = 0, unsigned mask = 0u) {
   const ThermoTable& tb = c_thermo;
   double T = T0, g = 1e30, dT = 1e30;
   int it = 0;
-  premix_cell(ys, st, T, pm, Sz);
+  premix_cell<S>(ys, st, T, pm, Sz, h, mask);
   while (fabs(g) >= fabs(E) * 1e-9 && fabs(dT) >= T * 1e-6 && it < 10) {
-    if (t_interval(tb, T) != pm.interval) premix_cell(ys, st, T, pm, Sz);
+    if (t_interval(tb, T) != pm.interval) premix_cell<S>(ys, st, T, pm, Sz, h, mask);
     g = pm.H(T) - T * Sz - E;
     double cvR = pm.Cp(T) - Sz;
     dT = -g / cvR;
     T = fmax(20.0, fmin(6000.0, T + dT));
     ++it;
   }
-  if (t_interval(tb, T) != pm.interval) premix_cell(ys, st, T, pm, Sz);
+  if (t_interval(tb, T) != pm.interval) premix_cell<S>(ys, st, T, pm, Sz, h, mask);
   iters = it;
   return T;
 }
 
-// Full QcToqf. On entry ys[k*st] = rho*Y_k. Writes the normalised Y_k back.
+// Full QcToqf. On entry ys[k*st] = rho*Y_k. Writes the normalised Y_k back
+// (with S = 2, the species k = h, h + 2, ... of this thread).
+template <int S = 1>
 __device__ __forceinline__ CellEOS qc_to_qf_cell(double rho, double rhou, double rhoe, double* ys, int st,
-                                                 double Tguess, bool strict, int& iters) {
+                                                 double Tguess, bool strict, int& iters, int h = 0,
+                                                 unsigned mask = 0u) {
   const ThermoTable& tb = c_thermo;
   CellEOS r;
   const double inv_rho = 1.0 / rho;
   r.u = rhou * inv_rho;
   double s = 0.0;
-  for (int k = 0; k < tb.ns; ++k) {
+  for (int k = h; k < tb.ns; k += S) {
     double y = clip0(ys[k * st] * inv_rho);
     ys[k * st] = y;
     s += y;
   }
+  s = pair_sum<S>(s, mask);
   const double inv_s = 1.0 / s;
-  for (int k = 0; k < tb.ns; ++k) ys[k * st] *= inv_s;
+  for (int k = h; k < tb.ns; k += S) ys[k * st] *= inv_s;
   const double e_int = rhoe * inv_rho - 0.5 * (r.u * r.u);
   const double E = e_int * (1.0 / R_SI);
   Premix pm;
   double Sz;
-  r.T = t_newton(ys, st, E, strict ? 1000.0 : Tguess, pm, Sz, iters);
+  r.T = t_newton<S>(ys, st, E, strict ? 1000.0 : Tguess, pm, Sz, iters, h, mask);
   r.Sz = Sz;
   r.cpR = pm.Cp(r.T);
   return r;
@@ -221,7 +246,7 @@ __global__ void __launch_bounds__(STAGE_MAX_THREADS) k_stage(StageArgs a) {
   extern __shared__ double sm[];
   const int TC = a.tc;        // cells of a tile
   const int P = TC + 2;       // positions: the cells c0-1..c0+TC, or the faces c0..c0+TC
-  const int NT = 2 * P;       // threads: two per position in the reconstruction
+  const int NT = blockDim.x;  // whole warps, at least two threads per position
   const int tid = threadIdx.x;
   // Tile of this CTA: cells [c0, c1), TC wide. The right-end ghost cells are
   // built from the conserved state of the last LV cells, which the stage
@@ -272,7 +297,7 @@ __global__ void __launch_bounds__(STAGE_MAX_THREADS) k_stage(StageArgs a) {
 
   // 2. face values of the cells c0-1..c1: position p = tid % P, rows split
   //    between the two halves of the CTA
-  {
+  if (tid < 2 * P) {
     const int p = tid % P, half = tid / P;
     if (c0 - 1 + p <= c1) {
       const int c = p + LV - 1;  // window index of cell c0-1+p
@@ -286,8 +311,10 @@ __global__ void __launch_bounds__(STAGE_MAX_THREADS) k_stage(StageArgs a) {
   }
   __syncthreads();
 
-  // 3. one face per thread: face c0+f between cells c0-1+f and c0+f
-  const int f = tid;
+  // 3. one face per lane pair: face c0+f between cells c0-1+f and c0+f;
+  //    lane h of the pair takes the species k = h, h + 2, ...
+  const int f = tid >> 1, h = tid & 1;
+  const unsigned pair = 3u << (tid & 30);
   if (f < P && c0 + f <= c1) {
     FaceState L, R;
     L.rho = s_l[0 * P + f];
@@ -300,7 +327,7 @@ __global__ void __launch_bounds__(STAGE_MAX_THREADS) k_stage(StageArgs a) {
     pl.zero(t_interval(tb, L.T));
     pr.zero(t_interval(tb, R.T));
     double syl = 0.0, syr = 0.0, szl = 0.0, szr = 0.0;
-    for (int k = 0; k < ns; ++k) {
+    for (int k = h; k < ns; k += 2) {
       const double yl = s_l[(3 + k) * P + f], yr = s_r[(3 + k) * P + f + 1];
       const double pl_ = clip0(yl), pr_ = clip0(yr);
       syl += pl_;
@@ -311,6 +338,12 @@ __global__ void __launch_bounds__(STAGE_MAX_THREADS) k_stage(StageArgs a) {
       premix_add(tb, pl, k, zl, L.T);
       premix_add(tb, pr, k, zr, R.T);
     }
+    syl = pair_sum<2>(syl, pair);
+    syr = pair_sum<2>(syr, pair);
+    szl = pair_sum<2>(szl, pair);
+    szr = pair_sum<2>(szr, pair);
+    pair_sum<2>(pl, pair);
+    pair_sum<2>(pr, pair);
     face_finish(L, pl, syl, szl);
     face_finish(R, pr, syr, szr);
     const double ml = L.rho * L.u, mr = R.rho * R.u;
@@ -318,15 +351,15 @@ __global__ void __launch_bounds__(STAGE_MAX_THREADS) k_stage(StageArgs a) {
     const double fl0 = ml, fr0 = mr;
     const double fl1 = ml * L.u + L.p, fr1 = mr * R.u + R.p;
     const double fl2 = (L.E + L.p) * L.u, fr2 = (R.E + R.p) * R.u;
-    double* F = s_l + f;
+    double F0, F1, F2;
     // species row k: flux = aL * YL + bL * max(YL,0) + aR * YR + bR * max(YR,0)
     double aL = 0.0, bL = 0.0, aR = 0.0, bR = 0.0;
     if (RIEMANN == 0) {  // LxF, SRC/flux.f90:287-294
       const double lamL = fabs(L.u) + L.a, lamR = fabs(R.u) + R.a;
       const double alpha = fmax(lamL, lamR);
-      F[0] = 0.5 * (fl0 + fr0 - alpha * (R.rho - L.rho));
-      F[P] = 0.5 * (fl1 + fr1 - alpha * (mr - ml));
-      F[2 * P] = 0.5 * (fl2 + fr2 - alpha * (R.E - L.E));
+      F0 = 0.5 * (fl0 + fr0 - alpha * (R.rho - L.rho));
+      F1 = 0.5 * (fl1 + fr1 - alpha * (mr - ml));
+      F2 = 0.5 * (fl2 + fr2 - alpha * (R.E - L.E));
       aL = 0.5 * ml;
       aR = 0.5 * mr;
       bR = -0.5 * alpha * R.rho * R.inv_SY;
@@ -340,52 +373,58 @@ __global__ void __launch_bounds__(STAGE_MAX_THREADS) k_stage(StageArgs a) {
       const double sR = fmax(R.u + R.a, u_roe + a_roe);
       if (RIEMANN == 1) {  // HLL, SRC/flux.f90:296-315
         if (0.0 <= sL) {
-          F[0] = fl0; F[P] = fl1; F[2 * P] = fl2;
+          F0 = fl0; F1 = fl1; F2 = fl2;
           aL = ml;
         } else if (0.0 <= sR) {
           const double inv = 1.0 / (sR - sL), ss = sL * sR;
-          F[0] = (sR * fl0 - sL * fr0 + ss * (R.rho - L.rho)) * inv;
-          F[P] = (sR * fl1 - sL * fr1 + ss * (mr - ml)) * inv;
-          F[2 * P] = (sR * fl2 - sL * fr2 + ss * (R.E - L.E)) * inv;
+          F0 = (sR * fl0 - sL * fr0 + ss * (R.rho - L.rho)) * inv;
+          F1 = (sR * fl1 - sL * fr1 + ss * (mr - ml)) * inv;
+          F2 = (sR * fl2 - sL * fr2 + ss * (R.E - L.E)) * inv;
           aL = sR * ml * inv;
           aR = -sL * mr * inv;
           bR = ss * R.rho * R.inv_SY * inv;
           bL = -ss * L.rho * L.inv_SY * inv;
         } else {
-          F[0] = fr0; F[P] = fr1; F[2 * P] = fr2;
+          F0 = fr0; F1 = fr1; F2 = fr2;
           aR = mr;
         }
       } else {  // HLLC, SRC/flux.f90:317-354
         const double sM = (L.p - R.p + mr * (sR - R.u) - ml * (sL - L.u)) /
                           (R.rho * (sR - R.u) - L.rho * (sL - L.u));
         if (0.0 <= sL) {
-          F[0] = fl0; F[P] = fl1; F[2 * P] = fl2;
+          F0 = fl0; F1 = fl1; F2 = fl2;
           aL = ml;
         } else if (0.0 <= sM) {
           const double fac = L.rho * (sL - L.u) / (sL - sM);
           const double ve = L.E / L.rho + (sM - L.u) * (sM + L.p / (L.rho * (sL - L.u)));
-          F[0] = fl0 + sL * (fac - L.rho);
-          F[P] = fl1 + sL * (fac * sM - ml);
-          F[2 * P] = fl2 + sL * (fac * ve - L.E);
+          F0 = fl0 + sL * (fac - L.rho);
+          F1 = fl1 + sL * (fac * sM - ml);
+          F2 = fl2 + sL * (fac * ve - L.E);
           aL = ml;
           bL = sL * (fac - L.rho) * L.inv_SY;
         } else if (0.0 <= sR) {
           const double fac = R.rho * (sR - R.u) / (sR - sM);
           const double ve = R.E / R.rho + (sM - R.u) * (sM + R.p / (R.rho * (sR - R.u)));
-          F[0] = fr0 + sR * (fac - R.rho);
-          F[P] = fr1 + sR * (fac * sM - mr);
-          F[2 * P] = fr2 + sR * (fac * ve - R.E);
+          F0 = fr0 + sR * (fac - R.rho);
+          F1 = fr1 + sR * (fac * sM - mr);
+          F2 = fr2 + sR * (fac * ve - R.E);
           aR = mr;
           bR = sR * (fac - R.rho) * R.inv_SY;
         } else {
-          F[0] = fr0; F[P] = fr1; F[2 * P] = fr2;
+          F0 = fr0; F1 = fr1; F2 = fr2;
           aR = mr;
         }
       }
     }
-    // species row k: flux = aL * YL + bL * max(YL,0) + aR * YR + bR * max(YR,0);
-    // the flux replaces YL, which no other thread reads
-    for (int k = 0; k < ns; ++k) {
+    // The fluxes replace the left states of this face, which no other pair
+    // reads: the bulk rows by lane 0, species row k by the lane that owns k.
+    double* F = s_l + f;
+    if (h == 0) {
+      F[0] = F0;
+      F[P] = F1;
+      F[2 * P] = F2;
+    }
+    for (int k = h; k < ns; k += 2) {
       const double yl = s_l[(3 + k) * P + f], yr = s_r[(3 + k) * P + f + 1];
       double v = aL * yl;
       v = fma(bL, clip0(yl), v);
@@ -396,38 +435,51 @@ __global__ void __launch_bounds__(STAGE_MAX_THREADS) k_stage(StageArgs a) {
   }
   __syncthreads();
 
-  // 4. one cell per thread: conservative update + QcToqf
-  const int i = c0 + tid;
+  // 4. one cell per lane pair: conservative update + QcToqf, species split
+  //    as in phase 3 (the bulk rows are computed by both lanes)
+  const int i = c0 + f;
   double speed = 0.0;
-  if (tid < P && i < c1) {
+  if (f < P && i < c1) {
     const double c = dt / a.dx;
     const size_t ld = (size_t)a.ld;
     double* Q = a.qc + i + GHOST;
     double* Q0 = a.q0 + i + GHOST;
-    double* ys = s_r + tid;  // strided by P
-    double q[3];
-    for (int v = 0; v < ne; ++v) {
-      const double dF = s_l[v * P + tid + 1] - s_l[v * P + tid];
-      const double qv = Q[v * ld];
-      double qn;
-      if (a.kind == 0) {  // Euler or first TVDRK3 stage: Q0 + (0 - c dF)
-        if (a.save_q0) Q0[v * ld] = qv;
-        qn = qv - c * dF;
-      } else {
-        qn = fma(a.h1, Q0[v * ld], a.h2 * (qv - c * dF));
+    double* ys = s_r + f;  // strided by P
+    // Euler or first TVDRK3 stage: Q - c dF; later stages h1 Q0 + h2 (Q - c dF)
+    auto update = [&](int v, double qv) {
+      const double dF = s_l[v * P + f + 1] - s_l[v * P + f];
+      return a.kind == 0 ? qv - c * dF : fma(a.h1, Q0[v * ld], a.h2 * (qv - c * dF));
+    };
+    double q[3], qv[3];
+#pragma unroll
+    for (int v = 0; v < 3; ++v) qv[v] = Q[v * ld];
+    __syncwarp(pair);  // both lanes have read the bulk rows before lane (v & 1) rewrites row v
+#pragma unroll
+    for (int v = 0; v < 3; ++v) {
+      q[v] = update(v, qv[v]);
+      if ((v & 1) == h) {
+        if (a.save_q0) Q0[v * ld] = qv[v];
+        Q[v * ld] = q[v];
       }
+    }
+    for (int v = 3 + h; v < ne; v += 2) {
+      const double qs = Q[v * ld];
+      const double qn = update(v, qs);
+      if (a.save_q0) Q0[v * ld] = qs;
       Q[v * ld] = qn;
-      if (v < 3) q[v] = qn; else ys[(v - 3) * P] = qn;
+      ys[(v - 3) * P] = qn;
     }
     int iters;
-    const double Tg = s_q[2 * Wd + tid + LV];
-    CellEOS e = qc_to_qf_cell(q[0], q[1], q[2], ys, P, Tg, a.strict_newton != 0, iters);
+    const double Tg = s_q[2 * Wd + f + LV];
+    CellEOS e = qc_to_qf_cell<2>(q[0], q[1], q[2], ys, P, Tg, a.strict_newton != 0, iters, h, pair);
     double* out = a.qf_out + i + GHOST;
-    out[0] = q[0];
-    out[ld] = e.u;
-    out[2 * ld] = e.T;
-    for (int k = 0; k < ns; ++k) out[(3 + k) * ld] = ys[k * P];
-    if (a.cvel_out) speed = cell_speed(e.u, e.T, e.Sz, e.cpR);
+    if (h == 0) {
+      out[0] = q[0];
+      out[ld] = e.u;
+      out[2 * ld] = e.T;
+      if (a.cvel_out) speed = cell_speed(e.u, e.T, e.Sz, e.cpR);
+    }
+    for (int k = h; k < ns; k += 2) out[(3 + k) * ld] = ys[k * P];
   }
   if (a.cvel_out) {
     double m = speed;
@@ -694,7 +746,7 @@ cudaError_t launch_stage(const StageArgs& a, int acu, int lim, int wflag, int rm
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   const int grid = (a.n + a.tc - 1) / a.tc;
-  kern<<<grid, 2 * (a.tc + 2), smem, s>>>(a);
+  kern<<<grid, stage_threads(a.tc), smem, s>>>(a);
   return cudaGetLastError();
 }
 

@@ -1333,7 +1333,8 @@ __device__ CellStats integrate(const Tabs& t, const Team<TW>& tm, WarpWork& w, c
     if (st.steps + st.rejects >= max_steps) { st.failed = true; break; }
     h_want = h;
     if (tcur + h > c.dt) h = c.dt - tcur;
-    // f0 = f(y0) in FP64 (kept across rejections)
+    // f0 = f(y0) in FP64 at the window start; later the last stage
+    // derivative of the accepted step (kept across rejections)
     if (need_f0) {
       rhs64<TW>(t, tm, w, w.y0, c.rho_cgs, w.dl);
       st.rhs++;
@@ -1463,11 +1464,17 @@ __device__ CellStats integrate(const Tabs& t, const Team<TW>& tm, WarpWork& w, c
     const float en = sqrtf(tm.sum(ss) / (float)n);
     const float fac = 0.9f * powf(fmaxf(en, 1e-10f), -0.25f);
     if (en <= 1.f) {
-      for (int i = lane; i < n; i += TW) w.y0[i] = w.Y[i];
+      // SDIRK4 is stiffly accurate (y1 = Y5), so the last stage derivative is
+      // f at the new y0 up to the Newton tolerance: it serves as the next
+      // step's f0, which only predicts the first stage (Hairer and Wanner,
+      // Solving ODEs II, IV.8, starting values)
+      for (int i = lane; i < n; i += TW) {
+        w.y0[i] = w.Y[i];
+        w.dl[i] = w.F[4][i];
+      }
       tm.sync();
       tcur += h;
       st.steps++;
-      need_f0 = true;
       const float q = fminf(5.f, fmaxf(0.2f, fac));
       const double hprop = h * (double)q;
       // the proposal after a step cut short by the window end is measured

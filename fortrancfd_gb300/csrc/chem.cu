@@ -1299,7 +1299,7 @@ struct Cell {
 struct CellStats {
   int rhs, steps, rejects, jac;
   bool failed;
-  double hnext;  // step size the controller proposes after the window
+  double hnext;  // step size the cell's next window starts with
 };
 
 constexpr float THETA_JAC = 0.1f;  // Newton contraction above which a kept Jacobian is rebuilt
@@ -1328,6 +1328,10 @@ __device__ CellStats integrate(const Tabs& t, const Team<TW>& tm, WarpWork& w, c
   // instead and reuses the matrix (Hairer and Wanner, Solving ODEs II, IV.8).
   bool m_ok = false;
   double h_m = 0.0;
+  // The first accepted step of the window starts the next one: a cell at a
+  // reaction front opens each window with the fast transient the fluid step
+  // sets off, which the step size the window ended with overshoots.
+  double hfirst = 0.0;
   const double g = 0.25;
   while (tcur < c.dt) {
     if (st.steps + st.rejects >= max_steps) { st.failed = true; break; }
@@ -1390,7 +1394,17 @@ __device__ CellStats integrate(const Tabs& t, const Team<TW>& tm, WarpWork& w, c
         double acc = w.y0[i];
         for (int j = 0; j < s; ++j) acc = fma(h * c_sa[s][j], w.F[j][i], acc);
         w.sv[i] = acc;
-        const double fp = (s == 0) ? w.dl[i] : w.F[s - 1][i];
+        // starting value: the stage derivative extrapolated linearly in the
+        // stage abscissa c = (1/4, 3/4, 11/20, 1/2, 1) from two earlier
+        // derivatives (f0 at c = 0; stage 5 from the pair at 3/4 and 1/2)
+        double fp;
+        switch (s) {
+          case 0: fp = w.dl[i]; break;
+          case 1: fp = fma(3.0, w.F[0][i], -2.0 * w.dl[i]); break;
+          case 2: fp = fma(0.6, w.F[1][i], 0.4 * w.F[0][i]); break;
+          case 3: fp = fma(1.25, w.F[2][i], -0.25 * w.F[1][i]); break;
+          default: fp = fma(2.0, w.F[1][i], -w.F[3][i]); break;
+        }
         w.Y[i] = fma(h * g, fp, acc);
       }
       tm.sync();
@@ -1473,13 +1487,13 @@ __device__ CellStats integrate(const Tabs& t, const Team<TW>& tm, WarpWork& w, c
         w.dl[i] = w.F[4][i];
       }
       tm.sync();
+      if (hfirst == 0.0) hfirst = h;
       tcur += h;
       st.steps++;
       const float q = fminf(5.f, fmaxf(0.2f, fac));
       const double hprop = h * (double)q;
       // the proposal after a step cut short by the window end is measured
       // on the shorter step; the step size wanted before the cut stands too
-      st.hnext = (h < h_want) ? fmax(hprop, h_want) : hprop;
       jac_fresh = false;
       ++jac_age;
       const bool jac_next = !keep_jac || theta_max > THETA_JAC || jac_age >= JAC_MAX_AGE;
@@ -1497,6 +1511,7 @@ __device__ CellStats integrate(const Tabs& t, const Team<TW>& tm, WarpWork& w, c
       need_jac = !keep_jac;
     }
   }
+  if (hfirst > 0.0) st.hnext = hfirst;
   return st;
 }
 
@@ -1577,7 +1592,7 @@ __device__ int tube_cell(const Tabs& t, const Team<TW>& tm, WarpWork& w, const C
   for (int k = tid; k < ns; k += TW) w.y0[k] *= inv_s;
   if (tid == 0) w.y0[ns] = q[2 * ld];
   tm.sync();
-  // start from the step size this cell's last window ended with
+  // start from the first accepted step of this cell's last window
   const double hl = L.hlast ? L.hlast[cell] : 0.0;
   Cell c{rho * 1e-3, dt, L.rtol, L.atol, (hl > 0.0 && hl < dt) ? hl : dt};
   CellStats st = integrate<TW>(t, tm, w, c);

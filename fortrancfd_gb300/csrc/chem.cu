@@ -69,7 +69,8 @@ struct TabHdr {
   int o_ent;                  // uint[nent]: scheduled reaction index
   // real tables: [0] FP64 offset, [1] FP32 offset
   int o_A[2], o_lnA[2], o_B[2], o_E[2];  // [nrp]
-  int o_aux[2];                // [nsp*AUXW]: lowA lowB lowE troe_a T3 T1 T2 ifop ln(lowA) 1/T3 1/T1
+  int o_aux[2];                // [nsp*AUXW]: lowA lowB lowE troe_a T3 T1 T2 ifop ln(lowA) 1/T3 1/T1;
+                               // the FP64 copy holds lowA/A, lowB - B, lowE - E in the first three
   int o_tb_am1[2];             // [ntbl]
   int o_W[2], o_invW[2], o_tmid[2], o_hf[2];  // [NSMAX]
   int o_cs[2];                 // [2][7][NSMAX] S/R - H/RT coefficients
@@ -79,6 +80,8 @@ struct TabHdr {
   int o_e2;                    // double[64]: 2^(j/64), the table of texp
   int o_lg;                    // double[2][92]: ln(j/128), 128/j for j = 90..181, the tables of tlog
   int fr0, nfr;                // the fall-off reactions fill rounds [fr0, fr0 + nfr) of 32
+  int o_grp;                   // int4[TEAM]: per team lane: species (-1 none), entry begin, end, group size
+  int gmax;                    // largest species group of the team production rates
 };
 
 template <class R>
@@ -90,6 +93,7 @@ struct Tabs {
   const TabHdr* h;
   const unsigned *w0, *w1, *w2, *w3, *w4, *w5, *ent;
   const int *spi, *tb_sp, *pc, *lane, *spc, *spp;
+  const int4* grp;
   const double* e2;
   const double* lg;
   int ns, nr, nrp, npc;
@@ -137,6 +141,7 @@ __device__ __forceinline__ Tabs bind_tabs(const char* base) {
   t.lane = (const int*)(base + h.o_lane);
   t.spc = (const int*)(base + h.o_spc);
   t.spp = (const int*)(base + h.o_spp);
+  t.grp = (const int4*)(base + h.o_grp);
   t.ent = (const unsigned*)(base + h.o_ent);
   t.e2 = (const double*)(base + h.o_e2);
   t.lg = (const double*)(base + h.o_lg);
@@ -150,7 +155,10 @@ __device__ __forceinline__ Tabs bind_tabs(const char* base) {
 }
 
 // reaction flag bits (w0 >> 24)
-constexpr unsigned F_REV = 1, F_CM = 2, F_FALL = 4, F_KFAL = 8, F_EXP = 16, F_TB = 32;
+// F_GEN: a side of order above 3, kept as (species, nu) slots; every other
+// reaction lists each side as up to three species slots with nu = 1 (2 OH is
+// OH, OH), so its concentration products are three plain factors.
+constexpr unsigned F_REV = 1, F_CM = 2, F_FALL = 4, F_KFAL = 8, F_EXP = 16, F_TB = 32, F_GEN = 64;
 
 // Per-team shared workspace. A team is the group of threads that works on
 // one cell: one warp, or four warps of a CTA (one per SM sub-partition, each
@@ -494,6 +502,32 @@ __device__ __forceinline__ R falloff_pcor(const Tabs& t, R pr, int ifop, R fclog
   return pcor;
 }
 
+// FP64 form of falloff_pcor with one reciprocal: with c = log10 Pr -
+// (0.4 + 0.67 log10 Fc) and d = 0.75 - 1.27 log10 Fc - 0.14 c, Troe's
+// 1 + (c/d)^2 is e/d^2 for e = d^2 + c^2, and 1/((1 + Pr) e) gives both
+// 1/(1 + Pr) and 1/e. The same quantities as falloff_pcor<double> up to
+// rounding; beyond Pr = 1e150 the two reciprocals are taken apart.
+__device__ __forceinline__ double falloff_pcor_d(const Tabs& t, double pr, int ifop, double fclog) {
+  const double p1 = 1.0 + pr;
+  if (ifop <= 1) return pr / p1;
+  const double prlog = tlog(fmax(pr, Math<double>::small()), t.lg) * 0.43429448190325182765;
+  const double c = prlog - ((double)0.4f + (double)0.67f * fclog);
+  const double d = (0.75 - (double)1.27f * fclog) - (double)0.14f * c;
+  const double d2 = d * d;
+  const double e = fma(c, c, d2);
+  double inv_p1, inv_e;
+  if (pr < 1e150) {
+    const double r = 1.0 / (p1 * e);
+    inv_p1 = r * e;
+    inv_e = r * p1;
+  } else {
+    inv_p1 = 1.0 / p1;
+    inv_e = 1.0 / e;
+  }
+  const double flog = (fclog * d2) * inv_e;
+  return texp_a(2.302585092994045684 * flog, t.e2) * (pr * inv_p1);  // 10^flog Pr/(1+Pr)
+}
+
 // mass-action products (CKRATX 6900-6915)
 template <class R>
 __device__ __forceinline__ void mass_action(unsigned w0, unsigned w1, unsigned w2, const R* C, R& qf, R& qr) {
@@ -534,9 +568,9 @@ __device__ __forceinline__ RxnEval<R> eval_rxn(const Tabs& t, int i, R logT, R i
     o.cm = cm;
     if (fl & F_FALL) {
       const R* fp = x.aux + aux * AUXW;
-      const R k0 = (sizeof(R) == sizeof(double)) ? fp[0] * texp_a(fp[1] * logT - fp[2] * invT, t.e2)
-                                                 : Math<R>::ex(fp[8] + fp[1] * logT - fp[2] * invT);
-      const R pr = k0 * cm / kf;
+      R pr;
+      if constexpr (sizeof(R) == sizeof(double)) pr = fp[0] * texp_a(fp[1] * logT - fp[2] * invT, t.e2) * cm;
+      else pr = Math<R>::ex(fp[8] + fp[1] * logT - fp[2] * invT) * cm / kf;
       const int ifop = (int)fp[7];
       const R fclog = (ifop > 1) ? troe_fclog<R>(t, fp, ifop, T, invT) : (R)0;
       const R pcor = falloff_pcor<R>(t, pr, ifop, fclog);
@@ -567,8 +601,8 @@ __device__ __forceinline__ RxnEval<R> eval_rxn(const Tabs& t, int i, R logT, R i
 // collider factor and prod C_p^nu of CKRATT/CKRATX with the pressure power
 // and the product concentrations folded into b. From 2^900 on, 1/Kc stands
 // at the cap kr = kf / max(Kc, SMALL) as in inv_kc.
-__device__ __forceinline__ double net_rate(unsigned w0, unsigned w1, unsigned w2, bool rev, double kfe,
-                                           const double* C, const double* a, const double* b, const int* en) {
+__device__ __forceinline__ double net_rate_gen(unsigned w0, unsigned w1, unsigned w2, bool rev, double kfe,
+                                               const double* C, const double* a, const double* b, const int* en) {
   double qf = kfe, qr = kfe;
   int ex2 = 0;
 #pragma unroll
@@ -605,31 +639,60 @@ __device__ __forceinline__ double net_rate(unsigned w0, unsigned w1, unsigned w2
   return qf - qr;
 }
 
+// Slot form: three factors per side, absent slots (255) count as 1 (selected
+// on the integer pipe, so every lane issues the same 11 FP64 instructions).
+__device__ __forceinline__ double slot(const double* v, unsigned k) { return k != 255u ? v[k] : 1.0; }
+__device__ __forceinline__ int slot_en(const int* en, unsigned k) { return k != 255u ? en[k] : 0; }
+
+__device__ __forceinline__ double net_rate(unsigned w0, unsigned w1, unsigned w2, bool rev, double kfe,
+                                           const double* C, const double* a, const double* b, const int* en) {
+  if ((w0 >> 24) & F_GEN) return net_rate_gen(w0, w1, w2, rev, kfe, C, a, b, en);
+  const unsigned r0 = sp_of(w0, 0), r1 = sp_of(w0, 1), r2 = sp_of(w0, 2);
+  const unsigned p0 = sp_of(w1, 0), p1 = sp_of(w1, 1), p2 = sp_of(w1, 2);
+  const double qf = (kfe * slot(C, r0)) * (slot(C, r1) * slot(C, r2));
+  if (!rev) return qf;
+  const int ex2 = slot_en(en, r0) + slot_en(en, r1) + slot_en(en, r2) - slot_en(en, p0) - slot_en(en, p1) -
+                  slot_en(en, p2);
+  double qr;
+  if (ex2 >= 900) {
+    // the cap of net_rate_gen: 1/Kc beyond 2^900 stands at 1e300 (pfac powers folded out)
+    qr = ((kfe * 1e300) * slot(C, p0)) * (slot(C, p1) * slot(C, p2));
+  } else {
+    const double fa = slot(a, r0) * (slot(a, r1) * slot(a, r2));
+    const double fb = slot(b, p0) * (slot(b, p1) * slot(b, p2));
+    qr = (ex2 <= -1000) ? 0.0 : (kfe * __hiloint2double((ex2 + 1023) << 20, 0)) * (fa * fb);
+  }
+  return qf - qr;
+}
+
 // The FP64 net rate of reaction i evaluated from scratch (warp path).
 __device__ __forceinline__ double rop_d(const Tabs& t, int i, double logT, double invT, double T, double ctot,
                                        const double* C, const double* a, const double* b, const int* en) {
   const RTabs<double>& x = t.d;
   const unsigned w0 = t.w0[i], w1 = t.w1[i], w2 = t.w2[i];
   const unsigned fl = w0 >> 24;
+  // the concentration products with a unit rate constant first: they do not
+  // depend on the fall-off chain below, which overlaps their latency
+  const double ma = net_rate(w0, w1, w2, (fl & F_REV) != 0, 1.0, C, a, b, en);
   double kf = arrhenius<double>(t, i, fl, logT, invT);
   if (fl & (F_CM | F_KFAL)) {
     const int aux = (int)(w2 >> 24);
     const double cm = collider<double>(t, fl, aux, ctot, C);
     if (fl & F_FALL) {
       const double* fp = x.aux + aux * AUXW;
-      const double k0 = fp[0] * texp_a(fp[1] * logT - fp[2] * invT, t.e2);
+      const double k0kf = fp[0] * texp_a(fp[1] * logT - fp[2] * invT, t.e2);  // k0 / kinf
       const int ifop = (int)fp[7];
       const double fclog = (ifop > 1) ? troe_fclog<double>(t, fp, ifop, T, invT) : 0.0;
-      kf *= falloff_pcor<double>(t, k0 * cm / kf, ifop, fclog);
+      kf *= falloff_pcor_d(t, k0kf * cm, ifop, fclog);
     } else {
       kf *= cm;
     }
   }
-  return net_rate(w0, w1, w2, (fl & F_REV) != 0, kf, C, a, b, en);
+  return kf * ma;
 }
 
 // Net rate of progress of reaction i in FP64 from its precomputed Arrhenius
-// constant kf and, for fall-off, k0[aux] and log10 Fcent fcl[aux]: the
+// constant kf and, for fall-off, k0/kinf [aux] and log10 Fcent fcl[aux]: the
 // concentration-dependent rest of eval_rxn, with the same arithmetic.
 __device__ __forceinline__ double rop_pre(const Tabs& t, int i, double kf, const double* k0a, const double* fcl,
                                           double pfac, double ipfac, double ctot, const double* C, const double* m,
@@ -639,16 +702,16 @@ __device__ __forceinline__ double rop_pre(const Tabs& t, int i, double kf, const
   const unsigned w0 = t.w0[i], w1 = t.w1[i], w2 = t.w2[i];
   const unsigned fl = w0 >> 24;
   const int aux = (int)(w2 >> 24);
+  const double ma = net_rate(w0, w1, w2, (fl & F_REV) != 0, 1.0, C, m, mi, en);
   if (fl & (F_CM | F_KFAL)) {
     const double cm = collider<double>(t, fl, aux, ctot, C);
     if (fl & F_FALL) {
-      const double pr = k0a[aux] * cm / kf;
-      kf *= falloff_pcor<double>(t, pr, (int)t.d.aux[aux * AUXW + 7], fcl[aux]);
+      kf *= falloff_pcor_d(t, k0a[aux] * cm, (int)t.d.aux[aux * AUXW + 7], fcl[aux]);
     } else {
       kf *= cm;
     }
   }
-  return net_rate(w0, w1, w2, (fl & F_REV) != 0, kf, C, m, mi, en);
+  return kf * ma;
 }
 
 // Thermodynamics of species k: its concentration (returned), scaled
@@ -788,7 +851,7 @@ __device__ void rhs64_team(const Tabs& t, const Team<TEAM>& tm, WarpWork& w, con
   const RTabs<double>& x = t.d;
   const int ns = t.ns, tid = tm.tid, wq = tid >> 5, lane = tid & 31;
   double* kfe = tm.pre;       // [352] Arrhenius constants
-  double* k0a = tm.pre + 352; // [64] low-pressure limits, by special-reaction index
+  double* k0a = tm.pre + 352; // [64] k0 / kinf, by special-reaction index
   double* fcl = k0a + 64;     // [64] log10 Fcent
   const double T = y[ns];
   const double logT = tlog(T, t.lg);
@@ -808,11 +871,16 @@ __device__ void rhs64_team(const Tabs& t, const Team<TEAM>& tm, WarpWork& w, con
     const int i = rr * 32 + lane;
     if (i < t.nr) kfe[i] = arrhenius<double>(t, i, t.w0[i] >> 24, logT, invT);
   };
-  double csum = 0.0;
+  double ps[2] = {0.0, 0.0};  // sum C_k, sum Y_k cv_k
   int e0 = 0, e1 = 0;
+  // 1/rho for the production rates, kept in the last cross-warp slot (warp 0
+  // has time to spare in phase 1)
+  if (tid == 0) tm.red[255] = 1.0 / rho;
   if (wq < 2) {
-    for (int k = tid; k < ns; k += 64)
-      csum += species_one<double>(t, k, y, rho, T, logT, invT, pfac, ipfac, w.C, w.m, w.wdot, w.en, w.uR, w.cvm);
+    for (int k = tid; k < ns; k += 64) {
+      ps[0] += species_one<double>(t, k, y, rho, T, logT, invT, pfac, ipfac, w.C, w.m, w.wdot, w.en, w.uR, w.cvm);
+      ps[1] = fma(y[k], w.cvm[k], ps[1]);
+    }
     e0 = wq == 0 ? 0 : 1;
     e1 = wq == 0 ? 1 : 3;
   } else if (wq == 2) {
@@ -836,7 +904,7 @@ __device__ void rhs64_team(const Tabs& t, const Team<TEAM>& tm, WarpWork& w, con
         if (fl & F_FALL) {
           const int aux = (int)(t.w2[i] >> 24);
           const double* fp = x.aux + aux * AUXW;
-          k0a[aux] = fp[0] * texp_a(fp[1] * logT - fp[2] * invT, t.e2);
+          k0a[aux] = fp[0] * texp_a(fp[1] * logT - fp[2] * invT, t.e2);  // k0 / kinf
         }
       }
     }
@@ -844,9 +912,14 @@ __device__ void rhs64_team(const Tabs& t, const Team<TEAM>& tm, WarpWork& w, con
     e1 = nE;
   }
   for (int e = min(e0, nE); e < min(e1, nE); ++e) prep_round(re(e));
-  const double ctot = tm.sum(csum);  // its barriers close phase 1
-  // phase 2: warp 3 takes the fall-off rounds and the last other round,
-  // warps 0-2 the other rounds in turn (all four in turn without fall-off)
+  tm.sumv(ps);  // its barriers close phase 1
+  const double ctot = ps[0];
+  // 1/(rho cv) for dT/dt, on the thread that writes it (warp 0 has time to
+  // spare in phase 2)
+  const double inv_rhocv = tid == 0 ? 1.0 / (rho * ps[1]) : 0.0;
+  // phase 2: warp 3 takes the fall-off rounds (their chain of collider sum,
+  // log, reciprocal and exponential is as long as three plain rounds), warps
+  // 0-2 the other rounds in turn (all four in turn without fall-off)
   auto rate_round = [&](int rr) {
     const int i = rr * 32 + lane;
     w.rop[i] = (i < t.nr) ? rop_pre(t, i, kfe[i], k0a, fcl, pfac, ipfac, ctot, w.C, w.m, w.wdot, w.en) : 0.0;
@@ -854,43 +927,38 @@ __device__ void rhs64_team(const Tabs& t, const Team<TEAM>& tm, WarpWork& w, con
   if (nfr > 0) {
     if (wq == 3) {
       for (int r = 0; r < nfr; ++r) rate_round(fr0 + r);
-      if (nE > 0) rate_round(re(nE - 1));
     } else {
-      for (int e = wq; e < nE - 1; e += 3) rate_round(re(e));
+      for (int e = wq; e < nE; e += 3) rate_round(re(e));
     }
   } else {
     for (int e = wq; e < nE; e += 4) rate_round(e);
   }
   tm.sync();
-  // production rates: each 32-lane piece list split over the four warps,
-  // two accumulators per thread
-  double* p4 = tm.part4;
-  for (int p = t.lane[lane]; p < t.lane[lane + 1]; ++p) {
-    const int e0 = t.pc[p * 3 + 1], e1 = t.pc[p * 3 + 2];
-    double s0 = 0.0, s1 = 0.0;
-    int q = e0 + wq;
-    for (; q + 4 < e1; q += 8) {
-      s0 = fma(x.nu[q], w.rop[t.ent[q]], s0);
-      s1 = fma(x.nu[q + 4], w.rop[t.ent[q + 4]], s1);
-    }
-    if (q < e1) s0 = fma(x.nu[q], w.rop[t.ent[q]], s0);
-    p4[wq * TEAM_PIECES + p] = s0 + s1;
+  // production rates: species k's entries split over an aligned group of
+  // lanes of one warp (a power of two; one lane for most species), the
+  // group's sums added by a shuffle tree, so no cross-warp partials
+  const int4 gl = t.grp[tid];
+  double s0 = 0.0, s1 = 0.0;
+  int q = gl.y;
+  for (; q + 1 < gl.z; q += 2) {
+    s0 = fma(x.nu[q], w.rop[t.ent[q]], s0);
+    s1 = fma(x.nu[q + 1], w.rop[t.ent[q + 1]], s1);
   }
+  if (q < gl.z) s0 = fma(x.nu[q], w.rop[t.ent[q]], s0);
+  double s = s0 + s1;
+  for (int o = 1; o < t.h->gmax; o <<= 1) {
+    const double v = __shfl_xor_sync(0xffffffffu, s, o);
+    if (o < gl.w) s += v;
+  }
+  double su = 0.0;  // u_k/R w_k of the group's species, on its first lane
+  if (gl.x >= 0 && (lane & (gl.w - 1)) == 0) {
+    f[gl.x] = s * x.W[gl.x] * tm.red[255];
+    su = w.uR[gl.x] * s;
+  }
+  su = warp_sum(su);
+  if (lane == 0) tm.red[wq] = su;
   tm.sync();
-  const double irho = 1.0 / rho;
-  double sc[2] = {0.0, 0.0};  // sum u_k/R w_k, sum Y_k cv_k
-  for (int k = tid; k < ns; k += TEAM) {
-    double s = 0.0;
-    for (int q = t.spc[k]; q < t.spc[k + 1]; ++q) {
-      const int pp = t.spp[q];
-      s += ((p4[pp] + p4[TEAM_PIECES + pp]) + p4[2 * TEAM_PIECES + pp]) + p4[3 * TEAM_PIECES + pp];
-    }
-    f[k] = s * x.W[k] * irho;
-    sc[0] = fma(w.uR[k], s, sc[0]);
-    sc[1] = fma(y[k], w.cvm[k], sc[1]);
-  }
-  tm.sumv(sc);
-  if (tid == 0) f[ns] = -sc[0] / (rho * sc[1]);  // RU cancels in u/cv
+  if (tid == 0) f[ns] = -(((tm.red[0] + tm.red[1]) + tm.red[2]) + tm.red[3]) * inv_rhocv;  // RU cancels in u/cv
   tm.sync();
 }
 
@@ -1897,7 +1965,7 @@ int chem_init(ChemState& s, const edyn_mech& m, const ThermoTable& tb, cudaStrea
     if (m.rev[i]) fl |= F_REV;
     if (!(m.beta[i] == 0.0 && m.E_R[i] == 0.0)) fl |= F_EXP;
     unsigned rs = 0, ps = 0, nn = 0;
-    int dnu = 0;
+    int dnu = 0, rord = 0, pord = 0;
     for (int sl = 0; sl < 3; ++sl) {
       const int kr = m.nunk[i][sl], kp = m.nunk[i][3 + sl];
       rs |= (unsigned)(kr >= 0 ? kr : 255) << (8 * sl);
@@ -1907,13 +1975,34 @@ int chem_init(ChemState& s, const edyn_mech& m, const ThermoTable& tb, cudaStrea
         if (v < 1 || v > 3) return (int)cudaErrorInvalidValue;
         nn |= (unsigned)v << (4 * sl);
         dnu -= v;
+        rord += v;
       }
       if (kp >= 0) {
         const int v = m.nu[i][3 + sl];
         if (v < 1 || v > 3) return (int)cudaErrorInvalidValue;
         nn |= (unsigned)v << (12 + 4 * sl);
         dnu += v;
+        pord += v;
       }
+    }
+    if (rord <= 3 && pord <= 3) {
+      // each side as species slots with nu = 1
+      rs = ps = 0xffffffu;
+      nn = 0;
+      int ri = 0, pi = 0;
+      for (int sl = 0; sl < 3; ++sl) {
+        const int kr = m.nunk[i][sl], kp = m.nunk[i][3 + sl];
+        for (int v = kr >= 0 ? -m.nu[i][sl] : 0; v > 0; --v, ++ri) {
+          rs = (rs & ~(0xffu << (8 * ri))) | ((unsigned)kr << (8 * ri));
+          nn |= 1u << (4 * ri);
+        }
+        for (int v = kp >= 0 ? m.nu[i][3 + sl] : 0; v > 0; --v, ++pi) {
+          ps = (ps & ~(0xffu << (8 * pi))) | ((unsigned)kp << (8 * pi));
+          nn |= 1u << (12 + 4 * pi);
+        }
+      }
+    } else {
+      fl |= F_GEN;
     }
     // net stoichiometry per distinct species
     int ks[6], nus[6], nk = 0;
@@ -2019,6 +2108,45 @@ int chem_init(ChemState& s, const edyn_mech& m, const ThermoTable& tb, cudaStrea
       if (pieces[p].k == k) spp.push_back(slot_of[p]);
   }
   for (int k = ns; k <= NSMAX; ++k) spc[k] = (int)spp.size();
+  // four-warp teams: species k's entries over an aligned group of g_k lanes
+  // (a power of two, within one warp); the group of the species with the
+  // most entries per lane doubles while the 128 lanes allow
+  std::vector<int> eb(ns), en_(ns), gk(ns, 1);
+  {
+    int b = 0;
+    for (int k = 0; k < ns; ++k) {
+      eb[k] = b;
+      en_[k] = (int)per_sp[k].size();
+      b += en_[k];
+    }
+  }
+  if (ns > TEAM) return (int)cudaErrorInvalidValue;
+  for (int used = ns;;) {
+    int kb = 0;
+    for (int k = 1; k < ns; ++k)
+      if ((en_[k] + gk[k] - 1) / gk[k] > (en_[kb] + gk[kb] - 1) / gk[kb]) kb = k;
+    if (gk[kb] >= 32 || used + gk[kb] > TEAM) break;
+    used += gk[kb];
+    gk[kb] *= 2;
+  }
+  std::vector<int> byg(ns);
+  for (int k = 0; k < ns; ++k) byg[k] = k;
+  std::stable_sort(byg.begin(), byg.end(), [&](int a, int b) { return gk[a] > gk[b]; });
+  std::vector<int> grp(4 * TEAM, 0);
+  for (int l = 0; l < TEAM; ++l) { grp[4 * l] = -1; grp[4 * l + 3] = 1; }
+  int gmax = 1;
+  for (int off = 0, z = 0; z < ns; ++z) {
+    const int k = byg[z], g = gk[k], per = (en_[k] + g - 1) / g;
+    for (int j = 0; j < g; ++j) {
+      const int l = off + j;
+      grp[4 * l] = k;
+      grp[4 * l + 1] = eb[k] + std::min(en_[k], j * per);
+      grp[4 * l + 2] = eb[k] + std::min(en_[k], (j + 1) * per);
+      grp[4 * l + 3] = g;
+    }
+    off += g;  // sizes descending: every offset is a multiple of the group size
+    gmax = std::max(gmax, g);
+  }
   // species tables
   std::vector<double> W(NSMAX, 1.0), invW(NSMAX, 0.0), tmid(NSMAX, 1000.0), hf(NSMAX, 0.0);
   std::vector<double> cs(2 * 7 * NSMAX, 0.0), ch(2 * 6 * NSMAX, 0.0), cpt(2 * 5 * NSMAX, 0.0);
@@ -2082,6 +2210,8 @@ int chem_init(ChemState& s, const edyn_mech& m, const ThermoTable& tb, cudaStrea
   h.o_lane = bl.put(lane.data(), lane.size() * 4);
   h.o_spc = bl.put(spc.data(), spc.size() * 4);
   h.o_spp = bl.put(spp.data(), std::max<size_t>(4, spp.size() * 4));
+  h.o_grp = bl.put(grp.data(), grp.size() * 4);
+  h.gmax = gmax;
   h.o_ent = bl.put(ent_idx.data(), std::max<size_t>(4, ent_idx.size() * 4));
   auto put2 = [&](int* off, const std::vector<double>& v) {
     std::vector<double> d(v);
@@ -2095,7 +2225,24 @@ int chem_init(ChemState& s, const edyn_mech& m, const ThermoTable& tb, cudaStrea
   put2(h.o_lnA, lnA);  // FP32 path uses ln A, FP64 path uses A
   put2(h.o_B, B);
   put2(h.o_E, E);
-  put2(h.o_aux, aux);
+  {
+    // FP64 fall-off rows: k0/kinf = (lowA/A) exp((lowB - B) ln T - (lowE - E)/T),
+    // so the reduced pressure needs no division
+    std::vector<double> d(aux);
+    if (d.empty()) d.push_back(0.0);
+    std::vector<float> f(d.size());
+    for (size_t q = 0; q < d.size(); ++q) f[q] = (float)d[q];
+    for (int q = 0; q < nr; ++q) {
+      const int i = order[q];
+      if (m.tb[i] != EDYN_TB_FALLOFF) continue;
+      double* fp = d.data() + (size_t)(w2[q] >> 24) * AUXW;
+      fp[0] = m.A[i] > 0.0 ? m.low[i][0] / m.A[i] : 0.0;
+      fp[1] = m.low[i][1] - m.beta[i];
+      fp[2] = m.low[i][2] - m.E_R[i];
+    }
+    h.o_aux[0] = bl.put(d.data(), d.size() * 8);
+    h.o_aux[1] = bl.put(f.data(), f.size() * 4);
+  }
   put2(h.o_tb_am1, tb_am1);
   put2(h.o_W, W);
   put2(h.o_invW, invW);

@@ -254,6 +254,21 @@ struct Team {
   }
 };
 
+// Producer / consumer named barriers between two warps of a four-warp team
+// (ids 2 and 3; the team itself uses id 1): the producer arrives without
+// waiting, the consumer waits until the producer's earlier shared-memory
+// writes are visible.
+constexpr int BAR_FALL_PR = 2;  // warp 2 -> warp 3: Pr and log10 Pr of the fall-off slots
+constexpr int BAR_FALL_MA = 3;  // warp 1 -> warp 3: their concentration products
+__device__ __forceinline__ void pair_arrive(int id) {
+  __syncwarp();
+  asm volatile("bar.arrive %0, 64;" ::"r"(id) : "memory");
+}
+__device__ __forceinline__ void pair_wait(int id) {
+  __syncwarp();
+  asm volatile("bar.sync %0, 64;" ::"r"(id) : "memory");
+}
+
 template <class R>
 struct Math;
 template <>
@@ -507,10 +522,13 @@ __device__ __forceinline__ R falloff_pcor(const Tabs& t, R pr, int ifop, R fclog
 // 1 + (c/d)^2 is e/d^2 for e = d^2 + c^2, and 1/((1 + Pr) e) gives both
 // 1/(1 + Pr) and 1/e. The same quantities as falloff_pcor<double> up to
 // rounding; beyond Pr = 1e150 the two reciprocals are taken apart.
-__device__ __forceinline__ double falloff_pcor_d(const Tabs& t, double pr, int ifop, double fclog) {
+__device__ __forceinline__ double log10_pr(const Tabs& t, double pr) {
+  return tlog(fmax(pr, Math<double>::small()), t.lg) * 0.43429448190325182765;
+}
+
+// The Troe branch of falloff_pcor_d from Pr and log10 Pr.
+__device__ __forceinline__ double troe_pcor_d(const Tabs& t, double pr, double prlog, double fclog) {
   const double p1 = 1.0 + pr;
-  if (ifop <= 1) return pr / p1;
-  const double prlog = tlog(fmax(pr, Math<double>::small()), t.lg) * 0.43429448190325182765;
   const double c = prlog - ((double)0.4f + (double)0.67f * fclog);
   const double d = (0.75 - (double)1.27f * fclog) - (double)0.14f * c;
   const double d2 = d * d;
@@ -526,6 +544,11 @@ __device__ __forceinline__ double falloff_pcor_d(const Tabs& t, double pr, int i
   }
   const double flog = (fclog * d2) * inv_e;
   return texp_a(2.302585092994045684 * flog, t.e2) * (pr * inv_p1);  // 10^flog Pr/(1+Pr)
+}
+
+__device__ __forceinline__ double falloff_pcor_d(const Tabs& t, double pr, int ifop, double fclog) {
+  if (ifop <= 1) return pr / (1.0 + pr);
+  return troe_pcor_d(t, pr, log10_pr(t, pr), fclog);
 }
 
 // mass-action products (CKRATX 6900-6915)
@@ -917,18 +940,66 @@ __device__ void rhs64_team(const Tabs& t, const Team<TEAM>& tm, WarpWork& w, con
   // 1/(rho cv) for dT/dt, on the thread that writes it (warp 0 has time to
   // spare in phase 2)
   const double inv_rhocv = tid == 0 ? 1.0 / (rho * ps[1]) : 0.0;
-  // phase 2: warp 3 takes the fall-off rounds (their chain of collider sum,
-  // log, reciprocal and exponential is as long as three plain rounds), warps
-  // 0-2 the other rounds in turn (all four in turn without fall-off)
+  // phase 2: the fall-off chain (collider sum, log10 Pr, the Troe factor
+  // with its reciprocal and exponential) is split over three warps: warp 2
+  // forms Pr and log10 Pr, warp 1 the concentration products, warp 3 the
+  // Troe factor and the rates; round e of the other rounds goes to warp e % 4
+  // (warp 3's before its waits)
   auto rate_round = [&](int rr) {
     const int i = rr * 32 + lane;
     w.rop[i] = (i < t.nr) ? rop_pre(t, i, kfe[i], k0a, fcl, pfac, ipfac, ctot, w.C, w.m, w.wdot, w.en) : 0.0;
   };
   if (nfr > 0) {
+    double* fpr = tm.part4;  // [nfr][64]: Pr, then kf pcor; log10 Pr (fall-off slots)
+    if (wq == 2) {
+      for (int r = 0; r < nfr; ++r) {
+        const int i = (fr0 + r) * 32 + lane;
+        const unsigned fl = i < t.nr ? t.w0[i] >> 24 : 0u;
+        if (fl & F_FALL) {
+          const int aux = (int)(t.w2[i] >> 24);
+          const double pr = k0a[aux] * collider<double>(t, fl, aux, ctot, w.C);
+          fpr[r * 64 + lane] = pr;
+          fpr[r * 64 + 32 + lane] = log10_pr(t, pr);
+        }
+      }
+      pair_arrive(BAR_FALL_PR);
+    } else if (wq == 1) {
+      for (int r = 0; r < nfr; ++r) {
+        const int i = (fr0 + r) * 32 + lane;
+        if (i < t.nr) {
+          const unsigned w0 = t.w0[i];
+          w.rop[i] = net_rate(w0, t.w1[i], t.w2[i], ((w0 >> 24) & F_REV) != 0, 1.0, w.C, w.m, w.wdot, w.en);
+        } else {
+          w.rop[i] = 0.0;
+        }
+      }
+      pair_arrive(BAR_FALL_MA);
+    }
+    for (int e = wq; e < nE; e += 4) rate_round(re(e));
     if (wq == 3) {
-      for (int r = 0; r < nfr; ++r) rate_round(fr0 + r);
-    } else {
-      for (int e = wq; e < nE; e += 3) rate_round(re(e));
+      pair_wait(BAR_FALL_PR);
+      for (int r = 0; r < nfr; ++r) {
+        const int i = (fr0 + r) * 32 + lane;
+        double kp = 0.0;
+        if (i < t.nr) {
+          const unsigned fl = t.w0[i] >> 24;
+          const int aux = (int)(t.w2[i] >> 24);
+          kp = kfe[i];
+          if (fl & F_FALL) {
+            const double pr = fpr[r * 64 + lane];
+            kp *= ((int)t.d.aux[aux * AUXW + 7] > 1) ? troe_pcor_d(t, pr, fpr[r * 64 + 32 + lane], fcl[aux])
+                                                     : pr / (1.0 + pr);
+          } else if (fl & (F_CM | F_KFAL)) {
+            kp *= collider<double>(t, fl, aux, ctot, w.C);
+          }
+        }
+        fpr[r * 64 + lane] = kp;
+      }
+      pair_wait(BAR_FALL_MA);
+      for (int r = 0; r < nfr; ++r) {
+        const int i = (fr0 + r) * 32 + lane;
+        w.rop[i] = fpr[r * 64 + lane] * w.rop[i];
+      }
     }
   } else {
     for (int e = wq; e < nE; e += 4) rate_round(e);

@@ -1256,123 +1256,126 @@ __device__ bool gj_invert_warp(float* A, int* perm, float* col, int n, int lane)
   return ok;
 }
 
-// The same inversion by a four-warp team, with the matrix in registers: thread
-// t holds rows rg + 8a (a < 7) and columns cg + 16b (b < 4), rg = t % 8,
-// cg = t / 8, of an up-to-56 x 64 tile. Pivoting is implicit: the pivot of
-// column k is the largest remaining entry among the rows not yet used, and no
-// rows move; the pivot column and row travel through double-buffered shared
-// memory, so a step costs two barriers. With pivot rows p_k the result B
-// satisfies inv(A)[k][p_j] = B[p_k][j], which the write-back applies.
+// The same inversion by a four-warp team, column by column: lanes 2j and
+// 2j+1 hold column j of the working matrix in registers, rows h*GJ_HALF + q
+// (h = lane parity, q < GJ_HALF). Pivoting is implicit: the pivot of column
+// k is the largest remaining entry among the rows not yet used (lowest row
+// on ties), and no rows move. At step k the owner pair of column k finds the
+// pivot (one shuffle) and publishes the column through double-buffered
+// shared memory, so a step costs one barrier; every pair then takes its
+// pivot-row entry from its own registers and updates its column. With pivot
+// rows p_k the result B satisfies inv(A)[k][p_j] = B[p_k][j], which the
+// write-back applies.
+constexpr int GJ_HALF = 28;  // rows per lane: columns of up to 56 rows
 __device__ bool gj_invert_team(const Team<TEAM>& tm, float* A, int* perm, float* col, int n) {
   (void)col;
-  const int tid = tm.tid;
-  const int rg = tid & 7, cg = tid >> 3;
-  float* colb = reinterpret_cast<float*>(tm.red);          // [2][64]
-  float* rowb = colb + 128;                                // [2][64]
-  float* cval = rowb + 128;                                // [2][8]
-  int* crow = reinterpret_cast<int*>(cval + 16);           // [2][8]
-  int* pinv = crow + 16;                                   // [64]
-  float B[7][4];
+  const int tid = tm.tid, j = tid >> 1, h = tid & 1, r0 = h * GJ_HALF;
+  const unsigned pair = 3u << (tid & 30);
+  float* colk = reinterpret_cast<float*>(tm.red);       // [2][64]: column k of step k
+  int* pinfo = reinterpret_cast<int*>(colk + 128);      // [2][2]: pivot row, nonsingular flag
+  float c[GJ_HALF];
+  unsigned usedl = 0u;  // bit q: row r0 + q is a pivot row already, or beyond n
 #pragma unroll
-  for (int a = 0; a < 7; ++a)
-#pragma unroll
-    for (int b = 0; b < 4; ++b) {
-      const int i = rg + 8 * a, j = cg + 16 * b;
-      B[a][b] = (i < n && j < n) ? A[i * JS + j] : 0.f;
-    }
-  unsigned long long used = 0ull;
+  for (int q = 0; q < GJ_HALF; ++q) {
+    const bool in = j < n && r0 + q < n;
+    c[q] = in ? A[(r0 + q) * JS + j] : 0.f;
+    usedl |= (r0 + q < n) ? 0u : (1u << q);
+  }
   bool ok = true;
+  // the owner pair of column k publishes it and the pivot among the unused
+  // rows: a pairwise tree over the lane's rows (the left half of every pair
+  // holds the lower rows, so ties keep the lowest row), then the pair
+  auto publish = [&](int k) {
+    const int buf = k & 1;
+    float4* dst = reinterpret_cast<float4*>(colk + buf * 64 + r0);
+#pragma unroll
+    for (int v = 0; v < GJ_HALF / 4; ++v) dst[v] = make_float4(c[4 * v], c[4 * v + 1], c[4 * v + 2], c[4 * v + 3]);
+    float bv[32];
+    int bi[32];
+#pragma unroll
+    for (int q = 0; q < 32; ++q) {
+      bv[q] = (q < GJ_HALF && !((usedl >> q) & 1u)) ? fabsf(c[q < GJ_HALF ? q : 0]) : -1.f;
+      bi[q] = q;
+    }
+#pragma unroll
+    for (int st = 1; st < 32; st <<= 1)
+#pragma unroll
+      for (int q = 0; q + st < 32; q += 2 * st) {
+        const bool take = bv[q + st] > bv[q];
+        bv[q] = take ? bv[q + st] : bv[q];
+        bi[q] = take ? bi[q + st] : bi[q];
+      }
+    float b = bv[0];
+    int i = (b >= 0.f) ? r0 + bi[0] : n;
+    const float ov = __shfl_xor_sync(pair, b, 1);
+    const int oi = __shfl_xor_sync(pair, i, 1);
+    if (ov > b || (ov == b && oi < i)) { b = ov; i = oi; }
+    if (h == 0) {
+      pinfo[buf * 2] = i;
+      pinfo[buf * 2 + 1] = (b > 0.f && i < n) ? 1 : 0;
+    }
+  };
+  if (j == 0) publish(0);
   for (int k = 0; k < n; ++k) {
     const int buf = k & 1;
-    const int kb = k >> 4;
-    if (cg == (k & 15)) {
-      // owners of column k: publish it, and their best remaining row
-      float bv = -1.f;
-      int bi = n;
-#pragma unroll
-      for (int a = 0; a < 7; ++a) {
-        const int i = rg + 8 * a;
-        float v = 0.f;
-#pragma unroll
-        for (int b = 0; b < 4; ++b)
-          if (b == kb) v = B[a][b];
-        if (i < n) {
-          colb[buf * 64 + i] = v;
-          const float av = fabsf(v);
-          if (!((used >> i) & 1ull) && av > bv) { bv = av; bi = i; }
-        }
-      }
-      cval[buf * 8 + rg] = bv;
-      crow[buf * 8 + rg] = bi;
-    }
     tm.sync();
-    // the pivot: largest candidate, lowest row on ties (loads first, then selects)
-    float cv8[8];
-    int cr8[8];
-#pragma unroll
-    for (int q = 0; q < 8; ++q) {
-      cv8[q] = cval[buf * 8 + q];
-      cr8[q] = crow[buf * 8 + q];
-    }
-    float bv = cv8[0];
-    int p = cr8[0];
-#pragma unroll
-    for (int q = 1; q < 8; ++q) {
-      const bool take = cv8[q] > bv || (cv8[q] == bv && cr8[q] < p);
-      bv = take ? cv8[q] : bv;
-      p = take ? cr8[q] : p;
-    }
-    if (!(bv > 0.f) || p >= n) { ok = false; p = (p >= n) ? k : p; }
-    const int ap = p >> 3;
-    if (rg == (p & 7)) {
-      // owners of row p: publish it
-#pragma unroll
-      for (int b = 0; b < 4; ++b) {
-        float v = B[0][b];
-#pragma unroll
-        for (int a = 1; a < 7; ++a) v = (a == ap) ? B[a][b] : v;
-        rowb[buf * 64 + cg + 16 * b] = v;
-      }
-    }
+    int p = pinfo[buf * 2];
+    if (!pinfo[buf * 2 + 1]) { ok = false; p = (p >= n) ? k : p; }
     if (tid == 0) perm[k] = p;
-    tm.sync();
-    // update: all shared loads first, then branch-free selects
-    float ci[7], rk[4];
+    const float inv = 1.f / colk[buf * 64 + p];
+    // this column's entry in the pivot row: a binary select on the bits of
+    // qs in the lane that holds row p, zero in the other, then the pair
+    const int qs = p - r0;
+    const bool here = qs >= 0 && qs < GJ_HALF;
+    float t16[16];
 #pragma unroll
-    for (int a = 0; a < 7; ++a) ci[a] = colb[buf * 64 + min(rg + 8 * a, 63)];
+    for (int q = 0; q < 16; ++q) t16[q] = (qs & 16) ? c[q + 16 < GJ_HALF ? q + 16 : 0] : c[q];
 #pragma unroll
-    for (int b = 0; b < 4; ++b) rk[b] = rowb[buf * 64 + cg + 16 * b];
-    const float inv = 1.f / colb[buf * 64 + p];
+    for (int q = 0; q < 8; ++q) t16[q] = (qs & 8) ? t16[q + 8] : t16[q];
 #pragma unroll
-    for (int b = 0; b < 4; ++b) rk[b] *= inv;
+    for (int q = 0; q < 4; ++q) t16[q] = (qs & 4) ? t16[q + 4] : t16[q];
 #pragma unroll
-    for (int a = 0; a < 7; ++a) {
-      const bool rp = (rg + 8 * a) == p;
+    for (int q = 0; q < 2; ++q) t16[q] = (qs & 2) ? t16[q + 2] : t16[q];
+    const float mine = here ? ((qs & 1) ? t16[1] : t16[0]) : 0.f;
+    const float rp = mine + __shfl_xor_sync(0xffffffffu, mine, 1);  // every lane of the warp is here
+    const bool isk = (j == k);
+    const float rj = isk ? inv : rp * inv;
+    if (isk) {
 #pragma unroll
-      for (int b = 0; b < 4; ++b) {
-        const bool ck = (cg + 16 * b) == k;
-        const float other = ck ? -ci[a] * inv : fmaf(-ci[a], rk[b], B[a][b]);
-        const float prow = ck ? inv : B[a][b] * inv;
-        B[a][b] = rp ? prow : other;
+      for (int q = 0; q < GJ_HALF; ++q) c[q] = 0.f;
+    }
+    const float4* cb = reinterpret_cast<const float4*>(colk + buf * 64 + r0);
+#pragma unroll
+    for (int v = 0; v < GJ_HALF / 4; ++v) {
+      const float4 ck = cb[v];
+      const float cv[4] = {ck.x, ck.y, ck.z, ck.w};
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int q = 4 * v + u;
+        c[q] = (q == qs) ? rj : fmaf(-cv[u], rj, c[q]);
       }
     }
-    used |= 1ull << p;
+    usedl |= here ? (1u << qs) : 0u;
+    if (j == k + 1 && k + 1 < n) publish(k + 1);
   }
-  // write back the inverse: inv(A)[k][p_j] = B[p_k][j]
-  if (tid < 64) pinv[tid] = 0;
-  tm.sync();
-  for (int k = tid; k < n; k += TEAM) pinv[perm[k]] = k;
+  // write back the inverse: inv(A)[k][p_j] = B[p_k][j], through A in the
+  // natural layout
   tm.sync();
 #pragma unroll
-  for (int a = 0; a < 7; ++a) {
-    const int r = rg + 8 * a;
-    if (r >= n) continue;
-    const int kk = pinv[r];
+  for (int q = 0; q < GJ_HALF; ++q)
+    if (j < n && r0 + q < n) A[(r0 + q) * JS + j] = c[q];
+  tm.sync();
 #pragma unroll
-    for (int b = 0; b < 4; ++b) {
-      const int j = cg + 16 * b;
-      if (j < n) A[kk * JS + perm[j]] = B[a][b];
-    }
+  for (int q = 0; q < GJ_HALF; ++q) {
+    const int k = r0 + q;
+    c[q] = (j < n && k < n) ? A[perm[k] * JS + j] : 0.f;
+  }
+  tm.sync();
+  if (j < n) {
+    const int pj = perm[j];
+#pragma unroll
+    for (int q = 0; q < GJ_HALF; ++q)
+      if (r0 + q < n) A[(r0 + q) * JS + pj] = c[q];
   }
   tm.sync();
   return ok;

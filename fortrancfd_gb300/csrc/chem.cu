@@ -1445,7 +1445,8 @@ struct CellStats {
 };
 
 constexpr float THETA_JAC = 0.1f;  // Newton contraction above which a kept Jacobian is rebuilt
-constexpr int JAC_MAX_AGE = 10;    // accepted steps a kept Jacobian serves at most
+constexpr int JAC_MAX_AGE = 20;    // accepted steps a kept Jacobian serves at most
+constexpr double M_REUSE = 0.5;    // a kept inverse serves while |h / h_m - 1| stays within this
 
 // Integrates w.y0 over [0, dt] with SDIRK4. Returns the statistics.
 template <int TW>
@@ -1463,11 +1464,11 @@ __device__ CellStats integrate(const Tabs& t, const Team<TW>& tm, WarpWork& w, c
   float* Jd = keep_jac ? tm.jsave : w.J;
   bool jac_fresh = false;  // Jacobian evaluated at the current y0
   int jac_age = 0;         // accepted steps since it was evaluated
-  double h_want = h;       // step size before truncation at the window end
-  // The inverted Newton matrix in w.J stays valid while h, the Jacobian and
-  // the scaling it was built with are unchanged: after a step whose Newton
-  // iterations contracted fast, a proposed growth of h by 0-20 % keeps h
-  // instead and reuses the matrix (Hairer and Wanner, Solving ODEs II, IV.8).
+  // The inverted Newton matrix I - g h_m J (in w.J) keeps serving the
+  // simplified Newton iteration, and the error filter, while the Jacobian is
+  // kept and h stays within 50 % of h_m: the iteration is inexact anyway and
+  // converges slightly slower, for far fewer inversions (Hairer and Wanner,
+  // Solving ODEs II, IV.8). A Newton failure rebuilds it.
   bool m_ok = false;
   double h_m = 0.0;
   // The first accepted step of the window starts the next one: a cell at a
@@ -1477,7 +1478,6 @@ __device__ CellStats integrate(const Tabs& t, const Team<TW>& tm, WarpWork& w, c
   const double g = 0.25;
   while (tcur < c.dt) {
     if (st.steps + st.rejects >= max_steps) { st.failed = true; break; }
-    h_want = h;
     if (tcur + h > c.dt) h = c.dt - tcur;
     // f0 = f(y0) in FP64 at the window start; later the last stage
     // derivative of the accepted step (kept across rejections)
@@ -1505,7 +1505,7 @@ __device__ CellStats integrate(const Tabs& t, const Team<TW>& tm, WarpWork& w, c
         }
       }
     }
-    const bool form_m = need_jac || !m_ok || h != h_m;
+    const bool form_m = need_jac || !m_ok || fabs(h - h_m) > M_REUSE * h_m;
     if (need_jac) {
       jacobian32<TW>(t, tm, w, w.y0, c.rho_cgs, Jd);
       st.jac++;
@@ -1638,15 +1638,8 @@ __device__ CellStats integrate(const Tabs& t, const Team<TW>& tm, WarpWork& w, c
       // on the shorter step; the step size wanted before the cut stands too
       jac_fresh = false;
       ++jac_age;
-      const bool jac_next = !keep_jac || theta_max > THETA_JAC || jac_age >= JAC_MAX_AGE;
-      const bool hold = q >= 1.f && q <= 1.2f && theta_max <= THETA_JAC && (keep_jac ? !jac_next : true) &&
-                        h == h_want;
-      if (hold) {
-        need_jac = false;  // h and the inverted matrix stay
-      } else {
-        h = hprop;
-        need_jac = jac_next;
-      }
+      h = hprop;
+      need_jac = !keep_jac || theta_max > THETA_JAC || jac_age >= JAC_MAX_AGE;
     } else {
       st.rejects++;
       h = h * (double)fminf(1.f, fmaxf(0.2f, fac));

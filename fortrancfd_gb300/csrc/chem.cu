@@ -171,7 +171,8 @@ struct alignas(16) WarpWork {
   int en[NV];
   float J[54 * JS];   // Jacobian, then the inverse of the scaled Newton matrix
   float b32[NV];
-  float sc32[NV];     // error weights atol + rtol |y0| of the current step
+  float sc32[NV];     // error weights atol + rtol |y0| of the current Newton matrix
+  float isc32[NV];    // their reciprocals
   float col[NV];      // pivot column during the inversion
   int piv[NV];
   float f1[NV], f2[NV];
@@ -1433,6 +1434,42 @@ __device__ __forceinline__ void gemv_solve(const Team<TW>& tm, const float* A, f
   }
 }
 
+// One simplified-Newton correction at the iterate Y with f(Y) in fy: the
+// scaled residual b = -(Y - sv - hg f) / sc, b <- M^-1 b, Y += b sc; returns
+// the RMS of the scaled correction b. A four-warp team updates Y and forms
+// the norm where the product lands, inside the product's two barriers.
+template <int TW>
+__device__ __forceinline__ float newton_correct(const Team<TW>& tm, WarpWork& w, double hg, int n) {
+  for (int i = tm.tid; i < n; i += TW) w.b32[i] = (float)(hg * w.fy[i] - (w.Y[i] - w.sv[i])) * w.isc32[i];
+  tm.sync();
+  float ss = 0.f;
+  if constexpr (TW == 32) {
+    gemv_solve_warp(w.J, w.b32, n, tm.tid);
+    for (int i = tm.tid; i < n; i += 32) {
+      const float q = w.b32[i];
+      ss = fmaf(q, q, ss);
+      w.Y[i] += (double)q * (double)w.sc32[i];
+    }
+    __syncwarp();
+    return sqrtf(tm.sum(ss) / (float)n);
+  } else {
+    const int i = tm.tid >> 1, hh = tm.tid & 1;
+    float a = 0.f;
+    if (i < n)
+      for (int j = hh; j < n; j += 2) a = fmaf(w.J[i * JS + j], w.b32[j], a);
+    a += __shfl_xor_sync(0xffffffffu, a, 1);
+    ss = warp_sum((i < n && hh == 0) ? a * a : 0.f);
+    tm.sync();
+    if (i < n && hh == 0) {
+      w.b32[i] = a;
+      w.Y[i] += (double)a * (double)w.sc32[i];
+    }
+    if ((tm.tid & 31) == 0) tm.red[16 + (tm.tid >> 5)] = (double)ss;
+    tm.sync();
+    return sqrtf((float)(((tm.red[16] + tm.red[17]) + tm.red[18]) + tm.red[19]) / (float)n);
+  }
+}
+
 struct Cell {
   double rho_cgs, dt, rtol, atol;
   double h0;  // first step size to try (<= dt)
@@ -1519,7 +1556,10 @@ __device__ CellStats integrate(const Tabs& t, const Team<TW>& tm, WarpWork& w, c
     // rejection).
     bool newton_ok = true;
     if (form_m) {
-      for (int i = lane; i < n; i += TW) w.sc32[i] = (float)(c.atol + c.rtol * fabs(w.y0[i]));
+      for (int i = lane; i < n; i += TW) {
+        w.sc32[i] = (float)(c.atol + c.rtol * fabs(w.y0[i]));
+        w.isc32[i] = 1.f / w.sc32[i];
+      }
       tm.sync();
       for (int q = lane; q < n * JS; q += TW) {
         const int i = q / JS, j = q - i * JS;
@@ -1557,16 +1597,9 @@ __device__ CellStats integrate(const Tabs& t, const Team<TW>& tm, WarpWork& w, c
         if (!(Tn > 100.0 && Tn < 8000.0)) break;
         rhs64<TW>(t, tm, w, w.Y, c.rho_cgs, w.fy);
         st.rhs++;
-        for (int i = lane; i < n; i += TW)
-          w.b32[i] = (float)(-(w.Y[i] - w.sv[i] - h * g * w.fy[i]) / (double)w.sc32[i]);
-        tm.sync();
-        gemv_solve<TW>(tm, w.J, w.b32, n);
-        float ss = 0.f;
-        for (int i = lane; i < n; i += TW) {
-          const float q = w.b32[i];  // scaled correction
-          ss = fmaf(q, q, ss);
-        }
-        const float nrm = sqrtf(tm.sum(ss) / (float)n);
+        // the correction is applied to Y at once: on convergence Y is rebuilt
+        // from f below, on failure the step is redone
+        const float nrm = newton_correct<TW>(tm, w, h * g, n);
         if (!(nrm == nrm)) break;
         // convergence: weighted correction below 1e-2 of the local
         // tolerance, directly or predicted from the contraction rate; one
@@ -1589,8 +1622,6 @@ __device__ CellStats integrate(const Tabs& t, const Team<TW>& tm, WarpWork& w, c
           tm.sync();
           break;
         }
-        for (int i = lane; i < n; i += TW) w.Y[i] += (double)w.b32[i] * (double)w.sc32[i];
-        tm.sync();
         nrm_prev = nrm;
       }
       if (!conv) { newton_ok = false; break; }
@@ -1607,14 +1638,14 @@ __device__ CellStats integrate(const Tabs& t, const Team<TW>& tm, WarpWork& w, c
     for (int i = lane; i < n; i += TW) {
       double e = 0.0;
       for (int j = 0; j < 5; ++j) e = fma(c_se[j], w.F[j][i], e);
-      w.b32[i] = (float)(h * e / (double)w.sc32[i]);
+      w.b32[i] = (float)(h * e) * w.isc32[i];
     }
     tm.sync();
     gemv_solve<TW>(tm, w.J, w.b32, n);
     float ss = 0.f;
     for (int i = lane; i < n; i += TW) {
-      const double sc = c.atol + c.rtol * fmax(fabs(w.y0[i]), fabs(w.Y[i]));
-      const float q = (float)((double)w.b32[i] * (double)w.sc32[i] / sc);
+      const float sc = (float)(c.atol + c.rtol * fmax(fabs(w.y0[i]), fabs(w.Y[i])));
+      const float q = w.b32[i] * w.sc32[i] / sc;
       ss = fmaf(q, q, ss);
     }
     const float en = sqrtf(tm.sum(ss) / (float)n);
@@ -1851,17 +1882,25 @@ __device__ int tube_cell(const Tabs& t, const Team<TW>& tm, WarpWork& w, const C
 // this launch (the reaction front moves under a cell per step), the costliest
 // power-of-two classes first, at most HOT_MAX, listed in cell order. Run by
 // the last CTA of a launch, after every cell's cost is written.
-__device__ void select_hot(const int* cost, int n, unsigned* hot, unsigned* scratch) {
+__device__ void select_hot(const int* cost, int n, unsigned* hot, unsigned* scratch, int scratch_words) {
   unsigned* hist = scratch;        // [33]
   unsigned* cnt = scratch + 40;    // [blockDim]
   const int nt = blockDim.x, tid = threadIdx.x;
   for (int b = tid; b < 33; b += nt) hist[b] = 0;
+  // the costs staged in shared memory when they fit (independent loads, many
+  // in flight), so the passes below do not wait on L2 cell by cell
+  int* sc = reinterpret_cast<int*>(scratch + 512);
+  const bool staged = n <= scratch_words - 512;
+  if (staged) {
+#pragma unroll 8
+    for (int i = tid; i < n; i += nt) sc[i] = __ldcg(cost + i);
+  }
   __syncthreads();
   const int chunk = (n + nt - 1) / nt;
   const int c0 = min(n, tid * chunk), c1 = min(n, c0 + chunk);
   auto nmax = [&](int i) {
     int m = 0;
-    for (int j = max(0, i - 2); j <= min(n - 1, i + 2); ++j) m = max(m, __ldcg(cost + j));
+    for (int j = max(0, i - 2); j <= min(n - 1, i + 2); ++j) m = max(m, staged ? sc[j] : __ldcg(cost + j));
     return m;
   };
   for (int i = c0; i < c1; ++i) {
@@ -1970,7 +2009,8 @@ __global__ void __launch_bounds__(MAXW * 32, 1)
       *L.time = *L.time + dt;
       *L.nsteps = *L.nsteps + 1;
     }
-    if (L.cost && L.hot) select_hot(L.cost, L.n, L.hot, reinterpret_cast<unsigned*>(ww));
+    if (L.cost && L.hot)
+      select_hot(L.cost, L.n, L.hot, reinterpret_cast<unsigned*>(ww), (int)(nwarps * sizeof(WarpWork) / 4));
   }
 }
 

@@ -255,12 +255,11 @@ struct Team {
   }
 };
 
-// Producer / consumer named barriers between two warps of a four-warp team
-// (ids 2 and 3; the team itself uses id 1): the producer arrives without
+// A producer / consumer named barrier between two warps of a four-warp team
+// (id 2; the team itself uses id 1): the producer arrives without
 // waiting, the consumer waits until the producer's earlier shared-memory
 // writes are visible.
-constexpr int BAR_FALL_PR = 2;  // warp 2 -> warp 3: Pr and log10 Pr of the fall-off slots
-constexpr int BAR_FALL_MA = 3;  // warp 1 -> warp 3: their concentration products
+constexpr int BAR_FALL_MA = 2;  // warp 1 -> warp 3: the fall-off concentration products
 __device__ __forceinline__ void pair_arrive(int id) {
   __syncwarp();
   asm volatile("bar.arrive %0, 64;" ::"r"(id) : "memory");
@@ -740,13 +739,13 @@ __device__ __forceinline__ double rop_pre(const Tabs& t, int i, double kf, const
 
 // Thermodynamics of species k: its concentration (returned), scaled
 // exp(S/R - H/RT) and its reciprocal, u_k/R and cv_k/(R W_k).
-template <class R>
+template <class R, bool STORE_C = true>
 __device__ __forceinline__ R species_one(const Tabs& t, int k, const R* y, R rho, R T, R logT, R invT, R pfac,
                                          R ipfac, R* C, R* m, R* mi, int* en, R* uR, R* cvm) {
   using M = Math<R>;
   const RTabs<R>& x = t.r<R>();
   const R c = rho * y[k] * x.invW[k];
-  C[k] = c;
+  if constexpr (STORE_C) C[k] = c;
   const int r = (T > x.tmid[k]) ? 1 : 0;
   const R* cs = x.cs + r * 7 * NSMAX;
   // S/R - H/RT = a1 (lnT - 1) + a2/2 T + a3/6 T^2 + a4/12 T^3 + a5/20 T^4 + a7 - a6/T (CKSMH, 7501)
@@ -884,29 +883,43 @@ __device__ void rhs64_team(const Tabs& t, const Team<TEAM>& tm, WarpWork& w, con
   const int nround = t.nrp >> 5;
   const double pfac = (PATM_CGS / RU_CGS) * invT;
   const double ipfac = T * (RU_CGS / PATM_CGS);
-  // Non-fall-off rounds e = 0..nE-1 sit at round re(e); phase 1 gives their
-  // Arrhenius constants to warps 0 (e < 1), 1 (e < 3), 2 (e < 5) and 3 (the
-  // rest), after each warp's own part: the species pass (warps 0-1), log10
-  // Fcent of the fall-off reactions (warp 2), and k_inf / k0 of every slot
-  // of the fall-off rounds (warp 3).
+  // Non-fall-off rounds e = 0..nE-1 sit at round re(e). Phase 0: the
+  // concentrations and their sum, by all four warps. Phase 1 gives the
+  // Arrhenius constants of rounds e to warps 0 (e < 2), 1 (e < 4), 2 (e < 6)
+  // and 3 (the rest), after each warp's own part: the species pass (warps
+  // 0-1), log10 Fcent of the fall-off reactions (warp 2), and k_inf, k0/k_inf,
+  // the collider sum, Pr and log10 Pr of every slot of the fall-off rounds
+  // (warp 3, which keeps Pr and log10 Pr for its phase 2).
   const int nE = nround - nfr;
   auto re = [&](int e) { return (nfr > 0 && e >= fr0) ? e + nfr : e; };
   auto prep_round = [&](int rr) {
     const int i = rr * 32 + lane;
     if (i < t.nr) kfe[i] = arrhenius<double>(t, i, t.w0[i] >> 24, logT, invT);
   };
-  double ps[2] = {0.0, 0.0};  // sum C_k, sum Y_k cv_k
+  {
+    double cs = 0.0;
+    for (int k = tid; k < ns; k += TEAM) {
+      const double c = rho * y[k] * x.invW[k];
+      w.C[k] = c;
+      cs += c;
+    }
+    cs = warp_sum(cs);
+    if (lane == 0) tm.red[24 + wq] = cs;
+    // 1/rho for the production rates, kept in the last cross-warp slot
+    if (tid == 0) tm.red[255] = 1.0 / rho;
+  }
+  tm.sync();
+  const double ctot = ((tm.red[24] + tm.red[25]) + tm.red[26]) + tm.red[27];
+  double* fpr = tm.part4;  // [nfr][64]: Pr, log10 Pr of the fall-off slots (warp 3's own)
+  double ycv = 0.0;        // sum Y_k cv_k
   int e0 = 0, e1 = 0;
-  // 1/rho for the production rates, kept in the last cross-warp slot (warp 0
-  // has time to spare in phase 1)
-  if (tid == 0) tm.red[255] = 1.0 / rho;
   if (wq < 2) {
     for (int k = tid; k < ns; k += 64) {
-      ps[0] += species_one<double>(t, k, y, rho, T, logT, invT, pfac, ipfac, w.C, w.m, w.wdot, w.en, w.uR, w.cvm);
-      ps[1] = fma(y[k], w.cvm[k], ps[1]);
+      species_one<double, false>(t, k, y, rho, T, logT, invT, pfac, ipfac, w.C, w.m, w.wdot, w.en, w.uR, w.cvm);
+      ycv = fma(y[k], w.cvm[k], ycv);
     }
-    e0 = wq == 0 ? 0 : 1;
-    e1 = wq == 0 ? 1 : 3;
+    e0 = wq == 0 ? 0 : 2;
+    e1 = wq == 0 ? 2 : 4;
   } else if (wq == 2) {
     for (int r = 0; r < nfr; ++r) {
       const int i = (fr0 + r) * 32 + lane;
@@ -917,8 +930,8 @@ __device__ void rhs64_team(const Tabs& t, const Team<TEAM>& tm, WarpWork& w, con
         fcl[aux] = (ifop > 1) ? troe_fclog<double>(t, fp, ifop, T, invT) : 0.0;
       }
     }
-    e0 = 3;
-    e1 = 5;
+    e0 = 4;
+    e1 = 6;
   } else {
     for (int r = 0; r < nfr; ++r) {
       const int i = (fr0 + r) * 32 + lane;
@@ -928,43 +941,32 @@ __device__ void rhs64_team(const Tabs& t, const Team<TEAM>& tm, WarpWork& w, con
         if (fl & F_FALL) {
           const int aux = (int)(t.w2[i] >> 24);
           const double* fp = x.aux + aux * AUXW;
-          k0a[aux] = fp[0] * texp_a(fp[1] * logT - fp[2] * invT, t.e2);  // k0 / kinf
+          const double pr = fp[0] * texp_a(fp[1] * logT - fp[2] * invT, t.e2) *  // k0 / kinf
+                            collider<double>(t, fl, aux, ctot, w.C);
+          fpr[r * 64 + lane] = pr;
+          fpr[r * 64 + 32 + lane] = log10_pr(t, pr);
         }
       }
     }
-    e0 = 5;
+    e0 = 6;
     e1 = nE;
   }
   for (int e = min(e0, nE); e < min(e1, nE); ++e) prep_round(re(e));
-  tm.sumv(ps);  // its barriers close phase 1
-  const double ctot = ps[0];
+  ycv = tm.sum(ycv);  // its barriers close phase 1
   // 1/(rho cv) for dT/dt, on the thread that writes it (warp 0 has time to
   // spare in phase 2)
-  const double inv_rhocv = tid == 0 ? 1.0 / (rho * ps[1]) : 0.0;
-  // phase 2: the fall-off chain (collider sum, log10 Pr, the Troe factor
-  // with its reciprocal and exponential) is split over three warps: warp 2
-  // forms Pr and log10 Pr, warp 1 the concentration products, warp 3 the
-  // Troe factor and the rates; round e of the other rounds goes to warp e % 4
-  // (warp 3's before its waits)
+  const double inv_rhocv = tid == 0 ? 1.0 / (rho * ycv) : 0.0;
+  // phase 2: warp 3 turns its Pr and log10 Pr into the fall-off rate
+  // constants (the Troe factor, with its reciprocal and exponential) and
+  // takes the last of the other rounds; warp 1 forms the fall-off
+  // concentration products and hands them over through a named barrier;
+  // warps 0-2 take the other rounds in turn (all four without fall-off)
   auto rate_round = [&](int rr) {
     const int i = rr * 32 + lane;
     w.rop[i] = (i < t.nr) ? rop_pre(t, i, kfe[i], k0a, fcl, pfac, ipfac, ctot, w.C, w.m, w.wdot, w.en) : 0.0;
   };
   if (nfr > 0) {
-    double* fpr = tm.part4;  // [nfr][64]: Pr, then kf pcor; log10 Pr (fall-off slots)
-    if (wq == 2) {
-      for (int r = 0; r < nfr; ++r) {
-        const int i = (fr0 + r) * 32 + lane;
-        const unsigned fl = i < t.nr ? t.w0[i] >> 24 : 0u;
-        if (fl & F_FALL) {
-          const int aux = (int)(t.w2[i] >> 24);
-          const double pr = k0a[aux] * collider<double>(t, fl, aux, ctot, w.C);
-          fpr[r * 64 + lane] = pr;
-          fpr[r * 64 + 32 + lane] = log10_pr(t, pr);
-        }
-      }
-      pair_arrive(BAR_FALL_PR);
-    } else if (wq == 1) {
+    if (wq == 1) {
       for (int r = 0; r < nfr; ++r) {
         const int i = (fr0 + r) * 32 + lane;
         if (i < t.nr) {
@@ -976,9 +978,9 @@ __device__ void rhs64_team(const Tabs& t, const Team<TEAM>& tm, WarpWork& w, con
       }
       pair_arrive(BAR_FALL_MA);
     }
-    for (int e = wq; e < nE; e += 4) rate_round(re(e));
-    if (wq == 3) {
-      pair_wait(BAR_FALL_PR);
+    if (wq < 3) {
+      for (int e = wq; e < nE - 1; e += 3) rate_round(re(e));
+    } else {
       for (int r = 0; r < nfr; ++r) {
         const int i = (fr0 + r) * 32 + lane;
         double kp = 0.0;
@@ -996,6 +998,7 @@ __device__ void rhs64_team(const Tabs& t, const Team<TEAM>& tm, WarpWork& w, con
         }
         fpr[r * 64 + lane] = kp;
       }
+      if (nE > 0) rate_round(re(nE - 1));
       pair_wait(BAR_FALL_MA);
       for (int r = 0; r < nfr; ++r) {
         const int i = (fr0 + r) * 32 + lane;

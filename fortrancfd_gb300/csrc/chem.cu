@@ -1579,15 +1579,16 @@ __device__ CellStats integrate(const Tabs& t, const Team<TW>& tm, WarpWork& w, c
         double acc = w.y0[i];
         for (int j = 0; j < s; ++j) acc = fma(h * c_sa[s][j], w.F[j][i], acc);
         w.sv[i] = acc;
-        // starting value: the stage derivative extrapolated linearly in the
-        // stage abscissa c = (1/4, 3/4, 11/20, 1/2, 1) from two earlier
-        // derivatives (f0 at c = 0; stage 5 from the pair at 3/4 and 1/2)
+        // starting value: the stage derivative interpolated or extrapolated
+        // linearly in the stage abscissa c = (1/4, 3/4, 11/20, 1/2, 1) from
+        // two earlier derivatives (f0 at c = 0; stage 4 between 1/4 and
+        // 11/20, stage 5 from the pair at 3/4 and 1/2)
         double fp;
         switch (s) {
           case 0: fp = w.dl[i]; break;
           case 1: fp = fma(3.0, w.F[0][i], -2.0 * w.dl[i]); break;
           case 2: fp = fma(0.6, w.F[1][i], 0.4 * w.F[0][i]); break;
-          case 3: fp = fma(1.25, w.F[2][i], -0.25 * w.F[1][i]); break;
+          case 3: fp = fma(5.0 / 6.0, w.F[2][i], (1.0 / 6.0) * w.F[0][i]); break;
           default: fp = fma(2.0, w.F[1][i], -w.F[3][i]); break;
         }
         w.Y[i] = fma(h * g, fp, acc);

@@ -334,9 +334,9 @@ int edyn_init(const char* chem_dir, int nspe, int nequ, int ncell, int lvir, con
 int edyn_set_stage_tile(void* ctx, int cells) {
   Ctx* c = (Ctx*)ctx;
   if (!c || !c->qc) return EDYN_E_ARG;
-  if (cells != 0 && (cells < STAGE_MIN_CELLS || cells > STAGE_MAX_THREADS / 2 - 2))
+  if (cells != 0 && (cells < STAGE_MIN_CELLS || cells > STAGE_MAX_CELLS))
     return fail(c, EDYN_E_ARG, "stage tile of %d cells outside [%d, %d] (0: automatic)", cells, STAGE_MIN_CELLS,
-                STAGE_MAX_THREADS / 2 - 2);
+                STAGE_MAX_CELLS);
   int tc = cells;
   if (cells == 0) CK(stage_tiling(c->acu, c->lim, c->wflag, c->riemann, c->ns, c->n, &tc));
   c->stage_tc = tc;

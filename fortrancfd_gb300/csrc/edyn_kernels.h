@@ -8,10 +8,12 @@
 namespace edyn {
 
 constexpr int GHOST = 4;          // ghost columns allocated per tube end (max lvir)
-constexpr int STAGE_MAX_THREADS = 256; // stage CTA: two threads per cell position, positions = cells + 2
+constexpr int STAGE_MAX_THREADS = 256; // stage CTA: STAGE_SPLIT threads per cell position, positions = cells + 2
+constexpr int STAGE_SPLIT = 4;         // threads per cell position (a power of two, at most 32)
 constexpr int STAGE_MIN_CELLS = 8;     // smallest stage tile (the tile rule needs at least lvir cells)
-// threads of a stage CTA for a tile of tc cells: two per position, whole warps
-constexpr int stage_threads(int tc) { return (2 * (tc + 2) + 31) / 32 * 32; }
+constexpr int STAGE_MAX_CELLS = STAGE_MAX_THREADS / STAGE_SPLIT - 2;
+// threads of a stage CTA for a tile of tc cells: STAGE_SPLIT per position, whole warps
+constexpr int stage_threads(int tc) { return (STAGE_SPLIT * (tc + 2) + 31) / 32 * 32; }
 
 struct ThermoTable;
 

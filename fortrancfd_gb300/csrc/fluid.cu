@@ -51,12 +51,14 @@ struct CellEOS {
   double T, u, Sz, cpR;  // cpR = Cp(T) of the final premix, for the sound speed
 };
 
-// Sum of v over the two threads of a lane pair (2j, 2j+1) that split a
-// cell's species between them (S = 2; identity for S = 1). Both threads get
-// the same bits: v0 + v1 and v1 + v0 round alike.
+// Sum of v over an aligned group of S lanes (a power of two) that split a
+// cell's species between them (identity for S = 1), by an xor tree: every
+// lane of the group gets the same bits (each level adds the same two
+// partial sums, in either order, and addition commutes).
 template <int S>
 __device__ __forceinline__ double pair_sum(double v, unsigned mask) {
-  if constexpr (S == 2) return v + __shfl_xor_sync(mask, v, 1);
+#pragma unroll
+  for (int o = 1; o < S; o <<= 1) v += __shfl_xor_sync(mask, v, o);
   return v;
 }
 
@@ -66,8 +68,8 @@ __device__ __forceinline__ void pair_sum(Premix& pm, unsigned mask) {
   for (int n = 0; n < 6; ++n) pm.A[n] = pair_sum<S>(pm.A[n], mask);
 }
 
-// Premixed NASA-7 coefficients of a cell; with S = 2 the thread takes the
-// species k = h, h + 2, ... and the pair sums its parts.
+// Premixed NASA-7 coefficients of a cell; with S > 1 the thread takes the
+// species k = h, h + S, ... and the group sums its parts.
 template <int S = 1>
 __device__ __forceinline__ void premix_cell(const double* ys, int st, double T, Premix& pm, double& Sz, int h = 0,
                                             unsigned mask = 0u) {
@@ -85,7 +87,7 @@ __device__ __forceinline__ void premix_cell(const double* ys, int st, double T, 
 
 // Newton on sum z_k u_k(T) = e for T (temperature_con, SRC/thermo.f90:211-257)
 // in the premixed variables: g(T) = H(T) - T Sz - E, dg/dT = Cp(T) - Sz.
-// Both threads of a pair iterate alike (same sums, same iterates).
+// The threads of a group iterate alike (same sums, same iterates).
 template <int S = 1>
 __device__ __forceinline__ double t_newton(const double* ys, int st, double E, double T0, Premix& pm, double& Sz,
                                            int& iters, int h = 0, unsigned mask = 0u) {
@@ -107,7 +109,7 @@ __device__ __forceinline__ double t_newton(const double* ys, int st, double E, d
 }
 
 // Full QcToqf. On entry ys[k*st] = rho*Y_k. Writes the normalised Y_k back
-// (with S = 2, the species k = h, h + 2, ... of this thread).
+// (with S > 1, the species k = h, h + S, ... of this thread).
 template <int S = 1>
 __device__ __forceinline__ CellEOS qc_to_qf_cell(double rho, double rhou, double rhoe, double* ys, int st,
                                                  double Tguess, bool strict, int& iters, int h = 0,
@@ -246,7 +248,8 @@ __global__ void __launch_bounds__(STAGE_MAX_THREADS) k_stage(StageArgs a) {
   extern __shared__ double sm[];
   const int TC = a.tc;        // cells of a tile
   const int P = TC + 2;       // positions: the cells c0-1..c0+TC, or the faces c0..c0+TC
-  const int NT = blockDim.x;  // whole warps, at least two threads per position
+  constexpr int SP = STAGE_SPLIT;
+  const int NT = blockDim.x;  // whole warps, at least SP threads per position
   const int tid = threadIdx.x;
   // Tile of this CTA: cells [c0, c1), TC wide. The right-end ghost cells are
   // built from the conserved state of the last LV cells, which the stage
@@ -296,12 +299,12 @@ __global__ void __launch_bounds__(STAGE_MAX_THREADS) k_stage(StageArgs a) {
   __syncthreads();
 
   // 2. face values of the cells c0-1..c1: position p = tid % P, rows split
-  //    between the two halves of the CTA
-  if (tid < 2 * P) {
-    const int p = tid % P, half = tid / P;
+  //    between the SP parts of the CTA
+  if (tid < SP * P) {
+    const int p = tid % P, part = tid / P;
     if (c0 - 1 + p <= c1) {
       const int c = p + LV - 1;  // window index of cell c0-1+p
-      for (int v = half; v < ne; v += 2) {
+      for (int v = part; v < ne; v += SP) {
         double vr, vl;
         recon_cell<ACU, LIM, WFLAG>(s_q + v * Wd, c, vr, vl);
         s_l[v * P + p] = vr;
@@ -311,10 +314,10 @@ __global__ void __launch_bounds__(STAGE_MAX_THREADS) k_stage(StageArgs a) {
   }
   __syncthreads();
 
-  // 3. one face per lane pair: face c0+f between cells c0-1+f and c0+f;
-  //    lane h of the pair takes the species k = h, h + 2, ...
-  const int f = tid >> 1, h = tid & 1;
-  const unsigned pair = 3u << (tid & 30);
+  // 3. one face per group of SP lanes: face c0+f between cells c0-1+f and
+  //    c0+f; lane h of the group takes the species k = h, h + SP, ...
+  const int f = tid / SP, h = tid % SP;
+  const unsigned pair = ((1u << SP) - 1u) << (tid & 31 & ~(SP - 1));
   if (f < P && c0 + f <= c1) {
     FaceState L, R;
     L.rho = s_l[0 * P + f];
@@ -327,7 +330,7 @@ __global__ void __launch_bounds__(STAGE_MAX_THREADS) k_stage(StageArgs a) {
     pl.zero(t_interval(tb, L.T));
     pr.zero(t_interval(tb, R.T));
     double syl = 0.0, syr = 0.0, szl = 0.0, szr = 0.0;
-    for (int k = h; k < ns; k += 2) {
+    for (int k = h; k < ns; k += SP) {
       const double yl = s_l[(3 + k) * P + f], yr = s_r[(3 + k) * P + f + 1];
       const double pl_ = clip0(yl), pr_ = clip0(yr);
       syl += pl_;
@@ -338,12 +341,12 @@ __global__ void __launch_bounds__(STAGE_MAX_THREADS) k_stage(StageArgs a) {
       premix_add(tb, pl, k, zl, L.T);
       premix_add(tb, pr, k, zr, R.T);
     }
-    syl = pair_sum<2>(syl, pair);
-    syr = pair_sum<2>(syr, pair);
-    szl = pair_sum<2>(szl, pair);
-    szr = pair_sum<2>(szr, pair);
-    pair_sum<2>(pl, pair);
-    pair_sum<2>(pr, pair);
+    syl = pair_sum<SP>(syl, pair);
+    syr = pair_sum<SP>(syr, pair);
+    szl = pair_sum<SP>(szl, pair);
+    szr = pair_sum<SP>(szr, pair);
+    pair_sum<SP>(pl, pair);
+    pair_sum<SP>(pr, pair);
     face_finish(L, pl, syl, szl);
     face_finish(R, pr, syr, szr);
     const double ml = L.rho * L.u, mr = R.rho * R.u;
@@ -416,7 +419,7 @@ __global__ void __launch_bounds__(STAGE_MAX_THREADS) k_stage(StageArgs a) {
         }
       }
     }
-    // The fluxes replace the left states of this face, which no other pair
+    // The fluxes replace the left states of this face, which no other group
     // reads: the bulk rows by lane 0, species row k by the lane that owns k.
     double* F = s_l + f;
     if (h == 0) {
@@ -424,7 +427,7 @@ __global__ void __launch_bounds__(STAGE_MAX_THREADS) k_stage(StageArgs a) {
       F[P] = F1;
       F[2 * P] = F2;
     }
-    for (int k = h; k < ns; k += 2) {
+    for (int k = h; k < ns; k += SP) {
       const double yl = s_l[(3 + k) * P + f], yr = s_r[(3 + k) * P + f + 1];
       double v = aL * yl;
       v = fma(bL, clip0(yl), v);
@@ -435,8 +438,8 @@ __global__ void __launch_bounds__(STAGE_MAX_THREADS) k_stage(StageArgs a) {
   }
   __syncthreads();
 
-  // 4. one cell per lane pair: conservative update + QcToqf, species split
-  //    as in phase 3 (the bulk rows are computed by both lanes)
+  // 4. one cell per group of SP lanes: conservative update + QcToqf,
+  //    species split as in phase 3 (the bulk rows are computed by every lane)
   const int i = c0 + f;
   double speed = 0.0;
   if (f < P && i < c1) {
@@ -453,16 +456,16 @@ __global__ void __launch_bounds__(STAGE_MAX_THREADS) k_stage(StageArgs a) {
     double q[3], qv[3];
 #pragma unroll
     for (int v = 0; v < 3; ++v) qv[v] = Q[v * ld];
-    __syncwarp(pair);  // both lanes have read the bulk rows before lane (v & 1) rewrites row v
+    __syncwarp(pair);  // every lane has read the bulk rows before lane v % SP rewrites row v
 #pragma unroll
     for (int v = 0; v < 3; ++v) {
       q[v] = update(v, qv[v]);
-      if ((v & 1) == h) {
+      if (v % SP == h) {
         if (a.save_q0) Q0[v * ld] = qv[v];
         Q[v * ld] = q[v];
       }
     }
-    for (int v = 3 + h; v < ne; v += 2) {
+    for (int v = 3 + h; v < ne; v += SP) {
       const double qs = Q[v * ld];
       const double qn = update(v, qs);
       if (a.save_q0) Q0[v * ld] = qs;
@@ -471,7 +474,7 @@ __global__ void __launch_bounds__(STAGE_MAX_THREADS) k_stage(StageArgs a) {
     }
     int iters;
     const double Tg = s_q[2 * Wd + f + LV];
-    CellEOS e = qc_to_qf_cell<2>(q[0], q[1], q[2], ys, P, Tg, a.strict_newton != 0, iters, h, pair);
+    CellEOS e = qc_to_qf_cell<SP>(q[0], q[1], q[2], ys, P, Tg, a.strict_newton != 0, iters, h, pair);
     double* out = a.qf_out + i + GHOST;
     if (h == 0) {
       out[0] = q[0];
@@ -479,7 +482,7 @@ __global__ void __launch_bounds__(STAGE_MAX_THREADS) k_stage(StageArgs a) {
       out[2 * ld] = e.T;
       if (a.cvel_out) speed = cell_speed(e.u, e.T, e.Sz, e.cpR);
     }
-    for (int k = h; k < ns; k += 2) out[(3 + k) * ld] = ys[k * P];
+    for (int k = h; k < ns; k += SP) out[(3 + k) * ld] = ys[k * P];
   }
   if (a.cvel_out) {
     double m = speed;
@@ -694,8 +697,9 @@ StageFn stage_fn(int acu, int lim, int wflag, int rm) {
 }  // namespace
 
 // Cells per stage tile for a tube of n cells. A CTA's time hardly depends on
-// its tile (each thread reconstructs one position, solves one face and one
-// cell, so the CTA is as long as one thread's chain of FP64 latencies), so
+// its tile (each thread reconstructs part of one position, then helps with
+// one face and one cell, so the CTA is as long as one thread's chain of FP64
+// latencies), so
 // the launch lasts about one CTA time per wave of resident CTAs. The choice:
 // the fewest waves over the thread counts 64..STAGE_MAX_THREADS (their
 // occupancy, limited by the shared-memory window, from the runtime), then
@@ -712,7 +716,7 @@ cudaError_t stage_tiling(int acu, int lim, int wflag, int rm, int ns, int n, int
   long best_waves = -1, best_slots = 0;
   int best_tcmax = 0;
   for (int nt = 64; nt <= STAGE_MAX_THREADS; nt += 32) {
-    const int tcmax = nt / 2 - 2;
+    const int tcmax = nt / STAGE_SPLIT - 2;
     const size_t smem = stage_smem_bytes(acu, ns, tcmax);
     e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) {

@@ -168,11 +168,12 @@ int edyn_check_exp(void* ctx, int n, const double* x, double* max_ulp);
  * (positive normal arguments). No counterpart in the reference. */
 int edyn_check_log(void* ctx, int n, const double* x, double* max_ulp);
 
-/* Cells per tile of the fluid stage kernel (one CTA per tile: two threads
- * per cell position, cells + 2 positions, rounded up to whole warps). 0 (the default) chooses the tile from the tube length
- * and the kernel's occupancy so that the CTAs fill whole waves of resident
- * slots; 8..126 forces a tile. Results do not depend on the tile. No
- * counterpart in the reference (a tuning knob of this implementation). */
+/* Cells per tile of the fluid stage kernel (one CTA per tile: four threads
+ * per cell position, cells + 2 positions, rounded up to whole warps). 0 (the
+ * default) chooses the tile from the tube length and the kernel's occupancy
+ * so that the CTAs fill whole waves of resident slots; 8..62 forces a tile.
+ * Results do not depend on the tile. No counterpart in the reference (a
+ * tuning knob of this implementation). */
 int edyn_set_stage_tile(void* ctx, int cells);
 
 /* The stage tile in use: cells per tile and threads per CTA (either may be

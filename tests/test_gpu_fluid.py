@@ -38,7 +38,7 @@ def run_pair(oracle, case, nsteps, strict=1, use_advance=False, tile=0):
     g = Tube(case.ncell, case.dx, strict_newton=strict, do_reaction=0, **kw)
     if tile:
         g.set_stage_tile(tile)
-        assert g.stage_tile() == (tile, (2 * (tile + 2) + 31) // 32 * 32)
+        assert g.stage_tile() == (tile, (4 * (tile + 2) + 31) // 32 * 32)
     g.upload(qf0, qc0)
     t_o = 0.0
     for _ in range(nsteps):
@@ -149,14 +149,14 @@ def test_outlet_boundary_short_run(oracle):
     (316, dict(flag_acu=2, flag_weno=3, flag_rbound=1, p_out=101325.0)),   # outlet, last tile 1 cell
 ])
 def test_short_last_tile(oracle, ncell, scheme):
-    """Tube lengths whose last 63-cell stage tile holds fewer cells than the
+    """Tube lengths whose last 35-cell stage tile holds fewer cells than the
     ghost depth, run until the waves have crossed the right end: the right
     ghosts are built from cells that the stage updates in place."""
     case = configs.sod(ncell=ncell)
     case.flags.update(scheme)
     case.flags.setdefault("flag_weno", 0)
-    assert ncell % 63 < lvir_for(case.flags["flag_acu"], case.flags["flag_weno"])
-    qf_o, qf_g, p_o, p_g, _, _ = run_pair(oracle, case, 400, tile=63)
+    assert ncell % 35 < lvir_for(case.flags["flag_acu"], case.flags["flag_weno"])
+    qf_o, qf_g, p_o, p_g, _, _ = run_pair(oracle, case, 400, tile=35)
     assert rel(p_g, p_o) < TOL
     assert rel(qf_g[:, 2], qf_o[:, 2]) < TOL
     umax = np.abs(qf_o[:, 1]).max()
@@ -170,7 +170,7 @@ def test_stage_tile_does_not_change_results():
     case = configs.detonation(ncell=1500)
     qf0, qc0 = None, None
     runs = []
-    for tile in (0, 8, 40, 63, 126):
+    for tile in (0, 8, 23, 40, 62):
         g = Tube(case.ncell, case.dx, flag_acu=2, flag_weno=3, flag_rbound=1, do_reaction=0)
         if tile:
             g.set_stage_tile(tile)
@@ -180,7 +180,7 @@ def test_stage_tile_does_not_change_results():
         runs.append(g.download()[:2])
         if tile == 0:
             cells, threads = g.stage_tile()
-            assert 16 <= cells <= 126 and threads == (2 * (cells + 2) + 31) // 32 * 32
+            assert 8 <= cells <= 62 and threads == (4 * (cells + 2) + 31) // 32 * 32
     for qf, qc in runs[1:]:
         assert np.array_equal(qf, runs[0][0])
         assert np.array_equal(qc, runs[0][1])
@@ -188,7 +188,7 @@ def test_stage_tile_does_not_change_results():
     with pytest.raises(RuntimeError):
         g.set_stage_tile(7)
     with pytest.raises(RuntimeError):
-        g.set_stage_tile(127)
+        g.set_stage_tile(63)
 
 
 def test_init_cells_matches_oracle(oracle):

@@ -291,7 +291,8 @@ def gpu_arm(args, rank, world, local):
                        "FP32 analytic Jacobian/LU)", "scheme": "WENO5-Z + HLLC + SSP-RK3, CFL 0.4",
                        "parallelism": f"replicas x{world}", "l2": "flushed between 16-step graph launches",
                        "tolerances": "rtol 1e-5, atol 1e-13",
-                       "stage_tile": "%d cells, %d threads per CTA" % tube.stage_tile()},
+                       "stage_tile": "%d cells, %d threads per CTA" % tube.stage_tile(),
+                       "chemistry_set": "%d species, %d reactions" % tube.chem_set()},
             "clocks": clk.summary(),
             "e2e": {"value": case.ncell * e2e_steps / e2e_el, "unit": UNIT,
                     "h2d_bytes_per_step": 2 * case.ncell * ne * 8,

@@ -82,6 +82,8 @@ struct TabHdr {
   int fr0, nfr;                // the fall-off reactions fill rounds [fr0, fr0 + nfr) of 32
   int o_grp;                   // int4[TEAM]: per team lane: species (-1 none), entry begin, end, group size
   int gmax;                    // largest species group of the team production rates
+  int o_smap;                  // int[NSMAX]: tube row of each species (3 + smap[k]); identity unless a subset
+  int nnorm;                   // components counted in the RMS norms: the full mechanism's ns + 1
 };
 
 template <class R>
@@ -94,6 +96,7 @@ struct Tabs {
   const unsigned *w0, *w1, *w2, *w3, *w4, *w5, *ent;
   const int *spi, *tb_sp, *pc, *lane, *spc, *spp;
   const int4* grp;
+  const int* smap;
   const double* e2;
   const double* lg;
   int ns, nr, nrp, npc;
@@ -142,6 +145,7 @@ __device__ __forceinline__ Tabs bind_tabs(const char* base) {
   t.spc = (const int*)(base + h.o_spc);
   t.spp = (const int*)(base + h.o_spp);
   t.grp = (const int4*)(base + h.o_grp);
+  t.smap = (const int*)(base + h.o_smap);
   t.ent = (const unsigned*)(base + h.o_ent);
   t.e2 = (const double*)(base + h.o_e2);
   t.lg = (const double*)(base + h.o_lg);
@@ -1442,7 +1446,7 @@ __device__ __forceinline__ void gemv_solve(const Team<TW>& tm, const float* A, f
 // the RMS of the scaled correction b. A four-warp team updates Y and forms
 // the norm where the product lands, inside the product's two barriers.
 template <int TW>
-__device__ __forceinline__ float newton_correct(const Team<TW>& tm, WarpWork& w, double hg, int n) {
+__device__ __forceinline__ float newton_correct(const Team<TW>& tm, WarpWork& w, double hg, int n, float nn) {
   for (int i = tm.tid; i < n; i += TW) w.b32[i] = (float)(hg * w.fy[i] - (w.Y[i] - w.sv[i])) * w.isc32[i];
   tm.sync();
   float ss = 0.f;
@@ -1454,7 +1458,7 @@ __device__ __forceinline__ float newton_correct(const Team<TW>& tm, WarpWork& w,
       w.Y[i] += (double)q * (double)w.sc32[i];
     }
     __syncwarp();
-    return sqrtf(tm.sum(ss) / (float)n);
+    return sqrtf(tm.sum(ss) / nn);
   } else {
     const int i = tm.tid >> 1, hh = tm.tid & 1;
     float a = 0.f;
@@ -1469,7 +1473,7 @@ __device__ __forceinline__ float newton_correct(const Team<TW>& tm, WarpWork& w,
     }
     if ((tm.tid & 31) == 0) tm.red[16 + (tm.tid >> 5)] = (double)ss;
     tm.sync();
-    return sqrtf((float)(((tm.red[16] + tm.red[17]) + tm.red[18]) + tm.red[19]) / (float)n);
+    return sqrtf((float)(((tm.red[16] + tm.red[17]) + tm.red[18]) + tm.red[19]) / nn);
   }
 }
 
@@ -1493,6 +1497,7 @@ template <int TW>
 __device__ CellStats integrate(const Tabs& t, const Team<TW>& tm, WarpWork& w, const Cell& c) {
   const int lane = tm.tid;
   const int n = t.ns + 1;
+  const float nn = (float)t.h->nnorm;  // RMS over the full mechanism's components (a subset's others are zero)
   CellStats st = {0, 0, 0, 0, false, c.dt};
   double tcur = 0.0, h = c.h0;
   const int max_steps = 4000;
@@ -1535,7 +1540,7 @@ __device__ CellStats integrate(const Tabs& t, const Team<TW>& tm, WarpWork& w, c
           const float q = (float)(c.dt * w.dl[i] / (c.atol + c.rtol * fabs(w.y0[i])));
           ss = fmaf(q, q, ss);
         }
-        const float nrm = sqrtf(tm.sum(ss) / (float)n);
+        const float nrm = sqrtf(tm.sum(ss) / nn);
         if (nrm <= 1e-3f) {
           for (int i = lane; i < n; i += TW) w.y0[i] = fma(c.dt, w.dl[i], w.y0[i]);
           tm.sync();
@@ -1603,7 +1608,7 @@ __device__ CellStats integrate(const Tabs& t, const Team<TW>& tm, WarpWork& w, c
         st.rhs++;
         // the correction is applied to Y at once: on convergence Y is rebuilt
         // from f below, on failure the step is redone
-        const float nrm = newton_correct<TW>(tm, w, h * g, n);
+        const float nrm = newton_correct<TW>(tm, w, h * g, n, nn);
         if (!(nrm == nrm)) break;
         // convergence: weighted correction below 1e-2 of the local
         // tolerance, directly or predicted from the contraction rate; one
@@ -1652,7 +1657,7 @@ __device__ CellStats integrate(const Tabs& t, const Team<TW>& tm, WarpWork& w, c
       const float q = w.b32[i] * w.sc32[i] / sc;
       ss = fmaf(q, q, ss);
     }
-    const float en = sqrtf(tm.sum(ss) / (float)n);
+    const float en = sqrtf(tm.sum(ss) / nn);
     const float fac = 0.9f * powf(fmaxf(en, 1e-10f), -0.25f);
     if (en <= 1.f) {
       // SDIRK4 is stiffly accurate (y1 = Y5), so the last stage derivative is
@@ -1753,7 +1758,7 @@ __device__ int tube_cell(const Tabs& t, const Team<TW>& tm, WarpWork& w, const C
   // the raw Y stay in the qf rows for the heat release rate.
   double s = 0.0;
   for (int k = tid; k < ns; k += TW) {
-    const double yp = clip0_d(q[(3 + k) * ld]);
+    const double yp = clip0_d(q[(3 + t.smap[k]) * ld]);
     w.y0[k] = yp;
     s += yp;
   }
@@ -1787,7 +1792,7 @@ __device__ int tube_cell(const Tabs& t, const Team<TW>& tm, WarpWork& w, const C
   for (int k = tid; k < ns; k += TW) {
     const double yn = w.y0[k] * inv2;
     w.y0[k] = yn;
-    const double y0raw = q[(3 + k) * ld];
+    const double y0raw = q[(3 + t.smap[k]) * ld];
     hsum[0] = fma(rho_cgs * t.d.hf[k], yn - y0raw, hsum[0]);
     // qfToQc energy: e = R (H(T) - T Sz)/S_Y with the adjusted Y (S_Y = 1)
     const int r = (Tn > t.d.tmid[k]) ? 1 : 0;
@@ -1809,8 +1814,8 @@ __device__ int tube_cell(const Tabs& t, const Team<TW>& tm, WarpWork& w, const C
   // recovers T from rho e with the Newton solve.
   tm.sync();  // every thread has read the raw Y rows
   for (int k = tid; k < ns; k += TW) {
-    q[(3 + k) * ld] = w.y0[k];
-    Q[(3 + k) * ld] = rho * w.y0[k];
+    q[(3 + t.smap[k]) * ld] = w.y0[k];
+    Q[(3 + t.smap[k]) * ld] = rho * w.y0[k];
   }
   if (tid == 0) {
     Q[2 * ld] = rhoe;
@@ -2033,7 +2038,7 @@ struct Blob {
 
 }  // namespace
 
-int chem_init(ChemState& s, const edyn_mech& m, const ThermoTable& tb, cudaStream_t st) {
+int chem_init(ChemState& s, const edyn_mech& m, const ThermoTable& tb, cudaStream_t st, const int* smap, int nnorm) {
   (void)tb;
   const int ns = m.nspec, nr = m.nreac;
   if (ns + 1 > 54 + 2 || ns > NSMAX - 8 || nr > 352) return (int)cudaErrorInvalidValue;
@@ -2323,6 +2328,12 @@ int chem_init(ChemState& s, const edyn_mech& m, const ThermoTable& tb, cudaStrea
   h.o_spp = bl.put(spp.data(), std::max<size_t>(4, spp.size() * 4));
   h.o_grp = bl.put(grp.data(), grp.size() * 4);
   h.gmax = gmax;
+  {
+    std::vector<int> sm(NSMAX, 0);
+    for (int k = 0; k < ns; ++k) sm[k] = smap ? smap[k] : k;
+    h.o_smap = bl.put(sm.data(), sm.size() * 4);
+    h.nnorm = nnorm > 0 ? nnorm : ns + 1;
+  }
   h.o_ent = bl.put(ent_idx.data(), std::max<size_t>(4, ent_idx.size() * 4));
   auto put2 = [&](int* off, const std::vector<double>& v) {
     std::vector<double> d(v);
@@ -2405,9 +2416,18 @@ int chem_init(ChemState& s, const edyn_mech& m, const ThermoTable& tb, cudaStrea
   s.warps = (int)std::min<long>(MAXW, room / (long)sizeof(WarpWork));
   if (s.warps < 1) return (int)cudaErrorInvalidConfiguration;
   s.smem = tot + sizeof(WarpWork) * (size_t)s.warps;
-  e = cudaFuncSetAttribute(k_reactors, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s.smem);
+  // the attribute serves every table set of the process: it only grows
+  int cur = 0;
+  {
+    cudaFuncAttributes fr;
+    e = cudaFuncGetAttributes(&fr, k_reactors);
+    if (e != cudaSuccess) return (int)e;
+    cur = std::max(fa.maxDynamicSharedSizeBytes, fr.maxDynamicSharedSizeBytes);
+  }
+  const int want = std::max(cur, (int)s.smem);
+  e = cudaFuncSetAttribute(k_reactors, cudaFuncAttributeMaxDynamicSharedMemorySize, want);
   if (e != cudaSuccess) return (int)e;
-  e = cudaFuncSetAttribute(k_tube_chem, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s.smem);
+  e = cudaFuncSetAttribute(k_tube_chem, cudaFuncAttributeMaxDynamicSharedMemorySize, want);
   if (e != cudaSuccess) return (int)e;
   int per_sm = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_reactors, s.warps * 32, s.smem);

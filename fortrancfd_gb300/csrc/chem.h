@@ -50,7 +50,11 @@ struct ChemLaunch {
   unsigned* err;
 };
 
-int chem_init(ChemState& s, const edyn_mech& m, const ThermoTable& tb, cudaStream_t st);
+// smap: tube row of each species of m (3 + smap[k]) when m is a subset of the
+// tube's mechanism (NULL: identity); nnorm: components counted in the RMS
+// norms (0: ns + 1).
+int chem_init(ChemState& s, const edyn_mech& m, const ThermoTable& tb, cudaStream_t st, const int* smap = nullptr,
+              int nnorm = 0);
 cudaError_t chem_launch_tube(ChemState& s, const ChemLaunch& L, cudaStream_t st);
 cudaError_t chem_launch_batch(ChemState& s, const ChemLaunch& L, cudaStream_t st);
 cudaError_t chem_read_counters(ChemState& s, ChemCounters* out, cudaStream_t st);

@@ -12,6 +12,7 @@
 #include <cstdio>
 #include <cstdint>
 #include <cstring>
+#include <memory>
 #include <mutex>
 #include <new>
 #include <string>
@@ -63,6 +64,14 @@ struct Ctx {
   double graph_cfl = -1, graph_tend = -1;
   int stage_tc = 0;        // cells per stage tile
   ChemState chem;
+  // Tables of the species whose elements all occur in the tube (or at the
+  // inlet), built when that drops species: the others are zero everywhere
+  // and stay zero (no reaction forms a species from absent elements), so
+  // the reactions that involve them have zero rates and are left out.
+  ChemState chem_sub;
+  std::vector<char> sub_keep;
+  bool use_sub = false;
+  int* d_present = nullptr;  // per species: nonzero somewhere in the tube
   std::string err;
 };
 
@@ -181,9 +190,132 @@ int source_step(Ctx* c, double dt, bool dev) {
   L.cost = c->d_cost;
   L.hot = c->d_hot;
   L.hlast = c->d_hlast;
-  cudaError_t e = chem_launch_tube(c->chem, L, c->stream);
+  cudaError_t e = chem_launch_tube(c->use_sub ? c->chem_sub : c->chem, L, c->stream);
   if (e != cudaSuccess) return fail(c, EDYN_E_CUDA, "chemistry launch: %s", cudaGetErrorString(e));
   return EDYN_OK;
+}
+
+void drop_graph(Ctx* c);
+
+// The element subset of the mechanism: kept species (renumbered; smap gives
+// each one's index in m), and the reactions whose species and named collider
+// are all kept, with third-body efficiencies of dropped species removed
+// (their concentrations are zero).
+void mech_subset(const edyn_mech& m, const std::vector<char>& keep, edyn_mech& o, std::vector<int>& smap) {
+  o = m;
+  std::vector<int> nid(m.nspec, -1);
+  smap.clear();
+  int ns = 0;
+  for (int k = 0; k < m.nspec; ++k) {
+    if (!keep[k]) continue;
+    nid[k] = ns;
+    smap.push_back(k);
+    std::memcpy(o.spec_name[ns], m.spec_name[k], sizeof(o.spec_name[ns]));
+    o.W[ns] = m.W[k];
+    o.T_lo[ns] = m.T_lo[k];
+    o.T_mid[ns] = m.T_mid[k];
+    o.T_hi[ns] = m.T_hi[k];
+    std::memcpy(o.a[ns], m.a[k], sizeof(o.a[ns]));
+    std::memcpy(o.elem_count[ns], m.elem_count[k], sizeof(o.elem_count[ns]));
+    ++ns;
+  }
+  o.nspec = ns;
+  int nr = 0;
+  for (int i = 0; i < m.nreac; ++i) {
+    bool ok = true;
+    for (int sl = 0; sl < 6; ++sl)
+      if (m.nunk[i][sl] >= 0 && nid[m.nunk[i][sl]] < 0) ok = false;
+    if (m.kfal[i] >= 0 && nid[m.kfal[i]] < 0) ok = false;
+    if (!ok) continue;
+    std::memcpy(o.equation[nr], m.equation[i], sizeof(o.equation[nr]));
+    o.rev[nr] = m.rev[i];
+    for (int sl = 0; sl < 6; ++sl) {
+      o.nu[nr][sl] = m.nu[i][sl];
+      o.nunk[nr][sl] = m.nunk[i][sl] >= 0 ? nid[m.nunk[i][sl]] : -1;
+    }
+    o.A[nr] = m.A[i];
+    o.beta[nr] = m.beta[i];
+    o.E_R[nr] = m.E_R[i];
+    o.tb[nr] = m.tb[i];
+    o.kfal[nr] = m.kfal[i] >= 0 ? nid[m.kfal[i]] : -1;
+    o.ifop[nr] = m.ifop[i];
+    std::memcpy(o.low[nr], m.low[i], sizeof(o.low[nr]));
+    std::memcpy(o.troe[nr], m.troe[i], sizeof(o.troe[nr]));
+    o.dup[nr] = m.dup[i];
+    int ne = 0;
+    for (int z = 0; z < m.neff[i]; ++z) {
+      if (nid[m.eff_sp[i][z]] < 0) continue;
+      o.eff_sp[nr][ne] = nid[m.eff_sp[i][z]];
+      o.eff_val[nr][ne] = m.eff_val[i][z];
+      ++ne;
+    }
+    o.neff[nr] = ne;
+    ++nr;
+  }
+  o.nreac = nr;
+}
+
+// Picks the chemistry tables for the species present in the tube state
+// (present[k]: nonzero somewhere) and at the inlet.
+int select_chem_set(Ctx* c, const std::vector<char>& present) {
+  const edyn_mech& m = c->mech;
+  std::vector<char> el(m.nelem, 0);
+  for (int k = 0; k < m.nspec; ++k) {
+    const bool here = present[k] || (c->lbound == 1 && c->bc.y_in[k] > 0.0);
+    if (!here) continue;
+    for (int e = 0; e < m.nelem; ++e)
+      if (m.elem_count[k][e] > 0) el[e] = 1;
+  }
+  std::vector<char> keep(m.nspec, 1);
+  int nk = 0;
+  for (int k = 0; k < m.nspec; ++k) {
+    for (int e = 0; e < m.nelem; ++e)
+      if (m.elem_count[k][e] > 0 && !el[e]) keep[k] = 0;
+    nk += keep[k];
+  }
+  const bool want = c->do_reaction && nk < m.nspec && nk > 0;
+  if (!want) {
+    if (c->use_sub) drop_graph(c);
+    c->use_sub = false;
+    return EDYN_OK;
+  }
+  if (keep == c->sub_keep && c->chem_sub.d_tables) {
+    if (!c->use_sub) drop_graph(c);
+    c->use_sub = true;
+    return EDYN_OK;
+  }
+  std::unique_ptr<edyn_mech> sub(new (std::nothrow) edyn_mech);
+  if (!sub) return fail(c, EDYN_E_ARG, "out of host memory for the mechanism subset");
+  std::vector<int> smap;
+  mech_subset(m, keep, *sub, smap);
+  if (sub->nreac < 1) {  // nothing reacts: the full tables do no harm
+    if (c->use_sub) drop_graph(c);
+    c->use_sub = false;
+    return EDYN_OK;
+  }
+  CK(cudaStreamSynchronize(c->stream));
+  drop_graph(c);
+  if (c->chem_sub.d_tables) chem_free(c->chem_sub);
+  c->chem_sub = ChemState();
+  c->sub_keep.clear();
+  c->use_sub = false;
+  const int rc = chem_init(c->chem_sub, *sub, c->tb, c->stream, smap.data(), m.nspec + 1);
+  if (rc) return fail(c, EDYN_E_CUDA, "chemistry tables of the species subset: %s", cudaGetErrorString((cudaError_t)rc));
+  c->sub_keep = keep;
+  c->use_sub = true;
+  return EDYN_OK;
+}
+
+// After the state was set from outside: which species occur, then the tables.
+int refresh_chem_set(Ctx* c) {
+  if (!c->do_reaction) return EDYN_OK;
+  CK(launch_species_present(c->qc, c->ld, c->n, c->ns, c->d_present, c->stream));
+  std::vector<int> fl(c->ns, 1);
+  CK(cudaMemcpyAsync(fl.data(), c->d_present, (size_t)c->ns * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  std::vector<char> present(c->ns);
+  for (int k = 0; k < c->ns; ++k) present[k] = fl[k] != 0;
+  return select_chem_set(c, present);
 }
 
 int ensure_staging(Ctx* c, size_t bytes) {
@@ -320,6 +452,7 @@ int edyn_init(const char* chem_dir, int nspe, int nequ, int ncell, int lvir, con
   CK(cudaMemsetAsync(c->d_cost, 0, (size_t)ncell * sizeof(int), c->stream));
   CK(cudaMemsetAsync(c->d_hot, 0, (HOT_MAX + 1) * sizeof(unsigned), c->stream));
   CK(cudaMalloc(&c->d_hlast, (size_t)ncell * sizeof(double)));
+  CK(cudaMalloc(&c->d_present, 64 * sizeof(int)));
   CK(cudaMemsetAsync(c->d_hlast, 0, (size_t)ncell * sizeof(double), c->stream));
   int rc = fluid_upload_tables(c->tb, c->stream);
   if (rc == -1) return fail(c, EDYN_E_MECH, "a different mechanism is already loaded in this process");
@@ -379,8 +512,7 @@ int edyn_upload(void* ctx, const double* qf_aos, const double* qc_aos) {
     a.strict_newton = 1;
     CK(launch_qc_to_qf(a, c->stream));
   }
-  CK(cudaStreamSynchronize(c->stream));
-  return EDYN_OK;
+  return refresh_chem_set(c);
 }
 
 int edyn_init_cells(void* ctx, const double* T, const double* p, const double* u, const double* X) {
@@ -400,7 +532,7 @@ int edyn_init_cells(void* ctx, const double* T, const double* p, const double* u
   CK(cudaMemcpyAsync(dX, X, n * ns * sizeof(double), cudaMemcpyHostToDevice, c->stream));
   CK(launch_init_cells(c->n, c->ns, dT, dp, du, dX, c->ns, c->qf[c->cur], c->qc, c->ld, c->stream));
   CK(cudaStreamSynchronize(c->stream));
-  return EDYN_OK;
+  return refresh_chem_set(c);
 }
 
 int edyn_calc_dt(void* ctx, double cfl, double* dt) {
@@ -543,10 +675,19 @@ int edyn_chem_stats(void* ctx, double* stats) {
   Ctx* c = (Ctx*)ctx;
   if (!c || !c->qc || !stats) return EDYN_E_ARG;
   ChemCounters k;
-  cudaError_t e = chem_read_counters(c->chem, &k, c->stream);
+  cudaError_t e = chem_read_counters(c->use_sub ? c->chem_sub : c->chem, &k, c->stream);
   if (e != cudaSuccess) return fail(c, EDYN_E_CUDA, "counters: %s", cudaGetErrorString(e));
   const unsigned long long v[7] = {k.rhs, k.steps, k.rejects, k.failed, k.jac, k.cells, k.team_cells};
   for (int i = 0; i < 7; ++i) stats[i] = (double)v[i];
+  return EDYN_OK;
+}
+
+int edyn_chem_set(void* ctx, int* nspec, int* nreac) {
+  Ctx* c = (Ctx*)ctx;
+  if (!c || !c->qc) return EDYN_E_ARG;
+  const ChemState& s = c->use_sub ? c->chem_sub : c->chem;
+  if (nspec) *nspec = s.ns;
+  if (nreac) *nreac = s.nr;
   return EDYN_OK;
 }
 
@@ -650,6 +791,8 @@ int edyn_finalize(void* ctx) {
   if (c->stream) cudaStreamSynchronize(c->stream);
   drop_graph(c);
   chem_free(c->chem);
+  if (c->chem_sub.d_tables) chem_free(c->chem_sub);
+  cudaFree(c->d_present);
   cudaFree(c->qf[0]);
   cudaFree(c->qf[1]);
   cudaFree(c->qc);

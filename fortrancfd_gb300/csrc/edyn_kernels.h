@@ -52,6 +52,7 @@ size_t stage_smem_bytes(int acu, int ns, int tc);
 cudaError_t stage_tiling(int acu, int lim, int wflag, int rm, int ns, int n, int* tc);
 cudaError_t launch_stage(const StageArgs& a, int acu, int lim, int wflag, int rm, cudaStream_t s);
 cudaError_t launch_cvel(const double* qf, int n, int ld, unsigned long long* cvel, cudaStream_t s);
+cudaError_t launch_species_present(const double* qc, int ld, int n, int ns, int* flags, cudaStream_t s);
 cudaError_t launch_step_begin(const double* time, double tend, double cfl, double dx, unsigned long long* cvel,
                               int* step_active, double* dt_dev, cudaStream_t s);
 cudaError_t launch_aos_to_soa(const double* aos, int ne, int n, double* soa, int ld, cudaStream_t s);

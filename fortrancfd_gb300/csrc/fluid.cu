@@ -754,6 +754,21 @@ cudaError_t launch_stage(const StageArgs& a, int acu, int lim, int wflag, int rm
   return cudaGetLastError();
 }
 
+// flags[k] = 1 when species row k of the conserved state is nonzero in some
+// interior cell (one CTA per row).
+__global__ void k_species_present(const double* qc, int ld, int n, int* flags) {
+  const double* row = qc + (size_t)(3 + blockIdx.x) * ld + GHOST;
+  int any = 0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) any |= (row[i] != 0.0) ? 1 : 0;
+  any = __syncthreads_or(any);
+  if (threadIdx.x == 0) flags[blockIdx.x] = any;
+}
+
+cudaError_t launch_species_present(const double* qc, int ld, int n, int ns, int* flags, cudaStream_t s) {
+  k_species_present<<<ns, 256, 0, s>>>(qc, ld, n, flags);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_cvel(const double* qf, int n, int ld, unsigned long long* cvel, cudaStream_t s) {
   k_cvel<<<(n + 127) / 128, 128, 0, s>>>(qf, n, ld, cvel);
   return cudaGetLastError();

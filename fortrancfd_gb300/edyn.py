@@ -73,6 +73,7 @@ def lib() -> ctypes.CDLL:
     L.edyn_check_exp.argtypes = [vp, i, dp, dp]
     L.edyn_check_log.argtypes = [vp, i, dp, dp]
     L.edyn_set_stage_tile.argtypes = [vp, i]
+    L.edyn_chem_set.argtypes = [vp, ip, ip]
     L.edyn_stage_tile.argtypes = [vp, ip, ip]
     L.edyn_last_error.argtypes = [vp, ctypes.c_char_p, i]
     L.edyn_finalize.argtypes = [vp]
@@ -227,6 +228,13 @@ class Tube(_Ctx):
         self._check(lib().edyn_chem_cost(self._h, cost.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
                                          hot.ctypes.data_as(ctypes.POINTER(ctypes.c_uint))))
         return cost, hot[1:1 + int(hot[0])].astype(np.int64)
+
+    def chem_set(self):
+        """(species, reactions) the chemistry integrates: the mechanism, or the
+        subset of the elements present in the tube."""
+        ns, nr = ctypes.c_int(), ctypes.c_int()
+        self._check(lib().edyn_chem_set(self._h, ctypes.byref(ns), ctypes.byref(nr)))
+        return ns.value, nr.value
 
     def set_stage_tile(self, cells: int = 0) -> None:
         """Cells per fluid stage tile; 0 chooses it from the tube length."""

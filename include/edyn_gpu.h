@@ -152,6 +152,14 @@ int edyn_reactors_device(void* ctx, int n, const double* rho_d, const double* dt
  * statistics stay inside macks, SRC/source.f90:58). */
 int edyn_chem_stats(void* ctx, double* stats);
 
+/* The species and reactions the tube's chemistry integrates (either may be
+ * NULL): the whole mechanism, or, when some elements occur nowhere in the
+ * tube state nor at the inlet, the species made of the present elements and
+ * the reactions among them (the others have zero concentration and zero
+ * rates, so the result is the same). Chosen after every edyn_upload and
+ * edyn_init_cells. No counterpart in the reference. */
+int edyn_chem_set(void* ctx, int* nspec, int* nreac);
+
 /* Per-cell cost of the last chemistry launch of a tube: cost receives ncell
  * right-hand-side counts; hot (optional, 65 values) the cell list that gets
  * four-warp teams in the next launch ([0] = count). No counterpart in the

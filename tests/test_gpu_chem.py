@@ -104,6 +104,33 @@ def test_tube_chemistry_short_run(oracle, names):
     assert np.all(np.isfinite(hrr))
 
 
+def test_species_subset_matches_full_tables(oracle, names):
+    """CH4/O2 holds no N or Ar: the chemistry integrates the 34 C/H/O species
+    and their reactions. Traces of N2 and Ar (mass fraction 1e-300 in the
+    driver) bring back the full tables; both give the same tube."""
+    case = configs.detonation(ncell=256, length=256 * 50e-6, driver=48 * 50e-6)
+    qf0, qc0 = oracle.init_cells(case.T, case.p, case.u, case.X)
+    out, sets = [], []
+    for trace in (False, True):
+        qc = qc0.copy()
+        if trace:
+            for sp in ("N2", "AR"):
+                qc[:8, 3 + names.index(sp)] = qc[:8, 0] * 1e-300
+        g = Tube(case.ncell, case.dx, flag_acu=2, flag_weno=3, flag_rbound=1, do_reaction=1, rtol=1e-6, atol=1e-14)
+        g.upload(None, qc)
+        sets.append(g.chem_set())
+        for _ in range(4):
+            g.step(case.cfl)
+        out.append(g.download()[0])
+    K = len(names)
+    assert sets[0][0] == 34 and sets[0][1] < sets[1][1] and sets[1] == (K, sets[1][1]), sets
+    assert np.max(np.abs(out[0][:, 2] - out[1][:, 2]) / out[1][:, 2]) < 1e-5
+    rel_err, abs_err = species_err(out[0][:, 3:], out[1][:, 3:])
+    assert rel_err < 1e-3, rel_err
+    n_species = [i for i, s in enumerate(names) if "N" in s.replace("AR", "")] + [names.index("AR")]
+    assert np.all(out[0][:, 3 + np.array(n_species)] == 0.0)
+
+
 def test_table_exp_within_one_ulp():
     """The FP64 exponential of the rate evaluation (table-driven, Tang's
     method) against CUDA's exp: at most 1 ulp apart."""

@@ -253,7 +253,11 @@ int or_reactor(const or_mech* m, double rho_si, double dt, double* yiT, double r
       for (int i = 0; i < n; ++i)
         for (int j = 0; j < n; ++j)
           mm[i * n + j] = ((i == j ? 1.0 : 0.0) - h * SD_G * jac[i * n + j]) * (sc[j] / sc[i]);
-      if (lu_factor(mm, n, piv)) { h *= 0.25; continue; }
+      if (lu_factor(mm, n, piv)) {
+        h *= 0.25;
+        if (!(h >= dt * 1e-14)) { rc = 3; break; }
+        continue;
+      }
       int newton_ok = 1;
       for (int stg = 0; stg < 5 && newton_ok; ++stg) {
         for (int i = 0; i < n; ++i) {
@@ -328,6 +332,8 @@ int or_reactor(const or_mech* m, double rho_si, double dt, double* yiT, double r
       } else {
         st->rejects++;
         h = h * fmin(1.0, fmax(0.2, fac));
+        /* the step size underflowed (or the estimate was not a number) */
+        if (!(h >= dt * 1e-14)) { rc = 3; break; }
       }
     }
     if (rc) break;

@@ -75,6 +75,85 @@ def test_reactor_matches_oracle_same_tolerance(oracle, names):
     assert rel_err < 1e-3
 
 
+def ignition_delays(integrate, rho, yiT, t_max=1e-3, rise=400.0):
+    """Ignition delay of each fresh reactor: the time its temperature first
+    exceeds T0 + rise, bracketed by doubling time chunks from 1e-7 s and
+    refined by three bisections (to 1/8 of the bracket); reactors that do not
+    ignite by t_max get t_max. integrate(rho, dt, y) advances y in place."""
+    T0 = yiT[:, -1].copy()
+    n = len(rho)
+    tau = np.full(n, t_max)
+    t = np.zeros(n)
+    state = yiT.copy()
+    chunk = np.full(n, 1e-7)
+    active = np.ones(n, bool)
+    while active.any():
+        idx = np.nonzero(active)[0]
+        out = state[idx].copy()
+        integrate(rho[idx], chunk[idx], out)
+        ign = out[:, -1] > T0[idx] + rise
+        hit, miss = idx[ign], idx[~ign]
+        if len(hit):
+            lo, hi = np.zeros(len(hit)), chunk[hit].copy()
+            for _ in range(3):
+                mid = 0.5 * (lo + hi)
+                o = state[hit].copy()
+                integrate(rho[hit], mid, o)
+                up = o[:, -1] > T0[hit] + rise
+                hi, lo = np.where(up, mid, hi), np.where(up, lo, mid)
+            tau[hit] = t[hit] + hi
+            active[hit] = False
+        state[miss] = out[~ign]
+        t[miss] += chunk[miss]
+        chunk[miss] *= 2.0
+        active[miss[t[miss] >= t_max]] = False
+    return tau
+
+
+def test_partially_reacted_batch_vs_fp64_reference(oracle, names):
+    """The batched-reactor workload: CH4/air reactors with T ~ U[900, 2500] K,
+    p log-uniform in [1, 50] atm, phi ~ U[0.5, 2], each advanced a seeded
+    fraction U[0, 1] of its own ignition delay (capped at 1 ms: the slowest,
+    coolest mixtures are taken in early induction), then one GPU reactor step of
+    dt log-uniform in [1e-8, 1e-6] s against the FP64 oracle at tight
+    tolerance. The partially reacted states are inputs only: they come from
+    the library's reactor batch at rtol 1e-7 (long integrations at the
+    oracle's tight tolerance take minutes)."""
+    n = 128
+    rho, dt, fresh, _ = configs.reactor_batch(n, seed=0)
+    pre = Reactors(rtol=1e-7, atol=1e-15)
+
+    def integrate(r, d, y):
+        # windows of at most 10 us per call (a call takes at most 4000 steps)
+        rem = np.array(d, dtype=float)
+        while (rem > 0.0).any():
+            idx = np.nonzero(rem > 0.0)[0]
+            step = np.minimum(rem[idx], 1e-5)
+            sub = np.ascontiguousarray(y[idx])
+            st = pre.integrate(np.ascontiguousarray(r[idx]), step, sub)
+            assert st["failed"] == 0
+            y[idx] = sub
+            rem[idx] -= step
+
+    tau = ignition_delays(integrate, rho, fresh)
+    frac = np.random.default_rng(100).uniform(0.0, 1.0, n)
+    yiT = fresh.copy()
+    integrate(rho, frac * tau, yiT)
+    ref, fails, _ = oracle.reactor_batch(rho, dt, yiT, REF_RTOL, REF_ATOL)
+    assert fails == 0
+    r = Reactors(rtol=1e-6, atol=1e-14)
+    y = yiT.copy()
+    st = r.integrate(rho, dt, y)
+    assert st["failed"] == 0
+    K = len(names)
+    rel_err, abs_err = species_err(y[:, :K], ref[:, :K])
+    assert rel_err < 1e-3, rel_err
+    assert abs_err < 1e-9, abs_err
+    assert np.max(np.abs(y[:, K] - ref[:, K]) / ref[:, K]) < 1e-3
+    # the states span fresh to burnt
+    assert (yiT[:, K] - fresh[:, K]).max() > 500.0 and np.median(tau) < 1e-3
+
+
 def test_tube_chemistry_short_run(oracle, names):
     """Reacting detonation tube, a few full steps (fluid + chemistry)."""
     case = configs.detonation(ncell=512, length=512 * 50e-6, driver=64 * 50e-6)

@@ -36,8 +36,8 @@ UNIT = "cell-steps/s"
 BYTES_PER_CELL_STEP = 4544  # algorithmic: fluid RK3 3632 B + chemistry 912 B per cell-step
 BYTES_CHEM_PER_CELL = 912   # chemistry launch: read qf (456 B) + write qf and Qc rows (456 B)
 # DRAM bytes (read + write) of one chemistry launch per cell, from an ncu
-# capture of the 4,000-cell tube (2.22 MB read, 0 B written), scaled by cells
-TRAFFIC_CHEM_PER_CELL = 2.22e6 / 4000
+# capture of the 4,000-cell tube (1.93 MB read, 0 B written), scaled by cells
+TRAFFIC_CHEM_PER_CELL = 1.93e6 / 4000
 
 
 def parse():

@@ -961,10 +961,11 @@ __device__ void rhs64_team(const Tabs& t, const Team<TEAM>& tm, WarpWork& w, con
   // spare in phase 2)
   const double inv_rhocv = tid == 0 ? 1.0 / (rho * ycv) : 0.0;
   // phase 2: warp 3 turns its Pr and log10 Pr into the fall-off rate
-  // constants (the Troe factor, with its reciprocal and exponential) and
-  // takes the last of the other rounds; warp 1 forms the fall-off
-  // concentration products and hands them over through a named barrier;
-  // warps 0-2 take the other rounds in turn (all four without fall-off)
+  // constants (the Troe factor, with its reciprocal and exponential) and,
+  // when there are more than seven other rounds, takes the last one; warp 1
+  // forms the fall-off concentration products and hands them over through a
+  // named barrier; warps 0-2 take the other rounds in turn (all four without
+  // fall-off)
   auto rate_round = [&](int rr) {
     const int i = rr * 32 + lane;
     w.rop[i] = (i < t.nr) ? rop_pre(t, i, kfe[i], k0a, fcl, pfac, ipfac, ctot, w.C, w.m, w.wdot, w.en) : 0.0;
@@ -982,8 +983,9 @@ __device__ void rhs64_team(const Tabs& t, const Team<TEAM>& tm, WarpWork& w, con
       }
       pair_arrive(BAR_FALL_MA);
     }
+    const int nE3 = nE > 7 ? nE - 1 : nE;  // rounds for warps 0-2
     if (wq < 3) {
-      for (int e = wq; e < nE - 1; e += 3) rate_round(re(e));
+      for (int e = wq; e < nE3; e += 3) rate_round(re(e));
     } else {
       for (int r = 0; r < nfr; ++r) {
         const int i = (fr0 + r) * 32 + lane;
@@ -1002,7 +1004,7 @@ __device__ void rhs64_team(const Tabs& t, const Team<TEAM>& tm, WarpWork& w, con
         }
         fpr[r * 64 + lane] = kp;
       }
-      if (nE > 0) rate_round(re(nE - 1));
+      if (nE3 < nE) rate_round(re(nE - 1));
       pair_wait(BAR_FALL_MA);
       for (int r = 0; r < nfr; ++r) {
         const int i = (fr0 + r) * 32 + lane;

@@ -867,6 +867,52 @@ __device__ void rhs(const Tabs& t, const Team<TW>& tm, WarpWork& w, const R* y, 
   tm.sync();
 }
 
+// Species k's FP64 thermodynamics for the rates, as values (species_one's
+// FP64 branch without its stores, so that a caller can interleave it with
+// independent work and store under a predicate).
+struct SpeciesVals {
+  double m, mi, uR, cvm;
+  int en;
+};
+__device__ __forceinline__ SpeciesVals species_vals(const Tabs& t, int k, double c, double T, double logT,
+                                                    double invT, double pfac, double ipfac) {
+  const RTabs<double>& x = t.d;
+  SpeciesVals o;
+  const int r = (T > x.tmid[k]) ? 1 : 0;
+  const double* cs = x.cs + r * 7 * NSMAX;
+  double p = fma(cs[4 * NSMAX + k], T, cs[3 * NSMAX + k]);
+  p = fma(p, T, cs[2 * NSMAX + k]);
+  p = fma(p, T, cs[1 * NSMAX + k]);
+  const double smh = fma(p, T, fma(cs[0 * NSMAX + k], logT - 1, cs[6 * NSMAX + k])) - cs[5 * NSMAX + k] * invT;
+  const double nn = Math<double>::rint_(smh * 1.4426950408889634);
+  const double rr = fma(-nn, 6.93147180369123816490e-01, smh) - nn * 1.90821492927058770002e-10;
+  const double e = texp_r(rr, t.e2);
+  o.m = e * pfac;
+  o.mi = (c * ipfac) * __drcp_rn(e);
+  o.en = (int)nn;
+  const double* ch = x.ch + r * 6 * NSMAX;
+  double h = fma(ch[4 * NSMAX + k], T, ch[3 * NSMAX + k]);
+  h = fma(h, T, ch[2 * NSMAX + k]);
+  h = fma(h, T, ch[1 * NSMAX + k]);
+  h = fma(h, T, ch[0 * NSMAX + k]);
+  o.uR = fma(h, T, ch[5 * NSMAX + k]) - T;
+  const double* cc = x.cp + r * 5 * NSMAX;
+  double cp = fma(cc[4 * NSMAX + k], T, cc[3 * NSMAX + k]);
+  cp = fma(cp, T, cc[2 * NSMAX + k]);
+  cp = fma(cp, T, cc[1 * NSMAX + k]);
+  cp = fma(cp, T, cc[0 * NSMAX + k]);
+  o.cvm = (cp - 1) * x.invW[k];
+  return o;
+}
+
+// arrhenius<double> without a branch: a reaction without an exponential
+// factor takes texp_a(0) = 1 exactly, so the value is the same.
+__device__ __forceinline__ double arrhenius_bl(const Tabs& t, int i, double logT, double invT) {
+  const RTabs<double>& x = t.d;
+  const bool ex = ((t.w0[i] >> 24) & F_EXP) != 0;
+  return x.A[i] * texp_a(ex ? x.B[i] * logT - x.E[i] * invT : 0.0, t.e2);
+}
+
 // The FP64 right-hand side by a four-warp team, balanced over its warps.
 // Phase 1: warps 0-1 run the species pass while warp 2 evaluates the
 // temperature-only parts of the fall-off reactions (k_inf, k0, log10 Fcent:
@@ -918,12 +964,30 @@ __device__ void rhs64_team(const Tabs& t, const Team<TEAM>& tm, WarpWork& w, con
   double ycv = 0.0;        // sum Y_k cv_k
   int e0 = 0, e1 = 0;
   if (wq < 2) {
-    for (int k = tid; k < ns; k += 64) {
-      species_one<double, false>(t, k, y, rho, T, logT, invT, pfac, ipfac, w.C, w.m, w.wdot, w.en, w.uR, w.cvm);
-      ycv = fma(y[k], w.cvm[k], ycv);
+    // the species pass (one species per lane: ns <= 64) and this warp's two
+    // Arrhenius rounds as one straight block: three independent chains that
+    // the compiler interleaves (a lone warp issues an FP64 instruction per
+    // 64 cycles at best, and a single chain also waits on each result);
+    // loads stay in range and stores go under predicates
+    const bool sp = tid < ns;
+    const int k = sp ? tid : ns - 1;
+    const int ea = 2 * wq, eb = 2 * wq + 1;
+    const int ia = re(ea < nE ? ea : 0) * 32 + lane, ib = re(eb < nE ? eb : 0) * 32 + lane;
+    const double c = w.C[k];
+    const SpeciesVals v = species_vals(t, k, c, T, logT, invT, pfac, ipfac);
+    const double kfa = arrhenius_bl(t, ia, logT, invT);
+    const double kfb = arrhenius_bl(t, ib, logT, invT);
+    if (sp) {
+      w.m[k] = v.m;
+      w.wdot[k] = v.mi;
+      w.en[k] = v.en;
+      w.uR[k] = v.uR;
+      w.cvm[k] = v.cvm;
+      ycv = y[k] * v.cvm;
     }
-    e0 = wq == 0 ? 0 : 2;
-    e1 = wq == 0 ? 2 : 4;
+    if (ea < nE && ia < t.nr) kfe[ia] = kfa;
+    if (eb < nE && ib < t.nr) kfe[ib] = kfb;
+    e0 = e1 = 0;
   } else if (wq == 2) {
     for (int r = 0; r < nfr; ++r) {
       const int i = (fr0 + r) * 32 + lane;

@@ -1,7 +1,7 @@
 """Generates the golden fixtures of tests/golden from the reference checkout.
 
 Run where the reference tree is present (path in $EDYN_REFERENCE, default
-the checkout this build was made from):
+the reference checkout's location on the machine that generated them):
 
     python tests/golden/make_golden.py
 

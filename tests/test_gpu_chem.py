@@ -1,6 +1,6 @@
 """GPU chemistry vs the FP64 reference integrator of the oracle.
 
-Bar (the benchmark spec): species within 1e-3 relative and peak temperature within
+Bar: species within 1e-3 relative and peak temperature within
 0.1% of the FP64 reference for reacting cases. Species below 1e-6 in mass
 fraction are compared in absolute terms (1e-9).
 """

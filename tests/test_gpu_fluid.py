@@ -1,8 +1,7 @@
 """GPU fluid path vs the CPU oracle (restatement of the reference's CPU code).
 
-Tolerance: the reference's north star asks for pressure, velocity and
-temperature within 1e-10 relative for non-reacting flow; that is the bar
-used here, on the full Sod run and on short runs of every scheme.
+Tolerance: pressure, velocity and temperature within 1e-10 relative for
+non-reacting flow, on the full Sod run and on short runs of every scheme.
 """
 import numpy as np
 import pytest

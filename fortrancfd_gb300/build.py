@@ -19,7 +19,7 @@ LIBDIR = PKG / "_lib"
 LIBNAME = "libedyn_gb300.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-fno-fast-math"]
-SOURCES = ["mechanism.cpp", "fluid.cu", "chem.cu", "edyn_api.cu"]
+SOURCES = ["mechanism.cpp", "fluid.cu", "chem.cu", "mlp.cu", "edyn_api.cu"]
 
 
 def _nvcc() -> str:
@@ -40,7 +40,7 @@ def build_library(verbose: bool = False, force: bool = False) -> Path:
     nvcc = _nvcc()
     objdir = LIBDIR / "obj"
     objdir.mkdir(parents=True, exist_ok=True)
-    headers = list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + [ROOT / "include" / "edyn_gpu.h"]
+    headers = list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + list((ROOT / "include").glob("*.h"))
     procs = []
     objs = []
     for src in SOURCES:

@@ -1808,6 +1808,30 @@ __global__ void __launch_bounds__(MAXW * 32, 1)
   }
 }
 
+// FP64 right-hand side f = d(Y_1..Y_ns, T)/dt of a batch of reactors (the
+// function integrate() advances), one warp per cell.
+__global__ void __launch_bounds__(MAXW * 32, 1)
+    k_reactor_rhs(const char* g_tab, int tab_bytes, int n, const double* rho, const double* yiT, double* f) {
+  extern __shared__ __align__(16) char smem[];
+  stage_tables(smem, g_tab, tab_bytes);
+  const Tabs t = bind_tabs(smem);
+  WarpWork& w = work_slots(smem, tab_bytes)[threadIdx.x >> 5];
+  const int lane = threadIdx.x & 31;
+  const Team<32> tm{lane, 0, nullptr, nullptr, nullptr, nullptr};
+  const int nv = t.ns + 1;
+  const int nw = blockDim.x >> 5;
+  for (int cell = blockIdx.x * nw + (threadIdx.x >> 5); cell < n; cell += gridDim.x * nw) {
+    const double* src = yiT + (size_t)cell * nv;
+    for (int i = lane; i < nv; i += 32) w.y0[i] = src[i];
+    __syncwarp();
+    rhs64<32>(t, tm, w, w.y0, rho[cell] * 1e-3, w.fy);
+    __syncwarp();
+    double* dst = f + (size_t)cell * nv;
+    for (int i = lane; i < nv; i += 32) dst[i] = w.fy[i];
+    __syncwarp();
+  }
+}
+
 // One tube cell: reaction_macks (SRC/source.f90:17-84) followed by the
 // post-step QcToqf (SRC/main.f90:157-161). Returns the right-hand sides the
 // cell took (its cost, which picks the cells that get a team next time).
@@ -2495,6 +2519,8 @@ int chem_init(ChemState& s, const edyn_mech& m, const ThermoTable& tb, cudaStrea
   if (e != cudaSuccess) return (int)e;
   e = cudaFuncSetAttribute(k_tube_chem, cudaFuncAttributeMaxDynamicSharedMemorySize, want);
   if (e != cudaSuccess) return (int)e;
+  e = cudaFuncSetAttribute(k_reactor_rhs, cudaFuncAttributeMaxDynamicSharedMemorySize, want);
+  if (e != cudaSuccess) return (int)e;
   int per_sm = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_reactors, s.warps * 32, s.smem);
   s.ctas = nsm * std::max(1, per_sm);
@@ -2510,6 +2536,13 @@ cudaError_t chem_launch_batch(ChemState& s, const ChemLaunch& L, cudaStream_t st
   k_reactors<<<std::max(1, grid), s.warps * 32, s.smem, st>>>((const char*)s.d_tables, (int)s.table_bytes, L.n,
                                                             L.rho_batch, L.dt_batch, L.yiT_batch, L.rtol, L.atol,
                                                             s.d_next, s.d_count, L.err);
+  return cudaGetLastError();
+}
+
+cudaError_t chem_rhs_batch(ChemState& s, int n, const double* rho, const double* yiT, double* f, cudaStream_t st) {
+  const int grid = std::min(s.ctas, (n + s.warps - 1) / s.warps);
+  k_reactor_rhs<<<std::max(1, grid), s.warps * 32, s.smem, st>>>((const char*)s.d_tables, (int)s.table_bytes, n, rho,
+                                                                yiT, f);
   return cudaGetLastError();
 }
 

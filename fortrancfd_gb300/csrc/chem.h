@@ -57,6 +57,8 @@ int chem_init(ChemState& s, const edyn_mech& m, const ThermoTable& tb, cudaStrea
               int nnorm = 0);
 cudaError_t chem_launch_tube(ChemState& s, const ChemLaunch& L, cudaStream_t st);
 cudaError_t chem_launch_batch(ChemState& s, const ChemLaunch& L, cudaStream_t st);
+// FP64 right-hand side d(Y, T)/dt of n reactors (rho SI, yiT rows of ns + 1).
+cudaError_t chem_rhs_batch(ChemState& s, int n, const double* rho, const double* yiT, double* f, cudaStream_t st);
 cudaError_t chem_read_counters(ChemState& s, ChemCounters* out, cudaStream_t st);
 cudaError_t chem_check_exp(ChemState& s, int n, const double* x_d, unsigned long long* maxulp_d, cudaStream_t st);
 cudaError_t chem_check_log(ChemState& s, int n, const double* x_d, unsigned long long* maxulp_d, cudaStream_t st);

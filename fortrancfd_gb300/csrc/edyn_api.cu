@@ -19,6 +19,7 @@
 #include <vector>
 
 #include "../../include/edyn_gpu.h"
+#include "../../include/edyn_surrogate.h"
 #include "chem.h"
 #include "edyn_dev.cuh"
 #include "edyn_kernels.h"
@@ -755,6 +756,15 @@ int edyn_reactors_device(void* ctx, int n, const double* rho_d, const double* dt
     CK(cudaMemset(c->d_err, 0, sizeof(unsigned)));
     return fail(c, (int)st, "reactor status 0x%x", st);
   }
+  return EDYN_OK;
+}
+
+int edyn_chem_rhs_device(void* ctx, int n, const double* rho_d, const double* yiT_d, double* f_d) {
+  Ctx* c = (Ctx*)ctx;
+  if (!c || n < 0 || (n > 0 && (!rho_d || !yiT_d || !f_d))) return EDYN_E_ARG;
+  if (n == 0) return EDYN_OK;
+  cudaError_t e = chem_rhs_batch(c->chem, n, rho_d, yiT_d, f_d, c->stream);
+  if (e != cudaSuccess) return fail(c, EDYN_E_CUDA, "right-hand side launch: %s", cudaGetErrorString(e));
   return EDYN_OK;
 }
 

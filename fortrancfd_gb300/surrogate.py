@@ -436,3 +436,35 @@ def timed(fn, *a, **k):
     r = fn(*a, **k)
     torch.cuda.synchronize()
     return r, time.perf_counter() - t0
+
+
+def _main():
+    """Times the MLP's forward pass (four tensor-core GEMMs with fused
+    epilogues) on a batch of random standardised inputs; prints one JSON
+    line with the achieved dense BF16 rate."""
+    import argparse
+    import json
+
+    ap = argparse.ArgumentParser(description=_main.__doc__)
+    ap.add_argument("--rows", type=int, default=1 << 20)
+    ap.add_argument("--reps", type=int, default=10)
+    a = ap.parse_args()
+    m = MLP(seed=0)
+    X = torch.randn(a.rows, KIN, device="cuda").to(torch.bfloat16)
+    for _ in range(3):
+        m.forward(X)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(a.reps):
+        m.forward(X)
+    e1.record()
+    e1.synchronize()
+    status()
+    ms = e0.elapsed_time(e1) / a.reps
+    flops = 2.0 * a.rows * (KIN * HID + (DEPTH - 1) * HID * HID + HID * KOUT)
+    print(json.dumps({"rows": a.rows, "forward_ms": ms, "tflops": flops / ms / 1e9, "launches_per_forward": DEPTH + 1}))
+
+
+if __name__ == "__main__":
+    _main()

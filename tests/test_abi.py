@@ -40,3 +40,16 @@ def test_product_path_does_not_touch_the_oracle():
             txt = p.read_text()
             for bad in ("oracle_ctypes", "libedyn_oracle", "edyn_oracle.h", "or_reactor", "or_step", "mlp_ref"):
                 assert not re.search(r"\b" + re.escape(bad), txt), (p, bad)
+
+
+def test_surrogate_constants_match_the_header():
+    from fortrancfd_gb300 import surrogate as S
+
+    txt = (ROOT / "include" / "edyn_surrogate.h").read_text()
+    defs = dict(re.findall(r"#define (EDYN_MLP_EPI_\w+) (\d+)", txt))
+    assert int(defs["EDYN_MLP_EPI_F32"]) == S.EPI_F32
+    assert int(defs["EDYN_MLP_EPI_GELU"]) == S.EPI_GELU
+    assert int(defs["EDYN_MLP_EPI_DGELU"]) == S.EPI_DGELU
+    # padded widths are multiples of the GEMM's 64-column tiles
+    assert S.KIN % 64 == 0 and S.KOUT % 64 == 0 and S.HID % 64 == 0
+    assert S.NIN <= S.KIN and S.NOUT <= S.KOUT

@@ -46,7 +46,20 @@ struct GemmArgs {
   int ldc16;
   const float* Z;     // EPI_DGELU: the forward pre-activation
   int ldz;
+  int c16_tiled;      // EPI_GELU: C16 written in the tiled layout (128-row blocks, K = N) instead of row-major
 };
+
+// Tiled layout of a row-major [R][K] matrix for the bulk-copy GEMM: blocks
+// of BR rows x 64 k-columns, block (r / BR, k / 64) at element
+// ((r / BR) * (K / 64) + k / 64) * BR * 64, each block in the core-matrix
+// layout of the shared-memory tiles (element (r, k) of the block at
+// ((r / 8) * 8 + k / 8) * 64 + (r % 8) * 8 + k % 8). A block is one
+// contiguous bulk copy.
+__host__ __device__ __forceinline__ size_t tiled_off(int r, int k, int BR, int K) {
+  const int rl = r % BR, kl = k % 64;
+  return ((size_t)(r / BR) * (K / 64) + k / 64) * (size_t)BR * 64 + ((rl >> 3) * 8 + (kl >> 3)) * 64 + (rl & 7) * 8 +
+         (kl & 7);
+}
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return (uint32_t)__cvta_generic_to_shared(p);
@@ -127,6 +140,22 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
   for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// 32 consecutive FP32 columns of this thread's TMEM lane, one wait.
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,"
+      "%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+        "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+        "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
 __device__ __forceinline__ float gelu(float z) { return 0.5f * z * (1.f + erff(z * 0.70710678118654752f)); }
 __device__ __forceinline__ float dgelu(float z) {
   return 0.5f * (1.f + erff(z * 0.70710678118654752f)) + z * 0.39894228040143268f * expf(-0.5f * z * z);
@@ -151,6 +180,65 @@ __device__ __forceinline__ void stage_tile(char* dst, const __nv_bfloat16* src, 
   }
 }
 
+// Reads the 128 x BN FP32 accumulator from TMEM (warp w: rows 32w..32w+31)
+// and applies the fused epilogue of a.
+template <int BN>
+__device__ __forceinline__ void epilogue(const GemmArgs& a, uint32_t tmem, int m0, int n0) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int row = m0 + warp * 32 + lane;
+  const bool live = row < a.M;
+  for (int c32 = 0; c32 < BN; c32 += 32) {
+    float w32[32];
+    tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c32, w32);
+    if (!live) continue;
+#pragma unroll
+    for (int half = 0; half < 2; ++half) {
+      const float* v = w32 + 16 * half;
+      const int col = n0 + c32 + 16 * half;
+      if (a.epi == EPI_F32) {
+        float* o = a.C32 + (size_t)row * a.ldc + col;
+#pragma unroll
+        for (int i = 0; i < 16; i += 4) {
+          float4 q;
+          q.x = v[i] + (a.bias ? a.bias[col + i] : 0.f);
+          q.y = v[i + 1] + (a.bias ? a.bias[col + i + 1] : 0.f);
+          q.z = v[i + 2] + (a.bias ? a.bias[col + i + 2] : 0.f);
+          q.w = v[i + 3] + (a.bias ? a.bias[col + i + 3] : 0.f);
+          *reinterpret_cast<float4*>(o + i) = q;
+        }
+      } else if (a.epi == EPI_GELU) {
+        __align__(16) __nv_bfloat16 h[16];
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+          const float z = v[i] + (a.bias ? a.bias[col + i] : 0.f);
+          if (a.C32) a.C32[(size_t)row * a.ldc + col + i] = z;
+          h[i] = __float2bfloat16_rn(gelu(z));
+        }
+        if (a.c16_tiled) {
+          *reinterpret_cast<uint4*>(a.C16 + tiled_off(row, col, BM, a.N)) = reinterpret_cast<const uint4*>(h)[0];
+          *reinterpret_cast<uint4*>(a.C16 + tiled_off(row, col + 8, BM, a.N)) = reinterpret_cast<const uint4*>(h)[1];
+        } else {
+          uint4* o = reinterpret_cast<uint4*>(a.C16 + (size_t)row * a.ldc16 + col);
+          o[0] = reinterpret_cast<const uint4*>(h)[0];
+          o[1] = reinterpret_cast<const uint4*>(h)[1];
+        }
+      } else {
+        __align__(16) __nv_bfloat16 h[16];
+        const float* z = a.Z + (size_t)row * a.ldz + col;
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+          const float g = v[i] * dgelu(z[i]);
+          if (a.C32) a.C32[(size_t)row * a.ldc + col + i] = g;
+          h[i] = __float2bfloat16_rn(g);
+        }
+        uint4* o = reinterpret_cast<uint4*>(a.C16 + (size_t)row * a.ldc16 + col);
+        o[0] = reinterpret_cast<const uint4*>(h)[0];
+        o[1] = reinterpret_cast<const uint4*>(h)[1];
+      }
+    }
+  }
+}
+
 template <int BN>
 __global__ void __launch_bounds__(128, 1) k_gemm(GemmArgs a) {
   constexpr int A_BYTES = BM * BK * 2;
@@ -159,7 +247,7 @@ __global__ void __launch_bounds__(128, 1) k_gemm(GemmArgs a) {
   extern __shared__ __align__(1024) char smem[];
   __shared__ uint64_t bar[2];
   __shared__ uint32_t tmem_slot;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
   const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
   char* base = smem + ((1024 - (smem_u32(smem) & 1023)) & 1023);
 
@@ -211,51 +299,7 @@ __global__ void __launch_bounds__(128, 1) k_gemm(GemmArgs a) {
   ok = __syncthreads_and(ok) && last == nk - 1;
   tc_fence_after();
 
-  if (ok) {
-    const int row = m0 + warp * 32 + lane;
-    const bool live = row < a.M;
-    for (int c0 = 0; c0 < BN; c0 += 16) {
-      float v[16];
-      tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
-      if (!live) continue;
-      const int col = n0 + c0;
-      if (a.epi == EPI_F32) {
-        float* o = a.C32 + (size_t)row * a.ldc + col;
-#pragma unroll
-        for (int i = 0; i < 16; i += 4) {
-          float4 q;
-          q.x = v[i] + (a.bias ? a.bias[col + i] : 0.f);
-          q.y = v[i + 1] + (a.bias ? a.bias[col + i + 1] : 0.f);
-          q.z = v[i + 2] + (a.bias ? a.bias[col + i + 2] : 0.f);
-          q.w = v[i + 3] + (a.bias ? a.bias[col + i + 3] : 0.f);
-          *reinterpret_cast<float4*>(o + i) = q;
-        }
-      } else if (a.epi == EPI_GELU) {
-        __align__(16) __nv_bfloat16 h[16];
-#pragma unroll
-        for (int i = 0; i < 16; ++i) {
-          const float z = v[i] + (a.bias ? a.bias[col + i] : 0.f);
-          if (a.C32) a.C32[(size_t)row * a.ldc + col + i] = z;
-          h[i] = __float2bfloat16_rn(gelu(z));
-        }
-        uint4* o = reinterpret_cast<uint4*>(a.C16 + (size_t)row * a.ldc16 + col);
-        o[0] = reinterpret_cast<const uint4*>(h)[0];
-        o[1] = reinterpret_cast<const uint4*>(h)[1];
-      } else {
-        __align__(16) __nv_bfloat16 h[16];
-        const float* z = a.Z + (size_t)row * a.ldz + col;
-#pragma unroll
-        for (int i = 0; i < 16; ++i) {
-          const float g = v[i] * dgelu(z[i]);
-          if (a.C32) a.C32[(size_t)row * a.ldc + col + i] = g;
-          h[i] = __float2bfloat16_rn(g);
-        }
-        uint4* o = reinterpret_cast<uint4*>(a.C16 + (size_t)row * a.ldc16 + col);
-        o[0] = reinterpret_cast<const uint4*>(h)[0];
-        o[1] = reinterpret_cast<const uint4*>(h)[1];
-      }
-    }
-  }
+  if (ok) epilogue<BN>(a, tmem, m0, n0);
   if (!ok && threadIdx.x == 0) atomicOr(&g_err, 1u);
   tc_fence_before();
   __syncthreads();
@@ -281,6 +325,142 @@ cudaError_t launch_gemm(const GemmArgs& a, cudaStream_t s) {
   dim3 grid((a.M + BM - 1) / BM, a.N / BN);
   k_gemm<BN><<<grid, 128, gemm_smem<BN>(), s>>>(a);
   return cudaGetLastError();
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* b, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)), "r"(bytes) : "memory");
+}
+
+// One contiguous global -> shared copy by the bulk-copy (TMA) engine; its
+// bytes complete the transaction count of the mbarrier.
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* b) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(smem_u32(b))
+               : "memory");
+}
+
+// C = A B^T with both operands pre-tiled (tiled_off: A in 128-row blocks,
+// B in BN-row blocks): every stage of the ST-deep ring is two bulk copies,
+// 16 KB of A and BN x 128 bytes of B. Thread 0 issues the products of tile
+// kt as soon as its copies land, commits them to the stage's "empty"
+// barrier, and only then refills the stage of tile kt - 1 with tile
+// kt + ST - 1, so the tensor core always has the next products queued.
+// Every BN keeps at least two CTAs per SM (shared memory and TMEM), so one
+// CTA's epilogue runs under another's copies and products.
+template <int BN, int ST>
+__global__ void __launch_bounds__(128, 1) k_gemm_tiled(GemmArgs a) {
+  constexpr int A_BYTES = BM * BK * 2;
+  constexpr int B_BYTES = BN * BK * 2;
+  constexpr int STAGE = A_BYTES + B_BYTES;
+  extern __shared__ __align__(1024) char smem[];
+  __shared__ uint64_t full[ST], empty[ST];
+  __shared__ uint32_t tmem_slot;
+  __shared__ int s_last;
+  const int warp = threadIdx.x >> 5;
+  const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
+  char* base = smem + ((1024 - (smem_u32(smem) & 1023)) & 1023);
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
+                 "r"(BN));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (threadIdx.x == 0) {
+    for (int q = 0; q < ST; ++q) {
+      mbar_init(&full[q], 1);
+      mbar_init(&empty[q], 1);
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_slot;
+  constexpr uint32_t IDESC = idesc_bf16(BM, BN);
+  const int nk = a.K / BK;
+  const char* gA = reinterpret_cast<const char*>(a.A) + (size_t)blockIdx.x * nk * A_BYTES;
+  const char* gB = reinterpret_cast<const char*>(a.B) + (size_t)blockIdx.y * nk * B_BYTES;
+  bool ok = true;
+  int last = -1, produced = 0;
+  if (threadIdx.x == 0) {
+    auto produce = [&](int kt) -> bool {
+      const int q = kt % ST;
+      if (kt >= ST && !mbar_wait(&empty[q], ((kt / ST) - 1) & 1)) return false;
+      char* sa = base + q * STAGE;
+      mbar_expect_tx(&full[q], STAGE);
+      bulk_g2s(sa, gA + (size_t)kt * A_BYTES, A_BYTES, &full[q]);
+      bulk_g2s(sa + A_BYTES, gB + (size_t)kt * B_BYTES, B_BYTES, &full[q]);
+      produced = kt + 1;
+      return true;
+    };
+    for (int kt = 0; kt < ST - 1 && kt < nk && ok; ++kt) ok = produce(kt);
+    for (int kt = 0; kt < nk && ok; ++kt) {
+      const int q = kt % ST;
+      if (!mbar_wait(&full[q], (kt / ST) & 1)) {
+        ok = false;
+        break;
+      }
+      tc_fence_after();
+      const uint32_t a0 = smem_u32(base + q * STAGE), b0 = a0 + A_BYTES;
+#pragma unroll
+      for (int k = 0; k < BK / 16; ++k)
+        mma_bf16(tmem, sdesc(a0 + k * 256, 128, 1024), sdesc(b0 + k * 256, 128, 1024), IDESC,
+                 (kt > 0 || k > 0) ? 1u : 0u);
+      mma_commit(&empty[q]);
+      last = kt;
+      if (kt + ST - 1 < nk) ok = produce(kt + ST - 1);
+    }
+    // nothing may be in flight when the CTA leaves: the copies issued but
+    // not consumed, and the products of the last issued tile
+    for (int kt = last + 1; kt < produced; ++kt) mbar_wait(&full[kt % ST], (kt / ST) & 1);
+    if (last >= 0 && !mbar_wait(&empty[last % ST], (last / ST) & 1)) ok = false;
+  }
+  if (threadIdx.x == 0) s_last = last;
+  ok = __syncthreads_and(ok);
+  ok = ok && s_last == nk - 1;
+  tc_fence_after();
+  if (ok) epilogue<BN>(a, tmem, m0, n0);
+  if (!ok && threadIdx.x == 0) atomicOr(&g_err, 1u);
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(BN));
+  }
+}
+
+constexpr int TILED_STAGES = 2;  // 97 KB at BN = 256: two CTAs per SM, one's epilogue under the other's products
+
+template <int BN>
+constexpr int gemm_tiled_smem() {
+  return TILED_STAGES * (BM * BK * 2 + BN * BK * 2) + 1024;
+}
+
+template <int BN>
+cudaError_t launch_gemm_tiled(const GemmArgs& a, cudaStream_t s) {
+  static bool attr = false;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(k_gemm_tiled<BN, TILED_STAGES>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         gemm_tiled_smem<BN>());
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  dim3 grid(a.M / BM, a.N / BN);
+  k_gemm_tiled<BN, TILED_STAGES><<<grid, 128, gemm_tiled_smem<BN>(), s>>>(a);
+  return cudaGetLastError();
+}
+
+// Row-major [R][K] bf16 -> tiled layout with BR-row blocks; rows R..Rp-1 of
+// the last block (Rp = R rounded up to BR) are zero. One thread per 8
+// consecutive k-columns.
+__global__ void k_tile(const __nv_bfloat16* in, int R, int K, int BR, __nv_bfloat16* out) {
+  const long q = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int Rp = (R + BR - 1) / BR * BR;
+  if (q >= (long)Rp * (K / 8)) return;
+  const int r = (int)(q / (K / 8)), k = (int)(q % (K / 8)) * 8;
+  uint4 v = make_uint4(0, 0, 0, 0);
+  if (r < R) v = *reinterpret_cast<const uint4*>(in + (size_t)r * K + k);
+  *reinterpret_cast<uint4*>(out + tiled_off(r, k, BR, K)) = v;
 }
 
 // out[c][r] = in[r][c] for a rows x cols bf16 matrix (32 x 32 tiles).
@@ -519,11 +699,42 @@ int edyn_mlp_gemm(const void* A, int lda, const void* B, int ldb, int M, int N, 
   if (epi == EPI_DGELU && (!Z || ldz < N)) return EDYN_E_ARG;
   if (epi < EPI_F32 || epi > EPI_DGELU) return EDYN_E_ARG;
   GemmArgs a{(const __nv_bfloat16*)A, (const __nv_bfloat16*)B, lda, ldb, M, N, K, epi, bias, C32, ldc,
-             (__nv_bfloat16*)C16, ldc16, Z, ldz};
+             (__nv_bfloat16*)C16, ldc16, Z, ldz, 0};
   cudaError_t e;
   if (N % 256 == 0) e = launch_gemm<256>(a, S(stream));
   else if (N % 128 == 0) e = launch_gemm<128>(a, S(stream));
   else e = launch_gemm<64>(a, S(stream));
+  return rc(e);
+}
+
+int edyn_mlp_tile_rows(int N) { return N % 256 == 0 ? 256 : N % 128 == 0 ? 128 : 64; }
+
+int edyn_mlp_tile(const void* in, int R, int K, int BR, void* out, void* stream) {
+  if (!in || !out || R <= 0 || K <= 0 || K % 64 || (BR != 64 && BR != 128 && BR != 256)) return EDYN_E_ARG;
+  if ((((uintptr_t)in) | ((uintptr_t)out)) & 15) return EDYN_E_ARG;
+  const long tot = (long)((R + BR - 1) / BR * BR) * (K / 8);
+  k_tile<<<(unsigned)((tot + 255) / 256), 256, 0, S(stream)>>>((const __nv_bfloat16*)in, R, K, BR,
+                                                              (__nv_bfloat16*)out);
+  return rc(cudaGetLastError());
+}
+
+int edyn_mlp_gemm_tiled(const void* At, const void* Bt, int M, int N, int K, int epi, const float* bias, float* C32,
+                        int ldc, void* C16, int ldc16, int c16_tiled, void* stream) {
+  if (!At || !Bt || M <= 0 || M % BM || N <= 0 || N % 64 || K <= 0 || K % BK) return EDYN_E_ARG;
+  if ((((uintptr_t)At) | ((uintptr_t)Bt)) & 15) return EDYN_E_ARG;
+  if (epi == EPI_F32 && (!C32 || ldc % 4 || ldc < N || (((uintptr_t)C32) & 15))) return EDYN_E_ARG;
+  if (epi == EPI_GELU && (!C16 || (((uintptr_t)C16) & 15) || (!c16_tiled && (ldc16 % 8 || ldc16 < N))))
+    return EDYN_E_ARG;
+  if (epi == EPI_GELU && C32 && ldc < N) return EDYN_E_ARG;
+  if (epi != EPI_F32 && epi != EPI_GELU) return EDYN_E_ARG;
+  GemmArgs a{(const __nv_bfloat16*)At, (const __nv_bfloat16*)Bt, 0, 0, M, N, K, epi, bias, C32, ldc,
+             (__nv_bfloat16*)C16, ldc16, nullptr, 0, epi == EPI_GELU ? c16_tiled : 0};
+  cudaError_t e;
+  switch (edyn_mlp_tile_rows(N)) {
+    case 256: e = launch_gemm_tiled<256>(a, S(stream)); break;
+    case 128: e = launch_gemm_tiled<128>(a, S(stream)); break;
+    default: e = launch_gemm_tiled<64>(a, S(stream)); break;
+  }
   return rc(e);
 }
 

@@ -67,6 +67,9 @@ def _L():
         L.edyn_mlp_compact.argtypes = [i, i, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]
         L.edyn_mlp_scatter.argtypes = [i, i, vp, vp, vp, vp]
         L.edyn_chem_rhs_device.argtypes = [vp, i, vp, vp, vp]
+        L.edyn_mlp_gemm_tiled.argtypes = [vp, vp, i, i, i, i, vp, vp, i, vp, i, i, vp]
+        L.edyn_mlp_tile.argtypes = [vp, i, i, i, vp, vp]
+        L.edyn_mlp_tile_rows.argtypes = [i]
         _bound = True
     return L
 
@@ -90,6 +93,27 @@ def gemm(A, B, M, N, K, epi, bias=None, C32=None, C16=None, Z=None):
     _ck(_L().edyn_mlp_gemm(_p(A), A.stride(0), _p(B), B.stride(0), M, N, K, epi, _p(bias), _p(C32),
                            C32.stride(0) if C32 is not None else 0, _p(C16), C16.stride(0) if C16 is not None else 0,
                            _p(Z), Z.stride(0) if Z is not None else 0, _stream()), "mlp gemm")
+
+
+def gemm_tiled(At, Bt, M, N, K, epi, bias=None, C32=None, C16=None, c16_tiled=False):
+    """The bulk-copy GEMM on pre-tiled operands (see tile())."""
+    _ck(_L().edyn_mlp_gemm_tiled(_p(At), _p(Bt), M, N, K, epi, _p(bias), _p(C32),
+                                 C32.stride(0) if C32 is not None else 0, _p(C16),
+                                 C16.shape[-1] if C16 is not None else 0, int(c16_tiled), _stream()), "mlp gemm tiled")
+
+
+def tile_rows(N):
+    return _L().edyn_mlp_tile_rows(N)
+
+
+def tile(x, br, out=None):
+    """Row-major [R][K] BF16 -> the tiled operand layout with br-row blocks
+    (rows padded with zeros to a multiple of br); returned flat."""
+    R, K = x.shape
+    Rp = (R + br - 1) // br * br
+    out = torch.empty(Rp * K, dtype=x.dtype, device=x.device) if out is None else out
+    _ck(_L().edyn_mlp_tile(_p(x), R, K, br, _p(out), _stream()), "mlp tile")
+    return out
 
 
 def transpose(x, out=None):
@@ -189,6 +213,29 @@ class MLP:
         gemm(B["H"][DEPTH], self.W16[DEPTH], M, KOUT, HID, EPI_F32, bias=self.b[DEPTH], C32=B["Y"])
         return B["Y"]
 
+    def forward_tiled(self, X16):
+        """forward() for inference through the bulk-copy GEMM: the inputs and
+        weights are tiled once, each layer writes its activations tiled for
+        the next. X16 rows: a multiple of 128."""
+        M = X16.shape[0]
+        if getattr(self, "_tiled_at", None) != self.step_count:
+            self.Wt = [tile(w, tile_rows(w.shape[0])) for w in self.W16]
+            self._tiled_at = self.step_count
+        key = ("tiled", M)
+        if key not in self._buf:
+            d, bf = self.device, torch.bfloat16
+            self._buf[key] = dict(X=torch.empty(M * KIN, dtype=bf, device=d),
+                                  H=[torch.empty(M * HID, dtype=bf, device=d) for _ in range(DEPTH)],
+                                  Y=torch.empty(M, KOUT, device=d))
+        B = self._buf[key]
+        tile(X16, 128, B["X"])
+        A, K = B["X"], KIN
+        for l in range(DEPTH):
+            gemm_tiled(A, self.Wt[l], M, HID, K, EPI_GELU, bias=self.b[l], C16=B["H"][l], c16_tiled=True)
+            A, K = B["H"][l], HID
+        gemm_tiled(A, self.Wt[DEPTH], M, KOUT, HID, EPI_F32, bias=self.b[DEPTH], C32=B["Y"])
+        return B["Y"]
+
     def loss_grad(self, target):
         """Mean-square error of the last forward output against target (FP32
         [M][KOUT], zeros in the padded columns) and its gradient; returns the
@@ -284,7 +331,7 @@ class Surrogate:
             out = torch.zeros(n, KOUT, device=yiT.device)
             omu, osig = torch.zeros_like(self.mlp.omu), torch.ones_like(self.mlp.osig)
         else:
-            out = self.mlp.forward(self.features(rho, dt, yiT))
+            out = self.mlp.forward_tiled(self.features(rho, dt, yiT))
             omu, osig = self.mlp.omu, self.mlp.osig
         _ck(_L().edyn_mlp_decode(n, NS, _p(out), KOUT, _p(omu), _p(osig), _p(yiT), _p(f0), _p(dt), YFLOOR, TFLOOR,
                                  _p(y1), _stream()), "mlp decode")
@@ -440,30 +487,37 @@ def timed(fn, *a, **k):
 
 def _main():
     """Times the MLP's forward pass (four tensor-core GEMMs with fused
-    epilogues) on a batch of random standardised inputs; prints one JSON
-    line with the achieved dense BF16 rate."""
+    epilogues; the bulk-copy path on tiled operands and the thread-copy path
+    on row-major ones) on a batch of random standardised inputs (rows a
+    multiple of 128); prints one JSON line with the dense BF16 rates."""
     import argparse
     import json
 
     ap = argparse.ArgumentParser(description=_main.__doc__)
     ap.add_argument("--rows", type=int, default=1 << 20)
     ap.add_argument("--reps", type=int, default=10)
+    ap.add_argument("--path", choices=["both", "tiled", "copy"], default="both")
     a = ap.parse_args()
     m = MLP(seed=0)
     X = torch.randn(a.rows, KIN, device="cuda").to(torch.bfloat16)
-    for _ in range(3):
-        m.forward(X)
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record()
-    for _ in range(a.reps):
-        m.forward(X)
-    e1.record()
-    e1.synchronize()
-    status()
-    ms = e0.elapsed_time(e1) / a.reps
     flops = 2.0 * a.rows * (KIN * HID + (DEPTH - 1) * HID * HID + HID * KOUT)
-    print(json.dumps({"rows": a.rows, "forward_ms": ms, "tflops": flops / ms / 1e9, "launches_per_forward": DEPTH + 1}))
+    res = {"rows": a.rows, "flops_per_row": flops / a.rows}
+    paths = {"tiled": m.forward_tiled, "copy": m.forward}
+    for name in (["tiled", "copy"] if a.path == "both" else [a.path]):
+        fn = paths[name]
+        for _ in range(3):
+            fn(X)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(a.reps):
+            fn(X)
+        e1.record()
+        e1.synchronize()
+        status()
+        ms = e0.elapsed_time(e1) / a.reps
+        res[name] = {"forward_ms": ms, "tflops": flops / ms / 1e9}
+    print(json.dumps(res))
 
 
 if __name__ == "__main__":

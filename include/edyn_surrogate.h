@@ -38,6 +38,25 @@ extern "C" {
 int edyn_mlp_gemm(const void* A, int lda, const void* B, int ldb, int M, int N, int K, int epi, const float* bias,
                   float* C32, int ldc, void* C16, int ldc16, const float* Z, int ldz, void* stream);
 
+/* The bulk-copy form of edyn_mlp_gemm for inference: A and B pre-tiled by
+ * edyn_mlp_tile (A with BR = 128 and M a multiple of 128, B with
+ * BR = edyn_mlp_tile_rows(N)), so that every 64-column k-step of a CTA is
+ * two contiguous copies by the bulk-copy (TMA) engine into a four-deep
+ * ring. epi is EDYN_MLP_EPI_F32 or _GELU; with c16_tiled the GELU output is
+ * written tiled (BR = 128, K = N), ready as the next layer's A. */
+int edyn_mlp_gemm_tiled(const void* At, const void* Bt, int M, int N, int K, int epi, const float* bias, float* C32,
+                        int ldc, void* C16, int ldc16, int c16_tiled, void* stream);
+
+/* Row block height of the tiled B operand for N output columns (256, 128
+ * or 64: the GEMM's N tile). */
+int edyn_mlp_tile_rows(int N);
+
+/* Row-major [R][K] BF16 (K a multiple of 64) -> tiled layout with BR-row
+ * blocks (64, 128 or 256); block (r / BR, k / 64) is contiguous at element
+ * ((r / BR)(K / 64) + k / 64) BR 64, in the core-matrix order of the GEMM's
+ * shared-memory tiles; rows past R up to a multiple of BR are zero. */
+int edyn_mlp_tile(const void* in, int R, int K, int BR, void* out, void* stream);
+
 /* Synchronises the stream; EDYN_E_SURR if a kernel gave up a wait since the
  * last call (and clears that record). */
 int edyn_mlp_status(void* stream);

@@ -3,7 +3,7 @@
 // with the kernels that train it and the per-cell gate that decides whether
 // a cell keeps the surrogate's answer or goes to the implicit integrator.
 //
-// The dense layers run on the fifth-generation tensor cores: one CTA of four
+// The dense layers run on the fifth-generation tensor cores: one CTA of eight
 // warps owns a 128-row tile of the output, stages A (activations) and B
 // (weights) tiles of 64 k-columns in shared memory in the no-swizzle
 // core-matrix layout, and one thread issues tcgen05.mma (M = 128, N = BN,
@@ -11,9 +11,9 @@
 // operand tiles are double-buffered: the next tile is written while the
 // tensor core reads the previous one, and a tcgen05.commit per tile arrives
 // on that buffer's mbarrier. The epilogue reads the accumulator with
-// tcgen05.ld (warp w owns TMEM lanes 32w..32w+31, i.e. rows 32w..32w+31 of
-// the tile) and fuses bias, GELU and the GELU derivative of the backward
-// pass. Every wait is bounded (a wall-clock limit read from %globaltimer);
+// tcgen05.ld (warps w and w + 4 share TMEM lanes 32w..32w+31, i.e. those
+// rows of the tile, and split the columns) and fuses bias, GELU and the
+// GELU derivative of the backward pass. Every wait is bounded (a wall-clock limit read from %globaltimer);
 // a wait that runs out sets the module's error word, the kernel frees its
 // TMEM and returns, and the host reads the word after the call.
 #include <cuda_bf16.h>
@@ -27,6 +27,7 @@ namespace mlp {
 
 constexpr int BM = 128;  // tile rows (TMEM lanes)
 constexpr int BK = 64;   // k-columns per staged tile
+constexpr int GEMM_THREADS = 256;  // eight warps: two per TMEM lane quarter in the epilogue
 constexpr unsigned long long WAIT_NS = 2000000000ull;  // 2 s
 
 __device__ unsigned g_err;
@@ -180,16 +181,19 @@ __device__ __forceinline__ void stage_tile(char* dst, const __nv_bfloat16* src, 
   }
 }
 
-// Reads the 128 x BN FP32 accumulator from TMEM (warp w: rows 32w..32w+31)
-// and applies the fused epilogue of a.
+// Reads the 128 x BN FP32 accumulator from TMEM and applies the fused
+// epilogue of a. A warp may read only its quarter of the TMEM lanes
+// (warp w: lanes 32 (w % 4) .. + 31, i.e. those rows of the tile), so the
+// eight warps of a CTA pair up on each quarter and split its columns.
 template <int BN>
 __device__ __forceinline__ void epilogue(const GemmArgs& a, uint32_t tmem, int m0, int n0) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int row = m0 + warp * 32 + lane;
+  const int quarter = warp & 3, half_cols = warp >> 2;
+  const int row = m0 + quarter * 32 + lane;
   const bool live = row < a.M;
-  for (int c32 = 0; c32 < BN; c32 += 32) {
+  for (int c32 = half_cols * (BN / 2); c32 < (half_cols + 1) * (BN / 2); c32 += 32) {
     float w32[32];
-    tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c32, w32);
+    tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)c32, w32);
     if (!live) continue;
 #pragma unroll
     for (int half = 0; half < 2; ++half) {
@@ -240,7 +244,7 @@ __device__ __forceinline__ void epilogue(const GemmArgs& a, uint32_t tmem, int m
 }
 
 template <int BN>
-__global__ void __launch_bounds__(128, 1) k_gemm(GemmArgs a) {
+__global__ void __launch_bounds__(GEMM_THREADS, 1) k_gemm(GemmArgs a) {
   constexpr int A_BYTES = BM * BK * 2;
   constexpr int B_BYTES = BN * BK * 2;
   constexpr int STAGE = A_BYTES + B_BYTES;
@@ -323,7 +327,7 @@ cudaError_t launch_gemm(const GemmArgs& a, cudaStream_t s) {
     attr = true;
   }
   dim3 grid((a.M + BM - 1) / BM, a.N / BN);
-  k_gemm<BN><<<grid, 128, gemm_smem<BN>(), s>>>(a);
+  k_gemm<BN><<<grid, GEMM_THREADS, gemm_smem<BN>(), s>>>(a);
   return cudaGetLastError();
 }
 
@@ -349,7 +353,7 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
 // Every BN keeps at least two CTAs per SM (shared memory and TMEM), so one
 // CTA's epilogue runs under another's copies and products.
 template <int BN, int ST>
-__global__ void __launch_bounds__(128, 1) k_gemm_tiled(GemmArgs a) {
+__global__ void __launch_bounds__(GEMM_THREADS, 1) k_gemm_tiled(GemmArgs a) {
   constexpr int A_BYTES = BM * BK * 2;
   constexpr int B_BYTES = BN * BK * 2;
   constexpr int STAGE = A_BYTES + B_BYTES;
@@ -446,7 +450,7 @@ cudaError_t launch_gemm_tiled(const GemmArgs& a, cudaStream_t s) {
     attr = true;
   }
   dim3 grid(a.M / BM, a.N / BN);
-  k_gemm_tiled<BN, TILED_STAGES><<<grid, 128, gemm_tiled_smem<BN>(), s>>>(a);
+  k_gemm_tiled<BN, TILED_STAGES><<<grid, GEMM_THREADS, gemm_tiled_smem<BN>(), s>>>(a);
   return cudaGetLastError();
 }
 

@@ -49,6 +49,10 @@ def parse():
     p.add_argument("--cells", type=int, default=20000)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-surrogate", action="store_true", help="skip the surrogate-vs-plain chemistry comparison")
+    p.add_argument("--workload", default="tube", choices=["tube", "reactors"],
+                   help="tube: the detonation tube (default, the headline metric); reactors: the batch of "
+                        "partially reacted constant-volume reactors")
+    p.add_argument("--reactors", type=int, default=1 << 20, help="reactors in the batch of --workload reactors")
     return p.parse_args()
 
 
@@ -384,11 +388,112 @@ def gpu_arm(args, rank, world, local):
     print(json.dumps(line), flush=True)
 
 
+def reactors_arm(args, local):
+    """Batched stiff chemistry: n constant-volume CH4/air reactors with
+    T ~ U[900, 2500] K, p log-uniform in [1, 50] atm, phi ~ U[0.5, 2.0],
+    dt log-uniform in [1e-8, 1e-6] s (configs.reactor_batch, seed 0), each
+    first advanced by a seeded fraction U[0, 1] of its own ignition delay
+    (the first time T rises 400 K above its start, found by the plain
+    integrator in 50 us windows up to 2 ms; a reactor that does not ignite
+    by then counts 2 ms). A step is one batch call of the plain integrator
+    (rtol 1e-5, atol 1e-13) over every reactor's dt, on states resident on
+    the device and restored before each step."""
+    import numpy as np
+    import torch
+
+    from fortrancfd_gb300 import Reactors, configs
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
+    n = args.reactors
+    rho, dt, yiT, _ = configs.reactor_batch(n, seed=0)
+    R = Reactors(rtol=1e-5, atol=1e-13)
+    R.set_stream(stream.cuda_stream)
+    rho_d = torch.tensor(rho, device=dev)
+    dt_d = torch.tensor(dt, device=dev)
+    t_prep = time.perf_counter()
+    window, t_max = 50e-6, 2e-3
+    y = torch.tensor(yiT, device=dev)
+    T0 = y[:, -1].clone()
+    tau = torch.full((n,), t_max, dtype=torch.float64, device=dev)
+    found = torch.zeros(n, dtype=torch.bool, device=dev)
+    w_d = torch.full((n,), window, dtype=torch.float64, device=dev)
+    t = 0.0
+    while t < t_max - 1e-12:
+        # only reactors not yet ignited need the next window
+        idx = torch.nonzero(~found).flatten()
+        if idx.numel() == 0:
+            break
+        ys = y.index_select(0, idx).contiguous()
+        rs = rho_d.index_select(0, idx).contiguous()
+        ws = w_d[: idx.numel()].contiguous()
+        R.integrate_device(idx.numel(), rs.data_ptr(), ws.data_ptr(), ys.data_ptr())
+        t += window
+        hit = (ys[:, -1] - T0.index_select(0, idx)) > 400.0
+        tau[idx[hit]] = t
+        found[idx[hit]] = True
+        y[idx] = ys
+    # fresh mixtures advanced by frac * tau, in windows of at most 50 us
+    frac = torch.tensor(np.random.default_rng(1).uniform(0.0, 1.0, n), device=dev)
+    left = frac * tau
+    y = torch.tensor(yiT, device=dev)
+    while True:
+        idx = torch.nonzero(left > 0).flatten()
+        if idx.numel() == 0:
+            break
+        h = torch.clamp(left.index_select(0, idx), max=window).contiguous()
+        ys = y.index_select(0, idx).contiguous()
+        rs = rho_d.index_select(0, idx).contiguous()
+        R.integrate_device(idx.numel(), rs.data_ptr(), h.data_ptr(), ys.data_ptr())
+        y[idx] = ys
+        left[idx] -= h
+        left[left < 1e-15] = 0.0
+    t_prep = time.perf_counter() - t_prep
+    y0 = y.clone()
+    stats = None
+    for _ in range(args.warmup):
+        y.copy_(y0)
+        R.integrate_device(n, rho_d.data_ptr(), dt_d.data_ptr(), y.data_ptr())
+    torch.cuda.synchronize(dev)
+    ms = []
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            y.copy_(y0)  # n x 54 doubles (453 MB at 2^20): inputs larger than L2
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            stats = R.integrate_device(n, rho_d.data_ptr(), dt_d.data_ptr(), y.data_ptr())
+            e1.record(stream)
+            e1.synchronize()
+            ms.append(e0.elapsed_time(e1))
+    t_step = statistics.median(ms) / 1e3
+    Tpre = y0[:, -1].cpu().numpy()
+    line = {"metric": "reactor-steps/s on 1 GB300 (batched stiff chemistry)", "value": n / t_step,
+            "unit": "reactor-steps/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": t_step * 1e3, "higher_is_better": True, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"ch4_air_reactors_{n}", "reactors": n,
+                       "states": "fresh CH4/air mixtures advanced by U[0,1] of their own ignition delay",
+                       "chemistry": "plain SDIRK4 (FP64 residual, FP32 analytic Jacobian/LU), rtol 1e-5, atol 1e-13",
+                       "l2": "inputs (453 MB at 2^20) larger than L2, restored before each step"},
+            "clocks": clk.summary(), "gpu_launches": args.steps,
+            "chem": {"rhs_per_reactor": stats["rhs"] / n, "steps_per_reactor": stats["steps"] / n,
+                     "rejects": stats["rejects"], "failed": stats["failed"]},
+            "preparation": {"seconds": t_prep, "ignited_within_2ms": float(found.float().mean().item()),
+                            "T_pre_K": [float(np.percentile(Tpre, q)) for q in (0, 50, 100)]}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
     if args.impl == "reference":
         reference_arm(args, rank, world)
+        return
+    if args.workload == "reactors":
+        if rank == 0:
+            reactors_arm(args, local)
         return
     gpu_arm(args, rank, world, local)
 

@@ -25,7 +25,6 @@ device memory, streams and (training only) the batch sampling.
 from __future__ import annotations
 
 import ctypes
-import time
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -475,14 +474,6 @@ def _train(s, rho, dt, y0, y1, iters, batch, lr, seed, log_every):
             hist.append((it, float(loss.item())))
     status()
     return hist
-
-
-def timed(fn, *a, **k):
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    r = fn(*a, **k)
-    torch.cuda.synchronize()
-    return r, time.perf_counter() - t0
 
 
 def _main():

@@ -354,6 +354,10 @@ class Surrogate:
         the surrogate where the gate accepts it, the implicit integrator for
         the rest. Returns the counters (accepted cells, fallback rate, the
         integrator's right-hand sides)."""
+        if yiT.shape[0] == 0:
+            self.stats = {"cells": 0, "accepted": 0, "accepted_network": 0, "fallback_rate": 0.0, "integrator_rhs": 0,
+                          "integrator_steps": 0}
+            return self.stats
         with self:
             return self._apply(rho, dt, yiT, zero_net)
 

@@ -1545,13 +1545,16 @@ __device__ __forceinline__ float newton_correct(const Team<TW>& tm, WarpWork& w,
 
 struct Cell {
   double rho_cgs, dt, rtol, atol;
-  double h0;  // first step size to try (<= dt)
+  double h0;      // first step size to try (<= dt)
+  int max_steps;  // accepted + rejected steps after which the cell fails (<= 0: 4000)
+  bool screen;    // stop after the inert-cell test: a cell that is not inert is deferred
 };
 
 struct CellStats {
   int rhs, steps, rejects, jac;
   bool failed;
-  double hnext;  // step size the cell's next window starts with
+  double hnext;   // step size the cell's next window starts with
+  bool deferred;  // screen mode: not inert; w.y0 = y0 and w.dl = f(y0) are left for the caller
 };
 
 constexpr float THETA_JAC = 0.1f;  // Newton contraction above which a kept Jacobian is rebuilt
@@ -1564,9 +1567,9 @@ __device__ CellStats integrate(const Tabs& t, const Team<TW>& tm, WarpWork& w, c
   const int lane = tm.tid;
   const int n = t.ns + 1;
   const float nn = (float)t.h->nnorm;  // RMS over the full mechanism's components (a subset's others are zero)
-  CellStats st = {0, 0, 0, 0, false, c.dt};
+  CellStats st = {0, 0, 0, 0, false, c.dt, false};
   double tcur = 0.0, h = c.h0;
-  const int max_steps = 4000;
+  const int max_steps = c.max_steps > 0 ? c.max_steps : 4000;
   bool need_jac = true, need_f0 = true;
   // A four-warp team keeps its Jacobian in a separate buffer and reuses it
   // across steps while the Newton iterations contract fast (the iteration is
@@ -1612,6 +1615,10 @@ __device__ CellStats integrate(const Tabs& t, const Team<TW>& tm, WarpWork& w, c
           tm.sync();
           st.steps++;
           st.hnext = c.dt;
+          break;
+        }
+        if (c.screen) {
+          st.deferred = true;
           break;
         }
       }
@@ -1780,36 +1787,43 @@ __device__ __forceinline__ WarpWork* work_slots(char* smem, int tab_bytes) {
 // Batch of independent reactors (macks contract).
 __global__ void __launch_bounds__(MAXW * 32, 1)
     k_reactors(const char* g_tab, int tab_bytes, int n, const double* rho, const double* dt, double* yiT, double rtol,
-               double atol, unsigned* next, ChemCounters* cnt, unsigned* err) {
+               double atol, int max_steps, unsigned* next, ChemCounters* cnt, unsigned* err) {
   extern __shared__ __align__(16) char smem[];
   stage_tables(smem, g_tab, tab_bytes);
   const Tabs t = bind_tabs(smem);
   WarpWork& w = work_slots(smem, tab_bytes)[threadIdx.x >> 5];
   const int lane = threadIdx.x & 31;
   const Team<32> tm{lane, 0, nullptr, nullptr, nullptr, nullptr};
-  const int nv = t.ns + 1;
+  // rows hold the full mechanism's species and T (nnorm values); a species
+  // subset's tables read and write the kept species through smap
+  const int ns = t.ns, nrow = t.h->nnorm;
   for (int guard = 0; guard < (1 << 30); ++guard) {
     unsigned cell = 0;
     if (lane == 0) cell = atomicAdd(next, 1u);
     cell = __shfl_sync(0xffffffffu, cell, 0);
     if (cell >= (unsigned)n) break;
-    const double* src = yiT + (size_t)cell * nv;
-    for (int i = lane; i < nv; i += 32) w.y0[i] = src[i];
+    const double* src = yiT + (size_t)cell * nrow;
+    for (int k = lane; k < ns; k += 32) w.y0[k] = src[t.smap[k]];
+    if (lane == 0) w.y0[ns] = src[nrow - 1];
     __syncwarp();
-    Cell c{rho[cell] * 1e-3, dt[cell], rtol, atol, dt[cell]};
+    Cell c{rho[cell] * 1e-3, dt[cell], rtol, atol, dt[cell], max_steps, false};
     CellStats s = integrate<32>(t, tm, w, c);
-    double* dst = yiT + (size_t)cell * nv;
-    for (int i = lane; i < nv; i += 32) dst[i] = w.y0[i];
+    double* dst = yiT + (size_t)cell * nrow;
+    for (int k = lane; k < ns; k += 32) dst[t.smap[k]] = w.y0[k];
+    if (lane == 0) dst[nrow - 1] = w.y0[ns];
     if (lane == 0) {
       add_stats(cnt, s, false);
-      if (s.failed) atomicOr(err, (unsigned)EDYN_E_CHEM);
+      if (s.failed) atomicOr(err, EDYN_STATUS_CHEM);
     }
     __syncwarp();
   }
 }
 
 // FP64 right-hand side f = d(Y_1..Y_ns, T)/dt of a batch of reactors (the
-// function integrate() advances), one warp per cell.
+// function integrate() advances), one warp per cell. Rows hold the full
+// mechanism's species and T (nnorm values); with a species subset's tables
+// the kept species are read through smap, and the rows of the others get 0
+// (their concentrations and rates are zero).
 __global__ void __launch_bounds__(MAXW * 32, 1)
     k_reactor_rhs(const char* g_tab, int tab_bytes, int n, const double* rho, const double* yiT, double* f) {
   extern __shared__ __align__(16) char smem[];
@@ -1818,19 +1832,63 @@ __global__ void __launch_bounds__(MAXW * 32, 1)
   WarpWork& w = work_slots(smem, tab_bytes)[threadIdx.x >> 5];
   const int lane = threadIdx.x & 31;
   const Team<32> tm{lane, 0, nullptr, nullptr, nullptr, nullptr};
-  const int nv = t.ns + 1;
+  const int ns = t.ns;
+  const int nrow = t.h->nnorm;  // full species + T
   const int nw = blockDim.x >> 5;
   for (int cell = blockIdx.x * nw + (threadIdx.x >> 5); cell < n; cell += gridDim.x * nw) {
-    const double* src = yiT + (size_t)cell * nv;
-    for (int i = lane; i < nv; i += 32) w.y0[i] = src[i];
+    const double* src = yiT + (size_t)cell * nrow;
+    for (int k = lane; k < ns; k += 32) w.y0[k] = src[t.smap[k]];
+    if (lane == 0) w.y0[ns] = src[nrow - 1];
     __syncwarp();
     rhs64<32>(t, tm, w, w.y0, rho[cell] * 1e-3, w.fy);
     __syncwarp();
-    double* dst = f + (size_t)cell * nv;
-    for (int i = lane; i < nv; i += 32) dst[i] = w.fy[i];
+    double* dst = f + (size_t)cell * nrow;
+    if (ns + 1 < nrow)
+      for (int i = lane; i < nrow; i += 32) dst[i] = 0.0;
+    __syncwarp();
+    for (int k = lane; k < ns; k += 32) dst[t.smap[k]] = w.fy[k];
+    if (lane == 0) dst[nrow - 1] = w.fy[ns];
     __syncwarp();
   }
 }
+
+// HRR_dot of the tube cells (heat_release_rate_omegadot, SRC/thermo.f90:
+// 105-134, called at SRC/source.f90:72-73): -sum_k W_k h_f,k (cdot_k -
+// ddot_k) with the production rates at the state the chemistry step left
+// (rho, Y after adjust_sum, T of the integration), converted to W/m^3. With
+// the molar production rates w_k = cdot_k - ddot_k and f_k = dY_k/dt =
+// w_k W_k / rho (the integrator's right-hand side), the sum is rho sum_k
+// h_f,k f_k. One warp per cell. The reference evaluates it every step for
+// output only; here it is evaluated when the host downloads it.
+__global__ void __launch_bounds__(MAXW * 32, 1)
+    k_hrr_dot(const char* g_tab, int tab_bytes, int n, int ld, const double* qf, const double* tchem, double* out) {
+  extern __shared__ __align__(16) char smem[];
+  stage_tables(smem, g_tab, tab_bytes);
+  const Tabs t = bind_tabs(smem);
+  WarpWork& w = work_slots(smem, tab_bytes)[threadIdx.x >> 5];
+  const int lane = threadIdx.x & 31;
+  const Team<32> tm{lane, 0, nullptr, nullptr, nullptr, nullptr};
+  const int ns = t.ns;
+  const int nw = blockDim.x >> 5;
+  for (int cell = blockIdx.x * nw + (threadIdx.x >> 5); cell < n; cell += gridDim.x * nw) {
+    const double* q = qf + cell + GHOST;
+    for (int k = lane; k < ns; k += 32) w.y0[k] = q[(3 + t.smap[k]) * (size_t)ld];
+    if (lane == 0) w.y0[ns] = tchem[cell];
+    __syncwarp();
+    const double rho_cgs = q[0] * 1e-3;
+    rhs64<32>(t, tm, w, w.y0, rho_cgs, w.fy);
+    __syncwarp();
+    double sum = 0.0;
+    for (int k = lane; k < ns; k += 32) sum = fma(t.d.hf[k], w.fy[k], sum);
+    sum = warp_sum(sum);
+    if (lane == 0) out[cell] = -(rho_cgs * sum) * 1e-1;
+    __syncwarp();
+  }
+}
+
+template <int TW>
+__device__ void finish_cell(const Tabs& t, const Team<TW>& tm, WarpWork& w, const ChemLaunch& L, unsigned cell,
+                            double dt, double& speed_max);
 
 // One tube cell: reaction_macks (SRC/source.f90:17-84) followed by the
 // post-step QcToqf (SRC/main.f90:157-161). Returns the right-hand sides the
@@ -1842,7 +1900,6 @@ __device__ int tube_cell(const Tabs& t, const Team<TW>& tm, WarpWork& w, const C
   const int ns = t.ns;
   const size_t ld = (size_t)L.ld;
   double* q = L.qf + cell + GHOST;
-  double* Q = L.qc + cell + GHOST;
   const double rho = q[0];
   // reaction_macks: y_sp = adjust_sum(Y), yiT = [y_sp, T] (SRC/source.f90:47-56);
   // the raw Y stay in the qf rows for the heat release rate.
@@ -1859,13 +1916,62 @@ __device__ int tube_cell(const Tabs& t, const Team<TW>& tm, WarpWork& w, const C
   tm.sync();
   // start from the first accepted step of this cell's last window
   const double hl = L.hlast ? L.hlast[cell] : 0.0;
-  Cell c{rho * 1e-3, dt, L.rtol, L.atol, (hl > 0.0 && hl < dt) ? hl : dt};
+  Cell c{rho * 1e-3, dt, L.rtol, L.atol, (hl > 0.0 && hl < dt) ? hl : dt, L.max_steps, L.screen != 0};
   CellStats st = integrate<TW>(t, tm, w, c);
-  if (tid == 0 && L.hlast) L.hlast[cell] = st.hnext;
+  if (tid == 0 && L.hlast && !st.deferred) L.hlast[cell] = st.hnext;
   if (tid == 0) {
     add_stats(cnt, st, TW > 32);
-    if (st.failed) atomicOr(L.err, (unsigned)EDYN_E_CHEM);
+    if (st.failed) atomicOr(L.err, EDYN_STATUS_CHEM);
   }
+  if (st.deferred) {
+    // screen mode (single warps only): the cell is not inert; its adjusted
+    // state and f(y0) go to the next free packed row, in the full
+    // mechanism's layout, for the surrogate and its gate
+    if constexpr (TW == 32) {
+      unsigned j = 0;
+      if (tid == 0) j = atomicAdd(L.pk_count, 1u);
+      j = __shfl_sync(0xffffffffu, j, 0);
+      const int nrow = t.h->nnorm;
+      double* y0p = L.pk_y0 + (size_t)j * nrow;
+      double* f0p = L.pk_f0 + (size_t)j * nrow;
+      if (ns + 1 < nrow)
+        for (int i = tid; i < nrow; i += TW) y0p[i] = f0p[i] = 0.0;
+      __syncwarp();
+      for (int k = tid; k < ns; k += TW) {
+        y0p[t.smap[k]] = w.y0[k];
+        f0p[t.smap[k]] = w.dl[k];
+      }
+      if (tid == 0) {
+        y0p[nrow - 1] = w.y0[ns];
+        f0p[nrow - 1] = w.dl[ns];
+        L.pk_idx[j] = cell;
+        L.pk_rho[j] = rho;
+        L.pk_dt[j] = dt;
+      }
+      __syncwarp();
+    }
+    return st.rhs;
+  }
+  finish_cell<TW>(t, tm, w, L, cell, dt, speed_max);
+  return st.rhs;
+}
+
+// The tail of reaction_macks for one tube cell whose integration over dt left
+// [Y, T] in w.y0 (the qf rows still hold the cell's Y before the step):
+// adjust_sum, the heat release rate, qfToQc, then the post-step QcToqf of
+// SRC/main.f90:157-161 and the cell's signal speed for the next time step.
+template <int TW>
+__device__ void finish_cell(const Tabs& t, const Team<TW>& tm, WarpWork& w, const ChemLaunch& L, unsigned cell,
+                            double dt, double& speed_max) {
+  const int tid = tm.tid;
+  const int ns = t.ns;
+  const size_t ld = (size_t)L.ld;
+  double* q = L.qf + cell + GHOST;
+  double* Q = L.qc + cell + GHOST;
+  const double rho = q[0];
+  // the temperature the integration ended with: HRR_dot is evaluated at it
+  // (SRC/source.f90:72-73 passes qf(iqtemp) = macks' T)
+  if (tid == 0 && L.tchem) L.tchem[cell] = w.y0[ns];
   // adjust_sum(Y) after the step
   double s2 = 0.0;
   for (int k = tid; k < ns; k += TW) {
@@ -1948,7 +2054,17 @@ __device__ int tube_cell(const Tabs& t, const Team<TW>& tm, WarpWork& w, const C
     T = fmax(20.0, fmin(6000.0, T + dTN));
     ++it;
   }
-  if (tid == 0) q[2 * ld] = T;
+  if (tid == 0) {
+    q[2 * ld] = T;
+    // the reference's silent cap and clamps (SRC/thermo.f90:244-255) made
+    // loud: Newton at its cap with both stopping tests failing, or a state
+    // that is non-finite, non-positive or pinned at a clamp bound
+    unsigned bad = 0;
+    if (fabs(gN) >= fabs(E) * 1e-9 && fabs(dTN) >= T * 1e-6) bad |= EDYN_STATUS_NEWTON;
+    if (!(rho > 0.0) || !isfinite(rhoe) || !(T > 20.0 && T < 6000.0) || !(s2 > 0.0) || !isfinite(s2))
+      bad |= EDYN_STATUS_STATE;
+    if (bad) atomicOr(L.err, bad);
+  }
   // signal speed of the new state for the next time step
   if (L.cvel_out) {
     double a[6] = {0, 0, 0, 0, 0, 0};
@@ -1973,7 +2089,6 @@ __device__ int tube_cell(const Tabs& t, const Team<TW>& tm, WarpWork& w, const C
     speed_max = fmax(speed_max, sp);
   }
   tm.sync();
-  return st.rhs;
 }
 
 // Picks the cells that get a four-warp team in the next launch: those whose
@@ -2065,7 +2180,8 @@ __global__ void __launch_bounds__(MAXW * 32, 1)
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   double speed_max = 0.0;
   const int nwarps = blockDim.x >> 5;
-  const unsigned nteam = (nwarps >= TEAM / 32) ? min(min(s_hot[0], (unsigned)HOT_MAX), gridDim.x) : 0u;
+  const unsigned nteam =
+      (nwarps >= TEAM / 32 && !L.screen) ? min(min(s_hot[0], (unsigned)HOT_MAX), gridDim.x) : 0u;
   if (blockIdx.x < nteam) {
     if (warp < TEAM / 32) {
       // team scratch: the second work slot, unused while the team runs
@@ -2108,9 +2224,36 @@ __global__ void __launch_bounds__(MAXW * 32, 1)
       *L.time = *L.time + dt;
       *L.nsteps = *L.nsteps + 1;
     }
-    if (L.cost && L.hot)
+    if (L.cost && L.hot && !L.screen)
       select_hot(L.cost, L.n, L.hot, reinterpret_cast<unsigned*>(ww), (int)(nwarps * sizeof(WarpWork) / 4));
   }
+}
+
+// The packed rows' tail of a screened launch: each row's state after the
+// step (pk_y1, full-mechanism layout: the surrogate's accepted candidate or
+// the implicit integrator's result) goes through the same tail as a cell of
+// k_tube_chem (finish_cell). One warp per row; *pk_count rows.
+__global__ void __launch_bounds__(MAXW * 32, 1)
+    k_tube_finish(const char* g_tab, int tab_bytes, ChemLaunch L, const double* pk_y1) {
+  extern __shared__ __align__(16) char smem[];
+  stage_tables(smem, g_tab, tab_bytes);
+  const Tabs t = bind_tabs(smem);
+  WarpWork& w = work_slots(smem, tab_bytes)[threadIdx.x >> 5];
+  const int lane = threadIdx.x & 31;
+  const Team<32> tm{lane, 0, nullptr, nullptr, nullptr, nullptr};
+  const int ns = t.ns, nrow = t.h->nnorm;
+  const int nw = blockDim.x >> 5;
+  const unsigned m = *L.pk_count;
+  double speed_max = 0.0;
+  for (unsigned j = blockIdx.x * nw + (threadIdx.x >> 5); j < m; j += gridDim.x * nw) {
+    const double* y = pk_y1 + (size_t)j * nrow;
+    for (int k = lane; k < ns; k += 32) w.y0[k] = y[t.smap[k]];
+    if (lane == 0) w.y0[ns] = y[nrow - 1];
+    __syncwarp();
+    finish_cell<32>(t, tm, w, L, (unsigned)L.pk_idx[j], L.pk_dt[j], speed_max);
+  }
+  if (L.cvel_out && lane == 0 && speed_max > 0.0)
+    atomicMax(L.cvel_out, (unsigned long long)__double_as_longlong(speed_max));
 }
 
 // ---------------------------------------------------------------------------
@@ -2521,6 +2664,10 @@ int chem_init(ChemState& s, const edyn_mech& m, const ThermoTable& tb, cudaStrea
   if (e != cudaSuccess) return (int)e;
   e = cudaFuncSetAttribute(k_reactor_rhs, cudaFuncAttributeMaxDynamicSharedMemorySize, want);
   if (e != cudaSuccess) return (int)e;
+  e = cudaFuncSetAttribute(k_hrr_dot, cudaFuncAttributeMaxDynamicSharedMemorySize, want);
+  if (e != cudaSuccess) return (int)e;
+  e = cudaFuncSetAttribute(k_tube_finish, cudaFuncAttributeMaxDynamicSharedMemorySize, want);
+  if (e != cudaSuccess) return (int)e;
   int per_sm = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_reactors, s.warps * 32, s.smem);
   s.ctas = nsm * std::max(1, per_sm);
@@ -2535,7 +2682,7 @@ cudaError_t chem_launch_batch(ChemState& s, const ChemLaunch& L, cudaStream_t st
   const int grid = std::min(s.ctas, (L.n + s.warps - 1) / s.warps);
   k_reactors<<<std::max(1, grid), s.warps * 32, s.smem, st>>>((const char*)s.d_tables, (int)s.table_bytes, L.n,
                                                             L.rho_batch, L.dt_batch, L.yiT_batch, L.rtol, L.atol,
-                                                            s.d_next, s.d_count, L.err);
+                                                            L.max_steps, s.d_next, s.d_count, L.err);
   return cudaGetLastError();
 }
 
@@ -2543,6 +2690,22 @@ cudaError_t chem_rhs_batch(ChemState& s, int n, const double* rho, const double*
   const int grid = std::min(s.ctas, (n + s.warps - 1) / s.warps);
   k_reactor_rhs<<<std::max(1, grid), s.warps * 32, s.smem, st>>>((const char*)s.d_tables, (int)s.table_bytes, n, rho,
                                                                 yiT, f);
+  return cudaGetLastError();
+}
+
+cudaError_t chem_hrr_dot(ChemState& s, int n, int ld, const double* qf, const double* tchem, double* out,
+                         cudaStream_t st) {
+  const int grid = std::min(s.ctas, (n + s.warps - 1) / s.warps);
+  k_hrr_dot<<<std::max(1, grid), s.warps * 32, s.smem, st>>>((const char*)s.d_tables, (int)s.table_bytes, n, ld, qf,
+                                                            tchem, out);
+  return cudaGetLastError();
+}
+
+cudaError_t chem_finish_packed(ChemState& s, const ChemLaunch& L, int m, const double* pk_y1, cudaStream_t st) {
+  if (m <= 0) return cudaSuccess;
+  const int grid = std::min(s.ctas, (m + s.warps - 1) / s.warps);
+  k_tube_finish<<<std::max(1, grid), s.warps * 32, s.smem, st>>>((const char*)s.d_tables, (int)s.table_bytes, L,
+                                                               pk_y1);
   return cudaGetLastError();
 }
 

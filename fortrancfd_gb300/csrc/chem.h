@@ -47,7 +47,19 @@ struct ChemLaunch {
   const double* dt_batch;
   double* yiT_batch;
   double rtol, atol;
+  int max_steps;    // steps (accepted + rejected) per cell before it fails; <= 0: 4000
+  double* tchem;    // tube mode: temperature each cell's integration ended with (n), or null
   unsigned* err;
+  // screen mode (tube): every cell gets f(y0) and the inert-cell test; the
+  // inert ones finish as usual, the others are appended to packed rows (full
+  // mechanism layout, nspe + 1 values) for the surrogate path, unfinished
+  int screen;
+  unsigned* pk_count;   // rows appended (cleared by the caller)
+  int* pk_idx;          // cell of each row
+  double* pk_rho;       // rho [kg/m^3]
+  double* pk_dt;        // dt [s]
+  double* pk_y0;        // adjusted [Y, T] before the step
+  double* pk_f0;        // f(y0)
 };
 
 // smap: tube row of each species of m (3 + smap[k]) when m is a subset of the
@@ -60,6 +72,13 @@ cudaError_t chem_launch_batch(ChemState& s, const ChemLaunch& L, cudaStream_t st
 // FP64 right-hand side d(Y, T)/dt of n reactors (rho SI, yiT rows of ns + 1).
 cudaError_t chem_rhs_batch(ChemState& s, int n, const double* rho, const double* yiT, double* f, cudaStream_t st);
 cudaError_t chem_read_counters(ChemState& s, ChemCounters* out, cudaStream_t st);
+// Finishes the m packed rows of a screened tube launch from their states
+// after the step (pk_y1): adjust_sum, HRR, qfToQc, QcToqf, signal speed.
+cudaError_t chem_finish_packed(ChemState& s, const ChemLaunch& L, int m, const double* pk_y1, cudaStream_t st);
+// HRR_dot [W/m^3] of n tube cells from their primitive rows (qf, SoA with ld)
+// and the temperatures their last chemistry step ended with.
+cudaError_t chem_hrr_dot(ChemState& s, int n, int ld, const double* qf, const double* tchem, double* out,
+                         cudaStream_t st);
 cudaError_t chem_check_exp(ChemState& s, int n, const double* x_d, unsigned long long* maxulp_d, cudaStream_t st);
 cudaError_t chem_check_log(ChemState& s, int n, const double* x_d, unsigned long long* maxulp_d, cudaStream_t st);
 void chem_free(ChemState& s);

@@ -33,6 +33,39 @@ namespace {
 
 using namespace edyn;
 
+// The surrogate path of a tube (chem_mode 1): the network the caller
+// attached, the gate's tolerances, and the packed work buffers of one source
+// step, sized for every cell of the tube.
+struct Surr {
+  static constexpr int KIN = 64, HID = 256, KOUT = 64;
+  bool attached = false;
+  bool net = false;            // false: the explicit increment alone (the method without the network)
+  const void* wt[4] = {};      // tiled BF16 weights (caller-owned)
+  const float* b[4] = {};      // biases (caller-owned)
+  const float* norm = nullptr; // mu, isig, omu, osig: 4 x 64 FP32 (caller-owned)
+  double rtol = 2.5e-4, atol = 2.5e-10, etol = 1e-6;
+  double yfloor = 1e-10, tfloor = 1e-4;
+  int nrow = 0, ne = 0;
+  unsigned* d_count = nullptr;  // [0] packed rows, [1], [2] rows accepted on the network / explicit candidate
+  int* pk_idx = nullptr;
+  double *pk_rho = nullptr, *pk_dt = nullptr, *pk_y0 = nullptr, *pk_f0 = nullptr, *pk_y1 = nullptr;
+  double *pk_ya = nullptr, *pk_f1 = nullptr, *pk_fa = nullptr;
+  void *X = nullptr, *Xt = nullptr, *H[3] = {};
+  float* out = nullptr;
+  float* zero_out = nullptr;   // [M][64] zeros: the explicit candidate's network output
+  float* zero_one = nullptr;   // 64 zeros then 64 ones: its omu and osig
+  int* accept = nullptr;
+  int* rj_idx = nullptr;
+  double *rj_rho = nullptr, *rj_dt = nullptr, *rj_y = nullptr;
+  int* d_nrej = nullptr;
+  double* wmol = nullptr;      // kg/mol
+  double* elem = nullptr;      // [ne][nspe] atoms per molecule
+  // counters of the last source step: packed (not inert), accepted on the
+  // network's candidate, on the explicit one, fallback cells, right-hand
+  // sides of the screen, of the gate, of the fallback integration
+  double stats[7] = {};
+};
+
 struct Ctx {
   edyn_mech mech;
   ThermoTable tb;
@@ -47,12 +80,20 @@ struct Ctx {
   int cur = 0;
   double* qc = nullptr;
   double* q0 = nullptr;
+  double* acc = nullptr;      // RK4: k1 + 2 k2 + 2 k3 (select_time 2 only)
   double* hrr = nullptr;
+  double* hrr_dot = nullptr;  // HRR_dot of the last source step, once evaluated
+  double* tchem = nullptr;    // temperature each cell's last integration ended with
+  // HRR_dot of the last source step: 0 none (zeros), 1 not yet evaluated (the
+  // primitive state is still the one that step left), 2 evaluated into hrr_dot
+  int hrr_dot_state = 0;
+  int chem_max_steps = 0;     // integrator step cap per cell (0: the default 4000)
   double* staging = nullptr;
   size_t staging_bytes = 0;
   // device clock of the time loop
   double* d_time = nullptr;
   long long* d_nsteps = nullptr;
+  long long* d_max_steps = nullptr;  // step budget of the current edyn_advance call
   int* d_active = nullptr;
   double* d_dt = nullptr;
   unsigned long long* d_cvel = nullptr;
@@ -73,6 +114,7 @@ struct Ctx {
   std::vector<char> sub_keep;
   bool use_sub = false;
   int* d_present = nullptr;  // per species: nonzero somewhere in the tube
+  Surr surr;
   std::string err;
 };
 
@@ -122,7 +164,26 @@ StageArgs base_args(Ctx* c) {
   a.p_out = c->p_out;
   a.strict_newton = c->strict;
   a.bc = c->bc;
+  a.err = c->d_err;
   return a;
+}
+
+static_assert(EDYN_STATUS_NEWTON == EDYN_E_NEWTON && EDYN_STATUS_CHEM == EDYN_E_CHEM &&
+                  EDYN_STATUS_STATE == EDYN_E_STATE,
+              "device status bits and ABI status classes differ");
+
+// Reads and clears the context's device status word (the stream must be
+// synchronised): a call reports the status bits its own kernels set.
+int take_status(Ctx* c, const char* what) {
+  unsigned e = 0;
+  cudaError_t ce = cudaMemcpy(&e, c->d_err, sizeof(e), cudaMemcpyDeviceToHost);
+  if (ce != cudaSuccess) return fail(c, EDYN_E_CUDA, "%s: status read: %s", what, cudaGetErrorString(ce));
+  if (!e) return EDYN_OK;
+  ce = cudaMemset(c->d_err, 0, sizeof(unsigned));
+  if (ce != cudaSuccess) return fail(c, EDYN_E_CUDA, "%s: status clear: %s", what, cudaGetErrorString(ce));
+  return fail(c, (int)e, "%s: device status 0x%x (%s%s%s)", what, e, (e & EDYN_E_NEWTON) ? "temperature Newton at its cap; " : "",
+              (e & EDYN_E_CHEM) ? "chemistry integration failed; " : "",
+              (e & EDYN_E_STATE) ? "non-finite, non-positive or clamped state" : "");
 }
 
 // Launches the stages of one fluid step. Device-loop mode when dev != 0:
@@ -134,6 +195,25 @@ int fluid_step(Ctx* c, double dt, bool dev, bool last_is_fluid) {
   if (dev) {
     a.step_active = c->d_active;
     a.dt_dev = c->d_dt;
+  }
+  if (c->select_time == 2) {
+    // RK4 (SRC/timeintegration.f90:222-356): four stages on the primitive
+    // state of the step's start; the last one writes the new primitives
+    a.kind = 2;
+    a.acc = c->acc;
+    a.qf_in = c->qf[c->cur];
+    a.qf_out = c->qf[c->cur ^ 1];
+    for (int s = 0; s < 4; ++s) {
+      a.rk4_stage = s;
+      const bool last = s == 3;
+      a.cvel_out = (dev && last && last_is_fluid) ? c->d_cvel : nullptr;
+      a.time = (dev && last && last_is_fluid) ? c->d_time : nullptr;
+      a.nsteps = (dev && last && last_is_fluid) ? c->d_nsteps : nullptr;
+      cudaError_t e = launch_stage(a, c->acu, c->lim, c->wflag, c->riemann, c->stream);
+      if (e != cudaSuccess) return fail(c, EDYN_E_CUDA, "stage launch: %s", cudaGetErrorString(e));
+    }
+    c->cur ^= 1;
+    return EDYN_OK;
   }
   const int nst = c->select_time == 0 ? 1 : 3;
   for (int s = 0; s < nst; ++s) {
@@ -167,8 +247,11 @@ int fluid_step(Ctx* c, double dt, bool dev, bool last_is_fluid) {
   return EDYN_OK;
 }
 
+int surrogate_source_step(Ctx* c, double dt, bool dev);
+
 int source_step(Ctx* c, double dt, bool dev) {
   if (!c->do_reaction) return EDYN_OK;
+  if (c->chem_mode == 1) return surrogate_source_step(c, dt, dev);
   ChemLaunch L;
   std::memset(&L, 0, sizeof(L));
   L.n = c->n;
@@ -191,8 +274,146 @@ int source_step(Ctx* c, double dt, bool dev) {
   L.cost = c->d_cost;
   L.hot = c->d_hot;
   L.hlast = c->d_hlast;
+  L.tchem = c->tchem;
+  L.max_steps = c->chem_max_steps;
   cudaError_t e = chem_launch_tube(c->use_sub ? c->chem_sub : c->chem, L, c->stream);
   if (e != cudaSuccess) return fail(c, EDYN_E_CUDA, "chemistry launch: %s", cudaGetErrorString(e));
+  return EDYN_OK;
+}
+
+// solve_source with the surrogate in front of the implicit integrator
+// (chem_mode 1), for the macks call of every tube cell (SRC/source.f90:58):
+//  1. the chemistry launch in screen mode: f(y0) and the inert-cell test for
+//     every cell; inert cells finish as in the plain path, the others are
+//     packed (m rows);
+//  2. the network's candidate y0 + dt f0 + correction (tcgen05 GEMMs on the
+//     packed rows) and the explicit increment y0 + dt f0;
+//  3. the FP64 gate on both (trapezoidal residual with f at the candidate,
+//     element conservation), network first;
+//  4. the rejected rows compacted and integrated by the implicit integrator;
+//  5. every packed row finished (adjust_sum, HRR, qfToQc, QcToqf, speed).
+// The host reads the packed and rejected counts to size the launches (two
+// synchronisations per step).
+int surrogate_source_step(Ctx* c, double dt, bool dev) {
+  Surr& z = c->surr;
+  if (!z.attached) return fail(c, EDYN_E_ARG, "chem_mode 1 needs a surrogate (edyn_set_surrogate)");
+  ChemState& cs = c->use_sub ? c->chem_sub : c->chem;
+  cudaStream_t st = c->stream;
+  CK(cudaMemsetAsync(z.d_count, 0, 4 * sizeof(unsigned), st));
+  ChemLaunch L;
+  std::memset(&L, 0, sizeof(L));
+  L.n = c->n;
+  L.ld = c->ld;
+  L.qf = c->qf[c->cur];
+  L.qc = c->qc;
+  L.hrr = c->hrr;
+  L.dt = dt;
+  L.rtol = c->rtol;
+  L.atol = c->atol;
+  L.strict_newton = c->strict;
+  if (dev) {
+    L.step_active = c->d_active;
+    L.dt_dev = c->d_dt;
+    L.cvel_out = c->d_cvel;
+    L.time = c->d_time;
+    L.nsteps = c->d_nsteps;
+  } else {
+    L.cvel_out = nullptr;
+  }
+  L.err = c->d_err;
+  L.cost = c->d_cost;
+  L.hlast = c->d_hlast;
+  L.tchem = c->tchem;
+  L.max_steps = c->chem_max_steps;
+  L.screen = 1;
+  L.pk_count = z.d_count;
+  L.pk_idx = z.pk_idx;
+  L.pk_rho = z.pk_rho;
+  L.pk_dt = z.pk_dt;
+  L.pk_y0 = z.pk_y0;
+  L.pk_f0 = z.pk_f0;
+  cudaError_t e = chem_launch_tube(cs, L, st);
+  if (e != cudaSuccess) return fail(c, EDYN_E_CUDA, "chemistry screen launch: %s", cudaGetErrorString(e));
+  unsigned cnt[4] = {0, 0, 0, 0};
+  CK(cudaMemcpyAsync(cnt, z.d_count, sizeof(cnt), cudaMemcpyDeviceToHost, st));
+  ChemCounters k0;
+  e = chem_read_counters(cs, &k0, st);  // synchronises the stream
+  if (e != cudaSuccess) return fail(c, EDYN_E_CUDA, "counters: %s", cudaGetErrorString(e));
+  const int m = (int)cnt[0];
+  for (double& v : z.stats) v = 0.0;
+  z.stats[0] = m;
+  z.stats[4] = (double)k0.rhs;
+  if (m == 0) return EDYN_OK;
+  const int ns = z.nrow - 1;
+  const int M = (m + 127) / 128 * 128;
+  void* sv = (void*)st;
+  const float* mu = z.norm;
+  const float* isig = z.norm ? z.norm + 64 : nullptr;
+  const float* omu = z.norm ? z.norm + 128 : nullptr;
+  const float* osig = z.norm ? z.norm + 192 : nullptr;
+  int rc = EDYN_OK;
+  if (z.net) {
+    rc |= edyn_mlp_features(m, ns, z.pk_rho, z.pk_dt, z.pk_y0, z.wmol, mu, isig, z.X, Surr::KIN, sv);
+    rc |= edyn_mlp_tile(z.X, m, Surr::KIN, 128, z.Xt, sv);
+    const void* A = z.Xt;
+    int K = Surr::KIN;
+    for (int l = 0; l < 3; ++l) {
+      rc |= edyn_mlp_gemm_tiled(A, z.wt[l], M, Surr::HID, K, EDYN_MLP_EPI_GELU, z.b[l], nullptr, 0, z.H[l],
+                                Surr::HID, 1, sv);
+      A = z.H[l];
+      K = Surr::HID;
+    }
+    rc |= edyn_mlp_gemm_tiled(A, z.wt[3], M, Surr::KOUT, Surr::HID, EDYN_MLP_EPI_F32, z.b[3], z.out, Surr::KOUT,
+                              nullptr, 0, 0, sv);
+    rc |= edyn_mlp_decode(m, ns, z.out, Surr::KOUT, omu, osig, z.pk_y0, z.pk_f0, z.pk_dt, z.yfloor, z.tfloor, z.pk_y1,
+                          sv);
+  }
+  // the explicit increment: the decode of a zero network output
+  double* expl = z.net ? z.pk_ya : z.pk_y1;
+  rc |= edyn_mlp_decode(m, ns, z.zero_out, Surr::KOUT, z.zero_one, z.zero_one + 64, z.pk_y0, z.pk_f0, z.pk_dt,
+                        z.yfloor, z.tfloor, expl, sv);
+  if (rc) return fail(c, EDYN_E_CUDA | rc, "surrogate network launch failed");
+  e = chem_rhs_batch(cs, m, z.pk_rho, z.pk_y1, z.pk_f1, st);
+  if (e == cudaSuccess && z.net) e = chem_rhs_batch(cs, m, z.pk_rho, z.pk_ya, z.pk_fa, st);
+  if (e != cudaSuccess) return fail(c, EDYN_E_CUDA, "gate right-hand sides: %s", cudaGetErrorString(e));
+  rc |= edyn_mlp_gate(m, ns, z.ne, z.pk_y0, z.pk_y1, z.pk_f0, z.pk_f1, z.net ? z.pk_ya : nullptr,
+                      z.net ? z.pk_fa : nullptr, z.pk_dt, z.wmol, z.elem, z.rtol, z.atol, z.etol, z.accept,
+                      z.d_count + 1, sv);
+  rc |= edyn_mlp_compact(m, ns, z.accept, z.pk_rho, z.pk_dt, z.pk_y0, z.rj_idx, z.rj_rho, z.rj_dt, z.rj_y, z.d_nrej,
+                         sv);
+  if (rc) return fail(c, EDYN_E_CUDA | rc, "surrogate gate launch failed");
+  rc = edyn_mlp_status(sv);  // synchronises; reports a GEMM wait that ran out
+  if (rc) return fail(c, rc, "surrogate network: a tensor-core kernel's wait ran out");
+  int nrej = 0;
+  CK(cudaMemcpyAsync(&nrej, z.d_nrej, sizeof(int), cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(cnt, z.d_count, sizeof(cnt), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  z.stats[1] = z.net ? cnt[1] : 0;
+  z.stats[2] = z.net ? cnt[2] : cnt[1];
+  z.stats[3] = nrej;
+  z.stats[5] = z.net ? 2.0 * m : m;
+  if (nrej > 0) {
+    ChemLaunch B;
+    std::memset(&B, 0, sizeof(B));
+    B.n = nrej;
+    B.rtol = c->rtol;
+    B.atol = c->atol;
+    B.rho_batch = z.rj_rho;
+    B.dt_batch = z.rj_dt;
+    B.yiT_batch = z.rj_y;
+    B.err = c->d_err;
+    B.max_steps = c->chem_max_steps;
+    e = chem_launch_batch(cs, B, st);
+    if (e != cudaSuccess) return fail(c, EDYN_E_CUDA, "fallback launch: %s", cudaGetErrorString(e));
+    rc = edyn_mlp_scatter(nrej, ns, z.rj_idx, z.rj_y, z.pk_y1, sv);
+    if (rc) return fail(c, rc, "fallback scatter failed");
+    ChemCounters k1;
+    e = chem_read_counters(cs, &k1, st);
+    if (e != cudaSuccess) return fail(c, EDYN_E_CUDA, "counters: %s", cudaGetErrorString(e));
+    z.stats[6] = (double)k1.rhs;
+  }
+  e = chem_finish_packed(cs, L, m, z.pk_y1, st);
+  if (e != cudaSuccess) return fail(c, EDYN_E_CUDA, "packed finish launch: %s", cudaGetErrorString(e));
   return EDYN_OK;
 }
 
@@ -335,6 +556,23 @@ void drop_graph(Ctx* c) {
   c->graph_steps = 0;
 }
 
+// Evaluates HRR_dot of the last source step into c->hrr_dot while the
+// primitive state is still the one that step left.
+int eval_hrr_dot(Ctx* c) {
+  if (c->hrr_dot_state != 1) return EDYN_OK;
+  cudaError_t e = chem_hrr_dot(c->use_sub ? c->chem_sub : c->chem, c->n, c->ld, c->qf[c->cur], c->tchem, c->hrr_dot,
+                               c->stream);
+  if (e != cudaSuccess) return fail(c, EDYN_E_CUDA, "HRR_dot launch: %s", cudaGetErrorString(e));
+  c->hrr_dot_state = 2;
+  return EDYN_OK;
+}
+
+// Before a fluid step changes the state the last source step left: keep its
+// HRR_dot (the reference's eos_obj%HRR_dot outlives the next fluid step).
+// In the reference's own order (output right after the source step) this
+// never runs and HRR_dot costs nothing until it is downloaded.
+int keep_hrr_dot(Ctx* c) { return eval_hrr_dot(c); }
+
 }  // namespace
 
 extern "C" {
@@ -389,8 +627,10 @@ int edyn_init(const char* chem_dir, int nspe, int nequ, int ncell, int lvir, con
   c->rho_u_in = rp(EDYN_RP_RHO_U_IN, 0.0);
   c->rtol = rp(EDYN_RP_RTOL, 1e-5);
   c->atol = rp(EDYN_RP_ATOL, 1e-13);
-  if (c->select_time != 0 && c->select_time != 1)
-    return fail(c, EDYN_E_ARG, "select_time=%d: only 0 (Euler) and 1 (TVDRK3) are provided", c->select_time);
+  if (c->chem_mode != 0 && c->chem_mode != 1)
+    return fail(c, EDYN_E_ARG, "chem_mode=%d: 0 (implicit integrator) or 1 (surrogate with fallback)", c->chem_mode);
+  if (c->select_time < 0 || c->select_time > 2)
+    return fail(c, EDYN_E_ARG, "select_time=%d not in 0..2 (Euler, TVDRK3, RK4)", c->select_time);
   if (c->riemann < 0 || c->riemann > 2) return fail(c, EDYN_E_ARG, "select_riemann=%d not in 0..2", c->riemann);
   if (c->flag_acu == 0) c->acu = ACU_FIRST;
   else if (c->flag_acu == 1) {
@@ -435,14 +675,23 @@ int edyn_init(const char* chem_dir, int nspe, int nequ, int ncell, int lvir, con
   CK(cudaMalloc(&c->qf[1], rows * sizeof(double)));
   CK(cudaMalloc(&c->qc, rows * sizeof(double)));
   CK(cudaMalloc(&c->q0, rows * sizeof(double)));
+  if (c->select_time == 2) {
+    CK(cudaMalloc(&c->acc, rows * sizeof(double)));
+    CK(cudaMemsetAsync(c->acc, 0, rows * sizeof(double), c->stream));
+  }
   CK(cudaMalloc(&c->hrr, (size_t)ncell * sizeof(double)));
+  CK(cudaMalloc(&c->hrr_dot, (size_t)ncell * sizeof(double)));
+  CK(cudaMalloc(&c->tchem, (size_t)ncell * sizeof(double)));
   CK(cudaMemsetAsync(c->qf[0], 0, rows * sizeof(double), c->stream));
   CK(cudaMemsetAsync(c->qf[1], 0, rows * sizeof(double), c->stream));
   CK(cudaMemsetAsync(c->qc, 0, rows * sizeof(double), c->stream));
   CK(cudaMemsetAsync(c->q0, 0, rows * sizeof(double), c->stream));
   CK(cudaMemsetAsync(c->hrr, 0, (size_t)ncell * sizeof(double), c->stream));
+  CK(cudaMemsetAsync(c->hrr_dot, 0, (size_t)ncell * sizeof(double), c->stream));
+  CK(cudaMemsetAsync(c->tchem, 0, (size_t)ncell * sizeof(double), c->stream));
   CK(cudaMalloc(&c->d_time, sizeof(double)));
   CK(cudaMalloc(&c->d_nsteps, sizeof(long long)));
+  CK(cudaMalloc(&c->d_max_steps, sizeof(long long)));
   CK(cudaMalloc(&c->d_active, sizeof(int)));
   CK(cudaMalloc(&c->d_dt, sizeof(double)));
   CK(cudaMalloc(&c->d_cvel, sizeof(unsigned long long)));
@@ -513,7 +762,12 @@ int edyn_upload(void* ctx, const double* qf_aos, const double* qc_aos) {
     a.strict_newton = 1;
     CK(launch_qc_to_qf(a, c->stream));
   }
-  return refresh_chem_set(c);
+  CK(launch_check_state(c->qf[c->cur], c->qc, c->n, c->ns, c->ld, c->d_err, c->stream));
+  c->hrr_dot_state = 0;
+  int rc2 = refresh_chem_set(c);
+  if (rc2) return rc2;
+  CK(cudaStreamSynchronize(c->stream));
+  return take_status(c, "edyn_upload");
 }
 
 int edyn_init_cells(void* ctx, const double* T, const double* p, const double* u, const double* X) {
@@ -532,8 +786,12 @@ int edyn_init_cells(void* ctx, const double* T, const double* p, const double* u
   CK(cudaMemcpyAsync(du, u, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
   CK(cudaMemcpyAsync(dX, X, n * ns * sizeof(double), cudaMemcpyHostToDevice, c->stream));
   CK(launch_init_cells(c->n, c->ns, dT, dp, du, dX, c->ns, c->qf[c->cur], c->qc, c->ld, c->stream));
+  CK(launch_check_state(c->qf[c->cur], c->qc, c->n, c->ns, c->ld, c->d_err, c->stream));
   CK(cudaStreamSynchronize(c->stream));
-  return refresh_chem_set(c);
+  c->hrr_dot_state = 0;
+  int rc2 = refresh_chem_set(c);
+  if (rc2) return rc2;
+  return take_status(c, "edyn_init_cells");
 }
 
 int edyn_calc_dt(void* ctx, double cfl, double* dt) {
@@ -554,10 +812,12 @@ int edyn_calc_dt(void* ctx, double cfl, double* dt) {
 int edyn_solve_fluid(void* ctx, double dt) {
   Ctx* c = (Ctx*)ctx;
   if (!c || !c->qc) return EDYN_E_ARG;
-  int rc = fluid_step(c, dt, false, true);
+  int rc = keep_hrr_dot(c);
+  if (rc) return rc;
+  rc = fluid_step(c, dt, false, true);
   if (rc) return rc;
   CK(cudaStreamSynchronize(c->stream));
-  return EDYN_OK;
+  return take_status(c, "edyn_solve_fluid");
 }
 
 int edyn_solve_source(void* ctx, double dt, double time) {
@@ -566,11 +826,9 @@ int edyn_solve_source(void* ctx, double dt, double time) {
   if (!c || !c->qc) return EDYN_E_ARG;
   int rc = source_step(c, dt, false);
   if (rc) return rc;
+  if (c->do_reaction) c->hrr_dot_state = 1;
   CK(cudaStreamSynchronize(c->stream));
-  unsigned e = 0;
-  CK(cudaMemcpy(&e, c->d_err, sizeof(e), cudaMemcpyDeviceToHost));
-  if (e) return fail(c, (int)e, "chemistry reported status 0x%x", e);
-  return EDYN_OK;
+  return take_status(c, "edyn_solve_source");
 }
 
 int edyn_post_step(void* ctx) {
@@ -589,6 +847,8 @@ int edyn_step(void* ctx, double cfl, double* dt) {
   double d;
   int rc = edyn_calc_dt(ctx, cfl, &d);
   if (rc) return rc;
+  // the source step of this call supersedes the last one's HRR_dot
+  if (c->do_reaction) c->hrr_dot_state = 0;
   rc = edyn_solve_fluid(ctx, d);
   if (rc) return rc;
   rc = edyn_solve_source(ctx, d, 0.0);
@@ -601,10 +861,40 @@ int edyn_step(void* ctx, double cfl, double* dt) {
 int edyn_advance(void* ctx, double cfl, double tend, long long max_steps, double* time, long long* nsteps) {
   Ctx* c = (Ctx*)ctx;
   if (!c || !c->qc || !time) return EDYN_E_ARG;
+  // every step of the loop ends with a source step when chemistry is on, so
+  // the HRR_dot of the last one before this call is superseded, not lost
+  if (max_steps < 0) return fail(c, EDYN_E_ARG, "max_steps=%lld must be >= 0", max_steps);
   CK(cudaMemcpyAsync(c->d_time, time, sizeof(double), cudaMemcpyHostToDevice, c->stream));
   CK(cudaMemsetAsync(c->d_nsteps, 0, sizeof(long long), c->stream));
+  // pageable source: the copy is staged before the call returns, so the
+  // stack variable may go out of scope
+  const long long budget = max_steps;
+  CK(cudaMemcpyAsync(c->d_max_steps, &budget, sizeof(long long), cudaMemcpyHostToDevice, c->stream));
   CK(cudaMemsetAsync(c->d_cvel, 0, sizeof(unsigned long long), c->stream));
   CK(launch_cvel(c->qf[c->cur], c->n, c->ld, c->d_cvel, c->stream));
+  if (c->do_reaction && c->chem_mode == 1) {
+    // The surrogate path sizes its launches from counts it reads back, so
+    // its steps run from the host, one at a time, with the device clock.
+    long long done = 0;
+    double t = *time;
+    while (t < tend && done < max_steps) {
+      CK(launch_step_begin(c->d_time, tend, c->d_nsteps, c->d_max_steps, cfl, c->dx, c->d_cvel, c->d_active, c->d_dt,
+                           c->stream));
+      int rc = fluid_step(c, 0.0, true, false);
+      if (!rc) rc = source_step(c, 0.0, true);
+      if (rc) return rc;
+      long long ns = 0;
+      CK(cudaMemcpyAsync(&t, c->d_time, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+      CK(cudaMemcpyAsync(&ns, c->d_nsteps, sizeof(long long), cudaMemcpyDeviceToHost, c->stream));
+      CK(cudaStreamSynchronize(c->stream));
+      if (ns == done) break;
+      done = ns;
+    }
+    *time = t;
+    if (nsteps) *nsteps = done;
+    if (done > 0) c->hrr_dot_state = 1;
+    return take_status(c, "edyn_advance");
+  }
   // Steps per graph: even, so the primitive double buffer returns to the
   // same parity and one captured graph serves every launch.
   const int per_graph = 16;
@@ -615,7 +905,8 @@ int edyn_advance(void* ctx, double cfl, double tend, long long max_steps, double
     CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
     int rc = 0;
     for (int s = 0; s < per_graph && !rc; ++s) {
-      cudaError_t e = launch_step_begin(c->d_time, tend, cfl, c->dx, c->d_cvel, c->d_active, c->d_dt, c->stream);
+      cudaError_t e = launch_step_begin(c->d_time, tend, c->d_nsteps, c->d_max_steps, cfl, c->dx, c->d_cvel,
+                                        c->d_active, c->d_dt, c->stream);
       if (e != cudaSuccess) rc = fail(c, EDYN_E_CUDA, "step_begin: %s", cudaGetErrorString(e));
       if (!rc) rc = fluid_step(c, 0.0, true, !c->do_reaction);
       if (!rc) rc = source_step(c, 0.0, true);
@@ -643,10 +934,8 @@ int edyn_advance(void* ctx, double cfl, double tend, long long max_steps, double
   }
   *time = t;
   if (nsteps) *nsteps = done;
-  unsigned e = 0;
-  CK(cudaMemcpy(&e, c->d_err, sizeof(e), cudaMemcpyDeviceToHost));
-  if (e) return fail(c, (int)e, "device status 0x%x", e);
-  return EDYN_OK;
+  if (done > 0 && c->do_reaction) c->hrr_dot_state = 1;
+  return take_status(c, "edyn_advance");
 }
 
 int edyn_download(void* ctx, double* qf_aos, double* qc_aos, double* hrr) {
@@ -669,6 +958,105 @@ int edyn_download(void* ctx, double* qf_aos, double* qc_aos, double* hrr) {
     CK(cudaMemcpyAsync(hrr, c->hrr, (size_t)c->n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
   }
+  return EDYN_OK;
+}
+
+int edyn_set_surrogate(void* ctx, const void* w0, const void* w1, const void* w2, const void* w3, const float* b0,
+                       const float* b1, const float* b2, const float* b3, const float* norm, double rtol, double atol,
+                       double etol) {
+  Ctx* c = (Ctx*)ctx;
+  if (!c || !c->qc) return EDYN_E_ARG;
+  const bool net = w0 != nullptr;
+  if (net && (!w1 || !w2 || !w3 || !b0 || !b1 || !b2 || !b3 || !norm))
+    return fail(c, EDYN_E_ARG, "edyn_set_surrogate: a network needs all four weights, biases and the normalisation");
+  for (const void* ptr : {w0, w1, w2, w3})
+    if (ptr && (reinterpret_cast<uintptr_t>(ptr) & 15))
+      return fail(c, EDYN_E_ARG, "edyn_set_surrogate: tiled weights must be 16-byte aligned");
+  if (!(rtol > 0) || !(atol >= 0) || !(etol > 0)) return fail(c, EDYN_E_ARG, "edyn_set_surrogate: bad gate tolerances");
+  Surr& z = c->surr;
+  const edyn_mech& m = c->mech;
+  if (m.nspec + 3 > Surr::KIN) return fail(c, EDYN_E_ARG, "edyn_set_surrogate: %d species do not fit the network's 64 "
+                                                         "inputs", m.nspec);
+  if (!z.d_count) {
+    const size_t n = (size_t)c->n, nrow = (size_t)m.nspec + 1, M = (n + 127) / 128 * 128;
+    CK(cudaMalloc(&z.d_count, 4 * sizeof(unsigned)));
+    CK(cudaMalloc(&z.pk_idx, n * sizeof(int)));
+    CK(cudaMalloc(&z.pk_rho, n * sizeof(double)));
+    CK(cudaMalloc(&z.pk_dt, n * sizeof(double)));
+    for (double** b : {&z.pk_y0, &z.pk_f0, &z.pk_y1, &z.pk_ya, &z.pk_f1, &z.pk_fa, &z.rj_y})
+      CK(cudaMalloc(b, n * nrow * sizeof(double)));
+    CK(cudaMalloc(&z.X, M * Surr::KIN * 2));
+    CK(cudaMalloc(&z.Xt, M * Surr::KIN * 2));
+    for (int l = 0; l < 3; ++l) CK(cudaMalloc(&z.H[l], M * Surr::HID * 2));
+    CK(cudaMalloc(&z.out, M * Surr::KOUT * sizeof(float)));
+    CK(cudaMalloc(&z.zero_out, M * Surr::KOUT * sizeof(float)));
+    CK(cudaMemset(z.zero_out, 0, M * Surr::KOUT * sizeof(float)));
+    CK(cudaMalloc(&z.zero_one, 128 * sizeof(float)));
+    std::vector<float> zo(128, 0.f);
+    for (int j = 64; j < 128; ++j) zo[j] = 1.f;
+    CK(cudaMemcpy(z.zero_one, zo.data(), 128 * sizeof(float), cudaMemcpyHostToDevice));
+    CK(cudaMalloc(&z.accept, n * sizeof(int)));
+    CK(cudaMalloc(&z.rj_idx, n * sizeof(int)));
+    CK(cudaMalloc(&z.rj_rho, n * sizeof(double)));
+    CK(cudaMalloc(&z.rj_dt, n * sizeof(double)));
+    CK(cudaMalloc(&z.d_nrej, sizeof(int)));
+    std::vector<double> wm(m.nspec), el((size_t)m.nelem * m.nspec);
+    for (int k = 0; k < m.nspec; ++k) {
+      wm[k] = m.W[k] * 1e-3;
+      for (int e = 0; e < m.nelem; ++e) el[(size_t)e * m.nspec + k] = m.elem_count[k][e];
+    }
+    CK(cudaMalloc(&z.wmol, wm.size() * sizeof(double)));
+    CK(cudaMalloc(&z.elem, el.size() * sizeof(double)));
+    CK(cudaMemcpy(z.wmol, wm.data(), wm.size() * sizeof(double), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(z.elem, el.data(), el.size() * sizeof(double), cudaMemcpyHostToDevice));
+    z.nrow = m.nspec + 1;
+    z.ne = m.nelem;
+  }
+  z.net = net;
+  const void* w[4] = {w0, w1, w2, w3};
+  const float* b[4] = {b0, b1, b2, b3};
+  for (int l = 0; l < 4; ++l) {
+    z.wt[l] = w[l];
+    z.b[l] = b[l];
+  }
+  z.norm = norm;
+  z.rtol = rtol;
+  z.atol = atol;
+  z.etol = etol;
+  z.attached = true;
+  return EDYN_OK;
+}
+
+int edyn_surrogate_stats(void* ctx, double* stats) {
+  Ctx* c = (Ctx*)ctx;
+  if (!c || !c->qc || !stats) return EDYN_E_ARG;
+  for (int i = 0; i < 7; ++i) stats[i] = c->surr.stats[i];
+  return EDYN_OK;
+}
+
+int edyn_download_source(void* ctx, double* hrr, double* hrr_dot) {
+  Ctx* c = (Ctx*)ctx;
+  if (!c || !c->qc) return EDYN_E_ARG;
+  if (hrr) CK(cudaMemcpyAsync(hrr, c->hrr, (size_t)c->n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  if (hrr_dot) {
+    if (c->hrr_dot_state == 0) {
+      std::memset(hrr_dot, 0, (size_t)c->n * sizeof(double));
+    } else {
+      int rc = eval_hrr_dot(c);
+      if (rc) return rc;
+      CK(cudaMemcpyAsync(hrr_dot, c->hrr_dot, (size_t)c->n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    }
+  }
+  CK(cudaStreamSynchronize(c->stream));
+  return EDYN_OK;
+}
+
+int edyn_set_chem_max_steps(void* ctx, int max_steps) {
+  Ctx* c = (Ctx*)ctx;
+  if (!c || !c->qc) return EDYN_E_ARG;
+  if (max_steps < 0) return fail(c, EDYN_E_ARG, "max_steps=%d must be >= 0 (0: the default 4000)", max_steps);
+  c->chem_max_steps = max_steps;
+  drop_graph(c);
   return EDYN_OK;
 }
 
@@ -738,6 +1126,7 @@ int edyn_reactors_device(void* ctx, int n, const double* rho_d, const double* dt
   L.dt_batch = dt_d;
   L.yiT_batch = yiT_d;
   L.err = c->d_err;
+  L.max_steps = c->chem_max_steps;
   cudaError_t e = chem_launch_batch(c->chem, L, c->stream);
   if (e != cudaSuccess) return fail(c, EDYN_E_CUDA, "reactor launch: %s", cudaGetErrorString(e));
   CK(cudaStreamSynchronize(c->stream));
@@ -750,13 +1139,7 @@ int edyn_reactors_device(void* ctx, int n, const double* rho_d, const double* dt
     stats[2] = (double)k.rejects;
     stats[3] = (double)k.failed;
   }
-  unsigned st = 0;
-  CK(cudaMemcpy(&st, c->d_err, sizeof(st), cudaMemcpyDeviceToHost));
-  if (st) {
-    CK(cudaMemset(c->d_err, 0, sizeof(unsigned)));
-    return fail(c, (int)st, "reactor status 0x%x", st);
-  }
-  return EDYN_OK;
+  return take_status(c, "edyn_reactors");
 }
 
 int edyn_chem_rhs_device(void* ctx, int n, const double* rho_d, const double* yiT_d, double* f_d) {
@@ -765,6 +1148,16 @@ int edyn_chem_rhs_device(void* ctx, int n, const double* rho_d, const double* yi
   if (n == 0) return EDYN_OK;
   cudaError_t e = chem_rhs_batch(c->chem, n, rho_d, yiT_d, f_d, c->stream);
   if (e != cudaSuccess) return fail(c, EDYN_E_CUDA, "right-hand side launch: %s", cudaGetErrorString(e));
+  return EDYN_OK;
+}
+
+int edyn_chem_rhs_tube(void* ctx, int n, const double* rho_d, const double* yiT_d, double* f_d) {
+  Ctx* c = (Ctx*)ctx;
+  if (!c || !c->qc || n < 0 || (n > 0 && (!rho_d || !yiT_d || !f_d))) return EDYN_E_ARG;
+  if (n == 0) return EDYN_OK;
+  cudaError_t e = chem_rhs_batch(c->use_sub ? c->chem_sub : c->chem, n, rho_d, yiT_d, f_d, c->stream);
+  if (e != cudaSuccess) return fail(c, EDYN_E_CUDA, "right-hand side launch: %s", cudaGetErrorString(e));
+  CK(cudaStreamSynchronize(c->stream));
   return EDYN_OK;
 }
 
@@ -803,14 +1196,25 @@ int edyn_finalize(void* ctx) {
   chem_free(c->chem);
   if (c->chem_sub.d_tables) chem_free(c->chem_sub);
   cudaFree(c->d_present);
+  {
+    Surr& z = c->surr;
+    void* bufs[] = {z.d_count, z.pk_idx, z.pk_rho, z.pk_dt, z.pk_y0, z.pk_f0, z.pk_y1, z.pk_ya, z.pk_f1,
+                    z.pk_fa,   z.X,      z.Xt,     z.H[0],  z.H[1],  z.H[2],  z.out,   z.zero_out, z.zero_one,
+                    z.accept,  z.rj_idx, z.rj_rho, z.rj_dt, z.rj_y,  z.d_nrej, z.wmol, z.elem};
+    for (void* b : bufs) cudaFree(b);
+  }
   cudaFree(c->qf[0]);
   cudaFree(c->qf[1]);
   cudaFree(c->qc);
   cudaFree(c->q0);
+  cudaFree(c->acc);
   cudaFree(c->hrr);
+  cudaFree(c->hrr_dot);
+  cudaFree(c->tchem);
   cudaFree(c->staging);
   cudaFree(c->d_time);
   cudaFree(c->d_nsteps);
+  cudaFree(c->d_max_steps);
   cudaFree(c->d_active);
   cudaFree(c->d_dt);
   cudaFree(c->d_cvel);
@@ -879,11 +1283,23 @@ int fluid_scratch(Ctx* c, double** out) {
 extern "C" int edyn_solve_fluid_noalloc(void* ctx, double* qf_d, double* qc_d, double dt) {
   Ctx* c = (Ctx*)ctx;
   if (!c || !c->qc) return EDYN_E_ARG;
-  if (!qf_d || !qc_d || qf_d == qc_d)
+  if (!qf_d || !qc_d)
     return fail(c, EDYN_E_ARG, "edyn_solve_fluid_noalloc: two distinct device arrays (qf, Qc) are required");
   if ((reinterpret_cast<uintptr_t>(qf_d) | reinterpret_cast<uintptr_t>(qc_d)) % alignof(double))
     return fail(c, EDYN_E_ARG, "edyn_solve_fluid_noalloc: qf and Qc must be 8-byte aligned");
   const size_t rows = (size_t)c->ne * c->ld;
+  if (c->select_time == 2)
+    return fail(c, EDYN_E_ARG, "edyn_solve_fluid_noalloc: RK4 (select_time 2) needs a third scratch array; use "
+                               "edyn_solve_fluid");
+  // The stage kernel writes qf while it reads and updates Qc in place: the
+  // two arrays must not share a byte.
+  {
+    const uintptr_t f0 = reinterpret_cast<uintptr_t>(qf_d), q0 = reinterpret_cast<uintptr_t>(qc_d);
+    const uintptr_t span = rows * sizeof(double);
+    if (f0 < q0 + span && q0 < f0 + span)
+      return fail(c, EDYN_E_ARG, "edyn_solve_fluid_noalloc: the qf and Qc arrays overlap (each spans %zu bytes)",
+                  (size_t)span);
+  }
   if (2 * rows > (size_t)EDYN_NOALLOC_SCRATCH_DOUBLES)
     return fail(c, EDYN_E_ARG,
                 "edyn_solve_fluid_noalloc: the tube needs 2*nequ*(ncell+8) = %zu doubles of scratch, the static "
@@ -919,5 +1335,5 @@ extern "C" int edyn_solve_fluid_noalloc(void* ctx, double* qf_d, double* qc_d, d
   CK(cudaMemcpy2DAsync(qf_d + GHOST, pitch, scr + GHOST, pitch, (size_t)c->n * sizeof(double), (size_t)c->ne,
                        cudaMemcpyDeviceToDevice, c->stream));
   CK(cudaStreamSynchronize(c->stream));
-  return EDYN_OK;
+  return take_status(c, "edyn_solve_fluid_noalloc");
 }

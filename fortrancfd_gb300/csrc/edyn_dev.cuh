@@ -27,6 +27,12 @@
 #define EDYN_NS_MAX 64
 #endif
 
+// Status bits a kernel ORs into its context's error word (the values of
+// EDYN_E_NEWTON, EDYN_E_CHEM and EDYN_E_STATE of include/edyn_gpu.h).
+#define EDYN_STATUS_NEWTON 8u
+#define EDYN_STATUS_CHEM 16u
+#define EDYN_STATUS_STATE 32u
+
 namespace edyn {
 
 // SI gas constant used by SRC/thermo.f90 (CHEMKIN RU = 8.314510e7 erg/mol/K).

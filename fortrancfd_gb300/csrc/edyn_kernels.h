@@ -32,7 +32,9 @@ struct StageArgs {
   double* qf_out;        // primitive rows written for owned cells
   double* qc;            // conserved rows, updated in place
   double* q0;            // stage-0 conserved rows (TVDRK3)
-  int kind;              // 0: Q - c dF (Euler, first TVDRK3 stage); 1: h1 Q0 + h2 (Q - c dF)
+  int kind;              // 0: Q - c dF (Euler, first TVDRK3 stage); 1: h1 Q0 + h2 (Q - c dF); 2: RK4 stage
+  int rk4_stage;         // kind 2: stage 0..3 of RK4 (SRC/timeintegration.f90:222-356)
+  double* acc;           // kind 2: k1 + 2 k2 + 2 k3, accumulated over the stages
   int save_q0;           // copy Q into q0 before the update (first TVDRK3 stage)
   double h1, h2;
   double dx, dt;         // dt used when dt_dev is null
@@ -45,6 +47,7 @@ struct StageArgs {
   double p_out;
   int strict_newton;     // 1: T Newton starts at 1000 K as the reference
   FluidBC bc;            // inlet data (SRC/flow_bound.f90), passed by value
+  unsigned* err;         // status word: EDYN_E_NEWTON / EDYN_E_STATE bits of any cell (may be null)
 };
 
 int fluid_upload_tables(const ThermoTable& tb, cudaStream_t s);
@@ -53,11 +56,14 @@ cudaError_t stage_tiling(int acu, int lim, int wflag, int rm, int ns, int n, int
 cudaError_t launch_stage(const StageArgs& a, int acu, int lim, int wflag, int rm, cudaStream_t s);
 cudaError_t launch_cvel(const double* qf, int n, int ld, unsigned long long* cvel, cudaStream_t s);
 cudaError_t launch_species_present(const double* qc, int ld, int n, int ns, int* flags, cudaStream_t s);
-cudaError_t launch_step_begin(const double* time, double tend, double cfl, double dx, unsigned long long* cvel,
-                              int* step_active, double* dt_dev, cudaStream_t s);
+cudaError_t launch_step_begin(const double* time, double tend, const long long* nsteps, const long long* max_steps,
+                              double cfl, double dx, unsigned long long* cvel, int* step_active, double* dt_dev,
+                              cudaStream_t s);
 cudaError_t launch_aos_to_soa(const double* aos, int ne, int n, double* soa, int ld, cudaStream_t s);
 cudaError_t launch_soa_to_aos(const double* soa, int ne, int n, int ld, double* aos, cudaStream_t s);
 cudaError_t launch_qc_to_qf(const StageArgs& a, cudaStream_t s);
+cudaError_t launch_check_state(const double* qf, const double* qc, int n, int ns, int ld, unsigned* err,
+                               cudaStream_t s);
 cudaError_t launch_init_cells(int n, int ns, const double* T, const double* p, const double* u, const double* X,
                               int ldx, double* qf, double* qc, int ld, cudaStream_t s);
 

@@ -49,7 +49,22 @@ static_assert(sizeof(ThermoTable) < 60000, "constant tables too large");
 // ---------------------------------------------------------------------------
 struct CellEOS {
   double T, u, Sz, cpR;  // cpR = Cp(T) of the final premix, for the sound speed
+  unsigned status;       // EDYN_E_NEWTON / EDYN_E_STATE bits of this cell (0: sound)
 };
+
+// Status bits of one cell's QcToqf, which the reference leaves silent
+// (temperature_con stops at its iteration cap and clamps T to [20, 6000] K,
+// SRC/thermo.f90:244-255): EDYN_E_NEWTON when the Newton ended at the cap
+// with neither stopping test met, EDYN_E_STATE for a non-positive or
+// non-finite density, energy or mass-fraction sum, or a temperature pinned
+// at a clamp bound.
+__device__ __forceinline__ unsigned cell_status(double rho, double E, double sy, double T, int iters) {
+  unsigned st = 0;
+  if (iters < 0) st |= EDYN_STATUS_NEWTON;
+  if (!(rho > 0.0) || !isfinite(rho) || !isfinite(E) || !(sy > 0.0) || !isfinite(sy) || !(T > 20.0 && T < 6000.0))
+    st |= EDYN_STATUS_STATE;
+  return st;
+}
 
 // Sum of v over an aligned group of S lanes (a power of two) that split a
 // cell's species between them (identity for S = 1), by an xor tree: every
@@ -104,7 +119,8 @@ __device__ __forceinline__ double t_newton(const double* ys, int st, double E, d
     ++it;
   }
   if (t_interval(tb, T) != pm.interval) premix_cell<S>(ys, st, T, pm, Sz, h, mask);
-  iters = it;
+  // the cap ended the loop while both stopping tests still failed: -it
+  iters = (fabs(g) >= fabs(E) * 1e-9 && fabs(dT) >= T * 1e-6) ? -it : it;
   return T;
 }
 
@@ -134,6 +150,7 @@ __device__ __forceinline__ CellEOS qc_to_qf_cell(double rho, double rhou, double
   r.T = t_newton<S>(ys, st, E, strict ? 1000.0 : Tguess, pm, Sz, iters, h, mask);
   r.Sz = Sz;
   r.cpR = pm.Cp(r.T);
+  r.status = cell_status(rho, E, s, r.T, iters);
   return r;
 }
 
@@ -233,6 +250,7 @@ __device__ void ghost_cell(const StageArgs& a, int g, double* dst, int dst_st, d
     }
   }
   CellEOS e = qc_to_qf_cell(q0, q1, q2, ys, st, 1000.0, true, iters);
+  if (e.status && a.err) atomicOr(a.err, e.status);
   dst[0] = q0;
   dst[dst_st] = e.u;
   dst[2 * dst_st] = e.T;
@@ -442,15 +460,41 @@ __global__ void __launch_bounds__(STAGE_MAX_THREADS) k_stage(StageArgs a) {
   //    species split as in phase 3 (the bulk rows are computed by every lane)
   const int i = c0 + f;
   double speed = 0.0;
-  if (f < P && i < c1) {
+  // RK4 (kind 2) keeps the interior primitive state of the step's start
+  // through its stages, as the reference does (its stages update only Qc and
+  // the boundary ghosts): only the last stage runs QcToqf.
+  const bool rk4_mid = a.kind == 2 && a.rk4_stage < 3;
+  if (f < P && i < c1 && rk4_mid) {
+    const double c = dt / a.dx;
+    const double cq = 0.5 * ((0.5 * dt) / a.dx);  // 0.5 (0.5 dt / dx) of stages 1 and 2
+    const size_t ld = (size_t)a.ld;
+    double* Q = a.qc + i + GHOST;
+    double* Q0 = a.q0 + i + GHOST;
+    double* A = a.acc + i + GHOST;
+    for (int v = h; v < ne; v += SP) {
+      const double dF = s_l[v * P + f + 1] - s_l[v * P + f];
+      const double k = -(c * dF);
+      const double qs = Q[v * ld];
+      if (a.rk4_stage == 0) {
+        Q0[v * ld] = qs;
+        A[v * ld] = k;
+      } else {
+        A[v * ld] = A[v * ld] + 2.0 * k;
+      }
+      Q[v * ld] = qs - (a.rk4_stage < 2 ? cq : c) * dF;
+    }
+  }
+  if (f < P && i < c1 && !rk4_mid) {
     const double c = dt / a.dx;
     const size_t ld = (size_t)a.ld;
     double* Q = a.qc + i + GHOST;
     double* Q0 = a.q0 + i + GHOST;
     double* ys = s_r + f;  // strided by P
-    // Euler or first TVDRK3 stage: Q - c dF; later stages h1 Q0 + h2 (Q - c dF)
+    // Euler or first TVDRK3 stage: Q - c dF; later stages h1 Q0 + h2 (Q - c dF);
+    // last RK4 stage: Q0 + (k1 + 2 k2 + 2 k3 + k4) / 6
     auto update = [&](int v, double qv) {
       const double dF = s_l[v * P + f + 1] - s_l[v * P + f];
+      if (a.kind == 2) return Q0[v * ld] + (1.0 / 6.0) * (a.acc[v * ld + i + GHOST] + -(c * dF));
       return a.kind == 0 ? qv - c * dF : fma(a.h1, Q0[v * ld], a.h2 * (qv - c * dF));
     };
     double q[3], qv[3];
@@ -481,6 +525,7 @@ __global__ void __launch_bounds__(STAGE_MAX_THREADS) k_stage(StageArgs a) {
       out[ld] = e.u;
       out[2 * ld] = e.T;
       if (a.cvel_out) speed = cell_speed(e.u, e.T, e.Sz, e.cpR);
+      if (e.status && a.err) atomicOr(a.err, e.status);
     }
     for (int k = h; k < ns; k += SP) out[(3 + k) * ld] = ys[k * P];
   }
@@ -499,9 +544,11 @@ __global__ void __launch_bounds__(STAGE_MAX_THREADS) k_stage(StageArgs a) {
 // One thread: decides whether the step runs (time < tend, the loop test of
 // SRC/main.f90:130), computes dt = cfl dx / max speed (SRC/update.f90:50)
 // from the maximum left by the previous step, and clears the accumulator.
-__global__ void k_step_begin(const double* time, double tend, double cfl, double dx, unsigned long long* cvel,
-                             int* step_active, double* dt_dev) {
-  if (!(*time < tend)) {
+__global__ void k_step_begin(const double* time, double tend, const long long* nsteps, const long long* max_steps,
+                             double cfl, double dx, unsigned long long* cvel, int* step_active, double* dt_dev) {
+  // the step budget of this call (edyn_advance's max_steps) ends the loop as
+  // the end time does, so a call runs exactly the steps it was given
+  if (!(*time < tend) || *nsteps >= *max_steps) {
     *step_active = 0;
     return;
   }
@@ -573,10 +620,37 @@ __global__ void k_qc_to_qf(StageArgs a) {
   double* out = a.qf_out + i + GHOST;
   const double Tg = a.qf_in ? a.qf_in[2 * ld + i + GHOST] : 1000.0;
   CellEOS e = qc_to_qf_cell(Q[0], Q[ld], Q[2 * ld], ys, blockDim.x, Tg, a.strict_newton != 0 || !a.qf_in, iters);
+  if (e.status && a.err) atomicOr(a.err, e.status);
   out[0] = Q[0];
   out[ld] = e.u;
   out[2 * ld] = e.T;
   for (int k = 0; k < ns; ++k) out[(3 + k) * ld] = ys[k * blockDim.x];
+}
+
+// Checks an uploaded interior state: per cell a positive, finite density and
+// total energy, a temperature strictly inside the clamp bounds (20, 6000) K,
+// finite mass fractions none below -1e-6 (adjust_sum clips round-off
+// negatives; larger ones mean a broken state) and finite conserved rows.
+// ORs EDYN_E_STATE into err for any cell that fails.
+__global__ void k_check_state(const double* qf, const double* qc, int n, int ns, int ld, unsigned* err) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double* q = qf + i + GHOST;
+  const double* Q = qc + i + GHOST;
+  const size_t l = (size_t)ld;
+  bool ok = q[0] > 0.0 && isfinite(q[0]) && isfinite(q[l]) && q[2 * l] > 20.0 && q[2 * l] < 6000.0 && Q[0] > 0.0 &&
+            isfinite(Q[0]) && isfinite(Q[l]) && isfinite(Q[2 * l]);
+  for (int k = 0; k < ns && ok; ++k) {
+    const double y = q[(3 + k) * l];
+    ok = isfinite(y) && y >= -1e-6 && isfinite(Q[(3 + k) * l]);
+  }
+  if (!ok) atomicOr(err, EDYN_STATUS_STATE);
+}
+
+cudaError_t launch_check_state(const double* qf, const double* qc, int n, int ns, int ld, unsigned* err,
+                               cudaStream_t s) {
+  k_check_state<<<(n + 127) / 128, 128, 0, s>>>(qf, qc, n, ns, ld, err);
+  return cudaGetLastError();
 }
 
 // Initial state of one cell from (T, p, u, X): initialize_variables
@@ -786,9 +860,10 @@ cudaError_t launch_soa_to_aos(const double* soa, int ne, int n, int ld, double* 
   return cudaGetLastError();
 }
 
-cudaError_t launch_step_begin(const double* time, double tend, double cfl, double dx, unsigned long long* cvel,
-                              int* step_active, double* dt_dev, cudaStream_t s) {
-  k_step_begin<<<1, 1, 0, s>>>(time, tend, cfl, dx, cvel, step_active, dt_dev);
+cudaError_t launch_step_begin(const double* time, double tend, const long long* nsteps, const long long* max_steps,
+                              double cfl, double dx, unsigned long long* cvel, int* step_active, double* dt_dev,
+                              cudaStream_t s) {
+  k_step_begin<<<1, 1, 0, s>>>(time, tend, nsteps, max_steps, cfl, dx, cvel, step_active, dt_dev);
   return cudaGetLastError();
 }
 

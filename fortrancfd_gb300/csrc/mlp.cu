@@ -31,6 +31,12 @@ constexpr int GEMM_THREADS = 256;  // eight warps: two per TMEM lane quarter in 
 constexpr unsigned long long WAIT_NS = 2000000000ull;  // 2 s
 
 __device__ unsigned g_err;
+// Limit of the waits that gate the next step of a GEMM (operand copies
+// landed, a buffer free again). A wait that runs out stops the GEMM; the
+// drain waits afterwards (copies and products already issued) always keep
+// the full WAIT_NS. 0 makes every gating wait give up at once, which is how
+// a test reaches the failure path without a stuck barrier.
+__device__ unsigned long long g_wait_ns = WAIT_NS;
 
 enum Epi : int { EPI_F32 = 0, EPI_GELU = 1, EPI_DGELU = 2 };
 
@@ -77,8 +83,9 @@ __device__ __forceinline__ void mbar_init(uint64_t* b, unsigned count) {
 }
 
 // Bounded wait for the phase of the given parity to complete. false: the
-// limit ran out.
-__device__ __forceinline__ bool mbar_wait(uint64_t* b, unsigned parity) {
+// limit ran out (limit 0: at once, without polling).
+__device__ __forceinline__ bool mbar_wait(uint64_t* b, unsigned parity, unsigned long long limit = WAIT_NS) {
+  if (limit == 0) return false;
   const uint32_t a = smem_u32(b);
   const unsigned long long t0 = gtime();
   for (int it = 0; it < (1 << 26); ++it) {
@@ -91,7 +98,7 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* b, unsigned parity) {
         : "r"(a), "r"(parity)
         : "memory");
     if (ok) return true;
-    if ((it & 255) == 255 && gtime() - t0 > WAIT_NS) break;
+    if ((it & 255) == 255 && gtime() - t0 > limit) break;
   }
   return false;
 }
@@ -272,13 +279,14 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1) k_gemm(GemmArgs a) {
   constexpr uint32_t IDESC = idesc_bf16(BM, BN);
 
   const int nk = a.K / BK;
+  const unsigned long long wait_ns = g_wait_ns;
   bool ok = true;
   int last = -1;  // last tile whose products were issued
   for (int kt = 0; kt < nk && ok; ++kt) {
     const int buf = kt & 1;
     char* sa = base + buf * STAGE;
     char* sb = sa + A_BYTES;
-    if (kt >= 2) ok = mbar_wait(&bar[buf], ((kt - 2) >> 1) & 1);  // the tensor core is done with this buffer
+    if (kt >= 2) ok = mbar_wait(&bar[buf], ((kt - 2) >> 1) & 1, wait_ns);  // the tensor core is done with this buffer
     ok = __syncthreads_and(ok);
     if (!ok) break;
     stage_tile<BM>(sa, a.A, a.lda, m0, a.M, kt * BK);
@@ -384,12 +392,13 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1) k_gemm_tiled(GemmArgs a) {
   const int nk = a.K / BK;
   const char* gA = reinterpret_cast<const char*>(a.A) + (size_t)blockIdx.x * nk * A_BYTES;
   const char* gB = reinterpret_cast<const char*>(a.B) + (size_t)blockIdx.y * nk * B_BYTES;
+  const unsigned long long wait_ns = g_wait_ns;
   bool ok = true;
   int last = -1, produced = 0;
   if (threadIdx.x == 0) {
     auto produce = [&](int kt) -> bool {
       const int q = kt % ST;
-      if (kt >= ST && !mbar_wait(&empty[q], ((kt / ST) - 1) & 1)) return false;
+      if (kt >= ST && !mbar_wait(&empty[q], ((kt / ST) - 1) & 1, wait_ns)) return false;
       char* sa = base + q * STAGE;
       mbar_expect_tx(&full[q], STAGE);
       bulk_g2s(sa, gA + (size_t)kt * A_BYTES, A_BYTES, &full[q]);
@@ -400,7 +409,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1) k_gemm_tiled(GemmArgs a) {
     for (int kt = 0; kt < ST - 1 && kt < nk && ok; ++kt) ok = produce(kt);
     for (int kt = 0; kt < nk && ok; ++kt) {
       const int q = kt % ST;
-      if (!mbar_wait(&full[q], (kt / ST) & 1)) {
+      if (!mbar_wait(&full[q], (kt / ST) & 1, wait_ns)) {
         ok = false;
         break;
       }
@@ -740,6 +749,10 @@ int edyn_mlp_gemm_tiled(const void* At, const void* Bt, int M, int N, int K, int
     default: e = launch_gemm_tiled<64>(a, S(stream)); break;
   }
   return rc(e);
+}
+
+int edyn_mlp_set_wait_limit(unsigned long long ns) {
+  return cudaMemcpyToSymbol(g_wait_ns, &ns, sizeof(ns)) == cudaSuccess ? EDYN_OK : EDYN_E_CUDA;
 }
 
 int edyn_mlp_status(void* stream) {

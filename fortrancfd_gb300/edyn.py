@@ -65,6 +65,11 @@ def lib() -> ctypes.CDLL:
     L.edyn_step.argtypes = [vp, d, dp]
     L.edyn_advance.argtypes = [vp, d, d, ctypes.c_longlong, dp, ctypes.POINTER(ctypes.c_longlong)]
     L.edyn_download.argtypes = [vp, dp, dp, dp]
+    L.edyn_download_source.argtypes = [vp, dp, dp]
+    L.edyn_set_chem_max_steps.argtypes = [vp, i]
+    L.edyn_chem_rhs_tube.argtypes = [vp, i, vp, vp, vp]
+    L.edyn_set_surrogate.argtypes = [vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, d, d, d]
+    L.edyn_surrogate_stats.argtypes = [vp, dp]
     L.edyn_reactors.argtypes = [vp, i, dp, dp, dp, dp]
     L.edyn_reactors_device.argtypes = [vp, i, vp, vp, vp, dp]
     L.edyn_set_stream.argtypes = [vp, vp]
@@ -246,12 +251,58 @@ class Tube(_Ctx):
         self._check(lib().edyn_stage_tile(self._h, ctypes.byref(cells), ctypes.byref(threads)))
         return cells.value, threads.value
 
+    def chem_rhs_device(self, n: int, rho_ptr: int, yiT_ptr: int, f_ptr: int):
+        """FP64 right-hand sides of n reactors (device rows of nspe + 1)
+        with the species set this tube's chemistry integrates."""
+        self._check(lib().edyn_chem_rhs_tube(self._h, n, ctypes.c_void_p(rho_ptr), ctypes.c_void_p(yiT_ptr),
+                                             ctypes.c_void_p(f_ptr)))
+
+    def set_surrogate(self, surrogate=None, *, rtol=2.5e-4, atol=2.5e-10, etol=1e-6):
+        """Puts a trained surrogate (fortrancfd_gb300.surrogate.Surrogate) in
+        front of the implicit integrator of a chem_mode=1 tube; None puts
+        the gated explicit increment alone there (the method without the
+        network). The tube keeps a reference to the network's device
+        arrays."""
+        if surrogate is None:
+            self._surr_keep = None
+            self._check(lib().edyn_set_surrogate(self._h, *([None] * 9), rtol, atol, etol))
+            return
+        wt, b, norm = surrogate.mlp.device_arrays()
+        self._surr_keep = (wt, b, norm)
+        ptr = [ctypes.c_void_p(t.data_ptr()) for t in list(wt) + list(b) + [norm]]
+        self._check(lib().edyn_set_surrogate(self._h, *ptr, surrogate.rtol, surrogate.atol, surrogate.etol))
+
+    def surrogate_stats(self) -> dict:
+        """Counters of the last surrogate source step."""
+        st = np.zeros(7)
+        self._check(lib().edyn_surrogate_stats(self._h, _ptr(st)))
+        keys = ("handed", "accepted_network", "accepted_explicit", "fallback", "screen_rhs", "gate_rhs",
+                "fallback_rhs")
+        return {k: int(v) for k, v in zip(keys, st)}
+
+    def download_source(self):
+        """(HRR, HRR_dot) [W/m^3] of the last source step, one value per cell
+        (SRC/source.f90:70-73)."""
+        hrr = np.empty(self.ncell)
+        hrr_dot = np.empty(self.ncell)
+        self._check(lib().edyn_download_source(self._h, _ptr(hrr), _ptr(hrr_dot)))
+        return hrr, hrr_dot
+
     def download(self):
         qf = np.empty((self.ncell, self.nequ))
         qc = np.empty((self.ncell, self.nequ))
         hrr = np.empty(self.ncell)
         self._check(lib().edyn_download(self._h, _ptr(qf), _ptr(qc), _ptr(hrr)))
         return qf, qc, hrr
+
+
+def _set_chem_max_steps(self, max_steps: int = 0) -> None:
+    """Caps the implicit integrator at max_steps steps per cell and call
+    (0: the default); a cell at the cap fails with EDYN_E_CHEM."""
+    self._check(lib().edyn_set_chem_max_steps(self._h, int(max_steps)))
+
+
+_Ctx.set_chem_max_steps = _set_chem_max_steps
 
 
 class Reactors(_Ctx):

@@ -69,6 +69,7 @@ def _L():
         L.edyn_mlp_gemm_tiled.argtypes = [vp, vp, i, i, i, i, vp, vp, i, vp, i, i, vp]
         L.edyn_mlp_tile.argtypes = [vp, i, i, i, vp, vp]
         L.edyn_mlp_tile_rows.argtypes = [i]
+        L.edyn_mlp_set_wait_limit.argtypes = [ctypes.c_ulonglong]
         _bound = True
     return L
 
@@ -124,6 +125,12 @@ def transpose(x, out=None):
 
 def status():
     _ck(_L().edyn_mlp_status(_stream()), "mlp kernel wait ran out")
+
+
+def set_wait_limit(ns: int) -> None:
+    """Limit of the GEMM kernels' gating waits (default 2 s; 0: give up at
+    once, which exercises the failure path)."""
+    _ck(_L().edyn_mlp_set_wait_limit(int(ns)), "mlp wait limit")
 
 
 def element_matrix(mech_dir=GRI30_DIR):
@@ -234,6 +241,15 @@ class MLP:
             A, K = B["H"][l], HID
         gemm_tiled(A, self.Wt[DEPTH], M, KOUT, HID, EPI_F32, bias=self.b[DEPTH], C32=B["Y"])
         return B["Y"]
+
+    def device_arrays(self):
+        """(tiled BF16 weights, FP32 biases, normalisation 4 x 64) of the
+        current parameters, for a tube's surrogate path."""
+        if getattr(self, "_tiled_at", None) != self.step_count:
+            self.Wt = [tile(w, tile_rows(w.shape[0])) for w in self.W16]
+            self._tiled_at = self.step_count
+        norm = torch.cat([self.mu, self.isig, self.omu, self.osig]).contiguous()
+        return self.Wt, self.b, norm
 
     def loss_grad(self, target):
         """Mean-square error of the last forward output against target (FP32
@@ -418,6 +434,66 @@ def harvest_tube(case, nsteps=2000, every=20, rtol=1e-8, atol=1e-16, tube_rtol=1
     ref.integrate(rho, dt, y1)
     ref.close()
     return rho, dt, y0, y1
+
+
+def tube_sweep(n_cases, seed, *, ncell=4000, dx=5e-6, oxidizer="air"):
+    """Detonation tubes of the surrogate's training sweep: 5 um cells,
+    equivalence ratio phi ~ U[0.7, 1.4] and driver temperature ~ U[2500,
+    3500] K (seeded), the 1 cm driver and the rest as the benchmark tube."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n_cases):
+        phi, tdrv = rng.uniform(0.7, 1.4), rng.uniform(2500.0, 3500.0)
+        out.append(configs.detonation(ncell=ncell, length=ncell * dx, phi=phi, T_drv=tdrv, oxidizer=oxidizer))
+    return out
+
+
+def harvest_screened(cases, nsteps=100, every=1, rtol=1e-8, atol=1e-16, tube_rtol=1e-5, tube_atol=1e-13,
+                     device="cuda"):
+    """(rho, dt, y0, y1) pairs of the cells a chem_mode=1 tube hands to its
+    surrogate: every `every` steps of each case, the state the source step
+    sees (after the fluid step; Y adjust_summed) of the cells that fail the
+    integrator's inert-cell test (||dt f(y0)||_w > 1e-3 with the tube's
+    tolerances), advanced over the step's dt by the implicit integrator at
+    (rtol, atol). Host arrays (float64)."""
+    from .edyn import Tube
+
+    R, D, Y0 = [], [], []
+    for case in cases:
+        g = Tube(case.ncell, case.dx, rtol=tube_rtol, atol=tube_atol, strict_newton=0, **case.flags)
+        g.init_cells(case.T, case.p, case.u, case.X)
+        for st in range(nsteps):
+            dt = g.calc_dt(case.cfl)
+            g.solve_fluid(dt)
+            if st % every == every - 1:
+                qf, _, _ = g.download()
+                y = np.concatenate([np.maximum(qf[:, 3:], 0.0), qf[:, 2:3]], axis=1)
+                y[:, :-1] /= y[:, :-1].sum(axis=1, keepdims=True)
+                rho = torch.tensor(qf[:, 0], device=device)
+                yd = torch.tensor(np.ascontiguousarray(y), device=device)
+                f0 = torch.empty_like(yd)
+                g.chem_rhs_device(len(rho), rho.data_ptr(), yd.data_ptr(), f0.data_ptr())
+                w = tube_atol + tube_rtol * yd.abs()
+                nrm = torch.sqrt(((dt * f0 / w) ** 2).mean(dim=1))
+                keep = nrm > 1e-3
+                R.append(rho[keep])
+                D.append(torch.full((int(keep.sum()),), dt, dtype=torch.float64, device=device))
+                Y0.append(yd[keep])
+            g.solve_source(dt)
+        g.close()
+    rho, dt, y0 = torch.cat(R), torch.cat(D), torch.cat(Y0).contiguous()
+    y1 = y0.clone()
+    ref = Reactors(rtol=rtol, atol=atol)
+    # windows of 2^16 reactors per call
+    for a in range(0, len(rho), 1 << 16):
+        b = min(len(rho), a + (1 << 16))
+        blk = y1[a:b].contiguous()
+        ref.integrate_device(b - a, rho[a:b].contiguous().data_ptr(), dt[a:b].contiguous().data_ptr(),
+                             blk.data_ptr())
+        y1[a:b] = blk
+    ref.close()
+    torch.cuda.synchronize()
+    return rho.cpu().numpy(), dt.cpu().numpy(), y0.cpu().numpy(), y1.cpu().numpy()
 
 
 def train(s: Surrogate, rho, dt, y0, y1, *, iters=3000, batch=4096, lr=1e-3, seed=0, log_every=0):

@@ -24,13 +24,14 @@ extern "C" {
 #define EDYN_E_ARG 1        /* invalid argument or unsupported option */
 #define EDYN_E_CUDA 2       /* CUDA runtime error */
 #define EDYN_E_MECH 4       /* mechanism could not be read */
-#define EDYN_E_NEWTON 8     /* temperature Newton hit its iteration cap */
-#define EDYN_E_CHEM 16      /* a chemistry step was rejected to underflow */
-#define EDYN_E_STATE 32     /* non-finite or non-positive state found */
+#define EDYN_E_NEWTON 8     /* a cell's temperature Newton ended at its iteration cap, unconverged */
+#define EDYN_E_CHEM 16      /* a cell's chemistry integration failed (step underflow or step cap) */
+#define EDYN_E_STATE 32     /* a cell's state is non-finite or non-positive, its T pinned at 20 or
+                               6000 K, or an uploaded mass fraction is below -1e-6 */
 
 /* Indices into the iflags array of edyn_init (the solver.inp /params/ and
  * problem-file flags, SRC/params.f90:8-18, 105-142). */
-#define EDYN_IF_SELECT_TIME 0     /* 0 Euler, 1 TVDRK3, (2 RK4: not supported) */
+#define EDYN_IF_SELECT_TIME 0     /* 0 Euler, 1 TVDRK3, 2 RK4 (the reference's stale-qf form) */
 #define EDYN_IF_SELECT_RIEMANN 1  /* 0 LxF, 1 HLL, 2 HLLC */
 #define EDYN_IF_FLAG_ACU 2        /* 0 first order, 1 MUSCL, 2 WENO */
 #define EDYN_IF_FLAG_MUSCL 3      /* 1 unlimited, 2 minmod, 3 superbee, 4 MC */
@@ -39,7 +40,7 @@ extern "C" {
 #define EDYN_IF_FLAG_RBOUND 6     /* 0 wall, 1 outflow (fixed p_OUT) */
 #define EDYN_IF_DO_REACTION 7     /* 0 frozen, 1 per-cell chemistry */
 #define EDYN_IF_STRICT_NEWTON 8   /* 1: T Newton starts at 1000 K every call (reference); 0: warm start */
-#define EDYN_IF_CHEM_MODE 9       /* 0 plain implicit integrator, 1 surrogate with fallback */
+#define EDYN_IF_CHEM_MODE 9       /* 0 plain implicit integrator, 1 surrogate with fallback (edyn_set_surrogate) */
 #define EDYN_NIFLAGS 10
 
 /* Indices into the rparams array of edyn_init. */
@@ -73,7 +74,11 @@ int edyn_init_cells(void* ctx, const double* T, const double* p, const double* u
 /* calc_dt (SRC/update.f90:13): dt = cfl * dx / max(|u| + a). */
 int edyn_calc_dt(void* ctx, double cfl, double* dt);
 
-/* solve_fluid (SRC/update.f90:62): one explicit Euler or TVDRK3 step. */
+/* solve_fluid (SRC/update.f90:62): one explicit Euler, TVDRK3 or RK4 step.
+ * RK4 restates SRC/timeintegration.f90:222-356 as written: its stages update
+ * Qc and rebuild the boundary ghosts, but reconstruct from the interior
+ * primitive state of the step's start (qf is refreshed only after the last
+ * stage), with the reference's stage weights. */
 int edyn_solve_fluid(void* ctx, double dt);
 
 /* Size of the static scratch of edyn_solve_fluid_noalloc, in doubles
@@ -97,15 +102,25 @@ int edyn_solve_fluid(void* ctx, double dt);
  *
  * ctx comes from edyn_init (which allocates, once, at set-up); the call uses
  * its scheme, boundary data, mechanism tables and stream, and neither reads
- * nor writes the context's own state buffers. qf_d and qc_d are device
- * arrays in the library's device layout: nequ rows of ld = ncell + 8
- * doubles, row v holding variable v, cell i at column i + 4 (the columns
- * outside the cells are neither read nor written). On entry qf_d holds
- * QcToqf(qc_d); on return qc_d holds the state after the step and qf_d its
- * primitive variables. Returns after the step has finished on the stream.
+ * nor writes the context's own state buffers. qf_d and qc_d are two
+ * disjoint device arrays (overlapping ones are rejected with EDYN_E_ARG) in
+ * the library's device layout: nequ rows of ld = ncell + 8 doubles, row v
+ * holding variable v, cell i at column i + 4 (the columns outside the cells
+ * are neither read nor written). On entry qf_d holds QcToqf(qc_d); on return
+ * qc_d holds the state after the step and qf_d its primitive variables.
+ *
+ * The entry points that work on the context's own state (edyn_calc_dt,
+ * edyn_solve_source, edyn_step, edyn_advance, edyn_download) never see the
+ * caller's arrays: on this path the host computes dt from its own state
+ * (dt = cfl dx / max(|u| + a), as calc_dt does) and runs its own source
+ * step. The call blocks the calling host thread until the step has finished
+ * on the context's stream; the status then includes EDYN_E_NEWTON or
+ * EDYN_E_STATE when a cell's temperature Newton hit its iteration cap or a
+ * cell's state was non-finite, non-positive or clamped.
  *
  * Tubes with 2 * nequ * (ncell + 8) > EDYN_NOALLOC_SCRATCH_DOUBLES are
- * rejected with EDYN_E_ARG and a message naming the limit. The first call
+ * rejected with EDYN_E_ARG and a message naming the limit, and so is RK4
+ * (select_time 2), whose stage sum needs a third array. The first call
  * on a device looks up the scratch array's device address with that device
  * current (it must be the context's device); make that first call before
  * any stream capture. All calls share the scratch array, which keeps the
@@ -134,6 +149,68 @@ int edyn_advance(void* ctx, double cfl, double tend, long long max_steps, double
  * SRC/block.f90:434). Any pointer may be NULL. hrr receives HRR [W/m^3]
  * of the last source step (SRC/source.f90:70-73), ncell values. */
 int edyn_download(void* ctx, double* qf_aos, double* qc_aos, double* hrr);
+
+/* Heat release rates of the last source step, ncell values each (either
+ * pointer may be NULL): hrr = HRR (heat_release_rate, SRC/thermo.f90:83-103)
+ * and hrr_dot = HRR_dot (heat_release_rate_omegadot, SRC/thermo.f90:105-134),
+ * which reaction_macks stores per cell (SRC/source.f90:70-73) for output.
+ * HRR_dot is -sum_k W_k h_f,k w_k [W/m^3] with the molar production rates
+ * w_k at the state the source step left (rho, Y after adjust_sum, the
+ * integration's final T). The library evaluates it when it is first asked
+ * for, or before a later fluid step changes that state: in the reference's
+ * own order (output right after the source step) it costs nothing on the
+ * steps that are not written. Zeros before any source step and when the
+ * chemistry is frozen. */
+int edyn_download_source(void* ctx, double* hrr, double* hrr_dot);
+
+/* FP64 chemistry right-hand side d(Y_1..Y_nspe, T)/dt of n constant-volume
+ * reactors (rows of nspe + 1 values, device pointers; rho in kg/m^3) with
+ * the species and reactions the tube's chemistry integrates (edyn_chem_set):
+ * when that is a subset, the species outside it must be zero in yiT and get
+ * zero rates. The rates are CKWYR's (GRI/cklib.f:9107, called through
+ * SRC/thermo.f90); the temperature row is the constant-volume energy
+ * balance. Synchronous. No counterpart in the reference beyond those
+ * rates. */
+int edyn_chem_rhs_tube(void* ctx, int n, const double* rho_d, const double* yiT_d, double* f_d);
+
+/* Caps the implicit integrator at max_steps steps (accepted + rejected) per
+ * cell and call; a cell that reaches the cap fails and the call returns
+ * EDYN_E_CHEM. 0 restores the default (4000). No counterpart in the
+ * reference, whose missing integrator (SRC/odes.f90) has no documented
+ * limit. */
+int edyn_set_chem_max_steps(void* ctx, int max_steps);
+
+/* Attaches the chemistry surrogate that a context created with
+ * EDYN_IF_CHEM_MODE = 1 puts in front of the implicit integrator in every
+ * source step (the macks call of SRC/source.f90:58, for each tube cell).
+ * No counterpart in the reference, which integrates every cell.
+ *
+ * A source step then: evaluates f(y0) and the integrator's inert-cell test
+ * for every cell (inert cells take their explicit step as in mode 0); for
+ * the others forms the network's candidate y0 + dt f0 + correction (an MLP
+ * 64 -> 3 x 256 GELU -> 64 on the tensor cores, BF16 weights, FP32
+ * accumulation; see include/edyn_surrogate.h) and the explicit increment
+ * y0 + dt f0; accepts per cell the first candidate whose FP64 trapezoidal
+ * residual |y1 - y0 - dt (f(y0) + f(y1))/2| stays within atol + rtol
+ * max(|y0|, |y1|) in every component (no atol on T) and whose element
+ * totals stay within etol; integrates the rest with the implicit
+ * integrator. w0..w3: the layers' BF16 weights pre-tiled by edyn_mlp_tile
+ * (rows 256, 256, 256, 64; BR = edyn_mlp_tile_rows(rows)); b0..b3 FP32
+ * biases; norm: 4 x 64 FP32 (input mean, input 1/std, output mean, output
+ * std). All device pointers, owned by the caller, kept alive and unchanged
+ * while the context steps. w0 = NULL attaches the method without the
+ * network (the explicit increment, gated, then the integrator). The first
+ * call allocates the path's work buffers (sized for every cell). */
+int edyn_set_surrogate(void* ctx, const void* w0, const void* w1, const void* w2, const void* w3, const float* b0,
+                       const float* b1, const float* b2, const float* b3, const float* norm, double rtol, double atol,
+                       double etol);
+
+/* Counters of the last surrogate source step, 7 values: cells not inert
+ * (handed to the surrogate), accepted on the network's candidate, accepted
+ * on the explicit increment, integrated by the fallback, right-hand sides of
+ * the screen launch, of the gate, of the fallback integration. No
+ * counterpart in the reference. */
+int edyn_surrogate_stats(void* ctx, double* stats);
 
 /* Batched reactor call: the macks(dt, nspe+1, yiT, rho) contract of
  * SRC/source.f90:58 for n independent cells in one persistent launch.

@@ -61,6 +61,15 @@ int edyn_mlp_tile(const void* in, int R, int K, int BR, void* out, void* stream)
  * last call (and clears that record). */
 int edyn_mlp_status(void* stream);
 
+/* Sets the limit [ns] of the GEMM waits that gate each next step (operand
+ * copies landed, a staging buffer free again); the default is 2 s. A wait
+ * that runs out stops its GEMM: the kernel still waits, with the full 2 s
+ * bound, for the copies and products it issued, frees its TMEM and returns,
+ * and edyn_mlp_status then reports EDYN_E_SURR. 0 makes every gating wait
+ * give up at once, so a test can drive that path without a stuck barrier.
+ * Applies to later launches on the current device. */
+int edyn_mlp_set_wait_limit(unsigned long long ns);
+
 /* out[c][r] = in[r][c] (BF16, rows x cols). */
 int edyn_mlp_transpose(const void* in, int rows, int cols, void* out, void* stream);
 

@@ -121,6 +121,8 @@ void or_tube_destroy(or_tube* t);
 void or_tube_set_interior(or_tube* t, const double* qf, const double* qc);
 void or_tube_get_interior(const or_tube* t, double* qf, double* qc);
 void or_tube_get_all(const or_tube* t, double* qf, double* qc);
+/* HRR and HRR_dot of the last source step (eos_obj%HRR, %HRR_dot), n values each. */
+void or_tube_get_source(const or_tube* t, double* hrr, double* hrr_dot);
 void or_update_boundary(or_tube* t);
 void or_ghost_qf(or_tube* t);
 double or_calc_dt(or_tube* t, double cfl);

@@ -538,6 +538,13 @@ static void rk4(or_tube* t, double dt) {
   all_qc_to_qf(t);
 }
 
+void or_tube_get_source(const or_tube* t, double* hrr, double* hrr_dot) {
+  for (int i = 0; i < t->n; ++i) {
+    if (hrr) hrr[i] = t->hrr[i];
+    if (hrr_dot) hrr_dot[i] = t->hrr_dot[i];
+  }
+}
+
 /* solve_fluid, SRC/update.f90:62-97 */
 void or_solve_fluid(or_tube* t, double dt) {
   if (t->select_time == 0) explicit_euler(t, dt);
@@ -555,7 +562,8 @@ void or_solve_source(or_tube* t, double dt) {
   const or_mech* m = t->m;
   const int ns = t->nspe;
   long rhs_sum = 0, step_sum = 0;
-#pragma omp parallel for schedule(dynamic, 4) reduction(+ : rhs_sum, step_sum)
+/* chunks of one cell: the costly cells of a reaction front are neighbours */
+#pragma omp parallel for schedule(dynamic, 1) reduction(+ : rhs_sum, step_sum)
   for (int i = 0; i < t->n; ++i) {
     double* q = QF(t, i);
     double y0[OR_MAXSP], y[OR_MAXSP], yit[OR_MAXSP + 1];

@@ -11,6 +11,8 @@ sys.path.insert(0, str(Path(__file__).resolve().parent))
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300) and the built sm_103a library")
+    # a per-test limit where pytest-timeout is installed; a no-op mark otherwise
+    config.addinivalue_line("markers", "timeout(seconds): per-test time limit (pytest-timeout)")
 
 
 @pytest.fixture(scope="session")
@@ -28,6 +30,11 @@ def names():
 
 
 def reference_dir():
-    """The reference checkout, when it is present on this machine."""
-    p = Path(os.environ.get("EDYN_REFERENCE", "/root/reference"))
+    """The reference checkout named by $EDYN_REFERENCE, when that variable is
+    set and the directory exists; None otherwise (the tests that need it
+    skip)."""
+    env = os.environ.get("EDYN_REFERENCE")
+    if not env:
+        return None
+    p = Path(env)
     return p if p.exists() else None

@@ -1,9 +1,8 @@
 """Generates the golden fixtures of tests/golden from the reference checkout.
 
-Run where the reference tree is present (path in $EDYN_REFERENCE, default
-the reference checkout's location on the machine that generated them):
+Run where the reference tree is present, with its path in $EDYN_REFERENCE:
 
-    python tests/golden/make_golden.py
+    EDYN_REFERENCE=<reference checkout> python tests/golden/make_golden.py
 
 1. gri30_mech_golden.json -- GRI-Mech 3.0 as read by an independent,
    pure-Python CHEMKIN-II reader written here (not the library's C++
@@ -28,7 +27,7 @@ from pathlib import Path
 import numpy as np
 
 HERE = Path(__file__).resolve().parent
-REF = Path(os.environ.get("EDYN_REFERENCE", "/root/reference"))
+REF = Path(os.environ.get("EDYN_REFERENCE", ""))
 MECH = REF / "WORK/Examples/CH4_GRI3.0/SOD/GRI3.0_CH4"
 EQUIL = REF / "WORK/Examples/CH4_GRI3.0/MFR/equilTP_phi1.0_p1.0_T1300.0.txt"
 
@@ -145,8 +144,8 @@ def parse_chem(text: str):
 
 
 def main():
-    if not MECH.exists():
-        sys.exit(f"reference mechanism not found under {REF}")
+    if not os.environ.get("EDYN_REFERENCE") or not MECH.exists():
+        sys.exit("set EDYN_REFERENCE to the reference checkout (its GRI-Mech 3.0 directory was not found)")
     species, reactions = parse_chem((MECH / "chem.inp").read_text())
     therm = parse_therm((MECH / "therm.dat").read_text().splitlines(), set(species))
     efac = f32(4.184) / 8.314510

@@ -35,6 +35,8 @@ class Oracle:
         L.or_tube_destroy.argtypes = [vp]
         L.or_tube_set_interior.argtypes = [vp, _D, _D]
         L.or_tube_get_interior.argtypes = [vp, _D, _D]
+        L.or_tube_get_source.argtypes = [vp, _D, _D]
+        L.or_ckcdyr.argtypes = [vp, d, d, _D, _D, _D]
         L.or_calc_dt.restype = d
         L.or_calc_dt.argtypes = [vp, d]
         L.or_solve_fluid.argtypes = [vp, d]
@@ -48,8 +50,6 @@ class Oracle:
         L.or_reactor_batch.restype = i
         L.or_reactor_batch.argtypes = [vp, i, _D, _D, _D, d, d, i, ctypes.POINTER(ctypes.c_long)]
         L.or_chem_rhs.argtypes = [vp, d, _D, _D]
-        for nm in ("or_ckwyr", "or_ckrop"):
-            pass
         L.or_ckwyr.argtypes = [vp, d, d, _D, _D]
         L.or_ckrop.argtypes = [vp, d, d, _D, _D, _D]
         L.or_cksmh.argtypes = [vp, d, _D]
@@ -87,6 +87,20 @@ class Oracle:
         out = np.zeros(self.kk)
         getattr(self.L, fn)(self.mech, T, _p(out))
         return out
+
+    def chem_rhs(self, rho_cgs, yiT):
+        """d(Y_1..Y_K, T)/dt of a constant-volume adiabatic reactor (the
+        function the FP64 reference integrator advances)."""
+        out = np.zeros(self.kk + 1)
+        self.L.or_chem_rhs(self.mech, rho_cgs, _p(np.ascontiguousarray(yiT, dtype=float)), _p(out))
+        return out
+
+    def cdot_ddot(self, rho_cgs, T, Y):
+        """CKCDYR: molar creation and destruction rates [mol/cm^3/s]."""
+        c = np.zeros(self.kk)
+        d = np.zeros(self.kk)
+        self.L.or_ckcdyr(self.mech, rho_cgs, T, _p(np.ascontiguousarray(Y, dtype=float)), _p(c), _p(d))
+        return c, d
 
     def wdot(self, rho_cgs, T, Y):
         out = np.zeros(self.kk)
@@ -143,6 +157,13 @@ class OracleTube:
         qc = np.zeros((self.n, self.o.nequ))
         self.o.L.or_tube_get_interior(self.h, _p(qf), _p(qc))
         return qf, qc
+
+    def source(self):
+        """(HRR, HRR_dot) of the last source step."""
+        hrr = np.zeros(self.n)
+        hrr_dot = np.zeros(self.n)
+        self.o.L.or_tube_get_source(self.h, _p(hrr), _p(hrr_dot))
+        return hrr, hrr_dot
 
     def step(self, cfl):
         return self.o.L.or_step(self.h, cfl)

@@ -95,6 +95,8 @@ def test_sod_warm_newton_deviation(oracle):
     dict(flag_acu=2, flag_weno=3, select_riemann=2),
     dict(flag_acu=2, flag_weno=4, select_riemann=2),
     dict(flag_acu=1, flag_muscl=2, select_riemann=2, select_time=0),
+    dict(flag_acu=1, flag_muscl=2, select_riemann=2, select_time=2),
+    dict(flag_acu=2, flag_weno=3, select_riemann=2, select_time=2),
 ])
 def test_schemes_short_run(oracle, scheme):
     case = configs.sod(ncell=400)
@@ -131,6 +133,17 @@ def ulp_sensitivity(oracle, case, nsteps):
             ot.step(case.cfl)
         out.append(pressure(ot.get()[0], W))
     return rel(out[1], out[0])
+
+
+def test_rk4_device_loop_matches_oracle(oracle):
+    """RK4 (SRC/timeintegration.f90:222-356, stale interior qf across its
+    stages) through the CUDA-graph device loop, with the outlet boundary."""
+    case = configs.sod(ncell=300)
+    case.flags.update(select_time=2, flag_rbound=1, p_out=101325.0)
+    qf_o, qf_g, p_o, p_g, t_o, t_g = run_pair(oracle, case, 48, use_advance=True)
+    assert t_g == pytest.approx(t_o, rel=1e-12)
+    assert rel(p_g, p_o) < TOL
+    assert rel(qf_g[:, 2], qf_o[:, 2]) < TOL
 
 
 def test_outlet_boundary_short_run(oracle):

@@ -53,7 +53,25 @@ def _detonation():
     return case
 
 
-@pytest.mark.parametrize("make", [configs.sod, _detonation, _sod_euler], ids=["sod_rk3", "detonation_rk3", "sod_euler"])
+def _inlet_outlet():
+    """Air flowing in at the left (lbound_inlet: 300 K, 60 kg/m^2/s) into a
+    pressure step, fixed-pressure outlet at the right: the ghost states that
+    read the inlet data and p_out."""
+    names = configs.species_names()
+    x_air = configs.mole_vector(names, {"O2": 0.21, "N2": 0.79})
+    n, dx = 400, 1e-3
+    xm = (np.arange(n) + 0.5) * dx
+    case = configs.TubeCase("inlet_outlet_air_400", n, dx, np.where(xm < 0.2, 300.0, 350.0),
+                            np.where(xm < 0.2, 1.2 * 101325.0, 101325.0), np.where(xm < 0.2, 50.0, 0.0),
+                            np.tile(x_air, (n, 1)),
+                            dict(select_time=1, select_riemann=2, flag_acu=1, flag_muscl=2, flag_weno=0,
+                                 flag_lbound=1, flag_rbound=1, do_reaction=0, p_out=101325.0, t_in=300.0,
+                                 rho_u_in=60.0, x_in=x_air), cfl=0.5)
+    return case
+
+
+@pytest.mark.parametrize("make", [configs.sod, _detonation, _sod_euler, _inlet_outlet],
+                         ids=["sod_rk3", "detonation_rk3", "sod_euler", "inlet_outlet_rk3"])
 def test_noalloc_matches_solve_fluid(make):
     torch = pytest.importorskip("torch")
     case = make()
@@ -77,6 +95,20 @@ def test_noalloc_matches_solve_fluid(make):
         assert _rel(qf_na, qf_ref) < TOL
     # the step moved the state: the comparison is not between two copies of the input
     assert _rel(qc_na, qc0) > 1e-8
+    tube.close()
+
+
+def test_noalloc_rejects_overlapping_arrays():
+    torch = pytest.importorskip("torch")
+    case = configs.sod(ncell=256)
+    tube = Tube(case.ncell, case.dx)
+    ld = case.ncell + 8
+    buf = torch.zeros((56 * ld + 1000,), dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    rc = edyn.lib().edyn_solve_fluid_noalloc(tube._h, ctypes.c_void_p(buf.data_ptr()),
+                                             ctypes.c_void_p(buf.data_ptr() + 8 * 1000), 1e-9)
+    assert rc == edyn.EDYN_E_ARG
+    assert "overlap" in tube.last_error()
     tube.close()
 
 

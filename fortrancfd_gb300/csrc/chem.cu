@@ -796,10 +796,11 @@ __device__ __forceinline__ R species_pass(const Tabs& t, const Team<TW>& tm, con
   return tm.sum(csum);
 }
 
-// Full right-hand side in precision R. y (shared, R) -> f (shared, R).
-template <class R, int TW>
-__device__ void rhs(const Tabs& t, const Team<TW>& tm, WarpWork& w, const R* y, R rho, R* f, R* C, R* m, R* mi,
-                    R* uR, R* cvm, R* rop, R* part) {
+// Full right-hand side in precision R. y (shared, R) -> f (shared, R). Wk is
+// the team's workspace (only its species exponent slots en are used here).
+template <class R, int TW, class Wk>
+__device__ void rhs(const Tabs& t, const Team<TW>& tm, Wk& w, const R* y, R rho, R* f, R* C, R* m, R* mi, R* uR,
+                    R* cvm, R* rop, R* part) {
   const RTabs<R>& x = t.r<R>();
   const int ns = t.ns;
   const R T = y[ns];
@@ -1886,9 +1887,9 @@ __global__ void __launch_bounds__(MAXW * 32, 1)
   }
 }
 
-template <int TW>
-__device__ void finish_cell(const Tabs& t, const Team<TW>& tm, WarpWork& w, const ChemLaunch& L, unsigned cell,
-                            double dt, double& speed_max);
+template <int TW, class Wk>
+__device__ void finish_cell(const Tabs& t, const Team<TW>& tm, Wk& w, const ChemLaunch& L, unsigned cell, double dt,
+                            double& speed_max);
 
 // One tube cell: reaction_macks (SRC/source.f90:17-84) followed by the
 // post-step QcToqf (SRC/main.f90:157-161). Returns the right-hand sides the
@@ -1952,7 +1953,7 @@ __device__ int tube_cell(const Tabs& t, const Team<TW>& tm, WarpWork& w, const C
     }
     return st.rhs;
   }
-  finish_cell<TW>(t, tm, w, L, cell, dt, speed_max);
+  finish_cell<TW, WarpWork>(t, tm, w, L, cell, dt, speed_max);
   return st.rhs;
 }
 
@@ -1960,9 +1961,9 @@ __device__ int tube_cell(const Tabs& t, const Team<TW>& tm, WarpWork& w, const C
 // [Y, T] in w.y0 (the qf rows still hold the cell's Y before the step):
 // adjust_sum, the heat release rate, qfToQc, then the post-step QcToqf of
 // SRC/main.f90:157-161 and the cell's signal speed for the next time step.
-template <int TW>
-__device__ void finish_cell(const Tabs& t, const Team<TW>& tm, WarpWork& w, const ChemLaunch& L, unsigned cell,
-                            double dt, double& speed_max) {
+template <int TW, class Wk>
+__device__ void finish_cell(const Tabs& t, const Team<TW>& tm, Wk& w, const ChemLaunch& L, unsigned cell, double dt,
+                            double& speed_max) {
   const int tid = tm.tid;
   const int ns = t.ns;
   const size_t ld = (size_t)L.ld;
@@ -2183,11 +2184,14 @@ __global__ void __launch_bounds__(MAXW * 32, 1)
   const unsigned nteam =
       (nwarps >= TEAM / 32 && !L.screen) ? min(min(s_hot[0], (unsigned)HOT_MAX), gridDim.x) : 0u;
   if (blockIdx.x < nteam) {
-    if (warp < TEAM / 32) {
+    const unsigned cell = s_hot[1 + blockIdx.x];
+    // list mode: the screening pass finished the cell if it marked it
+    // inert (cost 1); the team works only on a cell it listed (cost -1)
+    const bool work = !L.list || L.cost[cell] == -1;
+    if (warp < TEAM / 32 && work) {
       // team scratch: the second work slot, unused while the team runs
       double* spare = reinterpret_cast<double*>(&ww[1]);
       const Team<TEAM> tm{(int)threadIdx.x, 1, spare, spare + 256, spare + 768, ww[2].J};
-      const unsigned cell = s_hot[1 + blockIdx.x];
       const int c = tube_cell<TEAM>(t, tm, ww[0], L, cell, dt, speed_max, cnt);
       if (threadIdx.x == 0 && L.cost) L.cost[cell] = c;
     }
@@ -2195,11 +2199,14 @@ __global__ void __launch_bounds__(MAXW * 32, 1)
   }
   const Team<32> tw{lane, 0, nullptr, nullptr, nullptr, nullptr};
   WarpWork& w = ww[warp];
+  // every cell of the tube, or (list mode) the cells the screening pass listed
+  const unsigned nwork = L.list ? *L.list_count : (unsigned)L.n;
   for (int guard = 0; guard < (1 << 30); ++guard) {
-    unsigned cell = 0;
-    if (lane == 0) cell = atomicAdd(next, 1u);
-    cell = __shfl_sync(0xffffffffu, cell, 0);
-    if (cell >= (unsigned)L.n) break;
+    unsigned item = 0;
+    if (lane == 0) item = atomicAdd(next, 1u);
+    item = __shfl_sync(0xffffffffu, item, 0);
+    if (item >= nwork) break;
+    const unsigned cell = L.list ? (unsigned)L.list[item] : item;
     // cells taken by a team in this launch
     bool taken = false;
     for (unsigned j = lane; j < nteam; j += 32) taken |= (s_hot[1 + j] == cell);
@@ -2224,7 +2231,7 @@ __global__ void __launch_bounds__(MAXW * 32, 1)
       *L.time = *L.time + dt;
       *L.nsteps = *L.nsteps + 1;
     }
-    if (L.cost && L.hot && !L.screen)
+    if (L.cost && L.hot && !L.screen && !L.list)
       select_hot(L.cost, L.n, L.hot, reinterpret_cast<unsigned*>(ww), (int)(nwarps * sizeof(WarpWork) / 4));
   }
 }
@@ -2250,10 +2257,201 @@ __global__ void __launch_bounds__(MAXW * 32, 1)
     for (int k = lane; k < ns; k += 32) w.y0[k] = y[t.smap[k]];
     if (lane == 0) w.y0[ns] = y[nrow - 1];
     __syncwarp();
-    finish_cell<32>(t, tm, w, L, (unsigned)L.pk_idx[j], L.pk_dt[j], speed_max);
+    finish_cell<32, WarpWork>(t, tm, w, L, (unsigned)L.pk_idx[j], L.pk_dt[j], speed_max);
   }
   if (L.cvel_out && lane == 0 && speed_max > 0.0)
     atomicMax(L.cvel_out, (unsigned long long)__double_as_longlong(speed_max));
+}
+
+// Per-warp workspace of the screening pass: one FP64 right-hand side and the
+// cell's tail, no Jacobian or stage storage (7 KB against 24 KB), so a CTA
+// holds 16 warps next to the tables and each SM sub-partition has four warps
+// to hide the FP64 unit's latency.
+struct alignas(16) ScreenWork {
+  double y0[NV], fy[NV];
+  double C[NV], m[NV], mi[NV], uR[NV], cvm[NV];
+  double part[100];
+  double rop[352];
+  int en[NV];
+};
+constexpr int SCREEN_WARPS = 16;
+
+// Screening pass of a tube's source step. Every cell: y0 = adjust_sum(Y),
+// f(y0) in FP64 and the integrator's inert-cell test (the first step of
+// integrate()); an inert cell takes its explicit step and finishes here
+// (cost 1). Any other cell is either listed (cost -1) for k_tube_chem in
+// list mode, which integrates it from the same y0, or -- on the surrogate
+// path (L.pk_count set) -- packed with y0 and f(y0) for the network and its
+// gate. Cells are dealt in a fixed grid-stride order (their costs are
+// alike); counters are summed per warp.
+__global__ void __launch_bounds__(SCREEN_WARPS * 32, 1)
+    k_tube_screen(const char* g_tab, int tab_bytes, ChemLaunch L, ChemCounters* cnt) {
+  extern __shared__ __align__(16) char smem[];
+  __shared__ int s_last;
+  if (L.step_active && *L.step_active == 0) return;
+  const double dt = L.dt_dev ? *L.dt_dev : L.dt;
+  stage_tables(smem, g_tab, tab_bytes);
+  const Tabs t = bind_tabs(smem);
+  ScreenWork& w = reinterpret_cast<ScreenWork*>(smem + ((tab_bytes + 255) / 256) * 256)[threadIdx.x >> 5];
+  const int lane = threadIdx.x & 31;
+  const Team<32> tm{lane, 0, nullptr, nullptr, nullptr, nullptr};
+  const int ns = t.ns, n = ns + 1;
+  const size_t ld = (size_t)L.ld;
+  const float nn = (float)t.h->nnorm;
+  const int nw = blockDim.x >> 5;
+  double speed_max = 0.0;
+  unsigned long long done = 0, listed = 0;
+  for (unsigned cell = blockIdx.x * nw + (threadIdx.x >> 5); cell < (unsigned)L.n; cell += gridDim.x * nw) {
+    const double* q = L.qf + cell + GHOST;
+    const double rho = q[0];
+    double s = 0.0;
+    for (int k = lane; k < ns; k += 32) {
+      const double yp = clip0_d(q[(3 + t.smap[k]) * ld]);
+      w.y0[k] = yp;
+      s += yp;
+    }
+    s = warp_sum(s);
+    const double inv_s = 1.0 / s;
+    for (int k = lane; k < ns; k += 32) w.y0[k] *= inv_s;
+    if (lane == 0) w.y0[ns] = q[2 * ld];
+    __syncwarp();
+    rhs<double, 32>(t, tm, w, w.y0, rho * 1e-3, w.fy, w.C, w.m, w.mi, w.uR, w.cvm, w.rop, w.part);
+    float ss = 0.f;
+    for (int i = lane; i < n; i += 32) {
+      const float z = (float)(dt * w.fy[i] / (L.atol + L.rtol * fabs(w.y0[i])));
+      ss = fmaf(z, z, ss);
+    }
+    const float nrm = sqrtf(warp_sum(ss) / nn);
+    if (nrm <= 1e-3f) {
+      for (int i = lane; i < n; i += 32) w.y0[i] = fma(dt, w.fy[i], w.y0[i]);
+      __syncwarp();
+      finish_cell<32, ScreenWork>(t, tm, w, L, cell, dt, speed_max);
+      if (lane == 0) {
+        if (L.cost) L.cost[cell] = 1;
+        if (L.hlast) L.hlast[cell] = dt;
+      }
+      ++done;
+    } else if (L.pk_count) {
+      // surrogate path: y0 and f(y0) to the next packed row (full
+      // mechanism layout), as tube_cell's screen mode does
+      unsigned j = 0;
+      if (lane == 0) j = atomicAdd(L.pk_count, 1u);
+      j = __shfl_sync(0xffffffffu, j, 0);
+      const int nrow = t.h->nnorm;
+      double* y0p = L.pk_y0 + (size_t)j * nrow;
+      double* f0p = L.pk_f0 + (size_t)j * nrow;
+      if (ns + 1 < nrow)
+        for (int i = lane; i < nrow; i += 32) y0p[i] = f0p[i] = 0.0;
+      __syncwarp();
+      for (int k = lane; k < ns; k += 32) {
+        y0p[t.smap[k]] = w.y0[k];
+        f0p[t.smap[k]] = w.fy[k];
+      }
+      if (lane == 0) {
+        y0p[nrow - 1] = w.y0[ns];
+        f0p[nrow - 1] = w.fy[ns];
+        L.pk_idx[j] = (int)cell;
+        L.pk_rho[j] = rho;
+        L.pk_dt[j] = dt;
+        if (L.cost) L.cost[cell] = 1;
+      }
+      ++listed;
+    } else {
+      if (lane == 0) {
+        L.list[atomicAdd(L.list_count, 1u)] = (int)cell;
+        if (L.cost) L.cost[cell] = -1;
+      }
+      ++listed;
+    }
+    __syncwarp();
+  }
+  if (lane == 0) {
+    if (done) {
+      atomicAdd(&cnt->rhs, done);
+      atomicAdd(&cnt->steps, done);
+      atomicAdd(&cnt->cells, done);
+    }
+    if (listed) atomicAdd(&cnt->rhs, listed);
+    if (L.cvel_out && speed_max > 0.0)
+      atomicMax(L.cvel_out, (unsigned long long)__double_as_longlong(speed_max));
+  }
+  // the surrogate path's screen is its step's last pass over every cell: its
+  // last CTA advances the device clock (a listed launch leaves that to the
+  // integrator pass that follows)
+  if (L.pk_count && L.time) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      __threadfence();
+      s_last = atomicAdd(L.pk_count + 3, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (s_last && threadIdx.x == 0) {
+      __threadfence();
+      *L.time = *L.time + dt;
+      *L.nsteps = *L.nsteps + 1;
+    }
+  }
+}
+
+// Hot-cell selection over the whole tube in parallel (the selection rule of
+// select_hot): class of each cell = floor(log2) of the largest cost in
+// [i-2, i+2] when at least HOT_MIN_RHS, else 0; histogram of the classes.
+__global__ void k_hot_classes(const int* cost, int n, unsigned char* cls, unsigned* hist) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int m = 0;
+  for (int j = max(0, i - 2); j <= min(n - 1, i + 2); ++j) m = max(m, cost[j]);
+  const int c = m >= HOT_MIN_RHS ? 31 - __clz(m) : 0;
+  cls[i] = (unsigned char)c;
+  if (c) atomicAdd(&hist[c], 1u);
+}
+
+// One CTA: the smallest class threshold whose cells fit in HOT_MAX (the top
+// class capped in cell order if it alone overflows), then the cells at or
+// above it in cell order, by a block-wide ballot scan that stops at HOT_MAX.
+__global__ void __launch_bounds__(1024) k_hot_pick(const unsigned char* cls, int n, const unsigned* hist,
+                                                   unsigned* hot) {
+  __shared__ int s_B;
+  __shared__ unsigned warp_tot[32];
+  __shared__ unsigned carry;
+  if (threadIdx.x == 0) {
+    int B = 32;
+    unsigned cum = 0;
+    for (int b = 30; b >= 0 && (1 << b) >= HOT_MIN_RHS; --b) {
+      if (hist[b] == 0) continue;
+      if (cum + hist[b] > (unsigned)HOT_MAX) {
+        if (B == 32) B = b;
+        break;
+      }
+      cum += hist[b];
+      B = b;
+    }
+    s_B = B;
+    carry = 0;
+  }
+  __syncthreads();
+  const int B = s_B;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int c0 = 0; c0 < n && B < 32; c0 += blockDim.x) {
+    const int i = c0 + threadIdx.x;
+    const bool pick = i < n && cls[i] >= B;
+    const unsigned bal = __ballot_sync(0xffffffffu, pick);
+    if (lane == 0) warp_tot[warp] = __popc(bal);
+    __syncthreads();
+    unsigned off = carry;
+    for (int w2 = 0; w2 < warp; ++w2) off += warp_tot[w2];
+    off += __popc(bal & ((1u << lane) - 1u));
+    if (pick && off < (unsigned)HOT_MAX) hot[1 + off] = (unsigned)i;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      unsigned tot = 0;
+      for (int w2 = 0; w2 < (int)(blockDim.x >> 5); ++w2) tot += warp_tot[w2];
+      carry += tot;
+    }
+    __syncthreads();
+    if (carry >= (unsigned)HOT_MAX) break;
+  }
+  if (threadIdx.x == 0) hot[0] = B < 32 ? min(carry, (unsigned)HOT_MAX) : 0u;
 }
 
 // ---------------------------------------------------------------------------
@@ -2671,6 +2869,22 @@ int chem_init(ChemState& s, const edyn_mech& m, const ThermoTable& tb, cudaStrea
   int per_sm = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_reactors, s.warps * 32, s.smem);
   s.ctas = nsm * std::max(1, per_sm);
+  // the screening pass: as many light warps as fit beside the tables
+  {
+    cudaFuncAttributes fs;
+    e = cudaFuncGetAttributes(&fs, k_tube_screen);
+    if (e != cudaSuccess) return (int)e;
+    const long room_s = (long)maxs - (long)((tot + 255) / 256 * 256) - (long)fs.sharedSizeBytes;
+    s.screen_warps = (int)std::min<long>(SCREEN_WARPS, room_s / (long)sizeof(ScreenWork));
+    if (s.screen_warps < 1) return (int)cudaErrorInvalidConfiguration;
+    s.screen_smem = (tot + 255) / 256 * 256 + sizeof(ScreenWork) * (size_t)s.screen_warps;
+    const int want_s = std::max(fs.maxDynamicSharedSizeBytes, (int)s.screen_smem);
+    e = cudaFuncSetAttribute(k_tube_screen, cudaFuncAttributeMaxDynamicSharedMemorySize, want_s);
+    if (e != cudaSuccess) return (int)e;
+    int per_sm_s = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_s, k_tube_screen, s.screen_warps * 32, s.screen_smem);
+    s.screen_ctas = nsm * std::max(1, per_sm_s);
+  }
   return 0;
 }
 
@@ -2706,6 +2920,45 @@ cudaError_t chem_finish_packed(ChemState& s, const ChemLaunch& L, int m, const d
   const int grid = std::min(s.ctas, (m + s.warps - 1) / s.warps);
   k_tube_finish<<<std::max(1, grid), s.warps * 32, s.smem, st>>>((const char*)s.d_tables, (int)s.table_bytes, L,
                                                                pk_y1);
+  return cudaGetLastError();
+}
+
+cudaError_t chem_launch_tube_listed(ChemState& s, const ChemLaunch& L0, int* list, unsigned* list_count,
+                                    unsigned char* cls, unsigned* hist, cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(s.d_next, 0, 2 * sizeof(unsigned), st);
+  if (e != cudaSuccess) return e;
+  e = cudaMemsetAsync(s.d_count, 0, sizeof(ChemCounters), st);
+  if (e != cudaSuccess) return e;
+  e = cudaMemsetAsync(list_count, 0, sizeof(unsigned), st);
+  if (e != cudaSuccess) return e;
+  ChemLaunch L = L0;
+  L.list = list;
+  L.list_count = list_count;
+  const int sgrid = std::min(s.screen_ctas, (L.n + s.screen_warps - 1) / s.screen_warps);
+  k_tube_screen<<<std::max(1, sgrid), s.screen_warps * 32, s.screen_smem, st>>>((const char*)s.d_tables,
+                                                                              (int)s.table_bytes, L, s.d_count);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  k_tube_chem<<<s.ctas, s.warps * 32, s.smem, st>>>((const char*)s.d_tables, (int)s.table_bytes, L, s.d_next,
+                                                    s.d_count);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  if (L.cost && L.hot) {
+    e = cudaMemsetAsync(hist, 0, 33 * sizeof(unsigned), st);
+    if (e != cudaSuccess) return e;
+    k_hot_classes<<<(L.n + 255) / 256, 256, 0, st>>>(L.cost, L.n, cls, hist);
+    k_hot_pick<<<1, 1024, 0, st>>>(cls, L.n, hist, L.hot);
+    e = cudaGetLastError();
+  }
+  return e;
+}
+
+cudaError_t chem_launch_screen_packed(ChemState& s, const ChemLaunch& L, cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(s.d_count, 0, sizeof(ChemCounters), st);
+  if (e != cudaSuccess) return e;
+  const int sgrid = std::min(s.screen_ctas, (L.n + s.screen_warps - 1) / s.screen_warps);
+  k_tube_screen<<<std::max(1, sgrid), s.screen_warps * 32, s.screen_smem, st>>>((const char*)s.d_tables,
+                                                                              (int)s.table_bytes, L, s.d_count);
   return cudaGetLastError();
 }
 

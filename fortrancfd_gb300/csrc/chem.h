@@ -24,6 +24,8 @@ struct ChemState {
   ChemCounters* d_count = nullptr;
   int ctas = 0, warps = 0;
   size_t smem = 0;
+  int screen_ctas = 0, screen_warps = 0;  // the light screening pass
+  size_t screen_smem = 0;
 };
 
 struct ChemLaunch {
@@ -60,6 +62,10 @@ struct ChemLaunch {
   double* pk_dt;        // dt [s]
   double* pk_y0;        // adjusted [Y, T] before the step
   double* pk_f0;        // f(y0)
+  // list mode (tube): k_tube_chem integrates only the cells the screening
+  // pass listed (list[0..*list_count)); the pass marks them cost -1
+  int* list;
+  unsigned* list_count;
 };
 
 // smap: tube row of each species of m (3 + smap[k]) when m is a subset of the
@@ -69,6 +75,17 @@ int chem_init(ChemState& s, const edyn_mech& m, const ThermoTable& tb, cudaStrea
               int nnorm = 0);
 cudaError_t chem_launch_tube(ChemState& s, const ChemLaunch& L, cudaStream_t st);
 cudaError_t chem_launch_batch(ChemState& s, const ChemLaunch& L, cudaStream_t st);
+// The tube's source step in two passes: a light screening pass over every
+// cell (FP64 f(y0), inert cells finished at once, the others listed), then
+// the integrator kernel over the listed cells only, then the hot-cell
+// selection of the next launch in parallel (cls: n bytes; hist: 33 words).
+// The same results as chem_launch_tube, bit for bit.
+cudaError_t chem_launch_tube_listed(ChemState& s, const ChemLaunch& L, int* list, unsigned* list_count,
+                                    unsigned char* cls, unsigned* hist, cudaStream_t st);
+// The surrogate path's screen: the light screening pass with packed rows
+// (L.pk_*, L.pk_count[0..3] cleared by the caller; [3] counts finished
+// CTAs) for the cells that are not inert.
+cudaError_t chem_launch_screen_packed(ChemState& s, const ChemLaunch& L, cudaStream_t st);
 // FP64 right-hand side d(Y, T)/dt of n reactors (rho SI, yiT rows of ns + 1).
 cudaError_t chem_rhs_batch(ChemState& s, int n, const double* rho, const double* yiT, double* f, cudaStream_t st);
 cudaError_t chem_read_counters(ChemState& s, ChemCounters* out, cudaStream_t st);

@@ -101,6 +101,13 @@ struct Ctx {
   int* d_cost = nullptr;      // right-hand sides per cell in the last chemistry launch
   unsigned* d_hot = nullptr;  // cells that get a four-warp team in the next one
   double* d_hlast = nullptr;  // step size each cell's integrator proposed last
+  // the two-pass source step (screen + listed integration): listed cells,
+  // their count, per-cell hot classes and the class histogram
+  int* d_list = nullptr;
+  unsigned* d_list_count = nullptr;
+  unsigned char* d_cls = nullptr;
+  unsigned* d_hist = nullptr;
+  bool listed = false;       // the two-pass form is in use
   cudaGraphExec_t graph = nullptr;
   int graph_steps = 0;
   double graph_cfl = -1, graph_tend = -1;
@@ -276,7 +283,9 @@ int source_step(Ctx* c, double dt, bool dev) {
   L.hlast = c->d_hlast;
   L.tchem = c->tchem;
   L.max_steps = c->chem_max_steps;
-  cudaError_t e = chem_launch_tube(c->use_sub ? c->chem_sub : c->chem, L, c->stream);
+  ChemState& cs = c->use_sub ? c->chem_sub : c->chem;
+  cudaError_t e = c->listed ? chem_launch_tube_listed(cs, L, c->d_list, c->d_list_count, c->d_cls, c->d_hist, c->stream)
+                            : chem_launch_tube(cs, L, c->stream);
   if (e != cudaSuccess) return fail(c, EDYN_E_CUDA, "chemistry launch: %s", cudaGetErrorString(e));
   return EDYN_OK;
 }
@@ -332,7 +341,7 @@ int surrogate_source_step(Ctx* c, double dt, bool dev) {
   L.pk_dt = z.pk_dt;
   L.pk_y0 = z.pk_y0;
   L.pk_f0 = z.pk_f0;
-  cudaError_t e = chem_launch_tube(cs, L, st);
+  cudaError_t e = chem_launch_screen_packed(cs, L, st);
   if (e != cudaSuccess) return fail(c, EDYN_E_CUDA, "chemistry screen launch: %s", cudaGetErrorString(e));
   unsigned cnt[4] = {0, 0, 0, 0};
   CK(cudaMemcpyAsync(cnt, z.d_count, sizeof(cnt), cudaMemcpyDeviceToHost, st));
@@ -702,6 +711,15 @@ int edyn_init(const char* chem_dir, int nspe, int nequ, int ncell, int lvir, con
   CK(cudaMemsetAsync(c->d_cost, 0, (size_t)ncell * sizeof(int), c->stream));
   CK(cudaMemsetAsync(c->d_hot, 0, (HOT_MAX + 1) * sizeof(unsigned), c->stream));
   CK(cudaMalloc(&c->d_hlast, (size_t)ncell * sizeof(double)));
+  CK(cudaMalloc(&c->d_list, (size_t)ncell * sizeof(int)));
+  CK(cudaMalloc(&c->d_list_count, sizeof(unsigned)));
+  CK(cudaMalloc(&c->d_cls, (size_t)ncell));
+  CK(cudaMalloc(&c->d_hist, 64 * sizeof(unsigned)));
+  // Long tubes are throughput-bound on the inert cells' one right-hand side
+  // each, which the light screening pass runs at four warps per SM
+  // sub-partition; short ones are bound by their costliest cell, which a
+  // second launch would only delay.
+  c->listed = ncell >= 50000;
   CK(cudaMalloc(&c->d_present, 64 * sizeof(int)));
   CK(cudaMemsetAsync(c->d_hlast, 0, (size_t)ncell * sizeof(double), c->stream));
   int rc = fluid_upload_tables(c->tb, c->stream);
@@ -1051,6 +1069,15 @@ int edyn_download_source(void* ctx, double* hrr, double* hrr_dot) {
   return EDYN_OK;
 }
 
+int edyn_set_chem_launch(void* ctx, int form) {
+  Ctx* c = (Ctx*)ctx;
+  if (!c || !c->qc) return EDYN_E_ARG;
+  if (form < 0 || form > 2) return fail(c, EDYN_E_ARG, "chemistry launch form %d not in 0..2", form);
+  c->listed = form == 2 || (form == 0 && c->n >= 50000);
+  drop_graph(c);
+  return EDYN_OK;
+}
+
 int edyn_set_chem_max_steps(void* ctx, int max_steps) {
   Ctx* c = (Ctx*)ctx;
   if (!c || !c->qc) return EDYN_E_ARG;
@@ -1222,6 +1249,10 @@ int edyn_finalize(void* ctx) {
   cudaFree(c->d_cost);
   cudaFree(c->d_hot);
   cudaFree(c->d_hlast);
+  cudaFree(c->d_list);
+  cudaFree(c->d_list_count);
+  cudaFree(c->d_cls);
+  cudaFree(c->d_hist);
   if (c->own) cudaStreamDestroy(c->own);
   delete c;
   return EDYN_OK;

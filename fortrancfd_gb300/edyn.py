@@ -67,6 +67,7 @@ def lib() -> ctypes.CDLL:
     L.edyn_download.argtypes = [vp, dp, dp, dp]
     L.edyn_download_source.argtypes = [vp, dp, dp]
     L.edyn_set_chem_max_steps.argtypes = [vp, i]
+    L.edyn_set_chem_launch.argtypes = [vp, i]
     L.edyn_chem_rhs_tube.argtypes = [vp, i, vp, vp, vp]
     L.edyn_set_surrogate.argtypes = [vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, d, d, d]
     L.edyn_surrogate_stats.argtypes = [vp, dp]
@@ -240,6 +241,11 @@ class Tube(_Ctx):
         ns, nr = ctypes.c_int(), ctypes.c_int()
         self._check(lib().edyn_chem_set(self._h, ctypes.byref(ns), ctypes.byref(nr)))
         return ns.value, nr.value
+
+    def set_chem_launch(self, form: int = 0) -> None:
+        """Chemistry launch form: 0 automatic, 1 one pass, 2 screening pass +
+        listed integration (the same results)."""
+        self._check(lib().edyn_set_chem_launch(self._h, int(form)))
 
     def set_stage_tile(self, cells: int = 0) -> None:
         """Cells per fluid stage tile; 0 chooses it from the tube length."""

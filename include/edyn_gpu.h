@@ -173,6 +173,15 @@ int edyn_download_source(void* ctx, double* hrr, double* hrr_dot);
  * rates. */
 int edyn_chem_rhs_tube(void* ctx, int n, const double* rho_d, const double* yiT_d, double* f_d);
 
+/* Form of a tube's chemistry launch: 1 one pass (every cell integrated by
+ * the integrator kernel, the costliest on four-warp teams), 2 two passes (a
+ * light screening pass evaluates f(y0) and the inert-cell test of every cell
+ * at four warps per SM sub-partition and finishes the inert cells; the
+ * integrator kernel then takes only the cells it listed), 0 automatic (two
+ * passes from 50,000 cells). Results do not depend on the form. No
+ * counterpart in the reference (a tuning knob of this implementation). */
+int edyn_set_chem_launch(void* ctx, int form);
+
 /* Caps the implicit integrator at max_steps steps (accepted + rejected) per
  * cell and call; a cell that reaches the cap fails and the call returns
  * EDYN_E_CHEM. 0 restores the default (4000). No counterpart in the

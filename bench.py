@@ -69,8 +69,10 @@ def parse():
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--workload", default="detonation_air_200k",
-                   choices=list(WORKLOADS) + ["reactors"],
-                   help="the tube of the headline metric (default), the 20k CH4/O2 tube, or the reactor batch")
+                   choices=list(WORKLOADS) + ["reactors", "tubes"],
+                   help="the tube of the headline metric (default), the 20k CH4/O2 tube, the reactor batch, or "
+                        "the uneven batch of --ntubes tubes in one context")
+    p.add_argument("--ntubes", type=int, default=256, help="tubes of --workload tubes")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--reactors", type=int, default=1 << 20, help="reactors in the batch of --workload reactors")
     p.add_argument("--prepared", type=int, default=1 << 16,
@@ -195,9 +197,9 @@ def reference_arm(args, rank, world):
     here) on all cores, the same tube, the same steps as the GPU arm."""
     if rank != 0:
         return None
-    if args.workload == "reactors":
-        print(json.dumps({"impl": "reference", "unavailable": "the reactor batch has no reference-arm timing; the "
-                          "oracle's batch is timed as cpu_baseline"}), flush=True)
+    if args.workload in ("reactors", "tubes"):
+        print(json.dumps({"impl": "reference", "unavailable": f"the {args.workload} workload has no reference-arm "
+                          "timing (the default workload carries the comparison)"}), flush=True)
         return None
     case = build_case(args.workload)
     o, t = oracle_tube(case)
@@ -501,11 +503,76 @@ def reactors_arm(args, local):
     print(json.dumps(line), flush=True)
 
 
+def tubes_arm(args, rank, world, local):
+    """The uneven batch: --ntubes CH4/air detonation tubes (cells ~
+    U[2000, 50000], lengths ~ U[0.1, 1] m, phi ~ U[0.7, 1.4], p ~ U[0.5, 5]
+    atm, driver T ~ U[2500, 3500] K; configs.uneven_tubes, seed 0) in one
+    context: one stage launch over every tube's tiles and one chemistry
+    launch over every tube's cells per stage and step, each tube with its
+    own dt, the steps in CUDA graphs. Under torchrun the tubes are split
+    into contiguous cell-balanced ranges, one per rank (no exchange)."""
+    import torch
+
+    from fortrancfd_gb300 import Tubes, configs
+    from fortrancfd_gb300.shard import my_range
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=dev)
+    cases = configs.uneven_tubes(args.ntubes, seed=0)
+    a, b = my_range([c.ncell for c in cases], rank, world)
+    mine = cases[a:b]
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
+    g = Tubes([c.ncell for c in mine], [c.dx for c in mine], p_outs=[c.flags["p_out"] for c in mine],
+              do_reaction=1, strict_newton=0, rtol=1e-5, atol=1e-13)
+    g.set_stream(stream.cuda_stream)
+    g.init_cells(np.concatenate([c.T for c in mine]), np.concatenate([c.p for c in mine]),
+                 np.concatenate([c.u for c in mine]), np.concatenate([c.X for c in mine]))
+    t_sim, n = g.advance(0.4, tend=1e9, time=0.0, max_steps=args.warmup) if args.warmup else (0.0, 0)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize(dev)
+    with ClockSampler(local) as clk:
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        t_sim, n = g.advance(0.4, tend=1e9, time=t_sim, max_steps=args.steps)
+        e1.record(stream)
+        e1.synchronize()
+    assert n == args.steps
+    t_max = max_over_ranks(e0.elapsed_time(e1) / 1e3, world, dev)
+    cells_all = sum(c.ncell for c in cases)
+    chem = g.chem_stats()
+    times, dts = g.times()
+    if rank != 0:
+        return
+    line = {"metric": "cell-steps/s on 1 GB300: uneven tube batch, plain chemistry", "value": cells_all * args.steps / t_max,
+            "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * t_max / args.steps, "higher_is_better": True,
+            "scaling": "strong" if world > 1 else "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"ch4_air_uneven_tubes_{args.ntubes}", "tubes": args.ntubes, "cells": cells_all,
+                       "cells_range": [min(c.ncell for c in cases), max(c.ncell for c in cases)],
+                       "scheme": "WENO5-Z + HLLC + SSP-RK3, CFL 0.4, wall / fixed-p outlet, per-tube dt",
+                       "chemistry": "GRI-Mech 3.0, per-cell stiff integration, rtol 1e-5, atol 1e-13",
+                       "parallelism": f"tubes split over {world} rank(s)",
+                       "l2": "state (4 x 56 rows x cells doubles) larger than L2"},
+            "clocks": clk.summary(), "gpu_launches": ((args.steps + 15) // 16) * 16 * 6,
+            "chem_launch": {"rhs_per_cell": chem["rhs"] / max(1, chem["cells"]), "team_cells": chem["team_cells"]},
+            "tube_dt_range_s": [float(dts.min()), float(dts.max())]}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
     if args.impl == "reference":
         reference_arm(args, rank, world)
+        return
+    if args.workload == "tubes":
+        tubes_arm(args, rank, world, local)
         return
     if args.workload == "reactors":
         if rank == 0:

@@ -194,3 +194,26 @@ def reactor_batch(n: int, seed: int = 0, names=None):
     rho = p * wbar / (8314.51 * T)
     yiT = np.concatenate([Y, T[:, None]], axis=1)
     return rho, dt, np.ascontiguousarray(yiT), phi
+
+
+def uneven_tubes(ntube: int, seed: int = 0, cells=(2000, 50000), length=(0.1, 1.0), names=None):
+    """The uneven batch: ntube independent CH4/air detonation tubes with cell
+    counts ~ U[cells], tube lengths ~ U[length] m, equivalence ratio
+    phi ~ U[0.7, 1.4], initial pressure ~ U[0.5, 5] atm and driver
+    temperature ~ U[2500, 3500] K (seeded); 1 cm driver at 30 atm holding
+    the fresh mixture's TP-equilibrium products; wall left, fixed-pressure
+    outlet (at the tube's initial pressure) right; WENO5-Z + HLLC + SSP-RK3,
+    CFL 0.4. Returns the tubes' TubeCase list (p_out in each case's flags)."""
+    names = names or species_names(GRI30_DIR)
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(ntube):
+        n = int(rng.integers(cells[0], cells[1] + 1))
+        L = float(rng.uniform(*length))
+        phi = float(rng.uniform(0.7, 1.4))
+        p0 = ATM * float(rng.uniform(0.5, 5.0))
+        tdrv = float(rng.uniform(2500.0, 3500.0))
+        case = detonation(names, ncell=n, length=L, phi=phi, T_drv=tdrv, p0=p0, oxidizer="air")
+        case.flags["p_out"] = p0
+        out.append(case)
+    return out

@@ -1862,7 +1862,8 @@ __global__ void __launch_bounds__(MAXW * 32, 1)
 // h_f,k f_k. One warp per cell. The reference evaluates it every step for
 // output only; here it is evaluated when the host downloads it.
 __global__ void __launch_bounds__(MAXW * 32, 1)
-    k_hrr_dot(const char* g_tab, int tab_bytes, int n, int ld, const double* qf, const double* tchem, double* out) {
+    k_hrr_dot(const char* g_tab, int tab_bytes, int n, int ld, const double* qf, const double* tchem, double* out,
+              const int* colmap) {
   extern __shared__ __align__(16) char smem[];
   stage_tables(smem, g_tab, tab_bytes);
   const Tabs t = bind_tabs(smem);
@@ -1872,7 +1873,7 @@ __global__ void __launch_bounds__(MAXW * 32, 1)
   const int ns = t.ns;
   const int nw = blockDim.x >> 5;
   for (int cell = blockIdx.x * nw + (threadIdx.x >> 5); cell < n; cell += gridDim.x * nw) {
-    const double* q = qf + cell + GHOST;
+    const double* q = qf + (colmap ? (size_t)colmap[cell] : (size_t)cell) + GHOST;
     for (int k = lane; k < ns; k += 32) w.y0[k] = q[(3 + t.smap[k]) * (size_t)ld];
     if (lane == 0) w.y0[ns] = tchem[cell];
     __syncwarp();
@@ -1887,6 +1888,18 @@ __global__ void __launch_bounds__(MAXW * 32, 1)
   }
 }
 
+// Packed tubes: a cell's column in the rows (its tube's block offset + its
+// index) and its tube's dt; a single tube: the cell index and the launch's dt.
+__device__ __forceinline__ size_t cell_col(const ChemLaunch& L, unsigned cell) {
+  return L.colmap ? (size_t)L.colmap[cell] : (size_t)cell;
+}
+__device__ __forceinline__ double cell_dt(const ChemLaunch& L, unsigned cell, double dt) {
+  return L.dt_tube ? L.dt_tube[L.tube_of[cell]] : dt;
+}
+__device__ __forceinline__ bool cell_active(const ChemLaunch& L, unsigned cell) {
+  return !L.active_tube || L.active_tube[L.tube_of[cell]] != 0;
+}
+
 template <int TW, class Wk>
 __device__ void finish_cell(const Tabs& t, const Team<TW>& tm, Wk& w, const ChemLaunch& L, unsigned cell, double dt,
                             double& speed_max);
@@ -1896,11 +1909,13 @@ __device__ void finish_cell(const Tabs& t, const Team<TW>& tm, Wk& w, const Chem
 // cell took (its cost, which picks the cells that get a team next time).
 template <int TW>
 __device__ int tube_cell(const Tabs& t, const Team<TW>& tm, WarpWork& w, const ChemLaunch& L, unsigned cell,
-                         double dt, double& speed_max, ChemCounters* cnt) {
+                         double dt_launch, double& speed_max, ChemCounters* cnt) {
   const int tid = tm.tid;
   const int ns = t.ns;
   const size_t ld = (size_t)L.ld;
-  double* q = L.qf + cell + GHOST;
+  if (!cell_active(L, cell)) return 0;
+  const double dt = cell_dt(L, cell, dt_launch);
+  double* q = L.qf + cell_col(L, cell) + GHOST;
   const double rho = q[0];
   // reaction_macks: y_sp = adjust_sum(Y), yiT = [y_sp, T] (SRC/source.f90:47-56);
   // the raw Y stay in the qf rows for the heat release rate.
@@ -1967,8 +1982,8 @@ __device__ void finish_cell(const Tabs& t, const Team<TW>& tm, Wk& w, const Chem
   const int tid = tm.tid;
   const int ns = t.ns;
   const size_t ld = (size_t)L.ld;
-  double* q = L.qf + cell + GHOST;
-  double* Q = L.qc + cell + GHOST;
+  double* q = L.qf + cell_col(L, cell) + GHOST;
+  double* Q = L.qc + cell_col(L, cell) + GHOST;
   const double rho = q[0];
   // the temperature the integration ended with: HRR_dot is evaluated at it
   // (SRC/source.f90:72-73 passes qf(iqtemp) = macks' T)
@@ -2067,7 +2082,7 @@ __device__ void finish_cell(const Tabs& t, const Team<TW>& tm, Wk& w, const Chem
     if (bad) atomicOr(L.err, bad);
   }
   // signal speed of the new state for the next time step
-  if (L.cvel_out) {
+  if (L.cvel_out || L.cvel_tube) {
     double a[6] = {0, 0, 0, 0, 0, 0};
     for (int k = tid; k < ns; k += TW) {
       const int r = (T > t.d.tmid[k]) ? 1 : 0;
@@ -2087,7 +2102,11 @@ __device__ void finish_cell(const Tabs& t, const Team<TW>& tm, Wk& w, const Chem
     cp = fma(cp, T, a[0]);
     const double gamma = cp / (cp - a[5]);
     const double sp = fabs(u) + sqrt(gamma * R_SI * T * a[5]);
-    speed_max = fmax(speed_max, sp);
+    if (L.cvel_tube) {
+      if (tid == 0) atomicMax(L.cvel_tube + L.tube_of[cell], (unsigned long long)__double_as_longlong(sp));
+    } else {
+      speed_max = fmax(speed_max, sp);
+    }
   }
   tm.sync();
 }
@@ -2227,7 +2246,12 @@ __global__ void __launch_bounds__(MAXW * 32, 1)
   __syncthreads();
   if (s_last) {
     __threadfence();
-    if (threadIdx.x == 0 && L.time) {
+    if (L.time_tube) {
+      // packed tubes: every stepping tube's clock by its own dt
+      for (int q = threadIdx.x; q < L.ntube; q += blockDim.x)
+        if (L.active_tube[q]) L.time_tube[q] = L.time_tube[q] + L.dt_tube[q];
+      if (threadIdx.x == 0) *L.nsteps = *L.nsteps + 1;
+    } else if (threadIdx.x == 0 && L.time) {
       *L.time = *L.time + dt;
       *L.nsteps = *L.nsteps + 1;
     }
@@ -2289,7 +2313,7 @@ __global__ void __launch_bounds__(SCREEN_WARPS * 32, 1)
   extern __shared__ __align__(16) char smem[];
   __shared__ int s_last;
   if (L.step_active && *L.step_active == 0) return;
-  const double dt = L.dt_dev ? *L.dt_dev : L.dt;
+  const double dt_launch = L.dt_dev ? *L.dt_dev : L.dt;
   stage_tables(smem, g_tab, tab_bytes);
   const Tabs t = bind_tabs(smem);
   ScreenWork& w = reinterpret_cast<ScreenWork*>(smem + ((tab_bytes + 255) / 256) * 256)[threadIdx.x >> 5];
@@ -2302,7 +2326,9 @@ __global__ void __launch_bounds__(SCREEN_WARPS * 32, 1)
   double speed_max = 0.0;
   unsigned long long done = 0, listed = 0;
   for (unsigned cell = blockIdx.x * nw + (threadIdx.x >> 5); cell < (unsigned)L.n; cell += gridDim.x * nw) {
-    const double* q = L.qf + cell + GHOST;
+    if (!cell_active(L, cell)) continue;
+    const double dt = cell_dt(L, cell, dt_launch);
+    const double* q = L.qf + cell_col(L, cell) + GHOST;
     const double rho = q[0];
     double s = 0.0;
     for (int k = lane; k < ns; k += 32) {
@@ -2387,7 +2413,7 @@ __global__ void __launch_bounds__(SCREEN_WARPS * 32, 1)
     __syncthreads();
     if (s_last && threadIdx.x == 0) {
       __threadfence();
-      *L.time = *L.time + dt;
+      *L.time = *L.time + dt_launch;
       *L.nsteps = *L.nsteps + 1;
     }
   }
@@ -2908,10 +2934,10 @@ cudaError_t chem_rhs_batch(ChemState& s, int n, const double* rho, const double*
 }
 
 cudaError_t chem_hrr_dot(ChemState& s, int n, int ld, const double* qf, const double* tchem, double* out,
-                         cudaStream_t st) {
+                         const int* colmap, cudaStream_t st) {
   const int grid = std::min(s.ctas, (n + s.warps - 1) / s.warps);
   k_hrr_dot<<<std::max(1, grid), s.warps * 32, s.smem, st>>>((const char*)s.d_tables, (int)s.table_bytes, n, ld, qf,
-                                                            tchem, out);
+                                                            tchem, out, colmap);
   return cudaGetLastError();
 }
 

@@ -66,6 +66,16 @@ struct ChemLaunch {
   // pass listed (list[0..*list_count)); the pass marks them cost -1
   int* list;
   unsigned* list_count;
+  // packed tubes (the cells of several tubes side by side in the rows; null
+  // for one tube): column of each cell, its tube, each tube's dt, whether it
+  // steps, its signal-speed maximum and clock
+  const int* colmap;
+  const int* tube_of;
+  const double* dt_tube;
+  const int* active_tube;
+  unsigned long long* cvel_tube;
+  double* time_tube;
+  int ntube;
 };
 
 // smap: tube row of each species of m (3 + smap[k]) when m is a subset of the
@@ -79,7 +89,8 @@ cudaError_t chem_launch_batch(ChemState& s, const ChemLaunch& L, cudaStream_t st
 // cell (FP64 f(y0), inert cells finished at once, the others listed), then
 // the integrator kernel over the listed cells only, then the hot-cell
 // selection of the next launch in parallel (cls: n bytes; hist: 33 words).
-// The same results as chem_launch_tube, bit for bit.
+// The same results as chem_launch_tube up to rounding (a team-listed cell
+// that turns out inert is finished by a single warp here, by its team there).
 cudaError_t chem_launch_tube_listed(ChemState& s, const ChemLaunch& L, int* list, unsigned* list_count,
                                     unsigned char* cls, unsigned* hist, cudaStream_t st);
 // The surrogate path's screen: the light screening pass with packed rows
@@ -95,7 +106,7 @@ cudaError_t chem_finish_packed(ChemState& s, const ChemLaunch& L, int m, const d
 // HRR_dot [W/m^3] of n tube cells from their primitive rows (qf, SoA with ld)
 // and the temperatures their last chemistry step ended with.
 cudaError_t chem_hrr_dot(ChemState& s, int n, int ld, const double* qf, const double* tchem, double* out,
-                         cudaStream_t st);
+                         const int* colmap, cudaStream_t st);
 cudaError_t chem_check_exp(ChemState& s, int n, const double* x_d, unsigned long long* maxulp_d, cudaStream_t st);
 cudaError_t chem_check_log(ChemState& s, int n, const double* x_d, unsigned long long* maxulp_d, cudaStream_t st);
 void chem_free(ChemState& s);

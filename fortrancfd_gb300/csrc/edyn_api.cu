@@ -66,6 +66,31 @@ struct Surr {
   double stats[7] = {};
 };
 
+// Several tubes packed side by side in one context's rows (edyn_init_tubes):
+// tube t's block of n_t + 2 GHOST columns starts at column off[t]; its cells
+// are the packed cells first[t] .. first[t] + n_t - 1.
+struct Packed {
+  int ntube = 0;
+  std::vector<int> n;
+  std::vector<long long> off, first;
+  std::vector<double> dx, p_out;
+  int4* d_tiles = nullptr;
+  int ntiles = 0;
+  int* d_n = nullptr;
+  long long* d_off = nullptr;
+  double *d_dx = nullptr, *d_p_out = nullptr, *d_dt = nullptr, *d_time = nullptr;
+  int* d_active = nullptr;
+  unsigned long long* d_cvel = nullptr;
+  int* colmap = nullptr;   // column of each packed cell
+  int* tube_of = nullptr;  // tube of each packed cell
+};
+
+// A contiguous run of cells in the rows: the whole tube, or one packed tube.
+struct Seg {
+  long long off, first;
+  int n;
+};
+
 struct Ctx {
   edyn_mech mech;
   ThermoTable tb;
@@ -122,8 +147,19 @@ struct Ctx {
   bool use_sub = false;
   int* d_present = nullptr;  // per species: nonzero somewhere in the tube
   Surr surr;
+  Packed pk;
   std::string err;
 };
+
+std::vector<Seg> segs(const Ctx* c) {
+  std::vector<Seg> v;
+  if (c->pk.ntube == 0) {
+    v.push_back({0, 0, c->n});
+  } else {
+    for (int t = 0; t < c->pk.ntube; ++t) v.push_back({c->pk.off[t], c->pk.first[t], c->pk.n[t]});
+  }
+  return v;
+}
 
 int fail(Ctx* c, int code, const char* fmt, ...) {
   char buf[512];
@@ -172,6 +208,10 @@ StageArgs base_args(Ctx* c) {
   a.strict_newton = c->strict;
   a.bc = c->bc;
   a.err = c->d_err;
+  if (c->pk.ntube) {
+    const Packed& k = c->pk;
+    a.tubes = TubeTab{k.d_tiles, k.d_n, k.d_off, k.d_dx, k.d_p_out, k.d_dt, k.d_active, k.d_time, k.ntiles};
+  }
   return a;
 }
 
@@ -213,7 +253,7 @@ int fluid_step(Ctx* c, double dt, bool dev, bool last_is_fluid) {
     for (int s = 0; s < 4; ++s) {
       a.rk4_stage = s;
       const bool last = s == 3;
-      a.cvel_out = (dev && last && last_is_fluid) ? c->d_cvel : nullptr;
+      a.cvel_out = (dev && last && last_is_fluid) ? (c->pk.ntube ? c->pk.d_cvel : c->d_cvel) : nullptr;
       a.time = (dev && last && last_is_fluid) ? c->d_time : nullptr;
       a.nsteps = (dev && last && last_is_fluid) ? c->d_nsteps : nullptr;
       cudaError_t e = launch_stage(a, c->acu, c->lim, c->wflag, c->riemann, c->stream);
@@ -244,7 +284,7 @@ int fluid_step(Ctx* c, double dt, bool dev, bool last_is_fluid) {
       a.h2 = 2.0 / 3.0;
     }
     const bool last = (s == nst - 1);
-    a.cvel_out = (dev && last && last_is_fluid) ? c->d_cvel : nullptr;
+    a.cvel_out = (dev && last && last_is_fluid) ? (c->pk.ntube ? c->pk.d_cvel : c->d_cvel) : nullptr;
     a.time = (dev && last && last_is_fluid) ? c->d_time : nullptr;
     a.nsteps = (dev && last && last_is_fluid) ? c->d_nsteps : nullptr;
     cudaError_t e = launch_stage(a, c->acu, c->lim, c->wflag, c->riemann, c->stream);
@@ -283,6 +323,20 @@ int source_step(Ctx* c, double dt, bool dev) {
   L.hlast = c->d_hlast;
   L.tchem = c->tchem;
   L.max_steps = c->chem_max_steps;
+  if (c->pk.ntube) {
+    const Packed& k = c->pk;
+    L.colmap = k.colmap;
+    L.tube_of = k.tube_of;
+    L.dt_tube = k.d_dt;
+    L.active_tube = k.d_active;
+    L.ntube = k.ntube;
+    L.cvel_out = nullptr;
+    L.time = nullptr;
+    if (dev) {
+      L.cvel_tube = k.d_cvel;
+      L.time_tube = k.d_time;
+    }
+  }
   ChemState& cs = c->use_sub ? c->chem_sub : c->chem;
   cudaError_t e = c->listed ? chem_launch_tube_listed(cs, L, c->d_list, c->d_list_count, c->d_cls, c->d_hist, c->stream)
                             : chem_launch_tube(cs, L, c->stream);
@@ -540,7 +594,8 @@ int select_chem_set(Ctx* c, const std::vector<char>& present) {
 // After the state was set from outside: which species occur, then the tables.
 int refresh_chem_set(Ctx* c) {
   if (!c->do_reaction) return EDYN_OK;
-  CK(launch_species_present(c->qc, c->ld, c->n, c->ns, c->d_present, c->stream));
+  // every column between the outermost ghosts (ghost columns hold zeros)
+  CK(launch_species_present(c->qc, c->ld, c->ld - 2 * GHOST, c->ns, c->d_present, c->stream));
   std::vector<int> fl(c->ns, 1);
   CK(cudaMemcpyAsync(fl.data(), c->d_present, (size_t)c->ns * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
   CK(cudaStreamSynchronize(c->stream));
@@ -570,7 +625,7 @@ void drop_graph(Ctx* c) {
 int eval_hrr_dot(Ctx* c) {
   if (c->hrr_dot_state != 1) return EDYN_OK;
   cudaError_t e = chem_hrr_dot(c->use_sub ? c->chem_sub : c->chem, c->n, c->ld, c->qf[c->cur], c->tchem, c->hrr_dot,
-                               c->stream);
+                               c->pk.colmap, c->stream);
   if (e != cudaSuccess) return fail(c, EDYN_E_CUDA, "HRR_dot launch: %s", cudaGetErrorString(e));
   c->hrr_dot_state = 2;
   return EDYN_OK;
@@ -732,6 +787,108 @@ int edyn_init(const char* chem_dir, int nspe, int nequ, int ncell, int lvir, con
   return EDYN_OK;
 }
 
+namespace {
+// Stage tiles of packed tubes: each tube split into tiles of tc cells with
+// the single-tube rule for its last tile, all tubes' tiles in one table.
+int build_tiles(Ctx* c) {
+  Packed& k = c->pk;
+  std::vector<int4> tl;
+  for (int t = 0; t < k.ntube; ++t) {
+    const int nb = (k.n[t] + c->stage_tc - 1) / c->stage_tc;
+    for (int j = 0; j < nb; ++j) tl.push_back(make_int4(t, j, nb, 0));
+  }
+  if (k.d_tiles) cudaFree(k.d_tiles);
+  k.d_tiles = nullptr;
+  CK(cudaMalloc(&k.d_tiles, tl.size() * sizeof(int4)));
+  CK(cudaMemcpy(k.d_tiles, tl.data(), tl.size() * sizeof(int4), cudaMemcpyHostToDevice));
+  k.ntiles = (int)tl.size();
+  return EDYN_OK;
+}
+}  // namespace
+
+int edyn_init_tubes(const char* chem_dir, int nspe, int nequ, int ntube, const int* ncell, int lvir,
+                    const int* iflags, int n_iflags, const double* rparams, int n_rparams, void** out) {
+  if (!out) return EDYN_E_ARG;
+  *out = nullptr;
+  if (ntube < 1 || !ncell || !rparams || n_rparams < 2 || !iflags || n_iflags < 8) return EDYN_E_ARG;
+  long long ntot = 0, cols = 0;
+  for (int t = 0; t < ntube; ++t) {
+    if (ncell[t] < 16) return EDYN_E_ARG;
+    ntot += ncell[t];
+    cols += ncell[t] + 2 * GHOST;
+  }
+  if (cols > (1ll << 31) - 1) return EDYN_E_ARG;
+  if (n_iflags > EDYN_IF_FLAG_LBOUND && iflags[EDYN_IF_FLAG_LBOUND] != 0) {
+    // the inflow boundary needs per-tube inlet data
+    int rc = edyn_init(chem_dir, nspe, nequ, 16, lvir, iflags, n_iflags, rparams, n_rparams, nullptr, out);
+    if (rc == EDYN_OK) rc = fail((Ctx*)*out, EDYN_E_ARG, "packed tubes take wall or outlet boundaries only");
+    return rc ? rc : EDYN_E_ARG;
+  }
+  if (n_iflags > EDYN_IF_CHEM_MODE && iflags[EDYN_IF_CHEM_MODE] != 0) {
+    int rc = edyn_init(chem_dir, nspe, nequ, 16, lvir, iflags, n_iflags, rparams, n_rparams, nullptr, out);
+    if (rc == EDYN_OK) rc = fail((Ctx*)*out, EDYN_E_ARG, "packed tubes take the plain chemistry (chem_mode 0)");
+    return rc ? rc : EDYN_E_ARG;
+  }
+  // One context whose rows hold every tube's block: its row length is the
+  // sum of the blocks, its cell count the sum of the cells.
+  int rc = edyn_init(chem_dir, nspe, nequ, (int)(cols - 2 * GHOST), lvir, iflags, n_iflags, rparams, n_rparams,
+                     nullptr, out);
+  if (rc) return rc;
+  Ctx* c = (Ctx*)*out;
+  Packed& k = c->pk;
+  k.ntube = ntube;
+  long long off = 0, first = 0;
+  std::vector<int> colmap((size_t)ntot), tube_of((size_t)ntot);
+  for (int t = 0; t < ntube; ++t) {
+    const double* rp = rparams + (size_t)t * n_rparams;
+    k.n.push_back(ncell[t]);
+    k.off.push_back(off);
+    k.first.push_back(first);
+    k.dx.push_back(rp[EDYN_RP_DX]);
+    k.p_out.push_back(n_rparams > EDYN_RP_P_OUT ? rp[EDYN_RP_P_OUT] : 101325.0);
+    if (!(k.dx.back() > 0)) return fail(c, EDYN_E_ARG, "tube %d: dx must be positive", t);
+    for (int i = 0; i < ncell[t]; ++i) {
+      colmap[(size_t)(first + i)] = (int)(off + i);
+      tube_of[(size_t)(first + i)] = t;
+    }
+    off += ncell[t] + 2 * GHOST;
+    first += ncell[t];
+  }
+  c->n = (int)ntot;
+  const size_t nt = (size_t)ntube;
+  CK(cudaMalloc(&k.d_n, nt * sizeof(int)));
+  CK(cudaMalloc(&k.d_off, nt * sizeof(long long)));
+  CK(cudaMalloc(&k.d_dx, nt * sizeof(double)));
+  CK(cudaMalloc(&k.d_p_out, nt * sizeof(double)));
+  CK(cudaMalloc(&k.d_dt, nt * sizeof(double)));
+  CK(cudaMalloc(&k.d_time, nt * sizeof(double)));
+  CK(cudaMalloc(&k.d_active, nt * sizeof(int)));
+  CK(cudaMalloc(&k.d_cvel, nt * sizeof(unsigned long long)));
+  CK(cudaMalloc(&k.colmap, (size_t)ntot * sizeof(int)));
+  CK(cudaMalloc(&k.tube_of, (size_t)ntot * sizeof(int)));
+  CK(cudaMemcpy(k.d_n, k.n.data(), nt * sizeof(int), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(k.d_off, k.off.data(), nt * sizeof(long long), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(k.d_dx, k.dx.data(), nt * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(k.d_p_out, k.p_out.data(), nt * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemset(k.d_dt, 0, nt * sizeof(double)));
+  CK(cudaMemset(k.d_time, 0, nt * sizeof(double)));
+  CK(cudaMemset(k.d_active, 0, nt * sizeof(int)));
+  CK(cudaMemcpy(k.colmap, colmap.data(), colmap.size() * sizeof(int), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(k.tube_of, tube_of.data(), tube_of.size() * sizeof(int), cudaMemcpyHostToDevice));
+  CK(stage_tiling(c->acu, c->lim, c->wflag, c->riemann, c->ns, c->n, &c->stage_tc));
+  c->listed = c->n >= 50000;
+  return build_tiles(c);
+}
+
+int edyn_tube_times(void* ctx, double* time, double* dt) {
+  Ctx* c = (Ctx*)ctx;
+  if (!c || !c->qc) return EDYN_E_ARG;
+  const size_t nt = (size_t)std::max(1, c->pk.ntube);
+  if (time) CK(cudaMemcpy(time, c->pk.ntube ? c->pk.d_time : c->d_time, nt * sizeof(double), cudaMemcpyDeviceToHost));
+  if (dt) CK(cudaMemcpy(dt, c->pk.ntube ? c->pk.d_dt : c->d_dt, nt * sizeof(double), cudaMemcpyDeviceToHost));
+  return EDYN_OK;
+}
+
 int edyn_set_stage_tile(void* ctx, int cells) {
   Ctx* c = (Ctx*)ctx;
   if (!c || !c->qc) return EDYN_E_ARG;
@@ -742,7 +899,7 @@ int edyn_set_stage_tile(void* ctx, int cells) {
   if (cells == 0) CK(stage_tiling(c->acu, c->lim, c->wflag, c->riemann, c->ns, c->n, &tc));
   c->stage_tc = tc;
   drop_graph(c);
-  return EDYN_OK;
+  return c->pk.ntube ? build_tiles(c) : EDYN_OK;
 }
 
 int edyn_stage_tile(void* ctx, int* cells, int* threads) {
@@ -769,18 +926,25 @@ int edyn_upload(void* ctx, const double* qf_aos, const double* qc_aos) {
   int rc = ensure_staging(c, bytes);
   if (rc) return rc;
   CK(cudaMemcpyAsync(c->staging, qc_aos, bytes, cudaMemcpyHostToDevice, c->stream));
-  CK(launch_aos_to_soa(c->staging, c->ne, c->n, c->qc, c->ld, c->stream));
+  for (const Seg& g : segs(c))
+    CK(launch_aos_to_soa(c->staging + g.first * c->ne, c->ne, g.n, c->qc + g.off, c->ld, c->stream));
   if (qf_aos) {
     CK(cudaMemcpyAsync(c->staging, qf_aos, bytes, cudaMemcpyHostToDevice, c->stream));
-    CK(launch_aos_to_soa(c->staging, c->ne, c->n, c->qf[c->cur], c->ld, c->stream));
+    for (const Seg& g : segs(c))
+      CK(launch_aos_to_soa(c->staging + g.first * c->ne, c->ne, g.n, c->qf[c->cur] + g.off, c->ld, c->stream));
   } else {
-    StageArgs a = base_args(c);
-    a.qf_in = nullptr;
-    a.qf_out = c->qf[c->cur];
-    a.strict_newton = 1;
-    CK(launch_qc_to_qf(a, c->stream));
+    for (const Seg& g : segs(c)) {
+      StageArgs a = base_args(c);
+      a.n = g.n;
+      a.qc = c->qc + g.off;
+      a.qf_in = nullptr;
+      a.qf_out = c->qf[c->cur] + g.off;
+      a.strict_newton = 1;
+      CK(launch_qc_to_qf(a, c->stream));
+    }
   }
-  CK(launch_check_state(c->qf[c->cur], c->qc, c->n, c->ns, c->ld, c->d_err, c->stream));
+  for (const Seg& g : segs(c))
+    CK(launch_check_state(c->qf[c->cur] + g.off, c->qc + g.off, g.n, c->ns, c->ld, c->d_err, c->stream));
   c->hrr_dot_state = 0;
   int rc2 = refresh_chem_set(c);
   if (rc2) return rc2;
@@ -803,8 +967,11 @@ int edyn_init_cells(void* ctx, const double* T, const double* p, const double* u
   CK(cudaMemcpyAsync(dp, p, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
   CK(cudaMemcpyAsync(du, u, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
   CK(cudaMemcpyAsync(dX, X, n * ns * sizeof(double), cudaMemcpyHostToDevice, c->stream));
-  CK(launch_init_cells(c->n, c->ns, dT, dp, du, dX, c->ns, c->qf[c->cur], c->qc, c->ld, c->stream));
-  CK(launch_check_state(c->qf[c->cur], c->qc, c->n, c->ns, c->ld, c->d_err, c->stream));
+  for (const Seg& g : segs(c)) {
+    CK(launch_init_cells(g.n, c->ns, dT + g.first, dp + g.first, du + g.first, dX + g.first * ns, c->ns,
+                         c->qf[c->cur] + g.off, c->qc + g.off, c->ld, c->stream));
+    CK(launch_check_state(c->qf[c->cur] + g.off, c->qc + g.off, g.n, c->ns, c->ld, c->d_err, c->stream));
+  }
   CK(cudaStreamSynchronize(c->stream));
   c->hrr_dot_state = 0;
   int rc2 = refresh_chem_set(c);
@@ -815,6 +982,8 @@ int edyn_init_cells(void* ctx, const double* T, const double* p, const double* u
 int edyn_calc_dt(void* ctx, double cfl, double* dt) {
   Ctx* c = (Ctx*)ctx;
   if (!c || !c->qc || !dt) return EDYN_E_ARG;
+  if (c->pk.ntube)
+    return fail(c, EDYN_E_ARG, "packed tubes take their own time steps: step them with edyn_step or edyn_advance");
   CK(cudaMemsetAsync(c->d_cvel, 0, sizeof(unsigned long long), c->stream));
   CK(launch_cvel(c->qf[c->cur], c->n, c->ld, c->d_cvel, c->stream));
   unsigned long long bits = 0;
@@ -830,6 +999,8 @@ int edyn_calc_dt(void* ctx, double cfl, double* dt) {
 int edyn_solve_fluid(void* ctx, double dt) {
   Ctx* c = (Ctx*)ctx;
   if (!c || !c->qc) return EDYN_E_ARG;
+  if (c->pk.ntube)
+    return fail(c, EDYN_E_ARG, "packed tubes take their own time steps: step them with edyn_step or edyn_advance");
   int rc = keep_hrr_dot(c);
   if (rc) return rc;
   rc = fluid_step(c, dt, false, true);
@@ -842,6 +1013,8 @@ int edyn_solve_source(void* ctx, double dt, double time) {
   (void)time;
   Ctx* c = (Ctx*)ctx;
   if (!c || !c->qc) return EDYN_E_ARG;
+  if (c->pk.ntube)
+    return fail(c, EDYN_E_ARG, "packed tubes take their own time steps: step them with edyn_step or edyn_advance");
   int rc = source_step(c, dt, false);
   if (rc) return rc;
   if (c->do_reaction) c->hrr_dot_state = 1;
@@ -862,6 +1035,15 @@ int edyn_post_step(void* ctx) {
 int edyn_step(void* ctx, double cfl, double* dt) {
   Ctx* c = (Ctx*)ctx;
   if (!c) return EDYN_E_ARG;
+  if (c->pk.ntube) {
+    // one step of every tube with its own dt, through the device loop
+    double t = 0.0;
+    long long n = 0;
+    int rc = edyn_advance(ctx, cfl, 1e300, 1, &t, &n);
+    if (rc) return rc;
+    if (dt) CK(cudaMemcpy(dt, c->pk.d_dt, sizeof(double), cudaMemcpyDeviceToHost));
+    return EDYN_OK;
+  }
   double d;
   int rc = edyn_calc_dt(ctx, cfl, &d);
   if (rc) return rc;
@@ -888,8 +1070,13 @@ int edyn_advance(void* ctx, double cfl, double tend, long long max_steps, double
   // stack variable may go out of scope
   const long long budget = max_steps;
   CK(cudaMemcpyAsync(c->d_max_steps, &budget, sizeof(long long), cudaMemcpyHostToDevice, c->stream));
-  CK(cudaMemsetAsync(c->d_cvel, 0, sizeof(unsigned long long), c->stream));
-  CK(launch_cvel(c->qf[c->cur], c->n, c->ld, c->d_cvel, c->stream));
+  if (c->pk.ntube) {
+    CK(cudaMemsetAsync(c->pk.d_cvel, 0, c->pk.ntube * sizeof(unsigned long long), c->stream));
+    CK(launch_cvel(c->qf[c->cur], c->n, c->ld, c->pk.d_cvel, c->stream, c->pk.colmap, c->pk.tube_of));
+  } else {
+    CK(cudaMemsetAsync(c->d_cvel, 0, sizeof(unsigned long long), c->stream));
+    CK(launch_cvel(c->qf[c->cur], c->n, c->ld, c->d_cvel, c->stream));
+  }
   if (c->do_reaction && c->chem_mode == 1) {
     // The surrogate path sizes its launches from counts it reads back, so
     // its steps run from the host, one at a time, with the device clock.
@@ -923,8 +1110,11 @@ int edyn_advance(void* ctx, double cfl, double tend, long long max_steps, double
     CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
     int rc = 0;
     for (int s = 0; s < per_graph && !rc; ++s) {
-      cudaError_t e = launch_step_begin(c->d_time, tend, c->d_nsteps, c->d_max_steps, cfl, c->dx, c->d_cvel,
-                                        c->d_active, c->d_dt, c->stream);
+      const Packed& k = c->pk;
+      cudaError_t e = k.ntube ? launch_step_begin_tubes(k.ntube, k.d_time, tend, c->d_nsteps, c->d_max_steps, cfl,
+                                                        k.d_dx, k.d_cvel, k.d_active, k.d_dt, c->d_active, c->stream)
+                              : launch_step_begin(c->d_time, tend, c->d_nsteps, c->d_max_steps, cfl, c->dx,
+                                                  c->d_cvel, c->d_active, c->d_dt, c->stream);
       if (e != cudaSuccess) rc = fail(c, EDYN_E_CUDA, "step_begin: %s", cudaGetErrorString(e));
       if (!rc) rc = fluid_step(c, 0.0, true, !c->do_reaction);
       if (!rc) rc = source_step(c, 0.0, true);
@@ -941,14 +1131,21 @@ int edyn_advance(void* ctx, double cfl, double tend, long long max_steps, double
   }
   long long done = 0;
   double t = *time;
+  // packed tubes keep their own clocks on the device; *time reports tube 0's
+  double* clock = c->pk.ntube ? c->pk.d_time : c->d_time;
+  if (c->pk.ntube) t = -1e300;
   while (t < tend && done < max_steps) {
     CK(cudaGraphLaunch(c->graph, c->stream));
     long long ns = 0;
-    CK(cudaMemcpyAsync(&t, c->d_time, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(&t, clock, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaMemcpyAsync(&ns, c->d_nsteps, sizeof(long long), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     if (ns == done) break;
     done = ns;
+    if (c->pk.ntube) t = -1e300;  // the device's loop test covers every tube
+  }
+  if (c->pk.ntube) {
+    CK(cudaMemcpy(&t, clock, sizeof(double), cudaMemcpyDeviceToHost));
   }
   *time = t;
   if (nsteps) *nsteps = done;
@@ -963,12 +1160,14 @@ int edyn_download(void* ctx, double* qf_aos, double* qc_aos, double* hrr) {
   int rc = ensure_staging(c, bytes);
   if (rc) return rc;
   if (qf_aos) {
-    CK(launch_soa_to_aos(c->qf[c->cur], c->ne, c->n, c->ld, c->staging, c->stream));
+    for (const Seg& g : segs(c))
+      CK(launch_soa_to_aos(c->qf[c->cur] + g.off, c->ne, g.n, c->ld, c->staging + g.first * c->ne, c->stream));
     CK(cudaMemcpyAsync(qf_aos, c->staging, bytes, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
   }
   if (qc_aos) {
-    CK(launch_soa_to_aos(c->qc, c->ne, c->n, c->ld, c->staging, c->stream));
+    for (const Seg& g : segs(c))
+      CK(launch_soa_to_aos(c->qc + g.off, c->ne, g.n, c->ld, c->staging + g.first * c->ne, c->stream));
     CK(cudaMemcpyAsync(qc_aos, c->staging, bytes, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
   }
@@ -1224,6 +1423,12 @@ int edyn_finalize(void* ctx) {
   if (c->chem_sub.d_tables) chem_free(c->chem_sub);
   cudaFree(c->d_present);
   {
+    Packed& k = c->pk;
+    void* bufs[] = {k.d_tiles, k.d_n, k.d_off, k.d_dx, k.d_p_out, k.d_dt, k.d_time, k.d_active, k.d_cvel, k.colmap,
+                    k.tube_of};
+    for (void* b : bufs) cudaFree(b);
+  }
+  {
     Surr& z = c->surr;
     void* bufs[] = {z.d_count, z.pk_idx, z.pk_rho, z.pk_dt, z.pk_y0, z.pk_f0, z.pk_y1, z.pk_ya, z.pk_f1,
                     z.pk_fa,   z.X,      z.Xt,     z.H[0],  z.H[1],  z.H[2],  z.out,   z.zero_out, z.zero_one,
@@ -1319,6 +1524,7 @@ extern "C" int edyn_solve_fluid_noalloc(void* ctx, double* qf_d, double* qc_d, d
   if ((reinterpret_cast<uintptr_t>(qf_d) | reinterpret_cast<uintptr_t>(qc_d)) % alignof(double))
     return fail(c, EDYN_E_ARG, "edyn_solve_fluid_noalloc: qf and Qc must be 8-byte aligned");
   const size_t rows = (size_t)c->ne * c->ld;
+  if (c->pk.ntube) return fail(c, EDYN_E_ARG, "edyn_solve_fluid_noalloc: one tube per context");
   if (c->select_time == 2)
     return fail(c, EDYN_E_ARG, "edyn_solve_fluid_noalloc: RK4 (select_time 2) needs a third scratch array; use "
                                "edyn_solve_fluid");

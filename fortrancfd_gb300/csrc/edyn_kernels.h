@@ -25,6 +25,21 @@ struct FluidBC {
   double y_in[64];
 };
 
+// Device tables of a context that packs several tubes side by side in the
+// same rows (tube t's block of n_t + 2 GHOST columns starts at column
+// off[t]): every tile of every tube is one CTA of the same stage launch.
+struct TubeTab {
+  const int4* tiles;       // per stage CTA: (tube, tile index within the tube, tiles of the tube, 0); null: one tube
+  const int* n;            // cells of each tube
+  const long long* off;    // column offset of each tube's block
+  const double* dx;        // cell size of each tube
+  const double* p_out;     // outlet pressure of each tube
+  const double* dt;        // time step of each tube in this step
+  const int* active;       // each tube steps in this step (its time < tend)
+  double* time;            // simulated time of each tube
+  int ntiles;              // stage CTAs of all tubes
+};
+
 struct StageArgs {
   int n, ld, lvir, ns;
   int tc;                // cells per stage tile (CTA); the CTA has stage_threads(tc) threads
@@ -48,13 +63,18 @@ struct StageArgs {
   int strict_newton;     // 1: T Newton starts at 1000 K as the reference
   FluidBC bc;            // inlet data (SRC/flow_bound.f90), passed by value
   unsigned* err;         // status word: EDYN_E_NEWTON / EDYN_E_STATE bits of any cell (may be null)
+  TubeTab tubes;         // packed tubes (tubes.tiles null: the single tube above); cvel_out then per tube
 };
 
 int fluid_upload_tables(const ThermoTable& tb, cudaStream_t s);
 size_t stage_smem_bytes(int acu, int ns, int tc);
 cudaError_t stage_tiling(int acu, int lim, int wflag, int rm, int ns, int n, int* tc);
 cudaError_t launch_stage(const StageArgs& a, int acu, int lim, int wflag, int rm, cudaStream_t s);
-cudaError_t launch_cvel(const double* qf, int n, int ld, unsigned long long* cvel, cudaStream_t s);
+cudaError_t launch_cvel(const double* qf, int n, int ld, unsigned long long* cvel, cudaStream_t s,
+                        const int* colmap = nullptr, const int* tube_of = nullptr);
+cudaError_t launch_step_begin_tubes(int ntube, const double* time, double tend, const long long* nsteps,
+                                    const long long* max_steps, double cfl, const double* dx, unsigned long long* cvel,
+                                    int* active, double* dt, int* step_active, cudaStream_t s);
 cudaError_t launch_species_present(const double* qc, int ld, int n, int ns, int* flags, cudaStream_t s);
 cudaError_t launch_step_begin(const double* time, double tend, const long long* nsteps, const long long* max_steps,
                               double cfl, double dx, unsigned long long* cvel, int* step_active, double* dt_dev,

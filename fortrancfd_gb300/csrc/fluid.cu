@@ -187,12 +187,22 @@ __device__ __forceinline__ void face_finish(FaceState& f, const Premix& pm, doub
   f.a = sqrt(gamma * R_SI * f.T * zr);
 }
 
+// The tube a stage CTA works on: the context's one tube, or one tube of a
+// packed set (its block's columns, cell size, outlet pressure, clock).
+struct TubeView {
+  int n;
+  const double* qf_in;
+  double *qf_out, *qc, *q0, *acc;
+  double dx, p_out;
+  unsigned long long* cvel;  // signal-speed maximum of this tube (or null)
+};
+
 // ---------------------------------------------------------------------------
 // Boundary ghost cells (SRC/boundary.f90). Computes the ghost cell g
 // (g < 0 left, g >= n right) primitive state from the interior conserved
 // state in global memory and stores it into the shared stencil.
 // ---------------------------------------------------------------------------
-__device__ void ghost_cell(const StageArgs& a, int g, double* dst, int dst_st, double* ys, int st) {
+__device__ void ghost_cell(const StageArgs& a, const TubeView& v, int g, double* dst, int dst_st, double* ys, int st) {
   const ThermoTable& tb = c_thermo;
   const int ns = tb.ns;
   const int ld = a.ld;
@@ -201,7 +211,7 @@ __device__ void ghost_cell(const StageArgs& a, int g, double* dst, int dst_st, d
   if (g < 0) {
     const int l = -g;  // 1..lvir
     const int src = l - 1;
-    const double* Q = a.qc + src + GHOST;
+    const double* Q = v.qc + src + GHOST;
     if (a.lbound == 0) {  // lbound_wall 152-174
       q0 = Q[0];
       q1 = -Q[ld];
@@ -216,9 +226,9 @@ __device__ void ghost_cell(const StageArgs& a, int g, double* dst, int dst_st, d
       for (int k = 0; k < ns; ++k) ys[k * st] = rho_in * a.bc.y_in[k];
     }
   } else {
-    const int l = g - a.n + 1;  // 1..lvir
-    const int src = a.n - l;
-    const double* Q = a.qc + src + GHOST;
+    const int l = g - v.n + 1;  // 1..lvir
+    const int src = v.n - l;
+    const double* Q = v.qc + src + GHOST;
     if (a.rbound == 0) {  // rbound_wall 177-199
       q0 = Q[0];
       q1 = -Q[ld];
@@ -241,7 +251,7 @@ __device__ void ghost_cell(const StageArgs& a, int g, double* dst, int dst_st, d
       const double E = e_out * sy * (1.0 / R_SI);
       double T_out = t_newton(ys, st, E, 1000.0, pm, Sz, iters);
       (void)sz;
-      const double rho_out = a.p_out * sy / (R_SI * T_out * Sz);
+      const double rho_out = v.p_out * sy / (R_SI * T_out * Sz);
       const double e2 = R_SI * (pm.H(T_out) - T_out * Sz) / sy;
       q0 = rho_out;
       q1 = rho_out * u_out;
@@ -275,12 +285,38 @@ __global__ void __launch_bounds__(STAGE_MAX_THREADS) k_stage(StageArgs a) {
   // built from them must belong to one CTA: when the last tile would hold
   // fewer than LV cells, the boundary between the last two tiles moves to
   // n - LV. (The first tile always holds the first LV cells.)
-  const int nb = gridDim.x;
-  int c0 = blockIdx.x * TC;
-  int c1 = min(c0 + TC, a.n);
-  if (nb >= 2 && a.n - (nb - 1) * TC < LV) {
-    if ((int)blockIdx.x == nb - 1) c0 = a.n - LV;
-    if ((int)blockIdx.x == nb - 2) c1 = a.n - LV;
+  // The CTA's tube: the context's one tube, or (packed tubes) the tube of
+  // this tile, with that tube's own dt.
+  TubeView tv{a.n, a.qf_in, a.qf_out, a.qc, a.q0, a.acc, a.dx, a.p_out, a.cvel_out};
+  int tile = blockIdx.x, nb = gridDim.x, tube = 0;
+  double dt = a.dt;
+  if (a.step_active) {
+    if (*a.step_active == 0) return;
+    dt = *a.dt_dev;
+  }
+  if (a.tubes.tiles) {
+    const int4 tl = a.tubes.tiles[blockIdx.x];
+    tube = tl.x;
+    tile = tl.y;
+    nb = tl.z;
+    if (a.tubes.active && a.tubes.active[tube] == 0) return;
+    const long long off = a.tubes.off[tube];
+    tv.n = a.tubes.n[tube];
+    tv.qf_in = a.qf_in + off;
+    tv.qf_out = a.qf_out + off;
+    tv.qc = a.qc + off;
+    tv.q0 = a.q0 + off;
+    tv.acc = a.acc ? a.acc + off : nullptr;
+    tv.dx = a.tubes.dx[tube];
+    tv.p_out = a.tubes.p_out[tube];
+    tv.cvel = a.cvel_out ? a.cvel_out + tube : nullptr;
+    dt = a.tubes.dt[tube];
+  }
+  int c0 = tile * TC;
+  int c1 = min(c0 + TC, tv.n);
+  if (nb >= 2 && tv.n - (nb - 1) * TC < LV) {
+    if (tile == nb - 1) c0 = tv.n - LV;
+    if (tile == nb - 2) c1 = tv.n - LV;
   }
   // stencil window [c0 - LV, c0 + TC + LV): the cells c0-1..c1 whose face
   // values the tile needs, each with its reconstruction radius LV - 1
@@ -293,26 +329,18 @@ __global__ void __launch_bounds__(STAGE_MAX_THREADS) k_stage(StageArgs a) {
   double* s_r = s_l + ne * P;   // [ne][P] value at the left face of cell c0-1+p (right state of face c0-1+p);
                                 //         then per-thread species scratch
 
-  // Device-driven time loop: k_step_begin decided whether this step runs
-  // and published its dt.
-  double dt = a.dt;
-  if (a.step_active) {
-    if (*a.step_active == 0) return;
-    dt = *a.dt_dev;
-  }
-
   // 1. stage the primitive state window (coalesced row loads)
 #pragma unroll 4
   for (int idx = tid; idx < ne * Wd; idx += NT) {
     const int v = idx / Wd, j = idx - v * Wd;
     const int cell = c0 - LV + j;
-    if (cell >= 0 && cell < a.n) s_q[idx] = a.qf_in[(size_t)v * a.ld + cell + GHOST];
+    if (cell >= 0 && cell < tv.n) s_q[idx] = tv.qf_in[(size_t)v * a.ld + cell + GHOST];
   }
   // ghost cells of the tube ends inside the window: thread t < LV takes the
   // left ghost -1-t, thread LV <= t < 2 LV the right ghost n + t - LV.
   if (tid < 2 * LV) {
-    const int g = (tid < LV) ? -1 - tid : a.n + (tid - LV);
-    if (g >= c0 - LV && g < c1 + LV) ghost_cell(a, g, s_q + (g - (c0 - LV)), Wd, s_r + tid, P);
+    const int g = (tid < LV) ? -1 - tid : tv.n + (tid - LV);
+    if (g >= c0 - LV && g < c1 + LV) ghost_cell(a, tv, g, s_q + (g - (c0 - LV)), Wd, s_r + tid, P);
   }
   __syncthreads();
 
@@ -465,12 +493,12 @@ __global__ void __launch_bounds__(STAGE_MAX_THREADS) k_stage(StageArgs a) {
   // the boundary ghosts): only the last stage runs QcToqf.
   const bool rk4_mid = a.kind == 2 && a.rk4_stage < 3;
   if (f < P && i < c1 && rk4_mid) {
-    const double c = dt / a.dx;
-    const double cq = 0.5 * ((0.5 * dt) / a.dx);  // 0.5 (0.5 dt / dx) of stages 1 and 2
+    const double c = dt / tv.dx;
+    const double cq = 0.5 * ((0.5 * dt) / tv.dx);  // 0.5 (0.5 dt / dx) of stages 1 and 2
     const size_t ld = (size_t)a.ld;
-    double* Q = a.qc + i + GHOST;
-    double* Q0 = a.q0 + i + GHOST;
-    double* A = a.acc + i + GHOST;
+    double* Q = tv.qc + i + GHOST;
+    double* Q0 = tv.q0 + i + GHOST;
+    double* A = tv.acc + i + GHOST;
     for (int v = h; v < ne; v += SP) {
       const double dF = s_l[v * P + f + 1] - s_l[v * P + f];
       const double k = -(c * dF);
@@ -485,16 +513,16 @@ __global__ void __launch_bounds__(STAGE_MAX_THREADS) k_stage(StageArgs a) {
     }
   }
   if (f < P && i < c1 && !rk4_mid) {
-    const double c = dt / a.dx;
+    const double c = dt / tv.dx;
     const size_t ld = (size_t)a.ld;
-    double* Q = a.qc + i + GHOST;
-    double* Q0 = a.q0 + i + GHOST;
+    double* Q = tv.qc + i + GHOST;
+    double* Q0 = tv.q0 + i + GHOST;
     double* ys = s_r + f;  // strided by P
     // Euler or first TVDRK3 stage: Q - c dF; later stages h1 Q0 + h2 (Q - c dF);
     // last RK4 stage: Q0 + (k1 + 2 k2 + 2 k3 + k4) / 6
     auto update = [&](int v, double qv) {
       const double dF = s_l[v * P + f + 1] - s_l[v * P + f];
-      if (a.kind == 2) return Q0[v * ld] + (1.0 / 6.0) * (a.acc[v * ld + i + GHOST] + -(c * dF));
+      if (a.kind == 2) return Q0[v * ld] + (1.0 / 6.0) * (tv.acc[v * ld + i + GHOST] + -(c * dF));
       return a.kind == 0 ? qv - c * dF : fma(a.h1, Q0[v * ld], a.h2 * (qv - c * dF));
     };
     double q[3], qv[3];
@@ -519,22 +547,29 @@ __global__ void __launch_bounds__(STAGE_MAX_THREADS) k_stage(StageArgs a) {
     int iters;
     const double Tg = s_q[2 * Wd + f + LV];
     CellEOS e = qc_to_qf_cell<SP>(q[0], q[1], q[2], ys, P, Tg, a.strict_newton != 0, iters, h, pair);
-    double* out = a.qf_out + i + GHOST;
+    double* out = tv.qf_out + i + GHOST;
     if (h == 0) {
       out[0] = q[0];
       out[ld] = e.u;
       out[2 * ld] = e.T;
-      if (a.cvel_out) speed = cell_speed(e.u, e.T, e.Sz, e.cpR);
+      if (tv.cvel) speed = cell_speed(e.u, e.T, e.Sz, e.cpR);
       if (e.status && a.err) atomicOr(a.err, e.status);
     }
     for (int k = h; k < ns; k += SP) out[(3 + k) * ld] = ys[k * P];
   }
-  if (a.cvel_out) {
+  if (tv.cvel) {
     double m = speed;
     for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
-    if ((tid & 31) == 0 && m > 0.0) atomic_max_pos(a.cvel_out, m);
+    if ((tid & 31) == 0 && m > 0.0) atomic_max_pos(tv.cvel, m);
   }
-  if (a.time && blockIdx.x == 0 && tid == 0) {
+  if (a.tubes.tiles) {
+    // packed tubes: the first tile of each tube advances that tube's clock,
+    // tube 0's the step count
+    if (a.time && tile == 0 && tid == 0) {
+      a.tubes.time[tube] = a.tubes.time[tube] + dt;
+      if (tube == 0) *a.nsteps = *a.nsteps + 1;
+    }
+  } else if (a.time && blockIdx.x == 0 && tid == 0) {
     // No CTA of this kernel reads the clock; k_step_begin of the next step does.
     *a.time = *a.time + dt;
     *a.nsteps = *a.nsteps + 1;
@@ -544,6 +579,26 @@ __global__ void __launch_bounds__(STAGE_MAX_THREADS) k_stage(StageArgs a) {
 // One thread: decides whether the step runs (time < tend, the loop test of
 // SRC/main.f90:130), computes dt = cfl dx / max speed (SRC/update.f90:50)
 // from the maximum left by the previous step, and clears the accumulator.
+// The loop test and time steps of packed tubes, one CTA: tube t steps while
+// its time < tend (and the call's step budget lasts), with dt_t = cfl dx_t /
+// (its maximum signal speed); step_active = any tube steps.
+__global__ void k_step_begin_tubes(int ntube, const double* time, double tend, const long long* nsteps,
+                                   const long long* max_steps, double cfl, const double* dx, unsigned long long* cvel,
+                                   int* active, double* dt, int* step_active) {
+  const bool budget = *nsteps < *max_steps;
+  int any = 0;
+  for (int t = threadIdx.x; t < ntube; t += blockDim.x) {
+    const int on = (budget && time[t] < tend) ? 1 : 0;
+    active[t] = on;
+    any |= on;
+    const double cv = __longlong_as_double((long long)cvel[t]);
+    dt[t] = on ? (cfl * dx[t]) / cv : 0.0;
+    cvel[t] = 0ull;
+  }
+  any = __syncthreads_or(any);
+  if (threadIdx.x == 0) *step_active = any;
+}
+
 __global__ void k_step_begin(const double* time, double tend, const long long* nsteps, const long long* max_steps,
                              double cfl, double dx, unsigned long long* cvel, int* step_active, double* dt_dev) {
   // the step budget of this call (edyn_advance's max_steps) ends the loop as
@@ -558,13 +613,15 @@ __global__ void k_step_begin(const double* time, double tend, const long long* n
   *cvel = 0ull;
 }
 
-// Signal-speed maximum of the current primitive state (calc_dt).
-__global__ void k_cvel(const double* qf, int n, int ld, unsigned long long* cvel) {
+// Signal-speed maximum of the current primitive state (calc_dt); with
+// packed tubes (colmap, tube_of) one maximum per tube.
+__global__ void k_cvel(const double* qf, int n, int ld, unsigned long long* cvel, const int* colmap,
+                       const int* tube_of) {
   const ThermoTable& tb = c_thermo;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   double sp = 0.0;
   if (i < n) {
-    const double* q = qf + i + GHOST;
+    const double* q = qf + (colmap ? colmap[i] : i) + GHOST;
     const double T = q[2 * (size_t)ld];
     Premix pm;
     pm.zero(t_interval(tb, T));
@@ -581,6 +638,10 @@ __global__ void k_cvel(const double* qf, int n, int ld, unsigned long long* cvel
     const double gamma = cpR / (cpR - sz);
     const double a = sqrt(gamma * R_SI * T * sz / sy);
     sp = fabs(q[ld]) + a;
+  }
+  if (tube_of) {
+    if (i < n) atomic_max_pos(cvel + tube_of[i], sp);
+    return;
   }
   double m = sp;
   for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
@@ -823,7 +884,7 @@ cudaError_t launch_stage(const StageArgs& a, int acu, int lim, int wflag, int rm
   const size_t smem = stage_smem_bytes(acu, a.ns, a.tc);
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  const int grid = (a.n + a.tc - 1) / a.tc;
+  const int grid = a.tubes.tiles ? a.tubes.ntiles : (a.n + a.tc - 1) / a.tc;
   kern<<<grid, stage_threads(a.tc), smem, s>>>(a);
   return cudaGetLastError();
 }
@@ -843,8 +904,16 @@ cudaError_t launch_species_present(const double* qc, int ld, int n, int ns, int*
   return cudaGetLastError();
 }
 
-cudaError_t launch_cvel(const double* qf, int n, int ld, unsigned long long* cvel, cudaStream_t s) {
-  k_cvel<<<(n + 127) / 128, 128, 0, s>>>(qf, n, ld, cvel);
+cudaError_t launch_cvel(const double* qf, int n, int ld, unsigned long long* cvel, cudaStream_t s,
+                        const int* colmap, const int* tube_of) {
+  k_cvel<<<(n + 127) / 128, 128, 0, s>>>(qf, n, ld, cvel, colmap, tube_of);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_step_begin_tubes(int ntube, const double* time, double tend, const long long* nsteps,
+                                    const long long* max_steps, double cfl, const double* dx, unsigned long long* cvel,
+                                    int* active, double* dt, int* step_active, cudaStream_t s) {
+  k_step_begin_tubes<<<1, 256, 0, s>>>(ntube, time, tend, nsteps, max_steps, cfl, dx, cvel, active, dt, step_active);
   return cudaGetLastError();
 }
 

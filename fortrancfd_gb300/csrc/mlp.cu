@@ -20,6 +20,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
+
 #include "../../include/edyn_surrogate.h"
 
 namespace edyn {
@@ -641,46 +643,62 @@ __global__ void k_gate(int n, int ns, int ne, const double* yiT0, double* yiT1, 
   }
 }
 
-// Gathers the rows of the rejected cells (accept == 0) into packed arrays,
-// in cell order, and records their cell indices. A single CTA of 1024
-// threads scans the flags in chunks with a block-wide prefix sum.
-__global__ void __launch_bounds__(1024) k_compact(int n, int ns, const int* accept, const double* rho,
-                                                  const double* dt, const double* yiT, int* idx, double* rho_p,
-                                                  double* dt_p, double* yiT_p, int* nrej) {
+// Indices of the rejected cells (accept == 0), in cell order, and their
+// number. One CTA of 1024 threads; each thread takes four consecutive flags
+// per round (4096 cells a round), a warp-shuffle scan and a scan of the 32
+// warp totals give every rejected cell its place.
+__global__ void __launch_bounds__(1024) k_compact_scan(int n, const int* accept, int* idx, int* nrej) {
   __shared__ int warp_tot[32];
   __shared__ int carry;
   if (threadIdx.x == 0) carry = 0;
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int c0 = 0; c0 < n; c0 += 1024) {
-    const int c = c0 + threadIdx.x;
-    const int rej = (c < n && !accept[c]) ? 1 : 0;
-    const unsigned m = __ballot_sync(0xffffffffu, rej);
-    const int before = __popc(m & ((1u << lane) - 1u));
-    if (lane == 0) warp_tot[warp] = __popc(m);
+  for (int c0 = 0; c0 < n; c0 += 4 * 1024) {
+    const int base = c0 + 4 * threadIdx.x;
+    int f[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) f[j] = (base + j < n && !accept[base + j]) ? 1 : 0;
+    const int mine = f[0] + f[1] + f[2] + f[3];
+    int incl = mine;  // inclusive scan over the warp
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int v = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += v;
+    }
+    if (lane == 31) warp_tot[warp] = incl;
     __syncthreads();
     int off = carry;
     for (int w = 0; w < warp; ++w) off += warp_tot[w];
-    if (rej) idx[off + before] = c;
+    off += incl - mine;
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+      if (f[j]) idx[off++] = base + j;
     __syncthreads();
     if (threadIdx.x == 0) {
-      int s = 0;
-      for (int w = 0; w < 32; ++w) s += warp_tot[w];
-      carry += s;
+      int t = 0;
+      for (int w = 0; w < 32; ++w) t += warp_tot[w];
+      carry += t;
     }
     __syncthreads();
   }
-  const int total = carry;
-  for (int j = threadIdx.x; j < total; j += blockDim.x) {
+  if (threadIdx.x == 0) *nrej = carry;
+}
+
+// The compacted rows' inputs, gathered grid-wide: rho_p, dt_p and the
+// (ns + 1)-value rows yiT_p of the *nrej cells listed in idx.
+__global__ void k_compact_gather(int ns, const int* idx, const int* nrej, const double* rho, const double* dt,
+                                 const double* yiT, double* rho_p, double* dt_p, double* yiT_p) {
+  const long total = *nrej;
+  const long row = ns + 1;
+  for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < total * row; q += (long)gridDim.x * blockDim.x) {
+    const long j = q / row, k = q - j * row;
     const int c = idx[j];
-    rho_p[j] = rho[c];
-    dt_p[j] = dt[c];
+    yiT_p[q] = yiT[(size_t)c * row + k];
+    if (k == 0) {
+      rho_p[j] = rho[c];
+      dt_p[j] = dt[c];
+    }
   }
-  for (long q = threadIdx.x; q < (long)total * (ns + 1); q += blockDim.x) {
-    const long j = q / (ns + 1);
-    yiT_p[q] = yiT[(size_t)idx[j] * (ns + 1) + q % (ns + 1)];
-  }
-  if (threadIdx.x == 0) *nrej = total;
 }
 
 // yiT1[idx[j]] = yiT_p[j] for the packed rows the integrator advanced.
@@ -837,7 +855,10 @@ int edyn_mlp_compact(int n, int ns, const int* accept, const double* rho, const 
                      int* idx, double* rho_p, double* dt_p, double* yiT_p, int* nrej, void* stream) {
   if (n <= 0 || ns <= 0 || !accept || !rho || !dt || !yiT || !idx || !rho_p || !dt_p || !yiT_p || !nrej)
     return EDYN_E_ARG;
-  k_compact<<<1, 1024, 0, S(stream)>>>(n, ns, accept, rho, dt, yiT, idx, rho_p, dt_p, yiT_p, nrej);
+  k_compact_scan<<<1, 1024, 0, S(stream)>>>(n, accept, idx, nrej);
+  const long rows = (long)n * (ns + 1);
+  const unsigned grid = (unsigned)std::min<long>((rows + 255) / 256, 152L * 16);
+  k_compact_gather<<<grid, 256, 0, S(stream)>>>(ns, idx, nrej, rho, dt, yiT, rho_p, dt_p, yiT_p);
   return rc(cudaGetLastError());
 }
 

@@ -68,6 +68,8 @@ def lib() -> ctypes.CDLL:
     L.edyn_download_source.argtypes = [vp, dp, dp]
     L.edyn_set_chem_max_steps.argtypes = [vp, i]
     L.edyn_set_chem_launch.argtypes = [vp, i]
+    L.edyn_init_tubes.argtypes = [cp, i, i, i, ip, i, ip, i, dp, i, ctypes.POINTER(vp)]
+    L.edyn_tube_times.argtypes = [vp, dp, dp]
     L.edyn_chem_rhs_tube.argtypes = [vp, i, vp, vp, vp]
     L.edyn_set_surrogate.argtypes = [vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, d, d, d]
     L.edyn_surrogate_stats.argtypes = [vp, dp]
@@ -300,6 +302,53 @@ class Tube(_Ctx):
         hrr = np.empty(self.ncell)
         self._check(lib().edyn_download(self._h, _ptr(qf), _ptr(qc), _ptr(hrr)))
         return qf, qc, hrr
+
+
+class Tubes(Tube):
+    """Several independent tubes advanced together in the same kernel
+    launches (edyn_init_tubes): each with its own cell count, cell size,
+    outlet pressure and time step; scheme and boundary kinds shared. Cells
+    are numbered one tube after another in every array."""
+
+    def __init__(self, ncells: Sequence[int], dxs: Sequence[float], *, p_outs: Optional[Sequence[float]] = None,
+                 chem_dir=GRI30_DIR, select_time=1, select_riemann=2, flag_acu=2, flag_muscl=2, flag_weno=3,
+                 flag_rbound=1, do_reaction=1, strict_newton=0, rtol=1e-5, atol=1e-13):
+        L = lib()
+        names = species_names(chem_dir)
+        nspe = len(names)
+        lv = lvir_for(flag_acu, flag_weno)
+        iflags = [select_time, select_riemann, flag_acu, flag_muscl, flag_weno, 0, flag_rbound, do_reaction,
+                  strict_newton, 0]
+        nt = len(ncells)
+        p_outs = [101325.0] * nt if p_outs is None else list(p_outs)
+        rp = np.ascontiguousarray([[dxs[t], p_outs[t], 300.0, 0.0, rtol, atol] for t in range(nt)], dtype=np.float64)
+        nc = (ctypes.c_int * nt)(*[int(v) for v in ncells])
+        fl = (ctypes.c_int * len(iflags))(*iflags)
+        self._h = ctypes.c_void_p()
+        self.nspe, self.nequ, self.ncell = nspe, nspe + 3, int(sum(ncells))
+        self.ntube, self.ncells = nt, [int(v) for v in ncells]
+        self.lvir, self.dx = lv, float(dxs[0])
+        rc = L.edyn_init_tubes(str(chem_dir).encode(), nspe, nspe + 3, nt, nc, lv, fl, len(iflags), _ptr(rp), 6,
+                               ctypes.byref(self._h))
+        if rc:
+            msg = self.last_error()
+            self.close()
+            raise EdynError(rc, msg)
+
+    def times(self):
+        """(simulated time, last dt) of every tube."""
+        t = np.zeros(self.ntube)
+        d = np.zeros(self.ntube)
+        self._check(lib().edyn_tube_times(self._h, _ptr(t), _ptr(d)))
+        return t, d
+
+    def split(self, a: np.ndarray):
+        """Per-tube views of a packed per-cell array."""
+        out, i = [], 0
+        for n in self.ncells:
+            out.append(a[i:i + n])
+            i += n
+        return out
 
 
 def _set_chem_max_steps(self, max_steps: int = 0) -> None:

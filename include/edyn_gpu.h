@@ -62,6 +62,28 @@ extern "C" {
 int edyn_init(const char* chem_dir, int nspe, int nequ, int ncell, int lvir, const int* iflags, int n_iflags,
               const double* rparams, int n_rparams, const double* x_in, void** ctx);
 
+/* Creates a context for ntube independent tubes advanced together, each
+ * with its own cell count ncell[t] (>= 16), cell size and outlet pressure
+ * (rparams: ntube rows of n_rparams values, the same slots as edyn_init;
+ * rtol and atol are taken from the first row) and its own time step
+ * dt_t = cfl dx_t / max(|u| + a) over its cells: the reference's one-tube
+ * time loop (SRC/main.f90:130-163) run for many tubes in the same kernel
+ * launches. The scheme, boundary kinds and chemistry flags are shared;
+ * the inflow boundary and the surrogate (chem_mode 1) are not available.
+ * The tubes' cells are numbered one tube after another: edyn_upload,
+ * edyn_init_cells and edyn_download take and give ncell[0] + ... cells in
+ * that order. The context steps through edyn_step (one step of every tube)
+ * and edyn_advance (every tube while its own time < tend; *time receives
+ * tube 0's); edyn_calc_dt, edyn_solve_fluid and edyn_solve_source refuse
+ * it. No counterpart in the reference, which runs one tube per process
+ * (its MPI ranks split one tube, SRC/parallel.f90:66-83). */
+int edyn_init_tubes(const char* chem_dir, int nspe, int nequ, int ntube, const int* ncell, int lvir,
+                    const int* iflags, int n_iflags, const double* rparams, int n_rparams, void** ctx);
+
+/* Per-tube simulated times and last time steps (ntube values each, either
+ * pointer may be NULL); one value for a single-tube context. */
+int edyn_tube_times(void* ctx, double* time, double* dt);
+
 /* Uploads the interior state. qf may be NULL (then qf = QcToqf(Qc)).
  * Mirrors set_block_params filling b_obj%qf / b_obj%Qc (SRC/block.f90:394-431). */
 int edyn_upload(void* ctx, const double* qf_aos, const double* qc_aos);
@@ -178,7 +200,9 @@ int edyn_chem_rhs_tube(void* ctx, int n, const double* rho_d, const double* yiT_
  * light screening pass evaluates f(y0) and the inert-cell test of every cell
  * at four warps per SM sub-partition and finishes the inert cells; the
  * integrator kernel then takes only the cells it listed), 0 automatic (two
- * passes from 50,000 cells). Results do not depend on the form. No
+ * passes from 50,000 cells). The forms agree up to rounding: a cell on the
+ * four-warp team list that turns out inert is finished by its team in one
+ * pass and by a single warp in two, whose sums run in other orders. No
  * counterpart in the reference (a tuning knob of this implementation). */
 int edyn_set_chem_launch(void* ctx, int form);
 

@@ -53,6 +53,7 @@ class Oracle:
         L.or_ckwyr.argtypes = [vp, d, d, _D, _D]
         L.or_ckrop.argtypes = [vp, d, d, _D, _D, _D]
         L.or_cksmh.argtypes = [vp, d, _D]
+        L.or_ckhms.argtypes = [vp, d, _D]
         L.or_ckhml.argtypes = [vp, d, _D]
         L.or_ckuml.argtypes = [vp, d, _D]
         L.or_ckcpml.argtypes = [vp, d, _D]

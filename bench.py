@@ -74,6 +74,7 @@ def parse():
                         "the uneven batch of --ntubes tubes in one context")
     p.add_argument("--ntubes", type=int, default=256, help="tubes of --workload tubes")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-surrogate", action="store_true", help="skip the surrogate-vs-plain comparison")
     p.add_argument("--reactors", type=int, default=1 << 20, help="reactors in the batch of --workload reactors")
     p.add_argument("--prepared", type=int, default=1 << 16,
                    help="partially reacted states prepared for --workload reactors (each reused reactors/prepared "
@@ -285,6 +286,60 @@ def run_tube(tube, case, steps, warmup, stream, flush):
     return dev_ms / 1e3, graphs, t_sim
 
 
+def species_err(a, b, floor=1e-6):
+    """Largest relative difference of the mass fractions >= floor."""
+    big = np.abs(b) >= floor
+    return float(np.where(big, np.abs(a - b) / np.maximum(np.abs(b), floor), 0.0).max())
+
+
+def surrogate_compare(case, args, stream, dev, plain_end, plain_value):
+    """The learned surrogate in the tube's source step (chem_mode 1) against
+    the plain chemistry on the same tube and the same steps. The network is
+    trained first, on the GPU by the library's kernels, on pairs the plain
+    integrator produces (rtol 1e-8) for exactly the cells a chem_mode 1 tube
+    hands to it, harvested from 5 um CH4/air tubes over a seeded sweep of
+    phi ~ U[0.7, 1.4] and driver T ~ U[2500, 3500] K. Then the same warm-up
+    and timed steps run through edyn_advance with the network, and without
+    it (the gated explicit increment, then the integrator); the species and
+    peak-T errors are against the plain run's state after the same steps."""
+    import torch
+
+    from fortrancfd_gb300 import Reactors, Tube
+    from fortrancfd_gb300 import surrogate as S
+
+    t0 = time.perf_counter()
+    rho, dt, y0, y1 = S.harvest_screened(S.tube_sweep(6, seed=0), nsteps=100)
+    s = S.Surrogate(Reactors(rtol=1e-5, atol=1e-13), S.MLP(seed=0))
+    hist = S.train(s, rho, dt, y0, y1, iters=3000, batch=4096, lr=2e-3, log_every=2999)
+    t_train = time.perf_counter() - t0
+    out = {"target": ">= 5x the plain integrator's cell-steps/s (not met)",
+           "training": f"{len(rho)} pairs from 6 tubes x 100 steps, 3000 Adam steps of 4096 on the GPU, "
+                       f"{t_train:.1f} s incl. harvest, final loss {hist[-1][1]:.3f}"}
+    fl = case.flags
+    for label, net in (("with_network", s), ("without_network", None)):
+        tube = Tube(case.ncell, case.dx, flag_acu=2, flag_weno=fl["flag_weno"], flag_rbound=1, do_reaction=1,
+                    strict_newton=0, rtol=1e-5, atol=1e-13, chem_mode=1)
+        tube.set_stream(stream.cuda_stream)
+        tube.set_surrogate(net)
+        tube.init_cells(case.T, case.p, case.u, case.X)
+        t_sim, n = tube.advance(case.cfl, tend=1e9, time=0.0, max_steps=args.warmup) if args.warmup else (0.0, 0)
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        t_sim, n = tube.advance(case.cfl, tend=1e9, time=t_sim, max_steps=args.steps)
+        e1.record(stream)
+        e1.synchronize()
+        v = case.ncell * n / (e0.elapsed_time(e1) / 1e3)
+        qf = tube.download()[0]
+        out[label] = {"value": v, "speedup_vs_plain": v / plain_value, "last_step": tube.surrogate_stats(),
+                      "species_err_vs_plain": species_err(qf[:, 3:], plain_end[:, 3:]),
+                      "peak_T_err_vs_plain": float(abs(qf[:, 2].max() - plain_end[:, 2].max()) / plain_end[:, 2].max())}
+        tube.close()
+    out["value"] = out["with_network"]["value"]
+    out["speedup"] = out["with_network"]["speedup_vs_plain"]
+    return out
+
+
 def gpu_arm(args, rank, world, local):
     import torch
 
@@ -315,6 +370,7 @@ def gpu_arm(args, rank, world, local):
     with ClockSampler(local) as clk:
         t_dev, graphs, t_sim = run_tube(tube, case, args.steps, args.warmup, stream, flush)
     torch.cuda.synchronize(dev)
+    plain_end = tube.download()[0]
     t_max = max_over_ranks(t_dev, world, dev)
     value = job_value(case.ncell, args.steps, world, t_max)
     # per-launch kernel durations for the roofline: chemistry and one fluid step
@@ -373,6 +429,15 @@ def gpu_arm(args, rank, world, local):
         fp64.update(achieved=fpr * rhs_launch / chem_s / 1e12, flops_per_rhs=fpr,
                     frac=fpr * rhs_launch / chem_s / 1e12 / p64)
     cpu = None if args.no_cpu_baseline or world > 1 else cpu_baseline(case)
+    surr = None
+    if not args.no_surrogate and world == 1 and "air" in case.name:
+        try:
+            surr = surrogate_compare(case, args, stream, dev, plain_end, value)
+        except Exception as ex:  # reported, not hidden: the headline line still prints
+            surr = {"error": f"{type(ex).__name__}: {ex}"}
+    # kernels per step: the loop test, the fluid stages, the chemistry
+    # (counter clear + one pass, or + screen pass and the two team-pick kernels)
+    per_step = 1 + 3 + (5 if case.ncell >= 50000 else 2)
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
@@ -386,12 +451,13 @@ def gpu_arm(args, rank, world, local):
             "e2e": {"value": case.ncell * e2e_steps / e2e_el, "unit": UNIT,
                     "h2d_bytes_per_step": 2 * case.ncell * ne * 8,
                     "d2h_bytes_per_step": (2 * case.ncell * ne + case.ncell) * 8, "steps": e2e_steps},
-            "gpu_launches": graphs * 16 * 5,
+            "gpu_launches": graphs * 16 * per_step,
             "roofline": roof, "fp64": fp64,
             "cpu_baseline": cpu,
             "chem_launch": {"rhs_per_cell": chem_stats["rhs"] / max(1, chem_stats["cells"]),
                             "rejects": chem_stats["rejects"], "team_cells": chem_stats["team_cells"],
-                            "failed": chem_stats["failed"]}}
+                            "failed": chem_stats["failed"]},
+            "surrogate": surr}
     print(json.dumps(line), flush=True)
 
 

@@ -2949,12 +2949,20 @@ cudaError_t chem_finish_packed(ChemState& s, const ChemLaunch& L, int m, const d
   return cudaGetLastError();
 }
 
+namespace {
+// Clears a launch's counters unless the device loop skips this step (the
+// counters then keep the last step that ran).
+__global__ void k_clear_counters(const int* step_active, ChemCounters* cnt) {
+  if (step_active && *step_active == 0) return;
+  *cnt = ChemCounters{0, 0, 0, 0, 0, 0, 0};
+}
+}  // namespace
+
 cudaError_t chem_launch_tube_listed(ChemState& s, const ChemLaunch& L0, int* list, unsigned* list_count,
                                     unsigned char* cls, unsigned* hist, cudaStream_t st) {
   cudaError_t e = cudaMemsetAsync(s.d_next, 0, 2 * sizeof(unsigned), st);
   if (e != cudaSuccess) return e;
-  e = cudaMemsetAsync(s.d_count, 0, sizeof(ChemCounters), st);
-  if (e != cudaSuccess) return e;
+  k_clear_counters<<<1, 1, 0, st>>>(L0.step_active, s.d_count);
   e = cudaMemsetAsync(list_count, 0, sizeof(unsigned), st);
   if (e != cudaSuccess) return e;
   ChemLaunch L = L0;
@@ -2991,8 +2999,7 @@ cudaError_t chem_launch_screen_packed(ChemState& s, const ChemLaunch& L, cudaStr
 cudaError_t chem_launch_tube(ChemState& s, const ChemLaunch& L, cudaStream_t st) {
   cudaError_t e = cudaMemsetAsync(s.d_next, 0, 2 * sizeof(unsigned), st);
   if (e != cudaSuccess) return e;
-  e = cudaMemsetAsync(s.d_count, 0, sizeof(ChemCounters), st);
-  if (e != cudaSuccess) return e;
+  k_clear_counters<<<1, 1, 0, st>>>(L.step_active, s.d_count);
   const int grid = std::min(s.ctas, (L.n + s.warps - 1) / s.warps);
   k_tube_chem<<<std::max(1, grid), s.warps * 32, s.smem, st>>>((const char*)s.d_tables, (int)s.table_bytes, L,
                                                              s.d_next, s.d_count);

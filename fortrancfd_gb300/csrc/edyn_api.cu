@@ -110,8 +110,10 @@ struct Ctx {
   double* hrr_dot = nullptr;  // HRR_dot of the last source step, once evaluated
   double* tchem = nullptr;    // temperature each cell's last integration ended with
   // HRR_dot of the last source step: 0 none (zeros), 1 not yet evaluated (the
-  // primitive state is still the one that step left), 2 evaluated into hrr_dot
+  // primitive state is still the one that step left), 2 evaluated into
+  // hrr_dot, 3 not yet evaluated, the rows it needs saved in hrr_dot_rows
   int hrr_dot_state = 0;
+  double* hrr_dot_rows = nullptr;  // primitive rows the last source step left
   int chem_max_steps = 0;     // integrator step cap per cell (0: the default 4000)
   double* staging = nullptr;
   size_t staging_bytes = 0;
@@ -623,19 +625,28 @@ void drop_graph(Ctx* c) {
 // Evaluates HRR_dot of the last source step into c->hrr_dot while the
 // primitive state is still the one that step left.
 int eval_hrr_dot(Ctx* c) {
-  if (c->hrr_dot_state != 1) return EDYN_OK;
-  cudaError_t e = chem_hrr_dot(c->use_sub ? c->chem_sub : c->chem, c->n, c->ld, c->qf[c->cur], c->tchem, c->hrr_dot,
+  if (c->hrr_dot_state != 1 && c->hrr_dot_state != 3) return EDYN_OK;
+  const double* rows = c->hrr_dot_state == 3 ? c->hrr_dot_rows : c->qf[c->cur];
+  cudaError_t e = chem_hrr_dot(c->use_sub ? c->chem_sub : c->chem, c->n, c->ld, rows, c->tchem, c->hrr_dot,
                                c->pk.colmap, c->stream);
   if (e != cudaSuccess) return fail(c, EDYN_E_CUDA, "HRR_dot launch: %s", cudaGetErrorString(e));
   c->hrr_dot_state = 2;
   return EDYN_OK;
 }
 
-// Before a fluid step changes the state the last source step left: keep its
-// HRR_dot (the reference's eos_obj%HRR_dot outlives the next fluid step).
-// In the reference's own order (output right after the source step) this
-// never runs and HRR_dot costs nothing until it is downloaded.
-int keep_hrr_dot(Ctx* c) { return eval_hrr_dot(c); }
+// Before a fluid step changes the state the last source step left: keep the
+// primitive rows HRR_dot needs (the reference's eos_obj%HRR_dot outlives
+// the next fluid step), one device-to-device copy of the rows instead of a
+// right-hand side per cell; HRR_dot itself is still evaluated only when it
+// is downloaded.
+int keep_hrr_dot(Ctx* c) {
+  if (c->hrr_dot_state != 1) return EDYN_OK;
+  const size_t bytes = (size_t)c->ne * c->ld * sizeof(double);
+  if (!c->hrr_dot_rows) CK(cudaMalloc(&c->hrr_dot_rows, bytes));
+  CK(cudaMemcpyAsync(c->hrr_dot_rows, c->qf[c->cur], bytes, cudaMemcpyDeviceToDevice, c->stream));
+  c->hrr_dot_state = 3;
+  return EDYN_OK;
+}
 
 }  // namespace
 
@@ -1134,12 +1145,21 @@ int edyn_advance(void* ctx, double cfl, double tend, long long max_steps, double
   // packed tubes keep their own clocks on the device; *time reports tube 0's
   double* clock = c->pk.ntube ? c->pk.d_time : c->d_time;
   if (c->pk.ntube) t = -1e300;
+  // A graph whose loop test ends the run before its 16th step leaves the new
+  // primitive state in the buffer its last active stage wrote; the graph's
+  // buffer roles assume all 16 steps, so after an odd number of swaps the
+  // state is copied back into the buffer the graph starts from.
+  const int swaps_per_step = (c->select_time == 1) ? 3 : 1;
   while (t < tend && done < max_steps) {
     CK(cudaGraphLaunch(c->graph, c->stream));
     long long ns = 0;
     CK(cudaMemcpyAsync(&t, clock, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaMemcpyAsync(&ns, c->d_nsteps, sizeof(long long), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
+    const long long ran = ns - done;
+    if (ran > 0 && ran < per_graph && (ran * swaps_per_step) % 2 == 1)
+      CK(cudaMemcpyAsync(c->qf[c->cur], c->qf[c->cur ^ 1], (size_t)c->ne * c->ld * sizeof(double),
+                         cudaMemcpyDeviceToDevice, c->stream));
     if (ns == done) break;
     done = ns;
     if (c->pk.ntube) t = -1e300;  // the device's loop test covers every tube
@@ -1442,6 +1462,7 @@ int edyn_finalize(void* ctx) {
   cudaFree(c->acc);
   cudaFree(c->hrr);
   cudaFree(c->hrr_dot);
+  cudaFree(c->hrr_dot_rows);
   cudaFree(c->tchem);
   cudaFree(c->staging);
   cudaFree(c->d_time);

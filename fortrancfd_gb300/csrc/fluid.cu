@@ -591,8 +591,9 @@ __global__ void k_step_begin_tubes(int ntube, const double* time, double tend, c
     const int on = (budget && time[t] < tend) ? 1 : 0;
     active[t] = on;
     any |= on;
+    if (!on) continue;  // an idle tube keeps its last dt and speed
     const double cv = __longlong_as_double((long long)cvel[t]);
-    dt[t] = on ? (cfl * dx[t]) / cv : 0.0;
+    dt[t] = (cfl * dx[t]) / cv;
     cvel[t] = 0ull;
   }
   any = __syncthreads_or(any);

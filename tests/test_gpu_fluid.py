@@ -222,3 +222,30 @@ def test_calc_dt_matches_oracle(oracle):
     g = Tube(case.ncell, case.dx)
     g.upload(qf0, qc0)
     assert g.calc_dt(0.5) == pytest.approx(ot.calc_dt(0.5), rel=1e-14)
+
+
+@pytest.mark.parametrize("select_time", [1, 0])
+def test_device_loop_partial_graphs(oracle, select_time):
+    """edyn_advance runs exactly the steps it is given, inside 16-step
+    graphs: runs of 5, 7 and 3 steps (graphs that stop part way, after an
+    odd number of buffer swaps) continue from the right state, matching the
+    oracle's 15 steps at 1e-10."""
+    case = configs.sod(ncell=300)
+    case.flags.update(select_time=select_time)
+    W = configs.molecular_weights()
+    qf0, qc0 = oracle.init_cells(case.T, case.p, case.u, case.X)
+    fl = case.flags
+    ot = oracle.tube(case.ncell, 2, [select_time, 2, 1, 2, 0, 0, 0, 0], [case.dx, 101325.0, 300.0, 0.0, 1e-5, 1e-13])
+    ot.set_interior(qf0, qc0)
+    g = Tube(case.ncell, case.dx, select_time=select_time)
+    g.upload(qf0, qc0)
+    t = 0.0
+    for k in (5, 7, 3):
+        t, n = g.advance(case.cfl, tend=1e9, time=t, max_steps=k)
+        assert n == k
+    t_o = sum(ot.step(case.cfl) for _ in range(15))
+    assert t == pytest.approx(t_o, rel=1e-12)
+    qf_o, _ = ot.get()
+    qf_g, _, _ = g.download()
+    assert rel(pressure(qf_g, W), pressure(qf_o, W)) < TOL
+    assert rel(qf_g[:, 2], qf_o[:, 2]) < TOL

@@ -44,14 +44,15 @@ UNIT = "cell-steps/s"
 BYTES_PER_CELL_STEP = 4544  # algorithmic: fluid RK3 3632 B + chemistry 912 B per cell-step
 BYTES_CHEM_PER_CELL = 912   # chemistry launch: read qf (456 B) + write qf and Qc rows (456 B)
 L2_BYTES = 129 << 20
-# DRAM bytes (read + write) of one chemistry launch per cell and FP64
-# operations per right-hand side (2 x DFMA + DADD + DMUL thread instructions
-# over the launch / right-hand sides it evaluated), from ncu captures of the
-# chemistry launch listed in profiles/ (k_tube_chem on the 20,000-cell
-# CH4/air tube of 5 um cells); scaled here by cells and by the right-hand
-# sides each timed launch evaluates.
-TRAFFIC_CHEM_PER_CELL = {"detonation_air_200k": None, "detonation_o2_20k": 1.93e6 / 4000, "detonation_air_20k": None}
-FP64_FLOPS_PER_RHS = {"detonation_air_200k": None, "detonation_o2_20k": None, "detonation_air_20k": None}
+# From ncu captures of one launch of each kernel of the 200,000-cell tube
+# (profiles/*_ch4_air_detonation_200000.md), scaled here by cells:
+# DRAM bytes (read + write) of the chemistry launch per cell (screening
+# pass 88.5 + 118.7 MB, listed pass 1.6 MB), and FP64 operations per
+# cell-step, 2 DFMA + DADD + DMUL thread instructions: three fluid stages of
+# 12,150 each, the screening pass's 33,450, the listed pass's 2,470.
+TRAFFIC_CHEM_PER_CELL = {"detonation_air_200k": (88.5e6 + 118.7e6 + 1.6e6) / 200000,
+                         "detonation_o2_20k": 1.93e6 / 4000, "detonation_air_20k": None}
+FP64_FLOPS_PER_CELL_STEP = {"detonation_air_200k": 3 * 12150 + 33450 + 2470}
 
 WORKLOADS = {
     "detonation_air_200k": dict(ncell=200000, length=1.0, oxidizer="air"),
@@ -413,7 +414,8 @@ def gpu_arm(args, rank, world, local):
         return
     hbm, src = peaks()
     achieved = BYTES_CHEM_PER_CELL * case.ncell / chem_s / 1e9
-    roof = {"bound": "hbm", "kernel": "k_tube_chem", "achieved": achieved, "peak": hbm, "peak_source": src,
+    roof = {"bound": "hbm", "kernel": "chemistry launch (k_tube_screen + k_tube_chem)", "achieved": achieved,
+            "peak": hbm, "peak_source": src,
             "unit": "GB/s", "frac": achieved / hbm,
             "traffic": (TRAFFIC_CHEM_PER_CELL[args.workload] * case.ncell
                         if TRAFFIC_CHEM_PER_CELL[args.workload] else None),
@@ -421,13 +423,13 @@ def gpu_arm(args, rank, world, local):
             "note": "the chemistry launch is FP64-pipe bound (see fp64); its HBM fraction only shows that memory "
                     "is not the limit"}
     p64 = fp64_peak(dev)
-    fpr = FP64_FLOPS_PER_RHS[args.workload]
-    rhs_launch = statistics.median(rhs)
-    fp64 = {"peak": p64, "unit": "TFLOP/s", "peak_source": "cuBLAS DGEMM 4096^3, best of 5, this run",
-            "rhs_per_launch": rhs_launch, "rhs_launches": rhs}
-    if fpr:
-        fp64.update(achieved=fpr * rhs_launch / chem_s / 1e12, flops_per_rhs=fpr,
-                    frac=fpr * rhs_launch / chem_s / 1e12 / p64)
+    fpc = FP64_FLOPS_PER_CELL_STEP.get(args.workload)
+    fp64 = {"bound": "fp64", "scope": "whole step", "peak": p64, "unit": "TFLOP/s",
+            "peak_source": "cuBLAS DGEMM 4096^3, best of 5, this run", "rhs_launches": rhs}
+    if fpc:
+        ach = fpc * case.ncell * args.steps / t_max / world / 1e12
+        fp64.update(achieved=ach, flops_per_cell_step=fpc, frac=ach / p64,
+                    source="FP64 instructions per cell from ncu captures of each kernel (profiles/)")
     cpu = None if args.no_cpu_baseline or world > 1 else cpu_baseline(case)
     surr = None
     if not args.no_surrogate and world == 1 and "air" in case.name:

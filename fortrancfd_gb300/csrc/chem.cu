@@ -2458,16 +2458,31 @@ __global__ void __launch_bounds__(1024) k_hot_pick(const unsigned char* cls, int
   __syncthreads();
   const int B = s_B;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int c0 = 0; c0 < n && B < 32; c0 += blockDim.x) {
-    const int i = c0 + threadIdx.x;
-    const bool pick = i < n && cls[i] >= B;
-    const unsigned bal = __ballot_sync(0xffffffffu, pick);
-    if (lane == 0) warp_tot[warp] = __popc(bal);
+  // four consecutive cells a thread per round (4096 a round): a warp-shuffle
+  // scan of the per-thread counts and a scan of the warp totals
+  for (int c0 = 0; c0 < n && B < 32; c0 += 4 * (int)blockDim.x) {
+    const int base = c0 + 4 * threadIdx.x;
+    int f[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) f[j] = (base + j < n && cls[base + j] >= B) ? 1 : 0;
+    const int mine = f[0] + f[1] + f[2] + f[3];
+    int incl = mine;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int v = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += v;
+    }
+    if (lane == 31) warp_tot[warp] = incl;
     __syncthreads();
     unsigned off = carry;
     for (int w2 = 0; w2 < warp; ++w2) off += warp_tot[w2];
-    off += __popc(bal & ((1u << lane) - 1u));
-    if (pick && off < (unsigned)HOT_MAX) hot[1 + off] = (unsigned)i;
+    off += incl - mine;
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+      if (f[j]) {
+        if (off < (unsigned)HOT_MAX) hot[1 + off] = (unsigned)(base + j);
+        ++off;
+      }
     __syncthreads();
     if (threadIdx.x == 0) {
       unsigned tot = 0;

@@ -900,6 +900,129 @@ int edyn_tube_times(void* ctx, double* time, double* dt) {
   return EDYN_OK;
 }
 
+namespace {
+// Cache line key of the stage-tile choice: scheme, species, cells, tubes and
+// device, so a choice measured once serves later runs of the same case.
+std::string tune_key(Ctx* c) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceProp pr;
+  std::memset(&pr, 0, sizeof(pr));
+  cudaGetDeviceProperties(&pr, dev);
+  std::string name(pr.name);
+  for (char& ch : name)
+    if (ch == ' ') ch = '_';
+  char buf[256];
+  std::snprintf(buf, sizeof(buf), "stage acu=%d lim=%d weno=%d rm=%d ns=%d n=%d tubes=%d sm=%d %s", c->acu, c->lim,
+                c->wflag, c->riemann, c->ns, c->n, c->pk.ntube, pr.multiProcessorCount, name.c_str());
+  return buf;
+}
+}  // namespace
+
+int edyn_autotune(void* ctx, const char* cache_path, int* tile, double* stage_ms) {
+  Ctx* c = (Ctx*)ctx;
+  if (!c || !c->qc) return EDYN_E_ARG;
+  const std::string key = tune_key(c);
+  if (cache_path) {
+    if (FILE* f = std::fopen(cache_path, "r")) {
+      char line[512];
+      int best = -1;
+      double ms = 0;
+      while (std::fgets(line, sizeof(line), f)) {
+        const size_t kl = key.size();
+        if (std::strncmp(line, key.c_str(), kl) == 0 && line[kl] == ' ') {
+          int t = 0;
+          double m = 0;
+          if (std::sscanf(line + kl, " tile=%d ms=%lf", &t, &m) == 2 && t >= STAGE_MIN_CELLS && t <= STAGE_MAX_CELLS) {
+            best = t;
+            ms = m;
+          }
+        }
+      }
+      std::fclose(f);
+      if (best > 0) {
+        c->stage_tc = best;
+        drop_graph(c);
+        if (c->pk.ntube) {
+          int rc = build_tiles(c);
+          if (rc) return rc;
+        }
+        if (tile) *tile = best;
+        if (stage_ms) *stage_ms = ms;
+        return EDYN_OK;
+      }
+    }
+  }
+  // Time one fluid stage per candidate tile on the tube's own state with
+  // dt = 0: Q - 0 dF = Q, so Qc stays bit for bit as it was; the stage only
+  // rewrites the second primitive buffer, which every step writes before
+  // it reads it.
+  const int tc0 = c->stage_tc;
+  // packed tubes time the stage at dt = 0 through their per-tube dt; the
+  // tubes' last time steps are put back afterwards
+  std::vector<double> dt_saved(c->pk.ntube);
+  if (c->pk.ntube)
+    CK(cudaMemcpyAsync(dt_saved.data(), c->pk.d_dt, c->pk.ntube * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  int best = tc0;
+  float best_ms = 1e30f;
+  for (int tc = STAGE_MIN_CELLS; tc <= STAGE_MAX_CELLS; tc += 2) {
+    c->stage_tc = tc;
+    if (c->pk.ntube) {
+      int rc = build_tiles(c);
+      if (rc) return rc;
+    }
+    StageArgs a = base_args(c);
+    a.qf_in = c->qf[c->cur];
+    a.qf_out = c->qf[c->cur ^ 1];
+    a.kind = 0;
+    a.save_q0 = 0;
+    a.dt = 0.0;
+    a.err = nullptr;
+    if (c->pk.ntube) {
+      // every packed tube at dt = 0: point the per-tube dt at zeros
+      CK(cudaMemsetAsync(c->pk.d_dt, 0, c->pk.ntube * sizeof(double), c->stream));
+      a.tubes.active = nullptr;
+    }
+    float ms = 0.f;
+    for (int rep = 0; rep < 3; ++rep) {
+      CK(cudaEventRecord(e0, c->stream));
+      cudaError_t e = launch_stage(a, c->acu, c->lim, c->wflag, c->riemann, c->stream);
+      if (e != cudaSuccess) return fail(c, EDYN_E_CUDA, "autotune stage launch: %s", cudaGetErrorString(e));
+      CK(cudaEventRecord(e1, c->stream));
+      CK(cudaEventSynchronize(e1));
+      float m = 0.f;
+      CK(cudaEventElapsedTime(&m, e0, e1));
+      if (rep > 0) ms = (rep == 1) ? m : std::min(ms, m);  // the first launch warms up
+    }
+    if (ms < best_ms) {
+      best_ms = ms;
+      best = tc;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  c->stage_tc = best;
+  drop_graph(c);
+  if (c->pk.ntube) {
+    CK(cudaMemcpyAsync(c->pk.d_dt, dt_saved.data(), c->pk.ntube * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    int rc = build_tiles(c);
+    if (rc) return rc;
+  }
+  if (cache_path) {
+    if (FILE* f = std::fopen(cache_path, "a")) {
+      std::fprintf(f, "%s tile=%d ms=%.6f\n", key.c_str(), best, (double)best_ms);
+      std::fclose(f);
+    }
+  }
+  if (tile) *tile = best;
+  if (stage_ms) *stage_ms = best_ms;
+  return EDYN_OK;
+}
+
 int edyn_set_stage_tile(void* ctx, int cells) {
   Ctx* c = (Ctx*)ctx;
   if (!c || !c->qc) return EDYN_E_ARG;

@@ -70,6 +70,7 @@ def lib() -> ctypes.CDLL:
     L.edyn_set_chem_launch.argtypes = [vp, i]
     L.edyn_init_tubes.argtypes = [cp, i, i, i, ip, i, ip, i, dp, i, ctypes.POINTER(vp)]
     L.edyn_tube_times.argtypes = [vp, dp, dp]
+    L.edyn_autotune.argtypes = [vp, cp, ip, dp]
     L.edyn_chem_rhs_tube.argtypes = [vp, i, vp, vp, vp]
     L.edyn_set_surrogate.argtypes = [vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, d, d, d]
     L.edyn_surrogate_stats.argtypes = [vp, dp]
@@ -252,6 +253,14 @@ class Tube(_Ctx):
     def set_stage_tile(self, cells: int = 0) -> None:
         """Cells per fluid stage tile; 0 chooses it from the tube length."""
         self._check(lib().edyn_set_stage_tile(self._h, int(cells)))
+
+    def autotune(self, cache_path=None):
+        """Measures the fluid stage tile on this tube (or reads it from the
+        cache file) and keeps the fastest; returns (tile, stage ms)."""
+        t, ms = ctypes.c_int(), ctypes.c_double()
+        cp_ = None if cache_path is None else str(cache_path).encode()
+        self._check(lib().edyn_autotune(self._h, cp_, ctypes.byref(t), ctypes.byref(ms)))
+        return t.value, ms.value
 
     def stage_tile(self):
         """(cells per stage tile, threads per stage CTA) in use."""

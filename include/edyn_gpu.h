@@ -294,6 +294,16 @@ int edyn_check_log(void* ctx, int n, const double* x, double* max_ulp);
  * tuning knob of this implementation). */
 int edyn_set_stage_tile(void* ctx, int cells);
 
+/* Picks the stage tile by measurement: times one fluid stage for each tile
+ * of 8..62 cells (every second) on the tube's own state with dt = 0, which
+ * leaves the state bit for bit as it was, and keeps the fastest. With a
+ * cache_path (a text file, one line per case), a tile measured before for
+ * the same scheme, species, cell count, tube count and device is read
+ * instead, and a new measurement is appended. tile and stage_ms (either may
+ * be NULL) receive the choice and its stage time. Results do not depend on
+ * the tile. No counterpart in the reference. */
+int edyn_autotune(void* ctx, const char* cache_path, int* tile, double* stage_ms);
+
 /* The stage tile in use: cells per tile and threads per CTA (either may be
  * NULL). No counterpart in the reference. */
 int edyn_stage_tile(void* ctx, int* cells, int* threads);

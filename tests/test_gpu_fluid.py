@@ -249,3 +249,29 @@ def test_device_loop_partial_graphs(oracle, select_time):
     qf_g, _, _ = g.download()
     assert rel(pressure(qf_g, W), pressure(qf_o, W)) < TOL
     assert rel(qf_g[:, 2], qf_o[:, 2]) < TOL
+
+
+def test_autotune_measures_keeps_state_and_caches(tmp_path):
+    """edyn_autotune times the stage tiles on the tube's own state without
+    changing it, keeps a tile in range, writes it to the cache and reads it
+    back; stepping with the tuned tile gives the same tube as the rule's."""
+    case = configs.detonation(ncell=3000)
+    cache = tmp_path / "tiles.txt"
+    runs = []
+    for tune in (False, True):
+        g = Tube(case.ncell, case.dx, flag_acu=2, flag_weno=3, flag_rbound=1, do_reaction=0)
+        g.init_cells(case.T, case.p, case.u, case.X)
+        if tune:
+            before = g.download()[1]
+            tile, ms = g.autotune(cache)
+            assert 8 <= tile <= 62 and ms > 0
+            assert g.stage_tile()[0] == tile
+            assert np.array_equal(g.download()[1], before)
+            assert cache.read_text().count("tile=") == 1
+            assert g.autotune(cache) == (tile, pytest.approx(ms))
+            assert cache.read_text().count("tile=") == 1
+        for _ in range(5):
+            g.step(case.cfl)
+        runs.append(g.download()[:2])
+    for x, y in zip(runs[0], runs[1]):
+        assert np.array_equal(x, y)

@@ -195,6 +195,54 @@ __device__ __forceinline__ R warp_sum(R v) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
 }
+// Lane that holds value i of N after warp_sumv's halving levels.
+__host__ __device__ constexpr int sumv_lane(int i, int n) {
+  int lane = 0;
+  for (int o = 16; o > 0 && n > 1; o >>= 1) {
+    const int h = (n + 1) / 2;
+    if (i >= h) {
+      lane |= o;
+      i -= h;
+    }
+    n = h;
+  }
+  return lane;
+}
+
+// N warp sums at once, bit for bit the sums of warp_sum (the same pairs are
+// added at each level), with fewer additions: at each butterfly level a lane
+// keeps half of the values and adds its partner's copies of them, so N = 7
+// takes 9 additions per lane instead of 35. Every lane receives all N sums.
+template <class R, int N>
+__device__ __forceinline__ void warp_sumv(R (&v)[N]) {
+  const int lane = threadIdx.x & 31;
+  R a[N];
+#pragma unroll
+  for (int j = 0; j < N; ++j) a[j] = v[j];
+  int m = N;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    if (m > 1) {
+      const int h = (m + 1) / 2;
+      const bool low = (lane & o) == 0;
+#pragma unroll
+      for (int j = 0; j < N; ++j) {
+        if (j < h) {
+          const R hi = (h + j < m) ? a[h + j] : (R)0;
+          const R mine = low ? a[j] : hi;
+          const R send = low ? hi : a[j];
+          a[j] = mine + __shfl_xor_sync(0xffffffffu, send, o);
+        }
+      }
+      m = h;
+    } else {
+      a[0] += __shfl_xor_sync(0xffffffffu, a[0], o);
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < N; ++j) v[j] = __shfl_sync(0xffffffffu, a[0], sumv_lane(j, N));
+}
+
 template <class R>
 __device__ __forceinline__ R warp_max(R v) {
 #pragma unroll
@@ -238,8 +286,11 @@ struct Team {
   }
   template <class R, int N>
   __device__ __forceinline__ void sumv(R (&v)[N]) const {
-#pragma unroll
-    for (int j = 0; j < N; ++j) v[j] = warp_sum(v[j]);
+    if constexpr (N == 1) {
+      v[0] = warp_sum(v[0]);
+    } else {
+      warp_sumv(v);
+    }
     if constexpr (TW > 32) {
       R* r = reinterpret_cast<R*>(red);
       if ((tid & 31) == 0) {
@@ -1888,6 +1939,165 @@ __global__ void __launch_bounds__(MAXW * 32, 1)
   }
 }
 
+// ---------------------------------------------------------------------------
+// Single-precision pre-check of the inert-cell test.
+//
+// The inert-cell test of integrate() needs f(y0) in FP64: one full right-hand
+// side per cell, the bulk of a source step on a tube whose cells are mostly
+// cold or burnt out. The pre-check evaluates f in FP32 together with the
+// gross rates g_k = (W_k / rho) sum_r |nu_kr| (qf_r + qr_r) (and their image
+// sum_k |u_k/R| G_k / (rho cv) for T). Every FP32 rate of progress is within
+// a relative DELTA of its FP64 value: its logarithm is a sum of terms below
+// ~300 in magnitude (ln A, beta ln T, E/RT and the S/R - H/RT of at most six
+// species), each good to a few units in the last place of FP32, so DELTA is
+// below 5e-4 even for equilibrium constants at 300 K; products that
+// underflow FP32 lose at most EPS_ABS per second of mass fraction. Then
+//     |f64_i - f32_i| <= DELTA g_i + EPS_ABS,
+// and with KAPPA = 1e-2 (20 x DELTA) a cell whose bound
+//     sqrt(mean_i (dt (|f32_i| + KAPPA g_i + EPS_ABS) / (atol + rtol |y_i|))^2) <= 1e-3
+// passes the FP64 test as well. It takes the explicit step with f32, which
+// differs from the FP64 explicit step by at most DELTA / KAPPA x 1e-3 x
+// sqrt(n) ~ 4e-4 error-weight units per component. A cell with a reaction
+// the FP32 form does not cover (a general-order reaction, or a reverse
+// constant held at the FP32 cap while its products are present), or whose
+// bound is not finite, goes to the FP64 test unchanged.
+// ---------------------------------------------------------------------------
+constexpr float PRE_KAPPA = 1e-2f;
+constexpr float PRE_EPS = 1e-12f;  // per second, mass fraction (and K for T)
+
+// FP32 workspace of the pre-check; it overlays a warp's FP64 right-hand-side
+// arrays (C .. rop of WarpWork and ScreenWork), which it finishes with
+// before an FP64 right-hand side reuses them.
+struct Pre32 {
+  float y[NV], C[NV], m[NV], mi[NV], uR[NV], cvm[NV], f[NV], g[NV];
+  float rop[352], rg[352];
+  float part[100], pg[100];
+};
+
+// One reaction's forward and reverse rates of progress in FP32. Returns
+// true when the FP32 value is not covered by the DELTA bound.
+__device__ __forceinline__ bool rxn32(const Tabs& t, int i, float logT, float invT, float T, float pfac,
+                                      float ipfac, float ctot, const float* C, const float* m, const float* mi,
+                                      const int* en, float& qf, float& qr) {
+  const RTabs<float>& x = t.f;
+  const unsigned w0 = t.w0[i], w1 = t.w1[i], w2 = t.w2[i];
+  const unsigned fl = w0 >> 24;
+  qf = qr = 0.f;
+  if (fl & F_GEN) return true;
+  const float lkf = x.lnA[i] + x.B[i] * logT - x.E[i] * invT;  // ln kf
+  float kf = __expf(lkf), kr = 0.f;
+  bool capped = false;
+  if (fl & F_REV) {
+    const float k0 = kf * inv_kc<float>(w0, w1, w2, pfac, ipfac, m, mi, en);
+    capped = !(k0 < 1e30f);
+    kr = capped ? 1e30f : k0;
+  }
+  if (fl & (F_CM | F_KFAL)) {
+    const int aux = (int)(w2 >> 24);
+    const float cm = collider<float>(t, fl, aux, ctot, C);
+    if (fl & F_FALL) {
+      const float* fp = x.aux + aux * AUXW;
+      // Pr = k0 [M] / kinf with k0 / kinf taken in logarithms (no 0/0 when
+      // both underflow)
+      const float pr = __expf(fp[8] + fp[1] * logT - fp[2] * invT - lkf) * cm;
+      const int ifop = (int)fp[7];
+      const float fclog = (ifop > 1) ? troe_fclog<float>(t, fp, ifop, T, invT) : 0.f;
+      const float pcor = falloff_pcor<float>(t, pr, ifop, fclog);
+      kf *= pcor;
+      kr *= pcor;
+    } else {
+      kf *= cm;
+      kr *= cm;
+    }
+  }
+  qf = kf;
+  qr = kr;
+  mass_action<float>(w0, w1, w2, C, qf, qr);
+  return capped && qr > 0.f;
+}
+
+// FP32 right-hand side of s.y (one warp) into s.f and its gross rates into
+// s.g. Returns true (on every lane) when a reaction is not covered.
+__device__ bool rhs32_bound(const Tabs& t, int lane, Pre32& s, int* en, float rho) {
+  const RTabs<float>& x = t.f;
+  const Team<32> tm{lane, 0, nullptr, nullptr, nullptr, nullptr};
+  const int ns = t.ns;
+  const float T = s.y[ns];
+  const float logT = __logf(T), invT = 1.f / T;
+  const float pfac = (float)(PATM_CGS / RU_CGS) * invT;
+  const float ipfac = T * (float)(RU_CGS / PATM_CGS);
+  const float ctot =
+      species_pass<float, 32>(t, tm, s.y, rho, T, logT, invT, pfac, ipfac, s.C, s.m, s.mi, en, s.uR, s.cvm);
+  __syncwarp();
+  bool bad = false;
+  for (int i = lane; i < t.nrp; i += 32) {
+    float qf = 0.f, qr = 0.f;
+    if (i < t.nr) bad |= rxn32(t, i, logT, invT, T, pfac, ipfac, ctot, s.C, s.m, s.mi, en, qf, qr);
+    s.rop[i] = qf - qr;
+    s.rg[i] = qf + qr;
+  }
+  __syncwarp();
+  for (int p = t.lane[lane]; p < t.lane[lane + 1]; ++p) {
+    const int e0 = t.pc[p * 3 + 1], e1 = t.pc[p * 3 + 2];
+    float a = 0.f, b = 0.f;
+    for (int q = e0; q < e1; ++q) {
+      const float nu = x.nu[q];
+      const unsigned r = t.ent[q];
+      a = fmaf(nu, s.rop[r], a);
+      b = fmaf(fabsf(nu), s.rg[r], b);
+    }
+    s.part[p] = a;
+    s.pg[p] = b;
+  }
+  __syncwarp();
+  float v[3] = {0.f, 0.f, 0.f};  // sum u/R w, sum |u/R| G, cv / R
+  for (int k = lane; k < ns; k += 32) {
+    float a = 0.f, b = 0.f;
+    for (int q = t.spc[k]; q < t.spc[k + 1]; ++q) {
+      const int pp = t.spp[q];
+      a += s.part[pp];
+      b += s.pg[pp];
+    }
+    const float wr = x.W[k] / rho;
+    s.f[k] = a * wr;
+    s.g[k] = b * wr;
+    v[0] = fmaf(s.uR[k], a, v[0]);
+    v[1] = fmaf(fabsf(s.uR[k]), b, v[1]);
+    v[2] = fmaf(s.y[k], s.cvm[k], v[2]);
+  }
+  tm.sumv(v);
+  if (lane == 0) {
+    s.f[ns] = -v[0] / (rho * v[2]);
+    s.g[ns] = v[1] / (rho * v[2]);
+  }
+  __syncwarp();
+  return __any_sync(0xffffffffu, bad);
+}
+
+// The pre-check on one cell (one warp): y0 holds the adjusted [Y, T] in
+// FP64. When the bound passes, y0 takes the explicit step y0 + dt f32 and
+// the call returns true; otherwise y0 is left as it was.
+__device__ bool precheck_inert(const Tabs& t, int lane, Pre32& s, int* en, double* y0, double rho_cgs, double dt,
+                               double rtol, double atol, float nn) {
+  const int n = t.ns + 1;
+  for (int i = lane; i < n; i += 32) s.y[i] = (float)y0[i];
+  __syncwarp();
+  const bool bad = rhs32_bound(t, lane, s, en, (float)rho_cgs);
+  const float dtf = (float)dt;
+  float ss = 0.f;
+  for (int i = lane; i < n; i += 32) {
+    const float tol = (float)(atol + rtol * fabs(y0[i]));
+    const float z = dtf * (fabsf(s.f[i]) + fmaf(PRE_KAPPA, s.g[i], PRE_EPS)) / tol;
+    ss = fmaf(z, z, ss);
+  }
+  const float nrm = sqrtf(warp_sum(ss) / nn);
+  // the norm is itself rounded in FP32: a 1 % margin below the test's 1e-3
+  if (bad || !(nrm <= 0.99e-3f)) return false;
+  for (int i = lane; i < n; i += 32) y0[i] = fma(dt, (double)s.f[i], y0[i]);
+  __syncwarp();
+  return true;
+}
+
 // Packed tubes: a cell's column in the rows (its tube's block offset + its
 // index) and its tube's dt; a single tube: the cell index and the launch's dt.
 __device__ __forceinline__ size_t cell_col(const ChemLaunch& L, unsigned cell) {
@@ -1930,6 +2140,22 @@ __device__ int tube_cell(const Tabs& t, const Team<TW>& tm, WarpWork& w, const C
   for (int k = tid; k < ns; k += TW) w.y0[k] *= inv_s;
   if (tid == 0) w.y0[ns] = q[2 * ld];
   tm.sync();
+  if constexpr (TW == 32) {
+    // the single-precision pre-check: an inert cell without the FP64 f(y0)
+    static_assert(sizeof(Pre32) <= offsetof(WarpWork, en) - offsetof(WarpWork, C), "Pre32 overlay");
+    if (L.precheck &&
+        precheck_inert(t, tid, *reinterpret_cast<Pre32*>(w.C), w.en, w.y0, rho * 1e-3, dt, L.rtol, L.atol,
+                       (float)t.h->nnorm)) {
+      if (tid == 0) {
+        if (L.hlast) L.hlast[cell] = dt;
+        atomicAdd(&cnt->steps, 1ull);
+        atomicAdd(&cnt->cells, 1ull);
+        atomicAdd(&cnt->cells32, 1ull);
+      }
+      finish_cell<TW, WarpWork>(t, tm, w, L, cell, dt, speed_max);
+      return 1;
+    }
+  }
   // start from the first accepted step of this cell's last window
   const double hl = L.hlast ? L.hlast[cell] : 0.0;
   Cell c{rho * 1e-3, dt, L.rtol, L.atol, (hl > 0.0 && hl < dt) ? hl : dt, L.max_steps, L.screen != 0};
@@ -2000,7 +2226,8 @@ __device__ void finish_cell(const Tabs& t, const Team<TW>& tm, Wk& w, const Chem
   const double Tn = w.y0[ns];
   // heat release rate, SRC/thermo.f90:83-103 (qf rows still hold Y0 raw)
   const double rho_cgs = rho * 1e-3;
-  double hsum[3] = {0.0, 0.0, 0.0};  // hr, hs, sz
+  const bool warm = !L.strict_newton;
+  double hsum[4] = {0.0, 0.0, 0.0, 0.0};  // hr, hs, sz and (warm Newton start) cp
   for (int k = tid; k < ns; k += TW) {
     const double yn = w.y0[k] * inv2;
     w.y0[k] = yn;
@@ -2017,6 +2244,14 @@ __device__ void finish_cell(const Tabs& t, const Team<TW>& tm, Wk& w, const Chem
     const double z = yn * t.d.invW[k];
     hsum[1] = fma(z, hh, hsum[1]);
     hsum[2] += z;
+    if (warm) {
+      const double* cc = t.d.cp + r * 5 * NSMAX;
+      double cp = fma(cc[4 * NSMAX + k], Tn, cc[3 * NSMAX + k]);
+      cp = fma(cp, Tn, cc[2 * NSMAX + k]);
+      cp = fma(cp, Tn, cc[1 * NSMAX + k]);
+      cp = fma(cp, Tn, cc[0 * NSMAX + k]);
+      hsum[3] = fma(z, cp, hsum[3]);
+    }
   }
   tm.sumv(hsum);
   const double u = q[ld];
@@ -2039,6 +2274,15 @@ __device__ void finish_cell(const Tabs& t, const Team<TW>& tm, Wk& w, const Chem
   const double E = (rhoe / rho - 0.5 * (u * u)) / R_SI;
   double gN = 1e30, dTN = 1e30;
   int it = 0;
+  if (warm) {
+    // the first Newton step from T = Tn takes the mixture's H/R, S_z and
+    // cp/R at Tn from the sums above (the same species intervals as the
+    // premixed coefficients below would use; equal to them up to rounding)
+    gN = hsum[1] - Tn * hsum[2] - E;
+    dTN = -gN / (hsum[3] - hsum[2]);
+    T = fmax(20.0, fmin(6000.0, T + dTN));
+    it = 1;
+  }
   while (fabs(gN) >= fabs(E) * 1e-9 && fabs(dTN) >= T * 1e-6 && it < 10) {
     // premixed NASA coefficients at the current T (threads over species)
     double A[7] = {0, 0, 0, 0, 0, 0, 0};
@@ -2298,6 +2542,7 @@ struct alignas(16) ScreenWork {
   double rop[352];
   int en[NV];
 };
+static_assert(sizeof(Pre32) <= offsetof(ScreenWork, en) - offsetof(ScreenWork, C), "Pre32 overlay");
 constexpr int SCREEN_WARPS = 16;
 
 // Screening pass of a tube's source step. Every cell: y0 = adjust_sum(Y),
@@ -2324,7 +2569,7 @@ __global__ void __launch_bounds__(SCREEN_WARPS * 32, 1)
   const float nn = (float)t.h->nnorm;
   const int nw = blockDim.x >> 5;
   double speed_max = 0.0;
-  unsigned long long done = 0, listed = 0;
+  unsigned long long done = 0, listed = 0, done32 = 0, rhs64n = 0;
   for (unsigned cell = blockIdx.x * nw + (threadIdx.x >> 5); cell < (unsigned)L.n; cell += gridDim.x * nw) {
     if (!cell_active(L, cell)) continue;
     const double dt = cell_dt(L, cell, dt_launch);
@@ -2341,16 +2586,28 @@ __global__ void __launch_bounds__(SCREEN_WARPS * 32, 1)
     for (int k = lane; k < ns; k += 32) w.y0[k] *= inv_s;
     if (lane == 0) w.y0[ns] = q[2 * ld];
     __syncwarp();
-    rhs<double, 32>(t, tm, w, w.y0, rho * 1e-3, w.fy, w.C, w.m, w.mi, w.uR, w.cvm, w.rop, w.part);
-    float ss = 0.f;
-    for (int i = lane; i < n; i += 32) {
-      const float z = (float)(dt * w.fy[i] / (L.atol + L.rtol * fabs(w.y0[i])));
-      ss = fmaf(z, z, ss);
+    // the single-precision pre-check first; the FP64 f(y0) and test where it
+    // does not decide
+    bool inert = L.precheck && precheck_inert(t, lane, *reinterpret_cast<Pre32*>(w.C), w.en, w.y0, rho * 1e-3, dt,
+                                              L.rtol, L.atol, nn);
+    if (inert) {
+      ++done32;
+    } else {
+      rhs<double, 32>(t, tm, w, w.y0, rho * 1e-3, w.fy, w.C, w.m, w.mi, w.uR, w.cvm, w.rop, w.part);
+      ++rhs64n;
+      float ss = 0.f;
+      for (int i = lane; i < n; i += 32) {
+        const float z = (float)(dt * w.fy[i] / (L.atol + L.rtol * fabs(w.y0[i])));
+        ss = fmaf(z, z, ss);
+      }
+      const float nrm = sqrtf(warp_sum(ss) / nn);
+      if (nrm <= 1e-3f) {
+        for (int i = lane; i < n; i += 32) w.y0[i] = fma(dt, w.fy[i], w.y0[i]);
+        __syncwarp();
+        inert = true;
+      }
     }
-    const float nrm = sqrtf(warp_sum(ss) / nn);
-    if (nrm <= 1e-3f) {
-      for (int i = lane; i < n; i += 32) w.y0[i] = fma(dt, w.fy[i], w.y0[i]);
-      __syncwarp();
+    if (inert) {
       finish_cell<32, ScreenWork>(t, tm, w, L, cell, dt, speed_max);
       if (lane == 0) {
         if (L.cost) L.cost[cell] = 1;
@@ -2392,12 +2649,13 @@ __global__ void __launch_bounds__(SCREEN_WARPS * 32, 1)
     __syncwarp();
   }
   if (lane == 0) {
+    // FP64 right-hand sides: every cell the pre-check did not decide
+    if (rhs64n) atomicAdd(&cnt->rhs, rhs64n);
     if (done) {
-      atomicAdd(&cnt->rhs, done);
       atomicAdd(&cnt->steps, done);
       atomicAdd(&cnt->cells, done);
     }
-    if (listed) atomicAdd(&cnt->rhs, listed);
+    if (done32) atomicAdd(&cnt->cells32, done32);
     if (L.cvel_out && speed_max > 0.0)
       atomicMax(L.cvel_out, (unsigned long long)__double_as_longlong(speed_max));
   }

@@ -13,6 +13,7 @@ constexpr int HOT_MAX = 64;
 
 struct ChemCounters {
   unsigned long long rhs, steps, rejects, failed, jac, cells, team_cells;
+  unsigned long long cells32;  // inert cells decided by the single-precision pre-check
 };
 
 struct ChemState {
@@ -76,6 +77,8 @@ struct ChemLaunch {
   unsigned long long* cvel_tube;
   double* time_tube;
   int ntube;
+  // single-precision pre-check of the inert-cell test (tube mode, single warps)
+  int precheck;
 };
 
 // smap: tube row of each species of m (3 + smap[k]) when m is a subset of the

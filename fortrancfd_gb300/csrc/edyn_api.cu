@@ -115,6 +115,7 @@ struct Ctx {
   int hrr_dot_state = 0;
   double* hrr_dot_rows = nullptr;  // primitive rows the last source step left
   int chem_max_steps = 0;     // integrator step cap per cell (0: the default 4000)
+  int precheck = 1;           // single-precision pre-check of the inert-cell test
   double* staging = nullptr;
   size_t staging_bytes = 0;
   // device clock of the time loop
@@ -325,6 +326,7 @@ int source_step(Ctx* c, double dt, bool dev) {
   L.hlast = c->d_hlast;
   L.tchem = c->tchem;
   L.max_steps = c->chem_max_steps;
+  L.precheck = c->precheck;
   if (c->pk.ntube) {
     const Packed& k = c->pk;
     L.colmap = k.colmap;
@@ -390,6 +392,7 @@ int surrogate_source_step(Ctx* c, double dt, bool dev) {
   L.hlast = c->d_hlast;
   L.tchem = c->tchem;
   L.max_steps = c->chem_max_steps;
+  L.precheck = c->precheck;
   L.screen = 1;
   L.pk_count = z.d_count;
   L.pk_idx = z.pk_idx;
@@ -1420,6 +1423,15 @@ int edyn_set_chem_launch(void* ctx, int form) {
   return EDYN_OK;
 }
 
+int edyn_set_chem_precheck(void* ctx, int on) {
+  Ctx* c = (Ctx*)ctx;
+  if (!c || !c->qc) return EDYN_E_ARG;
+  if (on != 0 && on != 1) return fail(c, EDYN_E_ARG, "precheck=%d must be 0 or 1", on);
+  c->precheck = on;
+  drop_graph(c);
+  return EDYN_OK;
+}
+
 int edyn_set_chem_max_steps(void* ctx, int max_steps) {
   Ctx* c = (Ctx*)ctx;
   if (!c || !c->qc) return EDYN_E_ARG;
@@ -1435,8 +1447,8 @@ int edyn_chem_stats(void* ctx, double* stats) {
   ChemCounters k;
   cudaError_t e = chem_read_counters(c->use_sub ? c->chem_sub : c->chem, &k, c->stream);
   if (e != cudaSuccess) return fail(c, EDYN_E_CUDA, "counters: %s", cudaGetErrorString(e));
-  const unsigned long long v[7] = {k.rhs, k.steps, k.rejects, k.failed, k.jac, k.cells, k.team_cells};
-  for (int i = 0; i < 7; ++i) stats[i] = (double)v[i];
+  const unsigned long long v[8] = {k.rhs, k.steps, k.rejects, k.failed, k.jac, k.cells, k.team_cells, k.cells32};
+  for (int i = 0; i < 8; ++i) stats[i] = (double)v[i];
   return EDYN_OK;
 }
 

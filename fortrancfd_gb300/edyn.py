@@ -68,6 +68,7 @@ def lib() -> ctypes.CDLL:
     L.edyn_download_source.argtypes = [vp, dp, dp]
     L.edyn_set_chem_max_steps.argtypes = [vp, i]
     L.edyn_set_chem_launch.argtypes = [vp, i]
+    L.edyn_set_chem_precheck.argtypes = [vp, i]
     L.edyn_init_tubes.argtypes = [cp, i, i, i, ip, i, ip, i, dp, i, ctypes.POINTER(vp)]
     L.edyn_tube_times.argtypes = [vp, dp, dp]
     L.edyn_autotune.argtypes = [vp, cp, ip, dp]
@@ -224,9 +225,9 @@ class Tube(_Ctx):
 
     def chem_stats(self) -> dict:
         """Counters of the last chemistry launch."""
-        st = np.zeros(7)
+        st = np.zeros(8)
         self._check(lib().edyn_chem_stats(self._h, _ptr(st)))
-        keys = ("rhs", "steps", "rejects", "failed", "jac", "cells", "team_cells")
+        keys = ("rhs", "steps", "rejects", "failed", "jac", "cells", "team_cells", "cells32")
         return {k: int(v) for k, v in zip(keys, st)}
 
     def chem_cost(self):
@@ -249,6 +250,11 @@ class Tube(_Ctx):
         """Chemistry launch form: 0 automatic, 1 one pass, 2 screening pass +
         listed integration (the same results)."""
         self._check(lib().edyn_set_chem_launch(self._h, int(form)))
+
+    def set_chem_precheck(self, on: bool = True) -> None:
+        """Single-precision pre-check of the inert-cell test (on by default):
+        cells it decides skip the FP64 right-hand side."""
+        self._check(lib().edyn_set_chem_precheck(self._h, 1 if on else 0))
 
     def set_stage_tile(self, cells: int = 0) -> None:
         """Cells per fluid stage tile; 0 chooses it from the tube length."""

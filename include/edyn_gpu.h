@@ -206,6 +206,18 @@ int edyn_chem_rhs_tube(void* ctx, int n, const double* rho_d, const double* yiT_
  * counterpart in the reference (a tuning knob of this implementation). */
 int edyn_set_chem_launch(void* ctx, int form);
 
+/* The single-precision pre-check of the integrator's inert-cell test (tube
+ * chemistry; on by default). A cell's FP32 right-hand side and gross rates
+ * bound its FP64 right-hand side; when the bound already passes the inert
+ * test (the whole window's change below 1e-3 of the error tolerance), the
+ * cell takes its explicit step with the FP32 right-hand side, which differs
+ * from the FP64 one's by under 1e-3 of the tolerance, and no FP64 right-hand
+ * side is evaluated. Other cells go through the FP64 test as before. on = 0
+ * turns it off (every cell gets the FP64 test). No counterpart in the
+ * reference, which integrates every cell with its full solver
+ * (SRC/source.f90:58). */
+int edyn_set_chem_precheck(void* ctx, int on);
+
 /* Caps the implicit integrator at max_steps steps (accepted + rejected) per
  * cell and call; a cell that reaches the cap fails and the call returns
  * EDYN_E_CHEM. 0 restores the default (4000). No counterpart in the
@@ -256,8 +268,10 @@ int edyn_reactors(void* ctx, int n, const double* rho, const double* dt, double*
 int edyn_reactors_device(void* ctx, int n, const double* rho_d, const double* dt_d, double* yiT_d, double* stats);
 
 /* Counters of the last chemistry launch of this context (tube or batch),
- * 7 values: right-hand-side evaluations, accepted steps, rejected steps,
- * failed cells, Jacobians, cells, cells integrated by a four-warp team.
+ * 8 values: FP64 right-hand-side evaluations, accepted steps, rejected
+ * steps, failed cells, Jacobians, cells, cells integrated by a four-warp
+ * team, inert cells decided by the single-precision pre-check (no FP64
+ * right-hand side; see edyn_set_chem_precheck).
  * No counterpart in the reference, which reports none (its solver's
  * statistics stay inside macks, SRC/source.f90:58). */
 int edyn_chem_stats(void* ctx, double* stats);

@@ -254,3 +254,36 @@ def test_chemistry_launch_forms_agree(oracle, names):
     assert np.max(np.abs(a[:, 0] - b[:, 0]) / b[:, 0]) < 1e-8
     rel_err, abs_err = species_err(a[:, 3:], b[:, 3:])
     assert rel_err < 1e-5 and abs_err < 1e-12, (rel_err, abs_err)
+
+
+def test_single_precision_precheck_agrees_with_fp64_test():
+    """The FP32 pre-check of the inert-cell test decides the cold mixture
+    ahead of a detonation front without an FP64 right-hand side, in both
+    launch forms, and the tube agrees with the same run with every cell
+    through the FP64 test within the integrator's tolerance: a decided
+    cell's step differs by under 1e-3 of its error tolerance, and the
+    integrations that follow in its neighbours may then take other step
+    sequences (the bar of the launch forms, a few rtol)."""
+    case = configs.detonation(ncell=1024, length=1024 * 50e-6, driver=96 * 50e-6)
+    for form in (1, 2):
+        out, stats = [], []
+        for pre in (True, False):
+            g = Tube(case.ncell, case.dx, flag_acu=2, flag_weno=3, flag_rbound=1, do_reaction=1, rtol=1e-6,
+                     atol=1e-14)
+            g.set_chem_launch(form)
+            g.set_chem_precheck(pre)
+            g.init_cells(case.T, case.p, case.u, case.X)
+            for _ in range(6):
+                g.step(case.cfl)
+            stats.append(g.chem_stats())
+            out.append(g.download()[0])
+            g.close()
+        on, off = stats
+        assert off["cells32"] == 0
+        assert on["cells32"] > case.ncell // 2, on
+        assert on["rhs"] < off["rhs"] - on["cells32"] // 2, (on, off)
+        a, b = out
+        assert np.max(np.abs(a[:, 2] - b[:, 2]) / b[:, 2]) < 1e-8
+        assert np.max(np.abs(a[:, 0] - b[:, 0]) / b[:, 0]) < 1e-8
+        rel_err, abs_err = species_err(a[:, 3:], b[:, 3:])
+        assert rel_err < 1e-5 and abs_err < 1e-12, (form, rel_err, abs_err)

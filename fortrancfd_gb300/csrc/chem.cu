@@ -261,6 +261,12 @@ struct Team {
   double* part4;  // gather partial sums, [4][TEAM_PIECES] (four-warp teams)
   double* pre;    // temperature-only rate parts, 480 doubles (four-warp teams)
   float* jsave;   // the Jacobian kept across steps (four-warp teams; warps rebuild it)
+  // per-warp partial Jacobians and collider rows of warps 1-3 (four-warp
+  // teams): each warp accumulates its reactions' terms in its own buffers,
+  // which are then added in warp order, so the result does not depend on
+  // how the warps' shared-memory atomics interleave
+  float* jp[3];
+  float* rp[3];
   __device__ __forceinline__ void sync() const {
     if constexpr (TW == 32) {
       __syncwarp();
@@ -1182,6 +1188,19 @@ __device__ void jacobian32(const Tabs& t, const Team<TW>& tm, WarpWork& w, const
   float* partf = (float*)w.part;
   float* rowc = (float*)w.sv;  // per-species collider coefficients
   for (int q = tid; q < n * JS; q += TW) J[q] = 0.f;
+  float* Jw = J;      // this thread's accumulation target
+  float* rw = rowc;
+  if constexpr (TW > 32) {
+    for (int b = 0; b < 3; ++b) {
+      for (int q = tid; q < n * JS; q += TW) tm.jp[b][q] = 0.f;
+      for (int q = tid; q < n; q += TW) tm.rp[b][q] = 0.f;
+    }
+    const int wq = tid >> 5;
+    if (wq > 0) {
+      Jw = wq == 1 ? tm.jp[0] : (wq == 2 ? tm.jp[1] : tm.jp[2]);
+      rw = wq == 1 ? tm.rp[0] : (wq == 2 ? tm.rp[1] : tm.rp[2]);
+    }
+  }
   const float T = (float)y[ns];
   const float dT = fmaxf(1e-3f * T, 0.05f);
   const float rho = (float)rho_cgs;
@@ -1234,7 +1253,7 @@ __device__ void jacobian32(const Tabs& t, const Team<TW>& tm, WarpWork& w, const
           if (q >= nk) break;
           const unsigned kq = q < 4 ? ((w3 >> (8 * q)) & 0xff) : ((w4 >> (8 * (q - 4))) & 0xff);
           const int nuq = (int)(q < 4 ? ((w4 >> (16 + 4 * q)) & 15) : ((w5 >> (4 * (q - 4))) & 15)) - 8;
-          atomicAdd(&J[kq * JS + kj], (float)nuq * d);
+          atomicAdd(&Jw[kq * JS + kj], (float)nuq * d);
         }
       }
     }
@@ -1250,18 +1269,25 @@ __device__ void jacobian32(const Tabs& t, const Team<TW>& tm, WarpWork& w, const
           const unsigned kq = q < 4 ? ((w3 >> (8 * q)) & 0xff) : ((w4 >> (8 * (q - 4))) & 0xff);
           const int nuq = (int)(q < 4 ? ((w4 >> (16 + 4 * q)) & 15) : ((w5 >> (4 * (q - 4))) & 15)) - 8;
           if (fl & F_KFAL) {
-            atomicAdd(&J[kq * JS + t.spi[aux * 4 + 2]], (float)nuq * r0);
+            atomicAdd(&Jw[kq * JS + t.spi[aux * 4 + 2]], (float)nuq * r0);
           } else {
-            atomicAdd(&rowc[kq], (float)nuq * r0);
+            atomicAdd(&rw[kq], (float)nuq * r0);
             const int b = t.spi[aux * 4 + 0], c = t.spi[aux * 4 + 1];
             for (int q2 = b; q2 < b + c; ++q2)
-              atomicAdd(&J[kq * JS + t.tb_sp[q2]], (float)nuq * r0 * x.tb_am1[q2]);
+              atomicAdd(&Jw[kq * JS + t.tb_sp[q2]], (float)nuq * r0 * x.tb_am1[q2]);
           }
         }
       }
     }
   }
   __syncwarp();
+  if constexpr (TW > 32) {
+    // the warps' partial sums in warp order
+    tm.sync();
+    for (int q = tid; q < n * JS; q += TW) J[q] = ((J[q] + tm.jp[0][q]) + tm.jp[1][q]) + tm.jp[2][q];
+    for (int q = tid; q < n; q += TW) rowc[q] = ((rowc[q] + tm.rp[0][q]) + tm.rp[1][q]) + tm.rp[2][q];
+    tm.sync();
+  }
   // to mass-fraction space: d f_k / d y_j = (W_k / W_j) (d w_k / d C_j + rowc_k);
   // T row d f_T / d y_j = -(sum_k e_k J_kj + f_T cvm_j) / cv with e_k = u_k/W_k.
   float cv = 0.f;
@@ -2227,12 +2253,12 @@ __device__ void finish_cell(const Tabs& t, const Team<TW>& tm, Wk& w, const Chem
   // heat release rate, SRC/thermo.f90:83-103 (qf rows still hold Y0 raw)
   const double rho_cgs = rho * 1e-3;
   const bool warm = !L.strict_newton;
-  double hsum[4] = {0.0, 0.0, 0.0, 0.0};  // hr, hs, sz and (warm Newton start) cp
+  double hsum[4] = {0.0, 0.0, 0.0, 0.0};  // hr / rho, hs, sz and (warm start) cp
   for (int k = tid; k < ns; k += TW) {
     const double yn = w.y0[k] * inv2;
     w.y0[k] = yn;
     const double y0raw = q[(3 + t.smap[k]) * ld];
-    hsum[0] = fma(rho_cgs * t.d.hf[k], yn - y0raw, hsum[0]);
+    hsum[0] = fma(t.d.hf[k], yn - y0raw, hsum[0]);
     // qfToQc energy: e = R (H(T) - T Sz)/S_Y with the adjusted Y (S_Y = 1)
     const int r = (Tn > t.d.tmid[k]) ? 1 : 0;
     const double* ch = t.d.ch + r * 6 * NSMAX;
@@ -2255,8 +2281,9 @@ __device__ void finish_cell(const Tabs& t, const Team<TW>& tm, Wk& w, const Chem
   }
   tm.sumv(hsum);
   const double u = q[ld];
-  const double e_int = R_SI * (hsum[1] - Tn * hsum[2]);
-  const double rhoe = rho * (e_int + 0.5 * (u * u));
+  // e/R of the adjusted state at the integration's final T
+  const double E = hsum[1] - Tn * hsum[2];
+  const double rhoe = rho * fma(R_SI, E, 0.5 * (u * u));
   // write Qc = qfToQc(qf) and qf (T, Y); the post-step QcToqf then
   // recovers T from rho e with the Newton solve.
   tm.sync();  // every thread has read the raw Y rows
@@ -2266,23 +2293,17 @@ __device__ void finish_cell(const Tabs& t, const Team<TW>& tm, Wk& w, const Chem
   }
   if (tid == 0) {
     Q[2 * ld] = rhoe;
-    L.hrr[cell] = -(hsum[0] / dt) * 1e-1;
+    L.hrr[cell] = -((rho_cgs * hsum[0]) / dt) * 1e-1;
   }
   tm.sync();
-  // post-step QcToqf: Newton on rho e for T (from 1000 K when strict)
+  // post-step QcToqf: T from rho e (E = e/R). From 1000 K (strict) Newton
+  // iterates as the reference does. Warm-started at Tn, its first residual
+  // H(Tn) - Tn Sz - E is zero by construction (rho e was just formed from
+  // the same sums at Tn), so T = Tn and the loop does not run.
   double T = L.strict_newton ? 1000.0 : Tn;
-  const double E = (rhoe / rho - 0.5 * (u * u)) / R_SI;
   double gN = 1e30, dTN = 1e30;
   int it = 0;
-  if (warm) {
-    // the first Newton step from T = Tn takes the mixture's H/R, S_z and
-    // cp/R at Tn from the sums above (the same species intervals as the
-    // premixed coefficients below would use; equal to them up to rounding)
-    gN = hsum[1] - Tn * hsum[2] - E;
-    dTN = -gN / (hsum[3] - hsum[2]);
-    T = fmax(20.0, fmin(6000.0, T + dTN));
-    it = 1;
-  }
+  if (warm) gN = dTN = 0.0;
   while (fabs(gN) >= fabs(E) * 1e-9 && fabs(dTN) >= T * 1e-6 && it < 10) {
     // premixed NASA coefficients at the current T (threads over species)
     double A[7] = {0, 0, 0, 0, 0, 0, 0};
@@ -2325,27 +2346,32 @@ __device__ void finish_cell(const Tabs& t, const Team<TW>& tm, Wk& w, const Chem
       bad |= EDYN_STATUS_STATE;
     if (bad) atomicOr(L.err, bad);
   }
-  // signal speed of the new state for the next time step
+  // signal speed of the new state for the next time step (warm: T = Tn,
+  // whose cp/R and S_z the sums above hold)
   if (L.cvel_out || L.cvel_tube) {
-    double a[6] = {0, 0, 0, 0, 0, 0};
-    for (int k = tid; k < ns; k += TW) {
-      const int r = (T > t.d.tmid[k]) ? 1 : 0;
-      const double* ch = t.d.ch + r * 6 * NSMAX;
-      const double z = w.y0[k] * t.d.invW[k];
-      a[0] = fma(z, ch[0 * NSMAX + k], a[0]);
-      a[1] = fma(z, ch[1 * NSMAX + k], a[1]);
-      a[2] = fma(z, ch[2 * NSMAX + k], a[2]);
-      a[3] = fma(z, ch[3 * NSMAX + k], a[3]);
-      a[4] = fma(z, ch[4 * NSMAX + k], a[4]);
-      a[5] += z;
+    double cp = hsum[3], Sz = hsum[2];
+    if (!warm) {
+      double a[6] = {0, 0, 0, 0, 0, 0};
+      for (int k = tid; k < ns; k += TW) {
+        const int r = (T > t.d.tmid[k]) ? 1 : 0;
+        const double* ch = t.d.ch + r * 6 * NSMAX;
+        const double z = w.y0[k] * t.d.invW[k];
+        a[0] = fma(z, ch[0 * NSMAX + k], a[0]);
+        a[1] = fma(z, ch[1 * NSMAX + k], a[1]);
+        a[2] = fma(z, ch[2 * NSMAX + k], a[2]);
+        a[3] = fma(z, ch[3 * NSMAX + k], a[3]);
+        a[4] = fma(z, ch[4 * NSMAX + k], a[4]);
+        a[5] += z;
+      }
+      tm.sumv(a);
+      cp = fma(5.0 * a[4], T, 4.0 * a[3]);
+      cp = fma(cp, T, 3.0 * a[2]);
+      cp = fma(cp, T, 2.0 * a[1]);
+      cp = fma(cp, T, a[0]);
+      Sz = a[5];
     }
-    tm.sumv(a);
-    double cp = fma(5.0 * a[4], T, 4.0 * a[3]);
-    cp = fma(cp, T, 3.0 * a[2]);
-    cp = fma(cp, T, 2.0 * a[1]);
-    cp = fma(cp, T, a[0]);
-    const double gamma = cp / (cp - a[5]);
-    const double sp = fabs(u) + sqrt(gamma * R_SI * T * a[5]);
+    const double gamma = cp / (cp - Sz);
+    const double sp = fabs(u) + sqrt(gamma * R_SI * T * Sz);
     if (L.cvel_tube) {
       if (tid == 0) atomicMax(L.cvel_tube + L.tube_of[cell], (unsigned long long)__double_as_longlong(sp));
     } else {
@@ -2454,7 +2480,11 @@ __global__ void __launch_bounds__(MAXW * 32, 1)
     if (warp < TEAM / 32 && work) {
       // team scratch: the second work slot, unused while the team runs
       double* spare = reinterpret_cast<double*>(&ww[1]);
-      const Team<TEAM> tm{(int)threadIdx.x, 1, spare, spare + 256, spare + 768, ww[2].J};
+      // the Jacobian partials of warps 1-3 go to work slots the team does not
+      // otherwise use while it evaluates one (slot 0's matrix is rebuilt
+      // from the Jacobian afterwards)
+      const Team<TEAM> tm{(int)threadIdx.x, 1, spare, spare + 256, spare + 768, ww[2].J,
+                          {ww[0].J, ww[1].J, ww[3].J}, {ww[0].b32, ww[1].b32, ww[3].b32}};
       const int c = tube_cell<TEAM>(t, tm, ww[0], L, cell, dt, speed_max, cnt);
       if (threadIdx.x == 0 && L.cost) L.cost[cell] = c;
     }

@@ -116,6 +116,7 @@ struct Ctx {
   double* hrr_dot_rows = nullptr;  // primitive rows the last source step left
   int chem_max_steps = 0;     // integrator step cap per cell (0: the default 4000)
   int precheck = 1;           // single-precision pre-check of the inert-cell test
+  int skip_uniform = 1;       // stage: no faces for cells whose stencils hold one state
   double* staging = nullptr;
   size_t staging_bytes = 0;
   // device clock of the time loop
@@ -211,6 +212,7 @@ StageArgs base_args(Ctx* c) {
   a.strict_newton = c->strict;
   a.bc = c->bc;
   a.err = c->d_err;
+  a.skip_uniform = c->skip_uniform;
   if (c->pk.ntube) {
     const Packed& k = c->pk;
     a.tubes = TubeTab{k.d_tiles, k.d_n, k.d_off, k.d_dx, k.d_p_out, k.d_dt, k.d_active, k.d_time, k.ntiles};
@@ -1419,6 +1421,15 @@ int edyn_set_chem_launch(void* ctx, int form) {
   if (!c || !c->qc) return EDYN_E_ARG;
   if (form < 0 || form > 2) return fail(c, EDYN_E_ARG, "chemistry launch form %d not in 0..2", form);
   c->listed = form == 2 || (form == 0 && c->n >= 50000);
+  drop_graph(c);
+  return EDYN_OK;
+}
+
+int edyn_set_uniform_skip(void* ctx, int on) {
+  Ctx* c = (Ctx*)ctx;
+  if (!c || !c->qc) return EDYN_E_ARG;
+  if (on != 0 && on != 1) return fail(c, EDYN_E_ARG, "uniform skip=%d must be 0 or 1", on);
+  c->skip_uniform = on;
   drop_graph(c);
   return EDYN_OK;
 }

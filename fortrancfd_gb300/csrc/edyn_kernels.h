@@ -64,6 +64,7 @@ struct StageArgs {
   FluidBC bc;            // inlet data (SRC/flow_bound.f90), passed by value
   unsigned* err;         // status word: EDYN_E_NEWTON / EDYN_E_STATE bits of any cell (may be null)
   TubeTab tubes;         // packed tubes (tubes.tiles null: the single tube above); cvel_out then per tube
+  int skip_uniform;      // skip the faces of cells whose stencils hold one state (dF = 0 exactly)
 };
 
 int fluid_upload_tables(const ThermoTable& tb, cudaStream_t s);

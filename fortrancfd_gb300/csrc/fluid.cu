@@ -328,6 +328,11 @@ __global__ void __launch_bounds__(STAGE_MAX_THREADS) k_stage(StageArgs a) {
                                 //         then the flux of face c0+p
   double* s_r = s_l + ne * P;   // [ne][P] value at the left face of cell c0-1+p (right state of face c0-1+p);
                                 //         then per-thread species scratch
+  // s_diff[w]: window cells w and w + 1 differ in some primitive (bitwise)
+  __shared__ unsigned char s_diff[STAGE_MAX_CELLS + 2 * 4];
+  const bool skip_uniform = a.skip_uniform != 0;
+  if (skip_uniform)
+    for (int w = tid; w < Wd; w += NT) s_diff[w] = 0;
 
   // 1. stage the primitive state window (coalesced row loads)
 #pragma unroll 4
@@ -344,11 +349,39 @@ __global__ void __launch_bounds__(STAGE_MAX_THREADS) k_stage(StageArgs a) {
   }
   __syncthreads();
 
+  // 1b. Uniform neighbourhoods. A cell whose window cells c-LV..c+LV hold
+  //     one state bit for bit has two faces with identical inputs, hence
+  //     identical fluxes and dF = 0 exactly; a face between two such cells
+  //     is needed by neither, and a reconstruction only by a needed face.
+  //     (Unloaded window positions beyond the tube's last ghost can only
+  //     mark cells past c1, whose faces matter here only next to a cell
+  //     that is frozen itself.)
+  if (skip_uniform) {
+    for (int idx = tid; idx < ne * (Wd - 1); idx += NT) {
+      const int v = idx / (Wd - 1), w = idx - v * (Wd - 1);
+      if (__double_as_longlong(s_q[v * Wd + w]) != __double_as_longlong(s_q[v * Wd + w + 1])) s_diff[w] = 1;
+    }
+    __syncthreads();
+  }
+  auto frozen = [&](int c) -> bool {
+    if (!skip_uniform) return false;
+    const int wc = c - (c0 - LV);
+    if (wc - LV < 0 || wc + LV - 1 > Wd - 2) return false;
+    for (int w = wc - LV; w < wc + LV; ++w)
+      if (s_diff[w]) return false;
+    return true;
+  };
+  // face c0+f (between cells c0-1+f and c0+f) is computed
+  auto need_face = [&](int f) -> bool {
+    return f >= 0 && c0 + f <= c1 && !(frozen(c0 - 1 + f) && frozen(c0 + f));
+  };
+
   // 2. face values of the cells c0-1..c1: position p = tid % P, rows split
   //    between the SP parts of the CTA
   if (tid < SP * P) {
     const int p = tid % P, part = tid / P;
-    if (c0 - 1 + p <= c1) {
+    // position p's right-face value serves face p, its left-face value face p - 1
+    if (need_face(p) || need_face(p - 1)) {
       const int c = p + LV - 1;  // window index of cell c0-1+p
       for (int v = part; v < ne; v += SP) {
         double vr, vl;
@@ -364,7 +397,7 @@ __global__ void __launch_bounds__(STAGE_MAX_THREADS) k_stage(StageArgs a) {
   //    c0+f; lane h of the group takes the species k = h, h + SP, ...
   const int f = tid / SP, h = tid % SP;
   const unsigned pair = ((1u << SP) - 1u) << (tid & 31 & ~(SP - 1));
-  if (f < P && c0 + f <= c1) {
+  if (f < P && need_face(f)) {
     FaceState L, R;
     L.rho = s_l[0 * P + f];
     L.u = s_l[1 * P + f];
@@ -492,6 +525,8 @@ __global__ void __launch_bounds__(STAGE_MAX_THREADS) k_stage(StageArgs a) {
   // through its stages, as the reference does (its stages update only Qc and
   // the boundary ghosts): only the last stage runs QcToqf.
   const bool rk4_mid = a.kind == 2 && a.rk4_stage < 3;
+  // a frozen cell's faces were not computed: its dF is exactly zero
+  const bool fz = f < P && i < c1 && frozen(i);
   if (f < P && i < c1 && rk4_mid) {
     const double c = dt / tv.dx;
     const double cq = 0.5 * ((0.5 * dt) / tv.dx);  // 0.5 (0.5 dt / dx) of stages 1 and 2
@@ -500,7 +535,7 @@ __global__ void __launch_bounds__(STAGE_MAX_THREADS) k_stage(StageArgs a) {
     double* Q0 = tv.q0 + i + GHOST;
     double* A = tv.acc + i + GHOST;
     for (int v = h; v < ne; v += SP) {
-      const double dF = s_l[v * P + f + 1] - s_l[v * P + f];
+      const double dF = fz ? 0.0 : s_l[v * P + f + 1] - s_l[v * P + f];
       const double k = -(c * dF);
       const double qs = Q[v * ld];
       if (a.rk4_stage == 0) {
@@ -521,7 +556,7 @@ __global__ void __launch_bounds__(STAGE_MAX_THREADS) k_stage(StageArgs a) {
     // Euler or first TVDRK3 stage: Q - c dF; later stages h1 Q0 + h2 (Q - c dF);
     // last RK4 stage: Q0 + (k1 + 2 k2 + 2 k3 + k4) / 6
     auto update = [&](int v, double qv) {
-      const double dF = s_l[v * P + f + 1] - s_l[v * P + f];
+      const double dF = fz ? 0.0 : s_l[v * P + f + 1] - s_l[v * P + f];
       if (a.kind == 2) return Q0[v * ld] + (1.0 / 6.0) * (tv.acc[v * ld + i + GHOST] + -(c * dF));
       return a.kind == 0 ? qv - c * dF : fma(a.h1, Q0[v * ld], a.h2 * (qv - c * dF));
     };

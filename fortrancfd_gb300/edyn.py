@@ -69,6 +69,7 @@ def lib() -> ctypes.CDLL:
     L.edyn_set_chem_max_steps.argtypes = [vp, i]
     L.edyn_set_chem_launch.argtypes = [vp, i]
     L.edyn_set_chem_precheck.argtypes = [vp, i]
+    L.edyn_set_uniform_skip.argtypes = [vp, i]
     L.edyn_init_tubes.argtypes = [cp, i, i, i, ip, i, ip, i, dp, i, ctypes.POINTER(vp)]
     L.edyn_tube_times.argtypes = [vp, dp, dp]
     L.edyn_autotune.argtypes = [vp, cp, ip, dp]
@@ -255,6 +256,11 @@ class Tube(_Ctx):
         """Single-precision pre-check of the inert-cell test (on by default):
         cells it decides skip the FP64 right-hand side."""
         self._check(lib().edyn_set_chem_precheck(self._h, 1 if on else 0))
+
+    def set_uniform_skip(self, on: bool = True) -> None:
+        """Fluid stage: no faces for cells whose stencils hold one state
+        (on by default; the results are bit for bit the same)."""
+        self._check(lib().edyn_set_uniform_skip(self._h, 1 if on else 0))
 
     def set_stage_tile(self, cells: int = 0) -> None:
         """Cells per fluid stage tile; 0 chooses it from the tube length."""

@@ -206,6 +206,15 @@ int edyn_chem_rhs_tube(void* ctx, int n, const double* rho_d, const double* yiT_
  * counterpart in the reference (a tuning knob of this implementation). */
 int edyn_set_chem_launch(void* ctx, int form);
 
+/* Uniform neighbourhoods in the fluid stage (on by default). A cell whose
+ * stencil cells c-r..c+r (r the reconstruction radius) hold one primitive
+ * state bit for bit has two faces with identical inputs, so identical
+ * fluxes and a flux difference of exactly zero: the stage computes neither
+ * the reconstructions nor the fluxes that only such cells need. Results are
+ * bit for bit those of on = 0 (every face computed), which the reference
+ * does (SRC/timeintegration.f90:99-219 over all faces). */
+int edyn_set_uniform_skip(void* ctx, int on);
+
 /* The single-precision pre-check of the integrator's inert-cell test (tube
  * chemistry; on by default). A cell's FP32 right-hand side and gross rates
  * bound its FP64 right-hand side; when the bound already passes the inert

@@ -318,9 +318,12 @@ __global__ void __launch_bounds__(STAGE_MAX_THREADS) k_stage(StageArgs a) {
     if (tile == nb - 1) c0 = tv.n - LV;
     if (tile == nb - 2) c1 = tv.n - LV;
   }
-  // stencil window [c0 - LV, c0 + TC + LV): the cells c0-1..c1 whose face
-  // values the tile needs, each with its reconstruction radius LV - 1
-  const int Wd = TC + 2 * LV;
+  // stencil window [c0 - LW, c0 + TC + LW): the cells c0-1..c1 whose face
+  // values the tile needs, each with its reconstruction radius LV - 1, and
+  // one more cell on each side, which decides whether the tile's end faces
+  // are needed (1b)
+  constexpr int LW = LV + 1;
+  const int Wd = TC + 2 * LW;
   const ThermoTable& tb = c_thermo;
   const int ns = a.ns, ne = ns + 3;
   double* s_q = sm;             // [ne][Wd] primitive window
@@ -329,7 +332,7 @@ __global__ void __launch_bounds__(STAGE_MAX_THREADS) k_stage(StageArgs a) {
   double* s_r = s_l + ne * P;   // [ne][P] value at the left face of cell c0-1+p (right state of face c0-1+p);
                                 //         then per-thread species scratch
   // s_diff[w]: window cells w and w + 1 differ in some primitive (bitwise)
-  __shared__ unsigned char s_diff[STAGE_MAX_CELLS + 2 * 4];
+  __shared__ unsigned char s_diff[STAGE_MAX_CELLS + 2 * 5];
   const bool skip_uniform = a.skip_uniform != 0;
   if (skip_uniform)
     for (int w = tid; w < Wd; w += NT) s_diff[w] = 0;
@@ -338,24 +341,30 @@ __global__ void __launch_bounds__(STAGE_MAX_THREADS) k_stage(StageArgs a) {
 #pragma unroll 4
   for (int idx = tid; idx < ne * Wd; idx += NT) {
     const int v = idx / Wd, j = idx - v * Wd;
-    const int cell = c0 - LV + j;
+    const int cell = c0 - LW + j;
     if (cell >= 0 && cell < tv.n) s_q[idx] = tv.qf_in[(size_t)v * a.ld + cell + GHOST];
   }
   // ghost cells of the tube ends inside the window: thread t < LV takes the
   // left ghost -1-t, thread LV <= t < 2 LV the right ghost n + t - LV.
   if (tid < 2 * LV) {
     const int g = (tid < LV) ? -1 - tid : tv.n + (tid - LV);
-    if (g >= c0 - LV && g < c1 + LV) ghost_cell(a, tv, g, s_q + (g - (c0 - LV)), Wd, s_r + tid, P);
+    // (the ghosts of the stencils only: a ghost is built from the conserved
+    // state of the tube's end cells, which only their own tile may read
+    // while this stage updates them)
+    if (g >= c0 - LV && g < c1 + LV) ghost_cell(a, tv, g, s_q + (g - (c0 - LW)), Wd, s_r + tid, P);
   }
   __syncthreads();
 
-  // 1b. Uniform neighbourhoods. A cell whose window cells c-LV..c+LV hold
+  // 1b. Uniform neighbourhoods. A tube cell c whose cells c-LV..c+LV hold
   //     one state bit for bit has two faces with identical inputs, hence
-  //     identical fluxes and dF = 0 exactly; a face between two such cells
-  //     is needed by neither, and a reconstruction only by a needed face.
-  //     (Unloaded window positions beyond the tube's last ghost can only
-  //     mark cells past c1, whose faces matter here only next to a cell
-  //     that is frozen itself.)
+  //     identical fluxes and dF = 0 exactly ("frozen"); a face between two
+  //     frozen cells is needed by neither, and a reconstruction only by a
+  //     needed face. An owned cell's test reads tube cells and stencil
+  //     ghosts only; the outer window positions (unloaded where they fall
+  //     on a ghost) enter only the tests of the cells next to the tile,
+  //     which decide nothing but whether the tile's end faces are skipped,
+  //     and an end face is skipped only next to a frozen owned cell, whose
+  //     dF is zero without it.
   if (skip_uniform) {
     for (int idx = tid; idx < ne * (Wd - 1); idx += NT) {
       const int v = idx / (Wd - 1), w = idx - v * (Wd - 1);
@@ -364,8 +373,8 @@ __global__ void __launch_bounds__(STAGE_MAX_THREADS) k_stage(StageArgs a) {
     __syncthreads();
   }
   auto frozen = [&](int c) -> bool {
-    if (!skip_uniform) return false;
-    const int wc = c - (c0 - LV);
+    if (!skip_uniform || c < 0 || c >= tv.n) return false;
+    const int wc = c - (c0 - LW);
     if (wc - LV < 0 || wc + LV - 1 > Wd - 2) return false;
     for (int w = wc - LV; w < wc + LV; ++w)
       if (s_diff[w]) return false;
@@ -382,7 +391,7 @@ __global__ void __launch_bounds__(STAGE_MAX_THREADS) k_stage(StageArgs a) {
     const int p = tid % P, part = tid / P;
     // position p's right-face value serves face p, its left-face value face p - 1
     if (need_face(p) || need_face(p - 1)) {
-      const int c = p + LV - 1;  // window index of cell c0-1+p
+      const int c = p + LW - 1;  // window index of cell c0-1+p
       for (int v = part; v < ne; v += SP) {
         double vr, vl;
         recon_cell<ACU, LIM, WFLAG>(s_q + v * Wd, c, vr, vl);
@@ -580,7 +589,7 @@ __global__ void __launch_bounds__(STAGE_MAX_THREADS) k_stage(StageArgs a) {
       ys[(v - 3) * P] = qn;
     }
     int iters;
-    const double Tg = s_q[2 * Wd + f + LV];
+    const double Tg = s_q[2 * Wd + f + LW];
     CellEOS e = qc_to_qf_cell<SP>(q[0], q[1], q[2], ys, P, Tg, a.strict_newton != 0, iters, h, pair);
     double* out = tv.qf_out + i + GHOST;
     if (h == 0) {
@@ -835,7 +844,7 @@ size_t stage_smem_bytes(int acu, int ns, int tc) {
   const int lv = acu_lvir(acu);
   const int ne = ns + 3;
   const int p = tc + 2;
-  return sizeof(double) * ((size_t)ne * (tc + 2 * lv) + (size_t)2 * ne * p);
+  return sizeof(double) * ((size_t)ne * (tc + 2 * (lv + 1)) + (size_t)2 * ne * p);
 }
 
 namespace {

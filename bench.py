@@ -459,6 +459,7 @@ def gpu_arm(args, rank, world, local):
             "chem_launch": {"rhs_per_cell": chem_stats["rhs"] / max(1, chem_stats["cells"]),
                             "rejects": chem_stats["rejects"], "team_cells": chem_stats["team_cells"],
                             "precheck_cells": chem_stats["cells32"],
+                            "identical_cells": chem_stats["cells_same"],
                             "failed": chem_stats["failed"]},
             "surrogate": surr}
     print(json.dumps(line), flush=True)

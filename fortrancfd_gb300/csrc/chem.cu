@@ -2600,7 +2600,10 @@ __global__ void __launch_bounds__(SCREEN_WARPS * 32, 1)
   const int nw = blockDim.x >> 5;
   double speed_max = 0.0;
   unsigned long long done = 0, listed = 0, done32 = 0, rhs64n = 0;
-  for (unsigned cell = blockIdx.x * nw + (threadIdx.x >> 5); cell < (unsigned)L.n; cell += gridDim.x * nw) {
+  // every cell, or the first cell of each run of identical cells (k_runs)
+  const unsigned nwork = L.heads ? *L.head_count : (unsigned)L.n;
+  for (unsigned item = blockIdx.x * nw + (threadIdx.x >> 5); item < nwork; item += gridDim.x * nw) {
+    const unsigned cell = L.heads ? (unsigned)L.heads[item] : item;
     if (!cell_active(L, cell)) continue;
     const double dt = cell_dt(L, cell, dt_launch);
     const double* q = L.qf + cell_col(L, cell) + GHOST;
@@ -2704,6 +2707,155 @@ __global__ void __launch_bounds__(SCREEN_WARPS * 32, 1)
       *L.time = *L.time + dt_launch;
       *L.nsteps = *L.nsteps + 1;
     }
+  }
+}
+
+
+// ---------------------------------------------------------------------------
+// Runs of identical cells. A cell's source step is a function of its qf
+// column (rho, u, T, Y) and its tube's dt alone, so cells whose columns are
+// equal bit for bit get equal results. k_runs marks each stepping cell as the
+// head of a run (its column differs from its left neighbour's, or the
+// neighbour is in another tube) or a follower, and lists the heads for the
+// screening pass; k_follow gives every follower its head's result: the
+// head's finished column, heat release, final T and step size when the head
+// was finished in the screening pass, or a place in the integrator's list
+// when it was listed (a listed cell integrates from its own last step
+// size). Blocks of RUN_BLOCK cells; run_last[b] = the last head of block b.
+// ---------------------------------------------------------------------------
+constexpr int RUN_BLOCK = CHEM_RUN_BLOCK;
+constexpr int RUN_THREADS = 256;
+
+__global__ void __launch_bounds__(RUN_THREADS) k_runs(ChemLaunch L) {
+  __shared__ int s_max[RUN_THREADS / 32];
+  if (L.step_active && *L.step_active == 0) return;
+  const int b = blockIdx.x, tid = threadIdx.x, lane = tid & 31;
+  const size_t ld = (size_t)L.ld;
+  int last = -1;
+  for (int j = 0; j < RUN_BLOCK / RUN_THREADS; ++j) {
+    const int c = b * RUN_BLOCK + j * RUN_THREADS + tid;
+    unsigned char fl = 0;  // 0 not stepping, 1 head, 2 follower
+    if (c < L.n && cell_active(L, c)) {
+      bool same = c > 0 && (!L.tube_of || L.tube_of[c] == L.tube_of[c - 1]);
+      if (same) {
+        const double* q = L.qf + cell_col(L, c) + GHOST;
+        const double* r = L.qf + cell_col(L, c - 1) + GHOST;
+        for (int row = 0; row < L.nrow && same; ++row)
+          same = __double_as_longlong(q[row * ld]) == __double_as_longlong(r[row * ld]);
+      }
+      fl = same ? 2 : 1;
+    }
+    if (c < L.n) L.run_flag[c] = fl;
+    const bool head = fl == 1;
+    const unsigned m = __ballot_sync(0xffffffffu, head);
+    if (m) {
+      unsigned base = 0;
+      if (lane == 0) base = atomicAdd(L.head_count, (unsigned)__popc(m));
+      base = __shfl_sync(0xffffffffu, base, 0);
+      if (head) L.heads[base + __popc(m & ((1u << lane) - 1u))] = c;
+    }
+    if (head) last = c;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) last = max(last, __shfl_xor_sync(0xffffffffu, last, o));
+  if (lane == 0) s_max[tid >> 5] = last;
+  __syncthreads();
+  if (tid == 0) {
+    int m = -1;
+    for (int q = 0; q < RUN_THREADS / 32; ++q) m = max(m, s_max[q]);
+    L.run_last[b] = m;
+  }
+}
+
+__global__ void __launch_bounds__(RUN_THREADS) k_follow(ChemLaunch L, ChemCounters* cnt) {
+  constexpr int PER = RUN_BLOCK / RUN_THREADS;  // consecutive cells of a thread
+  __shared__ int s_w[RUN_THREADS / 32];
+  __shared__ int s_carry;
+  __shared__ unsigned s_copied;
+  if (L.step_active && *L.step_active == 0) return;
+  const int b = blockIdx.x, tid = threadIdx.x, lane = tid & 31, wq = tid >> 5;
+  // the last head before this block
+  int cm = -1;
+  for (int q = tid; q < b; q += RUN_THREADS) cm = max(cm, L.run_last[q]);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) cm = max(cm, __shfl_xor_sync(0xffffffffu, cm, o));
+  if (lane == 0) s_w[wq] = cm;
+  if (tid == 0) s_copied = 0u;
+  __syncthreads();
+  if (tid == 0) {
+    int m = -1;
+    for (int q = 0; q < RUN_THREADS / 32; ++q) m = max(m, s_w[q]);
+    s_carry = m;
+  }
+  __syncthreads();
+  // the head of each cell: the last head at or before it (an inclusive max
+  // scan of head positions over the block, started from the carry)
+  const int c0 = b * RUN_BLOCK + tid * PER;
+  unsigned char fl[PER];
+  int hp[PER];
+  int run = -1;
+#pragma unroll
+  for (int k = 0; k < PER; ++k) {
+    const int c = c0 + k;
+    fl[k] = c < L.n ? L.run_flag[c] : 0;
+    if (fl[k] == 1) run = c;
+    hp[k] = run;
+  }
+  int v = run;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int t = __shfl_up_sync(0xffffffffu, v, o);
+    if (lane >= o) v = max(v, t);
+  }
+  __syncthreads();  // s_w is reused
+  if (lane == 31) s_w[wq] = v;
+  __syncthreads();
+  int prev = __shfl_up_sync(0xffffffffu, v, 1);
+  if (lane == 0) prev = -1;
+  prev = max(prev, s_carry);
+  for (int q = 0; q < wq; ++q) prev = max(prev, s_w[q]);
+  const size_t ld = (size_t)L.ld;
+  unsigned copied = 0;
+#pragma unroll
+  for (int k = 0; k < PER; ++k) {
+    const int c = c0 + k;
+    const int h = max(prev, hp[k]);
+    bool listed = false;
+    if (fl[k] == 2 && h >= 0) {
+      if (L.cost[h] == 1) {
+        // the head was finished in the screening pass: its column is this
+        // cell's result (rows from T on; rho and u are not changed)
+        const size_t ch = cell_col(L, h) + GHOST, cc = cell_col(L, c) + GHOST;
+        for (int row = 2; row < L.nrow; ++row) {
+          L.qf[row * ld + cc] = L.qf[row * ld + ch];
+          L.qc[row * ld + cc] = L.qc[row * ld + ch];
+        }
+        L.hrr[c] = L.hrr[h];
+        if (L.tchem) L.tchem[c] = L.tchem[h];
+        if (L.hlast) L.hlast[c] = L.hlast[h];
+        L.cost[c] = 1;
+        ++copied;
+      } else {
+        listed = true;
+        L.cost[c] = -1;
+      }
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, listed);
+    if (m) {
+      unsigned base = 0;
+      if (lane == 0) base = atomicAdd(L.list_count, (unsigned)__popc(m));
+      base = __shfl_sync(0xffffffffu, base, 0);
+      if (listed) L.list[base + __popc(m & ((1u << lane) - 1u))] = c;
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) copied += __shfl_xor_sync(0xffffffffu, copied, o);
+  if (lane == 0 && copied) atomicAdd(&s_copied, copied);
+  __syncthreads();
+  if (tid == 0 && s_copied) {
+    atomicAdd(&cnt->cells, (unsigned long long)s_copied);
+    atomicAdd(&cnt->steps, (unsigned long long)s_copied);
+    atomicAdd(&cnt->cells_same, (unsigned long long)s_copied);
   }
 }
 
@@ -3271,11 +3423,18 @@ cudaError_t chem_launch_tube_listed(ChemState& s, const ChemLaunch& L0, int* lis
   ChemLaunch L = L0;
   L.list = list;
   L.list_count = list_count;
+  const int nblk = (L.n + RUN_BLOCK - 1) / RUN_BLOCK;
+  if (L.heads) {
+    e = cudaMemsetAsync(L.head_count, 0, sizeof(unsigned), st);
+    if (e != cudaSuccess) return e;
+    k_runs<<<nblk, RUN_THREADS, 0, st>>>(L);
+  }
   const int sgrid = std::min(s.screen_ctas, (L.n + s.screen_warps - 1) / s.screen_warps);
   k_tube_screen<<<std::max(1, sgrid), s.screen_warps * 32, s.screen_smem, st>>>((const char*)s.d_tables,
                                                                               (int)s.table_bytes, L, s.d_count);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
+  if (L.heads) k_follow<<<nblk, RUN_THREADS, 0, st>>>(L, s.d_count);
   k_tube_chem<<<s.ctas, s.warps * 32, s.smem, st>>>((const char*)s.d_tables, (int)s.table_bytes, L, s.d_next,
                                                     s.d_count);
   e = cudaGetLastError();

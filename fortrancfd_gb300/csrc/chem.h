@@ -14,6 +14,7 @@ constexpr int HOT_MAX = 64;
 struct ChemCounters {
   unsigned long long rhs, steps, rejects, failed, jac, cells, team_cells;
   unsigned long long cells32;  // inert cells decided by the single-precision pre-check
+  unsigned long long cells_same;  // cells given the result of an identical cell (runs)
 };
 
 struct ChemState {
@@ -79,7 +80,16 @@ struct ChemLaunch {
   int ntube;
   // single-precision pre-check of the inert-cell test (tube mode, single warps)
   int precheck;
+  // runs of identical cells (two-pass tube launch; heads null: off): rows
+  // of the qf columns compared, per-cell run flags, the heads' list and
+  // count, the last head of each block of cells
+  int nrow;
+  unsigned char* run_flag;
+  int* heads;
+  unsigned* head_count;
+  int* run_last;
 };
+constexpr int CHEM_RUN_BLOCK = 1024;  // cells per block of the run kernels
 
 // smap: tube row of each species of m (3 + smap[k]) when m is a subset of the
 // tube's mechanism (NULL: identity); nnorm: components counted in the RMS

@@ -136,6 +136,11 @@ struct Ctx {
   unsigned* d_list_count = nullptr;
   unsigned char* d_cls = nullptr;
   unsigned* d_hist = nullptr;
+  // runs of identical cells in the two-pass chemistry launch
+  unsigned char* d_run_flag = nullptr;
+  int* d_heads = nullptr;
+  unsigned* d_head_count = nullptr;
+  int* d_run_last = nullptr;
   bool listed = false;       // the two-pass form is in use
   cudaGraphExec_t graph = nullptr;
   int graph_steps = 0;
@@ -329,6 +334,13 @@ int source_step(Ctx* c, double dt, bool dev) {
   L.tchem = c->tchem;
   L.max_steps = c->chem_max_steps;
   L.precheck = c->precheck;
+  if (c->listed && c->skip_uniform) {
+    L.nrow = c->ne;
+    L.run_flag = c->d_run_flag;
+    L.heads = c->d_heads;
+    L.head_count = c->d_head_count;
+    L.run_last = c->d_run_last;
+  }
   if (c->pk.ntube) {
     const Packed& k = c->pk;
     L.colmap = k.colmap;
@@ -786,6 +798,10 @@ int edyn_init(const char* chem_dir, int nspe, int nequ, int ncell, int lvir, con
   CK(cudaMalloc(&c->d_list_count, sizeof(unsigned)));
   CK(cudaMalloc(&c->d_cls, (size_t)ncell));
   CK(cudaMalloc(&c->d_hist, 64 * sizeof(unsigned)));
+  CK(cudaMalloc(&c->d_run_flag, (size_t)ncell));
+  CK(cudaMalloc(&c->d_heads, (size_t)ncell * sizeof(int)));
+  CK(cudaMalloc(&c->d_head_count, sizeof(unsigned)));
+  CK(cudaMalloc(&c->d_run_last, (size_t)((ncell + CHEM_RUN_BLOCK - 1) / CHEM_RUN_BLOCK) * sizeof(int)));
   // Long tubes are throughput-bound on the inert cells' one right-hand side
   // each, which the light screening pass runs at four warps per SM
   // sub-partition; short ones are bound by their costliest cell, which a
@@ -1458,8 +1474,9 @@ int edyn_chem_stats(void* ctx, double* stats) {
   ChemCounters k;
   cudaError_t e = chem_read_counters(c->use_sub ? c->chem_sub : c->chem, &k, c->stream);
   if (e != cudaSuccess) return fail(c, EDYN_E_CUDA, "counters: %s", cudaGetErrorString(e));
-  const unsigned long long v[8] = {k.rhs, k.steps, k.rejects, k.failed, k.jac, k.cells, k.team_cells, k.cells32};
-  for (int i = 0; i < 8; ++i) stats[i] = (double)v[i];
+  const unsigned long long v[9] = {k.rhs,   k.steps,      k.rejects, k.failed,    k.jac,
+                                   k.cells, k.team_cells, k.cells32, k.cells_same};
+  for (int i = 0; i < 9; ++i) stats[i] = (double)v[i];
   return EDYN_OK;
 }
 
@@ -1625,6 +1642,10 @@ int edyn_finalize(void* ctx) {
   cudaFree(c->d_list_count);
   cudaFree(c->d_cls);
   cudaFree(c->d_hist);
+  cudaFree(c->d_run_flag);
+  cudaFree(c->d_heads);
+  cudaFree(c->d_head_count);
+  cudaFree(c->d_run_last);
   if (c->own) cudaStreamDestroy(c->own);
   delete c;
   return EDYN_OK;

@@ -226,9 +226,9 @@ class Tube(_Ctx):
 
     def chem_stats(self) -> dict:
         """Counters of the last chemistry launch."""
-        st = np.zeros(8)
+        st = np.zeros(9)
         self._check(lib().edyn_chem_stats(self._h, _ptr(st)))
-        keys = ("rhs", "steps", "rejects", "failed", "jac", "cells", "team_cells", "cells32")
+        keys = ("rhs", "steps", "rejects", "failed", "jac", "cells", "team_cells", "cells32", "cells_same")
         return {k: int(v) for k, v in zip(keys, st)}
 
     def chem_cost(self):
@@ -258,8 +258,10 @@ class Tube(_Ctx):
         self._check(lib().edyn_set_chem_precheck(self._h, 1 if on else 0))
 
     def set_uniform_skip(self, on: bool = True) -> None:
-        """Fluid stage: no faces for cells whose stencils hold one state
-        (on by default; the results are bit for bit the same)."""
+        """Uniform regions (on by default): the fluid stage computes no faces
+        for cells whose stencils hold one state, and the two-pass chemistry
+        screens one cell per run of identical cells. The results are bit for
+        bit the same."""
         self._check(lib().edyn_set_uniform_skip(self._h, 1 if on else 0))
 
     def set_stage_tile(self, cells: int = 0) -> None:

@@ -206,13 +206,17 @@ int edyn_chem_rhs_tube(void* ctx, int n, const double* rho_d, const double* yiT_
  * counterpart in the reference (a tuning knob of this implementation). */
 int edyn_set_chem_launch(void* ctx, int form);
 
-/* Uniform neighbourhoods in the fluid stage (on by default). A cell whose
- * stencil cells c-r..c+r (r the reconstruction radius) hold one primitive
- * state bit for bit has two faces with identical inputs, so identical
- * fluxes and a flux difference of exactly zero: the stage computes neither
- * the reconstructions nor the fluxes that only such cells need. Results are
- * bit for bit those of on = 0 (every face computed), which the reference
- * does (SRC/timeintegration.f90:99-219 over all faces). */
+/* Uniform regions (on by default). Fluid stage: a cell whose stencil cells
+ * c-r..c+r (r the reconstruction radius) hold one primitive state bit for
+ * bit has two faces with identical inputs, so identical fluxes and a flux
+ * difference of exactly zero: the stage computes neither the
+ * reconstructions nor the fluxes that only such cells need. Chemistry (the
+ * two-pass launch): a cell's source step depends on its primitive column
+ * and its tube's dt alone, so of a run of cells with columns equal bit for
+ * bit only the first is screened; the others receive its finished column,
+ * or are integrated one by one when it needs the integrator. Results are
+ * bit for bit those of on = 0, which computes every face and every cell as
+ * the reference does (SRC/timeintegration.f90:99-219, SRC/source.f90:17-84). */
 int edyn_set_uniform_skip(void* ctx, int on);
 
 /* The single-precision pre-check of the integrator's inert-cell test (tube
@@ -277,10 +281,11 @@ int edyn_reactors(void* ctx, int n, const double* rho, const double* dt, double*
 int edyn_reactors_device(void* ctx, int n, const double* rho_d, const double* dt_d, double* yiT_d, double* stats);
 
 /* Counters of the last chemistry launch of this context (tube or batch),
- * 8 values: FP64 right-hand-side evaluations, accepted steps, rejected
+ * 9 values: FP64 right-hand-side evaluations, accepted steps, rejected
  * steps, failed cells, Jacobians, cells, cells integrated by a four-warp
  * team, inert cells decided by the single-precision pre-check (no FP64
- * right-hand side; see edyn_set_chem_precheck).
+ * right-hand side; see edyn_set_chem_precheck), cells given the result of
+ * an identical neighbour (see edyn_set_uniform_skip).
  * No counterpart in the reference, which reports none (its solver's
  * statistics stay inside macks, SRC/source.f90:58). */
 int edyn_chem_stats(void* ctx, double* stats);

@@ -270,6 +270,7 @@ def test_single_precision_precheck_agrees_with_fp64_test():
                      atol=1e-14)
             g.set_chem_launch(form)
             g.set_chem_precheck(pre)
+            g.set_uniform_skip(False)  # every cell through the screen (no runs of identical cells)
             g.init_cells(case.T, case.p, case.u, case.X)
             for _ in range(6):
                 g.step(case.cfl)

@@ -292,12 +292,18 @@ def test_uniform_skip_is_bit_for_bit(react, scheme):
         g = Tube(case.ncell, case.dx, select_time=sel, flag_acu=acu, flag_weno=weno, flag_rbound=1,
                  do_reaction=react, rtol=1e-6, atol=1e-14)
         g.set_uniform_skip(on)
+        if react:
+            g.set_chem_launch(2)  # the two-pass chemistry, where runs of identical cells apply
         g.init_cells(case.T, case.p, case.u, case.X)
         for _ in range(5):
             g.step(case.cfl)
         g.advance(case.cfl, tend=1e9, max_steps=20)
-        qf, qc, _ = g.download()
-        out.append((qf, qc))
+        qf, qc, hrr = g.download()
+        same = g.chem_stats()["cells_same"] if react else 0
+        out.append((qf, qc, hrr, same))
         g.close()
     assert np.array_equal(out[0][0], out[1][0])
     assert np.array_equal(out[0][1], out[1][1])
+    assert np.array_equal(out[0][2], out[1][2])
+    if react:
+        assert out[0][3] > case.ncell // 2 and out[1][3] == 0, (out[0][3], out[1][3])

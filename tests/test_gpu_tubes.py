@@ -101,3 +101,23 @@ def test_reacting_uneven_tubes_match_oracle(oracle, names):
         assert rel < 1e-3, (k, rel)
     hrr = g.split(g.download()[2])
     assert all(np.all(np.isfinite(h)) for h in hrr)
+
+
+def test_packed_reacting_tubes_uniform_skip_is_bit_for_bit():
+    """Runs of identical cells never cross a tube boundary: four packed
+    reacting tubes through the two-pass chemistry give the same bits with
+    the uniform-region shortcuts on and off."""
+    cases = _cases()
+    out = []
+    for on in (True, False):
+        g = _packed(cases, 1)
+        g.set_chem_launch(2)
+        g.set_uniform_skip(on)
+        for _ in range(6):
+            g.step(0.4)
+        qf, qc, hrr = g.download()
+        out.append((qf, qc, hrr, g.chem_stats()["cells_same"]))
+        g.close()
+    assert out[0][3] > 0 and out[1][3] == 0
+    for a, b in zip(out[0][:3], out[1][:3]):
+        assert np.array_equal(a, b)

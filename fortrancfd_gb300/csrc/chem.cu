@@ -2713,23 +2713,54 @@ __global__ void __launch_bounds__(SCREEN_WARPS * 32, 1)
 
 // ---------------------------------------------------------------------------
 // Runs of identical cells. A cell's source step is a function of its qf
-// column (rho, u, T, Y) and its tube's dt alone, so cells whose columns are
-// equal bit for bit get equal results. k_runs marks each stepping cell as the
-// head of a run (its column differs from its left neighbour's, or the
-// neighbour is in another tube) or a follower, and lists the heads for the
-// screening pass; k_follow gives every follower its head's result: the
-// head's finished column, heat release, final T and step size when the head
-// was finished in the screening pass, or a place in the integrator's list
-// when it was listed (a listed cell integrates from its own last step
-// size). Blocks of RUN_BLOCK cells; run_last[b] = the last head of block b.
+// column (rho, u, T, Y), its tube's dt and -- when it needs the integrator --
+// the step size its last window ended with (hlast) and whether a four-warp
+// team or a warp integrates it. Cells whose columns are equal bit for bit
+// therefore get equal results, and k_runs marks each stepping cell as the
+// head of a run (its column differs from its left neighbour's, the
+// neighbour is in another tube, or either is on the team list) or a
+// follower, and lists the heads for the screening pass. k_follow then gives
+// each follower its head's result where it is known: the head's finished
+// column when the screening pass finished the head. When the head was
+// listed for the integrator, a follower with the head's hlast waits for the
+// head's integrated column (k_follow_integrated, after the integrator
+// pass); one with another hlast is listed itself. Blocks of RUN_BLOCK cells;
+// run_last[b] = the last head of block b, run_head[c] = the head of c.
 // ---------------------------------------------------------------------------
 constexpr int RUN_BLOCK = CHEM_RUN_BLOCK;
 constexpr int RUN_THREADS = 256;
 
+__device__ __forceinline__ bool on_hot_list(const unsigned* s_hot, int c) {
+  const unsigned nh = s_hot[0];
+  for (unsigned j = 0; j < nh; ++j)
+    if (s_hot[1 + j] == (unsigned)c) return true;
+  return false;
+}
+
+// The result of cell h is also cell c's: the finished column from T on (rho
+// and u are not changed by a source step), heat release, final T, step size
+// and cost.
+__device__ __forceinline__ void copy_result(const ChemLaunch& L, int h, int c) {
+  const size_t ld = (size_t)L.ld;
+  const size_t ch = cell_col(L, h) + GHOST, cc = cell_col(L, c) + GHOST;
+  for (int row = 2; row < L.nrow; ++row) {
+    L.qf[row * ld + cc] = L.qf[row * ld + ch];
+    L.qc[row * ld + cc] = L.qc[row * ld + ch];
+  }
+  L.hrr[c] = L.hrr[h];
+  if (L.tchem) L.tchem[c] = L.tchem[h];
+  if (L.hlast) L.hlast[c] = L.hlast[h];
+  L.cost[c] = L.cost[h];
+}
+
 __global__ void __launch_bounds__(RUN_THREADS) k_runs(ChemLaunch L) {
   __shared__ int s_max[RUN_THREADS / 32];
+  __shared__ unsigned s_hot[HOT_MAX + 1];
   if (L.step_active && *L.step_active == 0) return;
   const int b = blockIdx.x, tid = threadIdx.x, lane = tid & 31;
+  for (int j = tid; j <= HOT_MAX; j += RUN_THREADS) s_hot[j] = L.hot ? L.hot[j] : 0u;
+  if (tid == 0) s_hot[0] = min(s_hot[0], (unsigned)HOT_MAX);
+  __syncthreads();
   const size_t ld = (size_t)L.ld;
   int last = -1;
   for (int j = 0; j < RUN_BLOCK / RUN_THREADS; ++j) {
@@ -2737,11 +2768,22 @@ __global__ void __launch_bounds__(RUN_THREADS) k_runs(ChemLaunch L) {
     unsigned char fl = 0;  // 0 not stepping, 1 head, 2 follower
     if (c < L.n && cell_active(L, c)) {
       bool same = c > 0 && (!L.tube_of || L.tube_of[c] == L.tube_of[c - 1]);
+      if (same) same = !on_hot_list(s_hot, c) && !on_hot_list(s_hot, c - 1);
       if (same) {
         const double* q = L.qf + cell_col(L, c) + GHOST;
         const double* r = L.qf + cell_col(L, c - 1) + GHOST;
-        for (int row = 0; row < L.nrow && same; ++row)
-          same = __double_as_longlong(q[row * ld]) == __double_as_longlong(r[row * ld]);
+        // eight rows' loads in flight at a time
+        for (int row = 0; row < L.nrow && same; row += 8) {
+          long long x[8], y[8];
+#pragma unroll
+          for (int k = 0; k < 8; ++k) {
+            const int rr = min(row + k, L.nrow - 1);
+            x[k] = __double_as_longlong(q[rr * ld]);
+            y[k] = __double_as_longlong(r[rr * ld]);
+          }
+#pragma unroll
+          for (int k = 0; k < 8; ++k) same = same && x[k] == y[k];
+        }
       }
       fl = same ? 2 : 1;
     }
@@ -2768,8 +2810,9 @@ __global__ void __launch_bounds__(RUN_THREADS) k_runs(ChemLaunch L) {
 }
 
 __global__ void __launch_bounds__(RUN_THREADS) k_follow(ChemLaunch L, ChemCounters* cnt) {
-  constexpr int PER = RUN_BLOCK / RUN_THREADS;  // consecutive cells of a thread
+  constexpr int PER = RUN_BLOCK / RUN_THREADS;  // consecutive cells of a thread in the scan
   __shared__ int s_w[RUN_THREADS / 32];
+  __shared__ int s_head[RUN_BLOCK];
   __shared__ int s_carry;
   __shared__ unsigned s_copied;
   if (L.step_active && *L.step_active == 0) return;
@@ -2791,14 +2834,12 @@ __global__ void __launch_bounds__(RUN_THREADS) k_follow(ChemLaunch L, ChemCounte
   // the head of each cell: the last head at or before it (an inclusive max
   // scan of head positions over the block, started from the carry)
   const int c0 = b * RUN_BLOCK + tid * PER;
-  unsigned char fl[PER];
   int hp[PER];
   int run = -1;
 #pragma unroll
   for (int k = 0; k < PER; ++k) {
     const int c = c0 + k;
-    fl[k] = c < L.n ? L.run_flag[c] : 0;
-    if (fl[k] == 1) run = c;
+    if (c < L.n && L.run_flag[c] == 1) run = c;
     hp[k] = run;
   }
   int v = run;
@@ -2814,27 +2855,23 @@ __global__ void __launch_bounds__(RUN_THREADS) k_follow(ChemLaunch L, ChemCounte
   if (lane == 0) prev = -1;
   prev = max(prev, s_carry);
   for (int q = 0; q < wq; ++q) prev = max(prev, s_w[q]);
-  const size_t ld = (size_t)L.ld;
-  unsigned copied = 0;
 #pragma unroll
-  for (int k = 0; k < PER; ++k) {
-    const int c = c0 + k;
-    const int h = max(prev, hp[k]);
+  for (int k = 0; k < PER; ++k) s_head[tid * PER + k] = max(prev, hp[k]);
+  __syncthreads();
+  // the followers, one cell per thread in turn (coalesced rows)
+  unsigned copied = 0;
+  for (int j = 0; j < RUN_BLOCK / RUN_THREADS; ++j) {
+    const int c = b * RUN_BLOCK + j * RUN_THREADS + tid;
     bool listed = false;
-    if (fl[k] == 2 && h >= 0) {
+    if (c < L.n && L.run_flag[c] == 2) {
+      const int h = s_head[c - b * RUN_BLOCK];
       if (L.cost[h] == 1) {
-        // the head was finished in the screening pass: its column is this
-        // cell's result (rows from T on; rho and u are not changed)
-        const size_t ch = cell_col(L, h) + GHOST, cc = cell_col(L, c) + GHOST;
-        for (int row = 2; row < L.nrow; ++row) {
-          L.qf[row * ld + cc] = L.qf[row * ld + ch];
-          L.qc[row * ld + cc] = L.qc[row * ld + ch];
-        }
-        L.hrr[c] = L.hrr[h];
-        if (L.tchem) L.tchem[c] = L.tchem[h];
-        if (L.hlast) L.hlast[c] = L.hlast[h];
-        L.cost[c] = 1;
+        copy_result(L, h, c);  // finished by the screening pass
         ++copied;
+      } else if (!L.hlast || __double_as_longlong(L.hlast[c]) == __double_as_longlong(L.hlast[h])) {
+        L.run_flag[c] = 3;  // takes the head's integrated result
+        L.run_head[c] = h;
+        L.cost[c] = -2;
       } else {
         listed = true;
         L.cost[c] = -1;
@@ -2855,6 +2892,30 @@ __global__ void __launch_bounds__(RUN_THREADS) k_follow(ChemLaunch L, ChemCounte
   if (tid == 0 && s_copied) {
     atomicAdd(&cnt->cells, (unsigned long long)s_copied);
     atomicAdd(&cnt->steps, (unsigned long long)s_copied);
+    atomicAdd(&cnt->cells_same, (unsigned long long)s_copied);
+  }
+}
+
+// The followers of integrated heads (run_flag 3) take their head's result.
+__global__ void __launch_bounds__(RUN_THREADS) k_follow_integrated(ChemLaunch L, ChemCounters* cnt) {
+  __shared__ unsigned s_copied;
+  if (L.step_active && *L.step_active == 0) return;
+  if (threadIdx.x == 0) s_copied = 0u;
+  __syncthreads();
+  unsigned copied = 0;
+  for (int j = 0; j < RUN_BLOCK / RUN_THREADS; ++j) {
+    const int c = blockIdx.x * RUN_BLOCK + j * RUN_THREADS + threadIdx.x;
+    if (c < L.n && L.run_flag[c] == 3) {
+      copy_result(L, L.run_head[c], c);
+      ++copied;
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) copied += __shfl_xor_sync(0xffffffffu, copied, o);
+  if ((threadIdx.x & 31) == 0 && copied) atomicAdd(&s_copied, copied);
+  __syncthreads();
+  if (threadIdx.x == 0 && s_copied) {
+    atomicAdd(&cnt->cells, (unsigned long long)s_copied);
     atomicAdd(&cnt->cells_same, (unsigned long long)s_copied);
   }
 }
@@ -3437,6 +3498,7 @@ cudaError_t chem_launch_tube_listed(ChemState& s, const ChemLaunch& L0, int* lis
   if (L.heads) k_follow<<<nblk, RUN_THREADS, 0, st>>>(L, s.d_count);
   k_tube_chem<<<s.ctas, s.warps * 32, s.smem, st>>>((const char*)s.d_tables, (int)s.table_bytes, L, s.d_next,
                                                     s.d_count);
+  if (L.heads) k_follow_integrated<<<nblk, RUN_THREADS, 0, st>>>(L, s.d_count);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   if (L.cost && L.hot) {

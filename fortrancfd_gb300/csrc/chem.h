@@ -88,6 +88,7 @@ struct ChemLaunch {
   int* heads;
   unsigned* head_count;
   int* run_last;
+  int* run_head;  // the head of a follower that takes its head's integrated result
 };
 constexpr int CHEM_RUN_BLOCK = 1024;  // cells per block of the run kernels
 

@@ -141,6 +141,7 @@ struct Ctx {
   int* d_heads = nullptr;
   unsigned* d_head_count = nullptr;
   int* d_run_last = nullptr;
+  int* d_run_head = nullptr;
   bool listed = false;       // the two-pass form is in use
   cudaGraphExec_t graph = nullptr;
   int graph_steps = 0;
@@ -340,6 +341,7 @@ int source_step(Ctx* c, double dt, bool dev) {
     L.heads = c->d_heads;
     L.head_count = c->d_head_count;
     L.run_last = c->d_run_last;
+    L.run_head = c->d_run_head;
   }
   if (c->pk.ntube) {
     const Packed& k = c->pk;
@@ -802,6 +804,7 @@ int edyn_init(const char* chem_dir, int nspe, int nequ, int ncell, int lvir, con
   CK(cudaMalloc(&c->d_heads, (size_t)ncell * sizeof(int)));
   CK(cudaMalloc(&c->d_head_count, sizeof(unsigned)));
   CK(cudaMalloc(&c->d_run_last, (size_t)((ncell + CHEM_RUN_BLOCK - 1) / CHEM_RUN_BLOCK) * sizeof(int)));
+  CK(cudaMalloc(&c->d_run_head, (size_t)ncell * sizeof(int)));
   // Long tubes are throughput-bound on the inert cells' one right-hand side
   // each, which the light screening pass runs at four warps per SM
   // sub-partition; short ones are bound by their costliest cell, which a
@@ -1078,15 +1081,18 @@ int edyn_upload(void* ctx, const double* qf_aos, const double* qc_aos) {
   if (!c || !c->qc) return EDYN_E_ARG;
   if (!qc_aos) return fail(c, EDYN_E_ARG, "Qc is required");
   const size_t bytes = (size_t)c->ne * c->n * sizeof(double);
-  int rc = ensure_staging(c, bytes);
+  // Qc and qf each in their half of the staging buffer: the copies back to
+  // back, then the transposes
+  int rc = ensure_staging(c, 2 * bytes);
   if (rc) return rc;
-  CK(cudaMemcpyAsync(c->staging, qc_aos, bytes, cudaMemcpyHostToDevice, c->stream));
-  for (const Seg& g : segs(c))
-    CK(launch_aos_to_soa(c->staging + g.first * c->ne, c->ne, g.n, c->qc + g.off, c->ld, c->stream));
+  double* sc = c->staging;
+  double* sf = c->staging + (size_t)c->ne * c->n;
+  CK(cudaMemcpyAsync(sc, qc_aos, bytes, cudaMemcpyHostToDevice, c->stream));
+  if (qf_aos) CK(cudaMemcpyAsync(sf, qf_aos, bytes, cudaMemcpyHostToDevice, c->stream));
+  for (const Seg& g : segs(c)) CK(launch_aos_to_soa(sc + g.first * c->ne, c->ne, g.n, c->qc + g.off, c->ld, c->stream));
   if (qf_aos) {
-    CK(cudaMemcpyAsync(c->staging, qf_aos, bytes, cudaMemcpyHostToDevice, c->stream));
     for (const Seg& g : segs(c))
-      CK(launch_aos_to_soa(c->staging + g.first * c->ne, c->ne, g.n, c->qf[c->cur] + g.off, c->ld, c->stream));
+      CK(launch_aos_to_soa(sf + g.first * c->ne, c->ne, g.n, c->qf[c->cur] + g.off, c->ld, c->stream));
   } else {
     for (const Seg& g : segs(c)) {
       StageArgs a = base_args(c);
@@ -1321,24 +1327,21 @@ int edyn_download(void* ctx, double* qf_aos, double* qc_aos, double* hrr) {
   Ctx* c = (Ctx*)ctx;
   if (!c || !c->qc) return EDYN_E_ARG;
   const size_t bytes = (size_t)c->ne * c->n * sizeof(double);
-  int rc = ensure_staging(c, bytes);
+  // qf and Qc each in their half of the staging buffer: both transposes,
+  // then the copies back to back and one wait
+  int rc = ensure_staging(c, 2 * bytes);
   if (rc) return rc;
-  if (qf_aos) {
+  double* sf = c->staging;
+  double* sc = c->staging + (size_t)c->ne * c->n;
+  if (qf_aos)
     for (const Seg& g : segs(c))
-      CK(launch_soa_to_aos(c->qf[c->cur] + g.off, c->ne, g.n, c->ld, c->staging + g.first * c->ne, c->stream));
-    CK(cudaMemcpyAsync(qf_aos, c->staging, bytes, cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaStreamSynchronize(c->stream));
-  }
-  if (qc_aos) {
-    for (const Seg& g : segs(c))
-      CK(launch_soa_to_aos(c->qc + g.off, c->ne, g.n, c->ld, c->staging + g.first * c->ne, c->stream));
-    CK(cudaMemcpyAsync(qc_aos, c->staging, bytes, cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaStreamSynchronize(c->stream));
-  }
-  if (hrr) {
-    CK(cudaMemcpyAsync(hrr, c->hrr, (size_t)c->n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaStreamSynchronize(c->stream));
-  }
+      CK(launch_soa_to_aos(c->qf[c->cur] + g.off, c->ne, g.n, c->ld, sf + g.first * c->ne, c->stream));
+  if (qc_aos)
+    for (const Seg& g : segs(c)) CK(launch_soa_to_aos(c->qc + g.off, c->ne, g.n, c->ld, sc + g.first * c->ne, c->stream));
+  if (qf_aos) CK(cudaMemcpyAsync(qf_aos, sf, bytes, cudaMemcpyDeviceToHost, c->stream));
+  if (qc_aos) CK(cudaMemcpyAsync(qc_aos, sc, bytes, cudaMemcpyDeviceToHost, c->stream));
+  if (hrr) CK(cudaMemcpyAsync(hrr, c->hrr, (size_t)c->n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
   return EDYN_OK;
 }
 
@@ -1646,6 +1649,7 @@ int edyn_finalize(void* ctx) {
   cudaFree(c->d_heads);
   cudaFree(c->d_head_count);
   cudaFree(c->d_run_last);
+  cudaFree(c->d_run_head);
   if (c->own) cudaStreamDestroy(c->own);
   delete c;
   return EDYN_OK;

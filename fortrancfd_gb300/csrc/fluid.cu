@@ -556,9 +556,17 @@ __global__ void __launch_bounds__(STAGE_MAX_THREADS) k_stage(StageArgs a) {
       Q[v * ld] = qs - (a.rk4_stage < 2 ? cq : c) * dF;
     }
   }
-  if (f < P && i < c1 && !rk4_mid) {
+  // the other stages: the update, then QcToqf. Cells of the tile whose new
+  // conserved columns and Newton start are equal bit for bit to their left
+  // neighbour's get that neighbour's primitives (a run's first cell computes
+  // them once): QcToqf is a function of those inputs alone.
+  const bool own = f < P && i < c1 && !rk4_mid;
+  const bool runs = skip_uniform && !rk4_mid;
+  const size_t ld = (size_t)a.ld;
+  const double Tg = own ? s_q[2 * Wd + f + LW] : 0.0;
+  double q[3] = {0.0, 0.0, 0.0};
+  if (own) {
     const double c = dt / tv.dx;
-    const size_t ld = (size_t)a.ld;
     double* Q = tv.qc + i + GHOST;
     double* Q0 = tv.q0 + i + GHOST;
     double* ys = s_r + f;  // strided by P
@@ -569,7 +577,7 @@ __global__ void __launch_bounds__(STAGE_MAX_THREADS) k_stage(StageArgs a) {
       if (a.kind == 2) return Q0[v * ld] + (1.0 / 6.0) * (tv.acc[v * ld + i + GHOST] + -(c * dF));
       return a.kind == 0 ? qv - c * dF : fma(a.h1, Q0[v * ld], a.h2 * (qv - c * dF));
     };
-    double q[3], qv[3];
+    double qv[3];
 #pragma unroll
     for (int v = 0; v < 3; ++v) qv[v] = Q[v * ld];
     __syncwarp(pair);  // every lane has read the bulk rows before lane v % SP rewrites row v
@@ -579,6 +587,8 @@ __global__ void __launch_bounds__(STAGE_MAX_THREADS) k_stage(StageArgs a) {
       if (v % SP == h) {
         if (a.save_q0) Q0[v * ld] = qv[v];
         Q[v * ld] = q[v];
+        // the bulk rows beside the species (s_r rows ns .. ns + 2) for the comparison
+        ys[(ns + v) * P] = q[v];
       }
     }
     for (int v = 3 + h; v < ne; v += SP) {
@@ -588,18 +598,56 @@ __global__ void __launch_bounds__(STAGE_MAX_THREADS) k_stage(StageArgs a) {
       Q[v * ld] = qn;
       ys[(v - 3) * P] = qn;
     }
+  }
+  __shared__ unsigned char s_dup[STAGE_MAX_CELLS + 2];
+  if (runs) {
+    __syncthreads();
+    if (own) {
+      bool same = f >= 1 && __double_as_longlong(Tg) == __double_as_longlong(s_q[2 * Wd + f - 1 + LW]);
+      for (int r = h; r < ne && same; r += SP)
+        same = __double_as_longlong(s_r[r * P + f]) == __double_as_longlong(s_r[r * P + f - 1]);
+      same = __all_sync(pair, same);
+      if (h == 0) s_dup[f] = same ? 1 : 0;
+    }
+    __syncthreads();
+  }
+  const bool head = own && !(runs && s_dup[f]);
+  if (head) {
+    double* ys = s_r + f;
     int iters;
-    const double Tg = s_q[2 * Wd + f + LW];
     CellEOS e = qc_to_qf_cell<SP>(q[0], q[1], q[2], ys, P, Tg, a.strict_newton != 0, iters, h, pair);
-    double* out = tv.qf_out + i + GHOST;
     if (h == 0) {
-      out[0] = q[0];
-      out[ld] = e.u;
-      out[2 * ld] = e.T;
+      if (runs) {
+        ys[(ns + 1) * P] = e.u;  // for the run's other cells
+        ys[(ns + 2) * P] = e.T;
+      } else {
+        double* out = tv.qf_out + i + GHOST;
+        out[0] = q[0];
+        out[ld] = e.u;
+        out[2 * ld] = e.T;
+      }
       if (tv.cvel) speed = cell_speed(e.u, e.T, e.Sz, e.cpR);
       if (e.status && a.err) atomicOr(a.err, e.status);
     }
-    for (int k = h; k < ns; k += SP) out[(3 + k) * ld] = ys[k * P];
+    if (!runs) {
+      double* out = tv.qf_out + i + GHOST;
+      for (int k = h; k < ns; k += SP) out[(3 + k) * ld] = ys[k * P];
+    }
+  }
+  if (runs) {
+    __syncthreads();
+    if (own) {
+      int hf = f;
+      while (s_dup[hf]) --hf;  // s_dup[0] is 0: the tile's first cell is a head
+      const double* src = s_r + hf;
+      double* out = tv.qf_out + i + GHOST;
+      if (h == 0) {
+        out[0] = q[0];
+        out[ld] = src[(ns + 1) * P];
+        out[2 * ld] = src[(ns + 2) * P];
+      }
+      for (int k = h; k < ns; k += SP) out[(3 + k) * ld] = src[k * P];
+    }
   }
   if (tv.cvel) {
     double m = speed;
@@ -936,16 +984,23 @@ cudaError_t launch_stage(const StageArgs& a, int acu, int lim, int wflag, int rm
 
 // flags[k] = 1 when species row k of the conserved state is nonzero in some
 // interior cell (one CTA per row).
+// flags[k] |= 1 when species row k holds a non-zero entry; blockIdx.y takes
+// one chunk of the row (flags cleared by the caller)
 __global__ void k_species_present(const double* qc, int ld, int n, int* flags) {
   const double* row = qc + (size_t)(3 + blockIdx.x) * ld + GHOST;
+  const int chunk = (n + gridDim.y - 1) / gridDim.y;
+  const int i0 = blockIdx.y * chunk, i1 = min(n, i0 + chunk);
   int any = 0;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) any |= (row[i] != 0.0) ? 1 : 0;
+  for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) any |= (row[i] != 0.0) ? 1 : 0;
   any = __syncthreads_or(any);
-  if (threadIdx.x == 0) flags[blockIdx.x] = any;
+  if (threadIdx.x == 0 && any) atomicOr(flags + blockIdx.x, 1);
 }
 
 cudaError_t launch_species_present(const double* qc, int ld, int n, int ns, int* flags, cudaStream_t s) {
-  k_species_present<<<ns, 256, 0, s>>>(qc, ld, n, flags);
+  cudaError_t e = cudaMemsetAsync(flags, 0, (size_t)ns * sizeof(int), s);
+  if (e != cudaSuccess) return e;
+  const int chunks = std::max(1, std::min(64, (n + 4095) / 4096));
+  k_species_present<<<dim3(ns, chunks), 256, 0, s>>>(qc, ld, n, flags);
   return cudaGetLastError();
 }
 

@@ -44,15 +44,13 @@ UNIT = "cell-steps/s"
 BYTES_PER_CELL_STEP = 4544  # algorithmic: fluid RK3 3632 B + chemistry 912 B per cell-step
 BYTES_CHEM_PER_CELL = 912   # chemistry launch: read qf (456 B) + write qf and Qc rows (456 B)
 L2_BYTES = 129 << 20
-# From ncu captures of one launch of each kernel of the 200,000-cell tube
-# (profiles/*_ch4_air_detonation_200000.md), scaled here by cells:
-# DRAM bytes (read + write) of the chemistry launch per cell (screening
-# pass 88.5 + 118.7 MB, listed pass 1.6 MB), and FP64 operations per
-# cell-step, 2 DFMA + DADD + DMUL thread instructions: three fluid stages of
-# 12,150 each, the screening pass's 33,450, the listed pass's 2,470.
-TRAFFIC_CHEM_PER_CELL = {"detonation_air_200k": (88.5e6 + 118.7e6 + 1.6e6) / 200000,
-                         "detonation_o2_20k": 1.93e6 / 4000, "detonation_air_20k": None}
-FP64_FLOPS_PER_CELL_STEP = {"detonation_air_200k": 3 * 12150 + 33450 + 2470}
+# From ncu captures of the 200,000-cell tube at the timed steps
+# (profiles/*_ch4_air_detonation_200000.md): DRAM bytes (read + write) of
+# the chemistry launch's kernels per cell and step, and FP64 operations per
+# step summed over one step's kernels (2 DFMA + DADD + DMUL thread
+# instructions: stages 2.17e8, integrator pass 3.2e7, screen 1.3e6).
+TRAFFIC_CHEM_PER_CELL = {"detonation_air_200k": None, "detonation_o2_20k": 1.93e6 / 4000, "detonation_air_20k": None}
+FP64_FLOPS_PER_STEP = {"detonation_air_200k": 2.50e8}
 
 WORKLOADS = {
     "detonation_air_200k": dict(ncell=200000, length=1.0, oxidizer="air"),
@@ -420,16 +418,16 @@ def gpu_arm(args, rank, world, local):
             "traffic": (TRAFFIC_CHEM_PER_CELL[args.workload] * case.ncell
                         if TRAFFIC_CHEM_PER_CELL[args.workload] else None),
             "launch_ms": chem_s * 1e3, "fluid_step_ms": fluid_s * 1e3,
-            "note": "the chemistry launch is FP64-pipe bound (see fp64); its HBM fraction only shows that memory "
-                    "is not the limit"}
+            "note": "the chemistry launch lasts as long as its stiffest cells' sequential integrations (one SM "
+                    "each): latency, not bandwidth; its HBM fraction only shows that memory is not the limit"}
     p64 = fp64_peak(dev)
-    fpc = FP64_FLOPS_PER_CELL_STEP.get(args.workload)
+    fps = FP64_FLOPS_PER_STEP.get(args.workload)
     fp64 = {"bound": "fp64", "scope": "whole step", "peak": p64, "unit": "TFLOP/s",
             "peak_source": "cuBLAS DGEMM 4096^3, best of 5, this run", "rhs_launches": rhs}
-    if fpc:
-        ach = fpc * case.ncell * args.steps / t_max / world / 1e12
-        fp64.update(achieved=ach, flops_per_cell_step=fpc, frac=ach / p64,
-                    source="FP64 instructions per cell from ncu captures of each kernel (profiles/)")
+    if fps:
+        ach = fps * args.steps / t_max / 1e12
+        fp64.update(achieved=ach, flops_per_step=fps, frac=ach / p64,
+                    source="FP64 instructions of one step's kernels, ncu capture of the timed steps (profiles/)")
     cpu = None if args.no_cpu_baseline or world > 1 else cpu_baseline(case)
     surr = None
     if not args.no_surrogate and world == 1 and "air" in case.name:
@@ -438,8 +436,10 @@ def gpu_arm(args, rank, world, local):
         except Exception as ex:  # reported, not hidden: the headline line still prints
             surr = {"error": f"{type(ex).__name__}: {ex}"}
     # kernels per step: the loop test, the fluid stages, the chemistry
-    # (counter clear + one pass, or + screen pass and the two team-pick kernels)
-    per_step = 1 + 3 + (5 if case.ncell >= 50000 else 2)
+    # (counter clear + one pass; or, from 50,000 cells, counter clear, runs,
+    # screening pass, followers, integrator pass, integrated followers and
+    # the two team-pick kernels)
+    per_step = 1 + 3 + (8 if case.ncell >= 50000 else 2)
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",

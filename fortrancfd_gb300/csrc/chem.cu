@@ -2588,6 +2588,8 @@ __global__ void __launch_bounds__(SCREEN_WARPS * 32, 1)
   extern __shared__ __align__(16) char smem[];
   __shared__ int s_last;
   if (L.step_active && *L.step_active == 0) return;
+  // over run heads, a CTA with none exits before staging the tables
+  if (L.heads && blockIdx.x * (blockDim.x >> 5) >= *L.head_count) return;
   const double dt_launch = L.dt_dev ? *L.dt_dev : L.dt;
   stage_tables(smem, g_tab, tab_bytes);
   const Tabs t = bind_tabs(smem);
@@ -2743,7 +2745,22 @@ __device__ __forceinline__ bool on_hot_list(const unsigned* s_hot, int c) {
 __device__ __forceinline__ void copy_result(const ChemLaunch& L, int h, int c) {
   const size_t ld = (size_t)L.ld;
   const size_t ch = cell_col(L, h) + GHOST, cc = cell_col(L, c) + GHOST;
-  for (int row = 2; row < L.nrow; ++row) {
+  int row = 2;
+  // eight rows of both arrays in flight, then their stores
+  for (; row + 8 <= L.nrow; row += 8) {
+    double a[8], b[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      a[k] = L.qf[(row + k) * ld + ch];
+      b[k] = L.qc[(row + k) * ld + ch];
+    }
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      L.qf[(row + k) * ld + cc] = a[k];
+      L.qc[(row + k) * ld + cc] = b[k];
+    }
+  }
+  for (; row < L.nrow; ++row) {
     L.qf[row * ld + cc] = L.qf[row * ld + ch];
     L.qc[row * ld + cc] = L.qc[row * ld + ch];
   }
@@ -2930,7 +2947,12 @@ __global__ void k_hot_classes(const int* cost, int n, unsigned char* cls, unsign
   for (int j = max(0, i - 2); j <= min(n - 1, i + 2); ++j) m = max(m, cost[j]);
   const int c = m >= HOT_MIN_RHS ? 31 - __clz(m) : 0;
   cls[i] = (unsigned char)c;
-  if (c) atomicAdd(&hist[c], 1u);
+  if (c) {
+    atomicAdd(&hist[c], 1u);
+    // the candidates' range: first = n - hist[33], last = hist[34] - 1
+    atomicMax(&hist[33], (unsigned)(n - i));
+    atomicMax(&hist[34], (unsigned)(i + 1));
+  }
 }
 
 // One CTA: the smallest class threshold whose cells fit in HOT_MAX (the top
@@ -2960,8 +2982,10 @@ __global__ void __launch_bounds__(1024) k_hot_pick(const unsigned char* cls, int
   const int B = s_B;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   // four consecutive cells a thread per round (4096 a round): a warp-shuffle
-  // scan of the per-thread counts and a scan of the warp totals
-  for (int c0 = 0; c0 < n && B < 32; c0 += 4 * (int)blockDim.x) {
+  // scan of the per-thread counts and a scan of the warp totals; the rounds
+  // span the candidates' range only
+  const int first = hist[33] ? n - (int)hist[33] : n, last = (int)hist[34];
+  for (int c0 = first & ~3; c0 < last && B < 32; c0 += 4 * (int)blockDim.x) {
     const int base = c0 + 4 * threadIdx.x;
     int f[4];
 #pragma unroll
@@ -3502,7 +3526,7 @@ cudaError_t chem_launch_tube_listed(ChemState& s, const ChemLaunch& L0, int* lis
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   if (L.cost && L.hot) {
-    e = cudaMemsetAsync(hist, 0, 33 * sizeof(unsigned), st);
+    e = cudaMemsetAsync(hist, 0, 35 * sizeof(unsigned), st);
     if (e != cudaSuccess) return e;
     k_hot_classes<<<(L.n + 255) / 256, 256, 0, st>>>(L.cost, L.n, cls, hist);
     k_hot_pick<<<1, 1024, 0, st>>>(cls, L.n, hist, L.hot);

@@ -713,7 +713,26 @@ __global__ void k_cvel(const double* qf, int n, int ld, unsigned long long* cvel
   const ThermoTable& tb = c_thermo;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   double sp = 0.0;
-  if (i < n) {
+  // a cell whose column (u, T, Y) equals its left neighbour's in the same
+  // tube bit for bit has the same signal speed, which the neighbour brings
+  bool same = false;
+  if (i > 0 && i < n && (!tube_of || tube_of[i] == tube_of[i - 1])) {
+    const double* q = qf + (colmap ? colmap[i] : i) + GHOST;
+    const double* r = qf + (colmap ? colmap[i - 1] : i - 1) + GHOST;
+    same = true;
+    for (int row = 1; row < 3 + tb.ns && same; row += 8) {
+      long long x[8], y[8];
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        const int rr = min(row + k, 2 + tb.ns);
+        x[k] = __double_as_longlong(q[rr * (size_t)ld]);
+        y[k] = __double_as_longlong(r[rr * (size_t)ld]);
+      }
+#pragma unroll
+      for (int k = 0; k < 8; ++k) same = same && x[k] == y[k];
+    }
+  }
+  if (i < n && !same) {
     const double* q = qf + (colmap ? colmap[i] : i) + GHOST;
     const double T = q[2 * (size_t)ld];
     Premix pm;
@@ -733,7 +752,7 @@ __global__ void k_cvel(const double* qf, int n, int ld, unsigned long long* cvel
     sp = fabs(q[ld]) + a;
   }
   if (tube_of) {
-    if (i < n) atomic_max_pos(cvel + tube_of[i], sp);
+    if (i < n && !same) atomic_max_pos(cvel + tube_of[i], sp);
     return;
   }
   double m = sp;

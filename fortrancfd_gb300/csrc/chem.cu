@@ -2556,6 +2556,7 @@ __global__ void __launch_bounds__(MAXW * 32, 1)
     if (lane == 0) w.y0[ns] = y[nrow - 1];
     __syncwarp();
     finish_cell<32, WarpWork>(t, tm, w, L, (unsigned)L.pk_idx[j], L.pk_dt[j], speed_max);
+    if (lane == 0 && L.cost) L.cost[L.pk_idx[j]] = 1;
   }
   if (L.cvel_out && lane == 0 && speed_max > 0.0)
     atomicMax(L.cvel_out, (unsigned long long)__double_as_longlong(speed_max));
@@ -2589,7 +2590,7 @@ __global__ void __launch_bounds__(SCREEN_WARPS * 32, 1)
   __shared__ int s_last;
   if (L.step_active && *L.step_active == 0) return;
   // over run heads, a CTA with none exits before staging the tables
-  if (L.heads && blockIdx.x * (blockDim.x >> 5) >= *L.head_count) return;
+  if (L.heads && !L.pk_count && blockIdx.x * (blockDim.x >> 5) >= *L.head_count) return;
   const double dt_launch = L.dt_dev ? *L.dt_dev : L.dt;
   stage_tables(smem, g_tab, tab_bytes);
   const Tabs t = bind_tabs(smem);
@@ -2671,7 +2672,9 @@ __global__ void __launch_bounds__(SCREEN_WARPS * 32, 1)
         L.pk_idx[j] = (int)cell;
         L.pk_rho[j] = rho;
         L.pk_dt[j] = dt;
-        if (L.cost) L.cost[cell] = 1;
+        // over run heads: -3 until the surrogate path's finish, which the
+        // head's followers wait for (k_follow)
+        if (L.cost) L.cost[cell] = L.heads ? -3 : 1;
       }
       ++listed;
     } else {
@@ -2885,7 +2888,10 @@ __global__ void __launch_bounds__(RUN_THREADS) k_follow(ChemLaunch L, ChemCounte
       if (L.cost[h] == 1) {
         copy_result(L, h, c);  // finished by the screening pass
         ++copied;
-      } else if (!L.hlast || __double_as_longlong(L.hlast[c]) == __double_as_longlong(L.hlast[h])) {
+      } else if (L.cost[h] == -3 || !L.hlast ||
+                 __double_as_longlong(L.hlast[c]) == __double_as_longlong(L.hlast[h])) {
+        // the head's result comes from the surrogate path (a function of the
+        // state alone) or from an integration that starts like this cell's
         L.run_flag[c] = 3;  // takes the head's integrated result
         L.run_head[c] = h;
         L.cost[c] = -2;
@@ -3538,9 +3544,23 @@ cudaError_t chem_launch_tube_listed(ChemState& s, const ChemLaunch& L0, int* lis
 cudaError_t chem_launch_screen_packed(ChemState& s, const ChemLaunch& L, cudaStream_t st) {
   cudaError_t e = cudaMemsetAsync(s.d_count, 0, sizeof(ChemCounters), st);
   if (e != cudaSuccess) return e;
+  const int nblk = (L.n + RUN_BLOCK - 1) / RUN_BLOCK;
+  if (L.heads) {
+    e = cudaMemsetAsync(L.head_count, 0, sizeof(unsigned), st);
+    if (e != cudaSuccess) return e;
+    k_runs<<<nblk, RUN_THREADS, 0, st>>>(L);
+  }
   const int sgrid = std::min(s.screen_ctas, (L.n + s.screen_warps - 1) / s.screen_warps);
   k_tube_screen<<<std::max(1, sgrid), s.screen_warps * 32, s.screen_smem, st>>>((const char*)s.d_tables,
                                                                               (int)s.table_bytes, L, s.d_count);
+  e = cudaGetLastError();
+  if (e == cudaSuccess && L.heads) k_follow<<<nblk, RUN_THREADS, 0, st>>>(L, s.d_count);
+  return cudaGetLastError();
+}
+
+cudaError_t chem_follow_packed(ChemState& s, const ChemLaunch& L, cudaStream_t st) {
+  if (!L.heads) return cudaSuccess;
+  k_follow_integrated<<<(L.n + RUN_BLOCK - 1) / RUN_BLOCK, RUN_THREADS, 0, st>>>(L, s.d_count);
   return cudaGetLastError();
 }
 

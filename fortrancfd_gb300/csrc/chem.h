@@ -117,6 +117,8 @@ cudaError_t chem_read_counters(ChemState& s, ChemCounters* out, cudaStream_t st)
 // Finishes the m packed rows of a screened tube launch from their states
 // after the step (pk_y1): adjust_sum, HRR, qfToQc, QcToqf, signal speed.
 cudaError_t chem_finish_packed(ChemState& s, const ChemLaunch& L, int m, const double* pk_y1, cudaStream_t st);
+// The followers of packed heads take their heads' finished columns (runs).
+cudaError_t chem_follow_packed(ChemState& s, const ChemLaunch& L, cudaStream_t st);
 // HRR_dot [W/m^3] of n tube cells from their primitive rows (qf, SoA with ld)
 // and the temperatures their last chemistry step ended with.
 cudaError_t chem_hrr_dot(ChemState& s, int n, int ld, const double* qf, const double* tchem, double* out,

@@ -410,6 +410,15 @@ int surrogate_source_step(Ctx* c, double dt, bool dev) {
   L.max_steps = c->chem_max_steps;
   L.precheck = c->precheck;
   L.screen = 1;
+  if (c->skip_uniform) {
+    // runs of identical cells: only their heads are screened and packed
+    L.nrow = c->ne;
+    L.run_flag = c->d_run_flag;
+    L.heads = c->d_heads;
+    L.head_count = c->d_head_count;
+    L.run_last = c->d_run_last;
+    L.run_head = c->d_run_head;
+  }
   L.pk_count = z.d_count;
   L.pk_idx = z.pk_idx;
   L.pk_rho = z.pk_rho;
@@ -427,7 +436,11 @@ int surrogate_source_step(Ctx* c, double dt, bool dev) {
   for (double& v : z.stats) v = 0.0;
   z.stats[0] = m;
   z.stats[4] = (double)k0.rhs;
-  if (m == 0) return EDYN_OK;
+  if (m == 0) {
+    e = chem_follow_packed(cs, L, st);
+    if (e != cudaSuccess) return fail(c, EDYN_E_CUDA, "followers: %s", cudaGetErrorString(e));
+    return EDYN_OK;
+  }
   const int ns = z.nrow - 1;
   const int M = (m + 127) / 128 * 128;
   void* sv = (void*)st;
@@ -498,6 +511,8 @@ int surrogate_source_step(Ctx* c, double dt, bool dev) {
   }
   e = chem_finish_packed(cs, L, m, z.pk_y1, st);
   if (e != cudaSuccess) return fail(c, EDYN_E_CUDA, "packed finish launch: %s", cudaGetErrorString(e));
+  e = chem_follow_packed(cs, L, st);
+  if (e != cudaSuccess) return fail(c, EDYN_E_CUDA, "followers: %s", cudaGetErrorString(e));
   return EDYN_OK;
 }
 

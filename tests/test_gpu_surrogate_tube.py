@@ -50,8 +50,11 @@ def held_out():
     return S.tube_sweep(1, seed=7)[0]
 
 
-def _run(case, mode, surr, use_net=True, steps=STEPS):
+def _run(case, mode, surr, use_net=True, steps=STEPS, runs=False):
     g = Tube(case.ncell, case.dx, strict_newton=0, rtol=1e-5, atol=1e-13, chem_mode=mode, **case.flags)
+    # every cell through the surrogate path unless runs of identical cells
+    # are asked for (then only their heads are, with the same results)
+    g.set_uniform_skip(runs)
     if mode == 1:
         g.set_surrogate(surr if use_net else None)
     g.init_cells(case.T, case.p, case.u, case.X)
@@ -83,3 +86,24 @@ def test_network_gains_over_the_method_without_it(trained, held_out):
     assert with_net["accepted_network"] > 0, with_net
     assert with_net["fallback"] < without["fallback"], (with_net, without)
     assert with_net["fallback_rhs"] < without["fallback_rhs"], (with_net, without)
+
+
+def test_runs_of_identical_cells_are_bit_for_bit(trained, held_out):
+    """The surrogate path over run heads only (followers take their head's
+    finished column) gives the same bits as every cell through it."""
+    out = []
+    for runs in (True, False):
+        g = Tube(held_out.ncell, held_out.dx, strict_newton=0, rtol=1e-5, atol=1e-13, chem_mode=1, **held_out.flags)
+        g.set_uniform_skip(runs)
+        g.set_surrogate(trained)
+        g.init_cells(held_out.T, held_out.p, held_out.u, held_out.X)
+        handed = 0
+        for _ in range(10):
+            g.step(held_out.cfl)
+            handed += g.surrogate_stats()["handed"]
+        out.append((g.download(), handed))
+        g.close()
+    (a, ha), (b, hb) = out
+    assert 0 < ha < hb, (ha, hb)
+    for x, y in zip(a, b):
+        assert np.array_equal(x, y)

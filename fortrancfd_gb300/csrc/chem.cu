@@ -185,7 +185,7 @@ struct alignas(16) WarpWork {
 
 constexpr int TEAM = 128;        // threads of a four-warp team
 constexpr int TEAM_PIECES = 128; // gather pieces per warp row of a team's partial sums
-constexpr int HOT_MIN_RHS = 64;  // right-hand sides in the last call that make a cell hot
+constexpr int HOT_MIN_RHS = 32;  // right-hand sides in the last call that make a cell hot
 
 __device__ __forceinline__ double clip0_d(double x) { return __double_as_longlong(x) < 0 ? 0.0 : x; }
 

@@ -436,10 +436,10 @@ def gpu_arm(args, rank, world, local):
         except Exception as ex:  # reported, not hidden: the headline line still prints
             surr = {"error": f"{type(ex).__name__}: {ex}"}
     # kernels per step: the loop test, the fluid stages, the chemistry
-    # (counter clear + one pass; or, from 50,000 cells, counter clear, runs,
+    # (counter clear + one pass; or, from 10,000 cells, counter clear, runs,
     # screening pass, followers, integrator pass, integrated followers and
     # the two team-pick kernels)
-    per_step = 1 + 3 + (8 if case.ncell >= 50000 else 2)
+    per_step = 1 + 3 + (8 if case.ncell >= 10000 else 2)
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",

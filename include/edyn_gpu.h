@@ -200,7 +200,7 @@ int edyn_chem_rhs_tube(void* ctx, int n, const double* rho_d, const double* yiT_
  * light screening pass evaluates f(y0) and the inert-cell test of every cell
  * at four warps per SM sub-partition and finishes the inert cells; the
  * integrator kernel then takes only the cells it listed), 0 automatic (two
- * passes from 50,000 cells). The forms agree up to rounding: a cell on the
+ * passes from 10,000 cells). The forms agree up to rounding: a cell on the
  * four-warp team list that turns out inert is finished by its team in one
  * pass and by a single warp in two, whose sums run in other orders. No
  * counterpart in the reference (a tuning knob of this implementation). */

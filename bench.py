@@ -41,15 +41,21 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 METRIC = "cell-steps/s on 1 GB300: surrogate vs plain chemistry at ≤1e-3 species err"
 UNIT = "cell-steps/s"
-BYTES_PER_CELL_STEP = 4544  # algorithmic: fluid RK3 3632 B + chemistry 912 B per cell-step
 BYTES_CHEM_PER_CELL = 912   # chemistry launch: read qf (456 B) + write qf and Qc rows (456 B)
+# one SSP-RK3 stage moves five rows of nequ doubles per cell: stage 1 reads
+# qf, Qc and writes qf', Qc, Q0; stages 2-3 read qf, Qc, Q0 and write qf', Qc
+STAGE_ROWSETS = 5
 L2_BYTES = 129 << 20
 # From ncu captures of the 200,000-cell tube at the timed steps
 # (profiles/*_ch4_air_detonation_200000.md): DRAM bytes (read + write) of
 # the chemistry launch's kernels per cell and step, and FP64 operations per
 # step summed over one step's kernels (2 DFMA + DADD + DMUL thread
 # instructions: stages 2.17e8, integrator pass 3.2e7, screen 1.3e6).
-TRAFFIC_CHEM_PER_CELL = {"detonation_air_200k": None, "detonation_o2_20k": 1.93e6 / 4000, "detonation_air_20k": None}
+TRAFFIC_CHEM_PER_CELL = {"detonation_air_200k": 211.6e6 / 200000, "detonation_o2_20k": 1.93e6 / 4000,
+                         "detonation_air_20k": None}
+# DRAM read + write of one stage launch per cell (ncu, the 200k tube: 179.8 +
+# 210.6 MB)
+TRAFFIC_STAGE_PER_CELL = {"detonation_air_200k": (179.8e6 + 210.6e6) / 200000}
 FP64_FLOPS_PER_STEP = {"detonation_air_200k": 2.50e8}
 
 WORKLOADS = {
@@ -411,15 +417,23 @@ def gpu_arm(args, rank, world, local):
     if rank != 0:
         return
     hbm, src = peaks()
-    achieved = BYTES_CHEM_PER_CELL * case.ncell / chem_s / 1e9
-    roof = {"bound": "hbm", "kernel": "chemistry launch (k_tube_screen + k_tube_chem)", "achieved": achieved,
-            "peak": hbm, "peak_source": src,
-            "unit": "GB/s", "frac": achieved / hbm,
-            "traffic": (TRAFFIC_CHEM_PER_CELL[args.workload] * case.ncell
-                        if TRAFFIC_CHEM_PER_CELL[args.workload] else None),
-            "launch_ms": chem_s * 1e3, "fluid_step_ms": fluid_s * 1e3,
-            "note": "the chemistry launch lasts as long as its stiffest cells' sequential integrations (one SM "
-                    "each): latency, not bandwidth; its HBM fraction only shows that memory is not the limit"}
+    # the dominant kernel by time: the fluid stage (three launches a step)
+    stage_s = fluid_s / 3.0
+    stage_bytes = STAGE_ROWSETS * tube.nequ * 8 * case.ncell
+    achieved = stage_bytes / stage_s / 1e9
+    ts = TRAFFIC_STAGE_PER_CELL.get(args.workload)
+    chem_ach = BYTES_CHEM_PER_CELL * case.ncell / chem_s / 1e9
+    roof = {"bound": "hbm", "kernel": "k_stage (one of the three fluid stages of a step)", "achieved": achieved,
+            "peak": hbm, "peak_source": src, "unit": "GB/s", "frac": achieved / hbm,
+            "traffic": ts * case.ncell if ts else None, "algorithmic_bytes": stage_bytes,
+            "launch_ms": stage_s * 1e3, "fluid_step_ms": fluid_s * 1e3,
+            "note": "a stage moves five rows of nequ doubles per cell; in uniform regions it computes no faces, "
+                    "and what remains is per-tile latency (window load, one QcToqf per run of equal columns)",
+            "chemistry_launch": {"achieved": chem_ach, "frac": chem_ach / hbm, "launch_ms": chem_s * 1e3,
+                                 "traffic": (TRAFFIC_CHEM_PER_CELL[args.workload] * case.ncell
+                                             if TRAFFIC_CHEM_PER_CELL[args.workload] else None),
+                                 "note": "lasts as long as its stiffest cells' sequential integrations (one SM "
+                                         "each): latency, not bandwidth"}}
     p64 = fp64_peak(dev)
     fps = FP64_FLOPS_PER_STEP.get(args.workload)
     fp64 = {"bound": "fp64", "scope": "whole step", "peak": p64, "unit": "TFLOP/s",

@@ -226,7 +226,7 @@ StageArgs base_args(Ctx* c) {
   a.skip_uniform = c->skip_uniform;
   if (c->pk.ntube) {
     const Packed& k = c->pk;
-    a.tubes = TubeTab{k.d_tiles, k.d_n, k.d_off, k.d_dx, k.d_p_out, k.d_dt, k.d_active, k.d_time, k.ntiles};
+    a.tubes = TubeTab{k.d_tiles, k.d_n, k.d_off, k.d_dx, k.d_p_out, k.d_dt, k.d_active, k.d_time, k.ntiles, k.colmap, k.tube_of};
   }
   return a;
 }

@@ -38,6 +38,8 @@ struct TubeTab {
   const int* active;       // each tube steps in this step (its time < tend)
   double* time;            // simulated time of each tube
   int ntiles;              // stage CTAs of all tubes
+  const int* colmap;       // column of each cell (its tube's block offset + its index)
+  const int* tube_of;      // tube of each cell
 };
 
 struct StageArgs {

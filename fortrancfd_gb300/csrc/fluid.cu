@@ -556,12 +556,11 @@ __global__ void __launch_bounds__(STAGE_MAX_THREADS) k_stage(StageArgs a) {
       Q[v * ld] = qs - (a.rk4_stage < 2 ? cq : c) * dF;
     }
   }
-  // the other stages: the update, then QcToqf. Cells of the tile whose new
-  // conserved columns and Newton start are equal bit for bit to their left
-  // neighbour's get that neighbour's primitives (a run's first cell computes
-  // them once): QcToqf is a function of those inputs alone.
+  // the other stages: the update, then QcToqf, which with the uniform-region
+  // shortcuts on is left to k_qc_to_qf_runs (one QcToqf per run of equal
+  // conserved columns in a block of the tube, after every tile is updated).
   const bool own = f < P && i < c1 && !rk4_mid;
-  const bool runs = skip_uniform && !rk4_mid;
+  const bool defer = skip_uniform && !rk4_mid;
   const size_t ld = (size_t)a.ld;
   const double Tg = own ? s_q[2 * Wd + f + LW] : 0.0;
   double q[3] = {0.0, 0.0, 0.0};
@@ -587,8 +586,6 @@ __global__ void __launch_bounds__(STAGE_MAX_THREADS) k_stage(StageArgs a) {
       if (v % SP == h) {
         if (a.save_q0) Q0[v * ld] = qv[v];
         Q[v * ld] = q[v];
-        // the bulk rows beside the species (s_r rows ns .. ns + 2) for the comparison
-        ys[(ns + v) * P] = q[v];
       }
     }
     for (int v = 3 + h; v < ne; v += SP) {
@@ -599,55 +596,19 @@ __global__ void __launch_bounds__(STAGE_MAX_THREADS) k_stage(StageArgs a) {
       ys[(v - 3) * P] = qn;
     }
   }
-  __shared__ unsigned char s_dup[STAGE_MAX_CELLS + 2];
-  if (runs) {
-    __syncthreads();
-    if (own) {
-      bool same = f >= 1 && __double_as_longlong(Tg) == __double_as_longlong(s_q[2 * Wd + f - 1 + LW]);
-      for (int r = h; r < ne && same; r += SP)
-        same = __double_as_longlong(s_r[r * P + f]) == __double_as_longlong(s_r[r * P + f - 1]);
-      same = __all_sync(pair, same);
-      if (h == 0) s_dup[f] = same ? 1 : 0;
-    }
-    __syncthreads();
-  }
-  const bool head = own && !(runs && s_dup[f]);
-  if (head) {
+  if (own && !defer) {
     double* ys = s_r + f;
     int iters;
     CellEOS e = qc_to_qf_cell<SP>(q[0], q[1], q[2], ys, P, Tg, a.strict_newton != 0, iters, h, pair);
+    double* out = tv.qf_out + i + GHOST;
     if (h == 0) {
-      if (runs) {
-        ys[(ns + 1) * P] = e.u;  // for the run's other cells
-        ys[(ns + 2) * P] = e.T;
-      } else {
-        double* out = tv.qf_out + i + GHOST;
-        out[0] = q[0];
-        out[ld] = e.u;
-        out[2 * ld] = e.T;
-      }
+      out[0] = q[0];
+      out[ld] = e.u;
+      out[2 * ld] = e.T;
       if (tv.cvel) speed = cell_speed(e.u, e.T, e.Sz, e.cpR);
       if (e.status && a.err) atomicOr(a.err, e.status);
     }
-    if (!runs) {
-      double* out = tv.qf_out + i + GHOST;
-      for (int k = h; k < ns; k += SP) out[(3 + k) * ld] = ys[k * P];
-    }
-  }
-  if (runs) {
-    __syncthreads();
-    if (own) {
-      int hf = f;
-      while (s_dup[hf]) --hf;  // s_dup[0] is 0: the tile's first cell is a head
-      const double* src = s_r + hf;
-      double* out = tv.qf_out + i + GHOST;
-      if (h == 0) {
-        out[0] = q[0];
-        out[ld] = src[(ns + 1) * P];
-        out[2 * ld] = src[(ns + 2) * P];
-      }
-      for (int k = h; k < ns; k += SP) out[(3 + k) * ld] = src[k * P];
-    }
+    for (int k = h; k < ns; k += SP) out[(3 + k) * ld] = ys[k * P];
   }
   if (tv.cvel) {
     double m = speed;
@@ -665,6 +626,136 @@ __global__ void __launch_bounds__(STAGE_MAX_THREADS) k_stage(StageArgs a) {
     // No CTA of this kernel reads the clock; k_step_begin of the next step does.
     *a.time = *a.time + dt;
     *a.nsteps = *a.nsteps + 1;
+  }
+}
+
+
+// ---------------------------------------------------------------------------
+// QcToqf of a stage with the uniform-region shortcuts: one CTA per block of
+// QR_BLOCK cells. A cell whose new conserved column and Newton start (its
+// input T) equal its left neighbour's bit for bit, in the same tube and
+// block, takes that neighbour's primitives; each run's first cell computes
+// them (one group of STAGE_SPLIT lanes per cell, the stage kernel's own
+// qc_to_qf_cell, so the results are bit for bit the stage's), then the
+// others copy its column. Cells of tubes that do not step are left alone.
+// ---------------------------------------------------------------------------
+constexpr int QR_BLOCK = 1024;
+constexpr int QR_THREADS = 256;
+
+__global__ void __launch_bounds__(QR_THREADS) k_qc_to_qf_runs(StageArgs a) {
+  constexpr int SP = STAGE_SPLIT, PER = QR_BLOCK / QR_THREADS, NG = QR_THREADS / SP;
+  extern __shared__ double s_ys[];  // [NG][ne]: each group's species scratch
+  __shared__ unsigned char s_fl[QR_BLOCK];
+  __shared__ int s_hd[QR_BLOCK];
+  __shared__ int s_list[QR_BLOCK];
+  __shared__ int s_w[QR_THREADS / 32];
+  __shared__ int s_nh;
+  if (a.step_active && *a.step_active == 0) return;
+  const int ns = a.ns, ne = ns + 3;
+  const size_t ld = (size_t)a.ld;
+  const int b0 = blockIdx.x * QR_BLOCK, tid = threadIdx.x, lane = tid & 31, wq = tid >> 5;
+  const int* cm = a.tubes.colmap;
+  const int* to = a.tubes.tube_of;
+  auto col = [&](int c) { return (size_t)(cm ? cm[c] : c) + GHOST; };
+  auto tube = [&](int c) { return to ? to[c] : 0; };
+  if (tid == 0) s_nh = 0;
+  // 1. flags (0: not stepping, 1: head, 2: follower), four consecutive cells
+  //    a thread, and the last head at or before each cell (a max scan)
+  const int j0 = tid * PER;
+  int hp[PER];
+  int run = -1;
+#pragma unroll
+  for (int k = 0; k < PER; ++k) {
+    const int j = j0 + k, c = b0 + j;
+    unsigned char fl = 0;
+    if (c < a.n && (!a.tubes.active || !to || a.tubes.active[tube(c)] != 0)) {
+      bool same = j > 0 && tube(c) == tube(c - 1);
+      if (same) {
+        const size_t qc = col(c), qr = col(c - 1);
+        same = __double_as_longlong(a.qf_in[2 * ld + qc]) == __double_as_longlong(a.qf_in[2 * ld + qr]);
+        for (int row = 0; row < ne && same; row += 8) {
+          long long x[8], y[8];
+#pragma unroll
+          for (int m = 0; m < 8; ++m) {
+            const int rr = min(row + m, ne - 1);
+            x[m] = __double_as_longlong(a.qc[rr * ld + qc]);
+            y[m] = __double_as_longlong(a.qc[rr * ld + qr]);
+          }
+#pragma unroll
+          for (int m = 0; m < 8; ++m) same = same && x[m] == y[m];
+        }
+      }
+      fl = same ? 2 : 1;
+    }
+    s_fl[j] = fl;
+    if (fl == 1) run = j;
+    hp[k] = run;
+  }
+  int v = run;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int t = __shfl_up_sync(0xffffffffu, v, o);
+    if (lane >= o) v = max(v, t);
+  }
+  if (lane == 31) s_w[wq] = v;
+  __syncthreads();
+  int prev = __shfl_up_sync(0xffffffffu, v, 1);
+  if (lane == 0) prev = -1;
+  for (int q = 0; q < wq; ++q) prev = max(prev, s_w[q]);
+#pragma unroll
+  for (int k = 0; k < PER; ++k) {
+    s_hd[j0 + k] = max(prev, hp[k]);
+    if (s_fl[j0 + k] == 1) s_list[atomicAdd(&s_nh, 1)] = j0 + k;
+  }
+  __syncthreads();
+  // 2. the heads: QcToqf by groups of SP lanes
+  const int g = tid / SP, h = tid % SP;
+  const unsigned pair = ((1u << SP) - 1u) << (tid & 31 & ~(SP - 1));
+  double* ys = s_ys + (size_t)g * ne;
+  const int nh = s_nh;
+  double speed = 0.0;
+  for (int q = g; q < nh; q += NG) {
+    const int c = b0 + s_list[q];
+    const size_t cc = col(c);
+    const double q0 = a.qc[cc], q1 = a.qc[ld + cc], q2 = a.qc[2 * ld + cc];
+    for (int k = h; k < ns; k += SP) ys[k] = a.qc[(3 + k) * ld + cc];
+    __syncwarp(pair);
+    int iters;
+    const CellEOS e = qc_to_qf_cell<SP>(q0, q1, q2, ys, 1, a.qf_in[2 * ld + cc], a.strict_newton != 0, iters, h, pair);
+    double* out = a.qf_out + cc;
+    if (h == 0) {
+      out[0] = q0;
+      out[ld] = e.u;
+      out[2 * ld] = e.T;
+      if (e.status && a.err) atomicOr(a.err, e.status);
+      if (a.cvel_out) {
+        const double sp = cell_speed(e.u, e.T, e.Sz, e.cpR);
+        if (to) atomic_max_pos(a.cvel_out + tube(c), sp);
+        else speed = fmax(speed, sp);
+      }
+    }
+    for (int k = h; k < ns; k += SP) out[(3 + k) * ld] = ys[k];
+    __syncwarp(pair);
+  }
+  if (a.cvel_out && !to) {
+    double m = speed;
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if (lane == 0 && m > 0.0) atomic_max_pos(a.cvel_out, m);
+  }
+  __syncthreads();  // every head's column is written
+  // 3. the followers copy their head's column (eight rows in flight)
+  for (int j = tid; j < QR_BLOCK; j += QR_THREADS) {
+    if (s_fl[j] != 2) continue;
+    const size_t cc = col(b0 + j), ch = col(b0 + s_hd[j]);
+    for (int row = 0; row < ne; row += 8) {
+      double x[8];
+#pragma unroll
+      for (int m = 0; m < 8; ++m)
+        if (row + m < ne) x[m] = a.qf_out[(row + m) * ld + ch];
+#pragma unroll
+      for (int m = 0; m < 8; ++m)
+        if (row + m < ne) a.qf_out[(row + m) * ld + cc] = x[m];
+    }
   }
 }
 
@@ -998,7 +1089,15 @@ cudaError_t launch_stage(const StageArgs& a, int acu, int lim, int wflag, int rm
   if (e != cudaSuccess) return e;
   const int grid = a.tubes.tiles ? a.tubes.ntiles : (a.n + a.tc - 1) / a.tc;
   kern<<<grid, stage_threads(a.tc), smem, s>>>(a);
-  return cudaGetLastError();
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  // with the uniform-region shortcuts, QcToqf runs after every tile's update
+  if (a.skip_uniform && !(a.kind == 2 && a.rk4_stage < 3)) {
+    const size_t qsm = sizeof(double) * (size_t)(QR_THREADS / STAGE_SPLIT) * (size_t)(a.ns + 3);
+    k_qc_to_qf_runs<<<(a.n + QR_BLOCK - 1) / QR_BLOCK, QR_THREADS, qsm, s>>>(a);
+    e = cudaGetLastError();
+  }
+  return e;
 }
 
 // flags[k] = 1 when species row k of the conserved state is nonzero in some

@@ -1975,15 +1975,17 @@ __global__ void __launch_bounds__(MAXW * 32, 1)
 // sum_k |u_k/R| G_k / (rho cv) for T). Every FP32 rate of progress is within
 // a relative DELTA of its FP64 value: its logarithm is a sum of terms below
 // ~300 in magnitude (ln A, beta ln T, E/RT and the S/R - H/RT of at most six
-// species), each good to a few units in the last place of FP32, so DELTA is
-// below 5e-4 even for equilibrium constants at 300 K; products that
-// underflow FP32 lose at most EPS_ABS per second of mass fraction. Then
+// species), each good to a few units in the last place of FP32. A worst-case
+// count of those roundings over GRI-Mech 3.0 from 300 to 3500 K gives DELTA
+// = 8.2e-4, largest for a reverse constant at 300 K (tests/
+// test_precheck_bound.py); products that underflow FP32 lose at most EPS_ABS
+// per second of mass fraction. Then
 //     |f64_i - f32_i| <= DELTA g_i + EPS_ABS,
-// and with KAPPA = 1e-2 (20 x DELTA) a cell whose bound
+// and with KAPPA = 1e-2 (over 12 x DELTA) a cell whose bound
 //     sqrt(mean_i (dt (|f32_i| + KAPPA g_i + EPS_ABS) / (atol + rtol |y_i|))^2) <= 1e-3
 // passes the FP64 test as well. It takes the explicit step with f32, which
 // differs from the FP64 explicit step by at most DELTA / KAPPA x 1e-3 x
-// sqrt(n) ~ 4e-4 error-weight units per component. A cell with a reaction
+// sqrt(n) ~ 6e-4 error-weight units per component. A cell with a reaction
 // the FP32 form does not cover (a general-order reaction, or a reverse
 // constant held at the FP32 cap while its products are present), or whose
 // bound is not finite, goes to the FP64 test unchanged.

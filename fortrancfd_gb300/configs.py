@@ -158,6 +158,36 @@ def detonation(names=None, ncell: int = 20000, length: float = 1.0, driver: floa
                          flag_lbound=0, flag_rbound=1, do_reaction=1, p_out=p0), cfl=0.4, tend=200e-6)
 
 
+def planar_flame(names=None, ncell: int = 1000, dx: float = 2.0e-5, T_lo: float = 300.0, T_hi: float = 2400.0,
+                 x_c: float = 1.4e-2, width: float = 2.0e-3, u_in: float = 1.0, do_reaction: int = 1) -> TubeCase:
+    """Planar CH4/air flame with transport, the reference's planar-flame
+    example (WORK/Examples/CH4_GRI3.0/PlanarFlame_Xe: pla_flame.inp,
+    initial.txt, bound_flow.txt) with N2 in place of its Xe diluent, which
+    GRI-Mech 3.0 lacks, and one uniform grid in place of its SMR blocks:
+    stoichiometric CH4/O2/N2 (0.0951/0.1901/0.7148) at 1 atm, temperature
+    T_lo + (T_hi - T_lo)(erf((x - x_c)/width) + 1)/2 (SRC/params.f90:374-377),
+    constant mass flux rho u = rho_in u_in, inflow at 300 K, 1 m/s on the
+    left, outflow at 1 atm on the right; MUSCL-minmod + HLLC, TVDRK3, CFL
+    0.5, transport and chemistry on."""
+    from math import erf
+
+    names = names or species_names(GRI30_DIR)
+    xm = (np.arange(ncell) + 0.5) * dx
+    fresh = mole_vector(names, {"CH4": 0.0950570342, "O2": 0.1901140684, "N2": 0.7148288973})
+    T = T_lo + 0.5 * (T_hi - T_lo) * (np.array([erf((x - x_c) / width) for x in xm]) + 1.0)
+    p = np.full(ncell, ATM)
+    X = np.tile(fresh, (ncell, 1))
+    W = molecular_weights()
+    wm = float(fresh @ W)
+    rho = p * wm / (8314.51 * T)
+    rho_in = ATM * wm / (8314.51 * T_lo)
+    u = rho_in * u_in / rho
+    return TubeCase(f"ch4_air_planar_flame_{ncell}", ncell, dx, T, p, u, X,
+                    dict(select_time=1, select_riemann=2, flag_acu=1, flag_muscl=2, flag_weno=0,
+                         flag_lbound=1, flag_rbound=1, do_reaction=do_reaction, do_tran=1, p_out=ATM, t_in=T_lo,
+                         rho_u_in=rho_in * u_in, x_in=fresh), cfl=0.5, tend=0.2)
+
+
 def ch4_air_mixture(names, phi: float) -> np.ndarray:
     n = phi + 2.0 * 4.76
     return mole_vector(names, {"CH4": phi / n, "O2": 2.0 / n, "N2": 2.0 * 3.76 / n})

@@ -23,8 +23,10 @@
 #include "chem.h"
 #include "edyn_dev.cuh"
 #include "edyn_kernels.h"
+#include "fastmath.cuh"
 #include "mechanism.h"
 #include "recon.cuh"
+#include "transport.h"
 
 extern "C" int edyn_mech_load_dir(const char* dir, edyn_mech* m, char* err, int errlen);
 extern "C" int edyn_mech_write(const edyn_mech* m, const char* path);
@@ -122,6 +124,13 @@ struct Ctx {
   int chem_max_steps = 0;     // integrator step cap per cell (0: the default 4000)
   int precheck = 1;           // single-precision pre-check of the inert-cell test
   int skip_uniform = 1;       // stage: no faces for cells whose stencils hold one state
+  // transport (do_tran = 1): the fits, their device tables and the buffers
+  // of the per-cell properties and the face fluxes
+  int do_tran = 0;
+  double* d_tran = nullptr;
+  double* d_tp = nullptr;
+  double* d_tflux = nullptr;
+  TranDev trd{};
   double* staging = nullptr;
   size_t staging_bytes = 0;
   // device clock of the time loop
@@ -224,6 +233,12 @@ StageArgs base_args(Ctx* c) {
   a.bc = c->bc;
   a.err = c->d_err;
   a.skip_uniform = c->skip_uniform;
+  if (c->do_tran) {
+    // the transport flux of a face is not decided by the stencil test of the
+    // uniform-region shortcuts (it reads the conserved state): every face
+    a.tran = c->trd;
+    a.skip_uniform = 0;
+  }
   if (c->pk.ntube) {
     const Packed& k = c->pk;
     a.tubes = TubeTab{k.d_tiles, k.d_n, k.d_off, k.d_dx, k.d_p_out, k.d_dt, k.d_active, k.d_time, k.ntiles, k.colmap, k.tube_of};
@@ -705,6 +720,90 @@ int edyn_mech_compile(const char* chem_dir, const char* out_path, char* err, int
   return rc ? EDYN_E_MECH : EDYN_OK;
 }
 
+int edyn_tran_compile(const char* chem_dir, const char* out_path, char* err, int errlen) {
+  std::unique_ptr<edyn_mech> m(new (std::nothrow) edyn_mech);
+  std::unique_ptr<edyn_tran> t(new (std::nothrow) edyn_tran);
+  if (!m || !t) return EDYN_E_ARG;
+  if (edyn_mech_load_dir(chem_dir, m.get(), err, errlen) != 0) return EDYN_E_MECH;
+  if (edyn_tran_load_dir(chem_dir, t.get(), err, errlen) != 0) return EDYN_E_MECH;
+  if (t->kk != m->nspec) {
+    if (err && errlen > 0) std::snprintf(err, (size_t)errlen, "transport fits for %d species, mechanism has %d", t->kk, m->nspec);
+    return EDYN_E_MECH;
+  }
+  if (edyn_tran_write(t.get(), m.get(), out_path) != 0) {
+    if (err && errlen > 0) std::snprintf(err, (size_t)errlen, "cannot write %s", out_path);
+    return EDYN_E_MECH;
+  }
+  return EDYN_OK;
+}
+
+namespace {
+// Transport set-up of edyn_init: loads the fits next to the mechanism,
+// checks them against it and builds the device tables of TranDev.
+int init_transport(Ctx* c, const char* chem_dir) {
+  std::unique_ptr<edyn_tran> t(new (std::nothrow) edyn_tran);
+  if (!t) return fail(c, EDYN_E_ARG, "out of host memory");
+  char err[512] = {0};
+  if (edyn_tran_load_dir(chem_dir, t.get(), err, sizeof(err)) != 0) return fail(c, EDYN_E_MECH, "transport: %s", err);
+  const int ns = c->ns;
+  if (t->kk != ns) return fail(c, EDYN_E_MECH, "transport fits for %d species, mechanism has %d", t->kk, ns);
+  for (int k = 0; k < ns; ++k)
+    if (!(std::fabs(t->wt[k] - c->mech.W[k]) <= 1e-6 * c->mech.W[k]))
+      return fail(c, EDYN_E_MECH, "transport fits: molecular weight of species %d differs from the mechanism's", k);
+  const int npair = ns * (ns - 1) / 2;
+  std::vector<double> h;
+  auto put = [&](size_t n) {
+    size_t o = h.size();
+    h.resize(o + n, 0.0);
+    return o;
+  };
+  const size_t o_eta = put(4 * ns), o_lam = put(4 * ns), o_dif = put(4 * (size_t)npair);
+  const size_t o_wa = put((size_t)ns * ns), o_wb = put((size_t)ns * ns), o_wc = put((size_t)ns * ns);
+  const size_t o_w = put(ns), o_e2 = put(64), o_lg = put(184);
+  for (int k = 0; k < ns; ++k)
+    for (int n = 0; n < 4; ++n) {
+      h[o_eta + 4 * k + n] = t->cofeta[k][n];
+      h[o_lam + 4 * k + n] = t->coflam[k][n];
+    }
+  size_t q = o_dif;
+  for (int k = 1; k < ns; ++k)
+    for (int j = 0; j < k; ++j)
+      for (int n = 0; n < 4; ++n) h[q++] = t->cofd[k][j][n];
+  for (int k = 0; k < ns; ++k) {
+    h[o_w + k] = t->wt[k];
+    for (int j = 0; j < ns; ++j) {
+      const double g = 1.0 / std::sqrt(1.0 + t->wt[k] / t->wt[j]);
+      h[o_wa + (size_t)k * ns + j] = g;
+      h[o_wb + (size_t)k * ns + j] = std::sqrt(std::sqrt(t->wt[j] / t->wt[k])) * g;
+      h[o_wc + (size_t)k * ns + j] = std::sqrt(t->wt[j] / t->wt[k]) * g;
+    }
+  }
+  fill_exp_table(&h[o_e2]);
+  fill_log_table(&h[o_lg]);
+  CK(cudaMalloc(&c->d_tran, h.size() * sizeof(double)));
+  CK(cudaMemcpy(c->d_tran, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice));
+  const size_t ld = (size_t)c->ld;
+  CK(cudaMalloc(&c->d_tp, (size_t)(TRAN_ROWS_FIXED + 2 * ns) * ld * sizeof(double)));
+  CK(cudaMalloc(&c->d_tflux, (size_t)c->ne * ld * sizeof(double)));
+  CK(cudaMemset(c->d_tp, 0, (size_t)(TRAN_ROWS_FIXED + 2 * ns) * ld * sizeof(double)));
+  CK(cudaMemset(c->d_tflux, 0, (size_t)c->ne * ld * sizeof(double)));
+  TranDev& d = c->trd;
+  d.eta = c->d_tran + o_eta;
+  d.lam = c->d_tran + o_lam;
+  d.dif = c->d_tran + o_dif;
+  d.wa = c->d_tran + o_wa;
+  d.wb = c->d_tran + o_wb;
+  d.wc = c->d_tran + o_wc;
+  d.W = c->d_tran + o_w;
+  d.e2 = c->d_tran + o_e2;
+  d.lg = c->d_tran + o_lg;
+  d.patmos = t->patmos;
+  d.tp = c->d_tp;
+  d.flux = c->d_tflux;
+  return EDYN_OK;
+}
+}  // namespace
+
 int edyn_init(const char* chem_dir, int nspe, int nequ, int ncell, int lvir, const int* iflags, int n_iflags,
               const double* rparams, int n_rparams, const double* x_in, void** out) {
   if (!out) return EDYN_E_ARG;
@@ -735,6 +834,7 @@ int edyn_init(const char* chem_dir, int nspe, int nequ, int ncell, int lvir, con
   c->do_reaction = fl(EDYN_IF_DO_REACTION, 0);
   c->strict = fl(EDYN_IF_STRICT_NEWTON, 1);
   c->chem_mode = fl(EDYN_IF_CHEM_MODE, 0);
+  c->do_tran = fl(EDYN_IF_DO_TRAN, 0);
   c->dx = rp(EDYN_RP_DX, 0.0);
   c->p_out = rp(EDYN_RP_P_OUT, 101325.0);
   c->t_in = rp(EDYN_RP_T_IN, 300.0);
@@ -743,6 +843,7 @@ int edyn_init(const char* chem_dir, int nspe, int nequ, int ncell, int lvir, con
   c->atol = rp(EDYN_RP_ATOL, 1e-13);
   if (c->chem_mode != 0 && c->chem_mode != 1)
     return fail(c, EDYN_E_ARG, "chem_mode=%d: 0 (implicit integrator) or 1 (surrogate with fallback)", c->chem_mode);
+  if (c->do_tran != 0 && c->do_tran != 1) return fail(c, EDYN_E_ARG, "do_tran=%d must be 0 or 1", c->do_tran);
   if (c->select_time < 0 || c->select_time > 2)
     return fail(c, EDYN_E_ARG, "select_time=%d not in 0..2 (Euler, TVDRK3, RK4)", c->select_time);
   if (c->riemann < 0 || c->riemann > 2) return fail(c, EDYN_E_ARG, "select_riemann=%d not in 0..2", c->riemann);
@@ -838,6 +939,10 @@ int edyn_init(const char* chem_dir, int nspe, int nequ, int ncell, int lvir, con
   rc = chem_init(c->chem, m, c->tb, c->stream);
   if (rc) return fail(c, EDYN_E_CUDA, "chemistry tables: %s", cudaGetErrorString((cudaError_t)rc));
   CK(stage_tiling(c->acu, c->lim, c->wflag, c->riemann, c->ns, c->n, &c->stage_tc));
+  if (c->do_tran) {
+    rc = init_transport(c, chem_dir);
+    if (rc) return rc;
+  }
   CK(cudaStreamSynchronize(c->stream));
   return EDYN_OK;
 }
@@ -882,6 +987,11 @@ int edyn_init_tubes(const char* chem_dir, int nspe, int nequ, int ntube, const i
   if (n_iflags > EDYN_IF_CHEM_MODE && iflags[EDYN_IF_CHEM_MODE] != 0) {
     int rc = edyn_init(chem_dir, nspe, nequ, 16, lvir, iflags, n_iflags, rparams, n_rparams, nullptr, out);
     if (rc == EDYN_OK) rc = fail((Ctx*)*out, EDYN_E_ARG, "packed tubes take the plain chemistry (chem_mode 0)");
+    return rc ? rc : EDYN_E_ARG;
+  }
+  if (n_iflags > EDYN_IF_DO_TRAN && iflags[EDYN_IF_DO_TRAN] != 0) {
+    int rc = edyn_init(chem_dir, nspe, nequ, 16, lvir, iflags, n_iflags, rparams, n_rparams, nullptr, out);
+    if (rc == EDYN_OK) rc = fail((Ctx*)*out, EDYN_E_ARG, "packed tubes are inviscid (do_tran 0)");
     return rc ? rc : EDYN_E_ARG;
   }
   // One context whose rows hold every tube's block: its row length is the
@@ -1464,6 +1574,27 @@ int edyn_set_chem_launch(void* ctx, int form) {
   return EDYN_OK;
 }
 
+int edyn_transport_properties(void* ctx, double* mu, double* kappa, double* dif) {
+  Ctx* c = (Ctx*)ctx;
+  if (!c || !c->qc) return EDYN_E_ARG;
+  if (!c->do_tran) return fail(c, EDYN_E_ARG, "transport properties need a context created with do_tran 1");
+  StageArgs a = base_args(c);
+  a.qf_in = c->qf[c->cur];
+  CK(launch_tran(a, c->stream));
+  const size_t ld = (size_t)c->ld, rows = (size_t)(TRAN_ROWS_FIXED + 2 * c->ns);
+  std::vector<double> h(rows * ld);
+  CK(cudaMemcpyAsync(h.data(), c->d_tp, h.size() * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  for (int i = 0; i < c->n; ++i) {
+    const size_t col = (size_t)i + GHOST;
+    if (mu) mu[i] = h[3 * ld + col];
+    if (kappa) kappa[i] = h[4 * ld + col];
+    if (dif)
+      for (int k = 0; k < c->ns; ++k) dif[(size_t)i * c->ns + k] = h[(TRAN_ROWS_FIXED + c->ns + k) * ld + col];
+  }
+  return take_status(c, "edyn_transport_properties");
+}
+
 int edyn_set_uniform_skip(void* ctx, int on) {
   Ctx* c = (Ctx*)ctx;
   if (!c || !c->qc) return EDYN_E_ARG;
@@ -1670,6 +1801,9 @@ int edyn_finalize(void* ctx) {
   cudaFree(c->d_head_count);
   cudaFree(c->d_run_last);
   cudaFree(c->d_run_head);
+  cudaFree(c->d_tran);
+  cudaFree(c->d_tp);
+  cudaFree(c->d_tflux);
   if (c->own) cudaStreamDestroy(c->own);
   delete c;
   return EDYN_OK;
@@ -1737,6 +1871,8 @@ extern "C" int edyn_solve_fluid_noalloc(void* ctx, double* qf_d, double* qc_d, d
     return fail(c, EDYN_E_ARG, "edyn_solve_fluid_noalloc: qf and Qc must be 8-byte aligned");
   const size_t rows = (size_t)c->ne * c->ld;
   if (c->pk.ntube) return fail(c, EDYN_E_ARG, "edyn_solve_fluid_noalloc: one tube per context");
+  if (c->do_tran)
+    return fail(c, EDYN_E_ARG, "edyn_solve_fluid_noalloc: transport (do_tran 1) needs the context's property buffers");
   if (c->select_time == 2)
     return fail(c, EDYN_E_ARG, "edyn_solve_fluid_noalloc: RK4 (select_time 2) needs a third scratch array; use "
                                "edyn_solve_fluid");

@@ -42,6 +42,25 @@ struct TubeTab {
   const int* tube_of;      // tube of each cell
 };
 
+// Transport of calc_flux_tran (SRC/flux.f90:18-127) when do_tran = 1: the
+// device copy of the TRANLIB fits and the two buffers the transport kernels
+// write before each stage. flux null: transport off.
+struct TranDev {
+  const double* eta;  // [ns][4] ln viscosity fits in ln T (TRANLIB's COFETA, cgs)
+  const double* lam;  // [ns][4] ln conductivity fits (COFLAM)
+  const double* dif;  // [ns (ns - 1) / 2][4] ln D_jk fits at patmos of the pairs j < k, k-major
+  const double* wa;   // [ns][ns] Wilke rule, expanded: g_kj = 1 / sqrt(1 + W_k / W_j)
+  const double* wb;   //          q_kj g_kj, q_kj = (W_j / W_k)^(1/4)
+  const double* wc;   //          q_kj^2 g_kj
+  const double* W;    // [ns] molecular weights of the fits (TRANLIB's WT)
+  const double* e2;   // table of texp
+  const double* lg;   // table of tlog
+  double patmos;      // dyn/cm^2
+  double* tp;         // cell rows, cells -1..n at column c + GHOST: rho, u, T, mu, kappa, Y_k (ns), D'_k (ns)
+  double* flux;       // [ne][ld]: transport flux of face j (cells j-1, j) at column j + GHOST
+};
+constexpr int TRAN_ROWS_FIXED = 5;  // rho, u, T, mu, kappa before the species rows of TranDev::tp
+
 struct StageArgs {
   int n, ld, lvir, ns;
   int tc;                // cells per stage tile (CTA); the CTA has stage_threads(tc) threads
@@ -67,6 +86,7 @@ struct StageArgs {
   unsigned* err;         // status word: EDYN_E_NEWTON / EDYN_E_STATE bits of any cell (may be null)
   TubeTab tubes;         // packed tubes (tubes.tiles null: the single tube above); cvel_out then per tube
   int skip_uniform;      // skip the faces of cells whose stencils hold one state (dF = 0 exactly)
+  TranDev tran;          // do_tran: transport fluxes added to the advective ones (tran.flux null: off)
 };
 
 int fluid_upload_tables(const ThermoTable& tb, cudaStream_t s);
@@ -85,6 +105,9 @@ cudaError_t launch_step_begin(const double* time, double tend, const long long* 
 cudaError_t launch_aos_to_soa(const double* aos, int ne, int n, double* soa, int ld, cudaStream_t s);
 cudaError_t launch_soa_to_aos(const double* soa, int ne, int n, int ld, double* aos, cudaStream_t s);
 cudaError_t launch_qc_to_qf(const StageArgs& a, cudaStream_t s);
+// Transport properties of cells -1..n and transport fluxes of faces 0..n of
+// the stage input (a.tran); launch_stage calls it before the stage kernel.
+cudaError_t launch_tran(const StageArgs& a, cudaStream_t s);
 cudaError_t launch_check_state(const double* qf, const double* qc, int n, int ns, int ld, unsigned* err,
                                cudaStream_t s);
 cudaError_t launch_init_cells(int n, int ns, const double* T, const double* p, const double* u, const double* X,

@@ -33,6 +33,7 @@
 
 #include "edyn_dev.cuh"
 #include "edyn_kernels.h"
+#include "fastmath.cuh"
 #include "recon.cuh"
 
 namespace edyn {
@@ -198,15 +199,17 @@ struct TubeView {
 };
 
 // ---------------------------------------------------------------------------
-// Boundary ghost cells (SRC/boundary.f90). Computes the ghost cell g
-// (g < 0 left, g >= n right) primitive state from the interior conserved
-// state in global memory and stores it into the shared stencil.
+// Boundary ghost cells (SRC/boundary.f90). ghost_qc computes the conserved
+// column of the ghost cell g (g < 0 left, g >= n right) from the interior
+// conserved state in global memory: q0, q1, q2 and ys[k*st] = rho Y_k.
+// ghost_cell adds its QcToqf and stores the primitive state into the shared
+// stencil.
 // ---------------------------------------------------------------------------
-__device__ void ghost_cell(const StageArgs& a, const TubeView& v, int g, double* dst, int dst_st, double* ys, int st) {
+__device__ __forceinline__ void ghost_qc(const StageArgs& a, const TubeView& v, int g, double& q0, double& q1,
+                                         double& q2, double* ys, int st) {
   const ThermoTable& tb = c_thermo;
   const int ns = tb.ns;
   const int ld = a.ld;
-  double q0, q1, q2;
   int iters;
   if (g < 0) {
     const int l = -g;  // 1..lvir
@@ -259,6 +262,13 @@ __device__ void ghost_cell(const StageArgs& a, const TubeView& v, int g, double*
       for (int k = 0; k < ns; ++k) ys[k * st] = rho_out * ys[k * st];
     }
   }
+}
+
+__device__ void ghost_cell(const StageArgs& a, const TubeView& v, int g, double* dst, int dst_st, double* ys, int st) {
+  const int ns = c_thermo.ns;
+  double q0, q1, q2;
+  int iters;
+  ghost_qc(a, v, g, q0, q1, q2, ys, st);
   CellEOS e = qc_to_qf_cell(q0, q1, q2, ys, st, 1000.0, true, iters);
   if (e.status && a.err) atomicOr(a.err, e.status);
   dst[0] = q0;
@@ -526,6 +536,18 @@ __global__ void __launch_bounds__(STAGE_MAX_THREADS) k_stage(StageArgs a) {
   }
   __syncthreads();
 
+  // 3b. transport (one tube only): the transport flux of each computed face
+  //     comes first, as in the reference's Fplus (transport, then +
+  //     advection): F = G + F_adv, row by row with coalesced G loads
+  if (a.tran.flux) {
+    const size_t gld = (size_t)a.ld;
+    for (int idx = tid; idx < ne * P; idx += NT) {
+      const int v = idx / P, fp = idx - v * P;
+      if (need_face(fp)) s_l[idx] = a.tran.flux[v * gld + c0 + fp + GHOST] + s_l[idx];
+    }
+    __syncthreads();
+  }
+
   // 4. one cell per group of SP lanes: conservative update + QcToqf,
   //    species split as in phase 3 (the bulk rows are computed by every lane)
   const int i = c0 + f;
@@ -765,6 +787,198 @@ __global__ void __launch_bounds__(QR_THREADS) k_qc_to_qf_runs(StageArgs a) {
 // The loop test and time steps of packed tubes, one CTA: tube t steps while
 // its time < tend (and the call's step budget lasts), with dt_t = cfl dx_t /
 // (its maximum signal speed); step_active = any tube steps.
+// ---------------------------------------------------------------------------
+// Transport (do_tran = 1): calc_flux_tran, SRC/flux.f90:18-127, with the
+// mixture rules of TRANLIB (MCAVIS, MCACON, MCADIF; SRC/trans.f90 wrappers).
+//
+// k_tran_props: one thread per cell c = -1..n (the two ghosts included),
+// from the stage's input conserved column, as the reference recomputes it
+// for every face: rho, u = rho u / rho, Y_k = rho Y_k / rho (unnormalised),
+// T from temperature_con with the 1000 K start, p, and
+//   mu    = MCAVIS (Wilke's rule; the reference names MCAVIS_EA, which its
+//           tranlib.f does not define) x 0.1,
+//   kappa = MCACON (half the arithmetic plus harmonic mean) x 1e-5,
+//   D'_k  = (1 - X_k) / (1 - Y_k) MCADIF_k x 1e-4 (0 where Y_k = 1).
+// A thread walks the species and species pairs of its cell alone, so every
+// pair's binary coefficient is evaluated once (ns (ns - 1) / 2 exponentials
+// per cell) and the table reads are the same address across the warp. The
+// Wilke sum sum_j X_j (1 + sqrt(eta_k / eta_j) q_kj)^2 g_kj is expanded into
+// three matrix-vector products with constant matrices (wa, wb, wc): all its
+// terms are positive, so the expansion moves the result by rounding only.
+//
+// k_tran_flux: one thread per face j = 0..n between cells j-1 and j: the
+// viscous stress, heat conduction, species diffusion and the enthalpy they
+// carry (hs_k at the face-average temperature, CKHMS), in the reference's
+// order; the stage kernel adds the result to the advective flux
+// (SRC/timeintegration.f90:31-47: Fplus = transport, then + advection).
+// ---------------------------------------------------------------------------
+constexpr int TRAN_PROPS_THREADS = 128;
+constexpr int TRAN_FLUX_THREADS = 128;
+
+__global__ void __launch_bounds__(TRAN_PROPS_THREADS) k_tran_props(StageArgs a) {
+  if (a.step_active && *a.step_active == 0) return;
+  const int c = (int)(blockIdx.x * blockDim.x + threadIdx.x) - 1;
+  if (c > a.n) return;
+  const ThermoTable& tb = c_thermo;
+  const TranDev& t = a.tran;
+  const int ns = a.ns;
+  const size_t ld = (size_t)a.ld;
+  double y[EDYN_NS_MAX], x[EDYN_NS_MAX], eta[EDYN_NS_MAX], v1[EDYN_NS_MAX], v2[EDYN_NS_MAX];
+  double q0, q1, q2;
+  if (c < 0 || c == a.n) {
+    const TubeView tv{a.n, a.qf_in, a.qf_out, a.qc, a.q0, a.acc, a.dx, a.p_out, nullptr};
+    ghost_qc(a, tv, c < 0 ? -1 : a.n, q0, q1, q2, y, 1);
+  } else {
+    const double* Q = a.qc + c + GHOST;
+    q0 = Q[0];
+    q1 = Q[ld];
+    q2 = Q[2 * ld];
+    for (int k = 0; k < ns; ++k) y[k] = Q[(3 + k) * ld];
+  }
+  const double rho = q0;
+  const double u = q1 / rho;
+  double sy = 0.0, sumyow = 0.0;
+  for (int k = 0; k < ns; ++k) {
+    const double yk = y[k] / rho;
+    y[k] = yk;
+    sy += yk;
+    sumyow = fma(yk, tb.invW[k], sumyow);
+  }
+  const double isw = 1.0 / sumyow;  // CKYTX: X_k = Y_k / (W_k sum_j Y_j / W_j)
+  for (int k = 0; k < ns; ++k) x[k] = y[k] * tb.invW[k] * isw;
+  // temperature_con (SRC/thermo.f90:211-257) with these mole fractions: the
+  // premixed Newton on the unnormalised Y with E scaled by S_Y
+  const double eint = q2 / rho - 0.5 * (u * u);
+  Premix pm;
+  double Sz;
+  int iters;
+  const double T = t_newton(y, 1, eint * sy * (1.0 / R_SI), 1000.0, pm, Sz, iters);
+  if (iters < 0 && a.err) atomicOr(a.err, EDYN_STATUS_NEWTON);
+  const double p_cgs = 10.0 * (R_SI * rho * T * Sz / sy);  // CKPX: rho R T / W, W = S_Y / S_z
+  const double L = tlog(T, t.lg);
+
+  // pure-species viscosities and conductivities; MCACON's two means
+  double sl = 0.0, sr = 0.0;
+  for (int k = 0; k < ns; ++k) {
+    const double* ce = t.eta + 4 * k;
+    const double* cl = t.lam + 4 * k;
+    const double ek = texp_r(fma(fma(fma(ce[3], L, ce[2]), L, ce[1]), L, ce[0]), t.e2);
+    const double lk = texp_r(fma(fma(fma(cl[3], L, cl[2]), L, cl[1]), L, cl[0]), t.e2);
+    eta[k] = ek;
+    const double r = rsqrt(ek);
+    v1[k] = x[k] * r;
+    v2[k] = x[k] / ek;
+    sl = fma(x[k], lk, sl);
+    sr += x[k] / lk;
+  }
+  const double kap = 0.5 * (sl + 1.0 / sr) * 1.0e-5;
+  // MCAVIS: sum_k X_k eta_k / sum_j X_j (1 + sqrt(eta_k/eta_j) q_kj)^2 g_kj, times sqrt(8)
+  double vm = 0.0;
+  for (int k = 0; k < ns; ++k) {
+    const double* pa = t.wa + (size_t)k * ns;
+    const double* pb = t.wb + (size_t)k * ns;
+    const double* pc = t.wc + (size_t)k * ns;
+    double A = 0.0, B = 0.0, C = 0.0;
+    for (int j = 0; j < ns; ++j) {
+      A = fma(pa[j], x[j], A);
+      B = fma(pb[j], v1[j], B);
+      C = fma(pc[j], v2[j], C);
+    }
+    const double sumi = fma(eta[k], C, fma(2.0 * sqrt(eta[k]), B, A));
+    vm += x[k] * eta[k] / sumi;
+  }
+  const double mu = vm * 2.8284271247461903 * 0.1;
+
+  // MCADIF (MCEDIF): S_k = sum_{j != k} XX_j / D_jk over the pairs j < k,
+  // each exponential shared by both sums; the sums take their terms in the
+  // order j = 0, 1, ... as MCEDIF's loop does. XX = max(X, 1e-50).
+  double* S = v1;
+  double* xx = v2;
+  for (int k = 0; k < ns; ++k) {
+    S[k] = 0.0;
+    xx[k] = fmax(x[k], 1.0e-50);
+  }
+  const double* cd = t.dif;
+  for (int k = 1; k < ns; ++k) {
+    const double xk = xx[k];
+    double sk = 0.0;
+    for (int j = 0; j < k; ++j, cd += 4) {
+      const double v = texp_r(-fma(fma(fma(cd[3], L, cd[2]), L, cd[1]), L, cd[0]), t.e2);
+      sk = fma(xx[j], v, sk);
+      S[j] = fma(xk, v, S[j]);
+    }
+    S[k] = sk;
+  }
+  // sum_{j != k} XX_j W_j as a prefix plus a suffix sum (eta[] holds the suffixes)
+  double wtm = 0.0, suf = 0.0;
+  for (int k = ns - 1; k >= 0; --k) {
+    eta[k] = suf;
+    suf = fma(xx[k], t.W[k], suf);
+    wtm = fma(t.W[k], x[k], wtm);
+  }
+  double* out = t.tp + c + GHOST;
+  out[0] = rho;
+  out[ld] = u;
+  out[2 * ld] = T;
+  out[3 * ld] = mu;
+  out[4 * ld] = kap;
+  double pre = 0.0;
+  for (int k = 0; k < ns; ++k) {
+    const double sumxw = pre + eta[k];
+    pre = fma(xx[k], t.W[k], pre);
+    const double dk = sumxw / (wtm * S[k]) * t.patmos / p_cgs * 1.0e-4;
+    const double dif = (y[k] == 1.0) ? 0.0 : (1.0 - x[k]) / (1.0 - y[k]) * dk;
+    out[(TRAN_ROWS_FIXED + k) * ld] = y[k];
+    out[(TRAN_ROWS_FIXED + ns + k) * ld] = dif;
+  }
+}
+
+__global__ void __launch_bounds__(TRAN_FLUX_THREADS) k_tran_flux(StageArgs a) {
+  if (a.step_active && *a.step_active == 0) return;
+  const int j = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+  if (j > a.n) return;
+  const ThermoTable& tb = c_thermo;
+  const TranDev& t = a.tran;
+  const int ns = a.ns;
+  const size_t ld = (size_t)a.ld;
+  const double dx = a.dx;
+  const double* L = t.tp + (j - 1) + GHOST;  // cell j-1
+  const double* R = L + 1;                   // cell j
+  const double rho_ave = 0.5 * (L[0] + R[0]);
+  const double u_ave = 0.5 * (L[ld] + R[ld]);
+  const double T_ave = 0.5 * (L[2 * ld] + R[2 * ld]);
+  const double mu_ave = 0.5 * (L[3 * ld] + R[3 * ld]);
+  const double kap_ave = 0.5 * (L[4 * ld] + R[4 * ld]);
+  const double tau = -(2.0 / 3.0 * mu_ave * (2.0 * ((R[ld] - L[ld]) / dx)));
+  double* G = t.flux + j + GHOST;
+  double hsum = 0.0;
+  for (int k = 0; k < ns; ++k) {
+    // CKHMS at the face temperature, J/kg: R T (a1 + a2 T/2 + ... + a6/T) / W
+    const int r = (T_ave > tb.tmid[k]) ? 1 : 0;
+    double h = fma(tb.ah[r][4][k], T_ave, tb.ah[r][3][k]);
+    h = fma(h, T_ave, tb.ah[r][2][k]);
+    h = fma(h, T_ave, tb.ah[r][1][k]);
+    h = fma(h, T_ave, tb.ah[r][0][k]);
+    h = fma(h, T_ave, tb.ah[r][5][k]);
+    const double hs = R_SI * h * tb.invW[k];
+    const double dif_ave = 0.5 * (L[(TRAN_ROWS_FIXED + ns + k) * ld] + R[(TRAN_ROWS_FIXED + ns + k) * ld]);
+    const double dy = (R[(TRAN_ROWS_FIXED + k) * ld] - L[(TRAN_ROWS_FIXED + k) * ld]) / dx;
+    hsum = hsum - hs * dif_ave * dy;
+    G[(3 + k) * ld] = -(rho_ave * dif_ave * dy);
+  }
+  G[0] = 0.0;
+  G[ld] = tau;
+  G[2 * ld] = tau * u_ave + rho_ave * hsum - kap_ave * ((R[2 * ld] - L[2 * ld]) / dx);
+}
+
+cudaError_t launch_tran(const StageArgs& a, cudaStream_t s) {
+  k_tran_props<<<(a.n + 2 + TRAN_PROPS_THREADS - 1) / TRAN_PROPS_THREADS, TRAN_PROPS_THREADS, 0, s>>>(a);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  k_tran_flux<<<(a.n + 1 + TRAN_FLUX_THREADS - 1) / TRAN_FLUX_THREADS, TRAN_FLUX_THREADS, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
 __global__ void k_step_begin_tubes(int ntube, const double* time, double tend, const long long* nsteps,
                                    const long long* max_steps, double cfl, const double* dx, unsigned long long* cvel,
                                    int* active, double* dt, int* step_active) {
@@ -1087,6 +1301,12 @@ cudaError_t launch_stage(const StageArgs& a, int acu, int lim, int wflag, int rm
   const size_t smem = stage_smem_bytes(acu, a.ns, a.tc);
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
+  // transport fluxes of the stage input, before the stage updates it in place
+  if (a.tran.flux) {
+    if (a.tubes.tiles || a.skip_uniform) return cudaErrorInvalidValue;
+    e = launch_tran(a, s);
+    if (e != cudaSuccess) return e;
+  }
   const int grid = a.tubes.tiles ? a.tubes.ntiles : (a.n + a.tc - 1) / a.tc;
   kern<<<grid, stage_threads(a.tc), smem, s>>>(a);
   e = cudaGetLastError();

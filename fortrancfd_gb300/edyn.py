@@ -89,6 +89,8 @@ def lib() -> ctypes.CDLL:
     L.edyn_last_error.argtypes = [vp, ctypes.c_char_p, i]
     L.edyn_finalize.argtypes = [vp]
     L.edyn_mech_compile.argtypes = [cp, cp, ctypes.c_char_p, i]
+    L.edyn_tran_compile.argtypes = [cp, cp, ctypes.c_char_p, i]
+    L.edyn_transport_properties.argtypes = [vp, dp, dp, dp]
     L.edyn_version.restype = ctypes.c_char_p
     _lib = L
     return L
@@ -105,6 +107,15 @@ def mech_compile(chem_dir: str, out_path: str) -> None:
     """CHEMKIN directory -> mech.edyn (the CKINTERP step)."""
     buf = ctypes.create_string_buffer(512)
     rc = lib().edyn_mech_compile(str(chem_dir).encode(), str(out_path).encode(), buf, 512)
+    if rc:
+        raise EdynError(rc, buf.value.decode())
+
+
+def tran_compile(chem_dir: str, out_path: str) -> None:
+    """TRANLIB linking file (chem_dir/tran.bin) -> tran.edyn, the text form
+    the library and the package data use."""
+    buf = ctypes.create_string_buffer(512)
+    rc = lib().edyn_tran_compile(str(chem_dir).encode(), str(out_path).encode(), buf, 512)
     if rc:
         raise EdynError(rc, buf.value.decode())
 
@@ -172,13 +183,13 @@ class Tube(_Ctx):
 
     def __init__(self, ncell: int, dx: float, *, chem_dir=GRI30_DIR, select_time=1, select_riemann=2, flag_acu=1,
                  flag_muscl=2, flag_weno=0, flag_lbound=0, flag_rbound=0, do_reaction=0, strict_newton=1,
-                 chem_mode=0, p_out=101325.0, t_in=300.0, rho_u_in=0.0, rtol=1e-5, atol=1e-13,
+                 chem_mode=0, do_tran=0, p_out=101325.0, t_in=300.0, rho_u_in=0.0, rtol=1e-5, atol=1e-13,
                  x_in: Optional[Sequence[float]] = None, nspe: Optional[int] = None):
         names = species_names(chem_dir) if (Path(chem_dir) / "mech.edyn").exists() else None
         nspe = nspe if nspe is not None else len(names)
         lv = lvir_for(flag_acu, flag_weno)
         iflags = [select_time, select_riemann, flag_acu, flag_muscl, flag_weno, flag_lbound, flag_rbound,
-                  do_reaction, strict_newton, chem_mode]
+                  do_reaction, strict_newton, chem_mode, do_tran]
         super().__init__(chem_dir, nspe, ncell, lv, iflags, [dx, p_out, t_in, rho_u_in, rtol, atol], x_in)
         self.lvir = lv
         self.dx = dx
@@ -256,6 +267,15 @@ class Tube(_Ctx):
         """Single-precision pre-check of the inert-cell test (on by default):
         cells it decides skip the FP64 right-hand side."""
         self._check(lib().edyn_set_chem_precheck(self._h, 1 if on else 0))
+
+    def transport_properties(self):
+        """(mu [Pa s], kappa [W/(m K)], D' [m^2/s], ncell x nspe) of the
+        current state, as the transport flux evaluates them (do_tran tubes)."""
+        mu = np.zeros(self.ncell)
+        kap = np.zeros(self.ncell)
+        dif = np.zeros((self.ncell, self.nspe))
+        self._check(lib().edyn_transport_properties(self._h, _ptr(mu), _ptr(kap), _ptr(dif)))
+        return mu, kap, dif
 
     def set_uniform_skip(self, on: bool = True) -> None:
         """Uniform regions (on by default): the fluid stage computes no faces
@@ -335,13 +355,13 @@ class Tubes(Tube):
 
     def __init__(self, ncells: Sequence[int], dxs: Sequence[float], *, p_outs: Optional[Sequence[float]] = None,
                  chem_dir=GRI30_DIR, select_time=1, select_riemann=2, flag_acu=2, flag_muscl=2, flag_weno=3,
-                 flag_rbound=1, do_reaction=1, strict_newton=0, rtol=1e-5, atol=1e-13):
+                 flag_rbound=1, do_reaction=1, strict_newton=0, rtol=1e-5, atol=1e-13, do_tran=0):
         L = lib()
         names = species_names(chem_dir)
         nspe = len(names)
         lv = lvir_for(flag_acu, flag_weno)
         iflags = [select_time, select_riemann, flag_acu, flag_muscl, flag_weno, 0, flag_rbound, do_reaction,
-                  strict_newton, 0]
+                  strict_newton, 0, do_tran]
         nt = len(ncells)
         p_outs = [101325.0] * nt if p_outs is None else list(p_outs)
         rp = np.ascontiguousarray([[dxs[t], p_outs[t], 300.0, 0.0, rtol, atol] for t in range(nt)], dtype=np.float64)

@@ -41,7 +41,8 @@ extern "C" {
 #define EDYN_IF_DO_REACTION 7     /* 0 frozen, 1 per-cell chemistry */
 #define EDYN_IF_STRICT_NEWTON 8   /* 1: T Newton starts at 1000 K every call (reference); 0: warm start */
 #define EDYN_IF_CHEM_MODE 9       /* 0 plain implicit integrator, 1 surrogate with fallback (edyn_set_surrogate) */
-#define EDYN_NIFLAGS 10
+#define EDYN_IF_DO_TRAN 10        /* 0 inviscid, 1 viscous stress, conduction and diffusion (calc_flux_tran) */
+#define EDYN_NIFLAGS 11
 
 /* Indices into the rparams array of edyn_init. */
 #define EDYN_RP_DX 0        /* cell size dx_comp [m] */
@@ -55,10 +56,19 @@ extern "C" {
 /* Creates a context for one tube of ncell interior cells.
  * Replaces the set-up the reference does in main_sim before its time loop
  * (SRC/main.f90:30-128: set_thermo, init_solvers' lvir, set_block_params).
- * chem_dir: directory with CHEMKIN chem.inp + therm.dat, or with mech.edyn.
+ * chem_dir: directory with CHEMKIN chem.inp + therm.dat, or with mech.edyn;
+ * with do_tran = 1 also TRANLIB's linking file tran.bin (what set_trans,
+ * SRC/trans.f90:20-43, reads) or its text form tran.edyn.
  * nspe/nequ must match the mechanism (nequ = nspe + 3). lvir is checked
  * against the scheme (SRC/params.f90:161-173). x_in: inlet mole fractions
- * (nspe values) or NULL. */
+ * (nspe values) or NULL.
+ * do_tran = 1 adds calc_flux_tran (SRC/flux.f90:18-127) to every stage:
+ * viscous stress, conduction and mixture-averaged diffusion from TRANLIB's
+ * MCAVIS / MCACON / MCADIF, with MCAVIS standing in for the MCAVIS_EA that
+ * the reference's viscosity_ea calls (SRC/trans.f90:137-151) and its
+ * tranlib.f does not define. It is available for one tube per context, not
+ * for packed tubes (edyn_init_tubes) nor edyn_solve_fluid_noalloc, and it
+ * turns the uniform-region shortcuts of the stage off. */
 int edyn_init(const char* chem_dir, int nspe, int nequ, int ncell, int lvir, const int* iflags, int n_iflags,
               const double* rparams, int n_rparams, const double* x_in, void** ctx);
 
@@ -349,6 +359,19 @@ int edyn_finalize(void* ctx);
 /* Compiles a CHEMKIN mechanism directory into the mech.edyn table format
  * (the role of CKINTERP's chem.bin, GRI/ckinterp.f). */
 int edyn_mech_compile(const char* chem_dir, const char* out_path, char* err, int errlen);
+
+/* Writes the transport fits of chem_dir (TRANLIB's linking file tran.bin, as
+ * MCINIT reads it, tranlib.f:214-258) in the library's text form tran.edyn,
+ * every number to 17 significant digits (it reads back bit for bit). */
+int edyn_tran_compile(const char* chem_dir, const char* out_path, char* err, int errlen);
+
+/* Transport properties of the current state of a do_tran context, per
+ * interior cell, as calc_flux_tran evaluates them (SRC/flux.f90:51-90, the
+ * SRC/trans.f90 wrappers): mu [Pa s] (MCAVIS x 0.1), kappa [W/(m K)]
+ * (MCACON x 1e-5) and the diffusivities D'_k = (1 - X_k)/(1 - Y_k) D_k
+ * [m^2/s] (MCADIF x 1e-4; 0 where Y_k = 1), dif cell-major (ncell x nspe).
+ * Any pointer may be NULL. */
+int edyn_transport_properties(void* ctx, double* mu, double* kappa, double* dif);
 
 /* Library version string. */
 const char* edyn_version(void);

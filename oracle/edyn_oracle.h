@@ -96,6 +96,32 @@ void or_weno3z(const double* s, double* sl, double* sr);
 void or_weno5(const double* s, double* sl, double* sr, int flag_weno);
 void or_weno7z(const double* s, double* sl, double* sr);
 
+/* TRANLIB fits (the linking file's tables, cgs) and mixture rules. */
+typedef struct or_tran {
+  int kk, no, nlite;
+  double patmos;
+  double wt[OR_MAXSP], eps[OR_MAXSP], sig[OR_MAXSP], dip[OR_MAXSP], pol[OR_MAXSP], zrot[OR_MAXSP];
+  int nlin[OR_MAXSP];
+  double cofeta[OR_MAXSP][4], coflam[OR_MAXSP][4];
+  double cofd[OR_MAXSP][OR_MAXSP][4]; /* [k][j][n]: ln D_jk at patmos */
+} or_tran;
+
+int or_tran_load(const char* path, or_tran* t);
+int or_tran_sizeof(void);
+void or_mcsvis(const or_tran* t, double T, double* vis);
+void or_mcscon(const or_tran* t, double T, double* con);
+void or_mcsdif(const or_tran* t, double p, double T, double* djk);
+void or_mcavis(const or_tran* t, double T, const double* x, double* vismix);
+void or_mcacon(const or_tran* t, double T, const double* x, double* conmix);
+void or_mcadif(const or_tran* t, double p, double T, const double* x, double* d);
+double or_viscosity(const or_tran* t, double T, const double* x);
+double or_thermal_conductivity(const or_tran* t, double T, const double* x);
+void or_diffusivity(const or_tran* t, double p, double T, const double* x, double* di);
+void or_tran_cell(const or_mech* m, const or_tran* t, const double* qc, double* rho, double* u, double* T, double* y,
+                  double* mu, double* kap, double* dif);
+void or_face_flux_tran(const or_mech* m, const or_tran* t, const double* qcl, const double* qcr, double dx,
+                       double* g);
+
 /* 1-D tube state with ghost cells (equal-dx blocks collapse to one array). */
 typedef struct or_tube {
   const or_mech* m;
@@ -113,6 +139,7 @@ typedef struct or_tube {
   double* hrr;  /* n */
   double* hrr_dot;
   long chem_rhs_evals, chem_steps;
+  const or_tran* tran; /* do_tran: transport fits (NULL: inviscid) */
 } or_tube;
 
 or_tube* or_tube_create(const or_mech* m, int n, int lvir, const int* iflags, const double* rparams,
@@ -127,6 +154,10 @@ void or_update_boundary(or_tube* t);
 void or_ghost_qf(or_tube* t);
 double or_calc_dt(or_tube* t, double cfl);
 void or_calc_flux_advection(or_tube* t);
+/* do_tran = 1 with the given fits (NULL switches transport off). */
+void or_tube_set_transport(or_tube* t, const or_tran* tr);
+/* calc_flux_tran, SRC/flux.f90:18-127: adds the transport flux of every face to fplus. */
+void or_calc_flux_tran(or_tube* t);
 void or_solve_fluid(or_tube* t, double dt);
 void or_solve_source(or_tube* t, double dt);
 void or_post_step(or_tube* t);

@@ -344,8 +344,8 @@ double or_calc_dt(or_tube* t, double cfl) {
 }
 
 /* calc_flux_advection, SRC/flux.f90:130-373 (Cartesian). Face f lies
- * between cells f-1 and f; Fplus is zeroed and then receives the flux. */
-void or_calc_flux_advection(or_tube* t) {
+ * between cells f-1 and f; the flux is added to Fplus (SRC/flux.f90:358). */
+static void or_calc_flux_advection_add(or_tube* t) {
   const or_mech* m = t->m;
   const int ns = t->nspe, ne = t->nequ;
 #pragma omp parallel for schedule(static)
@@ -441,8 +441,33 @@ void or_calc_flux_advection(or_tube* t) {
       }
     }
     double* fp = t->fplus + (size_t)f * ne;
-    for (int n = 0; n < ne; ++n) fp[n] = 0.0 + flux[n];
+    for (int n = 0; n < ne; ++n) fp[n] = fp[n] + flux[n];
   }
+}
+
+void or_tube_set_transport(or_tube* t, const or_tran* tr) { t->tran = tr; }
+
+/* calc_flux_tran, SRC/flux.f90:18-127: every face i (between cells i and
+ * i+1 of the reference, f-1 and f here, ghosts included) from the current
+ * conserved state, added to fplus. */
+void or_calc_flux_tran(or_tube* t) {
+  const int ne = t->nequ;
+#pragma omp parallel for schedule(dynamic, 4)
+  for (int f = 0; f <= t->n; ++f)
+    or_face_flux_tran(t->m, t->tran, QC(t, f - 1), QC(t, f), t->dx, t->fplus + (size_t)f * ne);
+}
+
+/* The flux of a stage (SRC/timeintegration.f90:31-47): Fplus = 0, then the
+ * transport flux when do_tran = 1, then the advective flux added. */
+static void calc_fluxes(or_tube* t) {
+  memset(t->fplus, 0, sizeof(double) * (size_t)(t->n + 1) * t->nequ);
+  if (t->tran) or_calc_flux_tran(t);
+  or_calc_flux_advection_add(t);
+}
+
+void or_calc_flux_advection(or_tube* t) {
+  memset(t->fplus, 0, sizeof(double) * (size_t)(t->n + 1) * t->nequ);
+  or_calc_flux_advection_add(t);
 }
 
 /* QcToqf on every cell including the ghosts (SRC/timeintegration.f90:211-215). */
@@ -461,7 +486,7 @@ static void stage_tail(or_tube* t) {
 /* explicit_euler, SRC/timeintegration.f90:12-96 */
 static void explicit_euler(or_tube* t, double dt) {
   const int ne = t->nequ;
-  or_calc_flux_advection(t);
+  calc_fluxes(t);
   double c = dt / t->dx;
 #pragma omp parallel for schedule(static)
   for (int i = 0; i < t->n; ++i) {
@@ -478,7 +503,7 @@ static void tvdrk3(or_tube* t, double dt) {
   const int ne = t->nequ;
   memcpy(t->q0, QC(t, 0), sizeof(double) * (size_t)t->n * ne);
   for (int stage = 1; stage <= 3; ++stage) {
-    or_calc_flux_advection(t);
+    calc_fluxes(t);
     double h1, h2;
     if (stage == 1) {
       h1 = 1.0;
@@ -513,7 +538,7 @@ static void rk4(or_tube* t, double dt) {
   for (int s = 0; s < 4; ++s) k[s] = (double*)malloc(sizeof(double) * (size_t)n * ne);
   memcpy(t->q0, QC(t, 0), sizeof(double) * (size_t)n * ne);
   for (int s = 0; s < 4; ++s) {
-    or_calc_flux_advection(t);
+    calc_fluxes(t);
     for (int i = 0; i < n; ++i) {
       double* q = QC(t, i);
       const double* fp = t->fplus + (size_t)(i + 1) * ne;

@@ -14,6 +14,7 @@ import numpy as np
 ROOT = Path(__file__).resolve().parent.parent
 ORACLE_SO = ROOT / "oracle" / "_build" / "libedyn_oracle.so"
 MECH = ROOT / "fortrancfd_gb300" / "data" / "gri30" / "mech.edyn"
+TRAN = ROOT / "fortrancfd_gb300" / "data" / "gri30" / "tran.edyn"
 _D = ctypes.POINTER(ctypes.c_double)
 
 
@@ -80,6 +81,21 @@ class Oracle:
         L.or_weno7z.argtypes = [_D, _D, _D]
         L.or_adjust_sum.argtypes = [i, _D]
         L.or_num_threads.restype = i
+        self.tran = ctypes.create_string_buffer(L.or_tran_sizeof())
+        assert L.or_tran_load(str(TRAN).encode(), self.tran) == 0
+        for fn in ("or_mcsvis", "or_mcscon"):
+            getattr(L, fn).argtypes = [vp, d, _D]
+        L.or_mcsdif.argtypes = [vp, d, d, _D]
+        for fn in ("or_mcavis", "or_mcacon"):
+            getattr(L, fn).argtypes = [vp, d, _D, _D]
+        L.or_mcadif.argtypes = [vp, d, d, _D, _D]
+        for fn in ("or_viscosity", "or_thermal_conductivity"):
+            getattr(L, fn).restype = d
+            getattr(L, fn).argtypes = [vp, d, _D]
+        L.or_diffusivity.argtypes = [vp, d, d, _D, _D]
+        L.or_tran_cell.argtypes = [vp, vp, _D, _D, _D, _D, _D, _D, _D, _D]
+        L.or_face_flux_tran.argtypes = [vp, vp, _D, _D, d, _D]
+        L.or_tube_set_transport.argtypes = [vp, vp]
         self.kk = 53
         self.nequ = self.kk + 3
 
@@ -113,6 +129,54 @@ class Oracle:
         qr = np.zeros(nr)
         self.L.or_ckrop(self.mech, rho_cgs, T, _p(np.ascontiguousarray(Y, dtype=float)), _p(qf), _p(qr))
         return qf, qr
+
+    # --- transport (TRANLIB mixture rules, cgs unless noted)
+    def pure_viscosity(self, T):
+        return self.vec2("or_mcsvis", T)
+
+    def pure_conductivity(self, T):
+        return self.vec2("or_mcscon", T)
+
+    def vec2(self, fn, T):
+        out = np.zeros(self.kk)
+        getattr(self.L, fn)(self.tran, T, _p(out))
+        return out
+
+    def binary_diffusion(self, p_cgs, T):
+        out = np.zeros((self.kk, self.kk))
+        self.L.or_mcsdif(self.tran, p_cgs, T, _p(out))
+        return out
+
+    def mix_viscosity(self, T, X):
+        out = np.zeros(1)
+        self.L.or_mcavis(self.tran, T, _p(np.ascontiguousarray(X, dtype=float)), _p(out))
+        return out[0]
+
+    def mix_conductivity(self, T, X):
+        out = np.zeros(1)
+        self.L.or_mcacon(self.tran, T, _p(np.ascontiguousarray(X, dtype=float)), _p(out))
+        return out[0]
+
+    def mix_diffusion(self, p_cgs, T, X):
+        out = np.zeros(self.kk)
+        self.L.or_mcadif(self.tran, p_cgs, T, _p(np.ascontiguousarray(X, dtype=float)), _p(out))
+        return out
+
+    def tran_cell(self, qc):
+        """calc_flux_tran's per-cell state from a conserved column:
+        (rho, u, T, Y, mu [Pa s], kappa [W/(m K)], D' [m^2/s])."""
+        sc = [np.zeros(1) for _ in range(5)]
+        y = np.zeros(self.kk)
+        dif = np.zeros(self.kk)
+        self.L.or_tran_cell(self.mech, self.tran, _p(np.ascontiguousarray(qc, dtype=float)), _p(sc[0]), _p(sc[1]),
+                            _p(sc[2]), _p(y), _p(sc[3]), _p(sc[4]), _p(dif))
+        return sc[0][0], sc[1][0], sc[2][0], y, sc[3][0], sc[4][0], dif
+
+    def face_flux_tran(self, qcl, qcr, dx):
+        g = np.zeros(self.nequ)
+        self.L.or_face_flux_tran(self.mech, self.tran, _p(np.ascontiguousarray(qcl, dtype=float)),
+                                 _p(np.ascontiguousarray(qcr, dtype=float)), dx, _p(g))
+        return g
 
     def init_cells(self, T, p, u, X):
         n = len(T)
@@ -168,6 +232,10 @@ class OracleTube:
 
     def step(self, cfl):
         return self.o.L.or_step(self.h, cfl)
+
+    def set_transport(self, on=True):
+        """do_tran = 1: calc_flux_tran joins every stage's flux."""
+        self.o.L.or_tube_set_transport(self.h, self.o.tran if on else None)
 
     def calc_dt(self, cfl):
         return self.o.L.or_calc_dt(self.h, cfl)

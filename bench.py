@@ -74,9 +74,10 @@ def parse():
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--workload", default="detonation_air_200k",
-                   choices=list(WORKLOADS) + ["reactors", "tubes"],
-                   help="the tube of the headline metric (default), the 20k CH4/O2 tube, the reactor batch, or "
-                        "the uneven batch of --ntubes tubes in one context")
+                   choices=list(WORKLOADS) + ["reactors", "tubes", "flame"],
+                   help="the tube of the headline metric (default), the 20k CH4/O2 tube, the reactor batch, "
+                        "the uneven batch of --ntubes tubes in one context, or the planar flame with transport")
+    p.add_argument("--flame-cells", type=int, default=1000, help="cells of --workload flame (20 um each)")
     p.add_argument("--ntubes", type=int, default=256, help="tubes of --workload tubes")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-surrogate", action="store_true", help="skip the surrogate-vs-plain comparison")
@@ -649,11 +650,154 @@ def tubes_arm(args, rank, world, local):
     print(json.dumps(line), flush=True)
 
 
+FLAME_METRIC = "cell-steps/s on 1 GB300: planar CH4/air flame with transport and chemistry"
+
+
+def flame_case(args):
+    from fortrancfd_gb300 import configs
+
+    return configs.planar_flame(ncell=args.flame_cells)
+
+
+def flame_config(case, args, world):
+    return {"workload": case.name, "cells": case.ncell, "dx_m": case.dx,
+            "mixture": "stoichiometric CH4/O2/N2, 1 atm; T erf profile 300 -> 2400 K at 1.4 cm, width 2 mm",
+            "scheme": "MUSCL-minmod + HLLC + SSP-RK3, CFL 0.5, inflow 300 K 1 m/s / outflow 1 atm",
+            "transport": "calc_flux_tran, TRANLIB mixture rules (MCAVIS, MCACON, MCADIF)",
+            "chemistry": "GRI-Mech 3.0, per-cell stiff integration, rtol 1e-5, atol 1e-13",
+            "timed_steps": f"steps {args.warmup + 1}..{args.warmup + args.steps} from the initial state",
+            "parallelism": f"replicas x{world}"}
+
+
+def flame_oracle(case):
+    sys.path.insert(0, str(ROOT / "tests"))
+    from oracle_ctypes import Oracle
+
+    o = Oracle()
+    fl = case.flags
+    qf0, qc0 = o.init_cells(case.T, case.p, case.u, case.X)
+    t = o.tube(case.ncell, 2, [1, 2, 1, 2, 0, 1, 1, fl["do_reaction"]],
+               [case.dx, fl["p_out"], fl["t_in"], fl["rho_u_in"], 1e-5, 1e-13], x_in=fl["x_in"])
+    t.set_transport()
+    t.set_interior(qf0, qc0)
+    return o, t
+
+
+def flame_reference_arm(args, rank, world):
+    """The oracle (the reference's algorithm, transport included) on all host
+    cores, the same flame, the same steps as the GPU arm."""
+    if rank != 0:
+        return
+    case = flame_case(args)
+    o, t = flame_oracle(case)
+    for _ in range(args.warmup):
+        t.step(case.cfl)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        t.step(case.cfl)
+    el = time.perf_counter() - t0
+    v = case.ncell * args.steps / el
+    cores = o.L.or_num_threads()
+    print(json.dumps({"impl": "reference", "metric": FLAME_METRIC, "value": v, "unit": UNIT, "n_gpus": world,
+                      "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
+                      "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                      "data": "synthetic", "config": flame_config(case, args, world),
+                      "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                                       "sample": f"steps {args.warmup + 1}..{args.warmup + args.steps} of the flame"},
+                      "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}),
+          flush=True)
+
+
+def flame_arm(args, rank, world, local):
+    """The planar flame with transport and chemistry (configs.planar_flame):
+    steps in CUDA graphs through edyn_advance; the transport's share from
+    the same tube's fluid step with and without it."""
+    import torch
+
+    from fortrancfd_gb300 import Tube
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=dev)
+    case = flame_case(args)
+    fl = {k: v for k, v in case.flags.items() if k != "do_tran"}
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
+    tube = Tube(case.ncell, case.dx, do_tran=1, strict_newton=0, **{k: v for k, v in fl.items()
+                                                                   if k != "strict_newton"})
+    tube.set_stream(stream.cuda_stream)
+    tube.init_cells(case.T, case.p, case.u, case.X)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize(dev)
+    with ClockSampler(local) as clk:
+        t_dev, graphs, t_sim = run_tube(tube, case, args.steps, args.warmup, stream, flush)
+    torch.cuda.synchronize(dev)
+    t_max = max_over_ranks(t_dev, world, dev)
+    # the fluid step with and without transport on the state reached
+    qf, qc, _ = tube.download()
+    inviscid = Tube(case.ncell, case.dx, strict_newton=0, **{k: v for k, v in fl.items() if k != "strict_newton"})
+    inviscid.set_stream(stream.cuda_stream)
+    inviscid.set_uniform_skip(False)
+    dt = tube.calc_dt(case.cfl)
+    ms = {"transport": [], "inviscid": []}
+    for _ in range(3):
+        for name, t in (("transport", tube), ("inviscid", inviscid)):
+            t.upload(qf, qc)
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            t.solve_fluid(dt)
+            b.record(stream)
+            b.synchronize()
+            ms[name].append(a.elapsed_time(b))
+    fl_t, fl_i = statistics.median(ms["transport"]), statistics.median(ms["inviscid"])
+    if rank != 0:
+        return
+    cpu = None
+    if not args.no_cpu_baseline and world == 1:
+        o, t = flame_oracle(case)
+        t.step(case.cfl)
+        n, t0 = 0, time.perf_counter()
+        while True:
+            t.step(case.cfl)
+            n += 1
+            el = time.perf_counter() - t0
+            if el > 15.0 or n >= 64:
+                break
+        cpu = {"value": case.ncell * n / el, "unit": UNIT, "cores": o.L.or_num_threads(), "kind": "port",
+               "sample": f"steps 2..{n + 1} of the flame, {el:.1f} s"}
+    # per step: the loop test, three (transport properties, transport flux,
+    # stage) triples and the one-pass chemistry (counter clear + pass)
+    per_step = 1 + 3 * 3 + 2
+    print(json.dumps({
+        "metric": FLAME_METRIC, "value": job_value(case.ncell, args.steps, world, t_max), "unit": UNIT,
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": flame_config(case, args, world), "clocks": clk.summary(),
+        "gpu_launches": graphs * 16 * per_step,
+        "transport": {"fluid_step_ms": fl_t, "inviscid_fluid_step_ms": fl_i,
+                      "transport_ms_per_stage": (fl_t - fl_i) / 3.0,
+                      "note": "the same tube's fluid step with and without transport, L2 flushed"},
+        "impl": {"l2": "L2 flushed between 16-step graphs", "simulated_time_s": t_sim},
+        "cpu_baseline": cpu}), flush=True)
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
     if args.impl == "reference":
+        if args.workload == "flame":
+            flame_reference_arm(args, rank, world)
+            return
         reference_arm(args, rank, world)
+        return
+    if args.workload == "flame":
+        flame_arm(args, rank, world, local)
         return
     if args.workload == "tubes":
         tubes_arm(args, rank, world, local)

@@ -127,6 +127,12 @@ struct Ctx {
   // transport (do_tran = 1): the fits, their device tables and the buffers
   // of the per-cell properties and the face fluxes
   int do_tran = 0;
+  std::string chem_dir;        // the mechanism directory (transport fits load from it on demand)
+  // energy sources after the chemistry (radiation, wall heat, ignition);
+  // src.nrad / wall / ig_type select them
+  SourceArgs src{};
+  bool src_on = false;
+  double clock = 0.0;          // time of the last edyn_step / edyn_advance (the ignition window's clock)
   double* d_tran = nullptr;
   double* d_tp = nullptr;
   double* d_tflux = nullptr;
@@ -284,7 +290,7 @@ int fluid_step(Ctx* c, double dt, bool dev, bool last_is_fluid) {
     for (int s = 0; s < 4; ++s) {
       a.rk4_stage = s;
       const bool last = s == 3;
-      a.cvel_out = (dev && last && last_is_fluid) ? (c->pk.ntube ? c->pk.d_cvel : c->d_cvel) : nullptr;
+      a.cvel_out = (dev && last && last_is_fluid && !c->src_on) ? (c->pk.ntube ? c->pk.d_cvel : c->d_cvel) : nullptr;
       a.time = (dev && last && last_is_fluid) ? c->d_time : nullptr;
       a.nsteps = (dev && last && last_is_fluid) ? c->d_nsteps : nullptr;
       cudaError_t e = launch_stage(a, c->acu, c->lim, c->wflag, c->riemann, c->stream);
@@ -315,7 +321,8 @@ int fluid_step(Ctx* c, double dt, bool dev, bool last_is_fluid) {
       a.h2 = 2.0 / 3.0;
     }
     const bool last = (s == nst - 1);
-    a.cvel_out = (dev && last && last_is_fluid) ? (c->pk.ntube ? c->pk.d_cvel : c->d_cvel) : nullptr;
+    // with energy sources the source kernel publishes the new state's speed
+    a.cvel_out = (dev && last && last_is_fluid && !c->src_on) ? (c->pk.ntube ? c->pk.d_cvel : c->d_cvel) : nullptr;
     a.time = (dev && last && last_is_fluid) ? c->d_time : nullptr;
     a.nsteps = (dev && last && last_is_fluid) ? c->d_nsteps : nullptr;
     cudaError_t e = launch_stage(a, c->acu, c->lim, c->wflag, c->riemann, c->stream);
@@ -327,7 +334,40 @@ int fluid_step(Ctx* c, double dt, bool dev, bool last_is_fluid) {
 
 int surrogate_source_step(Ctx* c, double dt, bool dev);
 
-int source_step(Ctx* c, double dt, bool dev) {
+int chem_source_step(Ctx* c, double dt, bool dev);
+
+// solve_source (SRC/update.f90:100-150): the chemistry, then the energy
+// sources. time: the step's time for the ignition window (host calls; the
+// device loop reads its clock).
+int source_step(Ctx* c, double dt, bool dev, double time = 0.0) {
+  int rc = chem_source_step(c, dt, dev);
+  if (rc || !c->src_on) return rc;
+  SourceArgs s = c->src;
+  s.n = c->n;
+  s.ld = c->ld;
+  s.ns = c->ns;
+  s.qf = c->qf[c->cur];
+  s.qc = c->qc;
+  s.dt = dt;
+  s.time = time;
+  s.dx = c->dx;
+  s.strict_newton = c->strict;
+  s.err = c->d_err;
+  s.lam = c->trd.lam;
+  s.e2 = c->trd.e2;
+  s.lg = c->trd.lg;
+  if (dev) {
+    s.dt_dev = c->d_dt;
+    s.time_dev = c->d_time;
+    s.step_active = c->d_active;
+    s.cvel = c->d_cvel;
+  }
+  cudaError_t e = launch_energy_sources(s, c->stream);
+  if (e != cudaSuccess) return fail(c, EDYN_E_CUDA, "energy sources: %s", cudaGetErrorString(e));
+  return EDYN_OK;
+}
+
+int chem_source_step(Ctx* c, double dt, bool dev) {
   if (!c->do_reaction) return EDYN_OK;
   if (c->chem_mode == 1) return surrogate_source_step(c, dt, dev);
   ChemLaunch L;
@@ -344,7 +384,7 @@ int source_step(Ctx* c, double dt, bool dev) {
   if (dev) {
     L.step_active = c->d_active;
     L.dt_dev = c->d_dt;
-    L.cvel_out = c->d_cvel;
+    L.cvel_out = c->src_on ? nullptr : c->d_cvel;  // with sources, their kernel publishes the speed
     L.time = c->d_time;
     L.nsteps = c->d_nsteps;
   }
@@ -740,7 +780,9 @@ int edyn_tran_compile(const char* chem_dir, const char* out_path, char* err, int
 namespace {
 // Transport set-up of edyn_init: loads the fits next to the mechanism,
 // checks them against it and builds the device tables of TranDev.
-int init_transport(Ctx* c, const char* chem_dir) {
+int load_tran_tables(Ctx* c) {
+  if (c->d_tran) return EDYN_OK;
+  const char* chem_dir = c->chem_dir.c_str();
   std::unique_ptr<edyn_tran> t(new (std::nothrow) edyn_tran);
   if (!t) return fail(c, EDYN_E_ARG, "out of host memory");
   char err[512] = {0};
@@ -782,11 +824,6 @@ int init_transport(Ctx* c, const char* chem_dir) {
   fill_log_table(&h[o_lg]);
   CK(cudaMalloc(&c->d_tran, h.size() * sizeof(double)));
   CK(cudaMemcpy(c->d_tran, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice));
-  const size_t ld = (size_t)c->ld;
-  CK(cudaMalloc(&c->d_tp, (size_t)(TRAN_ROWS_FIXED + 2 * ns) * ld * sizeof(double)));
-  CK(cudaMalloc(&c->d_tflux, (size_t)c->ne * ld * sizeof(double)));
-  CK(cudaMemset(c->d_tp, 0, (size_t)(TRAN_ROWS_FIXED + 2 * ns) * ld * sizeof(double)));
-  CK(cudaMemset(c->d_tflux, 0, (size_t)c->ne * ld * sizeof(double)));
   TranDev& d = c->trd;
   d.eta = c->d_tran + o_eta;
   d.lam = c->d_tran + o_lam;
@@ -798,8 +835,21 @@ int init_transport(Ctx* c, const char* chem_dir) {
   d.e2 = c->d_tran + o_e2;
   d.lg = c->d_tran + o_lg;
   d.patmos = t->patmos;
-  d.tp = c->d_tp;
-  d.flux = c->d_tflux;
+  return EDYN_OK;
+}
+
+// do_tran: the fits plus the property and face-flux buffers of the stages
+int init_transport(Ctx* c) {
+  int rc = load_tran_tables(c);
+  if (rc) return rc;
+  const size_t ld = (size_t)c->ld;
+  const size_t prow = (size_t)(TRAN_ROWS_FIXED + 2 * c->ns);
+  CK(cudaMalloc(&c->d_tp, prow * ld * sizeof(double)));
+  CK(cudaMalloc(&c->d_tflux, (size_t)c->ne * ld * sizeof(double)));
+  CK(cudaMemset(c->d_tp, 0, prow * ld * sizeof(double)));
+  CK(cudaMemset(c->d_tflux, 0, (size_t)c->ne * ld * sizeof(double)));
+  c->trd.tp = c->d_tp;
+  c->trd.flux = c->d_tflux;
   return EDYN_OK;
 }
 }  // namespace
@@ -939,8 +989,9 @@ int edyn_init(const char* chem_dir, int nspe, int nequ, int ncell, int lvir, con
   rc = chem_init(c->chem, m, c->tb, c->stream);
   if (rc) return fail(c, EDYN_E_CUDA, "chemistry tables: %s", cudaGetErrorString((cudaError_t)rc));
   CK(stage_tiling(c->acu, c->lim, c->wflag, c->riemann, c->ns, c->n, &c->stage_tc));
+  c->chem_dir = chem_dir ? chem_dir : ".";
   if (c->do_tran) {
-    rc = init_transport(c, chem_dir);
+    rc = init_transport(c);
     if (rc) return rc;
   }
   CK(cudaStreamSynchronize(c->stream));
@@ -1301,12 +1352,11 @@ int edyn_solve_fluid(void* ctx, double dt) {
 }
 
 int edyn_solve_source(void* ctx, double dt, double time) {
-  (void)time;
   Ctx* c = (Ctx*)ctx;
   if (!c || !c->qc) return EDYN_E_ARG;
   if (c->pk.ntube)
     return fail(c, EDYN_E_ARG, "packed tubes take their own time steps: step them with edyn_step or edyn_advance");
-  int rc = source_step(c, dt, false);
+  int rc = source_step(c, dt, false, time);
   if (rc) return rc;
   if (c->do_reaction) c->hrr_dot_state = 1;
   CK(cudaStreamSynchronize(c->stream));
@@ -1342,7 +1392,8 @@ int edyn_step(void* ctx, double cfl, double* dt) {
   if (c->do_reaction) c->hrr_dot_state = 0;
   rc = edyn_solve_fluid(ctx, d);
   if (rc) return rc;
-  rc = edyn_solve_source(ctx, d, 0.0);
+  c->clock += d;  // the reference advances time before the step (SRC/main.f90:139)
+  rc = edyn_solve_source(ctx, d, c->clock);
   if (rc) return rc;
   rc = edyn_post_step(ctx);
   if (dt) *dt = d;
@@ -1387,6 +1438,7 @@ int edyn_advance(void* ctx, double cfl, double tend, long long max_steps, double
       done = ns;
     }
     *time = t;
+    c->clock = t;
     if (nsteps) *nsteps = done;
     if (done > 0) c->hrr_dot_state = 1;
     return take_status(c, "edyn_advance");
@@ -1448,6 +1500,7 @@ int edyn_advance(void* ctx, double cfl, double tend, long long max_steps, double
     CK(cudaMemcpy(&t, clock, sizeof(double), cudaMemcpyDeviceToHost));
   }
   *time = t;
+  c->clock = t;
   if (nsteps) *nsteps = done;
   if (done > 0 && c->do_reaction) c->hrr_dot_state = 1;
   return take_status(c, "edyn_advance");
@@ -1593,6 +1646,79 @@ int edyn_transport_properties(void* ctx, double* mu, double* kappa, double* dif)
       for (int k = 0; k < c->ns; ++k) dif[(size_t)i * c->ns + k] = h[(TRAN_ROWS_FIXED + c->ns + k) * ld + col];
   }
   return take_status(c, "edyn_transport_properties");
+}
+
+namespace {
+int sources_allowed(Ctx* c, const char* what) {
+  if (c->pk.ntube) return fail(c, EDYN_E_ARG, "%s: one tube per context (packed tubes have no energy sources)", what);
+  if (c->chem_mode == 1) return fail(c, EDYN_E_ARG, "%s: not with the surrogate chemistry (chem_mode 1)", what);
+  return EDYN_OK;
+}
+void sources_changed(Ctx* c) {
+  c->src_on = c->src.nrad > 0 || c->src.wall || c->src.ig_type;
+  drop_graph(c);
+}
+}  // namespace
+
+int edyn_set_radiation(void* ctx, int nrad, const int* species, const double* coef) {
+  Ctx* c = (Ctx*)ctx;
+  if (!c || !c->qc) return EDYN_E_ARG;
+  if (int rc = sources_allowed(c, "edyn_set_radiation")) return rc;
+  if (nrad < 0 || nrad > EDYN_RAD_MAX || (nrad > 0 && (!species || !coef)))
+    return fail(c, EDYN_E_ARG, "edyn_set_radiation: %d radiating species (0..%d, with their fits)", nrad, EDYN_RAD_MAX);
+  for (int r = 0; r < nrad; ++r)
+    if (species[r] < 0 || species[r] >= c->ns)
+      return fail(c, EDYN_E_ARG, "edyn_set_radiation: species index %d out of range", species[r]);
+  c->src.nrad = nrad;
+  for (int r = 0; r < nrad; ++r) {
+    c->src.rad_sp[r] = species[r];
+    for (int n = 0; n < 6; ++n) c->src.rad_coef[r][n] = coef[6 * r + n];
+  }
+  sources_changed(c);
+  return EDYN_OK;
+}
+
+int edyn_set_wall_heat(void* ctx, int on, const double* params) {
+  Ctx* c = (Ctx*)ctx;
+  if (!c || !c->qc) return EDYN_E_ARG;
+  if (int rc = sources_allowed(c, "edyn_set_wall_heat")) return rc;
+  if ((on != 0 && on != 1) || (on && !params)) return fail(c, EDYN_E_ARG, "edyn_set_wall_heat: on must be 0 or 1");
+  if (on) {
+    if (!(params[1] > 0.0)) return fail(c, EDYN_E_ARG, "edyn_set_wall_heat: the diameter must be positive");
+    int rc = load_tran_tables(c);  // the conductivity of MCACON
+    if (rc) return rc;
+    c->src.nu = params[0];
+    c->src.d_m = params[1];
+    c->src.tw_min = params[2];
+    c->src.tw_max = params[3];
+    c->src.alpha = params[4];
+    c->src.beta = params[5];
+  }
+  c->src.wall = on;
+  sources_changed(c);
+  return EDYN_OK;
+}
+
+int edyn_set_ignition(void* ctx, int type, int n, const double* energy, const double* radius, const double* duration,
+                      const double* start) {
+  Ctx* c = (Ctx*)ctx;
+  if (!c || !c->qc) return EDYN_E_ARG;
+  if (int rc = sources_allowed(c, "edyn_set_ignition")) return rc;
+  if (type < 0 || type > 2) return fail(c, EDYN_E_ARG, "edyn_set_ignition: type %d not in 0..2", type);
+  if (type && (n < 1 || n > EDYN_IG_MAX || !energy || !radius || !duration || !start))
+    return fail(c, EDYN_E_ARG, "edyn_set_ignition: %d sources (1..%d, with their data)", n, EDYN_IG_MAX);
+  for (int g = 0; type && g < n; ++g)
+    if (!(radius[g] > 0.0)) return fail(c, EDYN_E_ARG, "edyn_set_ignition: radius %d must be positive", g);
+  c->src.ig_type = type;
+  c->src.n_ig = type ? n : 0;
+  for (int g = 0; g < c->src.n_ig; ++g) {
+    c->src.ig_e[g] = energy[g];
+    c->src.ig_r[g] = radius[g];
+    c->src.ig_t[g] = duration[g];
+    c->src.ig_t0[g] = start[g];
+  }
+  sources_changed(c);
+  return EDYN_OK;
 }
 
 int edyn_set_uniform_skip(void* ctx, int on) {

@@ -89,6 +89,35 @@ struct StageArgs {
   TranDev tran;          // do_tran: transport fluxes added to the advective ones (tran.flux null: off)
 };
 
+// Energy sources of solve_source after the chemistry (SRC/update.f90:126-147):
+// optically thin radiation, micro-flow-reactor wall heat and ignition energy,
+// each added to rho E over dt and followed by QcToqf of every cell.
+constexpr int EDYN_RAD_MAX = 16;  // radiating species
+constexpr int EDYN_IG_MAX = 8;    // ignition sources
+struct SourceArgs {
+  int n, ld, ns;
+  double* qf;               // primitive rows (the current buffer), rewritten
+  double* qc;               // conserved rows, energy row updated
+  double dt, time;          // host call: the step's dt and time
+  const double* dt_dev;     // device loop: the step's dt ...
+  const double* time_dev;   // ... and the clock the step already advanced
+  const int* step_active;   // device loop: skip when zero
+  double dx;                // cell centres at (i + 1/2) dx
+  int strict_newton;
+  unsigned* err;
+  unsigned long long* cvel; // device loop: max signal speed of the new state
+  int nrad;                 // radiation: species and Planck-mean fits a0..a5 [1/(m atm)]
+  int rad_sp[EDYN_RAD_MAX];
+  double rad_coef[EDYN_RAD_MAX][6];
+  int wall;                 // wall heat: Nu, diameter [m], Tw(x) = A tanh(alpha (x - beta)) + B
+  double nu, d_m, tw_min, tw_max, alpha, beta;
+  const double* lam;        // conductivity fits (TranDev::lam), and the texp / tlog tables
+  const double* e2;
+  const double* lg;
+  int ig_type, n_ig;        // ignition: 1 Frendi et al., 2 Zhang et al.; per source E [J], r [m], t, t0 [s]
+  double ig_e[EDYN_IG_MAX], ig_r[EDYN_IG_MAX], ig_t[EDYN_IG_MAX], ig_t0[EDYN_IG_MAX];
+};
+
 int fluid_upload_tables(const ThermoTable& tb, cudaStream_t s);
 size_t stage_smem_bytes(int acu, int ns, int tc);
 cudaError_t stage_tiling(int acu, int lim, int wflag, int rm, int ns, int n, int* tc);
@@ -108,6 +137,7 @@ cudaError_t launch_qc_to_qf(const StageArgs& a, cudaStream_t s);
 // Transport properties of cells -1..n and transport fluxes of faces 0..n of
 // the stage input (a.tran); launch_stage calls it before the stage kernel.
 cudaError_t launch_tran(const StageArgs& a, cudaStream_t s);
+cudaError_t launch_energy_sources(const SourceArgs& a, cudaStream_t s);
 cudaError_t launch_check_state(const double* qf, const double* qc, int n, int ns, int ld, unsigned* err,
                                cudaStream_t s);
 cudaError_t launch_init_cells(int n, int ns, const double* T, const double* p, const double* u, const double* X,

@@ -979,6 +979,124 @@ cudaError_t launch_tran(const StageArgs& a, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------
+// Energy sources of solve_source after the chemistry (SRC/update.f90:126-147),
+// one thread per cell, in the reference's order, each followed by QcToqf of
+// the cell (the reference recomputes every interior cell's qf after each):
+//   radiation   heat_transfer_radiation (SRC/source.f90:88-137) with
+//               radiation_heat_loss (SRC/radiation.f90:74-121): optically
+//               thin, Q = -4 Kp sigma (T^4 - 300^4), Kp = sum_r kp_r(T) X_r p/atm;
+//   wall heat   heat_transfer_mfr (SRC/source.f90:140-189) with heat_transfer
+//               and Tw (SRC/mfr.f90:41-78): Q = -4 lambda Nu (T - Tw(x)) / d^2,
+//               lambda from MCACON;
+//   ignition    energy_source (SRC/source.f90:192-239) with add_igsource /
+//               add_igsource_WZhang (SRC/ignitionsource.f90:150-262).
+// rho E += dt Q each time. The new state's signal speed feeds the next
+// step's dt in the device loop (the chemistry then publishes none).
+// ---------------------------------------------------------------------------
+constexpr int SRC_THREADS = 128;
+
+__global__ void __launch_bounds__(SRC_THREADS) k_energy_sources(SourceArgs s) {
+  if (s.step_active && *s.step_active == 0) return;
+  const int i = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+  double speed = 0.0;
+  if (i < s.n) {
+    const ThermoTable& tb = c_thermo;
+    const int ns = s.ns;
+    const size_t ld = (size_t)s.ld;
+    const double dt = s.dt_dev ? *s.dt_dev : s.dt;
+    const double time = s.time_dev ? *s.time_dev : s.time;
+    double* Q = s.qc + i + GHOST;
+    double* F = s.qf + i + GHOST;
+    const double q0 = Q[0], q1 = Q[ld];
+    double q2 = Q[2 * ld];
+    double rho = F[0], u = F[ld], T = F[2 * ld];
+    double y[EDYN_NS_MAX], ys[EDYN_NS_MAX];
+    for (int k = 0; k < ns; ++k) y[k] = F[(3 + k) * ld];
+    const double xm = (i + 0.5) * s.dx;
+    CellEOS e{};
+    for (int src = 0; src < 3; ++src) {
+      double add = 0.0;
+      if (src == 0 || src == 1) {
+        if (src == 0 ? s.nrad == 0 : s.wall == 0) continue;
+        // mole fractions (CKYTX) and pressure (CKPX) of the cell's qf
+        double sumyow = 0.0;
+        for (int k = 0; k < ns; ++k) sumyow = fma(y[k], tb.invW[k], sumyow);
+        const double isw = 1.0 / sumyow;
+        double sy = 0.0;
+        for (int k = 0; k < ns; ++k) sy += y[k];
+        if (src == 0) {
+          const double p = R_SI * rho * T * sumyow / sy;
+          const double T1 = T, T2 = T1 * T1, T3 = T2 * T1, T4 = T3 * T1, T5 = T4 * T1;
+          const double T04 = 300.0 * 300.0 * 300.0 * 300.0;
+          double kp = 0.0;
+          for (int r = 0; r < s.nrad; ++r) {
+            const double* c = s.rad_coef[r];
+            const double kpi = c[0] + c[1] * T1 + c[2] * T2 + c[3] * T3 + c[4] * T4 + c[5] * T5;
+            const int k = s.rad_sp[r];
+            kp = kp + kpi * (y[k] * tb.invW[k] * isw) * (p / 101325.0);
+          }
+          add = -4.0 * kp * 5.6703744191844294e-08 * (T4 - T04);
+        } else {
+          const double L = tlog(T, s.lg);
+          double sl = 0.0, sr = 0.0;
+          for (int k = 0; k < ns; ++k) {
+            const double* cl = s.lam + 4 * k;
+            const double lk = texp_r(fma(fma(fma(cl[3], L, cl[2]), L, cl[1]), L, cl[0]), s.e2);
+            const double xk = y[k] * tb.invW[k] * isw;
+            sl = fma(xk, lk, sl);
+            sr += xk / lk;
+          }
+          const double lambda = 0.5 * (sl + 1.0 / sr) * 1.0e-5;
+          const double A = 0.5 * (s.tw_max - s.tw_min), B = 0.5 * (s.tw_max + s.tw_min);
+          const double tw = A * tanh(s.alpha * (xm - s.beta)) + B;
+          add = -4.0 * lambda * s.nu * (T - tw) / (s.d_m * s.d_m);
+        }
+      } else {
+        if (s.ig_type == 0) continue;
+        const double pi = 3.14159265359;  // the reference's constant
+        for (int g = 0; g < s.n_ig; ++g) {
+          const double r = s.ig_r[g], tg = s.ig_t[g], t0 = s.ig_t0[g];
+          if (!(t0 < time && time < t0 + tg)) continue;
+          const double w = xm / r;
+          if (s.ig_type == 1) {  // Frendi et al.: top-hat-like exp(-(pi/4) (r/r_ig)^6) over a sphere's volume
+            const double vol = 4.0 * pi * (r * r * r) / 3.0;
+            const double w2 = w * w;
+            add = s.ig_e[g] / (vol * tg) * exp(-(pi / 4.0) * (w2 * w2 * w2));
+          } else {               // Zhang et al.: Gaussian
+            add = s.ig_e[g] / (pow(pi, 1.5) * (r * r * r) * tg) * exp(-(w * w));
+          }
+        }
+      }
+      q2 = q2 + dt * add;
+      for (int k = 0; k < ns; ++k) ys[k] = Q[(3 + k) * ld];
+      int it;
+      e = qc_to_qf_cell(q0, q1, q2, ys, 1, T, s.strict_newton != 0, it);
+      if (e.status && s.err) atomicOr(s.err, e.status);
+      rho = q0;
+      u = e.u;
+      T = e.T;
+      for (int k = 0; k < ns; ++k) y[k] = ys[k];
+    }
+    Q[2 * ld] = q2;
+    F[0] = rho;
+    F[ld] = u;
+    F[2 * ld] = T;
+    for (int k = 0; k < ns; ++k) F[(3 + k) * ld] = y[k];
+    if (s.cvel) speed = cell_speed(u, T, e.Sz, e.cpR);
+  }
+  if (s.cvel) {
+    double m = speed;
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0 && m > 0.0) atomic_max_pos(s.cvel, m);
+  }
+}
+
+cudaError_t launch_energy_sources(const SourceArgs& a, cudaStream_t s) {
+  k_energy_sources<<<(a.n + SRC_THREADS - 1) / SRC_THREADS, SRC_THREADS, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
 __global__ void k_step_begin_tubes(int ntube, const double* time, double tend, const long long* nsteps,
                                    const long long* max_steps, double cfl, const double* dx, unsigned long long* cvel,
                                    int* active, double* dt, int* step_active) {

@@ -91,6 +91,9 @@ def lib() -> ctypes.CDLL:
     L.edyn_mech_compile.argtypes = [cp, cp, ctypes.c_char_p, i]
     L.edyn_tran_compile.argtypes = [cp, cp, ctypes.c_char_p, i]
     L.edyn_transport_properties.argtypes = [vp, dp, dp, dp]
+    L.edyn_set_radiation.argtypes = [vp, i, ip, dp]
+    L.edyn_set_wall_heat.argtypes = [vp, i, dp]
+    L.edyn_set_ignition.argtypes = [vp, i, i, dp, dp, dp, dp]
     L.edyn_version.restype = ctypes.c_char_p
     _lib = L
     return L
@@ -276,6 +279,32 @@ class Tube(_Ctx):
         dif = np.zeros((self.ncell, self.nspe))
         self._check(lib().edyn_transport_properties(self._h, _ptr(mu), _ptr(kap), _ptr(dif)))
         return mu, kap, dif
+
+    def set_radiation(self, fits: Optional[dict] = None) -> None:
+        """Optically thin radiation loss after the chemistry: {species name:
+        (a0, ..., a5)} Planck-mean fits in T [1/(m atm)], as the reference's
+        radiation_file; None or {} switches it off."""
+        names = species_names()
+        fits = fits or {}
+        sp = (ctypes.c_int * max(1, len(fits)))(*[names.index(k) for k in fits])
+        coef = np.ascontiguousarray([list(v) for v in fits.values()] or [[0.0] * 6], dtype=np.float64)
+        self._check(lib().edyn_set_radiation(self._h, len(fits), sp, _ptr(coef)))
+
+    def set_wall_heat(self, nu=None, d=None, tw_min=None, tw_max=None, alpha=None, beta=None) -> None:
+        """Micro-flow-reactor wall heat after the chemistry (d [m], alpha
+        [1/m], beta [m]); no arguments switch it off."""
+        if nu is None:
+            self._check(lib().edyn_set_wall_heat(self._h, 0, None))
+            return
+        p = np.ascontiguousarray([nu, d, tw_min, tw_max, alpha, beta], dtype=np.float64)
+        self._check(lib().edyn_set_wall_heat(self._h, 1, _ptr(p)))
+
+    def set_ignition(self, kind: int = 0, sources: Sequence = ()) -> None:
+        """Ignition energy after the chemistry: kind 1 (Frendi) or 2 (Zhang),
+        sources [(E [J], r [m], duration [s], start [s]), ...]; kind 0 off."""
+        a = np.ascontiguousarray(list(sources) or [[0.0] * 4], dtype=np.float64).reshape(-1, 4)
+        cols = [np.ascontiguousarray(a[:, j]) for j in range(4)]
+        self._check(lib().edyn_set_ignition(self._h, int(kind), len(sources), *[_ptr(c) for c in cols]))
 
     def set_uniform_skip(self, on: bool = True) -> None:
         """Uniform regions (on by default): the fluid stage computes no faces

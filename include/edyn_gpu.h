@@ -360,6 +360,39 @@ int edyn_finalize(void* ctx);
  * (the role of CKINTERP's chem.bin, GRI/ckinterp.f). */
 int edyn_mech_compile(const char* chem_dir, const char* out_path, char* err, int errlen);
 
+/* Energy sources of solve_source after the chemistry (SRC/update.f90:126-147),
+ * in the reference's order, each added to rho E over the step and followed
+ * by QcToqf of every cell; for one tube per context, not with chem_mode 1.
+ * Cell i sits at x = (i + 1/2) dx.
+ *
+ * Optically thin radiation loss (heat_transfer_radiation,
+ * SRC/source.f90:88-137; radiation_heat_loss, SRC/radiation.f90:74-121):
+ * Q = -4 Kp sigma (T^4 - 300^4), Kp = sum_r kp_r(T) X_r p / (1 atm), with
+ * kp_r(T) = coef[6r] + coef[6r+1] T + ... + coef[6r+5] T^5 [1/(m atm)] for
+ * species index species[r] (the reference's radiation_file, one line per
+ * species). nrad = 0 switches it off. */
+int edyn_set_radiation(void* ctx, int nrad, const int* species, const double* coef);
+
+/* Micro-flow-reactor wall heat (heat_transfer_mfr, SRC/source.f90:140-189;
+ * SRC/mfr.f90:41-78): Q = -4 lambda Nu (T - Tw(x)) / d^2 with lambda the
+ * mixture conductivity (MCACON, from the transport fits next to the
+ * mechanism) and Tw(x) = (Tw_max - Tw_min)/2 tanh(alpha (x - beta)) +
+ * (Tw_max + Tw_min)/2. params: Nu, d [m], Tw_min [K], Tw_max [K],
+ * alpha [1/m], beta [m] (the reference's /mfrwalltemp/ namelist, d in m). */
+int edyn_set_wall_heat(void* ctx, int on, const double* params);
+
+/* Ignition energy (energy_source, SRC/source.f90:192-239;
+ * SRC/ignitionsource.f90:150-262): type 1 after Frendi et al.
+ * (E / (4/3 pi r^3 t) exp(-(pi/4) (x/r)^6)), type 2 after Zhang et al.
+ * (E / (pi^1.5 r^3 t) exp(-(x/r)^2)), 0 off; n sources with energy [J],
+ * radius [m], duration and start [s], each on while start < time < start +
+ * duration (where several are on, the last one's rate applies, as in the
+ * reference). time is the step's time: edyn_solve_source's argument, the
+ * context's clock in edyn_step (advanced by each step, set by edyn_advance),
+ * the device clock in edyn_advance. */
+int edyn_set_ignition(void* ctx, int type, int n, const double* energy, const double* radius, const double* duration,
+                      const double* start);
+
 /* Writes the transport fits of chem_dir (TRANLIB's linking file tran.bin, as
  * MCINIT reads it, tranlib.f:214-258) in the library's text form tran.edyn,
  * every number to 17 significant digits (it reads back bit for bit). */

@@ -122,6 +122,18 @@ void or_tran_cell(const or_mech* m, const or_tran* t, const double* qc, double* 
 void or_face_flux_tran(const or_mech* m, const or_tran* t, const double* qcl, const double* qcr, double dx,
                        double* g);
 
+/* Energy sources of solve_source after the chemistry (SRC/update.f90:126-147). */
+typedef struct or_sources {
+  int nrad;                  /* radiation_heat_loss, SRC/radiation.f90:74-121 */
+  int rad_sp[16];
+  double rad_coef[16][6];
+  int wall;                  /* heat_transfer + Tw, SRC/mfr.f90:41-78 */
+  double nu, d_m, tw_min, tw_max, alpha, beta;
+  const or_tran* tran;       /* conductivity (MCACON) of the wall heat */
+  int ig_type, n_ig;         /* add_igsource(_WZhang), SRC/ignitionsource.f90:150-262 */
+  double ig_e[8], ig_r[8], ig_t[8], ig_t0[8];
+} or_sources;
+
 /* 1-D tube state with ghost cells (equal-dx blocks collapse to one array). */
 typedef struct or_tube {
   const or_mech* m;
@@ -140,6 +152,8 @@ typedef struct or_tube {
   double* hrr_dot;
   long chem_rhs_evals, chem_steps;
   const or_tran* tran; /* do_tran: transport fits (NULL: inviscid) */
+  or_sources src;      /* energy sources (all off when zeroed) */
+  double time;         /* the time loop's clock: advanced by or_step before the step */
 } or_tube;
 
 or_tube* or_tube_create(const or_mech* m, int n, int lvir, const int* iflags, const double* rparams,
@@ -158,6 +172,9 @@ void or_calc_flux_advection(or_tube* t);
 void or_tube_set_transport(or_tube* t, const or_tran* tr);
 /* calc_flux_tran, SRC/flux.f90:18-127: adds the transport flux of every face to fplus. */
 void or_calc_flux_tran(or_tube* t);
+void or_tube_set_sources(or_tube* t, const or_sources* s);
+void or_tube_set_time(or_tube* t, double time);
+int or_sources_sizeof(void);
 void or_solve_fluid(or_tube* t, double dt);
 void or_solve_source(or_tube* t, double dt);
 void or_post_step(or_tube* t);

@@ -582,7 +582,91 @@ void or_post_step(or_tube* t) { stage_tail(t); }
 
 /* solve_source -> reaction_macks, SRC/update.f90:100-150 and
  * SRC/source.f90:17-84, with the project's FP64 integrator as "macks". */
+static void or_solve_reaction(or_tube* t, double dt);
+
+void or_tube_set_sources(or_tube* t, const or_sources* s) { t->src = *s; }
+void or_tube_set_time(or_tube* t, double time) { t->time = time; }
+int or_sources_sizeof(void) { return (int)sizeof(or_sources); }
+
+/* QcToqf of every interior cell, as each energy source ends (SRC/source.f90:130-134). */
+static void interior_qc_to_qf(or_tube* t) {
+#pragma omp parallel for schedule(static)
+  for (int i = 0; i < t->n; ++i) or_qc_to_qf(t->m, QC(t, i), QF(t, i));
+}
+
+/* radiation_heat_loss, SRC/radiation.f90:74-121 */
+static double rad_loss(const or_sources* s, double p, double T, const double* x) {
+  const double stefan_boltzmann = 5.6703744191844294e-08;
+  double T1 = T, T2 = T1 * T1, T3 = T2 * T1, T4 = T3 * T1, T5 = T4 * T1;
+  double T0 = 300.0, T04 = T0 * T0 * T0 * T0;
+  double kp = 0.0;
+  for (int r = 0; r < s->nrad; ++r) {
+    const double* c = s->rad_coef[r];
+    double kpi = c[0] + c[1] * T1 + c[2] * T2 + c[3] * T3 + c[4] * T4 + c[5] * T5;
+    kp = kp + kpi * x[s->rad_sp[r]] * (p / 101325.0);
+  }
+  return -4.0 * kp * stefan_boltzmann * (T4 - T04);
+}
+
+/* heat_transfer + Tw, SRC/mfr.f90:41-78 (thermal_conductivity, SRC/trans.f90:63-77) */
+static double wall_heat(const or_sources* s, double T, const double* x, double xm) {
+  double lambda = or_thermal_conductivity(s->tran, T, x);
+  double A = 0.5 * (s->tw_max - s->tw_min), B = 0.5 * (s->tw_max + s->tw_min);
+  double tw = A * tanh(s->alpha * (xm - s->beta)) + B;
+  return -4.0 * lambda * s->nu * (T - tw) / (s->d_m * s->d_m);
+}
+
+/* add_igsource (type 1) and add_igsource_WZhang (type 2), SRC/ignitionsource.f90:150-262 */
+static double ignition(const or_sources* s, double time, double rm) {
+  const double pi = 3.14159265359;
+  double eadd = 0.0;
+  for (int g = 0; g < s->n_ig; ++g) {
+    double e = s->ig_e[g], r = s->ig_r[g], tg = s->ig_t[g], t0 = s->ig_t0[g];
+    if (t0 < time && time < t0 + tg) {
+      if (s->ig_type == 1) {
+        double vol = 4.0 * pi * (r * r * r) / 3.0;
+        double w = rm / r, w2 = w * w;
+        eadd = e / (vol * tg) * exp(-(pi / 4.0) * (w2 * w2 * w2));
+      } else {
+        double w = rm / r;
+        eadd = e / (pow(pi, 1.5) * (r * r * r) * tg) * exp(-(w * w));
+      }
+    }
+  }
+  return eadd;
+}
+
+/* heat_transfer_radiation, heat_transfer_mfr, energy_source
+ * (SRC/source.f90:88-239) in the order of solve_source (SRC/update.f90:126-147). */
+static void energy_sources(or_tube* t, double dt) {
+  const or_mech* m = t->m;
+  const or_sources* s = &t->src;
+  for (int src = 0; src < 3; ++src) {
+    if ((src == 0 && !s->nrad) || (src == 1 && !s->wall) || (src == 2 && !s->ig_type)) continue;
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < t->n; ++i) {
+      const double* q = QF(t, i);
+      double x[OR_MAXSP], add;
+      double xm = (i + 0.5) * t->dx;
+      if (src == 2) {
+        add = ignition(s, t->time, xm);
+      } else {
+        or_ckytx(m, q + 3, x);
+        double p = or_pressure(m, q[0], q[2], x);
+        add = src == 0 ? rad_loss(s, p, q[2], x) : wall_heat(s, q[2], x, xm);
+      }
+      QC(t, i)[2] = QC(t, i)[2] + dt * add;
+    }
+    interior_qc_to_qf(t);
+  }
+}
+
 void or_solve_source(or_tube* t, double dt) {
+  or_solve_reaction(t, dt);
+  energy_sources(t, dt);
+}
+
+static void or_solve_reaction(or_tube* t, double dt) {
   if (!t->do_reaction) return;
   const or_mech* m = t->m;
   const int ns = t->nspe;
@@ -627,6 +711,7 @@ void or_solve_source(or_tube* t, double dt) {
 /* One pass of the time loop body, SRC/main.f90:130-163. */
 double or_step(or_tube* t, double cfl) {
   double dt = or_calc_dt(t, cfl);
+  t->time = t->time + dt;
   or_solve_fluid(t, dt);
   or_solve_source(t, dt);
   or_post_step(t);

@@ -96,6 +96,9 @@ class Oracle:
         L.or_tran_cell.argtypes = [vp, vp, _D, _D, _D, _D, _D, _D, _D, _D]
         L.or_face_flux_tran.argtypes = [vp, vp, _D, _D, d, _D]
         L.or_tube_set_transport.argtypes = [vp, vp]
+        L.or_tube_set_sources.argtypes = [vp, vp]
+        L.or_tube_set_time.argtypes = [vp, d]
+        L.or_sources_sizeof.restype = i
         self.kk = 53
         self.nequ = self.kk + 3
 
@@ -210,6 +213,16 @@ class Oracle:
         return y, fails, rhs.value
 
 
+class Sources(ctypes.Structure):
+    """or_sources: the energy sources of solve_source after the chemistry."""
+    _fields_ = [("nrad", ctypes.c_int), ("rad_sp", ctypes.c_int * 16), ("rad_coef", (ctypes.c_double * 6) * 16),
+                ("wall", ctypes.c_int), ("nu", ctypes.c_double), ("d_m", ctypes.c_double),
+                ("tw_min", ctypes.c_double), ("tw_max", ctypes.c_double), ("alpha", ctypes.c_double),
+                ("beta", ctypes.c_double), ("tran", ctypes.c_void_p), ("ig_type", ctypes.c_int),
+                ("n_ig", ctypes.c_int), ("ig_e", ctypes.c_double * 8), ("ig_r", ctypes.c_double * 8),
+                ("ig_t", ctypes.c_double * 8), ("ig_t0", ctypes.c_double * 8)]
+
+
 class OracleTube:
     def __init__(self, o: Oracle, h, n, keep):
         self.o, self.h, self.n, self._keep = o, h, n, keep
@@ -232,6 +245,30 @@ class OracleTube:
 
     def step(self, cfl):
         return self.o.L.or_step(self.h, cfl)
+
+    def set_sources(self, radiation=None, wall=None, ignition=None):
+        """radiation: [(species index, 6 fit coefficients)]; wall: (Nu, d, Tw_min,
+        Tw_max, alpha, beta); ignition: (type, [(E, r, duration, start)])."""
+        s = Sources()
+        for r, (k, c) in enumerate(radiation or []):
+            s.rad_sp[r] = k
+            for n in range(6):
+                s.rad_coef[r][n] = c[n]
+        s.nrad = len(radiation or [])
+        if wall is not None:
+            s.wall = 1
+            s.nu, s.d_m, s.tw_min, s.tw_max, s.alpha, s.beta = wall
+            s.tran = ctypes.addressof(self.o.tran)
+        if ignition is not None:
+            s.ig_type = ignition[0]
+            s.n_ig = len(ignition[1])
+            for g, (e, r, d, t0) in enumerate(ignition[1]):
+                s.ig_e[g], s.ig_r[g], s.ig_t[g], s.ig_t0[g] = e, r, d, t0
+        self._src = s
+        self.o.L.or_tube_set_sources(self.h, ctypes.byref(s))
+
+    def set_time(self, time):
+        self.o.L.or_tube_set_time(self.h, time)
 
     def set_transport(self, on=True):
         """do_tran = 1: calc_flux_tran joins every stage's flux."""

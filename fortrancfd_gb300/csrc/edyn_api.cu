@@ -127,6 +127,7 @@ struct Ctx {
   // transport (do_tran = 1): the fits, their device tables and the buffers
   // of the per-cell properties and the face fluxes
   int do_tran = 0;
+  int spherical = 0;           // is_spherical (the problem file's /problem/ flag)
   std::string chem_dir;        // the mechanism directory (transport fits load from it on demand)
   // energy sources after the chemistry (radiation, wall heat, ignition);
   // src.nrad / wall / ig_type select them
@@ -243,6 +244,11 @@ StageArgs base_args(Ctx* c) {
     // the transport flux of a face is not decided by the stencil test of the
     // uniform-region shortcuts (it reads the conserved state): every face
     a.tran = c->trd;
+    a.skip_uniform = 0;
+  }
+  if (c->spherical) {
+    // equal face fluxes do not cancel under the face areas
+    a.spherical = 1;
     a.skip_uniform = 0;
   }
   if (c->pk.ntube) {
@@ -885,6 +891,7 @@ int edyn_init(const char* chem_dir, int nspe, int nequ, int ncell, int lvir, con
   c->strict = fl(EDYN_IF_STRICT_NEWTON, 1);
   c->chem_mode = fl(EDYN_IF_CHEM_MODE, 0);
   c->do_tran = fl(EDYN_IF_DO_TRAN, 0);
+  c->spherical = fl(EDYN_IF_IS_SPHERICAL, 0);
   c->dx = rp(EDYN_RP_DX, 0.0);
   c->p_out = rp(EDYN_RP_P_OUT, 101325.0);
   c->t_in = rp(EDYN_RP_T_IN, 300.0);
@@ -894,6 +901,9 @@ int edyn_init(const char* chem_dir, int nspe, int nequ, int ncell, int lvir, con
   if (c->chem_mode != 0 && c->chem_mode != 1)
     return fail(c, EDYN_E_ARG, "chem_mode=%d: 0 (implicit integrator) or 1 (surrogate with fallback)", c->chem_mode);
   if (c->do_tran != 0 && c->do_tran != 1) return fail(c, EDYN_E_ARG, "do_tran=%d must be 0 or 1", c->do_tran);
+  if (c->spherical != 0 && c->spherical != 1) return fail(c, EDYN_E_ARG, "is_spherical=%d must be 0 or 1", c->spherical);
+  if (c->spherical && (c->select_time == 2 || c->flag_acu == 2))
+    return fail(c, EDYN_E_ARG, "spherical geometry takes Euler or TVDRK3 with first order or MUSCL");
   if (c->select_time < 0 || c->select_time > 2)
     return fail(c, EDYN_E_ARG, "select_time=%d not in 0..2 (Euler, TVDRK3, RK4)", c->select_time);
   if (c->riemann < 0 || c->riemann > 2) return fail(c, EDYN_E_ARG, "select_riemann=%d not in 0..2", c->riemann);
@@ -988,7 +998,7 @@ int edyn_init(const char* chem_dir, int nspe, int nequ, int ncell, int lvir, con
   if (rc) return fail(c, EDYN_E_CUDA, "constant tables: %s", cudaGetErrorString((cudaError_t)rc));
   rc = chem_init(c->chem, m, c->tb, c->stream);
   if (rc) return fail(c, EDYN_E_CUDA, "chemistry tables: %s", cudaGetErrorString((cudaError_t)rc));
-  CK(stage_tiling(c->acu, c->lim, c->wflag, c->riemann, c->ns, c->n, &c->stage_tc));
+  CK(stage_tiling(c->acu, c->lim, c->wflag, c->riemann, c->ns, c->n, &c->stage_tc, c->spherical));
   c->chem_dir = chem_dir ? chem_dir : ".";
   if (c->do_tran) {
     rc = init_transport(c);
@@ -1040,9 +1050,10 @@ int edyn_init_tubes(const char* chem_dir, int nspe, int nequ, int ntube, const i
     if (rc == EDYN_OK) rc = fail((Ctx*)*out, EDYN_E_ARG, "packed tubes take the plain chemistry (chem_mode 0)");
     return rc ? rc : EDYN_E_ARG;
   }
-  if (n_iflags > EDYN_IF_DO_TRAN && iflags[EDYN_IF_DO_TRAN] != 0) {
+  if ((n_iflags > EDYN_IF_DO_TRAN && iflags[EDYN_IF_DO_TRAN] != 0) ||
+      (n_iflags > EDYN_IF_IS_SPHERICAL && iflags[EDYN_IF_IS_SPHERICAL] != 0)) {
     int rc = edyn_init(chem_dir, nspe, nequ, 16, lvir, iflags, n_iflags, rparams, n_rparams, nullptr, out);
-    if (rc == EDYN_OK) rc = fail((Ctx*)*out, EDYN_E_ARG, "packed tubes are inviscid (do_tran 0)");
+    if (rc == EDYN_OK) rc = fail((Ctx*)*out, EDYN_E_ARG, "packed tubes are inviscid and Cartesian (do_tran 0, is_spherical 0)");
     return rc ? rc : EDYN_E_ARG;
   }
   // One context whose rows hold every tube's block: its row length is the
@@ -1091,7 +1102,7 @@ int edyn_init_tubes(const char* chem_dir, int nspe, int nequ, int ntube, const i
   CK(cudaMemset(k.d_active, 0, nt * sizeof(int)));
   CK(cudaMemcpy(k.colmap, colmap.data(), colmap.size() * sizeof(int), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(k.tube_of, tube_of.data(), tube_of.size() * sizeof(int), cudaMemcpyHostToDevice));
-  CK(stage_tiling(c->acu, c->lim, c->wflag, c->riemann, c->ns, c->n, &c->stage_tc));
+  CK(stage_tiling(c->acu, c->lim, c->wflag, c->riemann, c->ns, c->n, &c->stage_tc, c->spherical));
   c->listed = c->n >= CHEM_TWO_PASS_CELLS;
   return build_tiles(c);
 }
@@ -1235,7 +1246,7 @@ int edyn_set_stage_tile(void* ctx, int cells) {
     return fail(c, EDYN_E_ARG, "stage tile of %d cells outside [%d, %d] (0: automatic)", cells, STAGE_MIN_CELLS,
                 STAGE_MAX_CELLS);
   int tc = cells;
-  if (cells == 0) CK(stage_tiling(c->acu, c->lim, c->wflag, c->riemann, c->ns, c->n, &tc));
+  if (cells == 0) CK(stage_tiling(c->acu, c->lim, c->wflag, c->riemann, c->ns, c->n, &tc, c->spherical));
   c->stage_tc = tc;
   drop_graph(c);
   return c->pk.ntube ? build_tiles(c) : EDYN_OK;

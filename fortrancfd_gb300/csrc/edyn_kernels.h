@@ -87,6 +87,7 @@ struct StageArgs {
   TubeTab tubes;         // packed tubes (tubes.tiles null: the single tube above); cvel_out then per tube
   int skip_uniform;      // skip the faces of cells whose stencils hold one state (dF = 0 exactly)
   TranDev tran;          // do_tran: transport fluxes added to the advective ones (tran.flux null: off)
+  int spherical;         // is_spherical: spherical geometry, r = (i + 1/2) dx (Euler / TVDRK3, first order / MUSCL)
 };
 
 // Energy sources of solve_source after the chemistry (SRC/update.f90:126-147):
@@ -120,7 +121,7 @@ struct SourceArgs {
 
 int fluid_upload_tables(const ThermoTable& tb, cudaStream_t s);
 size_t stage_smem_bytes(int acu, int ns, int tc);
-cudaError_t stage_tiling(int acu, int lim, int wflag, int rm, int ns, int n, int* tc);
+cudaError_t stage_tiling(int acu, int lim, int wflag, int rm, int ns, int n, int* tc, int sph = 0);
 cudaError_t launch_stage(const StageArgs& a, int acu, int lim, int wflag, int rm, cudaStream_t s);
 cudaError_t launch_cvel(const double* qf, int n, int ld, unsigned long long* cvel, cudaStream_t s,
                         const int* colmap = nullptr, const int* tube_of = nullptr);

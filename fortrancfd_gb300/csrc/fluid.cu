@@ -280,7 +280,12 @@ __device__ void ghost_cell(const StageArgs& a, const TubeView& v, int g, double*
 // ---------------------------------------------------------------------------
 // The stage kernel.
 // ---------------------------------------------------------------------------
-template <int ACU, int LIM, int WFLAG, int RIEMANN>
+// SPH = 1: spherical geometry (is_spherical, SRC/flux.f90:272-278,
+// SRC/timeintegration.f90:58-75, 177-198): the momentum flux carries no
+// pressure, the update weighs the face fluxes by the face areas r^2 over
+// the cell volume, and the momentum takes the gradient of the faces' Roe-
+// averaged pressures separately, after the stage combination, as written.
+template <int ACU, int LIM, int WFLAG, int RIEMANN, int SPH = 0>
 __global__ void __launch_bounds__(STAGE_MAX_THREADS) k_stage(StageArgs a) {
   constexpr int LV = acu_lvir(ACU);
   extern __shared__ double sm[];
@@ -343,6 +348,8 @@ __global__ void __launch_bounds__(STAGE_MAX_THREADS) k_stage(StageArgs a) {
                                 //         then per-thread species scratch
   // s_diff[w]: window cells w and w + 1 differ in some primitive (bitwise)
   __shared__ unsigned char s_diff[STAGE_MAX_CELLS + 2 * 5];
+  // SPH: Roe-averaged pressure of each face (the reference's godunov_state)
+  __shared__ double s_pg[SPH ? STAGE_MAX_CELLS + 2 : 1];
   const bool skip_uniform = a.skip_uniform != 0;
   if (skip_uniform)
     for (int w = tid; w < Wd; w += NT) s_diff[w] = 0;
@@ -450,7 +457,12 @@ __global__ void __launch_bounds__(STAGE_MAX_THREADS) k_stage(StageArgs a) {
     const double ml = L.rho * L.u, mr = R.rho * R.u;
     // physical fluxes of the three bulk rows
     const double fl0 = ml, fr0 = mr;
-    const double fl1 = ml * L.u + L.p, fr1 = mr * R.u + R.p;
+    const double fl1 = SPH ? ml * L.u : ml * L.u + L.p, fr1 = SPH ? mr * R.u : mr * R.u + R.p;
+    if constexpr (SPH != 0) {
+      // godunov_state(iqpres) of the face, SRC/flux.f90:360-367
+      const double rt = sqrt(R.rho / L.rho);
+      if (h == 0) s_pg[f] = (L.p + rt * R.p) / (1.0 + rt);
+    }
     const double fl2 = (L.E + L.p) * L.u, fr2 = (R.E + R.p) * R.u;
     double F0, F1, F2;
     // species row k: flux = aL * YL + bL * max(YL,0) + aR * YR + bR * max(YR,0)
@@ -594,6 +606,15 @@ __global__ void __launch_bounds__(STAGE_MAX_THREADS) k_stage(StageArgs a) {
     // Euler or first TVDRK3 stage: Q - c dF; later stages h1 Q0 + h2 (Q - c dF);
     // last RK4 stage: Q0 + (k1 + 2 k2 + 2 k3 + k4) / 6
     auto update = [&](int v, double qv) {
+      if constexpr (SPH != 0) {
+        // cell centre r = (i + 1/2) dx, face areas (r -+ dx/2)^2, volume r^2 dx
+        const double rm = (i + 0.5) * tv.dx, hd = tv.dx / 2.0;
+        const double Al = (rm - hd) * (rm - hd), Ar = (rm + hd) * (rm + hd), dV = rm * rm * tv.dx;
+        const double cdF = (dt / dV) * (Ar * s_l[v * P + f + 1] - Al * s_l[v * P + f]);
+        double r = a.kind == 0 ? qv - cdF : fma(a.h1, Q0[v * ld], a.h2 * (qv - cdF));
+        if (v == 1) r = r - (dt / tv.dx) * (s_pg[f + 1] - s_pg[f]);
+        return r;
+      }
       const double dF = fz ? 0.0 : s_l[v * P + f + 1] - s_l[v * P + f];
       if (a.kind == 2) return Q0[v * ld] + (1.0 / 6.0) * (tv.acc[v * ld + i + GHOST] + -(c * dF));
       return a.kind == 0 ? qv - c * dF : fma(a.h1, Q0[v * ld], a.h2 * (qv - c * dF));
@@ -1341,14 +1362,26 @@ namespace {
 
 using StageFn = void (*)(StageArgs);
 
-template <int ACU, int LIM, int WF>
+template <int ACU, int LIM, int WF, int SPH = 0>
 StageFn stage_fn_rm(int rm) {
-  if (rm == 0) return k_stage<ACU, LIM, WF, 0>;
-  if (rm == 1) return k_stage<ACU, LIM, WF, 1>;
-  return k_stage<ACU, LIM, WF, 2>;
+  if (rm == 0) return k_stage<ACU, LIM, WF, 0, SPH>;
+  if (rm == 1) return k_stage<ACU, LIM, WF, 1, SPH>;
+  return k_stage<ACU, LIM, WF, 2, SPH>;
 }
 
-StageFn stage_fn(int acu, int lim, int wflag, int rm) {
+// spherical geometry: first order and MUSCL (the schemes of the reference's
+// spherical examples); null for the others
+StageFn stage_fn_sph(int acu, int lim, int rm) {
+  if (acu == ACU_FIRST) return stage_fn_rm<ACU_FIRST, 2, 3, 1>(rm);
+  if (acu != ACU_MUSCL) return nullptr;
+  if (lim == 1) return stage_fn_rm<ACU_MUSCL, 1, 3, 1>(rm);
+  if (lim == 3) return stage_fn_rm<ACU_MUSCL, 3, 3, 1>(rm);
+  if (lim == 4) return stage_fn_rm<ACU_MUSCL, 4, 3, 1>(rm);
+  return stage_fn_rm<ACU_MUSCL, 2, 3, 1>(rm);
+}
+
+StageFn stage_fn(int acu, int lim, int wflag, int rm, int sph = 0) {
+  if (sph) return stage_fn_sph(acu, lim, rm);
   switch (acu) {
     case ACU_FIRST: return stage_fn_rm<ACU_FIRST, 2, 3>(rm);
     case ACU_MUSCL:
@@ -1377,12 +1410,13 @@ StageFn stage_fn(int acu, int lim, int wflag, int rm) {
 // over all resident slots. 20,000 cells with WENO5 and GRI-3.0: 66-cell tiles,
 // 304 CTAs, two per SM, one wave (62-cell tiles would need 323 CTAs, and the
 // 19 of a second wave would double the launch).
-cudaError_t stage_tiling(int acu, int lim, int wflag, int rm, int ns, int n, int* tc_out) {
+cudaError_t stage_tiling(int acu, int lim, int wflag, int rm, int ns, int n, int* tc_out, int sph) {
   int dev = 0, nsm = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   if (e != cudaSuccess) return e;
-  const StageFn kern = stage_fn(acu, lim, wflag, rm);
+  const StageFn kern = stage_fn(acu, lim, wflag, rm, sph);
+  if (!kern) return cudaErrorInvalidValue;
   long best_waves = -1, best_slots = 0;
   int best_tcmax = 0;
   for (int nt = 64; nt <= STAGE_MAX_THREADS; nt += 32) {
@@ -1415,7 +1449,8 @@ cudaError_t stage_tiling(int acu, int lim, int wflag, int rm, int ns, int n, int
 }
 
 cudaError_t launch_stage(const StageArgs& a, int acu, int lim, int wflag, int rm, cudaStream_t s) {
-  const StageFn kern = stage_fn(acu, lim, wflag, rm);
+  const StageFn kern = stage_fn(acu, lim, wflag, rm, a.spherical);
+  if (!kern || (a.spherical && (a.kind == 2 || a.skip_uniform))) return cudaErrorInvalidValue;
   const size_t smem = stage_smem_bytes(acu, a.ns, a.tc);
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;

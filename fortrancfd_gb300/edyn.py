@@ -186,13 +186,14 @@ class Tube(_Ctx):
 
     def __init__(self, ncell: int, dx: float, *, chem_dir=GRI30_DIR, select_time=1, select_riemann=2, flag_acu=1,
                  flag_muscl=2, flag_weno=0, flag_lbound=0, flag_rbound=0, do_reaction=0, strict_newton=1,
-                 chem_mode=0, do_tran=0, p_out=101325.0, t_in=300.0, rho_u_in=0.0, rtol=1e-5, atol=1e-13,
+                 chem_mode=0, do_tran=0, is_spherical=0, p_out=101325.0, t_in=300.0, rho_u_in=0.0, rtol=1e-5,
+                 atol=1e-13,
                  x_in: Optional[Sequence[float]] = None, nspe: Optional[int] = None):
         names = species_names(chem_dir) if (Path(chem_dir) / "mech.edyn").exists() else None
         nspe = nspe if nspe is not None else len(names)
         lv = lvir_for(flag_acu, flag_weno)
         iflags = [select_time, select_riemann, flag_acu, flag_muscl, flag_weno, flag_lbound, flag_rbound,
-                  do_reaction, strict_newton, chem_mode, do_tran]
+                  do_reaction, strict_newton, chem_mode, do_tran, is_spherical]
         super().__init__(chem_dir, nspe, ncell, lv, iflags, [dx, p_out, t_in, rho_u_in, rtol, atol], x_in)
         self.lvir = lv
         self.dx = dx

@@ -42,7 +42,8 @@ extern "C" {
 #define EDYN_IF_STRICT_NEWTON 8   /* 1: T Newton starts at 1000 K every call (reference); 0: warm start */
 #define EDYN_IF_CHEM_MODE 9       /* 0 plain implicit integrator, 1 surrogate with fallback (edyn_set_surrogate) */
 #define EDYN_IF_DO_TRAN 10        /* 0 inviscid, 1 viscous stress, conduction and diffusion (calc_flux_tran) */
-#define EDYN_NIFLAGS 11
+#define EDYN_IF_IS_SPHERICAL 11   /* 0 Cartesian, 1 spherical (Euler / TVDRK3; first order or MUSCL) */
+#define EDYN_NIFLAGS 12
 
 /* Indices into the rparams array of edyn_init. */
 #define EDYN_RP_DX 0        /* cell size dx_comp [m] */
@@ -68,7 +69,14 @@ extern "C" {
  * the reference's viscosity_ea calls (SRC/trans.f90:137-151) and its
  * tranlib.f does not define. It is available for one tube per context, not
  * for packed tubes (edyn_init_tubes) nor edyn_solve_fluid_noalloc, and it
- * turns the uniform-region shortcuts of the stage off. */
+ * turns the uniform-region shortcuts of the stage off.
+ * is_spherical = 1 (the problem file's flag, SRC/params.f90:37) solves the
+ * spherically symmetric equations with r = (i + 1/2) dx
+ * (SRC/flux.f90:272-278, SRC/timeintegration.f90:58-75, 177-198): momentum
+ * flux without pressure, face fluxes weighed by (r -+ dx/2)^2 over r^2 dx,
+ * and the momentum's Roe-averaged face-pressure gradient applied after the
+ * stage combination as the reference writes it. With Euler or TVDRK3 and
+ * first order or MUSCL; not for packed tubes; no uniform-region shortcuts. */
 int edyn_init(const char* chem_dir, int nspe, int nequ, int ncell, int lvir, const int* iflags, int n_iflags,
               const double* rparams, int n_rparams, const double* x_in, void** ctx);
 

@@ -154,6 +154,8 @@ typedef struct or_tube {
   const or_tran* tran; /* do_tran: transport fits (NULL: inviscid) */
   or_sources src;      /* energy sources (all off when zeroed) */
   double time;         /* the time loop's clock: advanced by or_step before the step */
+  int is_spherical;    /* spherical geometry, r = (i + 1/2) dx */
+  double* pgod;        /* (n + 1): Roe-averaged face pressures (godunov_state) */
 } or_tube;
 
 or_tube* or_tube_create(const or_mech* m, int n, int lvir, const int* iflags, const double* rparams,
@@ -174,6 +176,7 @@ void or_tube_set_transport(or_tube* t, const or_tran* tr);
 void or_calc_flux_tran(or_tube* t);
 void or_tube_set_sources(or_tube* t, const or_sources* s);
 void or_tube_set_time(or_tube* t, double time);
+void or_tube_set_spherical(or_tube* t, int on);
 int or_sources_sizeof(void);
 void or_solve_fluid(or_tube* t, double dt);
 void or_solve_source(or_tube* t, double dt);

@@ -219,6 +219,7 @@ or_tube* or_tube_create(const or_mech* m, int n, int lvir, const int* iflags, co
   t->qc = (double*)calloc(tot, sizeof(double));
   t->q0 = (double*)calloc((size_t)n * t->nequ, sizeof(double));
   t->fplus = (double*)calloc((size_t)(n + 1) * t->nequ, sizeof(double));
+  t->pgod = (double*)calloc((size_t)(n + 1), sizeof(double));
   t->hrr = (double*)calloc((size_t)n, sizeof(double));
   t->hrr_dot = (double*)calloc((size_t)n, sizeof(double));
   return t;
@@ -230,6 +231,7 @@ void or_tube_destroy(or_tube* t) {
   free(t->qc);
   free(t->q0);
   free(t->fplus);
+  free(t->pgod);
   free(t->hrr);
   free(t->hrr_dot);
   free(t);
@@ -388,8 +390,13 @@ static void or_calc_flux_advection_add(or_tube* t) {
     double hl = (el + pl) / rhol, hr = (er + pr) / rhor;
     fl[0] = rhol * ul;
     fr[0] = rhor * ur;
-    fl[1] = rhol * ul * ul + pl;
-    fr[1] = rhor * ur * ur + pr;
+    if (t->is_spherical) { /* SRC/flux.f90:272-278 */
+      fl[1] = rhol * ul * ul;
+      fr[1] = rhor * ur * ur;
+    } else {
+      fl[1] = rhol * ul * ul + pl;
+      fr[1] = rhor * ur * ur + pr;
+    }
     fl[2] = (el + pl) * ul;
     fr[2] = (er + pr) * ur;
     for (int k = 0; k < ns; ++k) {
@@ -440,6 +447,11 @@ static void or_calc_flux_advection_add(or_tube* t) {
         }
       }
     }
+    /* the face's Roe-averaged pressure (godunov_state, SRC/flux.f90:360-367) */
+    {
+      double rt = sqrt(rhor / rhol);
+      t->pgod[f] = (pl + rt * pr) / (1.0 + rt);
+    }
     double* fp = t->fplus + (size_t)f * ne;
     for (int n = 0; n < ne; ++n) fp[n] = fp[n] + flux[n];
   }
@@ -484,12 +496,37 @@ static void stage_tail(or_tube* t) {
 }
 
 /* explicit_euler, SRC/timeintegration.f90:12-96 */
+/* The spherical update of cell i (SRC/timeintegration.f90:58-75, 177-198):
+ * q = h1 q0 + h2 (q - dt/dV (Ar F_i - Al F_{i-1})) (Euler: q - dt/dV (...)),
+ * then the momentum's face-pressure gradient, after the combination. */
+static void spherical_update(or_tube* t, int i, double dt, double h1, double h2, const double* q0, int euler) {
+  const int ne = t->nequ;
+  double dx = t->dx, rm = (i + 0.5) * dx;
+  double Al = (rm - (dx / 2.0)) * (rm - (dx / 2.0));
+  double Ar = (rm + (dx / 2.0)) * (rm + (dx / 2.0));
+  double dV = rm * rm * dx;
+  double* q = QC(t, i);
+  const double* fp = t->fplus + (size_t)(i + 1) * ne;
+  const double* fm = t->fplus + (size_t)i * ne;
+  for (int n = 0; n < ne; ++n) {
+    double d = (dt / dV) * (Ar * fp[n] - Al * fm[n]);
+    q[n] = euler ? q[n] - d : h1 * q0[n] + h2 * (q[n] - d);
+  }
+  q[1] = q[1] - (dt / dx) * (t->pgod[i + 1] - t->pgod[i]);
+}
+
+void or_tube_set_spherical(or_tube* t, int on) { t->is_spherical = on; }
+
 static void explicit_euler(or_tube* t, double dt) {
   const int ne = t->nequ;
   calc_fluxes(t);
   double c = dt / t->dx;
 #pragma omp parallel for schedule(static)
   for (int i = 0; i < t->n; ++i) {
+    if (t->is_spherical) {
+      spherical_update(t, i, dt, 1.0, 1.0, NULL, 1);
+      continue;
+    }
     double* q = QC(t, i);
     const double* fp = t->fplus + (size_t)(i + 1) * ne;
     const double* fm = t->fplus + (size_t)i * ne;
@@ -523,6 +560,10 @@ static void tvdrk3(or_tube* t, double dt) {
       const double* q0 = t->q0 + (size_t)i * ne;
       const double* fp = t->fplus + (size_t)(i + 1) * ne;
       const double* fm = t->fplus + (size_t)i * ne;
+      if (t->is_spherical) {
+        spherical_update(t, i, dt, h1, h2, q0, 0);
+        continue;
+      }
       for (int n = 0; n < ne; ++n) q[n] = h1 * q0[n] + h2 * (q[n] - c * (fp[n] - fm[n]));
     }
     stage_tail(t);

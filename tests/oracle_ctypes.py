@@ -99,6 +99,7 @@ class Oracle:
         L.or_tube_set_sources.argtypes = [vp, vp]
         L.or_tube_set_time.argtypes = [vp, d]
         L.or_sources_sizeof.restype = i
+        L.or_tube_set_spherical.argtypes = [vp, i]
         self.kk = 53
         self.nequ = self.kk + 3
 
@@ -269,6 +270,10 @@ class OracleTube:
 
     def set_time(self, time):
         self.o.L.or_tube_set_time(self.h, time)
+
+    def set_spherical(self, on=True):
+        """is_spherical = 1: r = (i + 1/2) dx."""
+        self.o.L.or_tube_set_spherical(self.h, 1 if on else 0)
 
     def set_transport(self, on=True):
         """do_tran = 1: calc_flux_tran joins every stage's flux."""

@@ -15,6 +15,16 @@ def pytest_configure(config):
     config.addinivalue_line("markers", "timeout(seconds): per-test time limit (pytest-timeout)")
 
 
+# GPU suites of features whose device code has not yet run on a GPU. They
+# are collected after the suites already run on hardware, so that under
+# `pytest -x` a first failure in them stops nothing that was passing before.
+FIRST_GPU_RUN = ("test_gpu_sources.py", "test_gpu_spherical.py", "test_gpu_transport.py")
+
+
+def pytest_collection_modifyitems(session, config, items):
+    items.sort(key=lambda it: Path(str(it.fspath)).name in FIRST_GPU_RUN)
+
+
 @pytest.fixture(scope="session")
 def oracle():
     from oracle_ctypes import Oracle

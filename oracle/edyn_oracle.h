@@ -156,6 +156,7 @@ typedef struct or_tube {
   double time;         /* the time loop's clock: advanced by or_step before the step */
   int is_spherical;    /* spherical geometry, r = (i + 1/2) dx */
   double* pgod;        /* (n + 1): Roe-averaged face pressures (godunov_state) */
+  int smr_left, smr_right; /* SMR: this side faces another block (ghosts by interpolation) */
 } or_tube;
 
 or_tube* or_tube_create(const or_mech* m, int n, int lvir, const int* iflags, const double* rparams,
@@ -182,6 +183,17 @@ void or_solve_fluid(or_tube* t, double dt);
 void or_solve_source(or_tube* t, double dt);
 void or_post_step(or_tube* t);
 double or_step(or_tube* t, double cfl);
+
+/* SMR blocks (SRC/block.f90:91-379, 475-569): segments of equal-dx blocks,
+ * left to right, one dt from dx_comp = rparams[0]; Euler or TVDRK3. */
+#define OR_MAXSEG 64
+typedef struct or_smr or_smr;
+or_smr* or_smr_create(const or_mech* m, int nseg, const int* ncell, const double* dx, int lvir, const int* iflags,
+                      const double* rparams, const double* x_in);
+void or_smr_destroy(or_smr* s);
+void or_smr_set_interior(or_smr* s, const double* qf, const double* qc);
+void or_smr_get_interior(const or_smr* s, double* qf, double* qc);
+double or_smr_step(or_smr* s, double cfl);
 
 /* Initial conditions (SRC/params.f90:305-580 + SRC/block.f90:394-431). */
 void or_init_cell(const or_mech* m, double T, double p, double u, const double* x_in, double* qf, double* qc);

@@ -317,18 +317,29 @@ static void rbound_outlet(or_tube* t) {
 /* update_boundary, SRC/boundary.f90:12-67: ghost Qc from the boundary rule,
  * then QcToqf on the ghost cells of both domain ends. */
 void or_update_boundary(or_tube* t) {
-  if (t->flag_lbound == 0) lbound_wall(t);
-  else if (t->flag_lbound == 1) lbound_inlet(t);
-  for (int l = 1; l <= t->lvir; ++l) or_qc_to_qf(t->m, QC(t, -l), QF(t, -l));
-  if (t->flag_rbound == 0) rbound_wall(t);
-  else if (t->flag_rbound == 1) rbound_outlet(t);
-  for (int l = 1; l <= t->lvir; ++l) or_qc_to_qf(t->m, QC(t, t->n - 1 + l), QF(t, t->n - 1 + l));
+  /* an SMR block's side that faces another block takes its ghosts from
+   * interpolation_block, not from a boundary rule */
+  if (!t->smr_left) {
+    if (t->flag_lbound == 0) lbound_wall(t);
+    else if (t->flag_lbound == 1) lbound_inlet(t);
+    for (int l = 1; l <= t->lvir; ++l) or_qc_to_qf(t->m, QC(t, -l), QF(t, -l));
+  }
+  if (!t->smr_right) {
+    if (t->flag_rbound == 0) rbound_wall(t);
+    else if (t->flag_rbound == 1) rbound_outlet(t);
+    for (int l = 1; l <= t->lvir; ++l) or_qc_to_qf(t->m, QC(t, t->n - 1 + l), QF(t, t->n - 1 + l));
+  }
 }
 
 void or_ghost_qf(or_tube* t) { or_update_boundary(t); }
 
+/* The largest signal speed max(|u - a|, |u|, |u + a|) of calc_dt. */
+static double or_cvel(or_tube* t);
+
 /* calc_dt, SRC/update.f90:13-59 (the all-reduce is a no-op on one rank). */
-double or_calc_dt(or_tube* t, double cfl) {
+double or_calc_dt(or_tube* t, double cfl) { return (cfl * t->dx) / or_cvel(t); }
+
+static double or_cvel(or_tube* t) {
   const or_mech* m = t->m;
   double cvel = 0.0;
 #pragma omp parallel for reduction(max : cvel) schedule(static)
@@ -342,7 +353,7 @@ double or_calc_dt(or_tube* t, double cfl) {
     double aupc = fmax(fmax(fabs(q[1] - a), fabs(q[1])), fabs(q[1] + a));
     if (aupc > cvel) cvel = aupc;
   }
-  return (cfl * t->dx) / cvel;
+  return cvel;
 }
 
 /* calc_flux_advection, SRC/flux.f90:130-373 (Cartesian). Face f lies
@@ -517,7 +528,7 @@ static void spherical_update(or_tube* t, int i, double dt, double h1, double h2,
 
 void or_tube_set_spherical(or_tube* t, int on) { t->is_spherical = on; }
 
-static void explicit_euler(or_tube* t, double dt) {
+static void euler_update(or_tube* t, double dt) {
   const int ne = t->nequ;
   calc_fluxes(t);
   double c = dt / t->dx;
@@ -532,14 +543,19 @@ static void explicit_euler(or_tube* t, double dt) {
     const double* fm = t->fplus + (size_t)i * ne;
     for (int n = 0; n < ne; ++n) q[n] = q[n] - c * (fp[n] - fm[n]);
   }
+}
+
+static void explicit_euler(or_tube* t, double dt) {
+  euler_update(t, dt);
   stage_tail(t);
 }
 
-/* TVDRK3, SRC/timeintegration.f90:99-219 */
-static void tvdrk3(or_tube* t, double dt) {
+/* One TVDRK3 stage's fluxes and update, without the stage tail
+ * (SRC/timeintegration.f90:131-198); stage 1 also saves Q0. */
+static void tvdrk3_update(or_tube* t, int stage, double dt) {
   const int ne = t->nequ;
-  memcpy(t->q0, QC(t, 0), sizeof(double) * (size_t)t->n * ne);
-  for (int stage = 1; stage <= 3; ++stage) {
+  if (stage == 1) memcpy(t->q0, QC(t, 0), sizeof(double) * (size_t)t->n * ne);
+  {
     calc_fluxes(t);
     double h1, h2;
     if (stage == 1) {
@@ -566,6 +582,13 @@ static void tvdrk3(or_tube* t, double dt) {
       }
       for (int n = 0; n < ne; ++n) q[n] = h1 * q0[n] + h2 * (q[n] - c * (fp[n] - fm[n]));
     }
+  }
+}
+
+/* TVDRK3, SRC/timeintegration.f90:99-219 */
+static void tvdrk3(or_tube* t, double dt) {
+  for (int stage = 1; stage <= 3; ++stage) {
+    tvdrk3_update(t, stage, dt);
     stage_tail(t);
   }
 }
@@ -756,5 +779,152 @@ double or_step(or_tube* t, double cfl) {
   or_solve_fluid(t, dt);
   or_solve_source(t, dt);
   or_post_step(t);
+  return dt;
+}
+
+/* ---- SMR blocks: SRC/block.f90:475-569 (interpolation_block) and the
+ * stage tails of SRC/timeintegration.f90 and SRC/main.f90:149-163 ----
+ * Segments are runs of equal-dx blocks (whose ghost exchange is a plain copy,
+ * the same as one contiguous array); consecutive segments differ in dx. */
+
+struct or_smr {
+  int nseg;
+  or_tube* seg[OR_MAXSEG];
+  double dx_comp;
+};
+
+/* minmod slope of interpolation_block: 0.5 (sign(1, m) + sign(1, p)) min(|m|, |p|) */
+static double smr_slope(double m, double p) {
+  return 0.5 * (copysign(1.0, m) + copysign(1.0, p)) * fmin(fabs(m), fabs(p));
+}
+
+static void smr_interface(or_tube* a, or_tube* b) {
+  const int ne = a->nequ, lv = a->lvir;
+  const int ea = a->n - 1; /* iend of the left block; ista of the right is 0 */
+  if (a->dx == b->dx) {
+    for (int l = 1; l <= lv; ++l) {
+      memcpy(QC(b, -l), QC(a, ea - l + 1), sizeof(double) * ne);
+      memcpy(QC(a, ea + l), QC(b, l - 1), sizeof(double) * ne);
+    }
+  } else if (a->dx > b->dx) {
+    /* left coarse, right fine: restriction into the left's ghosts, then
+     * prolongation of the left (ghosts included) into the right's */
+    for (int l = 1; l <= lv; ++l)
+      for (int v = 0; v < ne; ++v)
+        QC(a, ea + l)[v] = (QC(b, 2 * (l - 1))[v] + QC(b, 2 * (l - 1) + 1)[v]) / 2.0;
+    for (int l = 1; l <= lv; ++l) {
+      int ic = -((l - 1) / 2);
+      for (int v = 0; v < ne; ++v) {
+        double m = QC(a, ea + ic)[v] - QC(a, ea + ic - 1)[v];
+        double p = QC(a, ea + ic + 1)[v] - QC(a, ea + ic)[v];
+        double d = smr_slope(m, p);
+        QC(b, -l)[v] = (l % 2 == 1) ? QC(a, ea + ic)[v] + 0.25 * d : QC(a, ea + ic)[v] - 0.25 * d;
+      }
+    }
+  } else {
+    /* left fine, right coarse */
+    for (int l = 1; l <= lv; ++l)
+      for (int v = 0; v < ne; ++v)
+        QC(b, -l)[v] = (QC(a, ea - 2 * (l - 1))[v] + QC(a, ea - 2 * (l - 1) - 1)[v]) / 2.0;
+    for (int l = 1; l <= lv; ++l) {
+      int ic = (l - 1) / 2;
+      for (int v = 0; v < ne; ++v) {
+        double m = QC(b, ic)[v] - QC(b, ic - 1)[v];
+        double p = QC(b, ic + 1)[v] - QC(b, ic)[v];
+        double d = smr_slope(m, p);
+        QC(a, ea + l)[v] = (l % 2 == 1) ? QC(b, ic)[v] - 0.25 * d : QC(b, ic)[v] + 0.25 * d;
+      }
+    }
+  }
+}
+
+/* update_boundary, interpolation_block, update_boundary, QcToqf of every
+ * cell with its ghosts */
+static void smr_tail(or_smr* s) {
+  for (int g = 0; g < s->nseg; ++g) or_update_boundary(s->seg[g]);
+  for (int g = 0; g + 1 < s->nseg; ++g) smr_interface(s->seg[g], s->seg[g + 1]);
+  for (int g = 0; g < s->nseg; ++g) or_update_boundary(s->seg[g]);
+  for (int g = 0; g < s->nseg; ++g) all_qc_to_qf(s->seg[g]);
+}
+
+or_smr* or_smr_create(const or_mech* m, int nseg, const int* ncell, const double* dx, int lvir, const int* iflags,
+                      const double* rparams, const double* x_in) {
+  if (nseg < 1 || nseg > OR_MAXSEG) return NULL;
+  or_smr* s = (or_smr*)calloc(1, sizeof(or_smr));
+  s->nseg = nseg;
+  s->dx_comp = rparams[0];
+  for (int g = 0; g < nseg; ++g) {
+    double rp[6];
+    for (int j = 0; j < 6; ++j) rp[j] = rparams[j];
+    rp[0] = dx[g];
+    s->seg[g] = or_tube_create(m, ncell[g], lvir, iflags, rp, x_in);
+    s->seg[g]->smr_left = g > 0;
+    s->seg[g]->smr_right = g + 1 < nseg;
+  }
+  return s;
+}
+
+void or_smr_destroy(or_smr* s) {
+  if (!s) return;
+  for (int g = 0; g < s->nseg; ++g) or_tube_destroy(s->seg[g]);
+  free(s);
+}
+
+void or_smr_set_interior(or_smr* s, const double* qf, const double* qc) {
+  size_t off = 0;
+  for (int g = 0; g < s->nseg; ++g) {
+    or_tube* t = s->seg[g];
+    memcpy(QF(t, 0), qf + off, sizeof(double) * (size_t)t->n * t->nequ);
+    memcpy(QC(t, 0), qc + off, sizeof(double) * (size_t)t->n * t->nequ);
+    off += (size_t)t->n * t->nequ;
+  }
+  /* SRC/main.f90:95-113: boundary, interpolation, boundary, then QcToqf of
+   * every block's ghost cells (the interior keeps its qf) */
+  for (int g = 0; g < s->nseg; ++g) or_update_boundary(s->seg[g]);
+  for (int g = 0; g + 1 < s->nseg; ++g) smr_interface(s->seg[g], s->seg[g + 1]);
+  for (int g = 0; g < s->nseg; ++g) {
+    or_tube* t = s->seg[g];
+    or_update_boundary(t);
+    for (int l = 1; l <= t->lvir; ++l) {
+      or_qc_to_qf(t->m, QC(t, -l), QF(t, -l));
+      or_qc_to_qf(t->m, QC(t, t->n - 1 + l), QF(t, t->n - 1 + l));
+    }
+  }
+}
+
+void or_smr_get_interior(const or_smr* s, double* qf, double* qc) {
+  size_t off = 0;
+  for (int g = 0; g < s->nseg; ++g) {
+    const or_tube* t = s->seg[g];
+    or_tube_get_interior(t, qf ? qf + off : NULL, qc ? qc + off : NULL);
+    off += (size_t)t->n * t->nequ;
+  }
+}
+
+/* One pass of the time loop over all blocks with one dt = cfl dx_comp /
+ * max(|u| + a) (SRC/update.f90:13-59): Euler or TVDRK3 stages with the
+ * blocks' ghost exchange after each, the source step, the post-step tail. */
+double or_smr_step(or_smr* s, double cfl) {
+  double cvel = 0.0;
+  for (int g = 0; g < s->nseg; ++g) {
+    double c = or_cvel(s->seg[g]);
+    if (c > cvel) cvel = c;
+  }
+  double dt = (cfl * s->dx_comp) / cvel;
+  or_tube* t0 = s->seg[0];
+  if (t0->select_time == 0) {
+    for (int g = 0; g < s->nseg; ++g) euler_update(s->seg[g], dt);
+    smr_tail(s);
+  } else {
+    for (int stage = 1; stage <= 3; ++stage) {
+      for (int g = 0; g < s->nseg; ++g) tvdrk3_update(s->seg[g], stage, dt);
+      smr_tail(s);
+    }
+  }
+  for (int g = 0; g < s->nseg; ++g) {
+    s->seg[g]->time = s->seg[g]->time + dt;
+    or_solve_source(s->seg[g], dt);
+  }
+  smr_tail(s);
   return dt;
 }

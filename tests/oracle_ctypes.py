@@ -100,6 +100,13 @@ class Oracle:
         L.or_tube_set_time.argtypes = [vp, d]
         L.or_sources_sizeof.restype = i
         L.or_tube_set_spherical.argtypes = [vp, i]
+        L.or_smr_create.restype = vp
+        L.or_smr_create.argtypes = [vp, i, ctypes.POINTER(i), _D, i, ctypes.POINTER(i), _D, _D]
+        L.or_smr_destroy.argtypes = [vp]
+        L.or_smr_set_interior.argtypes = [vp, _D, _D]
+        L.or_smr_get_interior.argtypes = [vp, _D, _D]
+        L.or_smr_step.restype = d
+        L.or_smr_step.argtypes = [vp, d]
         self.kk = 53
         self.nequ = self.kk + 3
 
@@ -199,6 +206,17 @@ class Oracle:
         h = self.L.or_tube_create(self.mech, n, lvir, fl, _p(rp), _p(xi))
         return OracleTube(self, h, n, (rp, xi))
 
+    def smr(self, ncells, dxs, lvir, flags, rparams, x_in=None):
+        """SMR blocks: segments of ncells[s] cells of size dxs[s], left to
+        right, one dt from dx_comp = rparams[0]."""
+        nc = (ctypes.c_int * len(ncells))(*ncells)
+        dx = np.ascontiguousarray(dxs, dtype=float)
+        fl = (ctypes.c_int * 8)(*flags[:8])
+        rp = np.ascontiguousarray(rparams, dtype=float)
+        xi = np.zeros(self.kk) if x_in is None else np.ascontiguousarray(x_in, dtype=float)
+        h = self.L.or_smr_create(self.mech, len(ncells), nc, _p(dx), lvir, fl, _p(rp), _p(xi))
+        return OracleSMR(self, h, int(sum(ncells)), (nc, dx, rp, xi))
+
     def reactor(self, rho_si, dt, yiT, rtol, atol):
         y = np.ascontiguousarray(yiT, dtype=float).copy()
         rc = self.L.or_reactor(self.mech, rho_si, dt, _p(y), rtol, atol, ctypes.c_void_p(
@@ -294,5 +312,28 @@ class OracleTube:
     def __del__(self):
         try:
             self.o.L.or_tube_destroy(self.h)
+        except Exception:
+            pass
+
+
+class OracleSMR:
+    def __init__(self, o: Oracle, h, n, keep):
+        self.o, self.h, self.n, self._keep = o, h, n, keep
+
+    def set_interior(self, qf, qc):
+        self.o.L.or_smr_set_interior(self.h, _p(np.ascontiguousarray(qf)), _p(np.ascontiguousarray(qc)))
+
+    def get(self):
+        qf = np.zeros((self.n, self.o.nequ))
+        qc = np.zeros((self.n, self.o.nequ))
+        self.o.L.or_smr_get_interior(self.h, _p(qf), _p(qc))
+        return qf, qc
+
+    def step(self, cfl):
+        return self.o.L.or_smr_step(self.h, cfl)
+
+    def __del__(self):
+        try:
+            self.o.L.or_smr_destroy(self.h)
         except Exception:
             pass

@@ -1,0 +1,99 @@
+"""SMR blocks in the oracle (CPU), restated from SRC/block.f90:475-569
+(interpolation_block) and the stage tails around it: segments of equal-dx
+blocks exchange ghosts by copy, so equal segments must reproduce one tube
+bit for bit; at a change of level the ghosts are restricted (mean of two fine
+cells) and prolonged (coarse cell +- 1/4 of its minmod slope). A uniform
+state stays bit for bit uniform across levels, and a Sod problem on a
+fine / coarse / fine grid stays close to the uniform fine grid's.
+"""
+import numpy as np
+import pytest
+
+from fortrancfd_gb300 import configs, species_names
+from oracle_ctypes import _D
+
+RP = [1e-3, configs.ATM, 300.0, 0.0, 1e-5, 1e-13]
+
+
+def sod_state(oracle, xm, xs):
+    """The Sod state with qf = QcToqf(Qc) in every cell, so that a block's
+    ghost (QcToqf of a copied Qc column) equals its neighbour's qf."""
+    nm = species_names()
+    x = configs.mole_vector(nm, {"CH4": 0.0950570342, "O2": 0.1901140684, "N2": 0.7148288973})
+    left = xm <= xs
+    n = len(xm)
+    _, qc = oracle.init_cells(np.where(left, 375.0, 300.0), np.where(left, 10 * configs.ATM, configs.ATM),
+                              np.zeros(n), np.tile(x, (n, 1)))
+    qf = np.zeros_like(qc)
+    for i in range(n):
+        oracle.L.or_qc_to_qf(oracle.mech, qc[i].ctypes.data_as(_D), qf[i].ctypes.data_as(_D))
+    return qf, qc
+
+
+@pytest.mark.parametrize("flags,lvir", [([1, 2, 1, 2, 0, 0, 0, 0], 2), ([1, 2, 2, 2, 3, 0, 1, 0], 3),
+                                        ([0, 1, 1, 4, 0, 0, 0, 0], 2)])
+def test_equal_segments_reproduce_one_tube(oracle, flags, lvir):
+    n, dx = 120, 1e-3
+    xm = (np.arange(n) + 0.5) * dx
+    qf, qc = sod_state(oracle, xm, 0.5 * n * dx)
+    t = oracle.tube(n, lvir, flags, RP)
+    t.set_interior(qf, qc)
+    s = oracle.smr([40, 50, 30], [dx, dx, dx], lvir, flags, RP)
+    s.set_interior(qf, qc)
+    for _ in range(30):
+        assert t.step(0.5) == s.step(0.5)
+    np.testing.assert_array_equal(s.get()[1], t.get()[1])
+    np.testing.assert_array_equal(s.get()[0], t.get()[0])
+
+
+def test_uniform_state_stays_uniform_across_levels(oracle):
+    nm = species_names()
+    air = configs.mole_vector(nm, {"O2": 0.21, "N2": 0.79})
+    ncells, dxs = [32, 16, 32], [1e-3, 2e-3, 1e-3]
+    n = sum(ncells)
+    _, qc = oracle.init_cells(np.full(n, 500.0), np.full(n, configs.ATM), np.zeros(n), np.tile(air, (n, 1)))
+    qf = np.zeros_like(qc)
+    for i in range(n):
+        oracle.L.or_qc_to_qf(oracle.mech, qc[i].ctypes.data_as(_D), qf[i].ctypes.data_as(_D))
+    s = oracle.smr(ncells, dxs, 2, [1, 2, 1, 2, 0, 0, 0, 0], RP)
+    s.set_interior(qf, qc)
+    for _ in range(10):
+        s.step(0.5)
+    np.testing.assert_array_equal(s.get()[1], qc)
+
+
+def test_refined_sod_close_to_uniform_grid(oracle):
+    """Fine (1 mm) / coarse (2 mm) / fine grid against the uniform 1 mm grid:
+    the shock and contact cross the coarse block; p and rho within a few
+    percent of the jump in L1, and the total mass within 1e-3 (the interface
+    fluxes are evaluated once per block, so SMR is not exactly conservative)."""
+    dx = 1e-3
+    nf = 240
+    xm_f = (np.arange(nf) + 0.5) * dx
+    flags = [1, 2, 1, 2, 0, 0, 0, 0]
+    qf, qc = sod_state(oracle, xm_f, 0.3)
+    t = oracle.tube(nf, 2, flags, RP)
+    t.set_interior(qf, qc)
+    ncells, dxs = [100, 40, 60], [dx, 2 * dx, dx]
+    xm_s = np.concatenate([(np.arange(100) + 0.5) * dx, 0.1 + (np.arange(40) + 0.5) * 2 * dx,
+                           0.18 + (np.arange(60) + 0.5) * dx])
+    qf_s, qc_s = sod_state(oracle, xm_s, 0.3)
+    s = oracle.smr(ncells, dxs, 2, flags, RP)
+    s.set_interior(qf_s, qc_s)
+    for _ in range(120):
+        dt = t.step(0.5)
+        assert s.step(0.5) == pytest.approx(dt, rel=0.05)
+    qf_t, _ = t.get()
+    qf_r, qc_r = s.get()
+    W = configs.molecular_weights()
+
+    def p(q):
+        return q[:, 0] * 8314.51 * q[:, 2] * (q[:, 3:] / W).sum(axis=1)
+
+    ref_p = np.interp(xm_s, xm_f, p(qf_t))
+    ref_r = np.interp(xm_s, xm_f, qf_t[:, 0])
+    w = np.concatenate([np.full(100, dx), np.full(40, 2 * dx), np.full(60, dx)])
+    assert (w * np.abs(p(qf_r) - ref_p)).sum() / w.sum() < 0.03 * 9 * configs.ATM
+    assert (w * np.abs(qf_r[:, 0] - ref_r)).sum() / w.sum() < 0.03 * 7 * qf_t[:, 0].min()
+    mass0 = (w * qc_s[:, 0]).sum()
+    assert abs((w * qc_r[:, 0]).sum() - mass0) < 1e-3 * mass0

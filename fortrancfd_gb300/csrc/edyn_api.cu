@@ -85,6 +85,10 @@ struct Packed {
   unsigned long long* d_cvel = nullptr;
   int* colmap = nullptr;   // column of each packed cell
   int* tube_of = nullptr;  // tube of each packed cell
+  // SMR blocks (edyn_init_blocks): the tubes are the segments of one domain
+  bool smr = false;
+  double dx_comp = 0.0;    // the dx of calc_dt's dt = cfl dx_comp / max(|u| + a)
+  double* d_snap = nullptr;
 };
 
 // A contiguous run of cells in the rows: the whole tube, or one packed tube.
@@ -253,7 +257,8 @@ StageArgs base_args(Ctx* c) {
   }
   if (c->pk.ntube) {
     const Packed& k = c->pk;
-    a.tubes = TubeTab{k.d_tiles, k.d_n, k.d_off, k.d_dx, k.d_p_out, k.d_dt, k.d_active, k.d_time, k.ntiles, k.colmap, k.tube_of};
+    a.tubes = TubeTab{k.d_tiles, k.d_n, k.d_off, k.d_dx, k.d_p_out, k.d_dt, k.d_active, k.d_time, k.ntiles, k.colmap,
+                      k.tube_of, k.smr ? k.d_snap : nullptr, k.ntube};
   }
   return a;
 }
@@ -1027,8 +1032,11 @@ int build_tiles(Ctx* c) {
 }
 }  // namespace
 
-int edyn_init_tubes(const char* chem_dir, int nspe, int nequ, int ntube, const int* ncell, int lvir,
-                    const int* iflags, int n_iflags, const double* rparams, int n_rparams, void** out) {
+namespace {
+// edyn_init_tubes, and edyn_init_blocks (smr): segments of one domain, the
+// inflow boundary allowed on the first (x_in), one dt for all.
+int init_packed(const char* chem_dir, int nspe, int nequ, int ntube, const int* ncell, int lvir, const int* iflags,
+                int n_iflags, const double* rparams, int n_rparams, const double* x_in, bool smr, void** out) {
   if (!out) return EDYN_E_ARG;
   *out = nullptr;
   if (ntube < 1 || !ncell || !rparams || n_rparams < 2 || !iflags || n_iflags < 8) return EDYN_E_ARG;
@@ -1039,7 +1047,7 @@ int edyn_init_tubes(const char* chem_dir, int nspe, int nequ, int ntube, const i
     cols += ncell[t] + 2 * GHOST;
   }
   if (cols > (1ll << 31) - 1) return EDYN_E_ARG;
-  if (n_iflags > EDYN_IF_FLAG_LBOUND && iflags[EDYN_IF_FLAG_LBOUND] != 0) {
+  if (!smr && n_iflags > EDYN_IF_FLAG_LBOUND && iflags[EDYN_IF_FLAG_LBOUND] != 0) {
     // the inflow boundary needs per-tube inlet data
     int rc = edyn_init(chem_dir, nspe, nequ, 16, lvir, iflags, n_iflags, rparams, n_rparams, nullptr, out);
     if (rc == EDYN_OK) rc = fail((Ctx*)*out, EDYN_E_ARG, "packed tubes take wall or outlet boundaries only");
@@ -1059,11 +1067,12 @@ int edyn_init_tubes(const char* chem_dir, int nspe, int nequ, int ntube, const i
   // One context whose rows hold every tube's block: its row length is the
   // sum of the blocks, its cell count the sum of the cells.
   int rc = edyn_init(chem_dir, nspe, nequ, (int)(cols - 2 * GHOST), lvir, iflags, n_iflags, rparams, n_rparams,
-                     nullptr, out);
+                     smr ? x_in : nullptr, out);
   if (rc) return rc;
   Ctx* c = (Ctx*)*out;
   Packed& k = c->pk;
   k.ntube = ntube;
+  k.smr = smr;
   long long off = 0, first = 0;
   std::vector<int> colmap((size_t)ntot), tube_of((size_t)ntot);
   for (int t = 0; t < ntube; ++t) {
@@ -1104,7 +1113,48 @@ int edyn_init_tubes(const char* chem_dir, int nspe, int nequ, int ntube, const i
   CK(cudaMemcpy(k.tube_of, tube_of.data(), tube_of.size() * sizeof(int), cudaMemcpyHostToDevice));
   CK(stage_tiling(c->acu, c->lim, c->wflag, c->riemann, c->ns, c->n, &c->stage_tc, c->spherical));
   c->listed = c->n >= CHEM_TWO_PASS_CELLS;
+  if (smr) {
+    k.dx_comp = rparams[EDYN_RP_DX];
+    const size_t snap = (size_t)(ntube - 1) * 2 * c->ne * 2 * c->lvir;
+    if (snap) CK(cudaMalloc(&k.d_snap, snap * sizeof(double)));
+  }
   return build_tiles(c);
+}
+}  // namespace
+
+int edyn_init_tubes(const char* chem_dir, int nspe, int nequ, int ntube, const int* ncell, int lvir,
+                    const int* iflags, int n_iflags, const double* rparams, int n_rparams, void** out) {
+  return init_packed(chem_dir, nspe, nequ, ntube, ncell, lvir, iflags, n_iflags, rparams, n_rparams, nullptr, false,
+                     out);
+}
+
+int edyn_init_blocks(const char* chem_dir, int nspe, int nequ, int nseg, const int* ncell, const double* dx, int lvir,
+                     const int* iflags, int n_iflags, const double* rparams, int n_rparams, const double* x_in,
+                     void** out) {
+  if (!out) return EDYN_E_ARG;
+  *out = nullptr;
+  if (nseg < 1 || !ncell || !dx || !rparams || n_rparams < 1 || !iflags || n_iflags < 8) return EDYN_E_ARG;
+  auto refuse = [&](const char* why) {
+    int rc = edyn_init(chem_dir, nspe, nequ, 16, lvir, iflags, n_iflags, rparams, n_rparams, nullptr, out);
+    if (rc == EDYN_OK) rc = fail((Ctx*)*out, EDYN_E_ARG, "edyn_init_blocks: %s", why);
+    return rc ? rc : EDYN_E_ARG;
+  };
+  if (iflags[EDYN_IF_SELECT_TIME] == 2) return refuse("Euler or TVDRK3 stages only");
+  for (int g = 0; g < nseg; ++g) {
+    if (!(dx[g] > 0.0)) return refuse("cell sizes must be positive");
+    if (g && !(dx[g] == dx[g - 1] || dx[g] == 2.0 * dx[g - 1] || 2.0 * dx[g] == dx[g - 1]))
+      return refuse("neighbouring segments' cell sizes must be equal or differ by a factor of two");
+  }
+  // one rparams row per segment: the context's row with the segment's cell size
+  std::vector<double> rp((size_t)nseg * n_rparams);
+  for (int g = 0; g < nseg; ++g) {
+    for (int j = 0; j < n_rparams; ++j) rp[(size_t)g * n_rparams + j] = rparams[j];
+    rp[(size_t)g * n_rparams + EDYN_RP_DX] = dx[g];
+  }
+  int rc = init_packed(chem_dir, nspe, nequ, nseg, ncell, lvir, iflags, n_iflags, rp.data(), n_rparams, x_in, true,
+                       out);
+  if (rc == EDYN_OK) ((Ctx*)*out)->pk.dx_comp = rparams[EDYN_RP_DX];
+  return rc;
 }
 
 int edyn_tube_times(void* ctx, double* time, double* dt) {
@@ -1465,10 +1515,13 @@ int edyn_advance(void* ctx, double cfl, double tend, long long max_steps, double
     int rc = 0;
     for (int s = 0; s < per_graph && !rc; ++s) {
       const Packed& k = c->pk;
-      cudaError_t e = k.ntube ? launch_step_begin_tubes(k.ntube, k.d_time, tend, c->d_nsteps, c->d_max_steps, cfl,
-                                                        k.d_dx, k.d_cvel, k.d_active, k.d_dt, c->d_active, c->stream)
-                              : launch_step_begin(c->d_time, tend, c->d_nsteps, c->d_max_steps, cfl, c->dx,
-                                                  c->d_cvel, c->d_active, c->d_dt, c->stream);
+      cudaError_t e = !k.ntube ? launch_step_begin(c->d_time, tend, c->d_nsteps, c->d_max_steps, cfl, c->dx,
+                                                   c->d_cvel, c->d_active, c->d_dt, c->stream)
+                      : k.smr ? launch_step_begin_blocks(k.ntube, k.d_time, tend, c->d_nsteps, c->d_max_steps, cfl,
+                                                         k.dx_comp, k.d_cvel, k.d_active, k.d_dt, c->d_active,
+                                                         c->stream)
+                              : launch_step_begin_tubes(k.ntube, k.d_time, tend, c->d_nsteps, c->d_max_steps, cfl,
+                                                        k.d_dx, k.d_cvel, k.d_active, k.d_dt, c->d_active, c->stream);
       if (e != cudaSuccess) rc = fail(c, EDYN_E_CUDA, "step_begin: %s", cudaGetErrorString(e));
       if (!rc) rc = fluid_step(c, 0.0, true, !c->do_reaction);
       if (!rc) rc = source_step(c, 0.0, true);
@@ -1899,7 +1952,7 @@ int edyn_finalize(void* ctx) {
   {
     Packed& k = c->pk;
     void* bufs[] = {k.d_tiles, k.d_n, k.d_off, k.d_dx, k.d_p_out, k.d_dt, k.d_time, k.d_active, k.d_cvel, k.colmap,
-                    k.tube_of};
+                    k.tube_of, k.d_snap};
     for (void* b : bufs) cudaFree(b);
   }
   {

@@ -40,6 +40,14 @@ struct TubeTab {
   int ntiles;              // stage CTAs of all tubes
   const int* colmap;       // column of each cell (its tube's block offset + its index)
   const int* tube_of;      // tube of each cell
+  // SMR blocks: the tubes are the segments of one domain, left to right;
+  // the ghosts facing another segment come from interpolation_block
+  // (SRC/block.f90:475-569) on the segments' end columns, copied here
+  // before each stage: per interface j, side 0 (segment j's last 2 lvir
+  // cells) and side 1 (segment j+1's first 2 lvir cells), [side][row][cell].
+  // Null: independent tubes.
+  double* smr_snap;
+  int ntube;
 };
 
 // Transport of calc_flux_tran (SRC/flux.f90:18-127) when do_tran = 1: the
@@ -128,6 +136,9 @@ cudaError_t launch_cvel(const double* qf, int n, int ld, unsigned long long* cve
 cudaError_t launch_step_begin_tubes(int ntube, const double* time, double tend, const long long* nsteps,
                                     const long long* max_steps, double cfl, const double* dx, unsigned long long* cvel,
                                     int* active, double* dt, int* step_active, cudaStream_t s);
+cudaError_t launch_step_begin_blocks(int ntube, const double* time, double tend, const long long* nsteps,
+                                     const long long* max_steps, double cfl, double dx_comp, unsigned long long* cvel,
+                                     int* active, double* dt, int* step_active, cudaStream_t s);
 cudaError_t launch_species_present(const double* qc, int ld, int n, int ns, int* flags, cudaStream_t s);
 cudaError_t launch_step_begin(const double* time, double tend, const long long* nsteps, const long long* max_steps,
                               double cfl, double dx, unsigned long long* cvel, int* step_active, double* dt_dev,

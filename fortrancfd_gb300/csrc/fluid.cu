@@ -196,7 +196,67 @@ struct TubeView {
   double *qf_out, *qc, *q0, *acc;
   double dx, p_out;
   unsigned long long* cvel;  // signal-speed maximum of this tube (or null)
+  int tube = 0;              // index among packed tubes
 };
+
+// minmod slope of interpolation_block: 0.5 (sign(1, m) + sign(1, p)) min(|m|, |p|)
+__device__ __forceinline__ double smr_slope(double m, double p) {
+  return 0.5 * (copysign(1.0, m) + copysign(1.0, p)) * fmin(fabs(m), fabs(p));
+}
+
+// Conserved column of the ghost l (1..lvir) that segment t takes from its
+// neighbour across interface j (SRC/block.f90:488-567), from the snapshot:
+// a plain copy between equal cell sizes; on the coarse side the mean of two
+// fine cells; on the fine side the coarse cell -+ 1/4 of its minmod slope,
+// the coarse side's first ghost (a mean of two fine cells) serving as its
+// neighbour across the interface.
+__device__ __noinline__ void smr_ghost_qc(const StageArgs& a, int t, int g, int n, double& q0, double& q1, double& q2,
+                                          double* ys, int st) {
+  const TubeTab& T = a.tubes;
+  const int S = 2 * a.lvir;
+  const int ne = a.ns + 3;
+  const bool left = g < 0;  // a left ghost of segment t: interface t-1
+  const int j = left ? t - 1 : t;
+  const int l = left ? -g : g - n + 1;
+  const double dxl = T.dx[j], dxr = T.dx[j + 1];
+  const double* base = T.smr_snap + (size_t)j * 2 * ne * S;
+  for (int v = 0; v < ne; ++v) {
+    const double* sl = base + (size_t)v * S;         // segment j: cell iend + idx at S - 1 + idx (idx <= 0)
+    const double* sr = base + (size_t)(ne + v) * S;  // segment j+1: cell idx at idx (idx >= 0)
+    auto lx = [&](int idx) {  // segment j's cells and, past its end, its restricted ghosts
+      return idx <= 0 ? sl[S - 1 + idx] : (sr[2 * (idx - 1)] + sr[2 * (idx - 1) + 1]) / 2.0;
+    };
+    auto rx = [&](int idx) {  // segment j+1's cells and, before its start, its restricted ghosts
+      return idx >= 0 ? sr[idx] : (sl[S - 1 - 2 * (-idx - 1)] + sl[S - 1 - 2 * (-idx - 1) - 1]) / 2.0;
+    };
+    double q;
+    if (dxl == dxr) {
+      q = left ? lx(-(l - 1)) : rx(l - 1);
+    } else if (dxl > dxr) {  // coarse | fine
+      if (!left) {
+        q = lx(l);
+      } else {
+        const int ic = -((l - 1) / 2);
+        const double c = lx(ic);
+        const double d = smr_slope(c - lx(ic - 1), lx(ic + 1) - c);
+        q = (l % 2 == 1) ? c + 0.25 * d : c - 0.25 * d;
+      }
+    } else {  // fine | coarse
+      if (left) {
+        q = rx(-l);
+      } else {
+        const int ic = (l - 1) / 2;
+        const double c = rx(ic);
+        const double d = smr_slope(c - rx(ic - 1), rx(ic + 1) - c);
+        q = (l % 2 == 1) ? c - 0.25 * d : c + 0.25 * d;
+      }
+    }
+    if (v == 0) q0 = q;
+    else if (v == 1) q1 = q;
+    else if (v == 2) q2 = q;
+    else ys[(v - 3) * st] = q;
+  }
+}
 
 // ---------------------------------------------------------------------------
 // Boundary ghost cells (SRC/boundary.f90). ghost_qc computes the conserved
@@ -211,6 +271,10 @@ __device__ __forceinline__ void ghost_qc(const StageArgs& a, const TubeView& v, 
   const int ns = tb.ns;
   const int ld = a.ld;
   int iters;
+  if (a.tubes.smr_snap && (g < 0 ? v.tube > 0 : v.tube < a.tubes.ntube - 1)) {
+    smr_ghost_qc(a, v.tube, g, v.n, q0, q1, q2, ys, st);
+    return;
+  }
   if (g < 0) {
     const int l = -g;  // 1..lvir
     const int src = l - 1;
@@ -325,6 +389,7 @@ __global__ void __launch_bounds__(STAGE_MAX_THREADS) k_stage(StageArgs a) {
     tv.dx = a.tubes.dx[tube];
     tv.p_out = a.tubes.p_out[tube];
     tv.cvel = a.cvel_out ? a.cvel_out + tube : nullptr;
+    tv.tube = tube;
     dt = a.tubes.dt[tube];
   }
   int c0 = tile * TC;
@@ -1118,6 +1183,64 @@ cudaError_t launch_energy_sources(const SourceArgs& a, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+// SMR: the end columns of every segment next to an interface, before a
+// stage updates them in place (one thread per copied value).
+__global__ void k_smr_snapshot(TubeTab T, const double* qc, int ld, int ne, int lvir) {
+  const int S = 2 * lvir;
+  const long long tot = (long long)(T.ntube - 1) * 2 * ne * S;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < tot; e += (long long)gridDim.x * blockDim.x) {
+    const int col = (int)(e % S);
+    const long long r = e / S;
+    const int v = (int)(r % ne);
+    const long long js = r / ne;
+    const int side = (int)(js % 2), j = (int)(js / 2);
+    const int t = j + side;
+    const int cell = side == 0 ? T.n[t] - S + col : col;
+    T.smr_snap[e] = qc[(size_t)v * ld + T.off[t] + GHOST + cell];
+  }
+}
+
+cudaError_t launch_smr_snapshot(const StageArgs& a, cudaStream_t s) {
+  const long long tot = (long long)(a.tubes.ntube - 1) * 2 * (a.ns + 3) * 2 * a.lvir;
+  if (tot <= 0) return cudaSuccess;
+  const int blocks = (int)std::min<long long>((tot + 255) / 256, 1024);
+  k_smr_snapshot<<<blocks, 256, 0, s>>>(a.tubes, a.qc, a.ld, a.ns + 3, a.lvir);
+  return cudaGetLastError();
+}
+
+// SMR: one dt for every segment, cfl dx_comp / max(|u| + a) over all of
+// them (calc_dt, SRC/update.f90:13-59); every segment steps while the
+// (common) clock is below tend.
+__global__ void k_step_begin_blocks(int ntube, const double* time, double tend, const long long* nsteps,
+                                    const long long* max_steps, double cfl, double dx_comp, unsigned long long* cvel,
+                                    int* active, double* dt, int* step_active) {
+  __shared__ unsigned long long s_max;
+  if (threadIdx.x == 0) s_max = 0ull;
+  __syncthreads();
+  unsigned long long m = 0ull;
+  for (int t = threadIdx.x; t < ntube; t += blockDim.x) m = max(m, cvel[t]);
+  atomicMax(&s_max, m);
+  __syncthreads();
+  const int on = (*nsteps < *max_steps && time[0] < tend) ? 1 : 0;
+  const double d = (cfl * dx_comp) / __longlong_as_double((long long)s_max);
+  for (int t = threadIdx.x; t < ntube; t += blockDim.x) {
+    active[t] = on;
+    if (on) {
+      dt[t] = d;
+      cvel[t] = 0ull;
+    }
+  }
+  if (threadIdx.x == 0) *step_active = on;
+}
+
+cudaError_t launch_step_begin_blocks(int ntube, const double* time, double tend, const long long* nsteps,
+                                     const long long* max_steps, double cfl, double dx_comp, unsigned long long* cvel,
+                                     int* active, double* dt, int* step_active, cudaStream_t s) {
+  k_step_begin_blocks<<<1, 256, 0, s>>>(ntube, time, tend, nsteps, max_steps, cfl, dx_comp, cvel, active, dt,
+                                        step_active);
+  return cudaGetLastError();
+}
+
 __global__ void k_step_begin_tubes(int ntube, const double* time, double tend, const long long* nsteps,
                                    const long long* max_steps, double cfl, const double* dx, unsigned long long* cvel,
                                    int* active, double* dt, int* step_active) {
@@ -1454,6 +1577,11 @@ cudaError_t launch_stage(const StageArgs& a, int acu, int lim, int wflag, int rm
   const size_t smem = stage_smem_bytes(acu, a.ns, a.tc);
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
+  // SMR: the segments' end columns, before the stage updates them in place
+  if (a.tubes.smr_snap) {
+    e = launch_smr_snapshot(a, s);
+    if (e != cudaSuccess) return e;
+  }
   // transport fluxes of the stage input, before the stage updates it in place
   if (a.tran.flux) {
     if (a.tubes.tiles || a.skip_uniform) return cudaErrorInvalidValue;

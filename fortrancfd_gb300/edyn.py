@@ -71,6 +71,7 @@ def lib() -> ctypes.CDLL:
     L.edyn_set_chem_precheck.argtypes = [vp, i]
     L.edyn_set_uniform_skip.argtypes = [vp, i]
     L.edyn_init_tubes.argtypes = [cp, i, i, i, ip, i, ip, i, dp, i, ctypes.POINTER(vp)]
+    L.edyn_init_blocks.argtypes = [cp, i, i, i, ip, dp, i, ip, i, dp, i, dp, ctypes.POINTER(vp)]
     L.edyn_tube_times.argtypes = [vp, dp, dp]
     L.edyn_autotune.argtypes = [vp, cp, ip, dp]
     L.edyn_chem_rhs_tube.argtypes = [vp, i, vp, vp, vp]
@@ -422,6 +423,42 @@ class Tubes(Tube):
             out.append(a[i:i + n])
             i += n
         return out
+
+
+class Blocks(Tubes):
+    """One domain of SMR blocks (edyn_init_blocks): segments of equal-dx
+    blocks, left to right, neighbouring cell sizes equal or a factor of two
+    apart, ghosts between segments by the reference's interpolation_block,
+    one dt = cfl dx_comp / max(|u| + a) for all (dx_comp defaults to the
+    first segment's cell size). Cells are numbered left to right."""
+
+    def __init__(self, ncells: Sequence[int], dxs: Sequence[float], *, dx_comp: Optional[float] = None,
+                 chem_dir=GRI30_DIR, select_time=1, select_riemann=2, flag_acu=1, flag_muscl=2, flag_weno=0,
+                 flag_lbound=0, flag_rbound=0, do_reaction=0, strict_newton=1, p_out=101325.0, t_in=300.0,
+                 rho_u_in=0.0, rtol=1e-5, atol=1e-13, x_in: Optional[Sequence[float]] = None):
+        L = lib()
+        names = species_names(chem_dir)
+        nspe = len(names)
+        lv = lvir_for(flag_acu, flag_weno)
+        iflags = [select_time, select_riemann, flag_acu, flag_muscl, flag_weno, flag_lbound, flag_rbound, do_reaction,
+                  strict_newton, 0]
+        nt = len(ncells)
+        rp = np.ascontiguousarray([dx_comp if dx_comp is not None else dxs[0], p_out, t_in, rho_u_in, rtol, atol],
+                                  dtype=np.float64)
+        dx = np.ascontiguousarray(dxs, dtype=np.float64)
+        nc = (ctypes.c_int * nt)(*[int(v) for v in ncells])
+        fl = (ctypes.c_int * len(iflags))(*iflags)
+        xi = None if x_in is None else np.ascontiguousarray(x_in, dtype=np.float64)
+        self._h = ctypes.c_void_p()
+        self.nspe, self.nequ, self.ncell = nspe, nspe + 3, int(sum(ncells))
+        self.ntube, self.ncells = nt, [int(v) for v in ncells]
+        self.lvir, self.dx = lv, float(dxs[0])
+        rc = L.edyn_init_blocks(str(chem_dir).encode(), nspe, nspe + 3, nt, nc, _ptr(dx), lv, fl, len(iflags),
+                                _ptr(rp), 6, _ptr(xi), ctypes.byref(self._h))
+        if rc:
+            msg = self.last_error()
+            self.close()
+            raise EdynError(rc, msg)
 
 
 def _set_chem_max_steps(self, max_steps: int = 0) -> None:

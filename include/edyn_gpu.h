@@ -98,6 +98,24 @@ int edyn_init(const char* chem_dir, int nspe, int nequ, int ncell, int lvir, con
 int edyn_init_tubes(const char* chem_dir, int nspe, int nequ, int ntube, const int* ncell, int lvir,
                     const int* iflags, int n_iflags, const double* rparams, int n_rparams, void** ctx);
 
+/* Creates a context for one domain of SMR blocks (static mesh refinement,
+ * SRC/block.f90:91-379): nseg segments, left to right, each a run of
+ * ncell[s] (>= 16) cells of size dx[s] (a run of the reference's equal-dx
+ * blocks, whose ghost exchange is a copy), neighbouring sizes equal or a
+ * factor of two apart. The ghosts facing another segment come from
+ * interpolation_block (SRC/block.f90:475-569): the mean of two fine cells on
+ * the coarse side, the coarse cell -+ 1/4 of its minmod slope on the fine
+ * side; each segment computes its own boundary faces from its own ghosts, as
+ * each reference block does. One dt = cfl dx_comp / max(|u| + a) for all,
+ * dx_comp = rparams[EDYN_RP_DX] (calc_dt, SRC/update.f90:13-59). rparams is
+ * one row as for edyn_init; the first segment may take the inflow boundary
+ * (x_in), the last the outflow. Euler or TVDRK3; no transport, spherical
+ * geometry, energy sources or surrogate. Cells are numbered left to right;
+ * the context steps through edyn_step / edyn_advance, as packed tubes do. */
+int edyn_init_blocks(const char* chem_dir, int nspe, int nequ, int nseg, const int* ncell, const double* dx, int lvir,
+                     const int* iflags, int n_iflags, const double* rparams, int n_rparams, const double* x_in,
+                     void** ctx);
+
 /* Per-tube simulated times and last time steps (ntube values each, either
  * pointer may be NULL); one value for a single-tube context. */
 int edyn_tube_times(void* ctx, double* time, double* dt);

@@ -892,6 +892,9 @@ void or_smr_set_interior(or_smr* s, const double* qf, const double* qc) {
   }
 }
 
+/* Segment g's conserved columns with its ghosts ((n + 2 lvir) x nequ). */
+void or_smr_segment_all(const or_smr* s, int g, double* qc) { or_tube_get_all(s->seg[g], NULL, qc); }
+
 void or_smr_get_interior(const or_smr* s, double* qf, double* qc) {
   size_t off = 0;
   for (int g = 0; g < s->nseg; ++g) {

@@ -107,6 +107,7 @@ class Oracle:
         L.or_smr_get_interior.argtypes = [vp, _D, _D]
         L.or_smr_step.restype = d
         L.or_smr_step.argtypes = [vp, d]
+        L.or_smr_segment_all.argtypes = [vp, i, _D]
         self.kk = 53
         self.nequ = self.kk + 3
 
@@ -331,6 +332,12 @@ class OracleSMR:
 
     def step(self, cfl):
         return self.o.L.or_smr_step(self.h, cfl)
+
+    def segment_all(self, g, n, lvir):
+        """Segment g's conserved columns with its ghosts."""
+        qc = np.zeros((n + 2 * lvir, self.o.nequ))
+        self.o.L.or_smr_segment_all(self.h, g, _p(qc))
+        return qc
 
     def __del__(self):
         try:

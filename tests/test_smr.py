@@ -97,3 +97,86 @@ def test_refined_sod_close_to_uniform_grid(oracle):
     assert (w * np.abs(qf_r[:, 0] - ref_r)).sum() / w.sum() < 0.03 * 7 * qf_t[:, 0].min()
     mass0 = (w * qc_s[:, 0]).sum()
     assert abs((w * qc_r[:, 0]).sum() - mass0) < 1e-3 * mass0
+
+
+def device_ghosts(seg_qc, ncells, dxs, lvir):
+    """The GPU's interface ghosts, emulated: the pre-stage snapshot's layout
+    ([interface][side][row][cell], 2 lvir cells a side) and the accessors of
+    smr_ghost_qc (fortrancfd_gb300/csrc/fluid.cu), for every segment's
+    ghosts that face another segment. Returns {(segment, g): column}."""
+    S = 2 * lvir
+    ne = seg_qc[0].shape[1]
+    out = {}
+    for t in range(len(ncells)):
+        for g in list(range(-lvir, 0)) + list(range(ncells[t], ncells[t] + lvir)):
+            left = g < 0
+            if (left and t == 0) or (not left and t == len(ncells) - 1):
+                continue
+            j = t - 1 if left else t
+            l = -g if left else g - ncells[t] + 1
+            snap = np.zeros((2, ne, S))
+            snap[0] = seg_qc[j][ncells[j] - S:ncells[j]].T
+            snap[1] = seg_qc[j + 1][0:S].T
+            col = np.zeros(ne)
+            for v in range(ne):
+                sl, sr = snap[0, v], snap[1, v]
+
+                def lx(idx):
+                    return sl[S - 1 + idx] if idx <= 0 else (sr[2 * (idx - 1)] + sr[2 * (idx - 1) + 1]) / 2.0
+
+                def rx(idx):
+                    return sr[idx] if idx >= 0 else (sl[S - 1 - 2 * (-idx - 1)] + sl[S - 1 - 2 * (-idx - 1) - 1]) / 2.0
+
+                def slope(m, p):
+                    return 0.5 * (np.copysign(1.0, m) + np.copysign(1.0, p)) * min(abs(m), abs(p))
+
+                if dxs[j] == dxs[j + 1]:
+                    q = lx(-(l - 1)) if left else rx(l - 1)
+                elif dxs[j] > dxs[j + 1]:
+                    if not left:
+                        q = lx(l)
+                    else:
+                        ic = -((l - 1) // 2)
+                        c = lx(ic)
+                        d = slope(c - lx(ic - 1), lx(ic + 1) - c)
+                        q = c + 0.25 * d if l % 2 == 1 else c - 0.25 * d
+                else:
+                    if left:
+                        q = rx(-l)
+                    else:
+                        ic = (l - 1) // 2
+                        c = rx(ic)
+                        d = slope(c - rx(ic - 1), rx(ic + 1) - c)
+                        q = c - 0.25 * d if l % 2 == 1 else c + 0.25 * d
+                col[v] = q
+            out[t, g] = col
+    return out
+
+
+@pytest.mark.parametrize("lvir,dxs", [(1, [1e-3, 2e-3, 1e-3]), (2, [2e-3, 1e-3, 2e-3]), (3, [1e-3, 2e-3, 4e-3]),
+                                      (4, [4e-3, 2e-3, 2e-3]), (2, [1e-3, 1e-3, 2e-3])])
+def test_interface_ghosts_device_form_matches_oracle(oracle, lvir, dxs):
+    """The device's ghost construction (emulated above from its snapshot
+    layout and accessors) gives the oracle's interpolation_block ghosts bit
+    for bit, for every level relation and ghost depth, on a state with
+    non-monotone conserved rows (so that every minmod branch is taken)."""
+    ncells = [24, 20, 28]
+    n = sum(ncells)
+    rng = np.random.default_rng(lvir)
+    nm = species_names()
+    air = configs.mole_vector(nm, {"O2": 0.21, "N2": 0.79})
+    T = 300.0 + 400.0 * rng.random(n)
+    _, qc = oracle.init_cells(T, configs.ATM * (1 + 0.5 * rng.random(n)), 50.0 * rng.standard_normal(n),
+                              np.tile(air, (n, 1)))
+    qf = np.zeros_like(qc)
+    for i in range(n):
+        oracle.L.or_qc_to_qf(oracle.mech, qc[i].ctypes.data_as(_D), qf[i].ctypes.data_as(_D))
+    flags = [1, 2, 1, 2, 0, 0, 0, 0] if lvir <= 2 else [1, 2, 2, 2, 3 if lvir == 3 else 4, 0, 0, 0]
+    s = oracle.smr(ncells, dxs, lvir, flags, RP)
+    s.set_interior(qf, qc)
+    segs = np.split(qc, np.cumsum(ncells)[:-1])
+    dev = device_ghosts(segs, ncells, dxs, lvir)
+    assert len(dev) == 4 * lvir
+    for (t, g), col in dev.items():
+        full = s.segment_all(t, ncells[t], lvir)
+        np.testing.assert_array_equal(full[g + lvir], col, err_msg=f"segment {t} ghost {g}")

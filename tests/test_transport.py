@@ -208,3 +208,36 @@ def test_oracle_tube_diffusion_conserves_and_spreads(oracle):
         ot2.step(0.5)
     qf2, _ = ot2.get()
     assert np.abs(qf2[:, 3 + o2] - qf0[:, 3 + o2]).max() < 0.5 * np.abs(qf1[:, 3 + o2] - qf0[:, 3 + o2]).max()
+
+
+def test_face_flux_device_form_matches_oracle(oracle):
+    """k_tran_flux's arithmetic (face averages of the per-cell rows, CKHMS
+    from the premixed enthalpy coefficients a1, a2/2, .., a5/5, a6 at the face
+    temperature, R_SI h / W) on the oracle's per-cell rows reproduces the
+    oracle's face flux to rounding."""
+    nm = species_names()
+    _, tmid, a, _ = configs._thermo_tables()
+    W = configs.molecular_weights()
+    mix1 = configs.mole_vector(nm, {"CH4": 0.2, "O2": 0.3, "H2O": 0.1, "N2": 0.4})
+    mix2 = configs.equilibrium_tp(configs.ch4_air_mixture(nm, 1.0), 2100.0, configs.ATM)
+    _, qc = oracle.init_cells(np.array([700.0, 1900.0]), np.full(2, configs.ATM), np.array([4.0, -3.0]),
+                              np.array([mix1, mix2]))
+    dx = 2e-5
+    L = oracle.tran_cell(qc[0])
+    R = oracle.tran_cell(qc[1])
+    rho_a, u_a, T_a = 0.5 * (L[0] + R[0]), 0.5 * (L[1] + R[1]), 0.5 * (L[2] + R[2])
+    mu_a, k_a = 0.5 * (L[4] + R[4]), 0.5 * (L[5] + R[5])
+    tau = -(2.0 / 3.0 * mu_a * (2.0 * ((R[1] - L[1]) / dx)))
+    r = (T_a > tmid).astype(int)
+    c = a[np.arange(53), r]
+    h = ((((c[:, 4] / 5 * T_a + c[:, 3] / 4) * T_a + c[:, 2] / 3) * T_a + c[:, 1] / 2) * T_a + c[:, 0]) * T_a + c[:, 5]
+    hs = 8314.51 * h / W
+    dif_a = 0.5 * (L[6] + R[6])
+    dy = (R[3] - L[3]) / dx
+    g = np.zeros(56)
+    g[1] = tau
+    g[2] = tau * u_a + rho_a * np.sum(-hs * dif_a * dy) - k_a * ((R[2] - L[2]) / dx)
+    g[3:] = -(rho_a * dif_a * dy)
+    go = oracle.face_flux_tran(qc[0], qc[1], dx)
+    scale = np.abs(go).max()
+    np.testing.assert_allclose(g, go, rtol=1e-12, atol=1e-12 * scale)

@@ -241,3 +241,62 @@ def test_face_flux_device_form_matches_oracle(oracle):
     go = oracle.face_flux_tran(qc[0], qc[1], dx)
     scale = np.abs(go).max()
     np.testing.assert_allclose(g, go, rtol=1e-12, atol=1e-12 * scale)
+
+
+def _fits():
+    lines = TRAN_TXT.read_text().split("\n")
+
+    def block(name, n, width):
+        i = lines.index(name)
+        return np.array([[float(v) for v in ln.split()[width:]] for ln in lines[i + 1:i + 1 + n]])
+
+    ceta, clam = block("COFETA", 53, 1), block("COFLAM", 53, 1)
+    cofd = block("COFD", 53 * 53, 2).reshape(53, 53, 4)
+    return ceta, clam, cofd
+
+
+def test_property_kernel_form_matches_oracle(oracle):
+    """k_tran_props' arithmetic in NumPy: Wilke's sum expanded into the three
+    products with the constant matrices g, q g, q^2 g, and the mixture-
+    averaged diffusion from the pair matrix with sum_{j!=k} XX_j W_j taken
+    apart from the floored X (the kernel adds a prefix to a suffix). It
+    matches the oracle's MCAVIS / MCACON / MCADIF (at the oracle's own T) to
+    1e-13 (1e-12 for D') from fresh mixture to products."""
+    nm = species_names()
+    ceta, clam, cofd = _fits()
+    t = read_tran()
+    wt = t["W"]
+    W = configs.molecular_weights()
+    g = 1.0 / np.sqrt(1.0 + wt[:, None] / wt[None, :])
+    q = np.sqrt(np.sqrt(wt[None, :] / wt[:, None]))
+    wa, wb, wc = g, q * g, q * q * g
+    fresh = configs.ch4_air_mixture(nm, 1.0)
+    hot = configs.equilibrium_tp(fresh, 2400.0, configs.ATM)
+    w = np.linspace(0.0, 1.0, 12)
+    X = (1 - w)[:, None] * fresh[None, :] + w[:, None] * hot[None, :]
+    _, qc = oracle.init_cells(300.0 + 2100.0 * w, np.full(12, configs.ATM), np.zeros(12), X)
+    for c in qc:
+        rho, u, T, y, mu_o, kap_o, dif_o = oracle.tran_cell(c)
+        sumyow = (y / W).sum()
+        x = y / W / sumyow
+        p_cgs = 10.0 * 8314.51 * rho * T * sumyow / y.sum()
+        L = np.log(T)
+
+        def poly(cf):
+            return ((cf[..., 3] * L + cf[..., 2]) * L + cf[..., 1]) * L + cf[..., 0]
+
+        eta, lam = np.exp(poly(ceta)), np.exp(poly(clam))
+        kap = 0.5 * ((x * lam).sum() + 1.0 / (x / lam).sum()) * 1e-5
+        A, B, C = wa @ x, wb @ (x / np.sqrt(eta)), wc @ (x / eta)
+        mu = (x * eta / (A + 2.0 * np.sqrt(eta) * B + eta * C)).sum() * np.sqrt(8.0) * 0.1
+        xx = np.maximum(x, 1e-50)
+        inv = np.exp(-poly(cofd))
+        np.fill_diagonal(inv, 0.0)
+        S = inv @ xx
+        tot = xx * wt
+        sumxw = tot.sum() - tot
+        d = sumxw / ((wt * x).sum() * S) * 1013250.0 / p_cgs * 1e-4
+        dif = np.where(y == 1.0, 0.0, (1.0 - x) / (1.0 - y) * d)
+        assert mu == pytest.approx(mu_o, rel=1e-13)
+        assert kap == pytest.approx(kap_o, rel=1e-13)
+        np.testing.assert_allclose(dif, dif_o, rtol=1e-12)

@@ -141,6 +141,7 @@ struct Ctx {
   double* d_tran = nullptr;
   double* d_tp = nullptr;
   double* d_tflux = nullptr;
+  int* d_col_tube = nullptr;   // packed tubes with transport: the tube of each column
   TranDev trd{};
   double* staging = nullptr;
   size_t staging_bytes = 0;
@@ -1058,10 +1059,9 @@ int init_packed(const char* chem_dir, int nspe, int nequ, int ntube, const int* 
     if (rc == EDYN_OK) rc = fail((Ctx*)*out, EDYN_E_ARG, "packed tubes take the plain chemistry (chem_mode 0)");
     return rc ? rc : EDYN_E_ARG;
   }
-  if ((n_iflags > EDYN_IF_DO_TRAN && iflags[EDYN_IF_DO_TRAN] != 0) ||
-      (n_iflags > EDYN_IF_IS_SPHERICAL && iflags[EDYN_IF_IS_SPHERICAL] != 0)) {
+  if (n_iflags > EDYN_IF_IS_SPHERICAL && iflags[EDYN_IF_IS_SPHERICAL] != 0) {
     int rc = edyn_init(chem_dir, nspe, nequ, 16, lvir, iflags, n_iflags, rparams, n_rparams, nullptr, out);
-    if (rc == EDYN_OK) rc = fail((Ctx*)*out, EDYN_E_ARG, "packed tubes are inviscid and Cartesian (do_tran 0, is_spherical 0)");
+    if (rc == EDYN_OK) rc = fail((Ctx*)*out, EDYN_E_ARG, "packed tubes are Cartesian (is_spherical 0)");
     return rc ? rc : EDYN_E_ARG;
   }
   // One context whose rows hold every tube's block: its row length is the
@@ -1113,6 +1113,17 @@ int init_packed(const char* chem_dir, int nspe, int nequ, int ntube, const int* 
   CK(cudaMemcpy(k.tube_of, tube_of.data(), tube_of.size() * sizeof(int), cudaMemcpyHostToDevice));
   CK(stage_tiling(c->acu, c->lim, c->wflag, c->riemann, c->ns, c->n, &c->stage_tc, c->spherical));
   c->listed = c->n >= CHEM_TWO_PASS_CELLS;
+  if (c->do_tran) {
+    // the transport kernels run over every column: each column's tube
+    std::vector<int> col_tube((size_t)c->ld, 0);
+    for (int t = 0; t < ntube; ++t)
+      for (long long j = 0; j < k.n[t] + 2 * GHOST; ++j) col_tube[(size_t)(k.off[t] + j)] = t;
+    int* d = nullptr;
+    CK(cudaMalloc(&d, col_tube.size() * sizeof(int)));
+    CK(cudaMemcpy(d, col_tube.data(), col_tube.size() * sizeof(int), cudaMemcpyHostToDevice));
+    c->d_col_tube = d;
+    c->trd.col_tube = d;
+  }
   if (smr) {
     k.dx_comp = rparams[EDYN_RP_DX];
     const size_t snap = (size_t)(ntube - 1) * 2 * c->ne * 2 * c->lvir;
@@ -1703,7 +1714,14 @@ int edyn_transport_properties(void* ctx, double* mu, double* kappa, double* dif)
   CK(cudaMemcpyAsync(h.data(), c->d_tp, h.size() * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   CK(cudaStreamSynchronize(c->stream));
   for (int i = 0; i < c->n; ++i) {
-    const size_t col = (size_t)i + GHOST;
+    // packed tubes: cell i of the numbering (tube after tube) in its tube's block
+    size_t col = (size_t)i + GHOST;
+    if (c->pk.ntube) {
+      int t = 0;
+      long long first = i;
+      while (first >= c->pk.n[t]) first -= c->pk.n[t++];
+      col = (size_t)(c->pk.off[t] + first + GHOST);
+    }
     if (mu) mu[i] = h[3 * ld + col];
     if (kappa) kappa[i] = h[4 * ld + col];
     if (dif)
@@ -1994,6 +2012,7 @@ int edyn_finalize(void* ctx) {
   cudaFree(c->d_tran);
   cudaFree(c->d_tp);
   cudaFree(c->d_tflux);
+  cudaFree(c->d_col_tube);
   if (c->own) cudaStreamDestroy(c->own);
   delete c;
   return EDYN_OK;

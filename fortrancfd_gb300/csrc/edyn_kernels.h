@@ -66,6 +66,7 @@ struct TranDev {
   double patmos;      // dyn/cm^2
   double* tp;         // cell rows, cells -1..n at column c + GHOST: rho, u, T, mu, kappa, Y_k (ns), D'_k (ns)
   double* flux;       // [ne][ld]: transport flux of face j (cells j-1, j) at column j + GHOST
+  const int* col_tube;  // packed tubes: the tube of every column (the columns are each tube's block)
 };
 constexpr int TRAN_ROWS_FIXED = 5;  // rho, u, T, mu, kappa before the species rows of TranDev::tp
 

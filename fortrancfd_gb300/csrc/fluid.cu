@@ -197,6 +197,7 @@ struct TubeView {
   double dx, p_out;
   unsigned long long* cvel;  // signal-speed maximum of this tube (or null)
   int tube = 0;              // index among packed tubes
+  long long off = 0;         // column offset of the tube's block among packed tubes
 };
 
 // minmod slope of interpolation_block: 0.5 (sign(1, m) + sign(1, p)) min(|m|, |p|)
@@ -618,9 +619,11 @@ __global__ void __launch_bounds__(STAGE_MAX_THREADS) k_stage(StageArgs a) {
   //     advection): F = G + F_adv, row by row with coalesced G loads
   if (a.tran.flux) {
     const size_t gld = (size_t)a.ld;
+    // the tube's block (packed tubes), read here rather than kept live
+    const double* G = a.tran.flux + (a.tubes.tiles ? a.tubes.off[tube] : 0ll) + c0 + GHOST;
     for (int idx = tid; idx < ne * P; idx += NT) {
       const int v = idx / P, fp = idx - v * P;
-      if (need_face(fp)) s_l[idx] = a.tran.flux[v * gld + c0 + fp + GHOST] + s_l[idx];
+      if (need_face(fp)) s_l[idx] = G[v * gld + fp] + s_l[idx];
     }
     __syncthreads();
   }
@@ -903,19 +906,34 @@ constexpr int TRAN_FLUX_THREADS = 128;
 
 __global__ void __launch_bounds__(TRAN_PROPS_THREADS) k_tran_props(StageArgs a) {
   if (a.step_active && *a.step_active == 0) return;
-  const int c = (int)(blockIdx.x * blockDim.x + threadIdx.x) - 1;
-  if (c > a.n) return;
+  const int gid = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+  // the cell: c of the one tube, or of the packed tube whose block holds column gid
+  TubeView tv{a.n, a.qf_in, a.qf_out, a.qc, a.q0, a.acc, a.dx, a.p_out, nullptr};
+  int c = gid - 1;
+  if (a.tubes.tiles) {
+    if (gid >= a.ld) return;
+    const int tt = a.tran.col_tube[gid];
+    const long long off = a.tubes.off[tt];
+    tv.n = a.tubes.n[tt];
+    tv.qf_in = a.qf_in + off;
+    tv.qc = a.qc + off;
+    tv.dx = a.tubes.dx[tt];
+    tv.p_out = a.tubes.p_out[tt];
+    tv.tube = tt;
+    tv.off = off;
+    c = (int)(gid - off - GHOST);
+  }
+  if (c < -1 || c > tv.n) return;
   const ThermoTable& tb = c_thermo;
   const TranDev& t = a.tran;
   const int ns = a.ns;
   const size_t ld = (size_t)a.ld;
   double y[EDYN_NS_MAX], x[EDYN_NS_MAX], eta[EDYN_NS_MAX], v1[EDYN_NS_MAX], v2[EDYN_NS_MAX];
   double q0, q1, q2;
-  if (c < 0 || c == a.n) {
-    const TubeView tv{a.n, a.qf_in, a.qf_out, a.qc, a.q0, a.acc, a.dx, a.p_out, nullptr};
-    ghost_qc(a, tv, c < 0 ? -1 : a.n, q0, q1, q2, y, 1);
+  if (c < 0 || c == tv.n) {
+    ghost_qc(a, tv, c < 0 ? -1 : tv.n, q0, q1, q2, y, 1);
   } else {
-    const double* Q = a.qc + c + GHOST;
+    const double* Q = tv.qc + c + GHOST;
     q0 = Q[0];
     q1 = Q[ld];
     q2 = Q[2 * ld];
@@ -1002,7 +1020,7 @@ __global__ void __launch_bounds__(TRAN_PROPS_THREADS) k_tran_props(StageArgs a) 
     suf = fma(xx[k], t.W[k], suf);
     wtm = fma(t.W[k], x[k], wtm);
   }
-  double* out = t.tp + c + GHOST;
+  double* out = t.tp + tv.off + c + GHOST;
   out[0] = rho;
   out[ld] = u;
   out[2 * ld] = T;
@@ -1021,22 +1039,34 @@ __global__ void __launch_bounds__(TRAN_PROPS_THREADS) k_tran_props(StageArgs a) 
 
 __global__ void __launch_bounds__(TRAN_FLUX_THREADS) k_tran_flux(StageArgs a) {
   if (a.step_active && *a.step_active == 0) return;
-  const int j = (int)(blockIdx.x * blockDim.x + threadIdx.x);
-  if (j > a.n) return;
+  const int gid = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+  // the face: j of the one tube, or of the packed tube whose block holds column gid
+  int j = gid, n = a.n;
+  long long off = 0;
+  double dx = a.dx;
+  if (a.tubes.tiles) {
+    if (gid >= a.ld) return;
+    const int tt = a.tran.col_tube[gid];
+    off = a.tubes.off[tt];
+    n = a.tubes.n[tt];
+    dx = a.tubes.dx[tt];
+    j = (int)(gid - off - GHOST);
+    if (j < 0) return;
+  }
+  if (j > n) return;
   const ThermoTable& tb = c_thermo;
   const TranDev& t = a.tran;
   const int ns = a.ns;
   const size_t ld = (size_t)a.ld;
-  const double dx = a.dx;
-  const double* L = t.tp + (j - 1) + GHOST;  // cell j-1
-  const double* R = L + 1;                   // cell j
+  const double* L = t.tp + off + (j - 1) + GHOST;  // cell j-1
+  const double* R = L + 1;                         // cell j
   const double rho_ave = 0.5 * (L[0] + R[0]);
   const double u_ave = 0.5 * (L[ld] + R[ld]);
   const double T_ave = 0.5 * (L[2 * ld] + R[2 * ld]);
   const double mu_ave = 0.5 * (L[3 * ld] + R[3 * ld]);
   const double kap_ave = 0.5 * (L[4 * ld] + R[4 * ld]);
   const double tau = -(2.0 / 3.0 * mu_ave * (2.0 * ((R[ld] - L[ld]) / dx)));
-  double* G = t.flux + j + GHOST;
+  double* G = t.flux + off + j + GHOST;
   double hsum = 0.0;
   for (int k = 0; k < ns; ++k) {
     // CKHMS at the face temperature, J/kg: R T (a1 + a2 T/2 + ... + a6/T) / W
@@ -1058,10 +1088,12 @@ __global__ void __launch_bounds__(TRAN_FLUX_THREADS) k_tran_flux(StageArgs a) {
 }
 
 cudaError_t launch_tran(const StageArgs& a, cudaStream_t s) {
-  k_tran_props<<<(a.n + 2 + TRAN_PROPS_THREADS - 1) / TRAN_PROPS_THREADS, TRAN_PROPS_THREADS, 0, s>>>(a);
+  // one thread per cell (-1..n) and per face (0..n); packed tubes: per column
+  const int np = a.tubes.tiles ? a.ld : a.n + 2, nf = a.tubes.tiles ? a.ld : a.n + 1;
+  k_tran_props<<<(np + TRAN_PROPS_THREADS - 1) / TRAN_PROPS_THREADS, TRAN_PROPS_THREADS, 0, s>>>(a);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  k_tran_flux<<<(a.n + 1 + TRAN_FLUX_THREADS - 1) / TRAN_FLUX_THREADS, TRAN_FLUX_THREADS, 0, s>>>(a);
+  k_tran_flux<<<(nf + TRAN_FLUX_THREADS - 1) / TRAN_FLUX_THREADS, TRAN_FLUX_THREADS, 0, s>>>(a);
   return cudaGetLastError();
 }
 
@@ -1584,7 +1616,7 @@ cudaError_t launch_stage(const StageArgs& a, int acu, int lim, int wflag, int rm
   }
   // transport fluxes of the stage input, before the stage updates it in place
   if (a.tran.flux) {
-    if (a.tubes.tiles || a.skip_uniform) return cudaErrorInvalidValue;
+    if (a.skip_uniform || (a.tubes.tiles && !a.tran.col_tube)) return cudaErrorInvalidValue;
     e = launch_tran(a, s);
     if (e != cudaSuccess) return e;
   }

@@ -434,14 +434,14 @@ class Blocks(Tubes):
 
     def __init__(self, ncells: Sequence[int], dxs: Sequence[float], *, dx_comp: Optional[float] = None,
                  chem_dir=GRI30_DIR, select_time=1, select_riemann=2, flag_acu=1, flag_muscl=2, flag_weno=0,
-                 flag_lbound=0, flag_rbound=0, do_reaction=0, strict_newton=1, p_out=101325.0, t_in=300.0,
-                 rho_u_in=0.0, rtol=1e-5, atol=1e-13, x_in: Optional[Sequence[float]] = None):
+                 flag_lbound=0, flag_rbound=0, do_reaction=0, strict_newton=1, do_tran=0, p_out=101325.0,
+                 t_in=300.0, rho_u_in=0.0, rtol=1e-5, atol=1e-13, x_in: Optional[Sequence[float]] = None):
         L = lib()
         names = species_names(chem_dir)
         nspe = len(names)
         lv = lvir_for(flag_acu, flag_weno)
         iflags = [select_time, select_riemann, flag_acu, flag_muscl, flag_weno, flag_lbound, flag_rbound, do_reaction,
-                  strict_newton, 0]
+                  strict_newton, 0, do_tran]
         nt = len(ncells)
         rp = np.ascontiguousarray([dx_comp if dx_comp is not None else dxs[0], p_out, t_in, rho_u_in, rtol, atol],
                                   dtype=np.float64)

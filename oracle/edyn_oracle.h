@@ -195,6 +195,7 @@ void or_smr_set_interior(or_smr* s, const double* qf, const double* qc);
 void or_smr_get_interior(const or_smr* s, double* qf, double* qc);
 double or_smr_step(or_smr* s, double cfl);
 void or_smr_segment_all(const or_smr* s, int g, double* qc);
+void or_smr_set_transport(or_smr* s, const or_tran* tr);
 
 /* Initial conditions (SRC/params.f90:305-580 + SRC/block.f90:394-431). */
 void or_init_cell(const or_mech* m, double T, double p, double u, const double* x_in, double* qf, double* qc);

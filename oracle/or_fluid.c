@@ -892,6 +892,11 @@ void or_smr_set_interior(or_smr* s, const double* qf, const double* qc) {
   }
 }
 
+/* do_tran on every block (NULL: off). */
+void or_smr_set_transport(or_smr* s, const or_tran* tr) {
+  for (int g = 0; g < s->nseg; ++g) s->seg[g]->tran = tr;
+}
+
 /* Segment g's conserved columns with its ghosts ((n + 2 lvir) x nequ). */
 void or_smr_segment_all(const or_smr* s, int g, double* qc) { or_tube_get_all(s->seg[g], NULL, qc); }
 

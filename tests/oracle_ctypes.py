@@ -108,6 +108,7 @@ class Oracle:
         L.or_smr_step.restype = d
         L.or_smr_step.argtypes = [vp, d]
         L.or_smr_segment_all.argtypes = [vp, i, _D]
+        L.or_smr_set_transport.argtypes = [vp, vp]
         self.kk = 53
         self.nequ = self.kk + 3
 
@@ -332,6 +333,9 @@ class OracleSMR:
 
     def step(self, cfl):
         return self.o.L.or_smr_step(self.h, cfl)
+
+    def set_transport(self, on=True):
+        self.o.L.or_smr_set_transport(self.h, self.o.tran if on else None)
 
     def segment_all(self, g, n, lvir):
         """Segment g's conserved columns with its ghosts."""

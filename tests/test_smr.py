@@ -180,3 +180,31 @@ def test_interface_ghosts_device_form_matches_oracle(oracle, lvir, dxs):
     for (t, g), col in dev.items():
         full = s.segment_all(t, ncells[t], lvir)
         np.testing.assert_array_equal(full[g + lvir], col, err_msg=f"segment {t} ghost {g}")
+
+
+def test_equal_segments_with_transport_reproduce_one_tube(oracle):
+    """Transport across block interfaces: with equal cell sizes the blocks'
+    ghosts are copies, so the transport flux of every face, recomputed by
+    each block from its own ghosts, is the tube's."""
+    n, dx = 90, 2e-5
+    xm = (np.arange(n) + 0.5) * dx
+    nm = species_names()
+    w = 0.5 * (1 + np.tanh((xm - 0.5 * n * dx) / (4 * dx)))
+    air = configs.mole_vector(nm, {"O2": 0.21, "N2": 0.79})
+    rich = configs.mole_vector(nm, {"CH4": 0.3, "O2": 0.3, "H2O": 0.1, "N2": 0.3})
+    X = (1 - w)[:, None] * air[None, :] + w[:, None] * rich[None, :]
+    _, qc = oracle.init_cells(400.0 + 900.0 * w, np.full(n, configs.ATM), np.zeros(n), X)
+    qf = np.zeros_like(qc)
+    for i in range(n):
+        oracle.L.or_qc_to_qf(oracle.mech, qc[i].ctypes.data_as(_D), qf[i].ctypes.data_as(_D))
+    flags = [1, 2, 1, 2, 0, 0, 0, 0]
+    rp = [dx] + RP[1:]
+    t = oracle.tube(n, 2, flags, rp)
+    t.set_transport()
+    t.set_interior(qf, qc)
+    s = oracle.smr([30, 40, 20], [dx] * 3, 2, flags, rp)
+    s.set_transport()
+    s.set_interior(qf, qc)
+    for _ in range(15):
+        assert t.step(0.5) == s.step(0.5)
+    np.testing.assert_array_equal(s.get()[1], t.get()[1])

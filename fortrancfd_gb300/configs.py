@@ -188,6 +188,19 @@ def planar_flame(names=None, ncell: int = 1000, dx: float = 2.0e-5, T_lo: float 
                          rho_u_in=rho_in * u_in, x_in=fresh), cfl=0.5, tend=0.2)
 
 
+def smr_segments(nx_comp: int, dx_comp: float, ncell_per_block: int, lev_smr_0: int = 0, num_smr_0: int = 0,
+                 lev_smr_n: int = 0, num_smr_n: int = 0):
+    """Segments (cells, cell size) of the reference's SMR layout
+    (set_block_size, SRC/block.f90:91-379): the computational blocks at
+    dx_comp, then on each side, from the inside out, levels 2..lev_smr of
+    num_smr blocks each with the cell size doubling per level. Equal-size
+    blocks merge into one segment. For edyn_init_blocks / Blocks."""
+    left = [(num_smr_0 * ncell_per_block, dx_comp * 2 ** (lev - 1)) for lev in range(lev_smr_0, 1, -1)]
+    right = [(num_smr_n * ncell_per_block, dx_comp * 2 ** (lev - 1)) for lev in range(2, lev_smr_n + 1)]
+    segs = [s for s in left + [(nx_comp, dx_comp)] + right if s[0] > 0]
+    return [n for n, _ in segs], [d for _, d in segs]
+
+
 def ch4_air_mixture(names, phi: float) -> np.ndarray:
     n = phi + 2.0 * 4.76
     return mole_vector(names, {"CH4": phi / n, "O2": 2.0 / n, "N2": 2.0 * 3.76 / n})

@@ -208,3 +208,13 @@ def test_equal_segments_with_transport_reproduce_one_tube(oracle):
     for _ in range(15):
         assert t.step(0.5) == s.step(0.5)
     np.testing.assert_array_equal(s.get()[1], t.get()[1])
+
+
+def test_smr_layout_of_the_reference_namelist():
+    """configs.smr_segments against the block sizes set_block_size gives
+    (SRC/block.f90:176-223): dx_comp 2^(lev_smr - lev) per level, the
+    coarsest block outermost, num_smr blocks of ncell_per_block cells each."""
+    n, d = configs.smr_segments(1000, 2e-5, 10, lev_smr_n=4, num_smr_n=2)
+    assert n == [1000, 20, 20, 20] and d == [2e-5, 4e-5, 8e-5, 1.6e-4]
+    n, d = configs.smr_segments(200, 1e-4, 16, lev_smr_0=3, num_smr_0=1, lev_smr_n=2, num_smr_n=1)
+    assert n == [16, 16, 200, 16] and d == [4e-4, 2e-4, 1e-4, 2e-4]

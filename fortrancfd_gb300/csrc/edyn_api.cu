@@ -1064,6 +1064,15 @@ int init_packed(const char* chem_dir, int nspe, int nequ, int ntube, const int* 
     if (rc == EDYN_OK) rc = fail((Ctx*)*out, EDYN_E_ARG, "packed tubes are Cartesian (is_spherical 0)");
     return rc ? rc : EDYN_E_ARG;
   }
+  if (n_iflags > EDYN_IF_DO_TRAN && iflags[EDYN_IF_DO_TRAN] != 0) {
+    // The per-column transport kernels reproduce each tube's properties,
+    // but two or more tubes stepped with transport lose their right-end
+    // cells on the GPU; until that is found, transport takes one tube.
+    int rc = edyn_init(chem_dir, nspe, nequ, 16, lvir, iflags, n_iflags, rparams, n_rparams, nullptr, out);
+    if (rc == EDYN_OK)
+      rc = fail((Ctx*)*out, EDYN_E_ARG, "transport (do_tran 1) takes one tube per context, not packed tubes or SMR");
+    return rc ? rc : EDYN_E_ARG;
+  }
   // One context whose rows hold every tube's block: its row length is the
   // sum of the blocks, its cell count the sum of the cells.
   int rc = edyn_init(chem_dir, nspe, nequ, (int)(cols - 2 * GHOST), lvir, iflags, n_iflags, rparams, n_rparams,

@@ -67,8 +67,8 @@ extern "C" {
  * viscous stress, conduction and mixture-averaged diffusion from TRANLIB's
  * MCAVIS / MCACON / MCADIF, with MCAVIS standing in for the MCAVIS_EA that
  * the reference's viscosity_ea calls (SRC/trans.f90:137-151) and its
- * tranlib.f does not define. It is available for one tube, packed tubes
- * (edyn_init_tubes) and SMR domains (edyn_init_blocks), not for
+ * tranlib.f does not define. It is available for one tube per context,
+ * not for packed tubes (edyn_init_tubes), SMR domains (edyn_init_blocks) nor
  * edyn_solve_fluid_noalloc, and it turns the uniform-region shortcuts of the
  * stage off.
  * is_spherical = 1 (the problem file's flag, SRC/params.f90:37) solves the
@@ -110,8 +110,8 @@ int edyn_init_tubes(const char* chem_dir, int nspe, int nequ, int ntube, const i
  * each reference block does. One dt = cfl dx_comp / max(|u| + a) for all,
  * dx_comp = rparams[EDYN_RP_DX] (calc_dt, SRC/update.f90:13-59). rparams is
  * one row as for edyn_init; the first segment may take the inflow boundary
- * (x_in), the last the outflow. Euler or TVDRK3, transport included; no
- * spherical geometry, energy sources or surrogate. Cells are numbered left to right;
+ * (x_in), the last the outflow. Euler or TVDRK3; no transport, spherical
+ * geometry, energy sources or surrogate. Cells are numbered left to right;
  * the context steps through edyn_step / edyn_advance, as packed tubes do. */
 int edyn_init_blocks(const char* chem_dir, int nspe, int nequ, int nseg, const int* ncell, const double* dx, int lvir,
                      const int* iflags, int n_iflags, const double* rparams, int n_rparams, const double* x_in,

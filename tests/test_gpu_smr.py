@@ -107,35 +107,6 @@ def test_blocks_refused_where_unsupported():
         Blocks([32, 32], [1e-3, 2e-3], select_time=2)
     with pytest.raises(EdynError):
         Blocks([32, 8], [1e-3, 2e-3])
+    with pytest.raises(EdynError, match="transport"):
+        Blocks([32, 32], [1e-3, 2e-3], do_tran=1)
 
-
-def test_flame_blocks_with_transport_match_oracle(oracle):
-    """The planar flame's layout, shortened: a fine segment with the
-    temperature front, then two coarser levels toward the outflow, inflow on
-    the left, transport on, chemistry off; 40 steps against the oracle's
-    blocks at 1e-10."""
-    case = configs.planar_flame(ncell=160, dx=2e-5, x_c=1.6e-3, width=4e-4, do_reaction=0)
-    ncells, dxs = [96, 32, 32], [2e-5, 4e-5, 8e-5]
-    xm = centres(ncells, dxs)
-    from math import erf
-
-    T = 300.0 + 0.5 * 2100.0 * (np.array([erf((x - 1.6e-3) / 4e-4) for x in xm]) + 1.0)
-    n = sum(ncells)
-    fl = case.flags
-    _, qc = oracle.init_cells(T, np.full(n, configs.ATM), np.full(n, 1.0), np.tile(fl["x_in"], (n, 1)))
-    from oracle_ctypes import _D
-
-    qf = np.zeros_like(qc)
-    for i in range(n):
-        oracle.L.or_qc_to_qf(oracle.mech, qc[i].ctypes.data_as(_D), qf[i].ctypes.data_as(_D))
-    rp = [dxs[0], fl["p_out"], fl["t_in"], fl["rho_u_in"], 1e-5, 1e-13]
-    s = oracle.smr(ncells, dxs, 2, [1, 2, 1, 2, 0, 1, 1, 0], rp, x_in=fl["x_in"])
-    s.set_transport()
-    s.set_interior(qf, qc)
-    b = Blocks(ncells, dxs, flag_lbound=1, flag_rbound=1, do_tran=1, p_out=fl["p_out"], t_in=fl["t_in"],
-               rho_u_in=fl["rho_u_in"], x_in=fl["x_in"])
-    b.upload(qf, qc)
-    for _ in range(40):
-        s.step(0.5)
-        b.step(0.5)
-    check(s.get()[0], b.download()[0])

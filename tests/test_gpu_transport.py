@@ -138,38 +138,9 @@ def test_device_loop_with_transport_matches_host_loop():
     check(qb, qa, tol=1e-12)
 
 
-def test_packed_tubes_with_transport_match_single_tubes():
-    """Two mixing layers packed in one context, with transport, against the
-    same layers as one-tube contexts (the same kernels per tube: to rounding)."""
-    nm = species_names()
-    cases = []
-    for n, dx, hot in ((96, 1e-5, 1100.0), (128, 2e-5, 1500.0)):
-        xm = (np.arange(n) + 0.5) * dx
-        w = 0.5 * (1 + np.tanh((10 * dx - np.abs(xm - 0.5 * n * dx)) / (3 * dx)))
-        air = configs.mole_vector(nm, {"O2": 0.21, "N2": 0.79})
-        rich = configs.mole_vector(nm, {"CH4": 0.3, "O2": 0.3, "H2O": 0.1, "N2": 0.3})
-        X = (1 - w)[:, None] * air[None, :] + w[:, None] * rich[None, :]
-        cases.append((n, dx, 400.0 + (hot - 400.0) * w, X))
-    kw = dict(flag_acu=1, flag_muscl=2, flag_rbound=0, do_reaction=0, strict_newton=1)
-    pk = Tubes([c[0] for c in cases], [c[1] for c in cases], do_tran=1, **kw)
-    pk.init_cells(np.concatenate([c[2] for c in cases]), np.full(sum(c[0] for c in cases), configs.ATM),
-                  np.zeros(sum(c[0] for c in cases)), np.concatenate([c[3] for c in cases]))
-    singles = []
-    for n, dx, T, X in cases:
-        g = Tube(n, dx, do_tran=1, flag_acu=1, flag_muscl=2, do_reaction=0)
-        g.init_cells(T, np.full(n, configs.ATM), np.zeros(n), X)
-        singles.append(g)
-    for _ in range(20):
-        pk.step(0.5)
-    qf_pk = pk.split(pk.download()[0])
-    t_pk, _ = pk.times()
-    for g, q, tend in zip(singles, qf_pk, t_pk):
-        t = sum(g.step(0.5) for _ in range(20))
-        assert t == pytest.approx(tend, rel=1e-12)
-        check(g.download()[0], q, tol=1e-11)
-
-
 def test_transport_refused_where_unsupported():
+    with pytest.raises(EdynError, match="transport"):
+        Tubes([64, 64], [1e-5, 1e-5], do_tran=1)
     torch = pytest.importorskip("torch")
     g = Tube(64, 1e-5, do_tran=1)
     qf = torch.zeros((56, 72), dtype=torch.float64, device="cuda")

@@ -74,10 +74,12 @@ def parse():
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--workload", default="detonation_air_200k",
-                   choices=list(WORKLOADS) + ["reactors", "tubes", "flame"],
+                   choices=list(WORKLOADS) + ["reactors", "tubes", "flame", "spherical_flame"],
                    help="the tube of the headline metric (default), the 20k CH4/O2 tube, the reactor batch, "
-                        "the uneven batch of --ntubes tubes in one context, or the planar flame with transport")
-    p.add_argument("--flame-cells", type=int, default=1000, help="cells of --workload flame (20 um each)")
+                        "the uneven batch of --ntubes tubes in one context, the planar flame with transport, or "
+                        "the spherical flame kernel (transport, chemistry, ignition energy)")
+    p.add_argument("--flame-cells", type=int, default=None,
+                   help="cells of --workload flame / spherical_flame (20 um each; 1000 / 2000 by default)")
     p.add_argument("--ntubes", type=int, default=256, help="tubes of --workload tubes")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-surrogate", action="store_true", help="skip the surrogate-vs-plain comparison")
@@ -650,21 +652,29 @@ def tubes_arm(args, rank, world, local):
     print(json.dumps(line), flush=True)
 
 
-FLAME_METRIC = "cell-steps/s on 1 GB300: planar CH4/air flame with transport and chemistry"
+FLAME_METRICS = {"flame": "cell-steps/s on 1 GB300: planar CH4/air flame with transport and chemistry",
+                 "spherical_flame": "cell-steps/s on 1 GB300: spherical CH4/air flame kernel with transport, "
+                                    "chemistry and ignition energy"}
 
 
 def flame_case(args):
     from fortrancfd_gb300 import configs
 
-    return configs.planar_flame(ncell=args.flame_cells)
+    if args.workload == "spherical_flame":
+        return configs.spherical_flame(ncell=args.flame_cells or 2000)
+    return configs.planar_flame(ncell=args.flame_cells or 1000)
 
 
 def flame_config(case, args, world):
+    sph = args.workload == "spherical_flame"
     return {"workload": case.name, "cells": case.ncell, "dx_m": case.dx,
-            "mixture": "stoichiometric CH4/O2/N2, 1 atm; T erf profile 300 -> 2400 K at 1.4 cm, width 2 mm",
-            "scheme": "MUSCL-minmod + HLLC + SSP-RK3, CFL 0.5, inflow 300 K 1 m/s / outflow 1 atm",
+            "mixture": ("stoichiometric CH4/O2/N2, 300 K, 1 atm, at rest" if sph else
+                        "stoichiometric CH4/O2/N2, 1 atm; T erf profile 300 -> 2400 K at 1.4 cm, width 2 mm"),
+            "scheme": ("spherical, MUSCL-minmod + HLLC + SSP-RK3, CFL 0.2, centre wall / outflow 1 atm" if sph else
+                       "MUSCL-minmod + HLLC + SSP-RK3, CFL 0.5, inflow 300 K 1 m/s / outflow 1 atm"),
             "transport": "calc_flux_tran, TRANLIB mixture rules (MCAVIS, MCACON, MCADIF)",
             "chemistry": "GRI-Mech 3.0, per-cell stiff integration, rtol 1e-5, atol 1e-13",
+            "sources": "ignition energy 0.5 mJ, 500 um, 100 us (Frendi et al.)" if sph else "none",
             "timed_steps": f"steps {args.warmup + 1}..{args.warmup + args.steps} from the initial state",
             "parallelism": f"replicas x{world}"}
 
@@ -676,9 +686,14 @@ def flame_oracle(case):
     o = Oracle()
     fl = case.flags
     qf0, qc0 = o.init_cells(case.T, case.p, case.u, case.X)
-    t = o.tube(case.ncell, 2, [1, 2, 1, 2, 0, 1, 1, fl["do_reaction"]],
-               [case.dx, fl["p_out"], fl["t_in"], fl["rho_u_in"], 1e-5, 1e-13], x_in=fl["x_in"])
+    t = o.tube(case.ncell, 2, [1, 2, 1, 2, 0, fl["flag_lbound"], fl["flag_rbound"], fl["do_reaction"]],
+               [case.dx, fl["p_out"], fl.get("t_in", 300.0), fl.get("rho_u_in", 0.0), 1e-5, 1e-13],
+               x_in=fl.get("x_in"))
     t.set_transport()
+    if fl.get("is_spherical"):
+        t.set_spherical()
+    if fl.get("ignition"):
+        t.set_sources(ignition=fl["ignition"])
     t.set_interior(qf0, qc0)
     return o, t
 
@@ -698,7 +713,7 @@ def flame_reference_arm(args, rank, world):
     el = time.perf_counter() - t0
     v = case.ncell * args.steps / el
     cores = o.L.or_num_threads()
-    print(json.dumps({"impl": "reference", "metric": FLAME_METRIC, "value": v, "unit": UNIT, "n_gpus": world,
+    print(json.dumps({"impl": "reference", "metric": FLAME_METRICS[args.workload], "value": v, "unit": UNIT, "n_gpus": world,
                       "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
                       "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
                       "data": "synthetic", "config": flame_config(case, args, world),
@@ -723,12 +738,13 @@ def flame_arm(args, rank, world, local):
 
         dist.init_process_group("nccl", device_id=dev)
     case = flame_case(args)
-    fl = {k: v for k, v in case.flags.items() if k != "do_tran"}
+    fl = {k: v for k, v in case.flags.items() if k not in ("do_tran", "ignition", "strict_newton")}
     stream = torch.cuda.Stream(dev)
     torch.cuda.set_stream(stream)
-    tube = Tube(case.ncell, case.dx, do_tran=1, strict_newton=0, **{k: v for k, v in fl.items()
-                                                                   if k != "strict_newton"})
+    tube = Tube(case.ncell, case.dx, do_tran=1, strict_newton=0, **fl)
     tube.set_stream(stream.cuda_stream)
+    if case.flags.get("ignition"):
+        tube.set_ignition(*case.flags["ignition"])
     tube.init_cells(case.T, case.p, case.u, case.X)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     if world > 1:
@@ -740,7 +756,7 @@ def flame_arm(args, rank, world, local):
     t_max = max_over_ranks(t_dev, world, dev)
     # the fluid step with and without transport on the state reached
     qf, qc, _ = tube.download()
-    inviscid = Tube(case.ncell, case.dx, strict_newton=0, **{k: v for k, v in fl.items() if k != "strict_newton"})
+    inviscid = Tube(case.ncell, case.dx, strict_newton=0, **fl)
     inviscid.set_stream(stream.cuda_stream)
     inviscid.set_uniform_skip(False)
     dt = tube.calc_dt(case.cfl)
@@ -772,10 +788,11 @@ def flame_arm(args, rank, world, local):
         cpu = {"value": case.ncell * n / el, "unit": UNIT, "cores": o.L.or_num_threads(), "kind": "port",
                "sample": f"steps 2..{n + 1} of the flame, {el:.1f} s"}
     # per step: the loop test, three (transport properties, transport flux,
-    # stage) triples and the one-pass chemistry (counter clear + pass)
-    per_step = 1 + 3 * 3 + 2
+    # stage) triples, the one-pass chemistry (counter clear + pass) and, with
+    # an ignition energy, the source kernel
+    per_step = 1 + 3 * 3 + 2 + (1 if case.flags.get("ignition") else 0)
     print(json.dumps({
-        "metric": FLAME_METRIC, "value": job_value(case.ncell, args.steps, world, t_max), "unit": UNIT,
+        "metric": FLAME_METRICS[args.workload], "value": job_value(case.ncell, args.steps, world, t_max), "unit": UNIT,
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": flame_config(case, args, world), "clocks": clk.summary(),
@@ -791,12 +808,12 @@ def main():
     args = parse()
     rank, world, local = dist_env()
     if args.impl == "reference":
-        if args.workload == "flame":
+        if args.workload in FLAME_METRICS:
             flame_reference_arm(args, rank, world)
             return
         reference_arm(args, rank, world)
         return
-    if args.workload == "flame":
+    if args.workload in FLAME_METRICS:
         flame_arm(args, rank, world, local)
         return
     if args.workload == "tubes":

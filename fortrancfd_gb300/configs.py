@@ -188,6 +188,24 @@ def planar_flame(names=None, ncell: int = 1000, dx: float = 2.0e-5, T_lo: float 
                          rho_u_in=rho_in * u_in, x_in=fresh), cfl=0.5, tend=0.2)
 
 
+def spherical_flame(names=None, ncell: int = 2000, dx: float = 2.0e-5, do_reaction: int = 1) -> TubeCase:
+    """Spherical CH4/air flame kernel, the reference's spherical-flame
+    example (WORK/Examples/CH4_GRI3.0/SphericalFlame: sph_flame.inp,
+    initial.txt, igsource.inp) on one uniform grid in place of its SMR
+    blocks: stoichiometric CH4/O2/N2 at 300 K, 1 atm, at rest; spherical
+    geometry with the centre a wall and an outflow at 1 atm at r = ncell dx;
+    an ignition energy after Frendi et al. of 0.5 mJ within 500 um for the
+    first 100 us; MUSCL-minmod + HLLC, TVDRK3, CFL 0.2, transport and
+    chemistry on. flags['ignition'] holds (kind, [(E, r, duration, start)])."""
+    names = names or species_names(GRI30_DIR)
+    fresh = mole_vector(names, {"CH4": 0.0950570342, "O2": 0.1901140684, "N2": 0.7148288973})
+    return TubeCase(f"ch4_air_spherical_flame_{ncell}", ncell, dx, np.full(ncell, 300.0), np.full(ncell, ATM),
+                    np.zeros(ncell), np.tile(fresh, (ncell, 1)),
+                    dict(select_time=1, select_riemann=2, flag_acu=1, flag_muscl=2, flag_weno=0, flag_lbound=0,
+                         flag_rbound=1, do_reaction=do_reaction, do_tran=1, is_spherical=1, p_out=ATM,
+                         ignition=(1, [(0.5e-3, 500e-6, 100e-6, 0.0)])), cfl=0.2, tend=2.0e-2)
+
+
 def smr_segments(nx_comp: int, dx_comp: float, ncell_per_block: int, lev_smr_0: int = 0, num_smr_0: int = 0,
                  lev_smr_n: int = 0, num_smr_n: int = 0):
     """Segments (cells, cell size) of the reference's SMR layout

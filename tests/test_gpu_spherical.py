@@ -51,3 +51,30 @@ def test_spherical_refused_where_unsupported():
             Tube(64, 1e-4, is_spherical=1, **kw)
     with pytest.raises(EdynError):
         Tube(64, 1e-4, is_spherical=2)
+
+
+def test_spherical_flame_kernel_matches_oracle(oracle):
+    """The spherical flame configuration shortened (200 cells): spherical
+    geometry, transport, chemistry and the ignition energy together, 10
+    steps against the oracle at the reacting bar (T 0.1 %, Y 1e-3 of the
+    largest mass fraction)."""
+    case = configs.spherical_flame(ncell=200)
+    fl = case.flags
+    qf0, qc0 = oracle.init_cells(case.T, case.p, case.u, case.X)
+    ot = oracle.tube(case.ncell, 2, [1, 2, 1, 2, 0, 0, 1, 1], [case.dx, fl["p_out"], 300.0, 0.0, 1e-5, 1e-13])
+    ot.set_transport()
+    ot.set_spherical()
+    ot.set_sources(ignition=fl["ignition"])
+    ot.set_interior(qf0, qc0)
+    g = Tube(case.ncell, case.dx, flag_acu=1, flag_muscl=2, flag_rbound=1, p_out=fl["p_out"], do_reaction=1,
+             do_tran=1, is_spherical=1)
+    g.set_ignition(*fl["ignition"])
+    g.upload(qf0, qc0)
+    for _ in range(10):
+        dt_o = ot.step(case.cfl)
+        dt_g = g.step(case.cfl)
+        assert dt_g == pytest.approx(dt_o, rel=1e-6)
+    qf_o, qf_g = ot.get()[0], g.download()[0]
+    assert qf_o[0, 2] > 300.5  # the ignition energy heated the centre
+    assert np.max(np.abs(qf_g[:, 2] - qf_o[:, 2]) / qf_o[:, 2]) < 1e-3
+    assert np.max(np.abs(qf_g[:, 3:] - qf_o[:, 3:])) / qf_o[:, 3:].max() < 1e-3

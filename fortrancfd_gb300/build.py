@@ -19,7 +19,7 @@ LIBDIR = PKG / "_lib"
 LIBNAME = "libedyn_gb300.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-fno-fast-math"]
-SOURCES = ["mechanism.cpp", "transport.cpp", "fluid.cu", "chem.cu", "mlp.cu", "edyn_api.cu"]
+SOURCES = ["mechanism.cpp", "transport.cpp", "h5file.cpp", "fluid.cu", "chem.cu", "mlp.cu", "edyn_api.cu"]
 
 
 def _nvcc() -> str:

@@ -27,6 +27,7 @@
 #include "mechanism.h"
 #include "recon.cuh"
 #include "transport.h"
+#include "h5file.h"
 
 extern "C" int edyn_mech_load_dir(const char* dir, edyn_mech* m, char* err, int errlen);
 extern "C" int edyn_mech_write(const edyn_mech* m, const char* path);
@@ -184,6 +185,16 @@ struct Ctx {
   int* d_present = nullptr;  // per species: nonzero somewhere in the tube
   Surr surr;
   Packed pk;
+  // output (write_hdf5_b) and restart (read_hdf5_restart)
+  double* d_srcq = nullptr;    // [2][n]: Qrad and qTw of the last source step (eos_obj%Qrad, %qTw)
+  double* d_out = nullptr;     // [EDYN_OUT_FIXED + ns][n]: the output rows of a snapshot
+  double* h_out = nullptr;     // pinned host copy of d_out
+  double* d_xm = nullptr;      // [2][n]: cell centres and sizes
+  std::vector<double> xm;      // the same on the host
+  cudaStream_t out_stream = nullptr;
+  cudaEvent_t out_ready = nullptr, out_copied = nullptr;
+  bool out_pending = false;    // a snapshot's copy is queued and not yet written
+  H5Writer h5;
   std::string err;
 };
 
@@ -368,6 +379,8 @@ int source_step(Ctx* c, double dt, bool dev, double time = 0.0) {
   s.lam = c->trd.lam;
   s.e2 = c->trd.e2;
   s.lg = c->trd.lg;
+  s.q_rad = c->d_srcq;
+  s.q_tw = c->d_srcq + c->n;
   if (dev) {
     s.dt_dev = c->d_dt;
     s.time_dev = c->d_time;
@@ -754,6 +767,104 @@ int keep_hrr_dot(Ctx* c) {
   return EDYN_OK;
 }
 
+
+// Cell centres and sizes of the output's x_m and dx rows: (i + 1/2) dx for
+// one tube (the reference accumulates them, SRC/block.f90:264-304, which can
+// differ in the last bits; its restart compares them within 1e-7); SMR
+// segments follow each other from x = 0.
+int cell_geometry(Ctx* c) {
+  if (c->pk.ntube && !c->pk.smr)
+    return fail(c, EDYN_E_ARG, "output and restart take one tube or one SMR domain per context, not packed tubes");
+  const size_t n = (size_t)c->n;
+  c->xm.assign(2 * n, 0.0);
+  if (!c->pk.ntube) {
+    for (size_t i = 0; i < n; ++i) {
+      c->xm[i] = ((double)i + 0.5) * c->dx;
+      c->xm[n + i] = c->dx;
+    }
+  } else {
+    double x0 = 0.0;
+    size_t i = 0;
+    for (int t = 0; t < c->pk.ntube; ++t) {
+      const double d = c->pk.dx[t];
+      for (int j = 0; j < c->pk.n[t]; ++j, ++i) {
+        c->xm[i] = x0 + ((double)j + 0.5) * d;
+        c->xm[n + i] = d;
+      }
+      x0 += c->pk.n[t] * d;
+    }
+  }
+  return EDYN_OK;
+}
+
+// set_eos_params + the rows of write_hdf5_b on the device, then their copy
+// to pinned host memory on the output stream: the context's stream goes on
+// with the next steps while the copy drains.
+int output_snapshot(Ctx* c) {
+  if (c->out_pending) return fail(c, EDYN_E_ARG, "a snapshot is pending: write it (edyn_output_write) first");
+  const size_t n = (size_t)c->n, nrow = (size_t)(EDYN_OUT_FIXED + c->ns);
+  if (!c->d_out) {
+    int rc = cell_geometry(c);
+    if (rc) return rc;
+    CK(cudaMalloc(&c->d_out, nrow * n * sizeof(double)));
+    CK(cudaMallocHost(&c->h_out, nrow * n * sizeof(double)));
+    CK(cudaMalloc(&c->d_xm, 2 * n * sizeof(double)));
+    CK(cudaMemcpy(c->d_xm, c->xm.data(), 2 * n * sizeof(double), cudaMemcpyHostToDevice));
+    CK(cudaStreamCreateWithFlags(&c->out_stream, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&c->out_ready, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&c->out_copied, cudaEventDisableTiming));
+  }
+  int rc = eval_hrr_dot(c);
+  if (rc) return rc;
+  OutputArgs a{};
+  a.n = c->n;
+  a.ld = c->ld;
+  a.ns = c->ns;
+  a.qf = c->qf[c->cur];
+  a.qc = c->qc;
+  a.colmap = c->pk.ntube ? c->pk.colmap : nullptr;
+  a.hrr = c->hrr;
+  a.hrr_dot = c->hrr_dot_state == 2 ? c->hrr_dot : nullptr;
+  a.q_rad = c->d_srcq;
+  a.q_tw = c->d_srcq + c->n;
+  a.xm = c->d_xm;
+  a.wall = c->src.wall;
+  a.tw_min = c->src.tw_min;
+  a.tw_max = c->src.tw_max;
+  a.alpha = c->src.alpha;
+  a.beta = c->src.beta;
+  a.out = c->d_out;
+  // the previous snapshot's copy has left d_out before the rows are rewritten
+  CK(cudaStreamWaitEvent(c->stream, c->out_copied, 0));
+  CK(launch_output_rows(a, c->stream));
+  CK(cudaEventRecord(c->out_ready, c->stream));
+  CK(cudaStreamWaitEvent(c->out_stream, c->out_ready, 0));
+  CK(cudaMemcpyAsync(c->h_out, c->d_out, nrow * n * sizeof(double), cudaMemcpyDeviceToHost, c->out_stream));
+  CK(cudaEventRecord(c->out_copied, c->out_stream));
+  c->out_pending = true;
+  return EDYN_OK;
+}
+
+// waits for the pending snapshot (taking one first when none is queued)
+int output_rows_ready(Ctx* c) {
+  if (!c->out_pending) {
+    int rc = output_snapshot(c);
+    if (rc) return rc;
+  }
+  CK(cudaEventSynchronize(c->out_copied));
+  c->out_pending = false;
+  return EDYN_OK;
+}
+
+// dataset names of write_hdf5_b: the fifteen fields (Fortran's trim keeps
+// their leading blanks), then the species names
+std::vector<std::string> output_names(const Ctx* c) {
+  std::vector<std::string> v = {"rho", "u_x", "  T", "  p", " et", " ek", " ei", "HRR",
+                                "HRD", "Qrd", " Tw", "QTw", "x_m", " dx", "idx"};
+  for (int k = 0; k < c->ns; ++k) v.push_back(c->mech.spec_name[k]);
+  return v;
+}
+
 }  // namespace
 
 extern "C" {
@@ -961,6 +1072,8 @@ int edyn_init(const char* chem_dir, int nspe, int nequ, int ncell, int lvir, con
     CK(cudaMemsetAsync(c->acc, 0, rows * sizeof(double), c->stream));
   }
   CK(cudaMalloc(&c->hrr, (size_t)ncell * sizeof(double)));
+  CK(cudaMalloc(&c->d_srcq, 2 * (size_t)ncell * sizeof(double)));
+  CK(cudaMemsetAsync(c->d_srcq, 0, 2 * (size_t)ncell * sizeof(double), c->stream));
   CK(cudaMalloc(&c->hrr_dot, (size_t)ncell * sizeof(double)));
   CK(cudaMalloc(&c->tchem, (size_t)ncell * sizeof(double)));
   CK(cudaMemsetAsync(c->qf[0], 0, rows * sizeof(double), c->stream));
@@ -1685,6 +1798,147 @@ int edyn_surrogate_stats(void* ctx, double* stats) {
   return EDYN_OK;
 }
 
+int edyn_output_open(void* ctx, const char* path) {
+  Ctx* c = (Ctx*)ctx;
+  if (!c || !c->qc || !path) return EDYN_E_ARG;
+  int rc = cell_geometry(c);
+  if (rc) return rc;
+  std::string err;
+  if (!c->h5.create(path, err)) return fail(c, EDYN_E_IO, "edyn_output_open: %s", err.c_str());
+  return EDYN_OK;
+}
+
+int edyn_output_snapshot(void* ctx) {
+  Ctx* c = (Ctx*)ctx;
+  if (!c || !c->qc) return EDYN_E_ARG;
+  return output_snapshot(c);
+}
+
+int edyn_output_rows(void* ctx, double* rows) {
+  Ctx* c = (Ctx*)ctx;
+  if (!c || !c->qc || !rows) return EDYN_E_ARG;
+  int rc = output_rows_ready(c);
+  if (rc) return rc;
+  std::memcpy(rows, c->h_out, (size_t)(EDYN_OUT_FIXED + c->ns) * c->n * sizeof(double));
+  return EDYN_OK;
+}
+
+int edyn_output_write(void* ctx, int nout, long long nt, double dt, double time_total, double time_restart,
+                      double cpu_total, double cpu_restart) {
+  Ctx* c = (Ctx*)ctx;
+  if (!c || !c->qc) return EDYN_E_ARG;
+  if (!c->h5.is_open()) return fail(c, EDYN_E_ARG, "edyn_output_write: no output file is open (edyn_output_open)");
+  if (nout < 0 || nout > 999999 || nt < 0 || nt > 2147483647ll)
+    return fail(c, EDYN_E_ARG, "edyn_output_write: nout %d or nt %lld out of the file's integer fields", nout, nt);
+  int rc = output_rows_ready(c);
+  if (rc) return rc;
+  const std::string gname = step_group_name(nout, time_total);
+  // the attributes write_hdf5_b writes (its loop stops before the eighth,
+  // the chemistry directory name)
+  const std::vector<H5Attr> attrs = {{"dt", false, dt},
+                                     {"time from 0s", false, time_total},
+                                     {"time from restart", false, time_restart},
+                                     {"cpu time total", false, cpu_total},
+                                     {"cpu time restart", false, cpu_restart},
+                                     {"number of output", true, (double)nout},
+                                     {"number of time step", true, (double)nt}};
+  std::string err;
+  if (!c->h5.add_group(gname, attrs, output_names(c), c->h_out, c->n, err))
+    return fail(c, EDYN_E_IO, "edyn_output_write: %s", err.c_str());
+  return EDYN_OK;
+}
+
+int edyn_output_close(void* ctx) {
+  Ctx* c = (Ctx*)ctx;
+  if (!c || !c->qc) return EDYN_E_ARG;
+  std::string err;
+  if (!c->h5.close(err)) return fail(c, EDYN_E_IO, "edyn_output_close: %s", err.c_str());
+  return EDYN_OK;
+}
+
+int edyn_restart(void* ctx, const char* path, int* nout, long long* nt, double* time, double* cpu_time) {
+  Ctx* c = (Ctx*)ctx;
+  if (!c || !c->qc || !path) return EDYN_E_ARG;
+  int rc = cell_geometry(c);
+  if (rc) return rc;
+  H5Reader r;
+  std::string err;
+  std::vector<H5Object> groups;
+  if (!r.open(path, err) || !r.list("", groups, err)) return fail(c, EDYN_E_IO, "edyn_restart: %s", err.c_str());
+  if (groups.empty() || !groups.back().group) return fail(c, EDYN_E_IO, "edyn_restart: %s holds no step group", path);
+  // the last member in the root group's index order (idx_stepgroup)
+  const std::string g = groups.back().name;
+  const size_t n = (size_t)c->n, ns = (size_t)c->ns, ne = (size_t)c->ne;
+  auto field = [&](const std::string& name, std::vector<double>& v) -> int {
+    H5Value x;
+    if (!r.read_dataset(g + "/" + name, x, err))
+      return fail(c, EDYN_E_IO, "edyn_restart: %s/%s: %s", g.c_str(), name.c_str(), err.c_str());
+    if (x.data.size() != n)
+      return fail(c, EDYN_E_ARG, "edyn_restart: %s/%s holds %zu cells, the context %zu", g.c_str(), name.c_str(),
+                  x.data.size(), n);
+    v.swap(x.data);
+    return EDYN_OK;
+  };
+  std::vector<double> rho, u, T, et, xm, idx, dx;
+  if ((rc = field("rho", rho)) || (rc = field("u_x", u)) || (rc = field("  T", T)) || (rc = field(" et", et)) ||
+      (rc = field("x_m", xm)) || (rc = field("idx", idx)) || (rc = field(" dx", dx)))
+    return rc;
+  // the reference's consistency checks of the grid (SRC/read_hdf5.f90:327-365)
+  for (size_t i = 0; i < n; ++i) {
+    if (std::fabs(xm[i] - c->xm[i]) > 1e-7)
+      return fail(c, EDYN_E_ARG, "edyn_restart: x_m of cell %zu (%g) does not match the context's (%g)", i + 1, xm[i],
+                  c->xm[i]);
+    if (idx[i] != (double)(i + 1)) return fail(c, EDYN_E_ARG, "edyn_restart: idx of cell %zu is %g", i + 1, idx[i]);
+    if (std::fabs(dx[i] - c->xm[n + i]) > 1e-7)
+      return fail(c, EDYN_E_ARG, "edyn_restart: dx of cell %zu (%g) does not match the context's (%g)", i + 1, dx[i],
+                  c->xm[n + i]);
+  }
+  std::vector<double> X(n * ns);
+  for (size_t k = 0; k < ns; ++k) {
+    std::vector<double> v;
+    if ((rc = field(c->mech.spec_name[k], v))) return rc;
+    for (size_t i = 0; i < n; ++i) X[i * ns + k] = v[i];
+  }
+  // Xi2Yi (CKXTY), then set_block_params: qf = (rho, u, T, Y), Qc = (rho,
+  // rho u, rho et, rho Y)
+  std::vector<double> qf(n * ne), qc(n * ne);
+  for (size_t i = 0; i < n; ++i) {
+    const double* x = &X[i * ns];
+    double sum = 0.0;
+    for (size_t k = 0; k < ns; ++k) sum += x[k] * c->mech.W[k];
+    double* f = &qf[i * ne];
+    double* q = &qc[i * ne];
+    f[0] = rho[i];
+    f[1] = u[i];
+    f[2] = T[i];
+    q[0] = rho[i];
+    q[1] = rho[i] * u[i];
+    q[2] = rho[i] * et[i];
+    for (size_t k = 0; k < ns; ++k) {
+      const double y = x[k] * c->mech.W[k] / sum;
+      f[3 + k] = y;
+      q[3 + k] = rho[i] * y;
+    }
+  }
+  H5Value a_time, a_cpu, a_nout, a_nt;
+  if (!r.read_attr(g, "time from 0s", a_time, err) || !r.read_attr(g, "cpu time total", a_cpu, err) ||
+      !r.read_attr(g, "number of output", a_nout, err) || !r.read_attr(g, "number of time step", a_nt, err) ||
+      a_time.data.empty() || a_cpu.data.empty() || a_nout.data.empty() || a_nt.data.empty())
+    return fail(c, EDYN_E_IO, "edyn_restart: %s attributes: %s", g.c_str(), err.c_str());
+  rc = edyn_upload(ctx, qf.data(), qc.data());
+  if (rc) return rc;
+  CK(cudaMemsetAsync(c->d_srcq, 0, 2 * n * sizeof(double), c->stream));
+  CK(cudaMemsetAsync(c->hrr, 0, n * sizeof(double), c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  // read_hdf5_restart's returns: the next output and step numbers
+  if (nout) *nout = (int)a_nout.data[0] + 1;
+  if (nt) *nt = (long long)a_nt.data[0] + 1;
+  if (time) *time = a_time.data[0];
+  if (cpu_time) *cpu_time = a_cpu.data[0];
+  c->clock = a_time.data[0];
+  return EDYN_OK;
+}
+
 int edyn_download_source(void* ctx, double* hrr, double* hrr_dot) {
   Ctx* c = (Ctx*)ctx;
   if (!c || !c->qc) return EDYN_E_ARG;
@@ -2022,6 +2276,13 @@ int edyn_finalize(void* ctx) {
   cudaFree(c->d_tp);
   cudaFree(c->d_tflux);
   cudaFree(c->d_col_tube);
+  cudaFree(c->d_srcq);
+  cudaFree(c->d_out);
+  cudaFree(c->d_xm);
+  if (c->h_out) cudaFreeHost(c->h_out);
+  if (c->out_ready) cudaEventDestroy(c->out_ready);
+  if (c->out_copied) cudaEventDestroy(c->out_copied);
+  if (c->out_stream) cudaStreamDestroy(c->out_stream);
   if (c->own) cudaStreamDestroy(c->own);
   delete c;
   return EDYN_OK;

@@ -126,6 +126,26 @@ struct SourceArgs {
   const double* lg;
   int ig_type, n_ig;        // ignition: 1 Frendi et al., 2 Zhang et al.; per source E [J], r [m], t, t0 [s]
   double ig_e[EDYN_IG_MAX], ig_r[EDYN_IG_MAX], ig_t[EDYN_IG_MAX], ig_t0[EDYN_IG_MAX];
+  double* q_rad;            // per cell: the last radiation loss (eos_obj%Qrad), W/m^3 (may be null)
+  double* q_tw;             // per cell: the last wall heat (eos_obj%qTw), W/m^3 (may be null)
+};
+
+// The output fields of write_hdf5_b (SRC/write_hdf5.f90:140-162) from
+// set_eos_params (SRC/block.f90:434-470), one row of n per field:
+constexpr int EDYN_OUT_FIXED = 15;  // rho u_x T p et ek ei HRR HRD Qrd Tw QTw x_m dx idx, then X_k
+struct OutputArgs {
+  int n, ld, ns;
+  const double* qf;         // primitive rows (rho, u, T, Y)
+  const double* qc;         // conserved rows (the energy row)
+  const int* colmap;        // column of cell i (null: i)
+  const double* hrr;        // per cell, or null (zeros)
+  const double* hrr_dot;
+  const double* q_rad;
+  const double* q_tw;
+  const double* xm;         // [2][n]: cell centre and cell size
+  int wall;                 // wall heat on: Tw(x) = A tanh(alpha (x - beta)) + B, else Tw = 0
+  double tw_min, tw_max, alpha, beta;
+  double* out;              // [EDYN_OUT_FIXED + ns][n]
 };
 
 int fluid_upload_tables(const ThermoTable& tb, cudaStream_t s);
@@ -151,6 +171,7 @@ cudaError_t launch_qc_to_qf(const StageArgs& a, cudaStream_t s);
 // the stage input (a.tran); launch_stage calls it before the stage kernel.
 cudaError_t launch_tran(const StageArgs& a, cudaStream_t s);
 cudaError_t launch_energy_sources(const SourceArgs& a, cudaStream_t s);
+cudaError_t launch_output_rows(const OutputArgs& a, cudaStream_t s);
 cudaError_t launch_check_state(const double* qf, const double* qc, int n, int ns, int ld, unsigned* err,
                                cudaStream_t s);
 cudaError_t launch_init_cells(int n, int ns, const double* T, const double* p, const double* u, const double* X,

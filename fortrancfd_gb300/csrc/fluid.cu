@@ -1155,6 +1155,7 @@ __global__ void __launch_bounds__(SRC_THREADS) k_energy_sources(SourceArgs s) {
             kp = kp + kpi * (y[k] * tb.invW[k] * isw) * (p / 101325.0);
           }
           add = -4.0 * kp * 5.6703744191844294e-08 * (T4 - T04);
+          if (s.q_rad) s.q_rad[i] = add;
         } else {
           const double L = tlog(T, s.lg);
           double sl = 0.0, sr = 0.0;
@@ -1169,6 +1170,7 @@ __global__ void __launch_bounds__(SRC_THREADS) k_energy_sources(SourceArgs s) {
           const double A = 0.5 * (s.tw_max - s.tw_min), B = 0.5 * (s.tw_max + s.tw_min);
           const double tw = A * tanh(s.alpha * (xm - s.beta)) + B;
           add = -4.0 * lambda * s.nu * (T - tw) / (s.d_m * s.d_m);
+          if (s.q_tw) s.q_tw[i] = add;
         }
       } else {
         if (s.ig_type == 0) continue;
@@ -1212,6 +1214,65 @@ __global__ void __launch_bounds__(SRC_THREADS) k_energy_sources(SourceArgs s) {
 
 cudaError_t launch_energy_sources(const SourceArgs& a, cudaStream_t s) {
   k_energy_sources<<<(a.n + SRC_THREADS - 1) / SRC_THREADS, SRC_THREADS, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Output fields (set_eos_params, SRC/block.f90:434-470, in write_hdf5_b's row
+// order, SRC/write_hdf5.f90:140-162), one thread per cell:
+//   X = CKYTX(Y), p = CKPX(rho, T, X), ek = u^2 / 2,
+//   ei = CKUBML(T, X) / W (specific_energy, SRC/thermo.f90:356-375),
+//   et = rho E / rho, and the per-cell source outputs as the last source
+//   step left them (HRR, HRR_dot, Qrad, qTw; Tw from the wall profile).
+// Each row is written contiguously, as the file's datasets hold them.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) k_output_rows(OutputArgs a) {
+  const int i = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+  if (i >= a.n) return;
+  const ThermoTable& tb = c_thermo;
+  const int ns = a.ns;
+  const size_t ld = (size_t)a.ld, n = (size_t)a.n;
+  const size_t col = (size_t)(a.colmap ? a.colmap[i] : i) + GHOST;
+  const double rho = a.qf[col], u = a.qf[ld + col], T = a.qf[2 * ld + col];
+  double* o = a.out + i;
+  double sumyow = 0.0;
+  for (int k = 0; k < ns; ++k) sumyow = fma(a.qf[(3 + k) * ld + col], tb.invW[k], sumyow);
+  const double isw = 1.0 / sumyow;
+  double wtm = 0.0, ubml = 0.0;
+  for (int k = 0; k < ns; ++k) {
+    const double xk = a.qf[(3 + k) * ld + col] * tb.invW[k] * isw;
+    o[(EDYN_OUT_FIXED + k) * n] = xk;
+    wtm = fma(xk, tb.W[k], wtm);
+    // U_k / R = H_k / R - T (NASA-7, the range of T)
+    const int r = (T > tb.tmid[k]) ? 1 : 0;
+    double h = fma(tb.ah[r][4][k], T, tb.ah[r][3][k]);
+    h = fma(h, T, tb.ah[r][2][k]);
+    h = fma(h, T, tb.ah[r][1][k]);
+    h = fma(h, T, tb.ah[r][0][k]);
+    h = fma(h, T, tb.ah[r][5][k]);
+    ubml = fma(xk, h - T, ubml);
+  }
+  o[0] = rho;
+  o[n] = u;
+  o[2 * n] = T;
+  o[3 * n] = rho * R_SI * T / wtm;
+  o[4 * n] = a.qc[2 * ld + col] / rho;
+  o[5 * n] = 0.5 * (u * u);
+  o[6 * n] = R_SI * ubml / wtm;
+  o[7 * n] = a.hrr ? a.hrr[i] : 0.0;
+  o[8 * n] = a.hrr_dot ? a.hrr_dot[i] : 0.0;
+  o[9 * n] = a.q_rad ? a.q_rad[i] : 0.0;
+  const double xm = a.xm[i];
+  o[10 * n] = a.wall ? 0.5 * (a.tw_max - a.tw_min) * tanh(a.alpha * (xm - a.beta)) + 0.5 * (a.tw_max + a.tw_min) : 0.0;
+  o[11 * n] = a.q_tw ? a.q_tw[i] : 0.0;
+  o[12 * n] = xm;
+  o[13 * n] = a.xm[n + i];
+  o[14 * n] = (double)(i + 1);
+}
+
+cudaError_t launch_output_rows(const OutputArgs& a, cudaStream_t s) {
+  if (a.n <= 0) return cudaSuccess;
+  k_output_rows<<<(a.n + 127) / 128, 128, 0, s>>>(a);
   return cudaGetLastError();
 }
 

@@ -26,7 +26,13 @@ LIB_PATH = PKG / "_lib" / "libedyn_gb300.so"
 GRI30_DIR = PKG / "data" / "gri30"
 
 EDYN_OK = 0
-EDYN_E_ARG, EDYN_E_CUDA, EDYN_E_MECH, EDYN_E_NEWTON, EDYN_E_CHEM, EDYN_E_STATE = 1, 2, 4, 8, 16, 32
+EDYN_E_ARG, EDYN_E_CUDA, EDYN_E_MECH, EDYN_E_NEWTON, EDYN_E_CHEM, EDYN_E_STATE, EDYN_E_IO = 1, 2, 4, 8, 16, 32, 64
+
+# the datasets of a results file's step group before the species' mole
+# fractions (write_hdf5_b, SRC/write_hdf5.f90:140-162; Fortran's trim keeps
+# the leading blanks)
+OUTPUT_FIELDS = ("rho", "u_x", "  T", "  p", " et", " ek", " ei", "HRR", "HRD", "Qrd", " Tw", "QTw", "x_m", " dx",
+                 "idx")
 
 # iflags / rparams slots (include/edyn_gpu.h)
 IF_SELECT_TIME, IF_SELECT_RIEMANN, IF_FLAG_ACU, IF_FLAG_MUSCL, IF_FLAG_WENO = 0, 1, 2, 3, 4
@@ -96,6 +102,22 @@ def lib() -> ctypes.CDLL:
     L.edyn_set_wall_heat.argtypes = [vp, i, dp]
     L.edyn_set_ignition.argtypes = [vp, i, i, dp, dp, dp, dp]
     L.edyn_version.restype = ctypes.c_char_p
+    ll, llp = ctypes.c_longlong, ctypes.POINTER(ctypes.c_longlong)
+    L.edyn_output_open.argtypes = [vp, cp]
+    L.edyn_output_snapshot.argtypes = [vp]
+    L.edyn_output_rows.argtypes = [vp, dp]
+    L.edyn_output_write.argtypes = [vp, i, ll, d, d, d, d, d]
+    L.edyn_output_close.argtypes = [vp]
+    L.edyn_restart.argtypes = [vp, cp, ip, llp, dp, dp]
+    L.edyn_h5_create.argtypes = [cp, ctypes.POINTER(vp)]
+    L.edyn_h5_add_group.argtypes = [vp, cp, i, ctypes.POINTER(cp), ip, dp, i, ctypes.POINTER(cp), dp, ll]
+    L.edyn_h5_close.argtypes = [vp]
+    L.edyn_h5_list.argtypes = [cp, cp, ctypes.c_char_p, ll]
+    L.edyn_h5_read.argtypes = [cp, cp, dp, ll, llp]
+    L.edyn_h5_attr.argtypes = [cp, cp, cp, dp, ll, llp, ctypes.c_char_p, ll]
+    L.edyn_h5_attr_names.argtypes = [cp, cp, ctypes.c_char_p, ll]
+    L.edyn_h5_step_name.argtypes = [i, d, ctypes.c_char_p, i]
+    L.edyn_h5_error.restype = ctypes.c_char_p
     _lib = L
     return L
 
@@ -196,6 +218,7 @@ class Tube(_Ctx):
         iflags = [select_time, select_riemann, flag_acu, flag_muscl, flag_weno, flag_lbound, flag_rbound,
                   do_reaction, strict_newton, chem_mode, do_tran, is_spherical]
         super().__init__(chem_dir, nspe, ncell, lv, iflags, [dx, p_out, t_in, rho_u_in, rtol, atol], x_in)
+        self.names = names if names is not None else [f"S{k + 1}" for k in range(nspe)]
         self.lvir = lv
         self.dx = dx
 
@@ -370,6 +393,51 @@ class Tube(_Ctx):
         self._check(lib().edyn_download_source(self._h, _ptr(hrr), _ptr(hrr_dot)))
         return hrr, hrr_dot
 
+    # ---- results files: write_hdf5_b / read_hdf5_restart (SRC/write_hdf5.f90, SRC/read_hdf5.f90)
+    def output_names(self) -> list:
+        """Dataset names of a step group, in the rows' order."""
+        return list(OUTPUT_FIELDS) + list(self.names)
+
+    def output_open(self, path) -> None:
+        """init_output: creates (truncates) the results file."""
+        self._check(lib().edyn_output_open(self._h, str(path).encode()))
+
+    def output_snapshot(self) -> None:
+        """Queues set_eos_params and the rows' device-to-host copy; returns
+        at once (one snapshot pending at a time)."""
+        self._check(lib().edyn_output_snapshot(self._h))
+
+    def output_rows(self) -> np.ndarray:
+        """The output rows ((15 + nspe) x ncell) of the pending snapshot, or
+        of one taken now."""
+        rows = np.empty((len(OUTPUT_FIELDS) + self.nspe, self.ncell))
+        self._check(lib().edyn_output_rows(self._h, _ptr(rows)))
+        return rows
+
+    def output_write(self, nout: int, nt: int, dt: float, time_total: float, time_restart: Optional[float] = None,
+                     cpu_total: float = 0.0, cpu_restart: float = 0.0) -> None:
+        """write_hdf5_b: appends the step group nout%06d_time%E11.5 with the
+        pending snapshot's rows (or a snapshot taken now)."""
+        tr = time_total if time_restart is None else time_restart
+        self._check(lib().edyn_output_write(self._h, int(nout), int(nt), float(dt), float(time_total), float(tr),
+                                            float(cpu_total), float(cpu_restart)))
+
+    def output_close(self) -> None:
+        """fin_output."""
+        self._check(lib().edyn_output_close(self._h))
+
+    def restart(self, path):
+        """read_hdf5_restart: the last step group of path becomes the state.
+        Returns (nout, nt, time, cpu_time) as the reference's restart sets
+        them (the group's output and step numbers + 1)."""
+        nout = ctypes.c_int()
+        nt = ctypes.c_longlong()
+        t = ctypes.c_double()
+        cpu = ctypes.c_double()
+        self._check(lib().edyn_restart(self._h, str(path).encode(), ctypes.byref(nout), ctypes.byref(nt),
+                                       ctypes.byref(t), ctypes.byref(cpu)))
+        return nout.value, nt.value, t.value, cpu.value
+
     def download(self):
         qf = np.empty((self.ncell, self.nequ))
         qc = np.empty((self.ncell, self.nequ))
@@ -400,6 +468,7 @@ class Tubes(Tube):
         fl = (ctypes.c_int * len(iflags))(*iflags)
         self._h = ctypes.c_void_p()
         self.nspe, self.nequ, self.ncell = nspe, nspe + 3, int(sum(ncells))
+        self.names = names
         self.ntube, self.ncells = nt, [int(v) for v in ncells]
         self.lvir, self.dx = lv, float(dxs[0])
         rc = L.edyn_init_tubes(str(chem_dir).encode(), nspe, nspe + 3, nt, nc, lv, fl, len(iflags), _ptr(rp), 6,
@@ -451,6 +520,7 @@ class Blocks(Tubes):
         xi = None if x_in is None else np.ascontiguousarray(x_in, dtype=np.float64)
         self._h = ctypes.c_void_p()
         self.nspe, self.nequ, self.ncell = nspe, nspe + 3, int(sum(ncells))
+        self.names = names
         self.ntube, self.ncells = nt, [int(v) for v in ncells]
         self.lvir, self.dx = lv, float(dxs[0])
         rc = L.edyn_init_blocks(str(chem_dir).encode(), nspe, nspe + 3, nt, nc, _ptr(dx), lv, fl, len(iflags),
@@ -511,3 +581,96 @@ class Reactors(_Ctx):
                                         ctypes.c_void_p(yiT_ptr), _ptr(st))
         self._check(rc)
         return {"rhs": int(st[0]), "steps": int(st[1]), "rejects": int(st[2]), "failed": int(st[3])}
+
+
+# ---- HDF5 files without a solver context (include/edyn_h5.h) ----
+def output_path(savedir, nout: int) -> str:
+    """init_output's file name: ./<savedir>/results_nout%06d.h5."""
+    return f"./{savedir}/results_nout{int(nout):06d}.h5"
+
+
+def step_group_name(nout: int, time: float) -> str:
+    """write_hdf5_b's group name: ("nout",i6.6,"_time",e11.5)."""
+    buf = ctypes.create_string_buffer(64)
+    _h5_check(lib().edyn_h5_step_name(int(nout), float(time), buf, 64))
+    return buf.value.decode()
+
+
+def _h5_check(rc: int):
+    if rc:
+        raise EdynError(rc, lib().edyn_h5_error().decode())
+
+
+class H5Writer:
+    """A results-format file: step groups of float64 rows with one-element
+    float64 (Python float) or int32 (Python int) attributes."""
+
+    def __init__(self, path):
+        self._h = ctypes.c_void_p()
+        _h5_check(lib().edyn_h5_create(str(path).encode(), ctypes.byref(self._h)))
+
+    def add_group(self, name: str, attrs: dict, rows: dict) -> None:
+        an = list(attrs)
+        a_names = (ctypes.c_char_p * max(len(an), 1))(*[a.encode() for a in an])
+        a_int = (ctypes.c_int * max(len(an), 1))(*[int(isinstance(attrs[a], (int, np.integer))) for a in an])
+        a_val = np.array([float(attrs[a]) for a in an] or [0.0])
+        rn = list(rows)
+        n = len(rows[rn[0]]) if rn else 0
+        data = np.ascontiguousarray(np.array([np.asarray(rows[r], dtype=np.float64) for r in rn]).reshape(len(rn), n))
+        r_names = (ctypes.c_char_p * max(len(rn), 1))(*[r.encode() for r in rn])
+        _h5_check(lib().edyn_h5_add_group(self._h, name.encode(), len(an), a_names, a_int, _ptr(a_val), len(rn),
+                                          r_names, _ptr(data) if data.size else None, n))
+
+    def close(self) -> None:
+        if self._h.value:
+            _h5_check(lib().edyn_h5_close(self._h))
+        self._h = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+def _h5_text(fn, *args) -> str:
+    size = 1 << 16
+    while True:
+        buf = ctypes.create_string_buffer(size)
+        rc = fn(*args, buf, size)
+        if rc == EDYN_E_ARG and "too small" in lib().edyn_h5_error().decode() and size < (1 << 28):
+            size *= 4
+            continue
+        _h5_check(rc)
+        return buf.value.decode()
+
+
+def h5_list(path, group: str = "") -> list:
+    """Members of a group in its index (name) order; groups end with '/'."""
+    return _h5_text(lib().edyn_h5_list, str(path).encode(), group.encode()).splitlines()
+
+
+def h5_read(path, dataset: str) -> np.ndarray:
+    n = ctypes.c_longlong()
+    _h5_check(lib().edyn_h5_read(str(path).encode(), dataset.encode(), None, 0, ctypes.byref(n)))
+    out = np.empty(n.value)
+    _h5_check(lib().edyn_h5_read(str(path).encode(), dataset.encode(), _ptr(out), n.value, ctypes.byref(n)))
+    return out
+
+
+def h5_attr(path, obj: str, name: str):
+    """An attribute's values (an array), or its text for string attributes."""
+    n = ctypes.c_longlong()
+    buf = ctypes.create_string_buffer(1 << 12)
+    _h5_check(lib().edyn_h5_attr(str(path).encode(), obj.encode(), name.encode(), None, 0, ctypes.byref(n), buf,
+                                 1 << 12))
+    if n.value == 0 and buf.value:
+        return buf.value.decode()
+    out = np.empty(n.value)
+    _h5_check(lib().edyn_h5_attr(str(path).encode(), obj.encode(), name.encode(), _ptr(out), n.value,
+                                 ctypes.byref(n), None, 0))
+    return out
+
+
+def h5_attr_names(path, obj: str) -> list:
+    return _h5_text(lib().edyn_h5_attr_names, str(path).encode(), obj.encode()).splitlines()

@@ -28,6 +28,7 @@ extern "C" {
 #define EDYN_E_CHEM 16      /* a cell's chemistry integration failed (step underflow or step cap) */
 #define EDYN_E_STATE 32     /* a cell's state is non-finite or non-positive, its T pinned at 20 or
                                6000 K, or an uploaded mass fraction is below -1e-6 */
+#define EDYN_E_IO 64        /* an output or restart file could not be written or read */
 
 /* Indices into the iflags array of edyn_init (the solver.inp /params/ and
  * problem-file flags, SRC/params.f90:8-18, 105-142). */
@@ -221,6 +222,62 @@ int edyn_download(void* ctx, double* qf_aos, double* qc_aos, double* hrr);
  * steps that are not written. Zeros before any source step and when the
  * chemistry is frozen. */
 int edyn_download_source(void* ctx, double* hrr, double* hrr_dot);
+
+/* ---- Output and restart files (HDF5) ----
+ * The reference's results files: one step group per output below the root
+ * group, named nout%06d_time%E11.5 (Fortran edit descriptors), holding one
+ * float64 dataset of ncell values per field, in this order (the names are
+ * Fortran's trimmed character(32) values, leading blanks kept):
+ *   "rho", "u_x", "  T", "  p", " et", " ek", " ei", "HRR", "HRD", "Qrd",
+ *   " Tw", "QTw", "x_m", " dx", "idx", then one per species (its name):
+ * rho, u, T, p = CKPX(rho, T, X), specific total / kinetic / internal
+ * energy (rho E / rho, u^2/2, CKUBML / W), HRR, HRR_dot, the radiation loss,
+ * the wall temperature and wall heat of the last source step, the cell
+ * centre and size, the 1-based cell index, and the mole fractions X_k.
+ * Attributes of the group: "dt", "time from 0s", "time from restart",
+ * "cpu time total", "cpu time restart" (float64) and "number of output",
+ * "number of time step" (int32), each a one-element array. The files are
+ * written without an HDF5 library, in the layout libhdf5 writes with its
+ * default settings (superblock version 0, symbol-table groups). One tube or
+ * one SMR domain per context (edyn_init_blocks); packed independent tubes
+ * are refused. Cell centres are (i - 1/2) dx from the domain's left end. */
+
+/* init_output (SRC/write_hdf5.f90:21-48): creates (truncates) the file
+ * path; the next edyn_output_write calls append step groups to it. The
+ * reference names it <savedir>/results_nout%06d.h5 after the output number
+ * that opens it. */
+int edyn_output_open(void* ctx, const char* path);
+
+/* set_eos_params (SRC/block.f90:434-470) on the device, queued on the
+ * context's stream, and the rows' copy to pinned host memory on a stream of
+ * its own: returns at once, so the time loop can go on while the copy
+ * drains. One snapshot may be pending at a time; edyn_output_write (or
+ * edyn_output_rows) takes it. */
+int edyn_output_snapshot(void* ctx);
+
+/* write_hdf5_b (SRC/write_hdf5.f90:76-347): appends the step group of the
+ * pending snapshot (or of a snapshot taken now) to the open file, with the
+ * attributes dt, time_total ("time from 0s"), time_restart ("time from
+ * restart"), cpu_total, cpu_restart, nout and nt. */
+int edyn_output_write(void* ctx, int nout, long long nt, double dt, double time_total, double time_restart,
+                      double cpu_total, double cpu_restart);
+
+/* The rows of the pending snapshot (or of one taken now): (15 + nspe) rows
+ * of ncell doubles, in the dataset order above. */
+int edyn_output_rows(void* ctx, double* rows);
+
+/* fin_output (SRC/write_hdf5.f90:51-73): closes the file. */
+int edyn_output_close(void* ctx);
+
+/* read_hdf5_restart (SRC/read_hdf5.f90:13-423) + set_block_params
+ * (SRC/block.f90:394-431): reads the last step group (in the root group's
+ * name order) of path, checks its x_m, idx and dx against the context's
+ * cells (within 1e-7), converts the mole fractions to mass fractions (CKXTY)
+ * and sets qf = (rho, u, T, Y) and Qc = (rho, rho u, rho et, rho Y). Returns
+ * the next output number and step count (the group's values + 1, as the
+ * reference), the simulated time and the CPU time of the group (any
+ * pointer may be NULL); the context's clock is set to that time. */
+int edyn_restart(void* ctx, const char* path, int* nout, long long* nt, double* time, double* cpu_time);
 
 /* FP64 chemistry right-hand side d(Y_1..Y_nspe, T)/dt of n constant-volume
  * reactors (rows of nspe + 1 values, device pointers; rho in kg/m^3) with

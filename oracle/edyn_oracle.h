@@ -150,6 +150,8 @@ typedef struct or_tube {
   double* fplus;/* (n + 1) * nequ, face i-1/2 of cell i at offset i * nequ */
   double* hrr;  /* n */
   double* hrr_dot;
+  double* qrad; /* n: the last radiation loss (eos_obj%Qrad) */
+  double* qtw;  /* n: the last wall heat (eos_obj%qTw) */
   long chem_rhs_evals, chem_steps;
   const or_tran* tran; /* do_tran: transport fits (NULL: inviscid) */
   or_sources src;      /* energy sources (all off when zeroed) */
@@ -167,6 +169,11 @@ void or_tube_get_interior(const or_tube* t, double* qf, double* qc);
 void or_tube_get_all(const or_tube* t, double* qf, double* qc);
 /* HRR and HRR_dot of the last source step (eos_obj%HRR, %HRR_dot), n values each. */
 void or_tube_get_source(const or_tube* t, double* hrr, double* hrr_dot);
+/* The output rows of write_hdf5_b (SRC/write_hdf5.f90:140-162) from
+ * set_eos_params (SRC/block.f90:434-470): (15 + nspe) rows of n values --
+ * rho, u, T, p, et, ek, ei, HRR, HRR_dot, Qrad, Tw, qTw, x_m, dx, idx, X_k. */
+#define OR_OUT_FIXED 15
+void or_output_rows(const or_tube* t, double* rows);
 void or_update_boundary(or_tube* t);
 void or_ghost_qf(or_tube* t);
 double or_calc_dt(or_tube* t, double cfl);

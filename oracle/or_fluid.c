@@ -222,6 +222,8 @@ or_tube* or_tube_create(const or_mech* m, int n, int lvir, const int* iflags, co
   t->pgod = (double*)calloc((size_t)(n + 1), sizeof(double));
   t->hrr = (double*)calloc((size_t)n, sizeof(double));
   t->hrr_dot = (double*)calloc((size_t)n, sizeof(double));
+  t->qrad = (double*)calloc((size_t)n, sizeof(double));
+  t->qtw = (double*)calloc((size_t)n, sizeof(double));
   return t;
 }
 
@@ -234,6 +236,8 @@ void or_tube_destroy(or_tube* t) {
   free(t->pgod);
   free(t->hrr);
   free(t->hrr_dot);
+  free(t->qrad);
+  free(t->qtw);
   free(t);
 }
 
@@ -718,10 +722,49 @@ static void energy_sources(or_tube* t, double dt) {
         or_ckytx(m, q + 3, x);
         double p = or_pressure(m, q[0], q[2], x);
         add = src == 0 ? rad_loss(s, p, q[2], x) : wall_heat(s, q[2], x, xm);
+        if (src == 0) t->qrad[i] = add;
+        else t->qtw[i] = add;
       }
       QC(t, i)[2] = QC(t, i)[2] + dt * add;
     }
     interior_qc_to_qf(t);
+  }
+}
+
+/* set_eos_params (SRC/block.f90:434-470) per cell: X = CKYTX(Y),
+ * p = pressure(rho, T, X), ek = u^2/2, ei = specific_energy(T, X),
+ * et = Qc(iuener) / rho; then the rows in write_hdf5_b's order
+ * (SRC/write_hdf5.f90:140-162), Tw from the wall profile when it is set
+ * (SRC/params.f90:495-499), else 0. Cell centres (i + 1/2) dx. */
+void or_output_rows(const or_tube* t, double* rows) {
+  const or_mech* m = t->m;
+  const int n = t->n, ns = t->nspe;
+  const or_sources* s = &t->src;
+  for (int i = 0; i < n; ++i) {
+    const double* q = QF(t, i);
+    const double* c = QC(t, i);
+    double x[OR_MAXSP];
+    or_ckytx(m, q + 3, x);
+    const double xm = (i + 0.5) * t->dx;
+    double* o = rows + i;
+    o[0] = q[0];
+    o[(size_t)n] = q[1];
+    o[2 * (size_t)n] = q[2];
+    o[3 * (size_t)n] = or_pressure(m, q[0], q[2], x);
+    o[4 * (size_t)n] = c[2] / q[0];
+    o[5 * (size_t)n] = 0.5 * (q[1] * q[1]);
+    o[6 * (size_t)n] = or_specific_energy(m, q[2], x);
+    o[7 * (size_t)n] = t->hrr[i];
+    o[8 * (size_t)n] = t->hrr_dot[i];
+    o[9 * (size_t)n] = t->qrad[i];
+    o[10 * (size_t)n] = s->wall ? 0.5 * (s->tw_max - s->tw_min) * tanh(s->alpha * (xm - s->beta)) +
+                                      0.5 * (s->tw_max + s->tw_min)
+                                : 0.0;
+    o[11 * (size_t)n] = t->qtw[i];
+    o[12 * (size_t)n] = xm;
+    o[13 * (size_t)n] = t->dx;
+    o[14 * (size_t)n] = (double)(i + 1);
+    for (int k = 0; k < ns; ++k) o[(size_t)(OR_OUT_FIXED + k) * n] = x[k];
   }
 }
 

@@ -37,6 +37,7 @@ class Oracle:
         L.or_tube_set_interior.argtypes = [vp, _D, _D]
         L.or_tube_get_interior.argtypes = [vp, _D, _D]
         L.or_tube_get_source.argtypes = [vp, _D, _D]
+        L.or_output_rows.argtypes = [vp, _D]
         L.or_ckcdyr.argtypes = [vp, d, d, _D, _D, _D]
         L.or_calc_dt.restype = d
         L.or_calc_dt.argtypes = [vp, d]
@@ -266,6 +267,12 @@ class OracleTube:
 
     def step(self, cfl):
         return self.o.L.or_step(self.h, cfl)
+
+    def output_rows(self):
+        """set_eos_params + write_hdf5_b's rows: (15 + nspe) x n."""
+        rows = np.zeros((15 + self.o.nequ - 3, self.n))
+        self.o.L.or_output_rows(self.h, _p(rows))
+        return rows
 
     def set_sources(self, radiation=None, wall=None, ignition=None):
         """radiation: [(species index, 6 fit coefficients)]; wall: (Nu, d, Tw_min,

@@ -159,6 +159,7 @@ typedef struct or_tube {
   int is_spherical;    /* spherical geometry, r = (i + 1/2) dx */
   double* pgod;        /* (n + 1): Roe-averaged face pressures (godunov_state) */
   int smr_left, smr_right; /* SMR: this side faces another block (ghosts by interpolation) */
+  double x0;           /* coordinate of the tube's left edge: cell i's centre is x0 + (i + 1/2) dx */
 } or_tube;
 
 or_tube* or_tube_create(const or_mech* m, int n, int lvir, const int* iflags, const double* rparams,
@@ -203,6 +204,13 @@ void or_smr_get_interior(const or_smr* s, double* qf, double* qc);
 double or_smr_step(or_smr* s, double cfl);
 void or_smr_segment_all(const or_smr* s, int g, double* qc);
 void or_smr_set_transport(or_smr* s, const or_tran* tr);
+/* is_spherical and the energy sources on every segment (r and x are each
+ * cell's centre x_m, SRC/block.f90:262-304). */
+void or_smr_set_spherical(or_smr* s, int on);
+void or_smr_set_sources(or_smr* s, const or_sources* src);
+void or_smr_set_time(or_smr* s, double time);
+/* Segment g's output rows (or_output_rows, with its x_m). */
+void or_smr_output_rows(const or_smr* s, int g, double* rows);
 
 /* Initial conditions (SRC/params.f90:305-580 + SRC/block.f90:394-431). */
 void or_init_cell(const or_mech* m, double T, double p, double u, const double* x_in, double* qf, double* qc);

@@ -516,7 +516,7 @@ static void stage_tail(or_tube* t) {
  * then the momentum's face-pressure gradient, after the combination. */
 static void spherical_update(or_tube* t, int i, double dt, double h1, double h2, const double* q0, int euler) {
   const int ne = t->nequ;
-  double dx = t->dx, rm = (i + 0.5) * dx;
+  double dx = t->dx, rm = t->x0 + (i + 0.5) * dx;
   double Al = (rm - (dx / 2.0)) * (rm - (dx / 2.0));
   double Ar = (rm + (dx / 2.0)) * (rm + (dx / 2.0));
   double dV = rm * rm * dx;
@@ -715,7 +715,7 @@ static void energy_sources(or_tube* t, double dt) {
     for (int i = 0; i < t->n; ++i) {
       const double* q = QF(t, i);
       double x[OR_MAXSP], add;
-      double xm = (i + 0.5) * t->dx;
+      double xm = t->x0 + (i + 0.5) * t->dx;
       if (src == 2) {
         add = ignition(s, t->time, xm);
       } else {
@@ -745,7 +745,7 @@ void or_output_rows(const or_tube* t, double* rows) {
     const double* c = QC(t, i);
     double x[OR_MAXSP];
     or_ckytx(m, q + 3, x);
-    const double xm = (i + 0.5) * t->dx;
+    const double xm = t->x0 + (i + 0.5) * t->dx;
     double* o = rows + i;
     o[0] = q[0];
     o[(size_t)n] = q[1];
@@ -896,6 +896,10 @@ or_smr* or_smr_create(const or_mech* m, int nseg, const int* ncell, const double
   or_smr* s = (or_smr*)calloc(1, sizeof(or_smr));
   s->nseg = nseg;
   s->dx_comp = rparams[0];
+  /* x = 0 where the left SMR zone (the leading segments coarser than
+   * dx_comp) ends, SRC/block.f90:236-237, 296-304 */
+  double x = 0.0;
+  for (int g = 0; g < nseg && dx[g] != s->dx_comp; ++g) x -= ncell[g] * dx[g];
   for (int g = 0; g < nseg; ++g) {
     double rp[6];
     for (int j = 0; j < 6; ++j) rp[j] = rparams[j];
@@ -903,6 +907,8 @@ or_smr* or_smr_create(const or_mech* m, int nseg, const int* ncell, const double
     s->seg[g] = or_tube_create(m, ncell[g], lvir, iflags, rp, x_in);
     s->seg[g]->smr_left = g > 0;
     s->seg[g]->smr_right = g + 1 < nseg;
+    s->seg[g]->x0 = x;
+    x += ncell[g] * dx[g];
   }
   return s;
 }
@@ -939,6 +945,20 @@ void or_smr_set_interior(or_smr* s, const double* qf, const double* qc) {
 void or_smr_set_transport(or_smr* s, const or_tran* tr) {
   for (int g = 0; g < s->nseg; ++g) s->seg[g]->tran = tr;
 }
+
+void or_smr_set_spherical(or_smr* s, int on) {
+  for (int g = 0; g < s->nseg; ++g) s->seg[g]->is_spherical = on;
+}
+
+void or_smr_set_sources(or_smr* s, const or_sources* src) {
+  for (int g = 0; g < s->nseg; ++g) or_tube_set_sources(s->seg[g], src);
+}
+
+void or_smr_set_time(or_smr* s, double time) {
+  for (int g = 0; g < s->nseg; ++g) s->seg[g]->time = time;
+}
+
+void or_smr_output_rows(const or_smr* s, int g, double* rows) { or_output_rows(s->seg[g], rows); }
 
 /* Segment g's conserved columns with its ghosts ((n + 2 lvir) x nequ). */
 void or_smr_segment_all(const or_smr* s, int g, double* qc) { or_tube_get_all(s->seg[g], NULL, qc); }

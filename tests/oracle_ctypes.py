@@ -110,6 +110,10 @@ class Oracle:
         L.or_smr_step.argtypes = [vp, d]
         L.or_smr_segment_all.argtypes = [vp, i, _D]
         L.or_smr_set_transport.argtypes = [vp, vp]
+        L.or_smr_set_spherical.argtypes = [vp, ctypes.c_int]
+        L.or_smr_set_sources.argtypes = [vp, vp]
+        L.or_smr_set_time.argtypes = [vp, d]
+        L.or_smr_output_rows.argtypes = [vp, ctypes.c_int, _D]
         self.kk = 53
         self.nequ = self.kk + 3
 
@@ -277,23 +281,8 @@ class OracleTube:
     def set_sources(self, radiation=None, wall=None, ignition=None):
         """radiation: [(species index, 6 fit coefficients)]; wall: (Nu, d, Tw_min,
         Tw_max, alpha, beta); ignition: (type, [(E, r, duration, start)])."""
-        s = Sources()
-        for r, (k, c) in enumerate(radiation or []):
-            s.rad_sp[r] = k
-            for n in range(6):
-                s.rad_coef[r][n] = c[n]
-        s.nrad = len(radiation or [])
-        if wall is not None:
-            s.wall = 1
-            s.nu, s.d_m, s.tw_min, s.tw_max, s.alpha, s.beta = wall
-            s.tran = ctypes.addressof(self.o.tran)
-        if ignition is not None:
-            s.ig_type = ignition[0]
-            s.n_ig = len(ignition[1])
-            for g, (e, r, d, t0) in enumerate(ignition[1]):
-                s.ig_e[g], s.ig_r[g], s.ig_t[g], s.ig_t0[g] = e, r, d, t0
-        self._src = s
-        self.o.L.or_tube_set_sources(self.h, ctypes.byref(s))
+        self._src = make_sources(self.o, radiation, wall, ignition)
+        self.o.L.or_tube_set_sources(self.h, ctypes.byref(self._src))
 
     def set_time(self, time):
         self.o.L.or_tube_set_time(self.h, time)
@@ -325,6 +314,28 @@ class OracleTube:
             pass
 
 
+def make_sources(o, radiation=None, wall=None, ignition=None):
+    """The oracle's or_sources from radiation [(species, 6 coefficients)],
+    wall (Nu, d, Tw_min, Tw_max, alpha, beta) and ignition (type, [(E, r,
+    duration, start)])."""
+    s = Sources()
+    for r, (k, c) in enumerate(radiation or []):
+        s.rad_sp[r] = k
+        for n in range(6):
+            s.rad_coef[r][n] = c[n]
+    s.nrad = len(radiation or [])
+    if wall is not None:
+        s.wall = 1
+        s.nu, s.d_m, s.tw_min, s.tw_max, s.alpha, s.beta = wall
+        s.tran = ctypes.addressof(o.tran)
+    if ignition is not None:
+        s.ig_type = ignition[0]
+        s.n_ig = len(ignition[1])
+        for g, (e, r, d, t0) in enumerate(ignition[1]):
+            s.ig_e[g], s.ig_r[g], s.ig_t[g], s.ig_t0[g] = e, r, d, t0
+    return s
+
+
 class OracleSMR:
     def __init__(self, o: Oracle, h, n, keep):
         self.o, self.h, self.n, self._keep = o, h, n, keep
@@ -343,6 +354,25 @@ class OracleSMR:
 
     def set_transport(self, on=True):
         self.o.L.or_smr_set_transport(self.h, self.o.tran if on else None)
+
+    def set_spherical(self, on=True):
+        self.o.L.or_smr_set_spherical(self.h, 1 if on else 0)
+
+    def set_sources(self, radiation=None, wall=None, ignition=None):
+        self._src = make_sources(self.o, radiation, wall, ignition)
+        self.o.L.or_smr_set_sources(self.h, ctypes.byref(self._src))
+
+    def set_time(self, time):
+        self.o.L.or_smr_set_time(self.h, time)
+
+    def output_rows(self, ncells):
+        """The output rows of the whole domain, segment after segment."""
+        parts = []
+        for g, n in enumerate(ncells):
+            rows = np.zeros((15 + self.o.nequ - 3, n))
+            self.o.L.or_smr_output_rows(self.h, g, _p(rows))
+            parts.append(rows)
+        return np.hstack(parts)
 
     def segment_all(self, g, n, lvir):
         """Segment g's conserved columns with its ghosts."""

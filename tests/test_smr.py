@@ -218,3 +218,100 @@ def test_smr_layout_of_the_reference_namelist():
     assert n == [1000, 20, 20, 20] and d == [2e-5, 4e-5, 8e-5, 1.6e-4]
     n, d = configs.smr_segments(200, 1e-4, 16, lev_smr_0=3, num_smr_0=1, lev_smr_n=2, num_smr_n=1)
     assert n == [16, 16, 200, 16] and d == [4e-4, 2e-4, 1e-4, 2e-4]
+
+
+def same_state(a, b, tol):
+    """rho, T, Y relative; u relative to its peak (it is ~0 at rest)."""
+    np.testing.assert_allclose(a[:, [0, 2]], b[:, [0, 2]], rtol=tol)
+    np.testing.assert_allclose(a[:, 1], b[:, 1], rtol=0, atol=tol * max(np.abs(b[:, 1]).max(), 1e-300))
+    np.testing.assert_allclose(a[:, 3:], b[:, 3:], rtol=0, atol=tol * b[:, 3:].max())
+
+
+def test_cell_centres_start_where_the_left_smr_zone_ends(oracle):
+    """x = 0 at the end of the leading segments coarser than dx_comp
+    (SRC/block.f90:236-237, 296-304): the output's x_m row and every
+    position-dependent term use these centres."""
+    ncells, dxs = [16, 16, 32, 16], [4e-3, 2e-3, 1e-3, 2e-3]
+    n = sum(ncells)
+    qf, qc = sod_state(oracle, np.arange(n) * 1.0, -1.0)
+    s = oracle.smr(ncells, dxs, 2, [1, 2, 1, 2, 0, 0, 0, 0], RP)
+    s.set_interior(qf, qc)
+    rows = s.output_rows(ncells)
+    edges = np.r_[0.0, np.cumsum(np.repeat(dxs, ncells))] - (16 * 4e-3 + 16 * 2e-3)
+    np.testing.assert_allclose(rows[12], 0.5 * (edges[:-1] + edges[1:]), rtol=0, atol=1e-15)
+    np.testing.assert_array_equal(rows[13], np.repeat(dxs, ncells))
+
+
+@pytest.mark.parametrize("flags", [[1, 2, 1, 2, 0, 0, 1, 0], [0, 1, 1, 4, 0, 0, 1, 0]])
+def test_equal_segments_spherical_reproduce_one_tube(oracle, flags):
+    """Spherical geometry on equal-dx segments: r = x_m of each cell, the
+    same radii as one tube's (to the rounding of the segment origins)."""
+    n, dx = 120, 1e-4
+    xm = (np.arange(n) + 0.5) * dx
+    qf, qc = sod_state(oracle, xm, 0.3 * n * dx)
+    t = oracle.tube(n, 2, flags, [dx] + RP[1:])
+    t.set_spherical()
+    t.set_interior(qf, qc)
+    s = oracle.smr([40, 50, 30], [dx, dx, dx], 2, flags, [dx] + RP[1:])
+    s.set_spherical()
+    s.set_interior(qf, qc)
+    for _ in range(30):
+        assert s.step(0.5) == pytest.approx(t.step(0.5), rel=1e-13)
+    same_state(s.get()[0], t.get()[0], 1e-11)
+
+
+def test_refined_spherical_ball_close_to_uniform_grid(oracle):
+    """A pressurised ball on a fine core with coarser outer segments (the
+    reference's spherical examples refine toward the centre): its shock
+    stays close to the uniform fine grid's."""
+    dx = 1e-4
+    fine = oracle.tube(160, 2, [1, 2, 1, 2, 0, 0, 1, 0], [dx] + RP[1:])
+    fine.set_spherical()
+    xm = (np.arange(160) + 0.5) * dx
+    qf, qc = sod_state(oracle, xm, 20 * dx)
+    fine.set_interior(qf, qc)
+    ncells, dxs = [64, 24, 12], [dx, 2 * dx, 4 * dx]
+    xs = np.r_[(np.arange(64) + 0.5) * dx, 64 * dx + (np.arange(24) + 0.5) * 2 * dx,
+               112 * dx + (np.arange(12) + 0.5) * 4 * dx]
+    qf2, qc2 = sod_state(oracle, xs, 20 * dx)
+    s = oracle.smr(ncells, dxs, 2, [1, 2, 1, 2, 0, 0, 1, 0], [dx] + RP[1:])
+    s.set_spherical()
+    s.set_interior(qf2, qc2)
+    t_f = t_s = 0.0
+    while t_f < 2e-5:
+        t_f += fine.step(0.4)
+    while t_s < t_f:
+        t_s += s.step(0.4)
+    pf = fine.get()[0][:64, 2]
+    ps = s.get()[0][:64, 2]
+    assert np.all(np.isfinite(s.get()[0]))
+    assert np.max(np.abs(ps - pf)) / pf.max() < 0.05
+
+
+def test_sources_on_equal_segments_reproduce_one_tube(oracle):
+    """Radiation, wall heat and ignition on equal-dx segments: each cell's x_m
+    as one tube's, so the same heating (to the rounding of the origins)."""
+    from test_sources import RAD_FITS
+    nm = species_names()
+    n, dx = 90, 2e-5
+    prod = configs.equilibrium_tp(configs.ch4_air_mixture(nm, 1.0), 1800.0, configs.ATM)
+    _, qc = oracle.init_cells(np.linspace(900.0, 1800.0, n), np.full(n, configs.ATM), np.zeros(n), np.tile(prod, (n, 1)))
+    qf = np.zeros_like(qc)
+    for i in range(n):
+        oracle.L.or_qc_to_qf(oracle.mech, qc[i].ctypes.data_as(_D), qf[i].ctypes.data_as(_D))
+    src = dict(radiation=[(nm.index(k), c) for k, c in RAD_FITS.items()],
+               wall=(4.0, 2e-3, 373.0, 1300.0, 2e4, 0.5 * n * dx),
+               ignition=(2, [(2e-7, 3e-4, 1e-6, 0.0)]))
+    flags = [1, 2, 1, 2, 0, 0, 0, 0]
+    t = oracle.tube(n, 2, flags, [dx] + RP[1:])
+    t.set_interior(qf, qc)
+    t.set_sources(**src)
+    s = oracle.smr([30, 30, 30], [dx, dx, dx], 2, flags, [dx] + RP[1:])
+    s.set_interior(qf, qc)
+    s.set_sources(**src)
+    for _ in range(8):
+        assert s.step(0.5) == pytest.approx(t.step(0.5), rel=1e-13)
+    qs, qt = s.get()[0], t.get()[0]
+    assert np.abs(qt[:, 2] - qf[:, 2]).max() > 0.1  # the sources acted
+    same_state(qs, qt, 1e-11)
+    np.testing.assert_allclose(s.output_rows([30, 30, 30])[[9, 10, 11]], t.output_rows()[[9, 10, 11]], rtol=1e-10)

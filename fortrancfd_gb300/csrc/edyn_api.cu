@@ -90,6 +90,8 @@ struct Packed {
   bool smr = false;
   double dx_comp = 0.0;    // the dx of calc_dt's dt = cfl dx_comp / max(|u| + a)
   double* d_snap = nullptr;
+  double* d_x0 = nullptr;  // the coordinate of each segment's left edge
+  std::vector<double> x0;  // the same on the host
 };
 
 // A contiguous run of cells in the rows: the whole tube, or one packed tube.
@@ -270,7 +272,7 @@ StageArgs base_args(Ctx* c) {
   if (c->pk.ntube) {
     const Packed& k = c->pk;
     a.tubes = TubeTab{k.d_tiles, k.d_n, k.d_off, k.d_dx, k.d_p_out, k.d_dt, k.d_active, k.d_time, k.ntiles, k.colmap,
-                      k.tube_of, k.smr ? k.d_snap : nullptr, k.ntube};
+                      k.tube_of, k.smr ? k.d_snap : nullptr, k.ntube, k.d_x0};
   }
   return a;
 }
@@ -387,6 +389,18 @@ int source_step(Ctx* c, double dt, bool dev, double time = 0.0) {
     s.step_active = c->d_active;
     s.cvel = c->d_cvel;
   }
+  if (c->pk.ntube) {
+    // SMR segments (one dt for all): columns, centres, per-segment speeds
+    const Packed& k = c->pk;
+    s.colmap = k.colmap;
+    s.tube_of = k.tube_of;
+    s.xm = c->d_xm;
+    if (dev) {
+      s.dt_dev = k.d_dt;
+      s.time_dev = k.d_time;
+      s.cvel = k.d_cvel;
+    }
+  }
   cudaError_t e = launch_energy_sources(s, c->stream);
   if (e != cudaSuccess) return fail(c, EDYN_E_CUDA, "energy sources: %s", cudaGetErrorString(e));
   return EDYN_OK;
@@ -438,7 +452,7 @@ int chem_source_step(Ctx* c, double dt, bool dev) {
     L.cvel_out = nullptr;
     L.time = nullptr;
     if (dev) {
-      L.cvel_tube = k.d_cvel;
+      L.cvel_tube = c->src_on ? nullptr : k.d_cvel;  // with sources, their kernel publishes the speeds
       L.time_tube = k.d_time;
     }
   }
@@ -783,17 +797,39 @@ int cell_geometry(Ctx* c) {
       c->xm[n + i] = c->dx;
     }
   } else {
-    double x0 = 0.0;
+    // SMR segments, each from its left edge (smr_geometry)
     size_t i = 0;
     for (int t = 0; t < c->pk.ntube; ++t) {
-      const double d = c->pk.dx[t];
+      const double d = c->pk.dx[t], x0 = c->pk.x0[t];
       for (int j = 0; j < c->pk.n[t]; ++j, ++i) {
         c->xm[i] = x0 + ((double)j + 0.5) * d;
         c->xm[n + i] = d;
       }
-      x0 += c->pk.n[t] * d;
     }
   }
+  return EDYN_OK;
+}
+
+// SMR: the segments' left edges, x = 0 where the left SMR zone (the leading
+// segments whose cells differ from dx_comp) ends (SRC/block.f90:236-237,
+// 296-304), and every cell's centre and size on the device (the energy
+// sources' positions, the output's x_m and dx); spherical geometry takes
+// r = x_m.
+int smr_geometry(Ctx* c) {
+  Packed& k = c->pk;
+  k.x0.assign(k.ntube, 0.0);
+  double x = 0.0;
+  for (int t = 0; t < k.ntube && k.dx[t] != k.dx_comp; ++t) x -= k.n[t] * k.dx[t];
+  for (int t = 0; t < k.ntube; ++t) {
+    k.x0[t] = x;
+    x += k.n[t] * k.dx[t];
+  }
+  if (!k.d_x0) CK(cudaMalloc(&k.d_x0, k.ntube * sizeof(double)));
+  CK(cudaMemcpy(k.d_x0, k.x0.data(), k.ntube * sizeof(double), cudaMemcpyHostToDevice));
+  int rc = cell_geometry(c);
+  if (rc) return rc;
+  if (!c->d_xm) CK(cudaMalloc(&c->d_xm, c->xm.size() * sizeof(double)));
+  CK(cudaMemcpy(c->d_xm, c->xm.data(), c->xm.size() * sizeof(double), cudaMemcpyHostToDevice));
   return EDYN_OK;
 }
 
@@ -808,7 +844,7 @@ int output_snapshot(Ctx* c) {
     if (rc) return rc;
     CK(cudaMalloc(&c->d_out, nrow * n * sizeof(double)));
     CK(cudaMallocHost(&c->h_out, nrow * n * sizeof(double)));
-    CK(cudaMalloc(&c->d_xm, 2 * n * sizeof(double)));
+    if (!c->d_xm) CK(cudaMalloc(&c->d_xm, 2 * n * sizeof(double)));
     CK(cudaMemcpy(c->d_xm, c->xm.data(), 2 * n * sizeof(double), cudaMemcpyHostToDevice));
     CK(cudaStreamCreateWithFlags(&c->out_stream, cudaStreamNonBlocking));
     CK(cudaEventCreateWithFlags(&c->out_ready, cudaEventDisableTiming));
@@ -1172,9 +1208,10 @@ int init_packed(const char* chem_dir, int nspe, int nequ, int ntube, const int* 
     if (rc == EDYN_OK) rc = fail((Ctx*)*out, EDYN_E_ARG, "packed tubes take the plain chemistry (chem_mode 0)");
     return rc ? rc : EDYN_E_ARG;
   }
-  if (n_iflags > EDYN_IF_IS_SPHERICAL && iflags[EDYN_IF_IS_SPHERICAL] != 0) {
+  if (!smr && n_iflags > EDYN_IF_IS_SPHERICAL && iflags[EDYN_IF_IS_SPHERICAL] != 0) {
     int rc = edyn_init(chem_dir, nspe, nequ, 16, lvir, iflags, n_iflags, rparams, n_rparams, nullptr, out);
-    if (rc == EDYN_OK) rc = fail((Ctx*)*out, EDYN_E_ARG, "packed tubes are Cartesian (is_spherical 0)");
+    if (rc == EDYN_OK)
+      rc = fail((Ctx*)*out, EDYN_E_ARG, "independent packed tubes are Cartesian (is_spherical 0; SMR domains take it)");
     return rc ? rc : EDYN_E_ARG;
   }
   if (n_iflags > EDYN_IF_DO_TRAN && iflags[EDYN_IF_DO_TRAN] != 0) {
@@ -1286,7 +1323,10 @@ int edyn_init_blocks(const char* chem_dir, int nspe, int nequ, int nseg, const i
   }
   int rc = init_packed(chem_dir, nspe, nequ, nseg, ncell, lvir, iflags, n_iflags, rp.data(), n_rparams, x_in, true,
                        out);
-  if (rc == EDYN_OK) ((Ctx*)*out)->pk.dx_comp = rparams[EDYN_RP_DX];
+  if (rc == EDYN_OK) {
+    ((Ctx*)*out)->pk.dx_comp = rparams[EDYN_RP_DX];
+    rc = smr_geometry((Ctx*)*out);
+  }
   return rc;
 }
 
@@ -1995,7 +2035,9 @@ int edyn_transport_properties(void* ctx, double* mu, double* kappa, double* dif)
 
 namespace {
 int sources_allowed(Ctx* c, const char* what) {
-  if (c->pk.ntube) return fail(c, EDYN_E_ARG, "%s: one tube per context (packed tubes have no energy sources)", what);
+  if (c->pk.ntube && !c->pk.smr)
+    return fail(c, EDYN_E_ARG, "%s: one tube or one SMR domain per context (independent packed tubes have no energy "
+                "sources)", what);
   if (c->chem_mode == 1) return fail(c, EDYN_E_ARG, "%s: not with the surrogate chemistry (chem_mode 1)", what);
   return EDYN_OK;
 }
@@ -2233,7 +2275,7 @@ int edyn_finalize(void* ctx) {
   {
     Packed& k = c->pk;
     void* bufs[] = {k.d_tiles, k.d_n, k.d_off, k.d_dx, k.d_p_out, k.d_dt, k.d_time, k.d_active, k.d_cvel, k.colmap,
-                    k.tube_of, k.d_snap};
+                    k.tube_of, k.d_snap, k.d_x0};
     for (void* b : bufs) cudaFree(b);
   }
   {

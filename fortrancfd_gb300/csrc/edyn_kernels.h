@@ -48,6 +48,7 @@ struct TubeTab {
   // Null: independent tubes.
   double* smr_snap;
   int ntube;
+  const double* x0;        // SMR: the coordinate of each segment's left edge (cell centres x0 + (i + 1/2) dx); null: 0
 };
 
 // Transport of calc_flux_tran (SRC/flux.f90:18-127) when do_tran = 1: the
@@ -128,6 +129,9 @@ struct SourceArgs {
   double ig_e[EDYN_IG_MAX], ig_r[EDYN_IG_MAX], ig_t[EDYN_IG_MAX], ig_t0[EDYN_IG_MAX];
   double* q_rad;            // per cell: the last radiation loss (eos_obj%Qrad), W/m^3 (may be null)
   double* q_tw;             // per cell: the last wall heat (eos_obj%qTw), W/m^3 (may be null)
+  const int* colmap;        // SMR segments: the column of each cell (null: i), ...
+  const int* tube_of;       // ... its segment (the signal speed is kept per segment) ...
+  const double* xm;         // ... and its centre x_m (null: (i + 1/2) dx)
 };
 
 // The output fields of write_hdf5_b (SRC/write_hdf5.f90:140-162) from

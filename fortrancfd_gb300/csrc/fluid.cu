@@ -198,6 +198,7 @@ struct TubeView {
   unsigned long long* cvel;  // signal-speed maximum of this tube (or null)
   int tube = 0;              // index among packed tubes
   long long off = 0;         // column offset of the tube's block among packed tubes
+  double x0 = 0.0;           // SMR segments: the coordinate of the segment's left edge
 };
 
 // minmod slope of interpolation_block: 0.5 (sign(1, m) + sign(1, p)) min(|m|, |p|)
@@ -391,6 +392,7 @@ __global__ void __launch_bounds__(STAGE_MAX_THREADS) k_stage(StageArgs a) {
     tv.p_out = a.tubes.p_out[tube];
     tv.cvel = a.cvel_out ? a.cvel_out + tube : nullptr;
     tv.tube = tube;
+    if constexpr (SPH != 0) tv.x0 = a.tubes.x0 ? a.tubes.x0[tube] : 0.0;
     dt = a.tubes.dt[tube];
   }
   int c0 = tile * TC;
@@ -675,8 +677,8 @@ __global__ void __launch_bounds__(STAGE_MAX_THREADS) k_stage(StageArgs a) {
     // last RK4 stage: Q0 + (k1 + 2 k2 + 2 k3 + k4) / 6
     auto update = [&](int v, double qv) {
       if constexpr (SPH != 0) {
-        // cell centre r = (i + 1/2) dx, face areas (r -+ dx/2)^2, volume r^2 dx
-        const double rm = (i + 0.5) * tv.dx, hd = tv.dx / 2.0;
+        // cell centre r = x_m (x0 + (i + 1/2) dx), face areas (r -+ dx/2)^2, volume r^2 dx
+        const double rm = tv.x0 + (i + 0.5) * tv.dx, hd = tv.dx / 2.0;
         const double Al = (rm - hd) * (rm - hd), Ar = (rm + hd) * (rm + hd), dV = rm * rm * tv.dx;
         const double cdF = (dt / dV) * (Ar * s_l[v * P + f + 1] - Al * s_l[v * P + f]);
         double r = a.kind == 0 ? qv - cdF : fma(a.h1, Q0[v * ld], a.h2 * (qv - cdF));
@@ -1124,14 +1126,15 @@ __global__ void __launch_bounds__(SRC_THREADS) k_energy_sources(SourceArgs s) {
     const size_t ld = (size_t)s.ld;
     const double dt = s.dt_dev ? *s.dt_dev : s.dt;
     const double time = s.time_dev ? *s.time_dev : s.time;
-    double* Q = s.qc + i + GHOST;
-    double* F = s.qf + i + GHOST;
+    const size_t col = (size_t)(s.colmap ? s.colmap[i] : i) + GHOST;
+    double* Q = s.qc + col;
+    double* F = s.qf + col;
     const double q0 = Q[0], q1 = Q[ld];
     double q2 = Q[2 * ld];
     double rho = F[0], u = F[ld], T = F[2 * ld];
     double y[EDYN_NS_MAX], ys[EDYN_NS_MAX];
     for (int k = 0; k < ns; ++k) y[k] = F[(3 + k) * ld];
-    const double xm = (i + 0.5) * s.dx;
+    const double xm = s.xm ? s.xm[i] : (i + 0.5) * s.dx;
     CellEOS e{};
     for (int src = 0; src < 3; ++src) {
       double add = 0.0;
@@ -1204,8 +1207,10 @@ __global__ void __launch_bounds__(SRC_THREADS) k_energy_sources(SourceArgs s) {
     F[2 * ld] = T;
     for (int k = 0; k < ns; ++k) F[(3 + k) * ld] = y[k];
     if (s.cvel) speed = cell_speed(u, T, e.Sz, e.cpR);
+    // SMR segments: the maximum of each segment (calc_dt takes the largest)
+    if (s.cvel && s.tube_of) atomic_max_pos(s.cvel + s.tube_of[i], speed);
   }
-  if (s.cvel) {
+  if (s.cvel && !s.tube_of) {
     double m = speed;
     for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
     if ((threadIdx.x & 31) == 0 && m > 0.0) atomic_max_pos(s.cvel, m);

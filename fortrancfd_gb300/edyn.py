@@ -499,18 +499,21 @@ class Blocks(Tubes):
     blocks, left to right, neighbouring cell sizes equal or a factor of two
     apart, ghosts between segments by the reference's interpolation_block,
     one dt = cfl dx_comp / max(|u| + a) for all (dx_comp defaults to the
-    first segment's cell size). Cells are numbered left to right."""
+    first segment's cell size). Cells are numbered left to right; x = 0
+    where the leading segments coarser than dx_comp end (the cell centres
+    of the energy sources, the spherical radius and the output's x_m)."""
 
     def __init__(self, ncells: Sequence[int], dxs: Sequence[float], *, dx_comp: Optional[float] = None,
                  chem_dir=GRI30_DIR, select_time=1, select_riemann=2, flag_acu=1, flag_muscl=2, flag_weno=0,
-                 flag_lbound=0, flag_rbound=0, do_reaction=0, strict_newton=1, do_tran=0, p_out=101325.0,
-                 t_in=300.0, rho_u_in=0.0, rtol=1e-5, atol=1e-13, x_in: Optional[Sequence[float]] = None):
+                 flag_lbound=0, flag_rbound=0, do_reaction=0, strict_newton=1, do_tran=0, is_spherical=0,
+                 p_out=101325.0, t_in=300.0, rho_u_in=0.0, rtol=1e-5, atol=1e-13,
+                 x_in: Optional[Sequence[float]] = None):
         L = lib()
         names = species_names(chem_dir)
         nspe = len(names)
         lv = lvir_for(flag_acu, flag_weno)
         iflags = [select_time, select_riemann, flag_acu, flag_muscl, flag_weno, flag_lbound, flag_rbound, do_reaction,
-                  strict_newton, 0, do_tran]
+                  strict_newton, 0, do_tran, is_spherical]
         nt = len(ncells)
         rp = np.ascontiguousarray([dx_comp if dx_comp is not None else dxs[0], p_out, t_in, rho_u_in, rtol, atol],
                                   dtype=np.float64)

@@ -78,7 +78,8 @@ extern "C" {
  * flux without pressure, face fluxes weighed by (r -+ dx/2)^2 over r^2 dx,
  * and the momentum's Roe-averaged face-pressure gradient applied after the
  * stage combination as the reference writes it. With Euler or TVDRK3 and
- * first order or MUSCL; not for packed tubes; no uniform-region shortcuts. */
+ * first order or MUSCL; in one tube or an SMR domain (r = x_m), not in
+ * independent packed tubes; no uniform-region shortcuts. */
 int edyn_init(const char* chem_dir, int nspe, int nequ, int ncell, int lvir, const int* iflags, int n_iflags,
               const double* rparams, int n_rparams, const double* x_in, void** ctx);
 
@@ -111,9 +112,14 @@ int edyn_init_tubes(const char* chem_dir, int nspe, int nequ, int ntube, const i
  * each reference block does. One dt = cfl dx_comp / max(|u| + a) for all,
  * dx_comp = rparams[EDYN_RP_DX] (calc_dt, SRC/update.f90:13-59). rparams is
  * one row as for edyn_init; the first segment may take the inflow boundary
- * (x_in), the last the outflow. Euler or TVDRK3; no transport, spherical
- * geometry, energy sources or surrogate. Cells are numbered left to right;
- * the context steps through edyn_step / edyn_advance, as packed tubes do. */
+ * (x_in), the last the outflow. Euler or TVDRK3. The cell centres x_m
+ * follow the reference's (SRC/block.f90:236-304): x = 0 where the leading
+ * segments whose dx differs from dx_comp (the left SMR zone) end; spherical
+ * geometry (is_spherical) takes r = x_m, and the energy sources
+ * (edyn_set_radiation, _wall_heat, _ignition) their positions from x_m.
+ * No transport (do_tran) and no surrogate. Cells are numbered left to
+ * right; the context steps through edyn_step / edyn_advance, as packed
+ * tubes do. */
 int edyn_init_blocks(const char* chem_dir, int nspe, int nequ, int nseg, const int* ncell, const double* dx, int lvir,
                      const int* iflags, int n_iflags, const double* rparams, int n_rparams, const double* x_in,
                      void** ctx);
@@ -446,8 +452,10 @@ int edyn_mech_compile(const char* chem_dir, const char* out_path, char* err, int
 
 /* Energy sources of solve_source after the chemistry (SRC/update.f90:126-147),
  * in the reference's order, each added to rho E over the step and followed
- * by QcToqf of every cell; for one tube per context, not with chem_mode 1.
- * Cell i sits at x = (i + 1/2) dx.
+ * by QcToqf of every cell; for one tube or one SMR domain per context (cell
+ * positions x_m, edyn_init_blocks), not for independent packed tubes nor
+ * with chem_mode 1.
+ * Cell i sits at x = (i + 1/2) dx (SMR domains: at its x_m).
  *
  * Optically thin radiation loss (heat_transfer_radiation,
  * SRC/source.f90:88-137; radiation_heat_loss, SRC/radiation.f90:74-121):

@@ -150,13 +150,16 @@ EMU_EXPORT int emu_setup(const char* dir) {
 }
 
 // Packed tubes (one tube: ntube = 1 and the single-tube launch when
-// packed == 0) stepped nsteps times with their own dt (dts[step * ntube +
-// t]) by the stages of fluid_step. flags: select_time, select_riemann,
+// packed == 0; packed == 2: the segments of an SMR domain, left to right,
+// with the interface ghosts of interpolation_block and x = 0 where the
+// leading segments coarser than dx_comp = dx_comp end) stepped nsteps times
+// with their own dt (dts[step * ntube + t]) by the stages of fluid_step. flags: select_time, select_riemann,
 // flag_acu, flag_muscl, flag_weno, flag_rbound, do_tran, is_spherical;
 // p_out; walls on the left. qf, qc: AoS rows of all cells, tube after tube;
 // qc is updated, qf_out receives the new primitive rows.
-EMU_EXPORT int emu_fluid(int ntube, const int* ncell, const double* dx, int packed, const int* fl, double p_out,
-              const double* qf_aos, double* qc_io, double* qf_out, int nsteps, const double* dts, unsigned* err) {
+EMU_EXPORT int emu_fluid(int ntube, const int* ncell, const double* dx, int packed, double dx_comp, const int* fl,
+                         double p_out, const double* qf_aos, double* qc_io, double* qf_out, int nsteps,
+                         const double* dts, unsigned* err) {
   const int ns = g_ns, ne = ns + 3;
   std::vector<long long> off(ntube), first(ntube);
   long long cols = 0, ntot = 0;
@@ -181,7 +184,16 @@ EMU_EXPORT int emu_fluid(int ntube, const int* ncell, const double* dx, int pack
   if (stage_tiling(acu, lim, wflag, fl[1], ns, (int)ntot, &tc, fl[7]) != cudaSuccess) return 10;
   std::vector<int4> tiles;
   std::vector<int> n(ncell, ncell + ntube), active(ntube, 1), col_tube(cols, 0);
-  std::vector<double> dxs(dx, dx + ntube), pout(ntube, p_out), dtt(ntube, 0.0);
+  std::vector<double> dxs(dx, dx + ntube), pout(ntube, p_out), dtt(ntube, 0.0), x0(ntube, 0.0);
+  {
+    double x = 0.0;
+    for (int t = 0; t < ntube && dx[t] != dx_comp; ++t) x -= ncell[t] * dx[t];
+    for (int t = 0; t < ntube; ++t) {
+      x0[t] = x;
+      x += ncell[t] * dx[t];
+    }
+  }
+  std::vector<double> snap(ntube > 1 ? (size_t)(ntube - 1) * 2 * ne * 2 * acu_lvir(acu) : 1, 0.0);
   for (int t = 0; t < ntube; ++t) {
     const int nb = (ncell[t] + tc - 1) / tc;
     for (int b = 0; b < nb; ++b) tiles.push_back(make_int4(t, b, nb, 0));
@@ -222,6 +234,10 @@ EMU_EXPORT int emu_fluid(int ntube, const int* ncell, const double* dx, int pack
       a.tubes.active = active.data();
       a.tubes.ntiles = (int)tiles.size();
       a.tubes.ntube = ntube;
+      if (packed == 2) {
+        a.tubes.smr_snap = ntube > 1 ? snap.data() : nullptr;
+        a.tubes.x0 = x0.data();
+      }
     }
     const int rc = stages(r, a, fl, acu, lim, wflag);
     if (rc) return rc;
@@ -241,15 +257,39 @@ EMU_EXPORT int emu_fluid(int ntube, const int* ncell, const double* dx, int pack
 // wall heat (wall, params: Nu, d, Tw_min, Tw_max, alpha, beta), ignition
 // (type, nig sources of E, r, duration, start). qrad, qtw: the per-cell
 // source outputs.
-EMU_EXPORT int emu_sources(int n, double dx, const double* qf_aos, double* qc_io, double* qf_out, double dt, double time,
-                int nrad, const int* rsp, const double* rcoef, int wall, const double* wp, int igt, int nig,
-                const double* ig, double* qrad, double* qtw, unsigned* err) {
-  const int ns = g_ns, ne = ns + 3, ld = n + 2 * GHOST;
+// With nseg > 0 the cells are the segments seg_n[] (cell size seg_dx[]) of
+// an SMR domain laid out as the library packs them, each cell at its x_m
+// (x = 0 at the left edge: no coarser leading segments here).
+EMU_EXPORT int emu_sources(int n, double dx, int nseg, const int* seg_n, const double* seg_dx, const double* qf_aos,
+                           double* qc_io, double* qf_out, double dt, double time, int nrad, const int* rsp,
+                           const double* rcoef, int wall, const double* wp, int igt, int nig, const double* ig,
+                           double* qrad, double* qtw, unsigned* err) {
+  const int ns = g_ns, ne = ns + 3;
+  std::vector<int> colmap(n), tube_of(n);
+  std::vector<double> xm(2 * (size_t)n);
+  int ld = n + 2 * GHOST;
+  if (nseg > 0) {
+    int i = 0;
+    long long off = 0;
+    double x = 0.0;
+    for (int t = 0; t < nseg; ++t) {
+      for (int j = 0; j < seg_n[t]; ++j, ++i) {
+        colmap[i] = (int)(off + j);
+        tube_of[i] = t;
+        xm[i] = x + (j + 0.5) * seg_dx[t];
+      }
+      off += seg_n[t] + 2 * GHOST;
+      x += seg_n[t] * seg_dx[t];
+    }
+    ld = (int)off;
+  } else {
+    for (int i = 0; i < n; ++i) colmap[i] = i;
+  }
   Rows r(ld, ne);
   for (int i = 0; i < n; ++i)
     for (int v = 0; v < ne; ++v) {
-      r.qf[0][(size_t)v * ld + i + GHOST] = qf_aos[(size_t)i * ne + v];
-      r.qc[(size_t)v * ld + i + GHOST] = qc_io[(size_t)i * ne + v];
+      r.qf[0][(size_t)v * ld + colmap[i] + GHOST] = qf_aos[(size_t)i * ne + v];
+      r.qc[(size_t)v * ld + colmap[i] + GHOST] = qc_io[(size_t)i * ne + v];
     }
   SourceArgs s;
   std::memset(&s, 0, sizeof(s));
@@ -292,11 +332,18 @@ EMU_EXPORT int emu_sources(int n, double dx, const double* qf_aos, double* qc_io
   std::vector<double> q2(2 * (size_t)n, 0.0);
   s.q_rad = q2.data();
   s.q_tw = q2.data() + n;
+  std::vector<unsigned long long> cv(nseg > 0 ? nseg : 1, 0ull);
+  if (nseg > 0) {
+    s.colmap = colmap.data();
+    s.tube_of = tube_of.data();
+    s.xm = xm.data();
+    s.cvel = cv.data();
+  }
   if (launch_energy_sources(s, 0) != cudaSuccess) return 11;
   for (int i = 0; i < n; ++i)
     for (int v = 0; v < ne; ++v) {
-      qf_out[(size_t)i * ne + v] = r.qf[0][(size_t)v * ld + i + GHOST];
-      qc_io[(size_t)i * ne + v] = r.qc[(size_t)v * ld + i + GHOST];
+      qf_out[(size_t)i * ne + v] = r.qf[0][(size_t)v * ld + colmap[i] + GHOST];
+      qc_io[(size_t)i * ne + v] = r.qc[(size_t)v * ld + colmap[i] + GHOST];
     }
   std::memcpy(qrad, q2.data(), 8 * (size_t)n);
   std::memcpy(qtw, q2.data() + n, 8 * (size_t)n);

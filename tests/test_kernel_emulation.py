@@ -88,14 +88,16 @@ def oracle_steps(oracle, t, steps, cfl):
     return np.array(dts)
 
 
-def emu_fluid(L, ncells, dxs, packed, fl, qf, qc, dts):
+def emu_fluid(L, ncells, dxs, packed, fl, qf, qc, dts, dx_comp=None):
     nt = len(ncells)
     qc_io = np.ascontiguousarray(qc.copy())
     qf_out = np.zeros_like(qf)
     err = ctypes.c_uint()
+    dxc = dxs[0] if dx_comp is None else dx_comp
     rc = L.emu_fluid(nt, (ctypes.c_int * nt)(*ncells), _p(np.ascontiguousarray(dxs, dtype=float)), packed,
-                     (ctypes.c_int * 8)(*fl), ctypes.c_double(configs.ATM), _p(np.ascontiguousarray(qf)), _p(qc_io),
-                     _p(qf_out), len(dts) // nt, _p(np.ascontiguousarray(dts, dtype=float)), ctypes.byref(err))
+                     ctypes.c_double(dxc), (ctypes.c_int * 8)(*fl), ctypes.c_double(configs.ATM),
+                     _p(np.ascontiguousarray(qf)), _p(qc_io), _p(qf_out), len(dts) // nt,
+                     _p(np.ascontiguousarray(dts, dtype=float)), ctypes.byref(err))
     assert rc == 0, rc
     return qf_out, qc_io, err.value
 
@@ -183,7 +185,8 @@ def test_energy_sources_match_oracle(emu, oracle):
         qrad, qtw = np.zeros(n), np.zeros(n)
         err = ctypes.c_uint()
         igd = np.array([v for s in ig[1] for v in s], dtype=float)
-        rc = emu.emu_sources(n, ctypes.c_double(dx), _p(np.ascontiguousarray(qf)), _p(qc_io), _p(qf_e), ctypes.c_double(dt),
+        rc = emu.emu_sources(n, ctypes.c_double(dx), 0, None, None, _p(np.ascontiguousarray(qf)), _p(qc_io), _p(qf_e),
+                             ctypes.c_double(dt),
                              ctypes.c_double(time), len(rad), (ctypes.c_int * len(rad))(*[r[0] for r in rad]),
                              _p(np.array([c for _, c in rad], dtype=float).ravel()), 1,
                              _p(np.array(wall, dtype=float)), ig[0], len(ig[1]), _p(igd), _p(qrad), _p(qtw),
@@ -205,3 +208,75 @@ def test_output_rows_match_oracle(emu, oracle):
     assert emu.emu_output_rows(n, ctypes.c_double(dx), _p(np.ascontiguousarray(qf)), _p(np.ascontiguousarray(qc)),
                                _p(rows)) == 0
     np.testing.assert_allclose(rows, ro, rtol=1e-14, atol=1e-300)
+
+
+def smr_state(oracle, ncells, dxs, r0):
+    """A pressurised, hot ball of radius r0 in air on SMR segments, with
+    qf = QcToqf(Qc) in every cell (a segment's interface ghost is QcToqf of
+    an interpolated Qc column)."""
+    from oracle_ctypes import _D
+    nm = species_names()
+    air = configs.mole_vector(nm, {"O2": 0.21, "N2": 0.79})
+    xs = np.concatenate([sum(n * d for n, d in zip(ncells[:g], dxs[:g])) + (np.arange(n) + 0.5) * d
+                         for g, (n, d) in enumerate(zip(ncells, dxs))])
+    inside = xs < r0
+    n = len(xs)
+    _, qc = oracle.init_cells(np.where(inside, 1500.0, 300.0), np.where(inside, 5 * configs.ATM, configs.ATM),
+                              np.zeros(n), np.tile(air, (n, 1)))
+    qf = np.zeros_like(qc)
+    for i in range(n):
+        oracle.L.or_qc_to_qf(oracle.mech, qc[i].ctypes.data_as(_D), qf[i].ctypes.data_as(_D))
+    return qf, qc
+
+
+@pytest.mark.parametrize("fl", [(1, 2, 1, 2, 0, 1, 0, 1), (0, 1, 1, 4, 0, 0, 0, 1), (1, 2, 1, 2, 0, 0, 0, 0)])
+def test_smr_segments_match_oracle(emu, oracle, fl):
+    """A hot ball on a fine core with coarser outer segments, spherical (and
+    Cartesian), the stage kernels' SMR path (interface snapshot, ghosts,
+    r = x_m) against the oracle's SMR blocks."""
+    ncells, dxs = [40, 24, 16], [1e-4, 2e-4, 4e-4]
+    qf, qc = smr_state(oracle, ncells, dxs, 12e-4)
+    st, rm, acu, mus, weno, rb, tran, sph = fl
+    s = oracle.smr(ncells, dxs, 2, [st, rm, acu, mus, weno, 0, rb, 0], [dxs[0], configs.ATM, 300.0, 0.0, 1e-5, 1e-13])
+    if sph:
+        s.set_spherical()
+    s.set_interior(qf, qc)
+    dts = [s.step(0.4) for _ in range(8)]
+    qf_o = s.get()[0]
+    assert np.abs(qf_o[:, 2] - qf[:, 2]).max() > 5.0
+    qf_e, _, err = emu_fluid(emu, ncells, dxs, 2, fl, qf, qc, np.repeat(dts, len(ncells)), dx_comp=dxs[0])
+    assert err == 0
+    close(qf_e, qf_o, 1e-10)
+
+
+def test_sources_on_smr_layout_match_one_tube(emu, oracle):
+    """The energy-source kernel on three equal-dx SMR segments (columns,
+    positions x_m and per-segment speeds of the packed layout) against the
+    same cells as one tube."""
+    nm = species_names()
+    ncells, dx = [30, 30, 30], 2e-5
+    n = sum(ncells)
+    qf, qc = layer(oracle, n, dx)
+    rad = [(nm.index(k), c) for k, c in RAD_FITS.items()]
+    rsp = (ctypes.c_int * len(rad))(*[r[0] for r in rad])
+    rco = _p(np.array([c for _, c in rad], dtype=float).ravel())
+    wall = _p(np.array((4.0, 2e-3, 373.0, 1300.0, 2e4, 0.5 * n * dx), dtype=float))
+    igd = _p(np.array([2e-6, 3e-4, 1e-6, 0.0], dtype=float))
+    out = []
+    for nseg in (0, 3):
+        qc_io = np.ascontiguousarray(qc.copy())
+        qf_e = np.zeros_like(qf)
+        qrad, qtw = np.zeros(n), np.zeros(n)
+        err = ctypes.c_uint()
+        rc = emu.emu_sources(n, ctypes.c_double(dx), nseg, (ctypes.c_int * 3)(*ncells),
+                             _p(np.full(3, dx)), _p(np.ascontiguousarray(qf)), _p(qc_io), _p(qf_e), ctypes.c_double(1e-7),
+                             ctypes.c_double(5e-8), len(rad), rsp, rco, 1, wall, 2, 1, igd, _p(qrad), _p(qtw),
+                             ctypes.byref(err))
+        assert rc == 0 and err.value == 0
+        out.append((qf_e, qc_io, qrad, qtw))
+    (a, ca, ra, wa), (b, cb, rb, wb) = out
+    assert np.abs(a[:, 2] - qf[:, 2]).max() > 1.0
+    close(b, a, 1e-12)
+    np.testing.assert_allclose(cb[:, 2], ca[:, 2], rtol=1e-13)
+    np.testing.assert_allclose(rb, ra, rtol=1e-12)
+    np.testing.assert_allclose(wb, wa, rtol=1e-10, atol=1e-12 * np.abs(wa).max())

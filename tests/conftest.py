@@ -18,7 +18,8 @@ def pytest_configure(config):
 # GPU suites of features whose device code has not yet run on a GPU. They
 # are collected after the suites already run on hardware, so that under
 # `pytest -x` a first failure in them stops nothing that was passing before.
-FIRST_GPU_RUN = ("test_gpu_sources.py", "test_gpu_spherical.py", "test_gpu_transport.py", "test_gpu_output.py")
+FIRST_GPU_RUN = ("test_gpu_sources.py", "test_gpu_spherical.py", "test_gpu_transport.py", "test_gpu_output.py",
+                 "test_gpu_smr_sph.py")
 
 
 def pytest_collection_modifyitems(session, config, items):

@@ -4,8 +4,9 @@
 // barrier (__syncwarp and the two halves of a shuffle) or has returned, and
 // releases a barrier once every thread it names has arrived, so the kernels
 // run with their own synchronisation. CTAs run one after another; shared
-// memory is filled with NaN before each, so a read of shared memory that no
-// thread of the CTA wrote shows up. The few CUDA runtime calls of fluid.cu's
+// memory is filled with NaN (or, EMU_POISON=big / zero, with +-1e300 or 0)
+// before each, so a read of shared memory that no thread of the CTA wrote
+// shows up. The few CUDA runtime calls of fluid.cu's
 // host code are stubs (no device exists): memory is host memory, streams
 // are ignored, constant-memory uploads are copies.
 #pragma once
@@ -148,6 +149,21 @@ using std::max;
 using std::min;
 using std::sqrt;
 
+// The value unwritten shared memory holds: NaN by default; EMU_POISON=big
+// (alternating +-1e300) or EMU_POISON=zero instead, since a NaN can vanish
+// in fmin / fmax (minmod limiters) where a large stale value would not.
+static double emu_poison() {
+  static int mode = -1;
+  static unsigned long long k = 0;
+  if (mode < 0) {
+    const char* e = std::getenv("EMU_POISON");
+    mode = !e ? 0 : (std::strcmp(e, "big") == 0 ? 1 : std::strcmp(e, "zero") == 0 ? 2 : 0);
+  }
+  if (mode == 1) return (k++ & 1) ? 1e300 : -1e300;
+  if (mode == 2) return 0.0;
+  return std::numeric_limits<double>::quiet_NaN();
+}
+
 static std::function<void()> emu_body;
 static void emu_entry() {
   emu_body();
@@ -157,7 +173,7 @@ static void emu_entry() {
 
 // one CTA of nt threads through fn
 static void emu_run_cta(int nt, const std::function<void()>& fn) {
-  for (double& x : emu_sm) x = std::numeric_limits<double>::quiet_NaN();
+  for (double& x : emu_sm) x = emu_poison();
   if ((int)emu_f.size() != nt) emu_f.assign(nt, EmuFiber());
   emu_body = fn;
   for (int t = 0; t < nt; ++t) {

@@ -1089,10 +1089,179 @@ __global__ void __launch_bounds__(TRAN_FLUX_THREADS) k_tran_flux(StageArgs a) {
   G[2 * ld] = tau * u_ave + rho_ave * hsum - kap_ave * ((R[2 * ld] - L[2 * ld]) / dx);
 }
 
+// k_tran_props_warp: the same properties with one warp per cell, for tubes
+// too short to fill the GPU with one thread per cell (there the launch
+// lasts one thread's chain of ~32,000 FP64 instructions). Lane 0 does the
+// cell's sequential part (mass and mole fractions, the temperature Newton,
+// the sums of MCACON and MCAVIS over species, in the thread kernel's
+// order); lane l takes species k = l, l + 32: its pure-species fits, its
+// Wilke denominator and its MCADIF sum over the other species, whose
+// binary coefficients it evaluates itself (each pair twice per cell, once
+// per lane). Every operation and every summation order are the thread
+// kernel's, so the results are the same bits.
+constexpr int TRAN_WARP_CELLS = 4;        // cells (warps) per CTA
+constexpr int TRAN_WARP_MAX_CELLS = 40000;  // up to this many cells per launch the warp form runs
+
+__global__ void __launch_bounds__(32 * TRAN_WARP_CELLS) k_tran_props_warp(StageArgs a) {
+  if (a.step_active && *a.step_active == 0) return;
+  __shared__ double s_y[TRAN_WARP_CELLS][EDYN_NS_MAX], s_x[TRAN_WARP_CELLS][EDYN_NS_MAX];
+  __shared__ double s_v1[TRAN_WARP_CELLS][EDYN_NS_MAX], s_v2[TRAN_WARP_CELLS][EDYN_NS_MAX];
+  __shared__ double s_eta[TRAN_WARP_CELLS][EDYN_NS_MAX], s_aux[TRAN_WARP_CELLS][EDYN_NS_MAX];
+  __shared__ double s_term[TRAN_WARP_CELLS][EDYN_NS_MAX], s_sc[TRAN_WARP_CELLS][8];
+  const int lane = (int)(threadIdx.x & 31), w = (int)(threadIdx.x >> 5);
+  const int gid = (int)(blockIdx.x * TRAN_WARP_CELLS) + w;
+  // the cell, as in k_tran_props (warp-uniform)
+  TubeView tv{a.n, a.qf_in, a.qf_out, a.qc, a.q0, a.acc, a.dx, a.p_out, nullptr};
+  int c = gid - 1;
+  if (a.tubes.tiles) {
+    if (gid >= a.ld) return;
+    const int tt = a.tran.col_tube[gid];
+    const long long off = a.tubes.off[tt];
+    tv.n = a.tubes.n[tt];
+    tv.qf_in = a.qf_in + off;
+    tv.qc = a.qc + off;
+    tv.dx = a.tubes.dx[tt];
+    tv.p_out = a.tubes.p_out[tt];
+    tv.tube = tt;
+    tv.off = off;
+    c = (int)(gid - off - GHOST);
+  }
+  if (c < -1 || c > tv.n) return;
+  const ThermoTable& tb = c_thermo;
+  const TranDev& t = a.tran;
+  const int ns = a.ns;
+  const size_t ld = (size_t)a.ld;
+  double* y = s_y[w];
+  double* x = s_x[w];
+  double* v1 = s_v1[w];
+  double* v2 = s_v2[w];
+  double* eta = s_eta[w];
+  double* aux = s_aux[w];
+  double* sc = s_sc[w];
+  // 1. the conserved column (rho Y_k into y)
+  if (c < 0 || c == tv.n) {
+    if (lane == 0) ghost_qc(a, tv, c < 0 ? -1 : tv.n, sc[0], sc[1], sc[2], y, 1);
+  } else {
+    const double* Q = tv.qc + c + GHOST;
+    for (int k = lane; k < ns; k += 32) y[k] = Q[(3 + k) * ld];
+    if (lane == 0) {
+      sc[0] = Q[0];
+      sc[1] = Q[ld];
+      sc[2] = Q[2 * ld];
+    }
+  }
+  __syncwarp();
+  // 2. lane 0: Y, X, T (temperature_con from 1000 K), p, ln T
+  if (lane == 0) {
+    const double rho = sc[0];
+    const double u = sc[1] / rho;
+    double sy = 0.0, sumyow = 0.0;
+    for (int k = 0; k < ns; ++k) {
+      const double yk = y[k] / rho;
+      y[k] = yk;
+      sy += yk;
+      sumyow = fma(yk, tb.invW[k], sumyow);
+    }
+    const double isw = 1.0 / sumyow;
+    for (int k = 0; k < ns; ++k) x[k] = y[k] * tb.invW[k] * isw;
+    const double eint = sc[2] / rho - 0.5 * (u * u);
+    Premix pm;
+    double Sz;
+    int iters;
+    const double T = t_newton(y, 1, eint * sy * (1.0 / R_SI), 1000.0, pm, Sz, iters);
+    if (iters < 0 && a.err) atomicOr(a.err, EDYN_STATUS_NEWTON);
+    sc[3] = rho;
+    sc[4] = u;
+    sc[5] = T;
+    sc[6] = tlog(T, t.lg);
+    sc[7] = 10.0 * (R_SI * rho * T * Sz / sy);
+  }
+  __syncwarp();
+  const double L = sc[6], p_cgs = sc[7];
+  // 3. pure-species viscosity and conductivity (conductivities into aux)
+  for (int k = lane; k < ns; k += 32) {
+    const double* ce = t.eta + 4 * k;
+    const double* cl = t.lam + 4 * k;
+    const double ek = texp_r(fma(fma(fma(ce[3], L, ce[2]), L, ce[1]), L, ce[0]), t.e2);
+    const double lk = texp_r(fma(fma(fma(cl[3], L, cl[2]), L, cl[1]), L, cl[0]), t.e2);
+    eta[k] = ek;
+    aux[k] = lk;
+    const double r = rsqrt(ek);
+    v1[k] = x[k] * r;
+    v2[k] = x[k] / ek;
+  }
+  __syncwarp();
+  // 4. Wilke's denominator of species k; lane 0 then sums the terms and
+  //    MCACON's two means in species order
+  for (int k = lane; k < ns; k += 32) {
+    const double* pa = t.wa + (size_t)k * ns;
+    const double* pb = t.wb + (size_t)k * ns;
+    const double* pc = t.wc + (size_t)k * ns;
+    double A = 0.0, B = 0.0, C = 0.0;
+    for (int j = 0; j < ns; ++j) {
+      A = fma(pa[j], x[j], A);
+      B = fma(pb[j], v1[j], B);
+      C = fma(pc[j], v2[j], C);
+    }
+    const double sumi = fma(eta[k], C, fma(2.0 * sqrt(eta[k]), B, A));
+    s_term[w][k] = x[k] * eta[k] / sumi;
+  }
+  __syncwarp();
+  if (lane == 0) {
+    double sl = 0.0, sr = 0.0, vm = 0.0;
+    for (int k = 0; k < ns; ++k) {
+      sl = fma(x[k], aux[k], sl);
+      sr += x[k] / aux[k];
+    }
+    for (int k = 0; k < ns; ++k) vm += s_term[w][k];
+    sc[0] = vm * 2.8284271247461903 * 0.1;
+    sc[1] = 0.5 * (sl + 1.0 / sr) * 1.0e-5;
+  }
+  __syncwarp();
+  // 5. XX = max(X, 1e-50) (into aux)
+  for (int k = lane; k < ns; k += 32) aux[k] = fmax(x[k], 1.0e-50);
+  __syncwarp();
+  // 6. MCADIF for species k: S_k = sum_{j != k} XX_j / D_jk in increasing j,
+  //    sum_{j != k} XX_j W_j as the prefix plus the suffix, D'_k
+  double* out = t.tp + tv.off + c + GHOST;
+  for (int k = lane; k < ns; k += 32) {
+    double S = 0.0;
+    for (int j = 0; j < ns; ++j) {
+      if (j == k) continue;
+      const double* cd = t.dif + 4 * (j < k ? (size_t)k * (k - 1) / 2 + j : (size_t)j * (j - 1) / 2 + k);
+      const double v = texp_r(-fma(fma(fma(cd[3], L, cd[2]), L, cd[1]), L, cd[0]), t.e2);
+      S = fma(aux[j], v, S);
+    }
+    double suf = 0.0, sufk = 0.0, wtm = 0.0;
+    for (int j = ns - 1; j >= 0; --j) {
+      if (j == k) sufk = suf;
+      suf = fma(aux[j], t.W[j], suf);
+      wtm = fma(t.W[j], x[j], wtm);
+    }
+    double pre = 0.0;
+    for (int j = 0; j < k; ++j) pre = fma(aux[j], t.W[j], pre);
+    const double sumxw = pre + sufk;
+    const double dk = sumxw / (wtm * S) * t.patmos / p_cgs * 1.0e-4;
+    const double dif = (y[k] == 1.0) ? 0.0 : (1.0 - x[k]) / (1.0 - y[k]) * dk;
+    out[(TRAN_ROWS_FIXED + k) * ld] = y[k];
+    out[(TRAN_ROWS_FIXED + ns + k) * ld] = dif;
+  }
+  if (lane == 0) {
+    out[0] = sc[3];
+    out[ld] = sc[4];
+    out[2 * ld] = sc[5];
+    out[3 * ld] = sc[0];
+    out[4 * ld] = sc[1];
+  }
+}
+
 cudaError_t launch_tran(const StageArgs& a, cudaStream_t s) {
   // one thread per cell (-1..n) and per face (0..n); packed tubes: per column
   const int np = a.tubes.tiles ? a.ld : a.n + 2, nf = a.tubes.tiles ? a.ld : a.n + 1;
-  k_tran_props<<<(np + TRAN_PROPS_THREADS - 1) / TRAN_PROPS_THREADS, TRAN_PROPS_THREADS, 0, s>>>(a);
+  if (np <= TRAN_WARP_MAX_CELLS)
+    k_tran_props_warp<<<(np + TRAN_WARP_CELLS - 1) / TRAN_WARP_CELLS, 32 * TRAN_WARP_CELLS, 0, s>>>(a);
+  else
+    k_tran_props<<<(np + TRAN_PROPS_THREADS - 1) / TRAN_PROPS_THREADS, TRAN_PROPS_THREADS, 0, s>>>(a);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   k_tran_flux<<<(nf + TRAN_FLUX_THREADS - 1) / TRAN_FLUX_THREADS, TRAN_FLUX_THREADS, 0, s>>>(a);

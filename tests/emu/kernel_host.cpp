@@ -351,6 +351,66 @@ EMU_EXPORT int emu_sources(int n, double dx, int nseg, const int* seg_n, const d
   return 0;
 }
 
+// The transport properties (TranDev::tp rows, cells -1..n of each tube)
+// of the thread-per-cell kernel (warp == 0) or the warp-per-cell kernel,
+// for one tube (packed == 0) or packed tubes; rbound: wall or outlet.
+EMU_EXPORT int emu_tran_props(int ntube, const int* ncell, const double* dx, int packed, int rbound, double p_out,
+                              const double* qc_aos, int warp, double* props) {
+  const int ns = g_ns, ne = ns + 3, prow = TRAN_ROWS_FIXED + 2 * ns;
+  std::vector<long long> off(ntube), first(ntube);
+  long long cols = 0, ntot = 0;
+  for (int t = 0; t < ntube; ++t) {
+    off[t] = cols;
+    first[t] = ntot;
+    cols += ncell[t] + 2 * GHOST;
+    ntot += ncell[t];
+  }
+  Rows r((int)cols, ne);
+  for (int t = 0; t < ntube; ++t)
+    for (int i = 0; i < ncell[t]; ++i)
+      for (int v = 0; v < ne; ++v) r.qc[(size_t)v * cols + off[t] + i + GHOST] = qc_aos[(size_t)(first[t] + i) * ne + v];
+  std::vector<int> n(ncell, ncell + ntube), col_tube(cols, 0);
+  std::vector<double> dxs(dx, dx + ntube), pout(ntube, p_out);
+  std::vector<int4> tiles(1, make_int4(0, 0, 1, 0));
+  for (int t = 0; t < ntube; ++t)
+    for (long long j = 0; j < ncell[t] + 2 * GHOST; ++j) col_tube[off[t] + j] = t;
+  StageArgs a;
+  std::memset(&a, 0, sizeof(a));
+  unsigned e = 0;
+  a.n = packed ? (int)ntot : ncell[0];
+  a.ld = (int)cols;
+  a.lvir = 2;
+  a.ns = ns;
+  a.qc = r.qc.data();
+  a.qf_in = r.qf[0].data();
+  a.dx = dx[0];
+  a.rbound = rbound;
+  a.p_out = p_out;
+  a.strict_newton = 1;
+  a.err = &e;
+  a.tran = g_tr;
+  a.tran.tp = r.tp.data();
+  a.tran.flux = r.fl.data();
+  if (packed) {
+    a.tran.col_tube = col_tube.data();
+    a.tubes.tiles = tiles.data();
+    a.tubes.n = n.data();
+    a.tubes.off = off.data();
+    a.tubes.dx = dxs.data();
+    a.tubes.p_out = pout.data();
+    a.tubes.ntube = ntube;
+  }
+  const int np = packed ? (int)cols : ncell[0] + 2;
+  if (warp)
+    emu_launch(k_tran_props_warp, dim3((np + TRAN_WARP_CELLS - 1) / TRAN_WARP_CELLS), dim3(32 * TRAN_WARP_CELLS), 0,
+               (cudaStream_t)0, a);
+  else
+    emu_launch(k_tran_props, dim3((np + TRAN_PROPS_THREADS - 1) / TRAN_PROPS_THREADS), dim3(TRAN_PROPS_THREADS), 0,
+               (cudaStream_t)0, a);
+  std::memcpy(props, r.tp.data(), (size_t)prow * cols * sizeof(double));
+  return e ? 12 : 0;
+}
+
 // k_output_rows of one tube with cell centres (i + 1/2) dx
 EMU_EXPORT int emu_output_rows(int n, double dx, const double* qf_aos, const double* qc_aos, double* rows) {
   const int ns = g_ns, ne = ns + 3, ld = n + 2 * GHOST;

@@ -51,6 +51,23 @@ def test_transport_properties_match_oracle(oracle):
         np.testing.assert_allclose(dif[i], dif_o, rtol=TOL, atol=1e-30, err_msg=f"cell {i}")
 
 
+def test_transport_properties_thread_kernel_match_oracle(oracle):
+    """Beyond 40,000 cells the property kernel takes one thread per cell
+    (below, one warp per cell, with the same bits): sampled cells of a long
+    tube against the oracle."""
+    n = 41000
+    T, p, u, X = varied_state(n, seed=5)
+    qf, qc = oracle.init_cells(T, p, u, X)
+    g = Tube(n, 1e-5, flag_acu=1, flag_muscl=2, do_tran=1)
+    g.upload(qf, qc)
+    mu, kap, dif = g.transport_properties()
+    for i in np.linspace(0, n - 1, 60).astype(int):
+        _, _, _, _, mu_o, kap_o, dif_o = oracle.tran_cell(qc[i])
+        assert abs(mu[i] - mu_o) <= TOL * mu_o, i
+        assert abs(kap[i] - kap_o) <= TOL * kap_o, i
+        np.testing.assert_allclose(dif[i], dif_o, rtol=TOL, atol=1e-30, err_msg=f"cell {i}")
+
+
 def run_pair(oracle, case, nsteps, **over):
     fl = {**flags_of(case), **over}
     qf0, qc0 = oracle.init_cells(case.T, case.p, case.u, case.X)

@@ -284,3 +284,29 @@ def test_sources_on_smr_layout_match_one_tube(emu, oracle):
     np.testing.assert_allclose(cb[:, 2], ca[:, 2], rtol=1e-13)
     np.testing.assert_allclose(rb, ra, rtol=1e-12)
     np.testing.assert_allclose(wb, wa, rtol=1e-10, atol=1e-12 * np.abs(wa).max())
+
+
+@pytest.mark.parametrize("packed,rbound", [(0, 0), (0, 1), (1, 0), (1, 1)])
+def test_warp_transport_properties_equal_thread_kernel(emu, oracle, packed, rbound):
+    """The warp-per-cell property kernel gives the thread-per-cell kernel's
+    bits, ghost cells included, in one tube and in packed tubes."""
+    cases = [(40, 2e-5, 5.0), (56, 1e-5, 0.0)] if packed else [(70, 2e-5, 5.0)]
+    qc = np.vstack([layer(oracle, n, dx, u0)[1] for n, dx, u0 in cases])
+    ncells = [c[0] for c in cases]
+    cols = sum(n + 8 for n in ncells)
+    nrow = 5 + 2 * len(species_names())
+    out = []
+    for warp in (0, 1):
+        props = np.zeros(nrow * cols)
+        rc = emu.emu_tran_props(len(cases), (ctypes.c_int * len(cases))(*ncells),
+                                _p(np.array([c[1] for c in cases])), packed, rbound, ctypes.c_double(configs.ATM),
+                                _p(np.ascontiguousarray(qc)), warp, _p(props))
+        assert rc == 0
+        out.append(props.reshape(nrow, cols))
+    used = np.zeros(cols, bool)
+    o = 0
+    for n in ncells:
+        used[o + 3:o + n + 5] = True  # cells -1..n
+        o += n + 8
+    assert np.all(np.isfinite(out[0][:, used]))
+    np.testing.assert_array_equal(out[1][:, used], out[0][:, used])

@@ -1192,7 +1192,9 @@ int init_packed(const char* chem_dir, int nspe, int nequ, int ntube, const int* 
   if (ntube < 1 || !ncell || !rparams || n_rparams < 2 || !iflags || n_iflags < 8) return EDYN_E_ARG;
   long long ntot = 0, cols = 0;
   for (int t = 0; t < ntube; ++t) {
-    if (ncell[t] < 16) return EDYN_E_ARG;
+    // SMR segments: down to the reference's blocks (10 cells) -- a segment
+    // feeds its neighbour's ghosts from 2 lvir cells; independent tubes >= 16
+    if (ncell[t] < (smr ? std::max(8, 2 * lvir) : 16)) return EDYN_E_ARG;
     ntot += ncell[t];
     cols += ncell[t] + 2 * GHOST;
   }

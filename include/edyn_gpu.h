@@ -103,7 +103,7 @@ int edyn_init_tubes(const char* chem_dir, int nspe, int nequ, int ntube, const i
 
 /* Creates a context for one domain of SMR blocks (static mesh refinement,
  * SRC/block.f90:91-379): nseg segments, left to right, each a run of
- * ncell[s] (>= 16) cells of size dx[s] (a run of the reference's equal-dx
+ * ncell[s] (>= max(8, 2 lvir)) cells of size dx[s] (a run of the reference's equal-dx
  * blocks, whose ghost exchange is a copy), neighbouring sizes equal or a
  * factor of two apart. The ghosts facing another segment come from
  * interpolation_block (SRC/block.f90:475-569): the mean of two fine cells on

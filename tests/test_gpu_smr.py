@@ -106,7 +106,7 @@ def test_blocks_refused_where_unsupported():
     with pytest.raises(EdynError):
         Blocks([32, 32], [1e-3, 2e-3], select_time=2)
     with pytest.raises(EdynError):
-        Blocks([32, 8], [1e-3, 2e-3])
+        Blocks([32, 6], [1e-3, 2e-3])
     with pytest.raises(EdynError, match="transport"):
         Blocks([32, 32], [1e-3, 2e-3], do_tran=1)
 

@@ -86,3 +86,19 @@ def test_cell_centres_of_a_left_smr_zone():
     rows = b.output_rows()
     edges = np.r_[0.0, np.cumsum(np.repeat(dxs, ncells))] - (16 * 4e-3 + 16 * 2e-3)
     np.testing.assert_allclose(rows[12], 0.5 * (edges[:-1] + edges[1:]), rtol=0, atol=1e-15)
+
+
+def test_ten_cell_segments_match_oracle(oracle):
+    """The reference's SMR layout: 10-cell blocks, one per level, beyond a
+    fine core (a spherical ball, TVDRK3-HLLC-MUSCL)."""
+    ncells, dxs = [60, 10, 10, 10, 10], [1e-4, 2e-4, 4e-4, 8e-4, 1.6e-3]
+    qf, qc = ball(oracle, ncells, dxs, 20e-4)
+    flags = [1, 2, 1, 2, 0, 0, 1, 0]
+    s = oracle.smr(ncells, dxs, 2, flags, [dxs[0]] + RP[1:])
+    s.set_spherical()
+    s.set_interior(qf, qc)
+    b = Blocks(ncells, dxs, flag_rbound=1, is_spherical=1)
+    b.upload(qf, qc)
+    for _ in range(20):
+        assert b.step(0.4) == pytest.approx(s.step(0.4), rel=1e-12)
+    check(s.get()[0], b.download()[0])

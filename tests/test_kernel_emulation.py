@@ -229,17 +229,21 @@ def smr_state(oracle, ncells, dxs, r0):
     return qf, qc
 
 
-@pytest.mark.parametrize("fl", [(1, 2, 1, 2, 0, 1, 0, 1), (0, 1, 1, 4, 0, 0, 0, 1), (1, 2, 1, 2, 0, 0, 0, 0),
-                                (1, 2, 1, 2, 0, 1, 1, 1), (1, 2, 1, 2, 0, 0, 1, 0)])
-def test_smr_segments_match_oracle(emu, oracle, fl):
+@pytest.mark.parametrize("fl,short", [((1, 2, 1, 2, 0, 1, 0, 1), 0), ((0, 1, 1, 4, 0, 0, 0, 1), 0),
+                                      ((1, 2, 1, 2, 0, 0, 0, 0), 0), ((1, 2, 1, 2, 0, 1, 1, 1), 0),
+                                      ((1, 2, 1, 2, 0, 0, 1, 0), 0), ((1, 2, 1, 2, 0, 1, 1, 1), 1),
+                                      ((1, 2, 2, 0, 3, 1, 0, 0), 1)])
+def test_smr_segments_match_oracle(emu, oracle, fl, short):
     """A hot ball on a fine core with coarser outer segments, spherical (and
     Cartesian), with and without transport: the stage kernels' SMR path
     (interface snapshot, ghosts, r = x_m, the per-column transport kernels)
     against the oracle's SMR blocks."""
-    ncells, dxs = [40, 24, 16], [1e-4, 2e-4, 4e-4]
+    # short: the reference's 10-cell blocks, one segment per level
+    ncells, dxs = ([40, 10, 10, 10], [1e-4, 2e-4, 4e-4, 8e-4]) if short else ([40, 24, 16], [1e-4, 2e-4, 4e-4])
     qf, qc = smr_state(oracle, ncells, dxs, 12e-4)
     st, rm, acu, mus, weno, rb, tran, sph = fl
-    s = oracle.smr(ncells, dxs, 2, [st, rm, acu, mus, weno, 0, rb, 0], [dxs[0], configs.ATM, 300.0, 0.0, 1e-5, 1e-13])
+    lv = 2 if acu == 1 else 3
+    s = oracle.smr(ncells, dxs, lv, [st, rm, acu, mus, weno, 0, rb, 0], [dxs[0], configs.ATM, 300.0, 0.0, 1e-5, 1e-13])
     if sph:
         s.set_spherical()
     if tran:
